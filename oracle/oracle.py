@@ -1,0 +1,250 @@
+"""ctypes front end of the FP64 C oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, the smoke check in __graft_entry__.py and the CPU-baseline leg of
+bench.py import this module.  It exposes the C restatement of the reference's
+likelihood path (oracle/gwat_oracle.c) and, where it was built, the reference
+pin library oracle/_ref/libgwatref.so (the reference's own IMRPhenomD.cpp /
+IMRPhenomP.cpp compiled against shim headers).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+IMRPhenomD = 0
+IMRPhenomPv2 = 1
+
+DETECTORS = ["Hanford", "Livingston", "Virgo", "Kagra", "Indigo", "CE", "ET1", "ET2", "ET3"]
+
+
+class GenParams(ctypes.Structure):
+    """Mirror of gwo_gen_params (oracle/gwat_oracle.h)."""
+
+    _fields_ = [
+        ("mass1", ctypes.c_double), ("mass2", ctypes.c_double),
+        ("spin1", ctypes.c_double * 3), ("spin2", ctypes.c_double * 3),
+        ("Luminosity_Distance", ctypes.c_double),
+        ("incl_angle", ctypes.c_double), ("phiRef", ctypes.c_double),
+        ("f_ref", ctypes.c_double), ("tc", ctypes.c_double),
+        ("RA", ctypes.c_double), ("DEC", ctypes.c_double),
+        ("psi", ctypes.c_double), ("gmst", ctypes.c_double),
+        ("chip", ctypes.c_double), ("phip", ctypes.c_double),
+        ("shift_time", ctypes.c_int), ("shift_phase", ctypes.c_int),
+        ("sky_average", ctypes.c_int), ("dep_postmerger", ctypes.c_int),
+    ]
+
+
+def make_params(**kw):
+    p = GenParams()
+    p.chip = -1.0
+    p.phip = -1.0
+    p.shift_time = 1
+    p.shift_phase = 1
+    for k, v in kw.items():
+        if k in ("spin1", "spin2"):
+            getattr(p, k)[:] = list(v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def params_from_dict(d):
+    return make_params(**d)
+
+
+_lib = None
+_ref = None
+
+
+def build(ref_dir=None):
+    """Compile liboracle.so (and the reference pin library if ref_dir exists)."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
+    if ref_dir and os.path.isdir(os.path.join(ref_dir, "src")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + ref_dir])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        gp = ctypes.POINTER(GenParams)
+        L.gwo_fourier_waveform.argtypes = [dp, ctypes.c_int, dp, dp, ctypes.c_int, gp]
+        L.gwo_fourier_detector_response.argtypes = [dp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, gp]
+        L.gwo_antenna.argtypes = [ctypes.c_int] + [ctypes.c_double] * 4 + [dp, dp]
+        L.gwo_dtoa.argtypes = [ctypes.c_double] * 3 + [ctypes.c_int] * 2
+        L.gwo_dtoa.restype = ctypes.c_double
+        L.gwo_log_likelihood_internal.argtypes = [dp, dp, dp, dp, ctypes.c_int]
+        L.gwo_log_likelihood_internal.restype = ctypes.c_double
+        L.gwo_loglik_extrinsic.argtypes = [gp, ctypes.c_int, ctypes.c_double, dp, ctypes.c_int, ctypes.c_int, ip,
+                                           ctypes.POINTER(dp), ctypes.POINTER(dp)]
+        L.gwo_loglik_extrinsic.restype = ctypes.c_double
+        L.gwo_loglik_batch.argtypes = [gp, ctypes.c_int, ip, ctypes.c_double, dp, ctypes.c_int, ctypes.c_int, ip,
+                                       ctypes.POINTER(dp), ctypes.POINTER(dp), dp, ctypes.c_int]
+        L.gwo_mcmc_repack.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, gp]
+        L.gwo_fisher_numerical.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, gp,
+                                           ctypes.c_int, dp, ctypes.c_double, ctypes.c_int]
+        L.gwo_fisher_numerical.restype = ctypes.c_int
+        L.gwo_fisher_network.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip, dp, gp, ctypes.c_int,
+                                         ctypes.POINTER(dp), ctypes.c_double, ctypes.c_int]
+        L.gwo_fisher_batch.argtypes = [gp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip,
+                                       ctypes.POINTER(dp), ctypes.c_double, ctypes.c_int, dp, ctypes.c_int]
+        L.gwo_cholesky_invert.argtypes = [dp, dp, ctypes.c_int]
+        L.gwo_cholesky_invert.restype = ctypes.c_int
+        L.gwo_analytic_psd.argtypes = [ctypes.c_double]
+        L.gwo_analytic_psd.restype = ctypes.c_double
+        L.gwo_cspline_coeffs.argtypes = [dp, dp, ctypes.c_int, dp]
+        L.gwo_cspline_eval.argtypes = [dp, dp, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        L.gwo_cspline_eval.restype = ctypes.c_double
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference pin library, or None where it was not built."""
+    global _ref
+    if _ref is None:
+        path = os.path.join(HERE, "_ref", "libgwatref.so")
+        if not os.path.exists(path):
+            return None
+        L = ctypes.CDLL(path)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.ref_fourier_waveform.argtypes = [dp, ctypes.c_int, dp, dp, ctypes.c_int, ctypes.POINTER(GenParams)]
+        _ref = L
+    return _ref
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def fourier_waveform(freqs, params, approximant=IMRPhenomD, use_ref=False):
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    n = freqs.size
+    hp = np.zeros(n, dtype=np.complex128)
+    hc = np.zeros(n, dtype=np.complex128)
+    L = ref_lib() if use_ref else lib()
+    fn = L.ref_fourier_waveform if use_ref else L.gwo_fourier_waveform
+    fn(_dp(freqs), n, _dp(hp), _dp(hc), approximant, ctypes.byref(params))
+    return hp, hc
+
+
+def detector_index(name):
+    return DETECTORS.index(name)
+
+
+def detector_response(freqs, params, detector, approximant=IMRPhenomD):
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    r = np.zeros(freqs.size, dtype=np.complex128)
+    lib().gwo_fourier_detector_response(_dp(freqs), freqs.size, _dp(r), detector_index(detector), approximant,
+                                        ctypes.byref(params))
+    return r
+
+
+def antenna(detector, ra, dec, psi, gmst):
+    fp = ctypes.c_double()
+    fc = ctypes.c_double()
+    lib().gwo_antenna(detector_index(detector), ra, dec, psi, gmst, ctypes.byref(fp), ctypes.byref(fc))
+    return fp.value, fc.value
+
+
+def dtoa(ra, dec, gmst, det1, det2):
+    return lib().gwo_dtoa(ra, dec, gmst, detector_index(det1), detector_index(det2))
+
+
+def analytic_psd(freqs):
+    return np.array([lib().gwo_analytic_psd(float(f)) for f in np.atleast_1d(freqs)])
+
+
+def _ptr_array(arrs):
+    arr_t = ctypes.POINTER(ctypes.c_double) * len(arrs)
+    return arr_t(*[_dp(a) for a in arrs])
+
+
+def loglik(params, freqs, detectors, data, psd, approximant=IMRPhenomD, T_segment=None):
+    """MCMC_likelihood_extrinsic for one request (all detectors on one grid)."""
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    if T_segment is None:
+        T_segment = 1.0 / (freqs[1] - freqs[0])
+    dets = (ctypes.c_int * len(detectors))(*[detector_index(d) for d in detectors])
+    data = [np.ascontiguousarray(d, dtype=np.complex128) for d in data]
+    psd = [np.ascontiguousarray(s, dtype=np.float64) for s in psd]
+    return lib().gwo_loglik_extrinsic(ctypes.byref(params), approximant, T_segment, _dp(freqs), freqs.size,
+                                      len(detectors), dets, _ptr_array(data), _ptr_array(psd))
+
+
+def loglik_batch(params_list, freqs, detectors, data, psd, approximants=None, T_segment=None, nthreads=0):
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    if T_segment is None:
+        T_segment = 1.0 / (freqs[1] - freqs[0])
+    n = len(params_list)
+    parr = (GenParams * n)(*params_list)
+    if approximants is None:
+        approximants = [IMRPhenomD] * n
+    aarr = (ctypes.c_int * n)(*approximants)
+    dets = (ctypes.c_int * len(detectors))(*[detector_index(d) for d in detectors])
+    data = [np.ascontiguousarray(d, dtype=np.complex128) for d in data]
+    psd = [np.ascontiguousarray(s, dtype=np.float64) for s in psd]
+    out = np.zeros(n)
+    lib().gwo_loglik_batch(parr, n, aarr, T_segment, _dp(freqs), freqs.size, len(detectors), dets,
+                           _ptr_array(data), _ptr_array(psd), _dp(out), nthreads)
+    return out
+
+
+def mcmc_repack(theta, approximant=IMRPhenomD, gmst=0.0):
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    p = GenParams()
+    lib().gwo_mcmc_repack(_dp(theta), theta.size, approximant, gmst, ctypes.byref(p))
+    return p
+
+
+FISHER_METHODS = {"IMRPhenomD": 0, "MCMC_IMRPhenomD": 1, "IMRPhenomPv2": 2, "MCMC_IMRPhenomPv2": 3}
+
+
+def fisher_numerical(freqs, params, detector, ref_detector, psd, method="IMRPhenomD", order=2,
+                     epsilon=1e-8, step_mode=0):
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    psd = np.ascontiguousarray(psd, dtype=np.float64)
+    out = np.zeros(15 * 15)
+    dim = lib().gwo_fisher_numerical(_dp(freqs), freqs.size, FISHER_METHODS[method], detector_index(detector),
+                                     detector_index(ref_detector), _dp(out), ctypes.byref(params), order, _dp(psd),
+                                     epsilon, step_mode)
+    return out[:dim * dim].reshape(dim, dim)
+
+
+def fisher_network(freqs, params, detectors, psds, method="IMRPhenomD", order=2, epsilon=1e-8, step_mode=0):
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    psds = [np.ascontiguousarray(s, dtype=np.float64) for s in psds]
+    dets = (ctypes.c_int * len(detectors))(*[detector_index(d) for d in detectors])
+    out = np.zeros(15 * 15)
+    lib().gwo_fisher_network(_dp(freqs), freqs.size, FISHER_METHODS[method], len(detectors), dets, _dp(out),
+                             ctypes.byref(params), order, _ptr_array(psds), epsilon, step_mode)
+    dim = 11 if method in ("IMRPhenomD", "MCMC_IMRPhenomD") else (13 if method == "IMRPhenomPv2" else 15)
+    return out[:dim * dim].reshape(dim, dim)
+
+
+def fisher_batch(params_list, freqs, detectors, psds, method="IMRPhenomD", epsilon=1e-8, step_mode=0,
+                 nthreads=0):
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    psds = [np.ascontiguousarray(s, dtype=np.float64) for s in psds]
+    n = len(params_list)
+    parr = (GenParams * n)(*params_list)
+    dets = (ctypes.c_int * len(detectors))(*[detector_index(d) for d in detectors])
+    dim = 11 if method in ("IMRPhenomD", "MCMC_IMRPhenomD") else (13 if method == "IMRPhenomPv2" else 15)
+    out = np.zeros(n * dim * dim)
+    lib().gwo_fisher_batch(parr, n, _dp(freqs), freqs.size, FISHER_METHODS[method], len(detectors), dets,
+                           _ptr_array(psds), epsilon, step_mode, _dp(out), nthreads)
+    return out.reshape(n, dim, dim)
+
+
+def cholesky_invert(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    inv = np.zeros_like(a)
+    st = lib().gwo_cholesky_invert(_dp(a), _dp(inv), a.shape[0])
+    return st, inv
