@@ -1,0 +1,63 @@
+// capi_internal.h -- the context object behind gwgpu_context* (host only).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gwgpu.h"
+#include "batch_internal.h"
+#include "kernels.h"
+
+struct gwgpu_context {
+  struct Workspace {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+  };
+  struct Stream {
+    gwk::StreamDev dev;
+    bool live = false;
+    std::vector<void *> mem;
+    std::vector<double> host_freqs;
+  };
+  // A captured batch launch (prologue + fused kernel) for one request shape.
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+  };
+  enum { kWsWave = 0, kWsInner, kWsPlain, kWsBatch, kWsBatchItems, kWsFisher, kWsServe };
+  enum { kHwsPlain = 0, kHwsBatch, kHwsFisher };
+
+  int device = 0;
+  size_t budget = 0, in_use = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::string last_error;
+  std::map<void *, size_t> sizes;
+  std::map<int, Workspace> ws, hws;
+  std::vector<double> qnm_host;
+  double *qnm_dev = nullptr;
+  gwt::Tables tables{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+  std::vector<void *> table_mem;
+  std::vector<Stream> streams;
+  gwk::StreamDev *streams_dev = nullptr;
+  size_t streams_dev_cap = 0;
+  unsigned *counters = nullptr;
+  std::map<std::string, Graph> graphs;
+  gwb::Plan plan;
+  int tile_override = 0;
+
+  ~gwgpu_context();
+  int fail(cudaError_t e, const char *where);
+  int dalloc(void **p, size_t bytes, const char *what);
+  void dfree(void *p);
+  int workspace(int slot, size_t bytes, void **out);
+  int pinned(int slot, size_t bytes, void **out);
+  int ensure_tables(int nmax);
+  int sync_streams_table();
+  const Stream *get_stream(int handle) const;
+  unsigned *counter(int i);
+};

@@ -1,0 +1,515 @@
+// kernels.cu -- sm_103a kernels of the likelihood path.
+//
+//   k_waveform / k_response   fourier_waveform / fourier_detector_response arrays (FP64)
+//   k_inner                   Log_Likelihood_internal on given arrays (FP64 Simpson)
+//   k_plain                   the drop-in: one request per launch, FP64, fused
+//                             waveform -> projection -> Simpson inner product
+//   k_prologue                batched per-request FP64 prologue, one thread per request
+//   k_batch<fp64|mixed>       persistent fused bin kernel over (request, bin tile) items
+//
+// Reductions are deterministic: per-block partial sums are written to a
+// scratch array and the last block to finish (per request) adds them in a
+// fixed order in FP64.
+#include <cstdint>
+#include <cstdio>
+
+#include "kernels.h"
+
+namespace gwk {
+using namespace gwt;
+
+struct PlainStreams {
+  StreamDev s[kMaxDet];
+};
+
+__device__ __forceinline__ double2 to_d2(cd a) { return make_double2(a.re, a.im); }
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide FP64 sums of NV values per thread; result valid in thread 0.
+// smem must hold 32 * NV doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double *smem) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; j++) v[j] = warp_sum(v[j]);
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < NV; j++) smem[warp * NV + j] = v[j];
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+      double x = (lane < nw) ? smem[lane * NV + j] : 0.0;
+      v[j] = warp_sum(x);
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------- waveform
+__global__ void k_waveform(const __grid_constant__ Request r, const double *__restrict__ freqs, int N,
+                           double2 *__restrict__ hp, double2 *__restrict__ hc) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+    cd a, b;
+    wave_bin(r, freqs[k], a, b);
+    hp[k] = to_d2(a);
+    hc[k] = to_d2(b);
+  }
+}
+__global__ void k_response(const __grid_constant__ Request r, int slot, int apply_shift,
+                           const double *__restrict__ freqs, int N, double2 *__restrict__ out) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+    cd a, b;
+    double f = freqs[k];
+    wave_bin(r, f, a, b);
+    out[k] = to_d2(response_bin(r.det[slot], a, b, f, apply_shift != 0));
+  }
+}
+
+cudaError_t launch_waveform(const Request &r, const double *freqs, int N, double *hp, double *hc, cudaStream_t s) {
+  int block = 128, grid = (N + block - 1) / block;
+  k_waveform<<<grid, block, 0, s>>>(r, freqs, N, (double2 *)hp, (double2 *)hc);
+  return cudaGetLastError();
+}
+cudaError_t launch_response(const Request &r, int slot, int apply_shift, const double *freqs, int N, double *out,
+                            cudaStream_t s) {
+  int block = 128, grid = (N + block - 1) / block;
+  k_response<<<grid, block, 0, s>>>(r, slot, apply_shift, freqs, N, (double2 *)out);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------ last-block finalisation
+// Returns true in every thread of the block that finished last.
+__device__ __forceinline__ bool arrive_last(unsigned *counter, unsigned expected) {
+  __shared__ bool s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned prev = atomicAdd(counter, 1u);
+    s_last = (prev == expected - 1);
+  }
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last;
+}
+
+// ------------------------------------------------------ Simpson inner product
+__global__ void k_inner(const double2 *__restrict__ data, const double *__restrict__ psd,
+                        const double2 *__restrict__ resp, int N, double simpson_df, double *partials,
+                        unsigned *counter, double *out) {
+  __shared__ double smem[32 * 2];
+  double v[2] = {0.0, 0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+    double w = simpson_weight(k, N);
+    double2 r = resp[k], d = data[k];
+    double S = psd[k];
+    v[0] += w * ((r.x * r.x + r.y * r.y) / S);
+    v[1] += w * ((d.x * r.x + d.y * r.y) / S);
+  }
+  block_sum<2>(v, smem);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x * 2 + 0] = v[0];
+    partials[blockIdx.x * 2 + 1] = v[1];
+  }
+  if (arrive_last(counter, gridDim.x)) {
+    if (threadIdx.x == 0) {
+      double hh = 0, dh = 0;
+      for (unsigned b = 0; b < gridDim.x; b++) {
+        hh += __ldcg(&partials[b * 2 + 0]);
+        dh += __ldcg(&partials[b * 2 + 1]);
+      }
+      double c = 4. * simpson_df / 3.;
+      out[0] = -0.5 * (c * hh - 2 * c * dh);
+      *counter = 0;
+    }
+  }
+}
+cudaError_t launch_inner_product(const double *data, const double *psd, const double *resp, int N, double simpson_df,
+                                 double *partials, unsigned *counter, double *out, cudaStream_t s) {
+  int block = 256, grid = (N + block - 1) / block;
+  if (grid > 1024) grid = 1024;
+  k_inner<<<grid, block, 0, s>>>((const double2 *)data, psd, (const double2 *)resp, N, simpson_df, partials, counter,
+                                 out);
+  return cudaGetLastError();
+}
+
+// --------------------------------------------------------------- FP64 bins
+// Accumulate one bin of the reference arithmetic into v[2*d] (HH) and
+// v[2*d+1] (DH), Simpson-weighted (mcmc_gw.cpp:801-873).
+template <int NDET>
+__device__ __forceinline__ void fp64_bin(const Request &r, const StreamDev *st, int k, int N, double (&v)[2 * NDET]) {
+  const double f = st[0].freqs[k];
+  cd hp, hc;
+  wave_bin(r, f, hp, hc);
+  const double w = simpson_weight(k, N);
+#pragma unroll
+  for (int d = 0; d < NDET; d++) {
+    cd x = response_bin(r.det[d], hp, hc, f, r.det[d].tau != 0.0);
+    double2 dd = ((const double2 *)st[d].data)[k];
+    double S = st[d].psd[k];
+    v[2 * d] += w * ((x.re * x.re + x.im * x.im) / S);
+    v[2 * d + 1] += w * ((dd.x * x.re + dd.y * x.im) / S);
+  }
+}
+template <int NDET>
+__device__ __forceinline__ double fp64_finalize(const double *s, const StreamDev *st) {
+  double ll = 0;
+#pragma unroll
+  for (int d = 0; d < NDET; d++) {
+    double c = 4. * st[d].simpson_df / 3.;
+    ll += -0.5 * (c * s[2 * d] - 2 * c * s[2 * d + 1]);
+  }
+  return ll;
+}
+
+// ------------------------------------------------------------------ plain
+template <int NDET>
+__global__ void __launch_bounds__(128) k_plain(const __grid_constant__ Request r, const __grid_constant__ PlainStreams ps,
+                                               double *partials, unsigned *counter, double *out, int *status) {
+  __shared__ double smem[32 * 2 * NDET];
+  const int N = ps.s[0].N;
+  double v[2 * NDET];
+#pragma unroll
+  for (int j = 0; j < 2 * NDET; j++) v[j] = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) fp64_bin<NDET>(r, ps.s, k, N, v);
+  block_sum<2 * NDET>(v, smem);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int j = 0; j < 2 * NDET; j++) partials[blockIdx.x * (2 * NDET) + j] = v[j];
+  if (arrive_last(counter, gridDim.x)) {
+    if (threadIdx.x == 0) {
+      double s[2 * NDET];
+#pragma unroll
+      for (int j = 0; j < 2 * NDET; j++) s[j] = 0.0;
+      for (unsigned b = 0; b < gridDim.x; b++)
+#pragma unroll
+        for (int j = 0; j < 2 * NDET; j++) s[j] += __ldcg(&partials[b * (2 * NDET) + j]);
+      out[0] = fp64_finalize<NDET>(s, ps.s);
+      if (status) status[0] = r.m.status ? 4 : 0;
+      *counter = 0;
+    }
+  }
+}
+int plain_blocks(int N) {
+  int g = (N + 127) / 128;
+  return g < 1 ? 1 : g;
+}
+cudaError_t launch_plain(const Request &r, const StreamDev *streams, int ndet, double *partials, unsigned *counter,
+                         double *out, int *status, cudaStream_t s) {
+  PlainStreams ps;
+  for (int d = 0; d < ndet; d++) ps.s[d] = streams[d];
+  int grid = plain_blocks(streams[0].N);
+  switch (ndet) {
+    case 1: k_plain<1><<<grid, 128, 0, s>>>(r, ps, partials, counter, out, status); break;
+    case 2: k_plain<2><<<grid, 128, 0, s>>>(r, ps, partials, counter, out, status); break;
+    case 3: k_plain<3><<<grid, 128, 0, s>>>(r, ps, partials, counter, out, status); break;
+    case 4: k_plain<4><<<grid, 128, 0, s>>>(r, ps, partials, counter, out, status); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- prologue
+__global__ void k_prologue(const GenParams *__restrict__ params, const int *__restrict__ approx, int n,
+                           const int *__restrict__ handles, int ndet, double T_segment, int tc_from_segment,
+                           const StreamDev *__restrict__ streams, const double *__restrict__ qnm, Request *req,
+                           MixedReq *mreq, int want_mixed, int *status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  GenParams p = params[i];
+  int ap = approx[i];
+  if (tc_from_segment) p.tc = T_segment - p.tc;  // mcmc_gw.cpp:2466-2473
+  int dets[kMaxDet];
+  const StreamDev &s0 = streams[handles[i * ndet]];
+  int st = 0;
+  for (int d = 0; d < ndet; d++) {
+    const StreamDev &sd = streams[handles[i * ndet + d]];
+    dets[d] = sd.det;
+    if (sd.N != s0.N) st = 1;
+  }
+  bool bad = !(p.mass1 > 0) || !(p.mass2 > 0) || !(p.Luminosity_Distance > 0) || (ap != 0 && ap != 1);
+  Request r;
+  if (!bad) {
+    request_prologue(r, p, ap, dets, ndet, qnm);
+    if (r.m.status) st = 4;
+    if (req) req[i] = r;
+    if (want_mixed) {
+      if (!s0.uniform_int) st = st ? st : 1;
+      mixed_prologue(r, s0.df, mreq[i]);
+    }
+  } else {
+    st = 4;
+  }
+  if (st && want_mixed) mreq[i].status = st;
+  if (st && req) req[i].m.status = st;
+  status[i] = st;
+}
+cudaError_t launch_prologue(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
+                            double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
+                            Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s) {
+  int block = 32, grid = (n + block - 1) / block;
+  k_prologue<<<grid, block, 0, s>>>(params, approx, n, handles, ndet, T_segment, tc_from_segment, streams, qnm, req,
+                                    mreq, want_mixed, status);
+  return cudaGetLastError();
+}
+
+// MCMC_prep_params + repack_parameters (mcmc_gw.cpp:2492-2510; fisher.cpp:2171-2284)
+__global__ void k_mcmc_repack(const double *__restrict__ theta, int dim, int n, int approximant, double gmst,
+                              GenParams *out, int *approx_out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double *th = theta + (size_t)i * dim;
+  GenParams o;
+  o.spin1[0] = o.spin1[1] = o.spin1[2] = 0;
+  o.spin2[0] = o.spin2[1] = o.spin2[2] = 0;
+  o.chip = -1;
+  o.phip = -1;
+  o.sky_average = 0;
+  o.dep_postmerger = 0;
+  o.f_ref = 20;
+  o.shift_time = 1;
+  o.shift_phase = 1;
+  o.gmst = gmst;
+  o.mass1 = calc_mass1(exp(th[7]), th[8]);
+  o.mass2 = calc_mass2(exp(th[7]), th[8]);
+  o.Luminosity_Distance = exp(th[6]);
+  o.RA = th[0];
+  o.DEC = asin(th[1]);
+  o.psi = th[2];
+  o.incl_angle = acos(th[3]);
+  o.phiRef = th[4];
+  o.tc = th[5];
+  if (approximant == kPhenomPv2 && dim >= 15) {
+    double t1 = th[11] > 1 ? 0 : (th[11] < -1 ? kPi : acos(th[11]));
+    double t2 = th[12] > 1 ? 0 : (th[12] < -1 ? kPi : acos(th[12]));
+    o.spin1[0] = th[9] * sin(t1) * cos(th[13]);
+    o.spin1[1] = th[9] * sin(t1) * sin(th[13]);
+    o.spin1[2] = th[9] * cos(t1);
+    o.spin2[0] = th[10] * sin(t2) * cos(th[14]);
+    o.spin2[1] = th[10] * sin(t2) * sin(th[14]);
+    o.spin2[2] = th[10] * cos(t2);
+  } else {
+    o.spin1[2] = th[9];
+    o.spin2[2] = th[10];
+  }
+  out[i] = o;
+  approx_out[i] = approximant;
+}
+cudaError_t launch_mcmc_repack(const double *theta, int dim, int n, int approximant, double gmst, GenParams *out,
+                               int *approx_out, cudaStream_t s) {
+  int block = 128, grid = (n + block - 1) / block;
+  k_mcmc_repack<<<grid, block, 0, s>>>(theta, dim, n, approximant, gmst, out, approx_out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------- batched kernels
+constexpr int kBatchBlock = 256;
+
+// Two-level compensated reduction of NV FP32 values per thread:
+// 16-element TwoSum columns, then FP64 across columns.  Result in res[0..NV).
+template <int NV>
+__device__ __forceinline__ void block_sum_mixed(const float (&v)[NV], float *sm, double *res) {
+  const int tid = threadIdx.x, nt = blockDim.x;  // nt == kBatchBlock
+#pragma unroll
+  for (int j = 0; j < NV; j++) sm[j * kBatchBlock + tid] = v[j];
+  __syncthreads();
+  constexpr int kCols = kBatchBlock / 16;
+  __shared__ float s_hi[kAcc * kCols], s_lo[kAcc * kCols];
+  for (int w = tid; w < NV * kCols; w += nt) {
+    int j = w / kCols, c = w % kCols;
+    const float *p = sm + j * kBatchBlock + c * 16;
+    float hi = 0.f, lo = 0.f;
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      float a = p[q];
+      float s = hi + a;
+      float bp = s - hi;
+      float e = (hi - (s - bp)) + (a - bp);
+      hi = s;
+      lo += e;
+    }
+    s_hi[j * kCols + c] = hi;
+    s_lo[j * kCols + c] = lo;
+  }
+  __syncthreads();
+  if (tid < NV) {
+    double acc = 0.0;
+    for (int c = 0; c < kCols; c++) acc += (double)s_hi[tid * kCols + c] + (double)s_lo[tid * kCols + c];
+    res[tid] = acc;
+  }
+  __syncthreads();
+}
+
+template <int NDET, int MIXED>
+__global__ void __launch_bounds__(kBatchBlock) k_batch(const BatchArgs a) {
+  constexpr int NV = MIXED ? NDET * kAccPerDet : 2 * NDET;
+  __shared__ int s_item;
+  __shared__ __align__(16) unsigned char s_req[MIXED ? sizeof(MixedReq) : sizeof(Request)];
+  __shared__ StreamDev s_st[NDET];
+  __shared__ double s_res[NV];
+  __shared__ float s_red[MIXED ? NV * kBatchBlock : 1];
+  __shared__ double s_dsm[32 * (MIXED ? 1 : NV)];
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= a.nitems) break;
+    const Item I = a.items[it];
+    // stage the request constants and its streams
+    {
+      const unsigned *src = MIXED ? (const unsigned *)(a.mreq + I.req) : (const unsigned *)(a.req + I.req);
+      unsigned *dst = (unsigned *)s_req;
+      constexpr int nw = (MIXED ? sizeof(MixedReq) : sizeof(Request)) / 4;
+      for (int w = tid; w < nw; w += blockDim.x) dst[w] = src[w];
+      if (tid < NDET) s_st[tid] = a.streams[a.handles[I.req * a.ndet + tid]];
+    }
+    __syncthreads();
+    const int N = s_st[0].N;
+    const int kend = min(I.k0 + a.tile, N);
+    if constexpr (MIXED) {
+      const MixedReq &x = *(const MixedReq *)s_req;
+      KSum acc[NV];
+#pragma unroll
+      for (int j = 0; j < NV; j++) acc[j] = KSum{0.f, 0.f};
+      if (x.status == 0) {
+        const int n0 = s_st[0].n0;
+        const float *dh[NDET];
+        const float *wh[NDET];
+#pragma unroll
+        for (int d = 0; d < NDET; d++) {
+          dh[d] = s_st[d].dhat;
+          wh[d] = s_st[d].what;
+        }
+        const int kcut = min(kend, x.n_cut - n0 + 1);
+        for (int k = I.k0 + tid; k < kcut; k += blockDim.x) {
+          const int n = n0 + k;
+          float dre[NDET], dim[NDET], w[NDET];
+#pragma unroll
+          for (int d = 0; d < NDET; d++) {
+            float2 v = __ldg(((const float2 *)dh[d]) + k);
+            dre[d] = v.x;
+            dim[d] = v.y;
+            w[d] = __ldg(wh[d] + k);
+          }
+          mixed_bin<NDET>(x, n, __ldg(a.tables.t13 + n), __ldg(a.tables.tm53 + n), __ldg(a.tables.tln + n),
+                          __ldg(a.tables.t34 + n), __ldg(a.tables.t13f + n), __ldg(a.tables.tm76f + n), dre, dim, w,
+                          acc);
+        }
+      }
+      float v[NV];
+#pragma unroll
+      for (int j = 0; j < NV; j++) v[j] = acc[j].s - acc[j].c;
+      block_sum_mixed<NV>(v, s_red, s_res);
+    } else {
+      const Request &r = *(const Request *)s_req;
+      double v[NV];
+#pragma unroll
+      for (int j = 0; j < NV; j++) v[j] = 0.0;
+      if (r.m.status == 0)
+        for (int k = I.k0 + tid; k < kend; k += blockDim.x) fp64_bin<NDET>(r, s_st, k, N, v);
+      block_sum<NV>(v, s_dsm);
+      if (tid == 0)
+#pragma unroll
+        for (int j = 0; j < NV; j++) s_res[j] = v[j];
+      __syncthreads();
+    }
+    if (tid < NV) a.partials[(size_t)it * kAcc + tid] = s_res[tid];
+    // last item of this request: fixed-order FP64 sum and log L
+    if (arrive_last(a.req_done + I.req, (unsigned)a.item_count[I.req])) {
+      if (tid == 0) {
+        double s[NV];
+#pragma unroll
+        for (int j = 0; j < NV; j++) s[j] = 0.0;
+        const int i0 = a.item_start[I.req], ic = a.item_count[I.req];
+        for (int q = 0; q < ic; q++)
+#pragma unroll
+          for (int j = 0; j < NV; j++) s[j] += __ldcg(&a.partials[(size_t)(i0 + q) * kAcc + j]);
+        double ll;
+        int st;
+        if constexpr (MIXED) {
+          const MixedReq &x = *(const MixedReq *)s_req;
+          double ds[kMaxDet], ws[kMaxDet];
+          for (int d = 0; d < NDET; d++) {
+            ds[d] = s_st[d].dscale;
+            ws[d] = s_st[d].wscale;
+          }
+          double full[kAcc];
+          for (int j = 0; j < kAcc; j++) full[j] = j < NV ? s[j] : 0.0;
+          ll = mixed_finalize(x, full, ds, ws);
+          st = x.status;
+        } else {
+          const Request &r = *(const Request *)s_req;
+          ll = fp64_finalize<NDET>(s, s_st);
+          st = r.m.status;
+        }
+        a.out[I.req] = st ? __longlong_as_double(0x7ff8000000000000ll) : ll;
+        a.status[I.req] = st;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+int batch_block_size(int) { return kBatchBlock; }
+
+int batch_occupancy(int mixed, int ndet) {
+  int nb = 0;
+  const void *f = nullptr;
+  switch (ndet * 2 + (mixed ? 1 : 0)) {
+    case 2: f = (const void *)k_batch<1, 0>; break;
+    case 3: f = (const void *)k_batch<1, 1>; break;
+    case 4: f = (const void *)k_batch<2, 0>; break;
+    case 5: f = (const void *)k_batch<2, 1>; break;
+    case 6: f = (const void *)k_batch<3, 0>; break;
+    case 7: f = (const void *)k_batch<3, 1>; break;
+    case 8: f = (const void *)k_batch<4, 0>; break;
+    case 9: f = (const void *)k_batch<4, 1>; break;
+    default: return 1;
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, kBatchBlock, 0) != cudaSuccess) return 1;
+  return nb;
+}
+
+cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int block, cudaStream_t s) {
+  (void)block;
+#define GWK_CASE(ND, MX) k_batch<ND, MX><<<grid, kBatchBlock, 0, s>>>(a)
+  if (mixed) {
+    switch (a.ndet) {
+      case 1: GWK_CASE(1, 1); break;
+      case 2: GWK_CASE(2, 1); break;
+      case 3: GWK_CASE(3, 1); break;
+      case 4: GWK_CASE(4, 1); break;
+      default: return cudaErrorInvalidValue;
+    }
+  } else {
+    switch (a.ndet) {
+      case 1: GWK_CASE(1, 0); break;
+      case 2: GWK_CASE(2, 0); break;
+      case 3: GWK_CASE(3, 0); break;
+      case 4: GWK_CASE(4, 0); break;
+      default: return cudaErrorInvalidValue;
+    }
+  }
+#undef GWK_CASE
+  return cudaGetLastError();
+}
+
+void qnm_host_table(double *o) {
+  const int n = kQnmLen;
+  for (int i = 0; i < n; i++) {
+    o[i] = gwt_qnm_a_h[i];
+    o[n + i] = gwt_qnm_fring_h[i];
+    o[2 * n + i] = gwt_qnm_fdamp_h[i];
+  }
+  double work[6 * kQnmLen];
+  cspline_coeffs(o, o + n, n, o + 3 * n, work);
+  cspline_coeffs(o, o + 2 * n, n, o + 4 * n, work);
+}
+
+}  // namespace gwk

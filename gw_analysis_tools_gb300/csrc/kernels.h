@@ -1,0 +1,82 @@
+// kernels.h -- launch interface of the GB300 kernels (host side, no CUDA types
+// beyond cudaStream_t in the launchers).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "phenom_mixed.h"
+
+namespace gwk {
+
+using gwt::GenParams;
+using gwt::MixedReq;
+using gwt::Request;
+
+// One registered detector stream, as the kernels see it.
+struct StreamDev {
+  int det;            // detector index into the constant tables
+  int N;              // bins
+  int n0;             // f_k = (n0 + k) df when uniform_int
+  int uniform_int;    // 1 when the grid is uniform with f0 an integer multiple of df
+  double df;          // f[1] - f[0]
+  double simpson_df;  // f[N/2] - f[N/2-1] (mcmc_gw.cpp:811)
+  const double *freqs, *data, *psd;  // FP64 originals (data interleaved complex)
+  const float *dhat, *what;          // mixed-form streams (interleaved complex, real)
+  double dscale, wscale;
+};
+
+struct Item {
+  int req, k0;
+};
+
+constexpr int kAcc = gwt::kMaxDet * gwt::kAccPerDet;  // per-request accumulators
+
+// Tables for the mixed form (device pointers).
+struct DevTables {
+  gwt::Tables t;
+};
+
+// ---- launchers (return cudaError_t of the launch) ----
+cudaError_t launch_waveform(const Request &r, const double *freqs, int N, double *hp, double *hc, cudaStream_t s);
+cudaError_t launch_response(const Request &r, int det_slot, int apply_shift, const double *freqs, int N, double *out,
+                            cudaStream_t s);
+// Simpson inner product of given response/data/psd arrays (Log_Likelihood_internal).
+cudaError_t launch_inner_product(const double *data, const double *psd, const double *resp, int N, double simpson_df,
+                                 double *partials, unsigned *counter, double *out, cudaStream_t s);
+// Plain form: one request, FP64, one launch.  out[0] = log L.
+cudaError_t launch_plain(const Request &r, const StreamDev *streams, int ndet, double *partials, unsigned *counter,
+                         double *out, int *status, cudaStream_t s);
+int plain_blocks(int N);
+
+// Batched: prologue (one thread per request) then the fused bin kernel.
+cudaError_t launch_prologue(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
+                            double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
+                            Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s);
+cudaError_t launch_mcmc_repack(const double *theta, int dim, int n, int approximant, double gmst, GenParams *out,
+                               int *approx_out, cudaStream_t s);
+struct BatchArgs {
+  const Request *req;
+  const MixedReq *mreq;
+  const int *handles;  // n * ndet
+  int ndet;
+  const StreamDev *streams;
+  const Item *items;
+  int nitems;
+  const int *item_start;  // per request
+  const int *item_count;
+  int tile;               // bins per item
+  unsigned *item_counter;  // dynamic item scheduler (zeroed before launch)
+  unsigned *req_done;      // per request finished-item counters (zeroed before launch)
+  double *partials;        // nitems * kAcc
+  double *out;
+  int *status;
+  gwt::Tables tables;
+};
+cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int block, cudaStream_t s);
+int batch_block_size(int mixed);
+int batch_occupancy(int mixed, int ndet);  // resident blocks per SM
+
+// Host-side helpers shared with the C API.
+void qnm_host_table(double *out5x1003);  // x, fring, fdamp, c_fring, c_fdamp
+
+}  // namespace gwk

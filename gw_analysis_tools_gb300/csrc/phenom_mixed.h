@@ -1,0 +1,465 @@
+// phenom_mixed.h -- mixed-precision per-bin evaluation of the extrinsic
+// log-likelihood (host and device).
+//
+// Same quantity as MCMC_likelihood_extrinsic (mcmc_gw.cpp:2374-2487) on a
+// uniform grid f_n = n * df (n = n0 + k, integer), regrouped so that:
+//  * the smooth PN/intermediate/ringdown phase stays FP64, evaluated as
+//    polynomials in per-bin table values n^(1/3), n^(-5/3), ln n, n^(3/4)
+//    that are shared by every request (no FP64 transcendental per bin);
+//  * every phase term linear in f (2 pi f t_c, phi_c, detector delays, the
+//    Pv2 time shift) is an exact 64-bit fixed-point count of turns;
+//  * amplitude, antenna projection and the data products are FP32, with
+//    per-request constants (A0, |G_d|^2, data scales) factored out and applied
+//    in FP64 at the end, and Kahan-compensated FP32 sums.
+#pragma once
+
+#include "phenom_bins.h"
+
+#if !defined(__CUDA_ARCH__)
+#include <cmath>
+#endif
+
+namespace gwt {
+
+// Per-bin tables indexed by n (shared by all requests on grids with integer n0).
+struct Tables {
+  const double *t13;   // n^(1/3)
+  const double *tm53;  // n^(-5/3)
+  const double *tln;   // ln n
+  const double *t34;   // n^(3/4)
+  const float *t13f;   // n^(1/3)
+  const float *tm76f;  // n^(-7/6)
+  int nmax;            // tables valid for 1 <= n <= nmax
+};
+
+// One detector stream of a registered grid, prepared for the mixed form:
+// dhat = W d / dscale (complex64), what = W / wscale with the Simpson-weighted
+// whitening W_k = (4 df/3) s_k / S_k (mcmc_gw.cpp:811-868, util.h:844-856).
+struct MixedStream {
+  const float *dhat;  // interleaved (re, im)
+  const float *what;
+  double dscale, wscale;
+};
+
+struct MixedDet {
+  uint64_t L0, L1;   // linear phase, turns * 2^64: L0 + L1 * n
+  double Gre, Gim;   // D: F+ (1+c^2)/2, -Fx c ; Pv2: P_d, Q_d (real); applied in FP64 at the end
+};
+
+struct MixedReq {
+  int approximant, status, ndet, pad;
+  int n_f1, n_f3, n_f1p, n_f2p, n_cut;  // region starts (first n in region) and last non-zero n
+  int n_mid, n_rd, n_c, pad2;
+  double A_scale;                       // amplitude scale applied in FP64
+  // phase, FP64
+  double qi[12];                        // inspiral: tm53 * sum qi_j t^j + tln * (bi0 + bi1 t)
+  double bi0, bi1;
+  double pA, pB, pC, pD;                // intermediate: pA + pB n + pC tln - pD n^-3
+  double mA, mB, mC, mD, mE;            // ringdown: mA + mB n - mC/n + mD n^(3/4) + mE atan(y)
+  // amplitude, FP32
+  // Per-request FP32 coefficients are stored as hi + lo pairs so that their
+  // rounding does not bias every bin the same way.
+  float ai[10], ai_lo[10];              // inspiral: sum ai_j t^j
+  float ei[5], ei_lo[5];                // intermediate: sum ei_j (n - n_mid)^j
+  float mrK, mrK_lo, mrExp, mrExp_lo;   // ringdown: mrK exp(-mrExp x) / (x^2 + mrG2), x = n - n_rd - frac
+  float mrG2, mrG2_lo, mrRDfrac, pad3;
+  float ncfrac, inv_nw;                 // atan argument y = (n - n_c - ncfrac) * inv_nw
+  // Pv2
+  double ea[6], ee[6];                  // alpha/epsilon: r*(a0 t^2 + a1 n + a2 n t) + a3 + a4 t + a5 tln
+  float Y[5], Y_lo[5];
+  // 1/s = (w0 + w1 x + w2 x^2)/sqrt(x) + w3 with x = x2c t^2 (L2PN, WignerD)
+  float w[4], w_lo[4];
+  float x2c, x2c_lo;
+  MixedDet det[kMaxDet];
+};
+
+GW_HD void split_f(double v, float &hi, float &lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+// Q64 turns helpers
+GW_HD uint64_t turns_q64(double turns) {  // frac(turns) * 2^64
+  double fr = turns - floor(turns);
+  double v = fr * 18446744073709551616.0;
+  if (v >= 18446744073709551616.0) return 0;
+  return (uint64_t)v;
+}
+
+// Build the mixed constants of one request for a grid with spacing df and
+// integer offset (f_n = n df).  Returns the status of the prologue.
+GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x) {
+  const ModelD &m = r.m;
+  const Source &s = m.s;
+  const double M = s.M, eta = s.eta, Mdf = M * df;
+  x.approximant = r.approximant;
+  x.status = m.status;
+  x.ndet = r.ndet;
+  // region starts in n: first n with n*df >= boundary (strict "<" tests of build_amp/build_phase)
+  auto first_ge = [&](double fb) -> int {
+    double q = ceil(fb / df);
+    if (!(q < 2.0e9)) return 2000000000;
+    int n = (int)q;
+    if (n < 0) n = 0;
+    while (n > 0 && (double)(n - 1) * df >= fb) n--;
+    while ((double)n * df < fb) n++;
+    return n;
+  };
+  x.n_f1 = first_ge(s.f1);          // amp: f < f1 inspiral
+  x.n_f1p = first_ge(s.f1_phase);   // phase: f < f1_phase inspiral
+  {                                 // amp: f > f3 ringdown -> first n with n*df > f3
+    int n = first_ge(s.f3);
+    while ((double)n * df <= s.f3) n++;
+    x.n_f3 = n;
+  }
+  {
+    int n = first_ge(s.f2_phase);
+    while ((double)n * df <= s.f2_phase) n++;
+    x.n_f2p = n;
+  }
+  {  // last n with n*df <= fcut
+    int n = first_ge(m.fcut);
+    while ((double)n * df > m.fcut) n--;
+    x.n_cut = n;
+  }
+  const bool pv2 = (r.approximant == kPhenomPv2);
+  // amplitude scale: A0eff * (M df)^(-7/6) [* 1/2 for the Pv2 amp/2]
+  x.A_scale = m.A0eff * pow(Mdf, -7. / 6.) * (pv2 ? 0.5 : 1.0);
+  // ---------------- inspiral phase: u = (M f)^(1/3) = cu t, t = n^(1/3)
+  const double cu = cbrt(Mdf);
+  const double K = 3. / (128. * eta) * m.pi.PIminus_5third;
+  const double *pn = m.pn_phase;
+  const double Lc = log(kPi * Mdf);  // ln(pi M f) = Lc + ln n
+  double q[12];
+  q[0] = K * pn[0];
+  q[1] = K * pn[1] * m.pi.PIthird;
+  q[2] = K * pn[2] * m.pi.PI2third;
+  q[3] = K * pn[3] * kPi;
+  q[4] = K * pn[4] * m.pi.PI4third;
+  q[5] = K * m.pi.PI5third * (pn[8] + pn[9] * Lc) - kPi / 4.;
+  q[6] = K * m.pi.PIsquare * (pn[10] - pn[11] * Lc);
+  q[7] = K * pn[7] * m.pi.PI7third;
+  q[8] = m.l.sigma[1] / eta;
+  q[9] = (3. / 4.) * m.l.sigma[2] / eta;
+  q[10] = (3. / 5.) * m.l.sigma[3] / eta;
+  q[11] = (1. / 2.) * m.l.sigma[4] / eta;
+  double cp = pow(cu, -5.);
+  for (int j = 0; j < 12; j++) {
+    x.qi[j] = q[j] * cp;
+    cp *= cu;
+  }
+  x.bi0 = K * m.pi.PI5third * pn[9];
+  x.bi1 = -K * m.pi.PIsquare * pn[11] * cu;
+  // ---------------- intermediate phase
+  x.pA = (m.l.beta[0] + m.l.beta[2] * log(Mdf)) / eta;
+  x.pB = m.l.beta[1] * Mdf / eta;
+  x.pC = m.l.beta[2] / eta;
+  x.pD = m.l.beta[3] / (3. * eta * Mdf * Mdf * Mdf);
+  // ---------------- ringdown phase
+  x.mA = m.l.alpha[0] / eta;
+  x.mB = m.l.alpha[1] * Mdf / eta;
+  x.mC = m.l.alpha[2] / (eta * Mdf);
+  x.mD = (4. / 3.) * m.l.alpha[3] * pow(Mdf, 0.75) / eta;
+  x.mE = m.l.alpha[4] / eta;
+  {
+    double nc = m.l.alpha[5] * s.fRD / df;
+    double nci = floor(nc);
+    x.n_c = (int)nci;
+    x.ncfrac = (float)(nc - nci);
+    x.inv_nw = (float)(df / s.fdamp);
+  }
+  // ---------------- inspiral amplitude: sum_i pn_i (pi M f)^(i/3) + rho (Mf)^(7..9)/3
+  {
+    const double *pa = m.pn_amp;
+    double a[10];
+    a[0] = pa[0];
+    a[1] = pa[1] * m.pi.PIthird;
+    a[2] = pa[2] * m.pi.PI2third;
+    a[3] = pa[3] * kPi;
+    a[4] = pa[4] * m.pi.PI4third;
+    a[5] = pa[5] * m.pi.PI5third;
+    a[6] = pa[6] * m.pi.PIsquare;
+    a[7] = m.l.rho[0];
+    a[8] = m.l.rho[1];
+    a[9] = m.l.rho[2];
+    double c = 1.0;
+    for (int j = 0; j < 10; j++) {
+      split_f(a[j] * c, x.ai[j], x.ai_lo[j]);
+      c *= cu;
+    }
+  }
+  // ---------------- intermediate amplitude: quartic in Mf re-centred on n_mid
+  {
+    double nmid = floor(0.5 * (s.f1 + s.f3) / df);
+    x.n_mid = (int)nmid;
+    const double *d = m.deltas;
+    double c0 = d[0], c1 = d[1] * Mdf, c2 = d[2] * Mdf * Mdf, c3 = d[3] * Mdf * Mdf * Mdf,
+           c4 = d[4] * Mdf * Mdf * Mdf * Mdf;  // polynomial in n
+    double h = nmid;  // p(n) = sum c_j n^j = sum e_j (n - h)^j
+    split_f(c4, x.ei[4], x.ei_lo[4]);
+    split_f(c3 + 4 * c4 * h, x.ei[3], x.ei_lo[3]);
+    split_f(c2 + 3 * c3 * h + 6 * c4 * h * h, x.ei[2], x.ei_lo[2]);
+    split_f(c1 + 2 * c2 * h + 3 * c3 * h * h + 4 * c4 * h * h * h, x.ei[1], x.ei_lo[1]);
+    split_f(c0 + c1 * h + c2 * h * h + c3 * h * h * h + c4 * h * h * h * h, x.ei[0], x.ei_lo[0]);
+  }
+  // ---------------- ringdown amplitude: g1 g3 fdamp M exp(-g2 (f-fRD)/(g3 fdamp)) / (M^2 ((f-fRD)^2 + (g3 fdamp)^2))
+  {
+    double g1 = m.l.gamma[0], g2 = m.l.gamma[1], g3 = m.l.gamma[2];
+    double nrd = s.fRD / df, nrdi = floor(nrd);
+    x.n_rd = (int)nrdi;
+    x.mrRDfrac = (float)(nrd - nrdi);
+    double w = g3 * s.fdamp / df;  // in bins
+    split_f(g1 * g3 * s.fdamp / (M * df * df), x.mrK, x.mrK_lo);
+    split_f(g2 / w, x.mrExp, x.mrExp_lo);
+    split_f(w * w, x.mrG2, x.mrG2_lo);
+  }
+  // ---------------- Pv2 angles
+  if (pv2) {
+    double cw = cbrt(kPi * Mdf);  // omega^(1/3) = cw t
+    const double *a = r.p.ac, *e = r.p.ec;
+    double Lw = log(kPi * Mdf);
+    // alpha = a0/w + a1/w^(2/3) + a2/w^(1/3) + a3 ln w + a4 w^(1/3); w = pi Mdf n
+    // with r = n^(-5/3): 1/n = r t^2, n^(-2/3) = r n, n^(-1/3) = r n t
+    x.ea[0] = a[0] / (kPi * Mdf);
+    x.ea[1] = a[1] / (cw * cw);
+    x.ea[2] = a[2] / cw;
+    x.ea[3] = a[3] * Lw + r.p.alpha_shift;
+    x.ea[4] = a[4] * cw;
+    x.ea[5] = a[3];
+    x.ee[0] = e[0] / (kPi * Mdf);
+    x.ee[1] = e[1] / (cw * cw);
+    x.ee[2] = e[2] / cw;
+    x.ee[3] = e[3] * Lw - r.p.eps_off;
+    x.ee[4] = e[4] * cw;
+    x.ee[5] = e[3];
+    for (int k = 0; k < 5; k++) split_f(r.p.Y[k], x.Y[k], x.Y_lo[k]);
+    // s = SP / (L + SL), L = eta (1 + l1 x + l2 x^2) / sqrt(x)  ->  1/s
+    double l1 = 1.5 + eta / 6.0, l2 = 3.375 - (19.0 * eta) / 8. - eta * eta / 24.0;
+    split_f(eta / s.SP, x.w[0], x.w_lo[0]);
+    split_f(eta * l1 / s.SP, x.w[1], x.w_lo[1]);
+    split_f(eta * l2 / s.SP, x.w[2], x.w_lo[2]);
+    split_f(s.SL / s.SP, x.w[3], x.w_lo[3]);
+    split_f(cw * cw, x.x2c, x.x2c_lo);  // L2PN x = (pi M f)^(2/3) = cw^2 t^2
+  }
+  // ---------------- linear phase per detector, in turns (f = n df):
+  // D:   psi_d = phi(f) - tcl (f - fref) - phic - tau_d f
+  // Pv2: psi_d = phi(f) + 2 eps(f) - tcl (f - fref) - phic + 2 pi t_corr f - tau_d f
+  const double inv2pi = 1.0 / (2.0 * kPi);
+  double c0 = (m.tcl * m.fref - m.phic) * inv2pi;
+  double c1 = -m.tcl * df * inv2pi;
+  if (pv2) c1 += r.p.t_corr * df;
+  double ci = cos(s.incl_angle);
+  for (int d = 0; d < r.ndet; d++) {
+    x.det[d].L0 = turns_q64(c0);
+    x.det[d].L1 = turns_q64(c1 - r.det[d].tau * df * inv2pi);
+    if (pv2) {
+      x.det[d].Gre = r.det[d].fp * r.p.c2z - r.det[d].fc * r.p.s2z;
+      x.det[d].Gim = r.det[d].fp * r.p.s2z + r.det[d].fc * r.p.c2z;
+    } else {
+      x.det[d].Gre = r.det[d].fp * .5 * (1 + ci * ci);
+      x.det[d].Gim = -r.det[d].fc * ci;
+    }
+  }
+  return x.status;
+}
+
+// ------------------------------------------------------------ per-bin math
+#if defined(__CUDA_ARCH__)
+GW_HD float __int_as_float_h(int i) { return __int_as_float(i); }
+GW_HD int __float_as_int_h(float f) { return __float_as_int(f); }
+GW_HD void gw_sincospif(float x, float *s, float *c) { sincospif(x, s, c); }
+GW_HD int64_t gw_llrint(double x) { return __double2ll_rn(x); }
+#else
+inline float __int_as_float_h(int i) {
+  float f;
+  std::memcpy(&f, &i, 4);
+  return f;
+}
+inline int __float_as_int_h(float f) {
+  int i;
+  std::memcpy(&i, &f, 4);
+  return i;
+}
+inline float rsqrtf(float x) { return 1.0f / std::sqrt(x); }
+GW_HD void gw_sincospif(float x, float *s, float *c) {
+  double a = 3.14159265358979323846 * (double)x;
+  *s = (float)std::sin(a);
+  *c = (float)std::cos(a);
+}
+GW_HD int64_t gw_llrint(double x) { return (int64_t)std::llrint(x); }
+#endif
+
+// Kahan-compensated FP32 accumulator: value = s - c.
+struct KSum {
+  float s, c;
+};
+GW_HD void kadd(KSum &k, float v) {
+  float y = v - k.c;
+  float t = k.s + y;
+  k.c = (t - k.s) - y;
+  k.s = t;
+}
+constexpr int kAccPerDet = 5;  // D uses 3 (hh, zr, zi); Pv2 uses 5 (spp, scc, spc, zp, zc)
+
+// Phase of the D model at bin n (FP64, radians), without the linear terms.
+GW_HD double mixed_phase_d(const MixedReq &x, int n, double t, double r, double lnn, double t34) {
+  if (n < x.n_f1p) {
+    const double *q = x.qi;
+    double p = q[11];
+    for (int j = 10; j >= 0; j--) p = p * t + q[j];
+    return r * p + lnn * (x.bi0 + x.bi1 * t);
+  }
+  double nd = (double)n;
+  if (n >= x.n_f2p) {
+    float y = ((float)(n - x.n_c) - x.ncfrac) * x.inv_nw;
+    double at = (double)atanf(y);
+    return x.mA + x.mB * nd - x.mC * (r * t * t) + x.mD * t34 + x.mE * at;
+  }
+  return x.pA + x.pB * nd + x.pC * lnn - x.pD * (r * r * t);
+}
+// Round hi + lo (|lo| < ulp(hi)) to FP32 stochastically with a per-bin
+// low-discrepancy dither u in [0, 1): the expectation over bins is hi + lo,
+// so the lo parts of per-request coefficients are not lost to round-to-nearest.
+GW_HD float sround(float hi, float lo, uint32_t u) {
+  float ahi = fabsf(hi);
+  float ulp = __int_as_float_h(__float_as_int_h(ahi) + 1) - ahi;
+  float p = fabsf(lo) / ulp;
+  float fu = (float)(u >> 8) * 5.9604644775390625e-08f;  // 2^-24
+  return (fu < p) ? hi + copysignf(ulp, lo) : hi;
+}
+GW_HD uint32_t dither(int n) { return (uint32_t)n * 2654435769u; }  // Weyl sequence, golden ratio
+
+// Amplitude / (A_scale) at bin n, FP32: hi part plus the lo part carried by
+// the hi/lo coefficient pairs, stochastically rounded.
+GW_HD float mixed_amp(const MixedReq &x, int n, float tf, float m76) {
+  float hi, lo;
+  if (n < x.n_f1) {
+    const float *c = x.ai, *cl = x.ai_lo;
+    hi = c[9];
+    lo = cl[9];
+#pragma unroll
+    for (int j = 8; j >= 0; j--) {
+      hi = fmaf(hi, tf, c[j]);
+      lo = fmaf(lo, tf, cl[j]);
+    }
+  } else if (n >= x.n_f3) {
+    float xx = (float)(n - x.n_rd) - x.mrRDfrac;
+    float den = fmaf(xx, xx, x.mrG2);
+    float e = expf(-x.mrExp * xx) / den;
+    hi = x.mrK * e;
+    lo = e * (x.mrK_lo - x.mrK * (x.mrExp_lo * xx + x.mrG2_lo / den));
+  } else {
+    float h = (float)(n - x.n_mid);
+    const float *e = x.ei, *el = x.ei_lo;
+    hi = e[4];
+    lo = el[4];
+#pragma unroll
+    for (int j = 3; j >= 0; j--) {
+      hi = fmaf(hi, h, e[j]);
+      lo = fmaf(lo, h, el[j]);
+    }
+  }
+  return sround(hi, lo, dither(n)) * m76;
+}
+GW_HD uint64_t phase_q64(double phase_rad) {  // radians -> turns * 2^64 (2^-32 turn resolution)
+  const double k = 4294967296.0 / (2.0 * 3.14159265358979323846);
+  return ((uint64_t)gw_llrint(phase_rad * k)) << 32;
+}
+GW_HD void q64_sincospi(uint64_t q, float *s, float *c) {
+  int32_t hi = (int32_t)(q >> 32);
+  gw_sincospif((float)hi * 4.656612873077393e-10f, s, c);  // 2^-31 half-turns
+}
+
+// One bin of the mixed form, accumulated into acc[d * kAccPerDet + j].
+// dre/dim/w: the detector streams at this bin.
+template <int NDET>
+GW_HD void mixed_bin(const MixedReq &x, int n, double t, double r, double lnn, double t34, float tf, float m76,
+                     const float *dre, const float *dim, const float *w, KSum *acc) {
+  if (n > x.n_cut) return;
+  float a = mixed_amp(x, n, tf, m76);
+  if (x.approximant != kPhenomPv2) {
+    uint64_t ph = phase_q64(mixed_phase_d(x, n, t, r, lnn, t34));
+    float aa = a * a;
+#pragma unroll
+    for (int d = 0; d < NDET; d++) {
+      uint64_t psi = ph + x.det[d].L0 + x.det[d].L1 * (uint64_t)n;
+      float sn, cs;
+      q64_sincospi(psi, &sn, &cs);
+      float ar = a * dre[d], ai = a * dim[d];
+      kadd(acc[d * kAccPerDet + 0], w[d] * aa);
+      kadd(acc[d * kAccPerDet + 1], ar * cs - ai * sn);
+      kadd(acc[d * kAccPerDet + 2], ar * sn + ai * cs);
+    }
+    return;
+  }
+  // Pv2: phase + 2 eps, Euler alpha (FP64), twist-up (FP32)
+  double nd = (double)n, t2 = t * t, nt = nd * t;
+  double alpha = r * (x.ea[0] * t2 + x.ea[1] * nd + x.ea[2] * nt) + x.ea[3] + x.ea[4] * t + x.ea[5] * lnn;
+  double eps = r * (x.ee[0] * t2 + x.ee[1] * nd + x.ee[2] * nt) + x.ee[3] + x.ee[4] * t + x.ee[5] * lnn;
+  uint64_t ph = phase_q64(mixed_phase_d(x, n, t, r, lnn, t34) + 2.0 * eps);
+  float sa, ca;
+  q64_sincospi(phase_q64(alpha), &sa, &ca);
+  // WignerD from L2PN (IMRPhenomP.cpp:665-693, 1214-1220)
+  float tf2 = tf * tf;
+  float xx = fmaf(x.x2c, tf2, x.x2c_lo * tf2);
+  float rs = 1.0f / sqrtf(xx);
+  float ph_ = fmaf(fmaf(x.w[2], xx, x.w[1]), xx, x.w[0]);
+  float pl_ = fmaf(fmaf(x.w_lo[2], xx, x.w_lo[1]), xx, x.w_lo[0]);
+  float us = sround(fmaf(ph_, rs, x.w[3]), fmaf(pl_, rs, x.w_lo[3]), dither(n) ^ 0x9e3779b9u);  // 1/s
+  float cb = us / sqrtf(fmaf(us, us, 1.0f));  // cos beta = 1/sqrt(1 + s^2)
+  float cbh = sqrtf((1.0f + cb) * 0.5f), sbh = sqrtf(fmaxf(1.0f - cb, 0.0f) * 0.5f);
+  float c2 = cbh * cbh, s2 = sbh * sbh;
+  float d2[5] = {s2 * s2, 2.f * cbh * s2 * sbh, 2.44948974278317788f * s2 * c2, 2.f * c2 * cbh * sbh, c2 * c2};
+  // exp(i m alpha), m = -2..2
+  float e2r = ca * ca - sa * sa, e2i = 2.f * ca * sa;
+  float er[5] = {e2r, ca, 1.f, ca, e2r}, ei[5] = {-e2i, -sa, 0.f, sa, e2i};
+  float hpr = 0.f, hpi = 0.f, hcr = 0.f, hci = 0.f;
+#pragma unroll
+  for (int m = -2; m <= 2; m++) {
+    float dm = (m == -1 || m == 1) ? -d2[2 - m] : d2[2 - m];  // dm2[m+2] = (-1)^m d2[2-m]
+    float y = x.Y[m + 2], yl = x.Y_lo[m + 2];
+    float a1 = fmaf(dm, y, dm * yl), a2 = fmaf(d2[m + 2], y, d2[m + 2] * yl);
+    float t2r = er[-m + 2] * a1, t2i = ei[-m + 2] * a1;  // T2m
+    float tmr = er[m + 2] * a2, tmi = ei[m + 2] * a2;    // Tm2m
+    hpr += t2r + tmr;
+    hpi += t2i + tmi;
+    hcr += -(t2i - tmi);
+    hci += (t2r - tmr);
+  }
+  float aa = a * a;
+  float spp = aa * (hpr * hpr + hpi * hpi), scc = aa * (hcr * hcr + hci * hci), spc = aa * (hpr * hcr + hpi * hci);
+#pragma unroll
+  for (int d = 0; d < NDET; d++) {
+    uint64_t psi = ph + x.det[d].L0 + x.det[d].L1 * (uint64_t)n;
+    float sn, cs;
+    q64_sincospi(psi, &sn, &cs);
+    // a * dhat * exp(i psi)
+    float qr = a * (dre[d] * cs - dim[d] * sn), qi = a * (dre[d] * sn + dim[d] * cs);
+    kadd(acc[d * kAccPerDet + 0], w[d] * spp);
+    kadd(acc[d * kAccPerDet + 1], w[d] * scc);
+    kadd(acc[d * kAccPerDet + 2], w[d] * spc);
+    kadd(acc[d * kAccPerDet + 3], qr * hpr + qi * hpi);  // Re(q conj(hpf))
+    kadd(acc[d * kAccPerDet + 4], qr * hcr + qi * hci);  // Re(q conj(hcf))
+  }
+}
+
+// log L of one request from its FP64 accumulated sums s[d * kAccPerDet + j].
+GW_HD double mixed_finalize(const MixedReq &x, const double *s, const double *dscale, const double *wscale) {
+  double ll = 0;
+  double A = x.A_scale;
+  for (int d = 0; d < x.ndet; d++) {
+    const double *v = s + d * kAccPerDet;
+    double G1 = x.det[d].Gre, G2 = x.det[d].Gim, HH, DH;
+    if (x.approximant != kPhenomPv2) {
+      HH = A * A * wscale[d] * (G1 * G1 + G2 * G2) * v[0];
+      DH = A * dscale[d] * (G1 * v[1] + G2 * v[2]);
+    } else {
+      HH = A * A * wscale[d] * (G1 * G1 * v[0] + G2 * G2 * v[1] + 2.0 * G1 * G2 * v[2]);
+      DH = A * dscale[d] * (G1 * v[3] + G2 * v[4]);
+    }
+    ll += -0.5 * (HH - 2 * DH);
+  }
+  return ll;
+}
+
+}  // namespace gwt

@@ -1,0 +1,467 @@
+// phenom_prologue.h -- per-request FP64 prologue (included by phenom_model.h).
+//
+// Computes every per-request constant of IMRPhenomD / IMRPhenomPv2 and of the
+// detector projection once, so that per-bin work is only the bin loop of
+// IMRPhenomD::construct_waveform (IMRPhenomD.cpp:476-501) or
+// IMRPhenomPv2::construct_waveform (IMRPhenomP.cpp:290-362).
+#pragma once
+
+namespace gwt {
+
+GW_HD double Damp_ins(double f, const ModelD &m) {  // IMRPhenomD.cpp:1407-1419
+  const double *pn = m.pn_amp;
+  double pn_amp = 0, M = m.s.M;
+  for (int i = 0; i < 7; i++) pn_amp += pn[i] * pow(kPi * (M), i / 3.) * pow(f, i / 3. - 1.) * (i / 3.);
+  double nr_amp = 0;
+  for (int i = 0; i < 3; i++) nr_amp += (m.l.rho[i]) * pow(M, (7. + i) / 3.) * pow(f, (7. + i) / 3. - 1.) * (7. + i) / 3.;
+  return pn_amp + nr_amp;
+}
+GW_HD double Damp_mr(double f, const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1514-1532
+  double g1 = l.gamma[0], g2 = l.gamma[1], g3 = l.gamma[2], fdamp = s.fdamp, fRD = s.fRD, M = s.M;
+  return -((exp(((-f + fRD) * g2) / (fdamp * g3)) * g1 *
+            (pow_int(f - fRD, 2) * g2 + 2 * fdamp * (f - fRD) * g3 + pow_int(fdamp, 2) * g2 * pow(g3, 2))) /
+           (pow(pow_int(f - fRD, 2) + pow_int(fdamp, 2) * pow_int(g3, 2), 2) * M));
+}
+GW_HD double Dphase_ins(double f, const Source &s, double *pn, const Lambda &l) {  // IMRPhenomD.cpp:1427-1460
+  double M = s.M, eta = s.eta;
+  pn_phase_coeff_nonstatic(s, pn, f);
+  double d0 = (1. / f) * (38645. * kPi / 756 - 65 * kPi * eta / 9 +
+                          s.delta_mass * (-732985. / 2268 - 140 * eta / 9) * s.chi_a +
+                          (-732985. / 2268 + 24260 * eta / 81 + 340 * eta * eta / 9) * s.chi_s);  // :1067-1081
+  double d1 = (-6848. * (1. / f) / 63);
+  double pn_phase = 0;
+  for (int i = 0; i < 8; i++) pn_phase += pn[i] * pow(kPi * M * f, i / 3.);
+  double phase_TF2 = +3. / (128 * eta) * pow(kPi * M, -5. / 3.) * (-5. / 3.) * pow(f, -5. / 3 - 1.) * pn_phase;
+  double pn_phase_deriv = 0;
+  for (int i = 0; i < 8; i++) pn_phase_deriv += pn[i] * pow(kPi * M, i / 3.) * (i / 3.) * pow(f, i / 3. - 1.);
+  pn_phase_deriv += d0 * pow(kPi * M * f, 5. / 3) + d1 * pow(kPi * M * f, 6. / 3);
+  phase_TF2 += pn_phase_deriv * (3. / (128 * eta) * pow(kPi * M * f, -5. / 3));
+  return phase_TF2 + (1. / eta) * (l.sigma[1] * M + l.sigma[2] * pow(M, 4. / 3.) * pow(f, 1. / 3) +
+                                   l.sigma[3] * pow(M, 5. / 3.) * pow(f, 2. / 3) + l.sigma[4] * pow(M, 2.) * f);
+}
+/* calculate_delta_parameter_0..4 (IMRPhenomD.cpp:1709-1785) */
+GW_HD double delta0(double f1, double f2, double f3, double v1, double v2, double v3, double dd1, double dd3, double M) {
+  (void)M;
+  return (-(dd3 * pow(f1, 2) * pow(f1 - f2, 2) * f2 * (f1 - f3) * (f2 - f3) * f3) +
+          dd1 * f1 * (f1 - f2) * f2 * (f1 - f3) * pow(f2 - f3, 2) * pow(f3, 2) - 4 * pow(f1, 2) * pow(f2, 3) * pow(f3, 2) * v1 +
+          3 * f1 * pow(f2, 4) * pow(f3, 2) * v1 + 8 * pow(f1, 2) * pow(f2, 2) * pow(f3, 3) * v1 -
+          4 * f1 * pow(f2, 3) * pow(f3, 3) * v1 - pow(f2, 4) * pow(f3, 3) * v1 - 4 * pow(f1, 2) * f2 * pow(f3, 4) * v1 -
+          f1 * pow(f2, 2) * pow(f3, 4) * v1 + 2 * pow(f2, 3) * pow(f3, 4) * v1 + 2 * f1 * f2 * pow(f3, 5) * v1 -
+          pow(f2, 2) * pow(f3, 5) * v1 + pow(f1, 5) * pow(f3, 2) * v2 - 3 * pow(f1, 4) * pow(f3, 3) * v2 +
+          3 * pow(f1, 3) * pow(f3, 4) * v2 - pow(f1, 2) * pow(f3, 5) * v2 + pow(f1, 5) * pow(f2, 2) * v3 -
+          2 * pow(f1, 4) * pow(f2, 3) * v3 + pow(f1, 3) * pow(f2, 4) * v3 - 2 * pow(f1, 5) * f2 * f3 * v3 +
+          pow(f1, 4) * pow(f2, 2) * f3 * v3 + 4 * pow(f1, 3) * pow(f2, 3) * f3 * v3 - 3 * pow(f1, 2) * pow(f2, 4) * f3 * v3 +
+          4 * pow(f1, 4) * f2 * pow(f3, 2) * v3 - 8 * pow(f1, 3) * pow(f2, 2) * pow(f3, 2) * v3 +
+          4 * pow(f1, 2) * pow(f2, 3) * pow(f3, 2) * v3) /
+         (pow(f1 - f2, 2) * pow(f1 - f3, 3) * pow(f2 - f3, 2));
+}
+GW_HD double delta1(double f1, double f2, double f3, double v1, double v2, double v3, double dd1, double dd3, double M) {
+  return (dd3 * f1 * pow(f1 - f2, 2) * (f1 - f3) * (f2 - f3) * (2 * f2 * f3 + f1 * (f2 + f3)) +
+          f3 * (-(dd1 * (f1 - f2) * (f1 - f3) * pow(f2 - f3, 2) * (f2 * f3 + f1 * (2 * f2 + f3))) -
+                2 * f1 *
+                    (pow(f3, 4) * (v1 - v2) +
+                     f1 * (2 * pow(f3, 3) * (-v1 + v2) - 4 * pow(f2, 3) * (v1 - v3) + 6 * pow(f2, 2) * f3 * (v1 - v3)) +
+                     3 * pow(f2, 4) * (v1 - v3) + pow(f1, 4) * (v2 - v3) + 4 * pow(f2, 3) * f3 * (-v1 + v3) +
+                     2 * pow(f1, 3) * f3 * (-v2 + v3)))) /
+         (pow(f1 - f2, 2) * pow(f1 - f3, 3) * pow(f2 - f3, 2) * M);
+}
+GW_HD double delta2(double f1, double f2, double f3, double v1, double v2, double v3, double dd1, double dd3, double M) {
+  return (-(dd3 * pow(f1 - f2, 2) * (f1 - f3) * (f2 - f3) * (pow(f1, 2) + f2 * f3 + 2. * f1 * (f2 + f3))) +
+          dd1 * (f1 - f3) * pow(f2 - f3, 2) * (-(f2 * f3 * (2 * f2 + f3)) + pow(f1, 2) * (f2 + 2 * f3) + f1 * (-pow(f2, 2) + pow(f3, 2))) -
+          4 * pow(f1, 2) * pow(f2, 3) * v1 + 3 * f1 * pow(f2, 4) * v1 - 4 * f1 * pow(f2, 3) * f3 * v1 + 3 * pow(f2, 4) * f3 * v1 +
+          12 * pow(f1, 2) * f2 * pow(f3, 2) * v1 - 4 * pow(f2, 3) * pow(f3, 2) * v1 - 8 * pow(f1, 2) * pow(f3, 3) * v1 +
+          f1 * pow(f3, 4) * v1 + pow(f3, 5) * v1 + pow(f1, 5) * v2 + pow(f1, 4) * f3 * v2 - 8 * pow(f1, 3) * pow(f3, 2) * v2 +
+          8 * pow(f1, 2) * pow(f3, 3) * v2 - f1 * pow(f3, 4) * v2 - pow(f3, 5) * v2 - pow(f1, 5) * v3 +
+          4 * pow(f1, 2) * pow(f2, 3) * v3 - 3 * f1 * pow(f2, 4) * v3 - pow(f1, 4) * f3 * v3 + 4 * f1 * pow(f2, 3) * f3 * v3 -
+          3 * pow(f2, 4) * f3 * v3 + 8 * pow(f1, 3) * pow(f3, 2) * v3 - 12 * pow(f1, 2) * f2 * pow(f3, 2) * v3 +
+          4 * pow(f2, 3) * pow(f3, 2) * v3) /
+         (pow(f1 - f2, 2) * pow(f1 - f3, 3) * pow(f2 - f3, 2) * pow(M, 2));
+}
+GW_HD double delta3(double f1, double f2, double f3, double v1, double v2, double v3, double dd1, double dd3, double M) {
+  return (dd3 * pow(f1 - f2, 2) * (f1 - f3) * (f2 - f3) * (2 * f1 + f2 + f3) -
+          dd1 * (f1 - f2) * (f1 - f3) * pow(f2 - f3, 2) * (f1 + f2 + 2 * f3) +
+          2 * (pow(f3, 4) * (-v1 + v2) + 2 * pow(f1, 2) * pow(f2 - f3, 2) * (v1 - v3) + 2 * pow(f2, 2) * pow(f3, 2) * (v1 - v3) +
+               2 * pow(f1, 3) * f3 * (v2 - v3) + pow(f2, 4) * (-v1 + v3) + pow(f1, 4) * (-v2 + v3) +
+               2 * f1 * f3 * (pow(f3, 2) * (v1 - v2) + pow(f2, 2) * (v1 - v3) + 2 * f2 * f3 * (-v1 + v3)))) /
+         (pow(f1 - f2, 2) * pow(f1 - f3, 3) * pow(f2 - f3, 2) * pow(M, 3));
+}
+GW_HD double delta4(double f1, double f2, double f3, double v1, double v2, double v3, double dd1, double dd3, double M) {
+  return (-(dd3 * pow(f1 - f2, 2) * (f1 - f3) * (f2 - f3)) + dd1 * (f1 - f2) * (f1 - f3) * pow(f2 - f3, 2) -
+          3 * f1 * pow(f2, 2) * v1 + 2 * pow(f2, 3) * v1 + 6 * f1 * f2 * f3 * v1 - 3 * pow(f2, 2) * f3 * v1 -
+          3 * f1 * pow(f3, 2) * v1 + pow(f3, 3) * v1 + pow(f1, 3) * v2 - 3 * pow(f1, 2) * f3 * v2 + 3 * f1 * pow(f3, 2) * v2 -
+          pow(f3, 3) * v2 - pow(f1, 3) * v3 + 3 * f1 * pow(f2, 2) * v3 - 2 * pow(f2, 3) * v3 + 3 * pow(f1, 2) * f3 * v3 -
+          6 * f1 * f2 * f3 * v3 + 3 * pow(f2, 2) * f3 * v3) /
+         (pow(f1 - f2, 2) * pow(f1 - f3, 3) * pow(f2 - f3, 2) * pow(M, 4));
+}
+
+GW_HDNI void d_connections(ModelD &m) {
+  Source &s = m.s;
+  Lambda &l = m.l;
+  // amp_connection_coeffs (IMRPhenomD.cpp:1679-1702)
+  {
+    double M = s.M, f1 = s.f1, f3 = s.f3;
+    Pows pw;
+    precalc_powers_ins(f1, M, pw);
+    double f2 = (f1 + f3) / 2.;
+    double v1 = amp_ins(f1, m, pw);
+    double v2 = l.v2;
+    double v3 = amp_mr(f3, s, l);
+    double dd1 = Damp_ins(f1, m);
+    double dd3 = Damp_mr(f3, s, l);
+    m.deltas[0] = delta0(f1, f2, f3, v1, v2, v3, dd1, dd3, M);
+    m.deltas[1] = delta1(f1, f2, f3, v1, v2, v3, dd1, dd3, M);
+    m.deltas[2] = delta2(f1, f2, f3, v1, v2, v3, dd1, dd3, M);
+    m.deltas[3] = delta3(f1, f2, f3, v1, v2, v3, dd1, dd3, M);
+    m.deltas[4] = delta4(f1, f2, f3, v1, v2, v3, dd1, dd3, M);
+  }
+  // phase_connection_coefficients (IMRPhenomD.cpp:1614-1674)
+  l.beta[0] = 0;
+  l.beta[1] = 0;
+  l.alpha[0] = 0;
+  l.alpha[1] = 0;
+  double M = s.M, eta = s.eta;
+  {
+    double f1 = s.f1_phase;
+    double Dins = Dphase_ins(f1, s, m.pn_phase, l);
+    double Dint = Dphase_int(f1, s, l);
+    l.beta[1] = (eta / M) * Dins - (eta / M) * Dint;
+  }
+  {
+    double f1 = s.f1_phase;
+    Pows pw;
+    precalc_powers_ins(f1, M, pw);
+    double ins = phase_ins(f1, s, m.pn_phase, l, m.pi, pw);
+    double intval = phase_int(f1, s, l);
+    l.beta[0] = (eta)*ins - eta * intval;
+  }
+  {
+    double f2 = s.f2_phase;
+    double Dint = Dphase_int(f2, s, l);
+    double Dmr = Dphase_mr(f2, s, l);
+    l.alpha[1] = (eta / M) * Dint - eta / M * Dmr;
+  }
+  {
+    double f2 = s.f2_phase;
+    double intval = phase_int(f2, s, l);
+    double mr = phase_mr(f2, s, l);
+    l.alpha[0] = (eta)*intval - eta * mr;
+  }
+}
+
+// Model setup shared by D and Pv2 (IMRPhenomD.cpp:410-432).
+GW_HDNI int model_d_prologue(ModelD &m, const double *qnm) {
+  Source &s = m.s;
+  Lambda &l = m.l;
+  for (int i = 0; i < 4; i++) l.rho[i] = 0, l.gamma[i] = 0;
+  for (int i = 0; i < 5; i++) l.sigma[i] = 0, l.beta[i] = 0;
+  for (int i = 0; i < 7; i++) l.alpha[i] = 0;
+  for (int i = 0; i < 3; i++) l.rho[i] = lambda_elem(s, i);  // IMRPhenomD.cpp:833-852
+  l.v2 = lambda_elem(s, 3);
+  for (int i = 0; i < 3; i++) l.gamma[i] = lambda_elem(s, i + 4);
+  for (int i = 0; i < 4; i++) l.sigma[i + 1] = lambda_elem(s, i + 7);
+  for (int i = 0; i < 3; i++) l.beta[i + 1] = lambda_elem(s, i + 11);
+  for (int i = 0; i < 5; i++) l.alpha[i + 1] = lambda_elem(s, i + 14);
+  post_merger(s, qnm);
+  s.f1_phase = 0.018 / (s.M);
+  s.f2_phase = s.fRD / 2.;
+  s.f1 = 0.014 / (s.M);
+  s.f3 = fpeak(s, l);
+  precalc_powers_PI(m.pi);
+  for (int i = 0; i < 5; i++) m.deltas[i] = 0;
+  pn_amp_coeff(s, m.pn_amp);
+  pn_phase_coeff_static(s, m.pn_phase);
+  d_connections(m);
+  m.fcut = .2 / s.M;
+  m.status = kModelOK;
+  if (!(s.eta > 0 && s.eta <= 0.25 + 1e-12) || !(s.fRD > 0) || !(s.fdamp > 0) || !(s.M > 0)) m.status |= kModelQnmRange;
+  return m.status;
+}
+
+// D-specific phase/time shift and amplitude scale (IMRPhenomD.cpp:434-470)
+GW_HDNI void model_d_finish(ModelD &m) {
+  Source &s = m.s;
+  double M = s.M;
+  if (s.shift_phase) {
+    m.fref = s.f_ref;
+    Pows pw;
+    precalc_powers_ins(m.fref, M, pw);
+    double phi_shift = build_phase(m.fref, m, m.pn_phase, pw);
+    m.phic = 2 * s.phiRef + phi_shift;
+  } else {
+    m.fref = 0;
+    m.phic = s.phiRef;
+  }
+  double tc_shift = 0;
+  if (s.shift_time) {
+    double alpha1_offset = lambda_elem(s, 14);
+    tc_shift = Dphase_mr(s.f3, s, m.l) + (-m.l.alpha[1] + alpha1_offset) * s.M / s.eta;
+  }
+  m.tcl = 2 * kPi * s.tc + tc_shift;
+  m.A0eff = s.A0 * pow(M, 7. / 6.);
+}
+
+// ------------------------------------------------------------- IMRPhenomPv2
+GW_HD double L2PN(double eta, double MF2third, double PI2third) {  // IMRPhenomP.cpp:1214-1220
+  double x = MF2third * PI2third, x2 = x * x, eta2 = eta * eta;
+  return (eta * (1.0 + (1.5 + eta / 6.0) * x + (3.375 - (19.0 * eta) / 8. - eta2 / 24.0) * x2)) / sqrt(x);
+}
+#define GWT_ROTATEZ(angle, vx, vy, vz)       \
+  tmp1 = vx * cos(angle) - vy * sin(angle); \
+  tmp2 = vx * sin(angle) + vy * cos(angle); \
+  vx = tmp1;                                \
+  vy = tmp2
+#define GWT_ROTATEY(angle, vx, vy, vz)       \
+  tmp1 = vx * cos(angle) + vz * sin(angle); \
+  tmp2 = -vx * sin(angle) + vz * cos(angle);\
+  vx = tmp1;                                \
+  vz = tmp2
+// PhenomPv2_Param_Transform (IMRPhenomP.cpp:1082-1210) / _reduced (:822-938)
+GW_HDNI void pv2_transform(Source &s, int reduced) {
+  double chi1_l = s.spin1z, chi2_l = s.spin2z;
+  double q = s.mass1 / s.mass2;
+  double chi_eff = (s.mass1 * chi1_l + s.mass2 * chi2_l) / s.M;
+  s.chil = (1.0 + q) / q * chi_eff;
+  double m1_2 = s.mass1 * s.mass1, m2_2 = s.mass2 * s.mass2;
+  if (!reduced) {
+    double S1_perp = m1_2 * sqrt(s.spin1y * s.spin1y + s.spin1x * s.spin1x);
+    double S2_perp = m2_2 * sqrt(s.spin2y * s.spin2y + s.spin2x * s.spin2x);
+    double A1 = 2 + (3 * s.mass2) / (2 * s.mass1), A2 = 2 + (3 * s.mass1) / (2 * s.mass2);
+    double ASp1 = A1 * S1_perp, ASp2 = A2 * S2_perp;
+    double num = (ASp2 > ASp1) ? ASp2 : ASp1;
+    double denom = (s.mass2 > s.mass1) ? A2 * m2_2 : A1 * m1_2;
+    s.chip = num / denom;
+  }
+  double m1 = q / (1 + q), m2 = 1. / (1 + q);
+  s.SP = s.chip * m1 * m1;
+  s.SL = chi1_l * m1 * m1 + chi2_l * m2 * m2;
+  Pows pw, pp;
+  precalc_powers_PI(pp);
+  precalc_powers_ins(s.f_ref, s.M, pw);
+  double L0 = s.M * s.M * L2PN(s.eta, pw.MF2third, pp.PI2third);
+  double J0x, J0y, J0z;
+  if (!reduced) {
+    J0x = m1_2 * s.spin1x + m2_2 * s.spin2x;
+    J0y = m1_2 * s.spin1y + m2_2 * s.spin2y;
+  } else {
+    J0x = m1_2 * s.chip * cos(s.phip);
+    J0y = m1_2 * s.chip * sin(s.phip);
+  }
+  J0z = L0 + m1_2 * s.spin1z + m2_2 * s.spin2z;
+  double J0 = sqrt(J0x * J0x + J0y * J0y + J0z * J0z);
+  double thetaJ_sf = acos(J0z / J0);
+  double phiJ_sf = atan2(J0y, J0x);
+  s.phi_aligned = -phiJ_sf;
+  double tmp1, tmp2;
+  double incl = s.incl_angle, phiRef = s.phiRef;
+  double Nx_sf = sin(incl) * cos(kPi / 2. - phiRef), Ny_sf = sin(incl) * sin(kPi / 2. - phiRef), Nz_sf = cos(incl);
+  double tx = Nx_sf, ty = Ny_sf, tz = Nz_sf;
+  GWT_ROTATEZ(-phiJ_sf, tx, ty, tz);
+  GWT_ROTATEY(-thetaJ_sf, tx, ty, tz);
+  double kappa = -atan2(ty, tx);
+  tx = 0.;
+  ty = 0.;
+  tz = 1.;
+  GWT_ROTATEZ(-phiJ_sf, tx, ty, tz);
+  GWT_ROTATEY(-thetaJ_sf, tx, ty, tz);
+  GWT_ROTATEZ(kappa, tx, ty, tz);
+  s.alpha0 = atan2(ty, tx);
+  tx = Nx_sf;
+  ty = Ny_sf;
+  tz = Nz_sf;
+  GWT_ROTATEZ(-phiJ_sf, tx, ty, tz);
+  GWT_ROTATEY(-thetaJ_sf, tx, ty, tz);
+  GWT_ROTATEZ(kappa, tx, ty, tz);
+  double Nx_Jf = tx, Nz_Jf = tz;
+  s.thetaJN = acos(Nz_Jf);
+  tx = -cos(incl) * sin(phiRef);
+  ty = -cos(incl) * cos(phiRef);
+  tz = sin(incl);
+  GWT_ROTATEZ(-phiJ_sf, tx, ty, tz);
+  GWT_ROTATEY(-thetaJ_sf, tx, ty, tz);
+  GWT_ROTATEZ(kappa, tx, ty, tz);
+  double XdotPArun = tx * 0. + ty * -1. + tz * 0.;
+  double XdotQArun = tx * Nz_Jf + ty * 0. + tz * -Nx_Jf;
+  s.zeta_polariz = atan2(XdotQArun, XdotPArun);
+}
+#undef GWT_ROTATEZ
+#undef GWT_ROTATEY
+
+GW_HDNI void pv2_euler_coeffs(double *a, double *e, const Source &s) {  // IMRPhenomP.cpp:65-144
+  double m2 = s.q / (1. + s.q), m1 = 1. / (1. + s.q), dm = m1 - m2, mtot = 1.;
+  double eta = m1 * m2, eta2 = eta * eta, eta3 = eta2 * eta, eta4 = eta3 * eta;
+  double mtot2 = mtot * mtot, mtot4 = mtot2 * mtot2, mtot6 = mtot4 * mtot2, mtot8 = mtot6 * mtot2;
+  double chil = s.chil, chil2 = chil * chil, chip2 = s.chip * s.chip, chip4 = chip2 * chip2;
+  double dm2 = dm * dm, dm3 = dm2 * dm;
+  double m2_2 = m2 * m2, m2_3 = m2_2 * m2, m2_4 = m2_3 * m2, m2_5 = m2_4 * m2, m2_6 = m2_5 * m2, m2_7 = m2_6 * m2,
+         m2_8 = m2_7 * m2;
+  a[0] = (-0.18229166666666666 - (5 * dm) / (64. * m2));
+  a[1] = ((-15 * dm * m2 * chil) / (128. * mtot2 * eta) - (35 * m2_2 * chil) / (128. * mtot2 * eta));
+  a[2] = (-1.7952473958333333 - (4555 * dm) / (7168. * m2) - (15 * chip2 * dm * m2_3) / (128. * mtot4 * eta2) -
+          (35 * chip2 * m2_4) / (128. * mtot4 * eta2) - (515 * eta) / 384. - (15 * dm2 * eta) / (256. * m2_2) -
+          (175 * dm * eta) / (256. * m2));
+  a[3] = -(35 * kPi) / 48. - (5 * dm * kPi) / (16. * m2) + (5 * dm2 * chil) / (16. * mtot2) +
+         (5 * dm * m2 * chil) / (3. * mtot2) + (2545 * m2_2 * chil) / (1152. * mtot2) -
+         (5 * chip2 * dm * m2_5 * chil) / (128. * mtot6 * eta3) - (35 * chip2 * m2_6 * chil) / (384. * mtot6 * eta3) +
+         (2035 * dm * m2 * chil) / (21504. * mtot2 * eta) + (2995 * m2_2 * chil) / (9216. * mtot2 * eta);
+  a[4] = (4.318908476114694 + (27895885 * dm) / (2.1676032e7 * m2) - (15 * chip4 * dm * m2_7) / (512. * mtot8 * eta4) -
+          (35 * chip4 * m2_8) / (512. * mtot8 * eta4) - (485 * chip2 * dm * m2_3) / (14336. * mtot4 * eta2) +
+          (475 * chip2 * m2_4) / (6144. * mtot4 * eta2) + (15 * chip2 * dm2 * m2_2) / (256. * mtot4 * eta) +
+          (145 * chip2 * dm * m2_3) / (512. * mtot4 * eta) + (575 * chip2 * m2_4) / (1536. * mtot4 * eta) +
+          (39695 * eta) / 86016. + (1615 * dm2 * eta) / (28672. * m2_2) - (265 * dm * eta) / (14336. * m2) +
+          (955 * eta2) / 576. + (15 * dm3 * eta2) / (1024. * m2_3) + (35 * dm2 * eta2) / (256. * m2_2) +
+          (2725 * dm * eta2) / (3072. * m2) - (15 * dm * m2 * kPi * chil) / (16. * mtot2 * eta) -
+          (35 * m2_2 * kPi * chil) / (16. * mtot2 * eta) + (15 * chip2 * dm * m2_7 * chil2) / (128. * mtot8 * eta4) +
+          (35 * chip2 * m2_8 * chil2) / (128. * mtot8 * eta4) + (375 * dm2 * m2_2 * chil2) / (256. * mtot4 * eta) +
+          (1815 * dm * m2_3 * chil2) / (256. * mtot4 * eta) + (1645 * m2_4 * chil2) / (192. * mtot4 * eta));
+  e[0] = (-0.18229166666666666 - (5 * dm) / (64. * m2));
+  e[1] = ((-15 * dm * m2 * chil) / (128. * mtot2 * eta) - (35 * m2_2 * chil) / (128. * mtot2 * eta));
+  e[2] = (-1.7952473958333333 - (4555 * dm) / (7168. * m2) - (515 * eta) / 384. - (15 * dm2 * eta) / (256. * m2_2) -
+          (175 * dm * eta) / (256. * m2));
+  e[3] = -(35 * kPi) / 48. - (5 * dm * kPi) / (16. * m2) + (5 * dm2 * chil) / (16. * mtot2) +
+         (5 * dm * m2 * chil) / (3. * mtot2) + (2545 * m2_2 * chil) / (1152. * mtot2) +
+         (2035 * dm * m2 * chil) / (21504. * mtot2 * eta) + (2995 * m2_2 * chil) / (9216. * mtot2 * eta);
+  e[4] = (4.318908476114694 + (27895885 * dm) / (2.1676032e7 * m2) + (39695 * eta) / 86016. +
+          (1615 * dm2 * eta) / (28672. * m2_2) - (265 * dm * eta) / (14336. * m2) + (955 * eta2) / 576. +
+          (15 * dm3 * eta2) / (1024. * m2_3) + (35 * dm2 * eta2) / (256. * m2_2) + (2725 * dm * eta2) / (3072. * m2) -
+          (15 * dm * m2 * kPi * chil) / (16. * mtot2 * eta) - (35 * m2_2 * kPi * chil) / (16. * mtot2 * eta) +
+          (375 * dm2 * m2_2 * chil2) / (256. * mtot4 * eta) + (1815 * dm * m2_3 * chil2) / (256. * mtot4 * eta) +
+          (1645 * m2_4 * chil2) / (192. * mtot4 * eta));
+}
+// calculate_euler_angles (IMRPhenomP.cpp:717-735) from MFthird
+GW_HD void pv2_euler_angles(double &alpha, double &eps, double MFthird, double PIthird, const double *a,
+                            const double *e) {
+  double oc = MFthird * PIthird, oc2 = oc * oc;
+  double logomega = log(oc2 * oc), omega = oc2 * oc;
+  alpha = (a[0] / omega + a[1] / oc2 + a[2] / oc + a[3] * logomega + a[4] * oc);
+  eps = (e[0] / omega + e[1] / oc2 + e[2] / oc + e[3] * logomega + e[4] * oc);
+}
+// calculate_time_shift (IMRPhenomP.cpp:551-606): d/df of a 10-node natural
+// spline of -phi(f) over [0.8, 1.2] fRD, at fRD, over 2 pi.
+GW_HDNI double pv2_time_shift(const ModelD &m) {
+  const Source &s = m.s;
+  double M = s.M, f_final = s.fRD;
+  double ff[10], ph[10], cc[10], work[60];
+  double pn[12];
+  for (int i = 0; i < 12; i++) pn[i] = m.pn_phase[i];
+  double fs = .8 * (f_final), fe = 1.2 * (f_final);
+  double dfx = (fe - fs) / (10 - 1);
+  if (dfx != dfx || dfx <= 0) return 0;
+  for (int j = 0; j < 10; j++) ff[j] = fs + j * dfx;
+  for (int j = 0; j < 10; j++) {
+    double f = ff[j];
+    Pows pw;
+    precalc_powers_ins(f, M, pw);
+    ph[j] = -build_phase(f, m, pn, pw);
+  }
+  cspline_coeffs(ff, ph, 10, cc, work);
+  return cspline_eval(ff, ph, cc, 10, f_final, 1) / (2. * kPi);
+}
+GW_HD double swsh_2m2(double theta, int m) {  // XLALSpinWeightedSphericalHarmonic s=-2 l=2 (util.cpp:1953-2333)
+  switch (m) {
+    case -2: return sqrt(5.0 / (64.0 * kPi)) * (1.0 - cos(theta)) * (1.0 - cos(theta));
+    case -1: return sqrt(5.0 / (16.0 * kPi)) * sin(theta) * (1.0 - cos(theta));
+    case 0: return sqrt(15.0 / (32.0 * kPi)) * sin(theta) * sin(theta);
+    case 1: return sqrt(5.0 / (16.0 * kPi)) * sin(theta) * (1.0 + cos(theta));
+    default: return sqrt(5.0 / (64.0 * kPi)) * (1.0 + cos(theta)) * (1.0 + cos(theta));
+  }
+}
+
+// Full Pv2 per-request setup: transform, D model, Euler/harmonic constants,
+// time shift (IMRPhenomP.cpp:195-262, 345-351; waveform_generator.cpp:1272-1281).
+GW_HDNI int model_p_prologue(ModelD &m, ModelP &pm, const GenParams &in, const double *qnm) {
+  Source &s = m.s;
+  s.pv2 = 1;
+  if ((in.chip + 1) > kCompThresh) {
+    s.chip = in.chip;
+    s.spin1z = in.spin1[2];
+    s.spin2z = in.spin2[2];
+    s.phip = in.phip;
+    pv2_transform(s, 1);
+  } else {
+    pv2_transform(s, 0);
+  }
+  for (int k = 0; k < 5; k++) pm.Y[k] = swsh_2m2(s.thetaJN, k - 2);
+  model_d_prologue(m, qnm);
+  m.fref = s.f_ref;
+  m.phic = 2 * s.phi_aligned;
+  m.tcl = 2 * kPi * s.tc;
+  m.A0eff = s.A0 * pow(s.M, 7. / 6.) / (2. * sqrt(5. / (64. * kPi)));
+  s.q = s.mass1 / s.mass2;
+  pv2_euler_coeffs(pm.ac, pm.ec, s);
+  double MFthird = pow(s.M * s.f_ref, 1. / 3.);
+  double aoff, eoff;
+  pv2_euler_angles(aoff, eoff, MFthird, m.pi.PIthird, pm.ac, pm.ec);
+  pm.alpha_shift = s.alpha0 - aoff;
+  pm.eps_off = eoff;
+  pm.t_corr = s.shift_time ? pv2_time_shift(m) : 0.0;
+  pm.c2z = cos(2. * s.zeta_polariz);
+  pm.s2z = sin(2. * s.zeta_polariz);
+  if (!(s.f_ref > 0)) m.status |= kModelBadInput;
+  return m.status;
+}
+
+// ------------------------------------------------------------- detectors
+GW_HD void antenna(int det, double ra, double dec, double psi, double gmst, double &fp, double &fc) {
+  // detector_util.cpp:901-1015, geometric factor detector_util.cpp:1158-1160
+  const double *D = GWT_T(gwt_det_tensor)[det];
+  double X[3], Y[3];
+  double gha = gmst - ra;
+  double cg = cos(gha), sg = sin(gha), cd = cos(dec), sd = sin(dec), cp = cos(psi), sp = sin(psi);
+  X[0] = -cp * sg - sp * cg * sd;
+  X[1] = -cp * cg + sp * sg * sd;
+  X[2] = sp * cd;
+  Y[0] = sp * sg - cp * cg * sd;
+  Y[1] = sp * cg + cp * sg * sd;
+  Y[2] = cp * cd;
+  fp = 0.0;
+  fc = 0.0;
+  for (int i = 0; i < 3; i++) {
+    double DX = D[i * 3 + 0] * X[0] + D[i * 3 + 1] * X[1] + D[i * 3 + 2] * X[2];
+    double DY = D[i * 3 + 0] * Y[0] + D[i * 3 + 1] * Y[1] + D[i * 3 + 2] * Y[2];
+    fp += X[i] * DX - Y[i] * DY;
+    fc += X[i] * DY + Y[i] * DX;
+  }
+  fp *= GWT_T(gwt_det_geometric)[det];
+  fc *= GWT_T(gwt_det_geometric)[det];
+}
+GW_HD double dtoa(double RA, double DEC, double gmst, int d1, int d2) {  // detector_util.cpp:760-780
+  const double *l1 = GWT_T(gwt_det_location)[d1], *l2 = GWT_T(gwt_det_location)[d2];
+  double hour_angle = gmst - RA;
+  double e0 = cos(DEC) * cos(hour_angle), e1 = cos(DEC) * -sin(hour_angle), e2 = sin(DEC);
+  return ((l1[0] - l2[0]) * e0 + (l1[1] - l2[1]) * e1 + (l1[2] - l2[2]) * e2) / kC;
+}
+
+// Everything one likelihood request needs.
+struct Request {
+  ModelD m;
+  ModelP p;
+  DetProj det[kMaxDet];
+  int approximant, ndet;
+};
+
+// Full prologue of one request.  `in.tc` must already hold the t_c the model
+// sees (MCMC_likelihood_extrinsic replaces it by T - t_c, mcmc_gw.cpp:2466-2473).
+GW_HDNI int request_prologue(Request &r, const GenParams &in, int approximant, const int *dets, int ndet,
+                             const double *qnm) {
+  r.approximant = approximant;
+  r.ndet = ndet;
+  populate(r.m.s, in);
+  int st;
+  if (approximant == kPhenomPv2) {
+    st = model_p_prologue(r.m, r.p, in, qnm);
+  } else {
+    st = model_d_prologue(r.m, qnm);
+    model_d_finish(r.m);
+    st = r.m.status;
+  }
+  for (int i = 0; i < ndet && i < kMaxDet; i++) {
+    antenna(dets[i], in.RA, in.DEC, in.psi, in.gmst, r.det[i].fp, r.det[i].fc);
+    double DTOA = dtoa(in.RA, in.DEC, in.gmst, dets[0], dets[i]);
+    double tc = -DTOA;
+    tc *= 2 * kPi;
+    r.det[i].tau = tc;
+  }
+  return st;
+}
+
+}  // namespace gwt

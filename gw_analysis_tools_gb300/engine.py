@@ -1,0 +1,233 @@
+"""Python front end of the C ABI (include/gwgpu.h).
+
+A Context owns one device, its stream, an HBM budget and the device-resident
+data registry.  Functions mirror the reference's entry points:
+
+  fourier_waveform            waveform_generator.cpp:104 (fourier_waveform)
+  fourier_detector_response   waveform_util.cpp:1070
+  log_likelihood_internal     mcmc_gw.cpp:801 (Log_Likelihood_internal, SIMPSONS)
+  mcmc_likelihood_extrinsic   mcmc_gw.cpp:2374 (MCMC_likelihood_extrinsic), plain FP64 form
+  loglik_batch                many MCMC_likelihood_extrinsic requests in one fused launch
+  mcmc_loglik_batch           MCMC_likelihood_wrapper (mcmc_gw.cpp:2569) on parameter vectors
+  fisher_numerical            fisher.cpp:81
+  fisher_batch                batched network Fisher + FP64 inverse
+
+Every call goes to the CUDA library; there is no CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native
+
+IMRPhenomD = 0
+IMRPhenomPv2 = 1
+PREC_FP64 = 0
+PREC_MIXED = 1
+METHODS = {"IMRPhenomD": IMRPhenomD, "IMRPhenomPv2": IMRPhenomPv2}
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "HBM budget exceeded", 4: "outside model domain",
+          5: "timed out", 6: "busy", 7: "not found", 8: "too large"}
+
+
+class GenParams(ctypes.Structure):
+    """gwgpu_gen_params: the gen_params_base<double> fields on the path."""
+
+    _fields_ = [
+        ("mass1", ctypes.c_double), ("mass2", ctypes.c_double),
+        ("spin1", ctypes.c_double * 3), ("spin2", ctypes.c_double * 3),
+        ("Luminosity_Distance", ctypes.c_double),
+        ("incl_angle", ctypes.c_double), ("phiRef", ctypes.c_double),
+        ("f_ref", ctypes.c_double), ("tc", ctypes.c_double),
+        ("RA", ctypes.c_double), ("DEC", ctypes.c_double),
+        ("psi", ctypes.c_double), ("gmst", ctypes.c_double),
+        ("chip", ctypes.c_double), ("phip", ctypes.c_double),
+        ("shift_time", ctypes.c_int32), ("shift_phase", ctypes.c_int32),
+        ("sky_average", ctypes.c_int32), ("dep_postmerger", ctypes.c_int32),
+    ]
+
+
+def gen_params(**kw):
+    """gen_params_py-style constructor (gwatpy/util.py): keyword fields, reference defaults."""
+    p = GenParams()
+    p.chip = -1.0
+    p.phip = -1.0
+    p.shift_time = 1
+    p.shift_phase = 1
+    for k, v in kw.items():
+        if k in ("spin1", "spin2"):
+            getattr(p, k)[:] = [float(x) for x in v]
+        elif k in ("shift_time", "shift_phase", "sky_average", "dep_postmerger"):
+            setattr(p, k, int(bool(v)))
+        else:
+            setattr(p, k, float(v))
+    return p
+
+
+def params_array(plist):
+    arr = (GenParams * len(plist))()
+    for i, p in enumerate(plist):
+        arr[i] = p if isinstance(p, GenParams) else gen_params(**p)
+    return arr
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+class GwGpuError(_native.GwGpuError):
+    pass
+
+
+class Context:
+    """One device, one stream, one HBM budget (bytes, 0 = unlimited)."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        self.lib = _native.load()
+        h = ctypes.c_void_p()
+        st = self.lib.gwgpu_context_create(device, hbm_budget, ctypes.byref(h))
+        if st != 0:
+            raise GwGpuError("gwgpu_context_create failed: %s" % STATUS.get(st, st))
+        self.h = h
+        self._data = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gwgpu_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st != 0:
+            msg = self.lib.gwgpu_last_error_string(self.h)
+            raise GwGpuError("%s: %s (%s)" % (what, STATUS.get(st, st), msg.decode() if msg else ""))
+
+    @property
+    def stream(self):
+        return self.lib.gwgpu_context_stream(self.h)
+
+    def bytes_in_use(self):
+        return self.lib.gwgpu_context_bytes_in_use(self.h)
+
+    # ------------------------------------------------------------ waveform
+    def fourier_waveform(self, freqs, method, params):
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        hp = np.zeros(f.size, dtype=np.complex128)
+        hc = np.zeros(f.size, dtype=np.complex128)
+        ok = self.lib.gwgpu_fourier_waveform(self.h, _dp(f), f.size, _dp(hp), _dp(hc), method.encode(),
+                                             ctypes.byref(params))
+        if ok != 1:
+            raise GwGpuError("fourier_waveform failed: %s" % self.lib.gwgpu_last_error_string(self.h))
+        return hp, hc
+
+    def fourier_detector_response(self, freqs, detector, method, params):
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        r = np.zeros(f.size, dtype=np.complex128)
+        ok = self.lib.gwgpu_fourier_detector_response(self.h, _dp(f), f.size, _dp(r), detector.encode(),
+                                                      method.encode(), ctypes.byref(params))
+        if ok != 1:
+            raise GwGpuError("fourier_detector_response failed")
+        return r
+
+    # ---------------------------------------------------------------- data
+    def register_data(self, detector, freqs, data, psd):
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        d = np.ascontiguousarray(data, dtype=np.complex128)
+        s = np.ascontiguousarray(psd, dtype=np.float64)
+        h = ctypes.c_int()
+        st = self.lib.gwgpu_data_register(self.h, detector.encode(), _dp(f), f.size, _dp(d), _dp(s), ctypes.byref(h))
+        self._check(st, "data_register")
+        self._data[h.value] = (detector, f.size)
+        return h.value
+
+    def release_data(self, handle):
+        self._check(self.lib.gwgpu_data_release(self.h, handle), "data_release")
+        self._data.pop(handle, None)
+
+    # ---------------------------------------------------------- likelihood
+    def log_likelihood_internal(self, data, psd, freqs, response):
+        d = np.ascontiguousarray(data, dtype=np.complex128)
+        s = np.ascontiguousarray(psd, dtype=np.float64)
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        r = np.ascontiguousarray(response, dtype=np.complex128)
+        out = ctypes.c_double()
+        st = self.lib.gwgpu_log_likelihood_internal(self.h, _dp(d), _dp(s), _dp(f), _dp(r), f.size,
+                                                    ctypes.byref(out))
+        self._check(st, "log_likelihood_internal")
+        return out.value
+
+    def mcmc_likelihood_extrinsic(self, params, method, handles, T_segment):
+        hs = np.ascontiguousarray(handles, dtype=np.int32)
+        out = ctypes.c_double()
+        st = self.lib.gwgpu_mcmc_likelihood_extrinsic(self.h, ctypes.byref(params), method.encode(), _ip(hs), hs.size,
+                                                      float(T_segment), ctypes.byref(out))
+        if st not in (0, 4):
+            self._check(st, "mcmc_likelihood_extrinsic")
+        return out.value
+
+    def loglik_batch(self, params, approximants, handles, T_segment, precision=PREC_MIXED):
+        """params: GenParams array or list; handles: (ndet,) shared or (n, ndet) per request."""
+        parr = params if isinstance(params, ctypes.Array) else params_array(params)
+        n = len(parr)
+        ap = np.ascontiguousarray(np.broadcast_to(np.asarray(approximants, dtype=np.int32), (n,)))
+        hs = np.asarray(handles, dtype=np.int32)
+        if hs.ndim == 1:
+            hs = np.broadcast_to(hs, (n, hs.size))
+        hs = np.ascontiguousarray(hs, dtype=np.int32)
+        out = np.zeros(n)
+        status = np.zeros(n, dtype=np.int32)
+        st = self.lib.gwgpu_loglik_batch(self.h, parr, _ip(ap), n, _ip(hs), hs.shape[1], float(T_segment), precision,
+                                         _dp(out), _ip(status))
+        self._check(st, "loglik_batch")
+        return out, status
+
+    def mcmc_loglik_batch(self, theta, approximant, gmst, handles, T_segment, precision=PREC_MIXED):
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        n, dim = th.shape
+        hs = np.asarray(handles, dtype=np.int32)
+        if hs.ndim == 1:
+            hs = np.broadcast_to(hs, (n, hs.size))
+        hs = np.ascontiguousarray(hs, dtype=np.int32)
+        out = np.zeros(n)
+        status = np.zeros(n, dtype=np.int32)
+        st = self.lib.gwgpu_mcmc_loglik_batch(self.h, _dp(th), dim, n, approximant, float(gmst), _ip(hs), hs.shape[1],
+                                              float(T_segment), precision, _dp(out), _ip(status))
+        self._check(st, "mcmc_loglik_batch")
+        return out, status
+
+    def set_tile(self, tile):
+        fn = getattr(self.lib, "gwgpu_batch_set_tile", None)
+        if fn is not None:
+            self._check(fn(self.h, int(tile)), "batch_set_tile")
+
+    # --------------------------------------------------------------- Fisher
+    def fisher_numerical(self, freqs, method, detector, reference_detector, params, noise, order=2, dimension=11):
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        s = np.ascontiguousarray(noise, dtype=np.float64)
+        out = np.zeros(dimension * dimension)
+        st = self.lib.gwgpu_fisher_numerical(self.h, _dp(f), f.size, method.encode(), detector.encode(),
+                                             reference_detector.encode(), _dp(out), dimension, ctypes.byref(params),
+                                             order, _dp(s))
+        self._check(st, "fisher_numerical")
+        return out.reshape(dimension, dimension)
+
+    def fisher_batch(self, params, method, handles, epsilon=1e-8, step_mode=0, covariance=True):
+        parr = params if isinstance(params, ctypes.Array) else params_array(params)
+        n = len(parr)
+        hs = np.ascontiguousarray(handles, dtype=np.int32)
+        dim = 11
+        fish = np.zeros((n, dim, dim))
+        cov = np.zeros((n, dim, dim)) if covariance else None
+        status = np.zeros(n, dtype=np.int32)
+        st = self.lib.gwgpu_fisher_batch(self.h, parr, n, method, _ip(hs), hs.size, float(epsilon), int(step_mode),
+                                         _dp(fish), _dp(cov) if cov is not None else None, _ip(status))
+        self._check(st, "fisher_batch")
+        return fish, cov, status

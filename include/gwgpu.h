@@ -1,0 +1,175 @@
+/*
+ * gwgpu.h -- C ABI of the GB300 likelihood engine for gw_analysis_tools.
+ *
+ * Plain C types only (pointers, sizes, ints, doubles).  Host buffers unless a
+ * name ends in _device.  Complex arrays are interleaved (re, im) doubles, the
+ * memory layout of std::complex<double>.  Every entry point returns a
+ * GWGPU_* status code unless documented otherwise; waveform entry points that
+ * mirror the reference return 1 on success like the reference does.
+ *
+ * Each declaration names the reference interface it replaces
+ * (file:line in gw_analysis_tools).
+ */
+#ifndef GWGPU_H
+#define GWGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define GWGPU_OK 0
+#define GWGPU_EINVAL 1      /* bad argument (null pointer, length < 2, unknown detector/method) */
+#define GWGPU_ECUDA 2       /* CUDA runtime error; see gwgpu_last_error_string */
+#define GWGPU_ENOMEM 3      /* HBM budget of the context exceeded */
+#define GWGPU_EDOMAIN 4     /* request outside the model domain (NaN, eta > 1/4, spin out of table) */
+#define GWGPU_ETIMEDOUT 5   /* a bounded wait gave up */
+#define GWGPU_EBUSY 6       /* queue full / resource in use */
+#define GWGPU_ENOTFOUND 7   /* unknown handle or ticket */
+#define GWGPU_ETOOLARGE 8   /* size beyond a fixed maximum */
+
+/* ---- approximants and precision forms ---- */
+#define GWGPU_IMRPHENOMD 0
+#define GWGPU_IMRPHENOMPV2 1
+#define GWGPU_PREC_FP64 0   /* the reference arithmetic in FP64 on the device */
+#define GWGPU_PREC_MIXED 1  /* FP32 amplitude/projection/products, FP64 phase, compensated sums */
+
+/* ---- Fisher parameterisations (unpack_parameters, fisher.cpp:1841-1961) ---- */
+#define GWGPU_FISHER_IMRPHENOMD 0        /* "IMRPhenomD": 11 params, D_L and M_c as log factors */
+#define GWGPU_FISHER_MCMC_IMRPHENOMD 1   /* "MCMC_IMRPhenomD": 11 MCMC params */
+#define GWGPU_FISHER_STEP_ABSOLUTE 0     /* epsilon added to each parameter (the reference: 1e-8, fisher.cpp:158) */
+#define GWGPU_FISHER_STEP_RELATIVE 1     /* epsilon * |theta_i| (epsilon when theta_i == 0) */
+
+typedef struct gwgpu_context gwgpu_context;
+typedef struct gwgpu_server gwgpu_server;
+
+/* POD mirror of the gen_params_base<double> fields on the path
+ * (include/gwat/util.h:121-378).  Solar masses, Mpc, seconds, radians, Hz.
+ * chip = -1 selects the full in-plane-spin transform for Pv2
+ * (waveform_generator.cpp:1272-1281). */
+typedef struct {
+  double mass1, mass2;
+  double spin1[3], spin2[3];
+  double Luminosity_Distance;
+  double incl_angle, phiRef, f_ref, tc;
+  double RA, DEC, psi, gmst;
+  double chip, phip;
+  int32_t shift_time, shift_phase, sky_average, dep_postmerger;
+} gwgpu_gen_params;
+
+void gwgpu_default_params(gwgpu_gen_params *p);
+const char *gwgpu_status_string(int status);
+
+/* ---- context: one device, one HBM budget, device-resident data registry ---- */
+int gwgpu_context_create(int device, size_t hbm_budget_bytes, gwgpu_context **out);
+int gwgpu_context_destroy(gwgpu_context *ctx);
+const char *gwgpu_last_error_string(gwgpu_context *ctx);
+/* The context's default stream (a cudaStream_t), for callers that time or
+ * order work around the engine. */
+void *gwgpu_context_stream(gwgpu_context *ctx);
+size_t gwgpu_context_bytes_in_use(gwgpu_context *ctx);
+
+/* ---- waveform and detector response ---- */
+/* fourier_waveform(double*, int, std::complex<double>* hplus, hcross, std::string,
+ * gen_params*)  (waveform_generator.h:70-74, waveform_generator.cpp:104-300).
+ * generation_method: "IMRPhenomD" or "IMRPhenomPv2".  Returns 1 on success,
+ * 0 on failure (reference convention). */
+int gwgpu_fourier_waveform(gwgpu_context *ctx, const double *frequencies, int length, double *hplus,
+                           double *hcross, const char *generation_method, const gwgpu_gen_params *params);
+
+/* fourier_detector_response(T*, int, std::complex<T>*, std::string detector,
+ * std::string method, gen_params_base<T>*, T *times)  (waveform_util.h:190-197,
+ * waveform_util.cpp:1070-1088), ground detectors, equatorial coordinates.
+ * Returns 1 on success, 0 on failure. */
+int gwgpu_fourier_detector_response(gwgpu_context *ctx, const double *frequencies, int length, double *response,
+                                    const char *detector, const char *generation_method,
+                                    const gwgpu_gen_params *params);
+
+/* ---- data registry (replaces the process-global mcmc_data/mcmc_noise/
+ * mcmc_frequencies pointers set at mcmc_gw.cpp:1464-1476) ---- */
+int gwgpu_data_register(gwgpu_context *ctx, const char *detector, const double *frequencies, int length,
+                        const double *data, const double *psd, int *handle);
+int gwgpu_data_release(gwgpu_context *ctx, int handle);
+
+/* ---- plain form: FP64, one request per launch (the drop-in) ---- */
+/* Log_Likelihood_internal(std::complex<double>* data, double* psd, double* freqs,
+ * double* weights, std::complex<double>* response, int length, bool log10F,
+ * std::string "SIMPSONS")  (mcmc_gw.h:276, mcmc_gw.cpp:801-873). */
+int gwgpu_log_likelihood_internal(gwgpu_context *ctx, const double *data, const double *psd,
+                                  const double *frequencies, const double *response, int length, double *out);
+
+/* MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double>*, std::string
+ * method, int* lengths, double** freqs, std::complex<double>** data, double** psd,
+ * double** weights, std::string "SIMPSONS", bool log10F, std::string* detectors,
+ * int num_detectors)  (mcmc_gw.h:473, mcmc_gw.cpp:2374-2487), over registered
+ * data.  T_segment is the value the reference forms at mcmc_gw.cpp:2466 before
+ * t_c <- T_segment - t_c; params is not mutated. */
+int gwgpu_mcmc_likelihood_extrinsic(gwgpu_context *ctx, const gwgpu_gen_params *params,
+                                    const char *generation_method, const int *handles, int num_detectors,
+                                    double T_segment, double *loglik);
+
+/* ---- batched form: n requests, one fused launch per step ---- */
+/* n independent MCMC_likelihood_extrinsic evaluations (the sampler calls
+ * mcmc_step -> sampler->ll once per chain, mcmc_sampler_internals.cpp:98).
+ * approximants[i] is GWGPU_IMRPHENOMD or GWGPU_IMRPHENOMPV2; all detectors of
+ * one request share one grid; requests may use different grids (handles per
+ * request: handles[i*num_detectors + d]).  status[i] is GWGPU_OK or
+ * GWGPU_EDOMAIN (loglik[i] = NaN then). */
+int gwgpu_loglik_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, const int *approximants, int n,
+                       const int *handles, int num_detectors, double T_segment, int precision, double *loglik,
+                       int *status);
+/* Same with every array already on the device, enqueued on `stream` (a
+ * cudaStream_t or NULL for the context stream); asynchronous. */
+int gwgpu_loglik_batch_device(gwgpu_context *ctx, const gwgpu_gen_params *d_params, const int *d_approximants,
+                              int n, const int *d_handles, int num_detectors, double T_segment, int precision,
+                              double *d_loglik, int *d_status, void *stream);
+/* MCMC_likelihood_wrapper(double *param, ...) (mcmc_gw.h:491, mcmc_gw.cpp:2569)
+ * for n parameter vectors: MCMC_prep_params + repack_parameters (MCMC_IMRPhenomD
+ * 11-dim, MCMC_IMRPhenomPv2 15-dim), then the batched likelihood. */
+int gwgpu_mcmc_loglik_batch(gwgpu_context *ctx, const double *theta, int dim, int n, int approximant,
+                            double gmst, const int *handles, int num_detectors, double T_segment, int precision,
+                            double *loglik, int *status);
+
+/* ---- Fisher ---- */
+/* fisher_numerical(double* freqs, int length, string method, string detector,
+ * string reference_detector, double** output, int dimension, gen_params_base<double>*,
+ * int order, int*, int*, double* noise)  (fisher.h:35-48, fisher.cpp:81-146).
+ * method "IMRPhenomD" or "MCMC_IMRPhenomD"; output dimension*dimension row major;
+ * order 2 or 4; epsilon 1e-8 absolute as the reference.  Returns GWGPU_OK. */
+int gwgpu_fisher_numerical(gwgpu_context *ctx, const double *frequencies, int length, const char *generation_method,
+                           const char *detector, const char *reference_detector, double *output, int dimension,
+                           const gwgpu_gen_params *params, int order, const double *noise);
+/* Batched network Fisher (MCMC_fisher_wrapper summing detectors,
+ * mcmc_gw.cpp:2283-2317) for n sources over registered data: fisher[n][dim][dim]
+ * and, if covariance != NULL, its FP64 inverse (gsl_cholesky_matrix_invert,
+ * util.cpp:857-900).  status[i]: GWGPU_OK, GWGPU_EDOMAIN. */
+int gwgpu_fisher_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, int method, const int *handles,
+                       int num_detectors, double epsilon, int step_mode, double *fisher, double *covariance,
+                       int *status);
+
+/* ---- serving: continuous batching of log-likelihood requests ---- */
+typedef struct {
+  int max_inflight;          /* request slots on the device */
+  int max_batch;             /* requests per fused launch */
+  int precision;             /* GWGPU_PREC_* */
+  double T_segment;          /* as for gwgpu_mcmc_likelihood_extrinsic */
+} gwgpu_server_config;
+int gwgpu_server_create(gwgpu_context *ctx, const gwgpu_server_config *cfg, gwgpu_server **out);
+int gwgpu_server_destroy(gwgpu_server *srv);
+/* Queue one request; returns a ticket.  GWGPU_EBUSY when every slot is taken. */
+int gwgpu_server_submit(gwgpu_server *srv, const gwgpu_gen_params *params, int approximant, const int *handles,
+                        int num_detectors, uint64_t *ticket);
+/* Non-blocking: GWGPU_OK with the result, GWGPU_EBUSY while still in flight. */
+int gwgpu_server_poll(gwgpu_server *srv, uint64_t ticket, double *loglik, int *status);
+/* Blocks until the ticket completes or timeout_ms passes (GWGPU_ETIMEDOUT). */
+int gwgpu_server_wait(gwgpu_server *srv, uint64_t ticket, int timeout_ms, double *loglik, int *status);
+/* Latency percentiles (seconds, submit -> result visible on host) and counts. */
+int gwgpu_server_stats(gwgpu_server *srv, double *p50, double *p99, uint64_t *completed, uint64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GWGPU_H */

@@ -68,47 +68,57 @@ def main(ref):
     def fmt(v):
         return repr(float(v))
 
-    def emit(path, prefix, qualifier):
+    def emit(path, prefix, dual):
+        """dual=False: plain static const arrays (C oracle).
+        dual=True: each table twice, a host copy NAME_h and, under nvcc, a
+        __constant__ device copy NAME_d; GWT_T(NAME) picks the right one."""
+        P = prefix.upper()
+        tabs = []
+        rows = []
+        for r in range(19):
+            rows.append("{" + ", ".join(fmt(x) for x in lam[r * 11:(r + 1) * 11]) + "}")
+        tabs.append(("lambda_fit", "[19][11]", "{" + ",\\\n  ".join(rows) + "}", True))
+        for name, arr in (("qnm_a", qa), ("qnm_fring", qr), ("qnm_fdamp", qd)):
+            body = ",\\\n  ".join(", ".join(fmt(x) for x in arr[i:i + 6]) for i in range(0, 1003, 6))
+            tabs.append((name, "[1003]", "{" + body + "}", False))
+        tabs.append(("det_location", "[9][3]", "{" + ", ".join("{" + ", ".join(fmt(x) for x in loc[s_]) + "}" for s_, _ in dets) + "}", True))
+        tabs.append(("det_tensor", "[9][9]", "{" + ", ".join("{" + ", ".join(fmt(x) for x in tens[s_]) + "}" for s_, _ in dets) + "}", True))
+        tabs.append(("det_geometric", "[9]", "{" + ", ".join(fmt(geo[s_]) for s_, _ in dets) + "}", True))
         lines = []
         lines.append("/* Generated by oracle/gen_tables.py -- constant data only, do not edit. */")
-        lines.append("#ifndef %sTABLES_H" % prefix.upper())
-        lines.append("#define %sTABLES_H" % prefix.upper())
-        lines.append("#define %sQNM_LEN 1003" % prefix.upper())
-        lines.append("#define %sNDET_KNOWN 9" % prefix.upper())
-        lines.append("/* IMRPhenomD calibration fits: row = lambda index (rho1..3, v2, gamma1..3,")
-        lines.append("   sigma1..4, beta1..3, alpha1..5), columns = polynomial in (eta, chi_PN - 1). */")
-        lines.append("%s double %slambda_fit[19][11] = {" % (qualifier, prefix))
-        for r in range(19):
-            row = lam[r * 11:(r + 1) * 11]
-            lines.append("  {" + ", ".join(fmt(x) for x in row) + "},")
-        lines.append("};")
-        for name, arr in (("qnm_a", qa), ("qnm_fring", qr), ("qnm_fdamp", qd)):
-            lines.append("%s double %s%s[1003] = {" % (qualifier, prefix, name))
-            for i in range(0, 1003, 6):
-                lines.append("  " + ", ".join(fmt(x) for x in arr[i:i + 6]) + ",")
-            lines.append("};")
-        lines.append("/* Ground detectors, in this order: Hanford, Livingston, Virgo, Kagra, Indigo,")
-        lines.append("   Cosmic Explorer, Einstein Telescope 1/2/3.  ECEF location (m), response")
-        lines.append("   tensor (row major), geometric factor. */")
-        lines.append("%s double %sdet_location[9][3] = {" % (qualifier, prefix))
-        for short, _ in dets:
-            lines.append("  {" + ", ".join(fmt(x) for x in loc[short]) + "},")
-        lines.append("};")
-        lines.append("%s double %sdet_tensor[9][9] = {" % (qualifier, prefix))
-        for short, _ in dets:
-            lines.append("  {" + ", ".join(fmt(x) for x in tens[short]) + "},")
-        lines.append("};")
-        lines.append("%s double %sdet_geometric[9] = {" % (qualifier, prefix))
-        lines.append("  " + ", ".join(fmt(geo[s]) for s, _ in dets))
-        lines.append("};")
+        lines.append("/* IMRPhenomD calibration fits (rows: rho1..3, v2, gamma1..3, sigma1..4, beta1..3,")
+        lines.append("   alpha1..5; columns: polynomial in eta and chi_PN - 1); quasi-normal-mode table")
+        lines.append("   (final spin, ringdown and damping frequency times M); ground detectors in the")
+        lines.append("   order Hanford, Livingston, Virgo, Kagra, Indigo, CE, ET1, ET2, ET3 (ECEF")
+        lines.append("   location in m, response tensor row major, geometric factor). */")
+        lines.append("#ifndef %sTABLES_H" % P)
+        lines.append("#define %sTABLES_H" % P)
+        lines.append("#define %sQNM_LEN 1003" % P)
+        lines.append("#define %sNDET_KNOWN 9" % P)
+        if dual:
+            lines.append("#if defined(__CUDA_ARCH__)")
+            lines.append("#define GWT_T(name) name##_d")
+            lines.append("#else")
+            lines.append("#define GWT_T(name) name##_h")
+            lines.append("#endif")
+        for name, dims, init, devcopy in tabs:
+            if dual:
+                lines.append("#define %s%s_INIT %s" % (P, name.upper(), init))
+                lines.append("static const double %s%s_h%s = %s%s_INIT;" % (prefix, name, dims, P, name.upper()))
+                if devcopy:
+                    lines.append("#if defined(__CUDACC__)")
+                    lines.append("static __constant__ double %s%s_d%s = %s%s_INIT;" % (prefix, name, dims, P, name.upper()))
+                    lines.append("#endif")
+            else:
+                lines.append("static const double %s%s%s = %s;" % (prefix, name, dims, init.replace("\\\n", "\n")))
         lines.append("#endif")
         with open(path, "w") as f:
             f.write("\n".join(lines) + "\n")
 
     here = os.path.dirname(os.path.abspath(__file__))
     root = os.path.dirname(here)
-    emit(os.path.join(here, "gwo_tables.h"), "gwo_", "static const")
-    emit(os.path.join(root, "gw_analysis_tools_gb300", "csrc", "phenom_tables.h"), "gwt_", "static const")
+    emit(os.path.join(here, "gwo_tables.h"), "gwo_", False)
+    emit(os.path.join(root, "gw_analysis_tools_gb300", "csrc", "phenom_tables.h"), "gwt_", True)
     print("wrote tables: lambda %d, qnm %d, detectors %d" % (len(lam), len(qa), len(dets)))
 
 

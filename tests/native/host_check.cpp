@@ -1,0 +1,151 @@
+// host_check.cpp -- TEST BUILD ONLY: the product's per-request prologue and
+// per-bin arithmetic (gw_analysis_tools_gb300/csrc/phenom_*.h) compiled for the
+// host, so the CPU test suite can check the kernels' math against the oracle
+// without a GPU.  Nothing in the product loads this library.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../gw_analysis_tools_gb300/csrc/phenom_mixed.h"
+
+using namespace gwt;
+
+static std::vector<double> g_qnm;
+static const double *qnm() {
+  if (g_qnm.empty()) {
+    const int n = kQnmLen;
+    g_qnm.resize(5 * n);
+    for (int i = 0; i < n; i++) {
+      g_qnm[i] = gwt_qnm_a_h[i];
+      g_qnm[n + i] = gwt_qnm_fring_h[i];
+      g_qnm[2 * n + i] = gwt_qnm_fdamp_h[i];
+    }
+    std::vector<double> work(6 * n);
+    cspline_coeffs(g_qnm.data(), g_qnm.data() + n, n, g_qnm.data() + 3 * n, work.data());
+    cspline_coeffs(g_qnm.data(), g_qnm.data() + 2 * n, n, g_qnm.data() + 4 * n, work.data());
+  }
+  return g_qnm.data();
+}
+
+extern "C" {
+
+int gwh_waveform(const double *freqs, int N, double *hp, double *hc, int approx, const GenParams *p) {
+  Request r;
+  int dets[1] = {0};
+  request_prologue(r, *p, approx, dets, 1, qnm());
+  for (int k = 0; k < N; k++) {
+    cd a, b;
+    wave_bin(r, freqs[k], a, b);
+    hp[2 * k] = a.re;
+    hp[2 * k + 1] = a.im;
+    hc[2 * k] = b.re;
+    hc[2 * k + 1] = b.im;
+  }
+  return 1;
+}
+
+// Model internals: fRD, fdamp, f1, f3, f1_phase, f2_phase, deltas[5], beta[4], alpha[6]
+int gwh_d_internals(const GenParams *p, double *out) {
+  Request r;
+  int dets[1] = {0};
+  request_prologue(r, *p, kPhenomD, dets, 1, qnm());
+  const ModelD &m = r.m;
+  int k = 0;
+  out[k++] = m.s.fRD;
+  out[k++] = m.s.fdamp;
+  out[k++] = m.s.f1;
+  out[k++] = m.s.f3;
+  out[k++] = m.s.f1_phase;
+  out[k++] = m.s.f2_phase;
+  for (int i = 0; i < 5; i++) out[k++] = m.deltas[i];
+  for (int i = 0; i < 4; i++) out[k++] = m.l.beta[i];
+  for (int i = 0; i < 6; i++) out[k++] = m.l.alpha[i];
+  return k;
+}
+
+double gwh_loglik_fp64(const GenParams *pin, int approx, double T_segment, const double *freqs, int N, int ndet,
+                       const int *dets, const double *const *data, const double *const *psd) {
+  GenParams p = *pin;
+  p.tc = T_segment - p.tc;
+  Request r;
+  request_prologue(r, p, approx, dets, ndet, qnm());
+  std::vector<double> hh(ndet, 0.0), dh(ndet, 0.0);
+  for (int k = 0; k < N; k++) {
+    cd a, b;
+    double f = freqs[k];
+    wave_bin(r, f, a, b);
+    double w = simpson_weight(k, N);
+    for (int d = 0; d < ndet; d++) {
+      cd x = response_bin(r.det[d], a, b, f, r.det[d].tau != 0.0);
+      double S = psd[d][k];
+      hh[d] += w * ((x.re * x.re + x.im * x.im) / S);
+      dh[d] += w * ((data[d][2 * k] * x.re + data[d][2 * k + 1] * x.im) / S);
+    }
+  }
+  double ll = 0, c = 4. * (freqs[N / 2] - freqs[N / 2 - 1]) / 3.;
+  for (int d = 0; d < ndet; d++) ll += -0.5 * (c * hh[d] - 2 * c * dh[d]);
+  return ll;
+}
+
+// Mixed form on the host: same registration whitening, tables, prologue and
+// per-bin code as the kernels; FP64 sums of the per-bin FP32 terms.
+double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, const double *freqs, int N, int ndet,
+                        const int *dets, const double *const *data, const double *const *psd) {
+  GenParams p = *pin;
+  p.tc = T_segment - p.tc;
+  Request r;
+  request_prologue(r, p, approx, dets, ndet, qnm());
+  double df = freqs[1] - freqs[0];
+  int n0 = (int)std::llround(freqs[0] / df);
+  MixedReq x;
+  std::memset(&x, 0, sizeof(x));
+  mixed_prologue(r, df, x);
+  if (x.status) return NAN;
+  double sdf = freqs[N / 2] - freqs[N / 2 - 1];
+  std::vector<std::vector<float>> dh(ndet), wh(ndet);
+  std::vector<double> dscale(ndet), wscale(ndet);
+  for (int d = 0; d < ndet; d++) {
+    std::vector<double> W(N);
+    double wmax = 0, dmax = 0;
+    for (int k = 0; k < N; k++) {
+      double sw = (k == 0 || k == N - 1) ? 1.0 : ((k & 1) ? 4.0 : 2.0);
+      W[k] = 4. * sdf / 3. * sw / psd[d][k];
+      wmax = std::max(wmax, std::fabs(W[k]));
+      dmax = std::max(dmax, std::fabs(W[k] * data[d][2 * k]) + std::fabs(W[k] * data[d][2 * k + 1]));
+    }
+    wscale[d] = wmax;
+    dscale[d] = dmax > 0 ? dmax : 1.0;
+    dh[d].resize(2 * N);
+    wh[d].resize(N);
+    for (int k = 0; k < N; k++) {
+      dh[d][2 * k] = (float)(W[k] * data[d][2 * k] / dscale[d]);
+      dh[d][2 * k + 1] = (float)(W[k] * data[d][2 * k + 1] / dscale[d]);
+      wh[d][k] = (float)(W[k] / wscale[d]);
+    }
+  }
+  double sums[kMaxDet * kAccPerDet] = {0};
+  for (int k = 0; k < N; k++) {
+    int n = n0 + k;
+    double xn = (double)n;
+    double t = std::cbrt(xn), rr = std::pow(xn, -5. / 3.), lnn = std::log(xn), t34 = std::pow(xn, 0.75);
+    float tf = (float)std::cbrt(xn), m76 = (float)std::pow(xn, -7. / 6.);
+    float dre[kMaxDet], dim[kMaxDet], w[kMaxDet];
+    for (int d = 0; d < ndet; d++) {
+      dre[d] = dh[d][2 * k];
+      dim[d] = dh[d][2 * k + 1];
+      w[d] = wh[d][k];
+    }
+    KSum acc[kMaxDet * kAccPerDet];
+    for (auto &a : acc) a = KSum{0.f, 0.f};
+    switch (ndet) {
+      case 1: mixed_bin<1>(x, n, t, rr, lnn, t34, tf, m76, dre, dim, w, acc); break;
+      case 2: mixed_bin<2>(x, n, t, rr, lnn, t34, tf, m76, dre, dim, w, acc); break;
+      case 3: mixed_bin<3>(x, n, t, rr, lnn, t34, tf, m76, dre, dim, w, acc); break;
+      default: mixed_bin<4>(x, n, t, rr, lnn, t34, tf, m76, dre, dim, w, acc); break;
+    }
+    for (int j = 0; j < kMaxDet * kAccPerDet; j++) sums[j] += (double)(acc[j].s - acc[j].c);
+  }
+  return mixed_finalize(x, sums, dscale.data(), wscale.data());
+}
+
+}  // extern "C"

@@ -1,0 +1,76 @@
+"""The kernels' prologue and per-bin arithmetic, compiled for the host
+(tests/native/host_check.cpp), against the oracle.  Runs without a GPU."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from gw_analysis_tools_gb300 import workloads as W
+
+
+@pytest.fixture(scope="module")
+def setup3(oracle):
+    f = W.config1_grid()
+    src = W.config1_source()
+    T = 1.0 / (f[1] - f[0])
+    dets = list(W.DETECTORS3)
+    injp = oracle.params_from_dict(dict(src, tc=T - src["tc"]))
+    data = []
+    for i, d in enumerate(dets):
+        r = oracle.detector_response(f, injp, d)
+        dt = oracle.dtoa(src["RA"], src["DEC"], src["gmst"], dets[0], d)
+        data.append(r * np.exp(1j * (-2 * np.pi * dt) * f) + W.noise(f, 100 + i))
+    psd = [W.analytic_psd(f)] * 3
+    return f, T, dets, data, psd
+
+
+def _call(lib_fn, oracle, p, ap, T, f, dets, data, psd):
+    idx = (ctypes.c_int * len(dets))(*[oracle.detector_index(d) for d in dets])
+    return lib_fn(ctypes.byref(p), ap, T, oracle._dp(f), f.size, len(dets), idx, oracle._ptr_array(data),
+                  oracle._ptr_array(psd))
+
+
+def test_host_waveform_matches_oracle(oracle, hostcheck):
+    f = W.config1_grid()
+    cases = [(0, W.config1_source()), (1, dict(W.config1_source(), spin1=(0.3, 0.2, 0.3), spin2=(-0.1, 0.4, -0.1)))]
+    for ap, d in cases:
+        p = oracle.params_from_dict(d)
+        a = oracle.fourier_waveform(f, p, ap)
+        hp = np.zeros(f.size, complex)
+        hc = np.zeros(f.size, complex)
+        hostcheck.gwh_waveform(oracle._dp(f), f.size, oracle._dp(hp), oracle._dp(hc), ap, ctypes.byref(p))
+        for x, y in ((a[0], hp), (a[1], hc)):
+            assert np.max(np.abs(x - y)) <= 1e-13 * np.abs(x).max()
+
+
+def test_host_fp64_loglik_matches_oracle(oracle, hostcheck, setup3):
+    f, T, dets, data, psd = setup3
+    for ap, draws in ((0, W.prior_draws(16, 7)), (1, W.prior_draws(8, 11, precessing=True))):
+        for d in draws:
+            p = oracle.params_from_dict(d)
+            ref = oracle.loglik(p, f, dets, data, psd, approximant=ap)
+            got = _call(hostcheck.gwh_loglik_fp64, oracle, p, ap, T, f, dets, data, psd)
+            assert abs(got - ref) <= 1e-9 * max(1.0, abs(ref))
+
+
+def test_host_mixed_loglik_within_tolerance(oracle, hostcheck, setup3):
+    """Mixed form: |delta log L| <= 1e-3 absolute against the FP64 oracle."""
+    f, T, dets, data, psd = setup3
+    worst = 0.0
+    for ap, draws in ((0, [W.config1_source()] + W.prior_draws(40, 7)), (1, W.prior_draws(20, 11, precessing=True))):
+        for d in draws:
+            p = oracle.params_from_dict(d)
+            ref = oracle.loglik(p, f, dets, data, psd, approximant=ap)
+            got = _call(hostcheck.gwh_loglik_mixed, oracle, p, ap, T, f, dets, data, psd)
+            worst = max(worst, abs(got - ref))
+    assert worst <= 1e-3, worst
+
+
+def test_host_internals_match_oracle(oracle, hostcheck):
+    for d in W.prior_draws(10, 5):
+        p = oracle.params_from_dict(d)
+        a = np.zeros(32)
+        b = np.zeros(32)
+        oracle.lib().gwo_d_internals(ctypes.byref(p), oracle._dp(a))
+        hostcheck.gwh_d_internals(ctypes.byref(p), oracle._dp(b))
+        np.testing.assert_allclose(b[:21], a[:21], rtol=1e-13, atol=0)
