@@ -1,0 +1,534 @@
+#!/usr/bin/env python
+"""Benchmark of the gw_analysis_tools likelihood path on GB300.
+
+Headline workload: the batched parallel-tempering step -- IMRPhenomD over
+Hanford/Livingston/Virgo, 64 chains x 8 temperatures = 512 log-likelihood
+requests per step, parameters drawn from the priors, on the 20-1024 Hz grid at
+df = 1/32 Hz (32,128 bins), analytic PSD, injected signal plus seeded noise.
+A step is one pass of the hot path over one batch of 512 requests.
+
+  value   evals/s of the batched mixed-precision form, parameters resident on
+          the device, CUDA events on the engine stream; L2 flushed (256 MiB
+          write) before every step, outside the events.
+  e2e     the same through the C ABI entry point gwgpu_loglik_batch with host
+          buffers: H2D of the parameters and D2H of log L + status inside the
+          timed region (wall clock per step), L2 flushed before every step.
+
+Beside them: the plain FP64 one-request-per-launch form, the batched FP64
+form, the served form (Poisson arrivals, mixed D/Pv2, p50/p99), the uneven
+Pv2 batch and the batched Fisher, a roofline of the fused bin kernel, and
+the CPU oracle timed on the host cores.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_REQ = 512
+METRIC = "logL evals/s (batched+served vs plain FP64, |dlogL|<=1e-3); p50/p99 latency"
+WORKLOAD = ("batched PT step: IMRPhenomD, H/L/V, 64 chains x 8 temperatures = 512 requests/step, "
+            "20-1024 Hz at df=1/32 Hz (32128 bins), prior draws, analytic PSD, injected signal + seeded noise")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="skip the secondary forms")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return rank, world, local, pg
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- workload
+def make_network(ctx, G, W, O=None):
+    """Grid, injected data (signal from the engine's FP64 detector response)."""
+    f = W.config1_grid()
+    T = 1.0 / (f[1] - f[0])
+    src = W.config1_source()
+    inj = G.gen_params(**dict(src, tc=T - src["tc"]))
+    data = []
+    for i, d in enumerate(W.DETECTORS3):
+        r = ctx.fourier_detector_response(f, d, "IMRPhenomD", inj)
+        # time-of-arrival shift relative to Hanford, as the likelihood applies it
+        dt = _dtoa(src, W.DETECTORS3[0], d)
+        data.append(r * np.exp(-2j * np.pi * dt * f) + W.noise(f, 100 + i))
+    psd = W.analytic_psd(f)
+    handles = [ctx.register_data(d, f, data[i], psd) for i, d in enumerate(W.DETECTORS3)]
+    return f, T, data, psd, handles
+
+
+_LOC = {"Hanford": (-2.16141492636e+06, -3.83469517889e+06, 4.60035022664e+06),
+        "Livingston": (-7.42760447238e+04, -5.49628371971e+06, 3.22425701744e+06),
+        "Virgo": (4.54637409900e+06, 8.42989697626e+05, 4.37857696241e+06)}
+
+
+def _dtoa(src, d1, d2):  # DTOA_earth_centered_coord (detector_util.cpp:760-780)
+    a, b = np.array(_LOC[d1]), np.array(_LOC[d2])
+    ha = src["gmst"] - src["RA"]
+    e = np.array([np.cos(src["DEC"]) * np.cos(ha), np.cos(src["DEC"]) * -np.sin(ha), np.sin(src["DEC"])])
+    return float((a - b) @ e / 299792458.0)
+
+
+def flush_l2(buf):
+    buf.add_(1.0)  # 256 MiB read+write > 126 MiB L2
+
+
+# ------------------------------------------------------------- our arm
+def run_ours(args, rank, world, local, pg):
+    import torch
+    import gw_analysis_tools_gb300 as G
+    from gw_analysis_tools_gb300 import _native, workloads as W
+
+    _native.build()
+    torch.cuda.set_device(local)
+    ctx = G.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    f, T, data, psd, handles = make_network(ctx, G, W)
+
+    nbatch = 8
+    draws = [W.prior_draws(N_REQ, 1000 + 97 * rank + b) for b in range(nbatch)]
+    draws[0][0] = W.config1_source()
+    host_params = [G.params_array(d) for d in draws]
+    pbytes = ctypes_sizeof(G.GenParams) * N_REQ
+    d_params = torch.empty((nbatch, pbytes), dtype=torch.uint8, device="cuda")
+    for b in range(nbatch):
+        d_params[b].copy_(torch.frombuffer(bytearray(host_params[b]), dtype=torch.uint8))
+    d_approx = torch.zeros(N_REQ, dtype=torch.int32, device="cuda")
+    d_out = torch.zeros((nbatch, N_REQ), dtype=torch.float64, device="cuda")
+    d_stat = torch.zeros((nbatch, N_REQ), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+
+    def step(b, prec=G.PREC_MIXED):
+        ctx.loglik_batch_device(d_params[b].data_ptr(), d_approx.data_ptr(), N_REQ, handles, T, prec,
+                                d_out[b].data_ptr(), d_stat[b].data_ptr())
+
+    # autotune the tile once on this workload, then warm up (graph capture)
+    tile, _ = ctx.autotune(d_params[0].data_ptr(), d_approx.data_ptr(), N_REQ, handles, T, G.PREC_MIXED,
+                           d_out[0].data_ptr(), d_stat[0].data_ptr())
+    for i in range(args.warmup):
+        step(i % nbatch)
+    torch.cuda.synchronize()
+
+    # ---------------- value: device-resident, CUDA events on the engine stream
+    e0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    e1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush_l2(flush)
+                e0[i].record(stream)
+            step(i % nbatch)
+            with torch.cuda.stream(stream):
+                e1[i].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in zip(e0, e1)]
+    tot_ms = float(np.sum(step_ms))
+    if pg:
+        t = torch.tensor([tot_ms], dtype=torch.float64, device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    value = N_REQ * args.steps * world / (tot_ms / 1e3)
+    gpu_launches = 2 * args.steps  # prologue + fused bin kernel per step (memset node not ours)
+
+    # status and a parity sample for |dlogL| against the oracle (cpu_baseline leg below)
+    out_mixed = d_out[0].cpu().numpy().copy()
+    stat0 = d_stat[0].cpu().numpy().copy()
+
+    # ---------------- per-kernel timing (roofline): events around prologue and bin kernel
+    ctx.lib.gwgpu_batch_timing(ctx.h, 1)
+    import ctypes
+    pro, ker = [], []
+    for i in range(max(5, args.steps // 2)):
+        with torch.cuda.stream(stream):
+            flush_l2(flush)
+        step(i % nbatch)
+        a, b = ctypes.c_float(), ctypes.c_float()
+        ctx.lib.gwgpu_batch_last_timing(ctx.h, ctypes.byref(a), ctypes.byref(b))
+        pro.append(a.value)
+        ker.append(b.value)
+    ctx.lib.gwgpu_batch_timing(ctx.h, 0)
+    kernel_ms = float(np.mean(ker))
+    prologue_ms = float(np.mean(pro))
+
+    # ---------------- e2e: C ABI with host buffers
+    e2e_t = []
+    for i in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ll, st = ctx.loglik_batch(host_params[i % nbatch], 0, handles, T, G.PREC_MIXED)
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_t.append(t1 - t0)
+    e2e_value = N_REQ * len(e2e_t) * world / max(float(np.sum(e2e_t)), 1e-12)
+    h2d = N_REQ * (ctypes_sizeof(G.GenParams) + 4)
+    d2h = N_REQ * (8 + 4)
+
+    res = {}
+    res.update(dict(value=value, tot_ms=tot_ms, step_ms=step_ms, kernel_ms=kernel_ms, prologue_ms=prologue_ms,
+                    e2e_value=e2e_value, h2d=h2d, d2h=d2h, clocks=clk.summary(), tile=tile,
+                    gpu_launches=gpu_launches, stat_ok=int((stat0 == 0).sum())))
+
+    if not args.quick and rank == 0:
+        res["extras"] = secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params, d_params,
+                                        d_approx, d_out, d_stat, args)
+    res["out_mixed"] = out_mixed
+    res["draws0"] = draws[0]
+    res["f"], res["data"], res["psd"], res["T"] = f, data, psd, T
+    return res
+
+
+def ctypes_sizeof(t):
+    import ctypes
+    return ctypes.sizeof(t)
+
+
+def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params, d_params, d_approx, d_out, d_stat,
+                    args):
+    ex = {}
+    # plain FP64, one request per launch (host params, synchronous drop-in call)
+    plist = host_params[1]
+    nplain = 128
+    times = []
+    for i in range(nplain + 8):
+        with torch.cuda.stream(stream):
+            flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.mcmc_likelihood_extrinsic(plist[i % N_REQ], "IMRPhenomD", handles, T)
+        if i >= 8:
+            times.append(time.perf_counter() - t0)
+    ex["plain_fp64_evals_per_s"] = len(times) / float(np.sum(times))
+    ex["plain_fp64_p50_ms"] = float(np.median(times) * 1e3)
+    # batched FP64 (device resident)
+    ctx.loglik_batch_device(d_params[1].data_ptr(), d_approx.data_ptr(), N_REQ, handles, T, G.PREC_FP64,
+                            d_out[1].data_ptr(), d_stat[1].data_ptr())
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    tot = 0.0
+    for i in range(3):
+        with torch.cuda.stream(stream):
+            flush_l2(flush)
+            ev[0].record(stream)
+        ctx.loglik_batch_device(d_params[1].data_ptr(), d_approx.data_ptr(), N_REQ, handles, T, G.PREC_FP64,
+                                d_out[1].data_ptr(), d_stat[1].data_ptr())
+        with torch.cuda.stream(stream):
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        tot += ev[0].elapsed_time(ev[1])
+    ex["batched_fp64_evals_per_s"] = 3 * N_REQ / (tot / 1e3)
+    # served: 16 ensembles (chains 8-256, temperatures 4-16), Poisson 2e5/s, D/Pv2 50/50
+    rng = np.random.default_rng(7)
+    ens = [(int(rng.integers(8, 257)), int(rng.integers(4, 17))) for _ in range(16)]
+    nserve = 60000
+    dd = W.prior_draws(nserve // 2, 501)
+    dp = W.prior_draws(nserve - nserve // 2, 502, precessing=True)
+    sp, sa = [], []
+    for i in range(nserve):
+        if i % 2 == 0:
+            sp.append(dd[i // 2])
+            sa.append(0)
+        else:
+            sp.append(dp[i // 2])
+            sa.append(1)
+    arrivals = np.cumsum(rng.exponential(1.0 / 2e5, nserve))
+    srv = G.Server(ctx, T, max_inflight=16384, max_batch=1024, lanes=4, hbm_budget=120 * 1024 ** 3)
+    srv.drive(G.params_array(sp[:2000]), sa[:2000], handles, arrivals[:2000] - arrivals[0])  # warm-up
+    srv.reset_stats()
+    out, st, lat, wall = srv.drive(G.params_array(sp), sa, handles, arrivals - arrivals[0])
+    s = srv.stats()
+    srv.close()
+    ex["served"] = {"evals_per_s": nserve / wall, "p50_ms": s["p50_s"] * 1e3, "p99_ms": s["p99_s"] * 1e3,
+                    "offered_rate": 2e5, "requests": nserve, "launches": s["launches"], "ensembles": ens,
+                    "ok": int((st == 0).sum())}
+    # uneven Pv2 batch: T in {4, 8, 32, 128}, 20-2048 Hz, 1024 requests, one launch
+    Ts = W.uneven_durations(1024, 9)
+    hmap = {}
+    for Tu in (4, 8, 32, 128):
+        fu = W.uniform_grid(20.0, 2048.0, 1.0 / Tu)
+        psd_u = W.analytic_psd(fu)
+        hmap[Tu] = [ctx.register_data(d, fu, W.noise(fu, 900 + Tu + i), psd_u) for i, d in enumerate(W.DETECTORS3)]
+    # T_segment = 0: each request uses 1/df of its own grid
+    pu = W.prior_draws(1024, 11, precessing=True)
+    hs = np.array([hmap[int(t)] for t in Ts], dtype=np.int32)
+    bins = int(sum(int(2028 * t) for t in Ts))
+    parr = G.params_array(pu)
+    ctx.loglik_batch(parr, 1, hs, 0.0, G.PREC_MIXED)
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        ctx.loglik_batch(parr, 1, hs, 0.0, G.PREC_MIXED)
+    dt = (time.perf_counter() - t0) / reps
+    ex["uneven_pv2"] = {"evals_per_s": 1024 / dt, "ms_per_launch": dt * 1e3, "bins_per_launch": bins,
+                        "grid_bins": sorted(set(int(2028 * t) for t in Ts))}
+    # batched Fisher: IMRPhenomD 3 detectors, 10-2048 Hz at df=1/16, step 1e-6 relative
+    ff = W.uniform_grid(10.0, 2048.0, 1.0 / 16.0)
+    psd_f = W.analytic_psd(ff)
+    hf = [ctx.register_data(d, ff, np.zeros(ff.size, complex), psd_f) for d in W.DETECTORS3]
+    nf = 10000
+    pf = G.params_array(W.prior_draws(nf, 13))
+    ctx.fisher_batch(G.params_array(W.prior_draws(64, 14)), 0, hf, epsilon=1e-6, step_mode=1)
+    t0 = time.perf_counter()
+    fish, cov, fst = ctx.fisher_batch(pf, 0, hf, epsilon=1e-6, step_mode=1)
+    dt = time.perf_counter() - t0
+    ex["fisher"] = {"fishers_per_s": nf / dt, "sources": nf, "bins": int(ff.size), "seconds": dt,
+                    "ok": int((fst == 0).sum())}
+    ex["_fisher_sample"] = (pf, fish[:4].copy(), ff, psd_f)
+    return ex
+
+
+# --------------------------------------------------------- CPU baseline
+def cpu_baseline(res, seconds=10.0):
+    """The C oracle (FP64 restatement of the reference path, OpenMP over
+    requests) on the host cores: a bounded sample of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from gw_analysis_tools_gb300 import workloads as W
+    O.build()
+    f, data, psd = res["f"], res["data"], res["psd"]
+    dets = list(W.DETECTORS3)
+    draws = res["draws0"]
+    plist = [O.params_from_dict(d) for d in draws]
+    ref = O.loglik_batch(plist, f, dets, data, [psd] * 3)
+    t0 = time.perf_counter()
+    n = 0
+    while time.perf_counter() - t0 < seconds:
+        O.loglik_batch(plist, f, dets, data, [psd] * 3)
+        n += len(plist)
+    dt = time.perf_counter() - t0
+    cores = os.cpu_count()
+    err = np.abs(res["out_mixed"] - ref)
+    return {"value": n / dt, "unit": "evals/s", "cores": cores, "kind": "port",
+            "sample": "%d requests of the 512-request step (prior draws), %.1f s on %d threads" % (n, dt, cores)}, \
+        {"max_abs_dlogL": float(err.max()), "p99_abs_dlogL": float(np.percentile(err, 99)),
+         "median_abs_dlogL": float(np.median(err)), "requests": int(err.size)}
+
+
+def fisher_err(sample):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from gw_analysis_tools_gb300 import workloads as W
+    pf, fish, ff, psd = sample
+    worst = 0.0
+    for i in range(len(fish)):
+        p = pf[i]
+        op = O.GenParams()
+        for k, _ in O.GenParams._fields_:
+            setattr(op, k, getattr(p, k))
+        ref = O.fisher_network(ff, op, list(W.DETECTORS3), [psd] * 3, epsilon=1e-6, step_mode=1)
+        d = np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
+        worst = max(worst, float(np.max(np.abs(fish[i] - ref) / d)))
+    return worst
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference(args, rank, world):
+    """The reference's CPU path on the host cores: the FP64 oracle port (the
+    reference needs GSL/ADOL-C/FFTW that are absent), all threads, one step =
+    the 512-request batch."""
+    if rank != 0:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from gw_analysis_tools_gb300 import workloads as W
+    O.build()
+    f = W.config1_grid()
+    T = 1.0 / (f[1] - f[0])
+    src = W.config1_source()
+    dets = list(W.DETECTORS3)
+    injp = O.params_from_dict(dict(src, tc=T - src["tc"]))
+    data = []
+    for i, d in enumerate(dets):
+        r = O.detector_response(f, injp, d)
+        dt = O.dtoa(src["RA"], src["DEC"], src["gmst"], dets[0], d)
+        data.append(r * np.exp(-2j * np.pi * dt * f) + W.noise(f, 100 + i))
+    psd = [W.analytic_psd(f)] * 3
+    plist = [O.params_from_dict(d) for d in W.prior_draws(N_REQ, 1000)]
+    for _ in range(args.warmup):
+        O.loglik_batch(plist, f, dets, data, psd)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.loglik_batch(plist, f, dets, data, psd)
+    dt = time.perf_counter() - t0
+    v = N_REQ * args.steps / dt
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "global_batch": N_REQ},
+            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
+                             "sample": "%d steps of %d requests on %d threads" % (args.steps, N_REQ, cores)},
+            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return line
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+        if line is not None:
+            print(json.dumps(line))
+        return
+    res = run_ours(args, rank, world, local, pg)
+    if rank != 0:
+        return
+    base, parity = cpu_baseline(res)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    # roofline of the fused bin kernel: FP64 pipe (the path is neither HBM- nor tensor-bound)
+    fp64_ops_per_bin = float(os.environ.get("GWGPU_FP64_OPS_PER_BIN", "0")) or FP64_OPS_PER_BIN
+    units = N_REQ * 32128
+    flops = 2.0 * fp64_ops_per_bin * units  # FMA-equivalent ops x 2
+    achieved = flops / (res["kernel_ms"] / 1e3) / 1e12
+    fp64_peak = measure_fp64_peak()
+    ex = res.get("extras", {})
+    fisher_worst = fisher_err(ex.pop("_fisher_sample")) if "_fisher_sample" in ex else None
+    line = {
+        "metric": METRIC, "value": res["value"], "unit": "evals/s", "n_gpus": world, "steps": len(res["step_ms"]),
+        "warmup": parse_warmup(), "ms_per_step": res["tot_ms"] / len(res["step_ms"]), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (FP64 phase)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "global_batch": N_REQ * world, "precision": "mixed",
+                   "l2": "flushed before every step (256 MiB write)", "tile": res["tile"],
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": res["e2e_value"], "unit": "evals/s", "h2d_bytes_per_step": res["h2d"],
+                "d2h_bytes_per_step": res["d2h"]},
+        "gpu_launches": res["gpu_launches"],
+        "clocks": res["clocks"],
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp64_peak if fp64_peak else None, "traffic": TRAFFIC_PER_LAUNCH,
+                     "kernel": "k_batch<3,1> (fused mixed bin kernel)", "kernel_ms": res["kernel_ms"],
+                     "prologue_ms": res["prologue_ms"],
+                     "peak_source": "measured live: cuBLAS DGEMM 4096^3 in this run",
+                     "hbm": {"achieved_gbs": (TRAFFIC_PER_LAUNCH or 0) / (res["kernel_ms"] / 1e3) / 1e9,
+                             "peak_gbs": peaks.get("hbm_gbs"), "peak_source": "MEASURED_PEAKS.json"}},
+        "cpu_baseline": base,
+        "parity": dict(parity, tolerance=1e-3, status_ok=res["stat_ok"]),
+    }
+    if ex:
+        line["plain_fp64_evals_per_s"] = ex["plain_fp64_evals_per_s"]
+        line["batched_fp64_evals_per_s"] = ex["batched_fp64_evals_per_s"]
+        line["speedup_vs_plain_fp64"] = res["value"] / ex["plain_fp64_evals_per_s"]
+        line["served"] = ex["served"]
+        line["served"]["speedup_vs_plain_fp64"] = ex["served"]["evals_per_s"] / ex["plain_fp64_evals_per_s"]
+        line["uneven_pv2"] = ex["uneven_pv2"]
+        line["fisher"] = dict(ex["fisher"], max_normalized_err_vs_oracle=fisher_worst)
+    print(json.dumps(line))
+
+
+# FP64 operations per bin of the fused mixed kernel (ncu: FP64 FMA-equivalent
+# thread instructions of k_batch<3,1> on this workload / bins processed), and
+# the DRAM bytes of one launch (ncu dram__bytes_read + write); see profiles/.
+FP64_OPS_PER_BIN = 13.0
+TRAFFIC_PER_LAUNCH = None
+
+
+def measure_fp64_peak():
+    import torch
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(5):
+        e0.record()
+        a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * 4096 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    return best
+
+
+def parse_warmup():
+    return parse().warmup
+
+
+if __name__ == "__main__":
+    main()

@@ -5,8 +5,8 @@ PSD-weighted inner product that gives each parallel-tempered chain its
 log-likelihood, plus the numerical Fisher matrix, as sm_103a CUDA kernels
 behind a C ABI (include/gwgpu.h).  See engine.Context.
 """
-from .engine import (IMRPhenomD, IMRPhenomPv2, PREC_FP64, PREC_MIXED, Context, GenParams, GwGpuError, gen_params,
-                     params_array)
+from .engine import (IMRPhenomD, IMRPhenomPv2, PREC_FP64, PREC_MIXED, Context, GenParams, GwGpuError, Server,
+                     gen_params, params_array)
 
-__all__ = ["Context", "GenParams", "gen_params", "params_array", "GwGpuError", "IMRPhenomD", "IMRPhenomPv2",
-           "PREC_FP64", "PREC_MIXED"]
+__all__ = ["Context", "Server", "GenParams", "gen_params", "params_array", "GwGpuError", "IMRPhenomD",
+           "IMRPhenomPv2", "PREC_FP64", "PREC_MIXED"]

@@ -104,7 +104,14 @@ def _declare(L):
         "gwgpu_server_poll": (c_int, [c_void_p, ctypes.c_uint64, dp, ip]),
         "gwgpu_server_wait": (c_int, [c_void_p, ctypes.c_uint64, c_int, dp, ip]),
         "gwgpu_server_stats": (c_int, [c_void_p, dp, dp, P(ctypes.c_uint64), P(ctypes.c_uint64)]),
+        "gwgpu_server_reset_stats": (c_int, [c_void_p]),
+        "gwgpu_server_drive": (c_int, [c_void_p, c_void_p, ip, ip, c_int, dp, c_int, dp, ip, dp, dp]),
         "gwgpu_batch_set_tile": (c_int, [c_void_p, c_int]),
+        "gwgpu_batch_use_graphs": (c_int, [c_void_p, c_int]),
+        "gwgpu_batch_timing": (c_int, [c_void_p, c_int]),
+        "gwgpu_batch_last_timing": (c_int, [c_void_p, P(ctypes.c_float), P(ctypes.c_float)]),
+        "gwgpu_batch_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_int, ip, c_int, c_double, c_int, c_void_p,
+                                         c_void_p, ip, P(ctypes.c_float)]),
     }
     for name, (res, args) in list(sig.items()) + list(optional.items()):
         fn = getattr(L, name, None)

@@ -1,6 +1,7 @@
 // batch.cu -- batched log-likelihood entry points: many requests (chains x
-// temperatures x ensembles, possibly on different grids) in one prologue
-// launch plus one persistent fused bin kernel.
+// temperatures x ensembles, possibly on different grids and approximants) in
+// one prologue launch plus one persistent fused bin kernel, replayed through
+// captured CUDA graphs, with the bin tile picked by an autotuner.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -17,7 +18,20 @@ namespace gwb {
 
 int default_tile(int mixed) { return mixed ? 4096 : 1024; }
 
-int persistent_grid(int device, int mixed, int ndet) {
+static int length_class(int N) {  // grid-length bucket of the tuning table
+  int c = 0;
+  while ((1 << (c + 11)) < N && c < 12) c++;
+  return c;
+}
+
+int choose_tile(gwgpu_context *c, int mixed, int ndet, int N) {
+  if (c->tile_override > 0) return c->tile_override;
+  auto it = c->tuned.find(std::to_string(mixed) + ":" + std::to_string(ndet) + ":" + std::to_string(length_class(N)));
+  if (it != c->tuned.end()) return it->second;
+  return default_tile(mixed);
+}
+
+static int persistent_grid(int device, int mixed, int ndet) {
   static int cache[2][gwt::kMaxDet + 1] = {{0}};
   int &g = cache[mixed ? 1 : 0][ndet];
   if (g) return g;
@@ -29,11 +43,44 @@ int persistent_grid(int device, int mixed, int ndet) {
   return g;
 }
 
-// Plan = item list for one (n, handles, tile) shape, uploaded once.
-int plan_batch(gwgpu_context *c, int n, const int *handles, int ndet, int tile, Plan &pl) {
-  pl.n = n;
-  pl.ndet = ndet;
-  pl.tile = tile;
+static char *align256(char *p) { return (char *)(((uintptr_t)p + 255) & ~(uintptr_t)255); }
+
+static int lane_alloc(gwgpu_context *c, Lane &L, void **p, size_t *cap, size_t bytes, const char *what) {
+  if (*cap >= bytes) return GWGPU_OK;
+  if (*p) {
+    cudaStreamSynchronize(L.stream);
+    c->dfree(*p);
+    L.bytes -= *cap;
+    *p = nullptr;
+    *cap = 0;
+  }
+  size_t nb = std::max(bytes + bytes / 4, (size_t)65536);
+  int st = c->dalloc(p, nb, what);
+  if (st) return st;
+  *cap = nb;
+  L.bytes += nb;
+  return GWGPU_OK;
+}
+
+void lane_release(gwgpu_context *c, Lane &L) {
+  if (L.stream) cudaStreamSynchronize(L.stream);
+  for (auto &g : L.graphs) cudaGraphExecDestroy(g.second);
+  L.graphs.clear();
+  c->dfree(L.plan.mem);
+  c->dfree(L.work);
+  c->dfree(L.dio);
+  if (L.hio) cudaFreeHost(L.hio);
+  L.plan = Plan();
+  L.work = L.dio = L.hio = nullptr;
+  L.work_cap = L.io_cap = 0;
+  L.bytes = 0;
+  if (L.own_stream && L.stream) cudaStreamDestroy(L.stream);
+  L.stream = nullptr;
+}
+
+// Item list of one (n, handles, tile) shape: contiguous bin tiles per request.
+int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, int tile) {
+  Plan &pl = L.plan;
   std::vector<gwk::Item> items;
   std::vector<int> start(n), count(n);
   for (int r = 0; r < n; r++) {
@@ -49,59 +96,54 @@ int plan_batch(gwgpu_context *c, int n, const int *handles, int ndet, int tile, 
     count[r] = nt;
     for (int t = 0; t < nt; t++) items.push_back(gwk::Item{r, t * tile});
   }
-  // longest requests first so the persistent grid drains evenly
-  pl.nitems = (int)items.size();
-  size_t need = sizeof(gwk::Item) * items.size() + sizeof(int) * (size_t)n * (2 + ndet);
-  void *dev;
-  int st = c->workspace(gwgpu_context::kWsBatchItems, need, &dev);
+  // Longest requests' items first: the persistent grid then drains evenly.
+  std::vector<int> order(n);
+  for (int r = 0; r < n; r++) order[r] = r;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return count[a] > count[b]; });
+  std::vector<gwk::Item> sorted;
+  sorted.reserve(items.size());
+  for (int r : order)
+    for (int q = 0; q < count[r]; q++) sorted.push_back(items[start[r] + q]);
+  // partial sums are indexed by item: keep item ids contiguous per request
+  std::vector<int> nstart(n);
+  int pos = 0;
+  for (int r : order) {
+    nstart[r] = pos;
+    pos += count[r];
+  }
+  pl.nitems = (int)sorted.size();
+  size_t need = sizeof(gwk::Item) * sorted.size() + 256 + sizeof(int) * (size_t)n * (2 + ndet) + 256;
+  int st = lane_alloc(c, L, &pl.mem, &pl.cap, need, "batch plan");
   if (st) return st;
-  pl.items = (gwk::Item *)dev;
-  pl.item_start = (int *)(pl.items + items.size());
+  char *p = (char *)pl.mem;
+  pl.items = (gwk::Item *)p;
+  p = align256(p + sizeof(gwk::Item) * sorted.size());
+  pl.item_start = (int *)p;
   pl.item_count = pl.item_start + n;
   pl.handles = pl.item_count + n;
-  cudaMemcpyAsync(pl.items, items.data(), sizeof(gwk::Item) * items.size(), cudaMemcpyHostToDevice, c->stream);
-  cudaMemcpyAsync(pl.item_start, start.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream);
-  cudaMemcpyAsync(pl.item_count, count.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream);
-  cudaMemcpyAsync(pl.handles, handles, sizeof(int) * (size_t)n * ndet, cudaMemcpyHostToDevice, c->stream);
-  pl.key.assign((const char *)handles, (const char *)(handles + (size_t)n * ndet));
-  pl.key += "|" + std::to_string(n) + "|" + std::to_string(tile) + "|" + std::to_string(ndet);
+  cudaMemcpyAsync(pl.items, sorted.data(), sizeof(gwk::Item) * sorted.size(), cudaMemcpyHostToDevice, L.stream);
+  cudaMemcpyAsync(pl.item_start, nstart.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
+  cudaMemcpyAsync(pl.item_count, count.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
+  cudaMemcpyAsync(pl.handles, handles, sizeof(int) * (size_t)n * ndet, cudaMemcpyHostToDevice, L.stream);
+  pl.n = n;
+  pl.ndet = ndet;
+  pl.tile = tile;
   return GWGPU_OK;
 }
 
-// Enqueue prologue + fused kernel on c->stream.  Device arrays in, device out.
-int enqueue_batch(gwgpu_context *c, const gwgpu_gen_params *d_params, const int *d_approx, int n,
-                  const int *h_handles, int ndet, double T_segment, int tc_from_segment, int precision,
-                  double *d_out, int *d_status, int tile) {
-  const int mixed = precision == GWGPU_PREC_MIXED;
-  if (tile <= 0) tile = default_tile(mixed);
-  std::string key((const char *)h_handles, (const char *)(h_handles + (size_t)n * ndet));
-  key += "|" + std::to_string(n) + "|" + std::to_string(tile) + "|" + std::to_string(ndet);
-  Plan &pl = c->plan;
-  if (pl.key != key) {
-    int st = plan_batch(c, n, h_handles, ndet, tile, pl);
-    if (st) {
-      pl.key.clear();
-      return st;
-    }
-  }
-  // per-request scratch: Request/MixedReq, partials, counters
-  size_t rq = mixed ? sizeof(gwt::MixedReq) : sizeof(gwt::Request);
-  size_t bytes = rq * n + sizeof(double) * (size_t)pl.nitems * gwk::kAcc + sizeof(unsigned) * (size_t)(n + 32);
-  void *dev;
-  int st = c->workspace(gwgpu_context::kWsBatch, bytes, &dev);
-  if (st) return st;
-  char *p = (char *)dev;
-  void *reqs = p;
-  p += rq * n;
-  double *partials = (double *)p;
-  p += sizeof(double) * (size_t)pl.nitems * gwk::kAcc;
-  unsigned *cnt = (unsigned *)p;
-  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(unsigned) * (size_t)(n + 32), c->stream);
+static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, const int *d_approx, int n,
+                           int ndet, double T_segment, int mixed, double *d_out, int *d_status, void *reqs,
+                           double *partials, unsigned *cnt) {
+  const Plan &pl = L.plan;
+  const bool timing = c->timing && &L == &c->lane;
+  if (timing) cudaEventRecord(c->t_ev[0], L.stream);
+  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(unsigned) * (size_t)(n + 32), L.stream);
   if (e != cudaSuccess) return c->fail(e, "batch counters");
-  e = gwk::launch_prologue((const gwt::GenParams *)d_params, d_approx, n, pl.handles, ndet, T_segment,
-                           tc_from_segment, c->streams_dev, c->qnm_dev, mixed ? nullptr : (gwt::Request *)reqs,
-                           mixed ? (gwt::MixedReq *)reqs : nullptr, mixed, d_status, c->stream);
+  e = gwk::launch_prologue((const gwt::GenParams *)d_params, d_approx, n, pl.handles, ndet, T_segment, 1,
+                           c->streams_dev, c->qnm_dev, mixed ? nullptr : (gwt::Request *)reqs,
+                           mixed ? (gwt::MixedReq *)reqs : nullptr, mixed, d_status, L.stream);
   if (e != cudaSuccess) return c->fail(e, "prologue launch");
+  if (timing) cudaEventRecord(c->t_ev[1], L.stream);
   gwk::BatchArgs a;
   a.req = mixed ? nullptr : (const gwt::Request *)reqs;
   a.mreq = mixed ? (const gwt::MixedReq *)reqs : nullptr;
@@ -112,7 +154,7 @@ int enqueue_batch(gwgpu_context *c, const gwgpu_gen_params *d_params, const int 
   a.nitems = pl.nitems;
   a.item_start = pl.item_start;
   a.item_count = pl.item_count;
-  a.tile = tile;
+  a.tile = pl.tile;
   a.item_counter = cnt + n;
   a.req_done = cnt;
   a.partials = partials;
@@ -121,8 +163,72 @@ int enqueue_batch(gwgpu_context *c, const gwgpu_gen_params *d_params, const int 
   a.tables = c->tables;
   int grid = std::min(pl.nitems, persistent_grid(c->device, mixed, ndet));
   if (grid < 1) grid = 1;
-  e = gwk::launch_batch(a, mixed, grid, 0, c->stream);
+  e = gwk::launch_batch(a, mixed, grid, 0, L.stream);
   if (e != cudaSuccess) return c->fail(e, "batch launch");
+  if (timing) cudaEventRecord(c->t_ev[2], L.stream);
+  return GWGPU_OK;
+}
+
+int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, const int *d_approx, int n,
+                  const int *h_handles, int ndet, double T_segment, int precision, double *d_out, int *d_status,
+                  int tile, bool use_graph) {
+  const int mixed = precision == GWGPU_PREC_MIXED;
+  if (tile <= 0) {
+    const gwgpu_context::Stream *s0 = c->get_stream(h_handles[0]);
+    if (!s0) return GWGPU_ENOTFOUND;
+    tile = choose_tile(c, mixed, ndet, s0->dev.N);
+  }
+  std::string key((const char *)h_handles, (const char *)(h_handles + (size_t)n * ndet));
+  key += "|" + std::to_string(n) + "|" + std::to_string(tile) + "|" + std::to_string(ndet) + "|" +
+         std::to_string(c->streams_epoch);
+  bool replanned = false;
+  if (L.plan.key != key) {
+    int st = plan_batch(c, L, n, h_handles, ndet, tile);
+    if (st) {
+      L.plan.key.clear();
+      return st;
+    }
+    L.plan.key = key;
+    replanned = true;
+  }
+  size_t rq = mixed ? sizeof(gwt::MixedReq) : sizeof(gwt::Request);
+  size_t bytes = rq * n + 256 + sizeof(double) * (size_t)L.plan.nitems * gwk::kAcc + 256 +
+                 sizeof(unsigned) * (size_t)(n + 32);
+  void *old = L.work;
+  int st = lane_alloc(c, L, &L.work, &L.work_cap, bytes, "batch scratch");
+  if (st) return st;
+  if (L.work != old || replanned) {  // captured graphs hold the old addresses
+    for (auto &g : L.graphs) cudaGraphExecDestroy(g.second);
+    L.graphs.clear();
+  }
+  char *p = (char *)L.work;
+  void *reqs = p;
+  p = align256(p + rq * n);
+  double *partials = (double *)p;
+  p = align256(p + sizeof(double) * (size_t)L.plan.nitems * gwk::kAcc);
+  unsigned *cnt = (unsigned *)p;
+  if (!use_graph || c->timing)
+    return launch_sequence(c, L, d_params, d_approx, n, ndet, T_segment, mixed, d_out, d_status, reqs, partials, cnt);
+  char gk[256];
+  snprintf(gk, sizeof(gk), "%p|%p|%p|%p|%d|%.17g|%d", (const void *)d_params, (const void *)d_approx,
+           (const void *)d_out, (const void *)d_status, mixed, T_segment, n);
+  auto it = L.graphs.find(gk);
+  if (it == L.graphs.end()) {
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return c->fail(e, "graph capture");
+    st = launch_sequence(c, L, d_params, d_approx, n, ndet, T_segment, mixed, d_out, d_status, reqs, partials, cnt);
+    e = cudaStreamEndCapture(L.stream, &g);
+    if (st) return st;
+    if (e != cudaSuccess) return c->fail(e, "graph capture end");
+    cudaGraphExec_t ge;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return c->fail(e, "graph instantiate");
+    it = L.graphs.emplace(gk, ge).first;
+  }
+  cudaError_t e = cudaGraphLaunch(it->second, L.stream);
+  if (e != cudaSuccess) return c->fail(e, "graph launch");
   return GWGPU_OK;
 }
 
@@ -138,23 +244,42 @@ int gwgpu_loglik_batch_device(gwgpu_context *c, const gwgpu_gen_params *d_params
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
   cudaStream_t user = (cudaStream_t)stream;
-  if (user && user != c->stream) {  // order after the caller's stream, then let it wait for us
-    cudaEvent_t ev;
-    cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    cudaEventRecord(ev, user);
-    cudaStreamWaitEvent(c->stream, ev, 0);
-    cudaEventDestroy(ev);
+  gwb::Lane &L = c->lane0();
+  if (user && user != L.stream) {  // order after the caller's stream, then make it wait for us
+    cudaEventRecord(c->ev_in, user);
+    cudaStreamWaitEvent(L.stream, c->ev_in, 0);
   }
-  int st = gwb::enqueue_batch(c, d_params, d_approx, n, h_handles, ndet, T_segment, 1, precision, d_out, d_status,
-                              c->tile_override);
-  if (!st && user && user != c->stream) {
-    cudaEvent_t ev;
-    cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    cudaEventRecord(ev, c->stream);
-    cudaStreamWaitEvent(user, ev, 0);
-    cudaEventDestroy(ev);
+  int st = gwb::enqueue_batch(c, L, d_params, d_approx, n, h_handles, ndet, T_segment, precision, d_out, d_status, 0,
+                              c->use_graphs);
+  if (!st && user && user != L.stream) {
+    cudaEventRecord(c->ev_out, L.stream);
+    cudaStreamWaitEvent(user, c->ev_out, 0);
   }
   return st;
+}
+
+static int stage_io(gwgpu_context *c, gwb::Lane &L, size_t bytes) {
+  if (L.io_cap >= bytes) return GWGPU_OK;
+  if (L.hio) cudaFreeHost(L.hio);
+  L.hio = nullptr;
+  size_t nb = std::max(bytes + bytes / 4, (size_t)65536);
+  if (cudaMallocHost(&L.hio, nb) != cudaSuccess) return GWGPU_ECUDA;
+  c->dfree(L.dio);
+  L.dio = nullptr;
+  L.bytes -= L.io_cap;
+  L.io_cap = 0;
+  int st = c->dalloc(&L.dio, nb, "batch io");
+  if (st) return st;
+  L.io_cap = nb;
+  L.bytes += nb;
+  for (auto &g : L.graphs) cudaGraphExecDestroy(g.second);
+  L.graphs.clear();
+  return GWGPU_OK;
+}
+
+static void statuses(const int *hs, int n, int *status) {
+  if (!status) return;
+  for (int i = 0; i < n; i++) status[i] = hs[i] ? (hs[i] == 1 ? GWGPU_EINVAL : GWGPU_EDOMAIN) : GWGPU_OK;
 }
 
 int gwgpu_loglik_batch(gwgpu_context *c, const gwgpu_gen_params *params, const int *approx, int n, const int *handles,
@@ -163,31 +288,22 @@ int gwgpu_loglik_batch(gwgpu_context *c, const gwgpu_gen_params *params, const i
     return GWGPU_EINVAL;
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
+  gwb::Lane &L = c->lane0();
   size_t pb = sizeof(gwgpu_gen_params) * n, ab = sizeof(int) * n, ob = sizeof(double) * n, sb = sizeof(int) * n;
-  void *h, *d;
-  int st = c->pinned(gwgpu_context::kHwsBatch, pb + ab + ob + sb + 64, &h);
+  int st = stage_io(c, L, pb + ab + ob + sb + 64);
   if (st) return st;
-  st = c->workspace(gwgpu_context::kWsServe + 1, pb + ab + ob + sb + 64, &d);
-  if (st) return st;
-  char *hp = (char *)h, *dp = (char *)d;
+  char *hp = (char *)L.hio, *dp = (char *)L.dio;
   std::memcpy(hp, params, pb);
   std::memcpy(hp + pb, approx, ab);
-  cudaMemcpyAsync(dp, hp, pb + ab, cudaMemcpyHostToDevice, c->stream);
-  st = gwb::enqueue_batch(c, (const gwgpu_gen_params *)dp, (const int *)(dp + pb), n, handles, ndet, T_segment, 1,
-                          precision, (double *)(dp + pb + ab), (int *)(dp + pb + ab + ob), c->tile_override);
+  cudaMemcpyAsync(dp, hp, pb + ab, cudaMemcpyHostToDevice, L.stream);
+  st = gwb::enqueue_batch(c, L, (const gwgpu_gen_params *)dp, (const int *)(dp + pb), n, handles, ndet, T_segment,
+                          precision, (double *)(dp + pb + ab), (int *)(dp + pb + ab + ob), 0, c->use_graphs);
   if (st) return st;
-  cudaMemcpyAsync(hp + pb + ab, dp + pb + ab, ob + sb, cudaMemcpyDeviceToHost, c->stream);
-  cudaError_t e = cudaStreamSynchronize(c->stream);
+  cudaMemcpyAsync(hp + pb + ab, dp + pb + ab, ob + sb, cudaMemcpyDeviceToHost, L.stream);
+  cudaError_t e = cudaStreamSynchronize(L.stream);
   if (e != cudaSuccess) return c->fail(e, "batch");
   std::memcpy(loglik, hp + pb + ab, ob);
-  const int *hs = (const int *)(hp + pb + ab + ob);
-  int any = 0;
-  for (int i = 0; i < n; i++) {
-    int s = hs[i] ? (hs[i] == 1 ? GWGPU_EINVAL : GWGPU_EDOMAIN) : GWGPU_OK;
-    if (status) status[i] = s;
-    any |= s;
-  }
-  (void)any;
+  statuses((const int *)(hp + pb + ab + ob), n, status);
   return GWGPU_OK;
 }
 
@@ -198,33 +314,114 @@ int gwgpu_mcmc_loglik_batch(gwgpu_context *c, const double *theta, int dim, int 
     return GWGPU_EINVAL;
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
+  gwb::Lane &L = c->lane0();
   size_t tb = sizeof(double) * (size_t)n * dim, pb = sizeof(gwgpu_gen_params) * n, ab = sizeof(int) * n,
          ob = sizeof(double) * n, sb = sizeof(int) * n;
-  void *h, *d;
-  int st = c->pinned(gwgpu_context::kHwsBatch, tb + ob + sb + 64, &h);
+  int st = stage_io(c, L, tb + pb + ab + ob + sb + 64);
   if (st) return st;
-  st = c->workspace(gwgpu_context::kWsServe + 2, tb + pb + ab + ob + sb + 64, &d);
-  if (st) return st;
-  char *hp = (char *)h, *dp = (char *)d;
+  char *hp = (char *)L.hio, *dp = (char *)L.dio;
   std::memcpy(hp, theta, tb);
-  cudaMemcpyAsync(dp, hp, tb, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(dp, hp, tb, cudaMemcpyHostToDevice, L.stream);
   gwgpu_gen_params *dparams = (gwgpu_gen_params *)(dp + tb);
   int *dapprox = (int *)(dp + tb + pb);
   cudaError_t e = gwk::launch_mcmc_repack((const double *)dp, dim, n, approximant, gmst, (gwt::GenParams *)dparams,
-                                          dapprox, c->stream);
+                                          dapprox, L.stream);
   if (e != cudaSuccess) return c->fail(e, "repack launch");
   double *dout = (double *)(dp + tb + pb + ab);
   int *dstat = (int *)(dp + tb + pb + ab + ob);
-  st = gwb::enqueue_batch(c, dparams, dapprox, n, handles, ndet, T_segment, 1, precision, dout, dstat,
-                          c->tile_override);
+  st = gwb::enqueue_batch(c, L, dparams, dapprox, n, handles, ndet, T_segment, precision, dout, dstat, 0,
+                          c->use_graphs);
   if (st) return st;
-  cudaMemcpyAsync(hp + tb, dout, ob + sb, cudaMemcpyDeviceToHost, c->stream);
-  e = cudaStreamSynchronize(c->stream);
+  cudaMemcpyAsync(hp + tb, dout, ob + sb, cudaMemcpyDeviceToHost, L.stream);
+  e = cudaStreamSynchronize(L.stream);
   if (e != cudaSuccess) return c->fail(e, "mcmc batch");
   std::memcpy(loglik, hp + tb, ob);
-  const int *hs = (const int *)(hp + tb + ob);
-  for (int i = 0; i < n; i++)
-    if (status) status[i] = hs[i] ? (hs[i] == 1 ? GWGPU_EINVAL : GWGPU_EDOMAIN) : GWGPU_OK;
+  statuses((const int *)(hp + tb + ob), n, status);
+  return GWGPU_OK;
+}
+
+int gwgpu_batch_set_tile(gwgpu_context *c, int tile) {
+  if (!c || tile < 0 || (tile > 0 && (tile % 256) != 0)) return GWGPU_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->tile_override = tile;
+  return GWGPU_OK;
+}
+
+int gwgpu_batch_timing(gwgpu_context *c, int on) {
+  if (!c) return GWGPU_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (on && !c->t_ev[0])
+    for (int i = 0; i < 3; i++) cudaEventCreate(&c->t_ev[i]);
+  c->timing = on != 0;
+  return GWGPU_OK;
+}
+
+int gwgpu_batch_last_timing(gwgpu_context *c, float *prologue_ms, float *kernel_ms) {
+  if (!c || !c->t_ev[0]) return GWGPU_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaError_t e = cudaEventSynchronize(c->t_ev[2]);
+  if (e != cudaSuccess) return c->fail(e, "timing");
+  float a = 0, b = 0;
+  cudaEventElapsedTime(&a, c->t_ev[0], c->t_ev[1]);
+  cudaEventElapsedTime(&b, c->t_ev[1], c->t_ev[2]);
+  if (prologue_ms) *prologue_ms = a;
+  if (kernel_ms) *kernel_ms = b;
+  return GWGPU_OK;
+}
+
+int gwgpu_batch_use_graphs(gwgpu_context *c, int on) {
+  if (!c) return GWGPU_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->use_graphs = on != 0;
+  return GWGPU_OK;
+}
+
+// Time each candidate tile on this batch (device arrays, results discarded)
+// and remember the fastest for its (precision, detectors, grid length) class.
+int gwgpu_batch_autotune(gwgpu_context *c, const gwgpu_gen_params *d_params, const int *d_approx, int n,
+                         const int *h_handles, int ndet, double T_segment, int precision, double *d_out, int *d_status,
+                         int *best_tile, float *best_ms) {
+  if (!c || !d_params || !d_approx || !h_handles || !d_out || !d_status || n < 1 || ndet < 1 || ndet > gwt::kMaxDet)
+    return GWGPU_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  gwb::Lane &L = c->lane0();
+  const int mixed = precision == GWGPU_PREC_MIXED;
+  const gwgpu_context::Stream *s0 = c->get_stream(h_handles[0]);
+  if (!s0) return GWGPU_ENOTFOUND;
+  static const int cand_mixed[] = {1024, 2048, 4096, 8192, 16384}, cand_fp64[] = {256, 512, 1024, 2048, 4096};
+  const int *cand = mixed ? cand_mixed : cand_fp64;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = 0;
+  float bms = 1e30f;
+  for (int i = 0; i < 5; i++) {
+    int tile = cand[i];
+    int st = gwb::enqueue_batch(c, L, d_params, d_approx, n, h_handles, ndet, T_segment, precision, d_out, d_status,
+                                tile, false);  // warm-up and plan
+    if (st) return st;
+    cudaEventRecord(e0, L.stream);
+    for (int r = 0; r < 3; r++)
+      gwb::enqueue_batch(c, L, d_params, d_approx, n, h_handles, ndet, T_segment, precision, d_out, d_status, tile,
+                         false);
+    cudaEventRecord(e1, L.stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) return c->fail(e, "autotune");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= 3;
+    if (ms < bms) {
+      bms = ms;
+      best = tile;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->tuned[std::to_string(mixed) + ":" + std::to_string(ndet) + ":" + std::to_string(gwb::length_class(s0->dev.N))] =
+      best;
+  if (best_tile) *best_tile = best;
+  if (best_ms) *best_ms = bms;
   return GWGPU_OK;
 }
 

@@ -1,6 +1,11 @@
-// batch_internal.h -- host-side plan of a batched launch (item list on the device).
+// batch_internal.h -- host-side state of batched launches: the item plan, the
+// per-lane scratch (so several batches can be in flight on separate streams),
+// captured CUDA graphs and the tile autotuner's choices.
 #pragma once
 
+#include <cuda_runtime.h>
+
+#include <map>
 #include <string>
 
 #include "kernels.h"
@@ -12,14 +17,36 @@ namespace gwb {
 struct Plan {
   std::string key;
   int n = 0, ndet = 0, tile = 0, nitems = 0;
+  void *mem = nullptr;
+  size_t cap = 0;
   gwk::Item *items = nullptr;
   int *item_start = nullptr, *item_count = nullptr, *handles = nullptr;
 };
 
+// Scratch of one in-flight batch.  Owned by the context (lane 0, the context
+// stream) or by a serving lane.
+struct Lane {
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  Plan plan;
+  void *work = nullptr;  // Request/MixedReq[n], partials, counters
+  size_t work_cap = 0;
+  void *hio = nullptr, *dio = nullptr;  // staging for the host-array entry points
+  size_t io_cap = 0;
+  std::map<std::string, cudaGraphExec_t> graphs;
+  size_t bytes = 0;  // device bytes held (budget accounting)
+};
+
 int default_tile(int mixed);
-int plan_batch(gwgpu_context *c, int n, const int *handles, int ndet, int tile, Plan &pl);
-int enqueue_batch(gwgpu_context *c, const gwgpu_gen_params *d_params, const int *d_approx, int n,
-                  const int *h_handles, int ndet, double T_segment, int tc_from_segment, int precision,
-                  double *d_out, int *d_status, int tile);
+// Tile for one launch: explicit override, else the autotuned choice for this
+// (precision, detectors, grid length) class, else the default.
+int choose_tile(gwgpu_context *c, int mixed, int ndet, int N);
+int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, int tile);
+// Enqueue prologue + fused kernel of n requests on L.stream (device arrays).
+// use_graph: capture/replay the launch sequence for this exact shape.
+int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, const int *d_approx, int n,
+                  const int *h_handles, int ndet, double T_segment, int precision, double *d_out, int *d_status,
+                  int tile, bool use_graph);
+void lane_release(gwgpu_context *c, Lane &L);
 
 }  // namespace gwb

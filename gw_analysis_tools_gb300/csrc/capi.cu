@@ -148,6 +148,24 @@ int gwgpu_context::ensure_tables(int nmax) {
   tables.t13f = (const float *)p[4];
   tables.tm76f = (const float *)p[5];
   tables.nmax = nm;
+  tm76d_n = 0;
+  return GWGPU_OK;
+}
+
+int gwgpu_context::ensure_tm76d(int nmax) {
+  int st = ensure_tables(nmax);
+  if (st) return st;
+  if (tm76d && tm76d_n >= tables.nmax) return GWGPU_OK;
+  dfree(tm76d);
+  tm76d = nullptr;
+  size_t n1 = (size_t)tables.nmax + 1;
+  std::vector<double> v(n1, 0.0);
+  for (size_t n = 1; n < n1; n++) v[n] = std::pow((double)n, -7. / 6.);
+  st = dalloc((void **)&tm76d, 8 * n1, "tm76d");
+  if (st) return st;
+  cudaError_t e = cudaMemcpy(tm76d, v.data(), 8 * n1, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return fail(e, "tm76d upload");
+  tm76d_n = tables.nmax;
   return GWGPU_OK;
 }
 
@@ -163,6 +181,7 @@ int gwgpu_context::sync_streams_table() {
   }
   std::vector<StreamDev> v(streams.size());
   for (size_t i = 0; i < streams.size(); i++) v[i] = streams[i].dev;
+  streams_epoch++;
   cudaError_t e = cudaMemcpyAsync(streams_dev, v.data(), bytes, cudaMemcpyHostToDevice, stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return fail(e, "stream table upload");
@@ -212,6 +231,8 @@ int gwgpu_context_create(int device, size_t budget, gwgpu_context **out) {
     delete c;
     return GWGPU_ECUDA;
   }
+  cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
   std::vector<double> q(5 * gwt::kQnmLen);
   gwk::qnm_host_table(q.data());
   c->qnm_host = q;
@@ -236,9 +257,13 @@ int gwgpu_context_destroy(gwgpu_context *c) {
   for (auto &kv : c->sizes) cudaFree(kv.first);
   for (auto &w : c->hws)
     if (w.second.ptr) cudaFreeHost(w.second.ptr);
-  for (auto &g : c->graphs) {
-    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
-  }
+  c->lane.stream = c->stream;
+  for (auto &g : c->lane.graphs) cudaGraphExecDestroy(g.second);
+  if (c->lane.hio) cudaFreeHost(c->lane.hio);
+  if (c->ev_in) cudaEventDestroy(c->ev_in);
+  for (int i = 0; i < 3; i++)
+    if (c->t_ev[i]) cudaEventDestroy(c->t_ev[i]);
+  if (c->ev_out) cudaEventDestroy(c->ev_out);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return GWGPU_OK;
@@ -313,6 +338,10 @@ int gwgpu_data_register(gwgpu_context *c, const char *detector, const double *fr
   s.live = true;
   s.mem = {pf, pd, pp, pdh, pwh};
   s.host_freqs.assign(freqs, freqs + N);
+  uint64_t hsh = 1469598103934665603ull;
+  const unsigned char *pb = (const unsigned char *)psd;
+  for (size_t i = 0; i < 8 * (size_t)N; i++) hsh = (hsh ^ pb[i]) * 1099511628211ull;
+  s.psd_hash = hsh ^ (uint64_t)N;
   if (d.uniform_int) {
     st = c->ensure_tables(d.n0 + N);
     if (st) return st;
@@ -330,7 +359,6 @@ int gwgpu_data_release(gwgpu_context *c, int handle) {
   for (void *p : c->streams[handle].mem) c->dfree(p);
   c->streams[handle].live = false;
   c->streams[handle].dev.N = 0;
-  c->graphs.clear();
   return c->sync_streams_table();
 }
 

@@ -23,10 +23,7 @@ struct gwgpu_context {
     bool live = false;
     std::vector<void *> mem;
     std::vector<double> host_freqs;
-  };
-  // A captured batch launch (prologue + fused kernel) for one request shape.
-  struct Graph {
-    cudaGraphExec_t exec = nullptr;
+    uint64_t psd_hash = 0;  // FNV-1a of the PSD bytes: detectors with equal PSDs share weights
   };
   enum { kWsWave = 0, kWsInner, kWsPlain, kWsBatch, kWsBatchItems, kWsFisher, kWsServe };
   enum { kHwsPlain = 0, kHwsBatch, kHwsFisher };
@@ -42,13 +39,24 @@ struct gwgpu_context {
   double *qnm_dev = nullptr;
   gwt::Tables tables{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
   std::vector<void *> table_mem;
+  double *tm76d = nullptr;  // FP64 n^(-7/6), built on first Fisher use
+  int tm76d_n = 0;
   std::vector<Stream> streams;
   gwk::StreamDev *streams_dev = nullptr;
   size_t streams_dev_cap = 0;
   unsigned *counters = nullptr;
-  std::map<std::string, Graph> graphs;
-  gwb::Plan plan;
+  gwb::Lane lane;                  // scratch of the context-stream batches
+  std::map<std::string, int> tuned;  // autotuned tile per (precision, detectors, grid length)
   int tile_override = 0;
+  bool use_graphs = true;
+  uint64_t streams_epoch = 0;      // bumped when the device stream table changes
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  bool timing = false;                                   // per-kernel events on context-stream batches
+  cudaEvent_t t_ev[3] = {nullptr, nullptr, nullptr};     // before prologue, after prologue, after bin kernel
+  gwb::Lane &lane0() {
+    lane.stream = stream;
+    return lane;
+  }
 
   ~gwgpu_context();
   int fail(cudaError_t e, const char *where);
@@ -57,6 +65,7 @@ struct gwgpu_context {
   int workspace(int slot, size_t bytes, void **out);
   int pinned(int slot, size_t bytes, void **out);
   int ensure_tables(int nmax);
+  int ensure_tm76d(int nmax);
   int sync_streams_table();
   const Stream *get_stream(int handle) const;
   unsigned *counter(int i);

@@ -1,0 +1,278 @@
+// fisher_math.h -- Fisher matrix arithmetic shared by the kernels
+// (fisher.cu) and the CPU test build: per-perturbation prologue, the
+// amplitude/phase central differences, the moment-form Gram sums and the FP64
+// assembly + pivoted Cholesky inverse.
+#pragma once
+
+#include "phenom_mixed.h"
+
+namespace gwf {
+using namespace gwt;
+
+constexpr int kDim = kFisherDim;
+constexpr int kSlots = 1 + 2 * kDim;  // centre, then (+, -) per parameter
+constexpr int kIntr = 4;              // parameters 7..10 change the waveform itself
+constexpr int kCheap = 7;             // parameters 0..6: projection, phase offset, tc, D_L
+constexpr int kSums = 3 + 10 + 16;    // M0, M1, M2 | Q (4x4 sym) | S_i, T_i (complex)
+
+struct SlotOut {
+  WaveF64 w;
+  double Gre[kMaxDet], Gim[kMaxDet], tau[kMaxDet];
+  int status;
+};
+
+struct FisherSrc {
+  WaveF64 w0, wp[kIntr], wm[kIntr];
+  double sp[kIntr], sm[kIntr];  // A_scale(+/-) / A_scale(centre)
+  double div[kDim];
+  double v[kDim];
+  int logf[kDim];
+  double G0re[kMaxDet], G0im[kMaxDet];
+  double ar[kMaxDet][kCheap], ai[kMaxDet][kCheap], br[kMaxDet][kCheap], bi[kMaxDet][kCheap];
+  int status;
+};
+// ----------------------------------------------------- pivoted Cholesky inverse
+// Symmetric diagonal pivoting on the largest remaining diagonal, LDL^T, inverse
+// (gsl_cholesky_matrix_invert, util.cpp:857-900).  Returns 0 on success.
+GW_HD int chol_invert(const double *a, double *inv, int dim) {
+  double A[kDim * kDim], Li[kDim * kDim], Dv[kDim];
+  int perm[kDim];
+  for (int i = 0; i < dim * dim; i++) A[i] = a[i];
+  for (int i = 0; i < dim; i++) perm[i] = i;
+  for (int j = 0; j < dim; j++) {
+    int piv = j;
+    for (int i = j + 1; i < dim; i++)
+      if (A[i * dim + i] > A[piv * dim + piv]) piv = i;
+    if (piv != j) {
+      for (int k = 0; k < dim; k++) {
+        double t = A[j * dim + k];
+        A[j * dim + k] = A[piv * dim + k];
+        A[piv * dim + k] = t;
+      }
+      for (int k = 0; k < dim; k++) {
+        double t = A[k * dim + j];
+        A[k * dim + j] = A[k * dim + piv];
+        A[k * dim + piv] = t;
+      }
+      int t = perm[j];
+      perm[j] = perm[piv];
+      perm[piv] = t;
+    }
+    double d = A[j * dim + j];
+    if (!(d > 0)) return 1;
+    Dv[j] = d;
+    for (int i = j + 1; i < dim; i++) A[i * dim + j] /= d;
+    for (int i = j + 1; i < dim; i++)
+      for (int k = j + 1; k <= i; k++) {
+        A[i * dim + k] -= A[i * dim + j] * A[k * dim + j] * d;
+        A[k * dim + i] = A[i * dim + k];
+      }
+  }
+  for (int i = 0; i < dim * dim; i++) Li[i] = 0;
+  for (int i = 0; i < dim; i++) {
+    Li[i * dim + i] = 1;
+    for (int j = 0; j < i; j++) {
+      double s = 0;
+      for (int k = j; k < i; k++) s += A[i * dim + k] * Li[k * dim + j];
+      Li[i * dim + j] = -s;
+    }
+  }
+  for (int i = 0; i < dim; i++)
+    for (int j = 0; j < dim; j++) {
+      double s = 0;
+      for (int k = (i > j ? i : j); k < dim; k++) s += Li[k * dim + i] * Li[k * dim + j] / Dv[k];
+      inv[perm[i] * dim + perm[j]] = s;
+    }
+  for (int i = 0; i < dim * dim; i++)
+    if (inv[i] != inv[i]) return 1;
+  return 0;
+}
+
+// One (source, slot) of the batched Fisher: perturbed parameters, prologue,
+// FP64 wave coefficients, projection constants.
+GW_HDNI void fisher_slot(const GenParams &in, int slot, int method, const int *dets, int ndet, double df,
+                         double epsilon, int step_mode, const double *qnm, SlotOut &o) {
+  double v[kDim], pv[kDim];
+  int logf[kDim];
+  fisher_unpack(in, method, v, logf);
+  if (slot == 0) {
+    for (int j = 0; j < kDim; j++) pv[j] = v[j];
+  } else {
+    int i = (slot - 1) / 2, sign = ((slot - 1) % 2 == 0) ? 1 : -1;
+    fisher_perturb(v, i, sign, fisher_step(v, i, epsilon, step_mode), pv);
+  }
+  GenParams p;
+  fisher_repack(pv, in, method, p);
+  Request r;
+  request_prologue(r, p, kPhenomD, dets, ndet, qnm);
+  wave64_prologue(r, df, o.w);
+  double ci = cos(p.incl_angle);
+  for (int d = 0; d < ndet; d++) {
+    o.Gre[d] = r.det[d].fp * .5 * (1 + ci * ci);
+    o.Gim[d] = -r.det[d].fc * ci;
+    o.tau[d] = r.det[d].tau;
+  }
+  bool bad = !(p.mass1 > 0) || !(p.mass2 > 0) || !(p.Luminosity_Distance > 0) || r.m.status != 0;
+  o.status = bad ? 4 : 0;
+}
+
+// Combine the slots of one source into the constants of the Gram sums.
+GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsilon, int step_mode, const SlotOut *S,
+                         FisherSrc &F) {
+  fisher_unpack(in, method, F.v, F.logf);
+  int st = 0;
+  for (int s = 0; s < kSlots; s++) st |= S[s].status;
+  for (int i = 0; i < kDim; i++) {
+    double eps = fisher_step(F.v, i, epsilon, step_mode);
+    double tmp[kDim];
+    F.div[i] = fisher_perturb(F.v, i, 1, eps, tmp);
+  }
+  F.w0 = S[0].w;
+  const double A0 = S[0].w.A_scale;
+  for (int k = 0; k < kIntr; k++) {
+    int i = 7 + k;
+    F.wp[k] = S[1 + 2 * i].w;
+    F.wm[k] = S[2 + 2 * i].w;
+    F.sp[k] = F.wp[k].A_scale / A0;
+    F.sm[k] = F.wm[k].A_scale / A0;
+  }
+  for (int d = 0; d < ndet; d++) {
+    double g0r = S[0].Gre[d], g0i = S[0].Gim[d];
+    F.G0re[d] = g0r;
+    F.G0im[d] = g0i;
+    for (int i = 0; i < kCheap; i++) {
+      const SlotOut &P = S[1 + 2 * i], &Mn = S[2 + 2 * i];
+      double dv = F.div[i];
+      double ar = 0, ai = 0, br = 0, bi = 0;
+      if (i <= 3) {  // RA, DEC, psi, iota: dG + i G f dtau
+        ar = (P.Gre[d] - Mn.Gre[d]) / dv;
+        ai = (P.Gim[d] - Mn.Gim[d]) / dv;
+        double dt = (P.tau[d] - Mn.tau[d]) / dv;
+        br = -g0i * dt;  // i G dtau
+        bi = g0r * dt;
+      } else if (i == 4) {  // phiRef: i G dphic
+        double dph = (P.w.phic - Mn.w.phic) / dv;
+        ar = -g0i * dph;
+        ai = g0r * dph;
+      } else if (i == 5) {  // tc: i G dtcl (f - fref)
+        double dt = (P.w.tcl - Mn.w.tcl) / dv;
+        double fr = S[0].w.fref;
+        br = -g0i * dt;
+        bi = g0r * dt;
+        ar = g0i * dt * fr;
+        ai = -g0r * dt * fr;
+      } else {  // D_L: G dA/A
+        double rel = (P.w.A_scale - Mn.w.A_scale) / (dv * A0);
+        ar = g0r * rel;
+        ai = g0i * rel;
+      }
+      if (F.logf[i]) {
+        ar *= F.v[i];
+        ai *= F.v[i];
+        br *= F.v[i];
+        bi *= F.v[i];
+      }
+      F.ar[d][i] = ar;
+      F.ai[d][i] = ai;
+      F.br[d][i] = br;
+      F.bi[d][i] = bi;
+    }
+  }
+  F.status = st;
+  return st;
+}
+
+
+// One bin: the intrinsic amplitude/phase differences and the moment sums,
+// accumulated for weight stream w with weight wh (Simpson-weighted 1/S).
+GW_HD bool fisher_bin_q(const FisherSrc &F, int n, double t, double r, double lnn, double t34, double m76, float &a0,
+                        float *qr, float *qi) {
+  double amp0, phi0;
+  wave64_eval(F.w0, n, t, r, lnn, t34, m76, amp0, phi0);
+  if (amp0 == 0.0) return false;
+  a0 = (float)amp0;
+  for (int q = 0; q < kIntr; q++) {
+    double ap, pp, am, pm;
+    wave64_eval(F.wp[q], n, t, r, lnn, t34, m76, ap, pp);
+    wave64_eval(F.wm[q], n, t, r, lnn, t34, m76, am, pm);
+    double inv = 1.0 / F.div[7 + q];
+    double dA = (ap * F.sp[q] - am * F.sm[q]) * inv;
+    double dP = ((pp - F.wp[q].phic) - (pm - F.wm[q].phic)) * inv;
+    qr[q] = (float)dA;  // q = dA - i A dPhi
+    qi[q] = (float)(-amp0 * dP);
+  }
+  return true;
+}
+GW_HD void fisher_accumulate(float wh, float a0, float fk, const float *qr, const float *qi, KSum *A) {
+  float wa2 = wh * a0 * a0;
+  kadd(A[0], wa2);
+  kadd(A[1], wa2 * fk);
+  kadd(A[2], wa2 * fk * fk);
+  int o = 3;
+  for (int i = 0; i < kIntr; i++)
+    for (int j = i; j < kIntr; j++) kadd(A[o++], wh * (qr[i] * qr[j] + qi[i] * qi[j]));
+  float wa = wh * a0;
+  for (int i = 0; i < kIntr; i++) {
+    kadd(A[13 + 4 * i + 0], wa * qr[i]);
+    kadd(A[13 + 4 * i + 1], wa * qi[i]);
+    kadd(A[13 + 4 * i + 2], wa * qr[i] * fk);
+    kadd(A[13 + 4 * i + 3], wa * qi[i] * fk);
+  }
+}
+// FP64 assembly of Gamma from the moment sums Ssum[w * kSums + j] of each
+// weight stream; wscale[w] * ratio restores the whitening scale and the
+// Simpson step of calculate_fisher_elements (fisher.cpp:2704-2781).
+GW_HDNI void fisher_assemble(const FisherSrc &F, const double *Ssum, int ndet, const int *wslot, const double *wscale,
+                         double ratio, double *Gm) {
+  for (int j = 0; j < kDim * kDim; j++) Gm[j] = 0;
+  const double A0 = F.w0.A_scale;
+  for (int d = 0; d < ndet; d++) {
+    const int w = wslot[d];
+    const double *Sv = Ssum + w * kSums;
+    const double c = A0 * A0 * wscale[w] * ratio;
+    const double M0 = Sv[0], M1 = Sv[1], M2 = Sv[2];
+    const double gr = F.G0re[d], gi = F.G0im[d], g2 = gr * gr + gi * gi;
+    // cheap x cheap
+    for (int i = 0; i < kCheap; i++)
+      for (int j = 0; j <= i; j++) {
+        double aiR = F.ar[d][i], aiI = F.ai[d][i], biR = F.br[d][i], biI = F.bi[d][i];
+        double ajR = F.ar[d][j], ajI = F.ai[d][j], bjR = F.br[d][j], bjI = F.bi[d][j];
+        double t0 = aiR * ajR + aiI * ajI;                            // Re(a_i a_j*)
+        double t1 = (aiR * bjR + aiI * bjI) + (biR * ajR + biI * ajI);  // Re(a_i b_j* + b_i a_j*)
+        double t2 = biR * bjR + biI * bjI;
+        Gm[i * kDim + j] += c * (t0 * M0 + t1 * M1 + t2 * M2);
+      }
+    // intrinsic x intrinsic
+    int o = 3;
+    for (int ii = 0; ii < kIntr; ii++)
+      for (int jj = ii; jj < kIntr; jj++) {
+        double val = c * g2 * Sv[o++];
+        int I = 7 + jj, J = 7 + ii;  // I >= J
+        Gm[I * kDim + J] += val;
+      }
+    // intrinsic x cheap: Re[G conj(a_j) S_i + G conj(b_j) T_i]
+    for (int ii = 0; ii < kIntr; ii++) {
+      double Sr = Sv[13 + 4 * ii], Si = Sv[14 + 4 * ii], Tr = Sv[15 + 4 * ii], Ti = Sv[16 + 4 * ii];
+      for (int j = 0; j < kCheap; j++) {
+        double ajR = F.ar[d][j], ajI = F.ai[d][j], bjR = F.br[d][j], bjI = F.bi[d][j];
+        // G conj(a_j) = (gr + i gi)(ajR - i ajI)
+        double car = gr * ajR + gi * ajI, cai = gi * ajR - gr * ajI;
+        double cbr = gr * bjR + gi * bjI, cbi = gi * bjR - gr * bjI;
+        double val = (car * Sr - cai * Si) + (cbr * Tr - cbi * Ti);
+        Gm[(7 + ii) * kDim + j] += c * val;
+      }
+    }
+  }
+  // log factor of M_c (parameter 7) on the intrinsic block
+  if (F.logf[7]) {
+    for (int j = 0; j < kDim; j++) {
+      if (j == 7) Gm[7 * kDim + 7] *= F.v[7] * F.v[7];
+      else if (j < 7) Gm[7 * kDim + j] *= F.v[7];
+      else Gm[j * kDim + 7] *= F.v[7];
+    }
+  }
+  for (int i = 0; i < kDim; i++)
+    for (int j = 0; j < i; j++) Gm[j * kDim + i] = Gm[i * kDim + j];
+}
+
+}  // namespace gwf

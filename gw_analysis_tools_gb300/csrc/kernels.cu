@@ -223,9 +223,10 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
   if (i >= n) return;
   GenParams p = params[i];
   int ap = approx[i];
-  if (tc_from_segment) p.tc = T_segment - p.tc;  // mcmc_gw.cpp:2466-2473
   int dets[kMaxDet];
   const StreamDev &s0 = streams[handles[i * ndet]];
+  // mcmc_gw.cpp:2466-2473; T_segment <= 0 selects 1/df of this request's grid
+  if (tc_from_segment) p.tc = (T_segment > 0 ? T_segment : 1.0 / s0.df) - p.tc;
   int st = 0;
   for (int d = 0; d < ndet; d++) {
     const StreamDev &sd = streams[handles[i * ndet + d]];

@@ -73,6 +73,157 @@ struct MixedReq {
   MixedDet det[kMaxDet];
 };
 
+// FP64 coefficients of the amplitude and phase of one request on a grid
+// f_n = n df, as polynomials in the per-bin tables (shared by the mixed form,
+// which rounds them to FP32 hi/lo pairs, and by the Fisher, which keeps FP64).
+struct WaveF64 {
+  int n_f1, n_f3, n_f1p, n_f2p, n_cut, n_mid;
+  double A_scale;                 // A0eff (M df)^(-7/6), times 1/2 for Pv2
+  double qi[12], bi0, bi1;        // inspiral phase
+  double pA, pB, pC, pD;          // intermediate phase
+  double mA, mB, mC, mD, mE;      // ringdown phase (atan term: mE atan((n - nc) inv_nw))
+  double nc, inv_nw;
+  double ai[10];                  // inspiral amplitude, polynomial in t = n^(1/3)
+  double ei[5];                   // intermediate amplitude, polynomial in n - n_mid
+  double mrK, mrExp, mrG2, nrd;   // ringdown amplitude: mrK exp(-mrExp x)/(x^2 + mrG2), x = n - nrd
+  double tcl, fref, phic;         // linear phase: - tcl (f - fref) - phic
+};
+
+GW_HDNI void wave64_prologue(const Request &r, double df, WaveF64 &x) {
+  const ModelD &m = r.m;
+  const Source &s = m.s;
+  const double M = s.M, eta = s.eta, Mdf = M * df;
+  auto first_ge = [&](double fb) -> int {
+    double q = ceil(fb / df);
+    if (!(q < 2.0e9)) return 2000000000;
+    int n = (int)q;
+    if (n < 0) n = 0;
+    while (n > 0 && (double)(n - 1) * df >= fb) n--;
+    while ((double)n * df < fb) n++;
+    return n;
+  };
+  x.n_f1 = first_ge(s.f1);         // amp: f < f1 inspiral
+  x.n_f1p = first_ge(s.f1_phase);  // phase: f < f1_phase inspiral
+  {
+    int n = first_ge(s.f3);  // amp: f > f3 ringdown
+    while ((double)n * df <= s.f3) n++;
+    x.n_f3 = n;
+  }
+  {
+    int n = first_ge(s.f2_phase);
+    while ((double)n * df <= s.f2_phase) n++;
+    x.n_f2p = n;
+  }
+  {
+    int n = first_ge(m.fcut);  // last n with n df <= fcut
+    while (n > 0 && (double)n * df > m.fcut) n--;
+    x.n_cut = n;
+  }
+  const bool pv2 = (r.approximant == kPhenomPv2);
+  x.A_scale = m.A0eff * pow(Mdf, -7. / 6.) * (pv2 ? 0.5 : 1.0);
+  const double cu = cbrt(Mdf);
+  const double K = 3. / (128. * eta) * m.pi.PIminus_5third;
+  const double *pn = m.pn_phase;
+  const double Lc = log(kPi * Mdf);
+  double q[12];
+  q[0] = K * pn[0];
+  q[1] = K * pn[1] * m.pi.PIthird;
+  q[2] = K * pn[2] * m.pi.PI2third;
+  q[3] = K * pn[3] * kPi;
+  q[4] = K * pn[4] * m.pi.PI4third;
+  q[5] = K * m.pi.PI5third * (pn[8] + pn[9] * Lc) - kPi / 4.;
+  q[6] = K * m.pi.PIsquare * (pn[10] - pn[11] * Lc);
+  q[7] = K * pn[7] * m.pi.PI7third;
+  q[8] = m.l.sigma[1] / eta;
+  q[9] = (3. / 4.) * m.l.sigma[2] / eta;
+  q[10] = (3. / 5.) * m.l.sigma[3] / eta;
+  q[11] = (1. / 2.) * m.l.sigma[4] / eta;
+  double cp = pow(cu, -5.);
+  for (int j = 0; j < 12; j++) {
+    x.qi[j] = q[j] * cp;
+    cp *= cu;
+  }
+  x.bi0 = K * m.pi.PI5third * pn[9];
+  x.bi1 = -K * m.pi.PIsquare * pn[11] * cu;
+  x.pA = (m.l.beta[0] + m.l.beta[2] * log(Mdf)) / eta;
+  x.pB = m.l.beta[1] * Mdf / eta;
+  x.pC = m.l.beta[2] / eta;
+  x.pD = m.l.beta[3] / (3. * eta * Mdf * Mdf * Mdf);
+  x.mA = m.l.alpha[0] / eta;
+  x.mB = m.l.alpha[1] * Mdf / eta;
+  x.mC = m.l.alpha[2] / (eta * Mdf);
+  x.mD = (4. / 3.) * m.l.alpha[3] * pow(Mdf, 0.75) / eta;
+  x.mE = m.l.alpha[4] / eta;
+  x.nc = m.l.alpha[5] * s.fRD / df;
+  x.inv_nw = df / s.fdamp;
+  {
+    const double *pa = m.pn_amp;
+    double a[10] = {pa[0], pa[1] * m.pi.PIthird, pa[2] * m.pi.PI2third, pa[3] * kPi, pa[4] * m.pi.PI4third,
+                    pa[5] * m.pi.PI5third, pa[6] * m.pi.PIsquare, m.l.rho[0], m.l.rho[1], m.l.rho[2]};
+    double c = 1.0;
+    for (int j = 0; j < 10; j++) {
+      x.ai[j] = a[j] * c;
+      c *= cu;
+    }
+  }
+  {
+    double h = floor(0.5 * (s.f1 + s.f3) / df);
+    x.n_mid = (int)h;
+    const double *d = m.deltas;
+    double c0 = d[0], c1 = d[1] * Mdf, c2 = d[2] * Mdf * Mdf, c3 = d[3] * Mdf * Mdf * Mdf,
+           c4 = d[4] * Mdf * Mdf * Mdf * Mdf;
+    x.ei[4] = c4;
+    x.ei[3] = c3 + 4 * c4 * h;
+    x.ei[2] = c2 + 3 * c3 * h + 6 * c4 * h * h;
+    x.ei[1] = c1 + 2 * c2 * h + 3 * c3 * h * h + 4 * c4 * h * h * h;
+    x.ei[0] = c0 + c1 * h + c2 * h * h + c3 * h * h * h + c4 * h * h * h * h;
+  }
+  {
+    double g1 = m.l.gamma[0], g2 = m.l.gamma[1], g3 = m.l.gamma[2];
+    x.nrd = s.fRD / df;
+    double w = g3 * s.fdamp / df;
+    x.mrK = g1 * g3 * s.fdamp / (M * df * df);
+    x.mrExp = g2 / w;
+    x.mrG2 = w * w;
+  }
+  x.tcl = m.tcl;
+  x.fref = m.fref;
+  x.phic = m.phic;
+}
+
+// FP64 amplitude / A_scale and nonlinear phase at bin n (tables: t = n^(1/3),
+// r = n^(-5/3), lnn = ln n, t34 = n^(3/4), m76 = n^(-7/6)).
+GW_HD void wave64_eval(const WaveF64 &x, int n, double t, double r, double lnn, double t34, double m76, double &amp,
+                       double &phi) {
+  if (n > x.n_cut) {
+    amp = 0.0;
+    phi = 0.0;
+    return;
+  }
+  double a;
+  if (n < x.n_f1) {
+    a = x.ai[9];
+    for (int j = 8; j >= 0; j--) a = a * t + x.ai[j];
+  } else if (n >= x.n_f3) {
+    double xx = (double)n - x.nrd;
+    a = x.mrK * exp(-x.mrExp * xx) / (xx * xx + x.mrG2);
+  } else {
+    double h = (double)(n - x.n_mid);
+    a = (((x.ei[4] * h + x.ei[3]) * h + x.ei[2]) * h + x.ei[1]) * h + x.ei[0];
+  }
+  amp = a * m76;
+  double nd = (double)n;
+  if (n < x.n_f1p) {
+    double p = x.qi[11];
+    for (int j = 10; j >= 0; j--) p = p * t + x.qi[j];
+    phi = r * p + lnn * (x.bi0 + x.bi1 * t);
+  } else if (n >= x.n_f2p) {
+    phi = x.mA + x.mB * nd - x.mC * (r * t * t) + x.mD * t34 + x.mE * atan((nd - x.nc) * x.inv_nw);
+  } else {
+    phi = x.pA + x.pB * nd + x.pC * lnn - x.pD * (r * r * t);
+  }
+}
+
 GW_HD void split_f(double v, float &hi, float &lo) {
   hi = (float)v;
   lo = (float)(v - (double)hi);

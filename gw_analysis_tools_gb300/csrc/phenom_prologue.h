@@ -465,3 +465,85 @@ GW_HDNI int request_prologue(Request &r, const GenParams &in, int approximant, c
 }
 
 }  // namespace gwt
+
+namespace gwt {
+
+// ------------------------------------------------------- Fisher parameters
+// unpack_parameters (fisher.cpp:1841-1961) / repack_parameters (fisher.cpp:2168-2300)
+// for "IMRPhenomD" (method 0: [RA, DEC, psi, iota, phiRef, tc, D_L*, M_c*, eta,
+// chi1, chi2], * = log factor) and "MCMC_IMRPhenomD" (method 1: [RA, sin DEC,
+// psi, cos iota, phiRef, tc, ln D_L, ln M_c, eta, chi1, chi2]).
+constexpr int kFisherDim = 11;
+
+GW_HD void fisher_unpack(const GenParams &p, int method, double *v, int *logf) {
+  for (int i = 0; i < kFisherDim; i++) logf[i] = 0;
+  int mcmc = (method == 1);
+  double mc = calc_chirpmass(p.mass1, p.mass2), eta = calc_eta(p.mass1, p.mass2);
+  v[0] = p.RA;
+  v[1] = mcmc ? sin(p.DEC) : p.DEC;
+  v[2] = p.psi;
+  v[3] = mcmc ? cos(p.incl_angle) : p.incl_angle;
+  v[4] = p.phiRef;
+  v[5] = p.tc;
+  if (mcmc) {
+    v[6] = log(p.Luminosity_Distance);
+    v[7] = log(mc);
+  } else {
+    logf[6] = 1;
+    logf[7] = 1;
+    v[6] = p.Luminosity_Distance;
+    v[7] = mc;
+  }
+  v[8] = eta;
+  v[9] = p.spin1[2];
+  v[10] = p.spin2[2];
+}
+
+// repack_non_parameter_options (fisher.cpp:2514-2535) + repack_parameters
+GW_HD void fisher_repack(const double *v, const GenParams &in, int method, GenParams &o) {
+  for (int k = 0; k < 3; k++) o.spin1[k] = o.spin2[k] = 0;
+  o.chip = -1;
+  o.phip = -1;
+  o.sky_average = in.sky_average;
+  o.f_ref = in.f_ref;
+  o.gmst = in.gmst;
+  o.shift_time = 0;
+  o.shift_phase = in.shift_phase;
+  o.dep_postmerger = in.dep_postmerger;
+  if (method == 1) {
+    o.mass1 = calc_mass1(exp(v[7]), v[8]);
+    o.mass2 = calc_mass2(exp(v[7]), v[8]);
+    o.Luminosity_Distance = exp(v[6]);
+    o.DEC = asin(v[1]);
+    o.incl_angle = acos(v[3]);
+  } else {
+    o.mass1 = calc_mass1(v[7], v[8]);
+    o.mass2 = calc_mass2(v[7], v[8]);
+    o.Luminosity_Distance = v[6];
+    o.DEC = v[1];
+    o.incl_angle = v[3];
+  }
+  o.RA = v[0];
+  o.psi = v[2];
+  o.phiRef = v[4];
+  o.tc = v[5];
+  o.spin1[2] = v[9];
+  o.spin2[2] = v[10];
+}
+
+// The perturbed parameter vector of calculate_derivatives (fisher.cpp:361-375):
+// sign +1 / -1, one-sided at the eta = 1/4 boundary.  Returns the divisor of
+// the central difference (2 eps, or eps when one-sided).
+GW_HD double fisher_perturb(const double *v, int i, int sign, double eps, double *out) {
+  for (int j = 0; j < kFisherDim; j++) out[j] = v[j];
+  bool onesided = (i == 8 && v[i] > .25 - eps);
+  if (sign > 0) out[i] = onesided ? v[i] : v[i] + eps;
+  else out[i] = v[i] - eps;
+  return onesided ? eps : 2. * eps;
+}
+GW_HD double fisher_step(const double *v, int i, double epsilon, int step_mode) {
+  if (step_mode == 1) return epsilon * (v[i] != 0 ? fabs(v[i]) : 1.0);
+  return epsilon;
+}
+
+}  // namespace gwt

@@ -231,3 +231,124 @@ class Context:
                                          _dp(fish), _dp(cov) if cov is not None else None, _ip(status))
         self._check(st, "fisher_batch")
         return fish, cov, status
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("max_inflight", ctypes.c_int), ("max_batch", ctypes.c_int), ("lanes", ctypes.c_int),
+                ("precision", ctypes.c_int), ("T_segment", ctypes.c_double), ("hbm_budget_bytes", ctypes.c_size_t)]
+
+
+class Server:
+    """Continuous-batching log-likelihood server on a Context (serve.cu)."""
+
+    def __init__(self, ctx, T_segment, max_inflight=8192, max_batch=1024, lanes=4, precision=PREC_MIXED,
+                 hbm_budget=0):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        cfg = ServerConfig(max_inflight, max_batch, lanes, precision, float(T_segment), hbm_budget)
+        h = ctypes.c_void_p()
+        ctx._check(self.lib.gwgpu_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(h)), "server_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gwgpu_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, params, approximant, handles):
+        hs = np.ascontiguousarray(handles, dtype=np.int32)
+        t = ctypes.c_uint64()
+        st = self.lib.gwgpu_server_submit(self.h, ctypes.byref(params), approximant, _ip(hs), hs.size, ctypes.byref(t))
+        if st != 0:
+            raise GwGpuError("server_submit: %s" % STATUS.get(st, st))
+        return t.value
+
+    def poll(self, ticket):
+        ll = ctypes.c_double()
+        s = ctypes.c_int()
+        st = self.lib.gwgpu_server_poll(self.h, ticket, ctypes.byref(ll), ctypes.byref(s))
+        if st == 6:
+            return None
+        if st != 0:
+            raise GwGpuError("server_poll: %s" % STATUS.get(st, st))
+        return ll.value, s.value
+
+    def wait(self, ticket, timeout_ms=10000):
+        ll = ctypes.c_double()
+        s = ctypes.c_int()
+        st = self.lib.gwgpu_server_wait(self.h, ticket, timeout_ms, ctypes.byref(ll), ctypes.byref(s))
+        if st != 0:
+            raise GwGpuError("server_wait: %s" % STATUS.get(st, st))
+        return ll.value, s.value
+
+    def stats(self):
+        p50 = ctypes.c_double()
+        p99 = ctypes.c_double()
+        done = ctypes.c_uint64()
+        launches = ctypes.c_uint64()
+        self.lib.gwgpu_server_stats(self.h, ctypes.byref(p50), ctypes.byref(p99), ctypes.byref(done),
+                                    ctypes.byref(launches))
+        return dict(p50_s=p50.value, p99_s=p99.value, completed=done.value, launches=launches.value)
+
+    def reset_stats(self):
+        self.lib.gwgpu_server_reset_stats(self.h)
+
+    def drive(self, params, approximants, handles, arrival_s):
+        """Open-loop load: request i submitted at t0 + arrival_s[i] (native thread)."""
+        parr = params if isinstance(params, ctypes.Array) else params_array(params)
+        n = len(parr)
+        ap = np.ascontiguousarray(np.broadcast_to(np.asarray(approximants, dtype=np.int32), (n,)))
+        hs = np.asarray(handles, dtype=np.int32)
+        if hs.ndim == 1:
+            hs = np.broadcast_to(hs, (n, hs.size))
+        hs = np.ascontiguousarray(hs, dtype=np.int32)
+        arr = np.ascontiguousarray(arrival_s, dtype=np.float64)
+        out = np.zeros(n)
+        status = np.zeros(n, dtype=np.int32)
+        lat = np.zeros(n)
+        wall = ctypes.c_double()
+        st = self.lib.gwgpu_server_drive(self.h, parr, _ip(ap), _ip(hs), hs.shape[1], _dp(arr), n, _dp(out),
+                                         _ip(status), _dp(lat), ctypes.byref(wall))
+        if st != 0:
+            raise GwGpuError("server_drive: %s" % STATUS.get(st, st))
+        return out, status, lat, wall.value
+
+
+def _ctx_batch_device(self, d_params_ptr, d_approx_ptr, n, handles, T_segment, precision, d_out_ptr, d_status_ptr,
+                      stream=None):
+    """gwgpu_loglik_batch_device on raw device pointers (e.g. torch tensors' data_ptr())."""
+    hs = np.ascontiguousarray(handles, dtype=np.int32)
+    ndet = hs.shape[-1] if hs.ndim == 2 else hs.size
+    if hs.ndim == 1:
+        hs = np.ascontiguousarray(np.broadcast_to(hs, (n, ndet)))
+    st = self.lib.gwgpu_loglik_batch_device(self.h, d_params_ptr, d_approx_ptr, n, _ip(hs), ndet, float(T_segment),
+                                            precision, d_out_ptr, d_status_ptr, stream)
+    self._check(st, "loglik_batch_device")
+
+
+def _ctx_autotune(self, d_params_ptr, d_approx_ptr, n, handles, T_segment, precision, d_out_ptr, d_status_ptr):
+    hs = np.ascontiguousarray(handles, dtype=np.int32)
+    ndet = hs.size if hs.ndim == 1 else hs.shape[1]
+    if hs.ndim == 1:
+        hs = np.ascontiguousarray(np.broadcast_to(hs, (n, ndet)))
+    tile = ctypes.c_int()
+    ms = ctypes.c_float()
+    st = self.lib.gwgpu_batch_autotune(self.h, d_params_ptr, d_approx_ptr, n, _ip(hs), ndet, float(T_segment),
+                                       precision, d_out_ptr, d_status_ptr, ctypes.byref(tile), ctypes.byref(ms))
+    self._check(st, "batch_autotune")
+    return tile.value, ms.value
+
+
+def _ctx_use_graphs(self, on):
+    self._check(self.lib.gwgpu_batch_use_graphs(self.h, int(bool(on))), "batch_use_graphs")
+
+
+Context.loglik_batch_device = _ctx_batch_device
+Context.autotune = _ctx_autotune
+Context.use_graphs = _ctx_use_graphs

@@ -116,15 +116,18 @@ int gwgpu_mcmc_likelihood_extrinsic(gwgpu_context *ctx, const gwgpu_gen_params *
  * mcmc_step -> sampler->ll once per chain, mcmc_sampler_internals.cpp:98).
  * approximants[i] is GWGPU_IMRPHENOMD or GWGPU_IMRPHENOMPV2; all detectors of
  * one request share one grid; requests may use different grids (handles per
- * request: handles[i*num_detectors + d]).  status[i] is GWGPU_OK or
- * GWGPU_EDOMAIN (loglik[i] = NaN then). */
+ * request: handles[i*num_detectors + d]).  T_segment <= 0 selects 1/df of
+ * each request's own grid.  status[i] is GWGPU_OK or GWGPU_EDOMAIN (loglik[i]
+ * = NaN then). */
 int gwgpu_loglik_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, const int *approximants, int n,
                        const int *handles, int num_detectors, double T_segment, int precision, double *loglik,
                        int *status);
-/* Same with every array already on the device, enqueued on `stream` (a
- * cudaStream_t or NULL for the context stream); asynchronous. */
+/* Same with params, approximants, log L and status arrays already on the
+ * device (handles stay a host array), enqueued on `stream` (a cudaStream_t or
+ * NULL for the context stream); asynchronous.  Repeated calls with the same
+ * shape and pointers replay one captured CUDA graph. */
 int gwgpu_loglik_batch_device(gwgpu_context *ctx, const gwgpu_gen_params *d_params, const int *d_approximants,
-                              int n, const int *d_handles, int num_detectors, double T_segment, int precision,
+                              int n, const int *handles, int num_detectors, double T_segment, int precision,
                               double *d_loglik, int *d_status, void *stream);
 /* MCMC_likelihood_wrapper(double *param, ...) (mcmc_gw.h:491, mcmc_gw.cpp:2569)
  * for n parameter vectors: MCMC_prep_params + repack_parameters (MCMC_IMRPhenomD
@@ -132,6 +135,22 @@ int gwgpu_loglik_batch_device(gwgpu_context *ctx, const gwgpu_gen_params *d_para
 int gwgpu_mcmc_loglik_batch(gwgpu_context *ctx, const double *theta, int dim, int n, int approximant,
                             double gmst, const int *handles, int num_detectors, double T_segment, int precision,
                             double *loglik, int *status);
+
+/* Tile (bins per work item, a multiple of 256; 0 = autotuned/default) of the
+ * batched kernels, and whether repeated batch shapes replay a captured CUDA
+ * graph (default on). */
+int gwgpu_batch_set_tile(gwgpu_context *ctx, int tile);
+int gwgpu_batch_use_graphs(gwgpu_context *ctx, int on);
+/* Per-kernel timing of context-stream batches (graphs bypassed while on):
+ * CUDA events around the prologue and the fused bin kernel of the last batch. */
+int gwgpu_batch_timing(gwgpu_context *ctx, int on);
+int gwgpu_batch_last_timing(gwgpu_context *ctx, float *prologue_ms, float *kernel_ms);
+/* Autotuner: time the candidate tiles on this batch (device arrays as for
+ * gwgpu_loglik_batch_device; results are overwritten) and keep the fastest for
+ * batches of the same precision, detector count and grid-length class. */
+int gwgpu_batch_autotune(gwgpu_context *ctx, const gwgpu_gen_params *d_params, const int *d_approximants, int n,
+                         const int *handles, int num_detectors, double T_segment, int precision, double *d_loglik,
+                         int *d_status, int *best_tile, float *best_ms);
 
 /* ---- Fisher ---- */
 /* fisher_numerical(double* freqs, int length, string method, string detector,
@@ -150,24 +169,41 @@ int gwgpu_fisher_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, int n
                        int num_detectors, double epsilon, int step_mode, double *fisher, double *covariance,
                        int *status);
 
-/* ---- serving: continuous batching of log-likelihood requests ---- */
+/* ---- serving: continuous batching of log-likelihood requests ----
+ * The reference serves one chain per host thread (mcmc_sampler.cpp:4585-4590,
+ * each calling MCMC_likelihood_wrapper).  Here requests from any number of
+ * chains / temperatures / ensembles are submitted into request slots; a
+ * scheduler keeps up to `lanes` fused batches in flight on separate streams
+ * and admits queued requests into the next launch as lanes and HBM budget
+ * free up.  Results are the same alone and in any mix. */
 typedef struct {
-  int max_inflight;          /* request slots on the device */
+  int max_inflight;          /* request slots (submitted, not yet collected) */
   int max_batch;             /* requests per fused launch */
+  int lanes;                 /* batches in flight at once, 1..16 */
   int precision;             /* GWGPU_PREC_* */
   double T_segment;          /* as for gwgpu_mcmc_likelihood_extrinsic */
+  size_t hbm_budget_bytes;   /* admission budget for in-flight scratch; 0 = the context budget */
 } gwgpu_server_config;
 int gwgpu_server_create(gwgpu_context *ctx, const gwgpu_server_config *cfg, gwgpu_server **out);
 int gwgpu_server_destroy(gwgpu_server *srv);
 /* Queue one request; returns a ticket.  GWGPU_EBUSY when every slot is taken. */
 int gwgpu_server_submit(gwgpu_server *srv, const gwgpu_gen_params *params, int approximant, const int *handles,
                         int num_detectors, uint64_t *ticket);
-/* Non-blocking: GWGPU_OK with the result, GWGPU_EBUSY while still in flight. */
+/* Non-blocking: GWGPU_OK with the result (the slot is freed), GWGPU_EBUSY while
+ * still in flight, GWGPU_ENOTFOUND for an unknown or collected ticket. */
 int gwgpu_server_poll(gwgpu_server *srv, uint64_t ticket, double *loglik, int *status);
 /* Blocks until the ticket completes or timeout_ms passes (GWGPU_ETIMEDOUT). */
 int gwgpu_server_wait(gwgpu_server *srv, uint64_t ticket, int timeout_ms, double *loglik, int *status);
-/* Latency percentiles (seconds, submit -> result visible on host) and counts. */
+/* Latency percentiles (seconds, submit -> result visible on host), counts. */
 int gwgpu_server_stats(gwgpu_server *srv, double *p50, double *p99, uint64_t *completed, uint64_t *launches);
+int gwgpu_server_reset_stats(gwgpu_server *srv);
+/* Load driver: submits request i at t0 + arrival_s[i] from the calling
+ * thread (open loop, arrival time counted as submit time), collects every
+ * result into loglik/status (request order) and the per-request latencies
+ * (completion order); wall_s = time from t0 to the last result. */
+int gwgpu_server_drive(gwgpu_server *srv, const gwgpu_gen_params *params, const int *approximants,
+                       const int *handles, int num_detectors, const double *arrival_s, int n, double *loglik,
+                       int *status, double *latency_s, double *wall_s);
 
 #ifdef __cplusplus
 }

@@ -149,3 +149,46 @@ double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, cons
 }
 
 }  // extern "C"
+
+#include "../../gw_analysis_tools_gb300/csrc/fisher_math.h"
+
+extern "C" int gwh_fisher_batch(const GenParams *p, int method, const double *freqs, int N, int ndet, const int *dets,
+                                const double *const *psd, double epsilon, int step_mode, double *out, double *cov) {
+  using namespace gwf;
+  double df = freqs[1] - freqs[0];
+  int n0 = (int)std::llround(freqs[0] / df);
+  std::vector<SlotOut> slots(kSlots);
+  for (int s = 0; s < kSlots; s++) fisher_slot(*p, s, method, dets, ndet, df, epsilon, step_mode, qnm(), slots[s]);
+  FisherSrc F;
+  int st = fisher_setup(*p, method, ndet, epsilon, step_mode, slots.data(), F);
+  if (st) return st;
+  double sdf = freqs[N / 2] - freqs[N / 2 - 1];
+  std::vector<double> Ssum(kMaxDet * kSums, 0.0);
+  std::vector<int> wslot(ndet);
+  std::vector<double> wscale(ndet);
+  for (int d = 0; d < ndet; d++) {
+    wslot[d] = d;
+    double wmax = 0;
+    for (int k = 0; k < N; k++) {
+      double sw = (k == 0 || k == N - 1) ? 1.0 : ((k & 1) ? 4.0 : 2.0);
+      wmax = std::max(wmax, 4. * sdf / 3. * sw / psd[d][k]);
+    }
+    wscale[d] = wmax;
+    std::vector<KSum> acc(kSums, KSum{0.f, 0.f});
+    for (int k = 0; k < N; k++) {
+      int n = n0 + k;
+      double x = n;
+      float a0, qr[kIntr], qi[kIntr];
+      if (!fisher_bin_q(F, n, std::cbrt(x), std::pow(x, -5. / 3.), std::log(x), std::pow(x, 0.75),
+                        std::pow(x, -7. / 6.), a0, qr, qi))
+        continue;
+      double sw = (k == 0 || k == N - 1) ? 1.0 : ((k & 1) ? 4.0 : 2.0);
+      float wh = (float)(4. * sdf / 3. * sw / psd[d][k] / wmax);
+      fisher_accumulate(wh, a0, (float)(x * df), qr, qi, acc.data());
+    }
+    for (int j = 0; j < kSums; j++) Ssum[d * kSums + j] = (double)acc[j].s - (double)acc[j].c;
+  }
+  fisher_assemble(F, Ssum.data(), ndet, wslot.data(), wscale.data(), df / sdf, out);
+  if (cov) return chol_invert(out, cov, kDim) ? 9 : 0;
+  return 0;
+}

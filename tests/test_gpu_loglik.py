@@ -1,0 +1,169 @@
+"""GPU parity tests through the C ABI: waveform, detector response, the plain
+FP64 form, the batched FP64 and mixed forms, against the FP64 oracle."""
+import numpy as np
+import pytest
+
+import gw_analysis_tools_gb300 as G
+from gw_analysis_tools_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 1e-3     # |delta log L| absolute, mixed form against the FP64 oracle
+FP64_RTOL = 1e-9     # relative, FP64 forms against the FP64 oracle
+
+
+@pytest.fixture(scope="module")
+def network(gpu_ctx, oracle):
+    f = W.config1_grid()
+    T = 1.0 / (f[1] - f[0])
+    src = W.config1_source()
+    dets = list(W.DETECTORS3)
+    injp = oracle.params_from_dict(dict(src, tc=T - src["tc"]))
+    data = []
+    for i, d in enumerate(dets):
+        r = oracle.detector_response(f, injp, d)
+        dt = oracle.dtoa(src["RA"], src["DEC"], src["gmst"], dets[0], d)
+        data.append(r * np.exp(-2j * np.pi * dt * f) + W.noise(f, 100 + i))
+    psd = [W.analytic_psd(f)] * 3
+    handles = [gpu_ctx.register_data(d, f, data[i], psd[i]) for i, d in enumerate(dets)]
+    return dict(f=f, T=T, src=src, dets=dets, data=data, psd=psd, handles=handles)
+
+
+def test_waveform_parity(gpu_ctx, oracle):
+    f = W.config1_grid()
+    cases = [("IMRPhenomD", 0, W.config1_source()),
+             ("IMRPhenomD", 0, W.prior_draws(1, 9)[0]),
+             ("IMRPhenomPv2", 1, dict(W.config1_source(), spin1=(0.3, 0.2, 0.3), spin2=(-0.1, 0.4, -0.1))),
+             ("IMRPhenomPv2", 1, W.prior_draws(1, 9, precessing=True)[0])]
+    for name, ap, d in cases:
+        a = oracle.fourier_waveform(f, oracle.params_from_dict(d), ap)
+        b = gpu_ctx.fourier_waveform(f, name, G.gen_params(**d))
+        for x, y in zip(a, b):
+            assert np.max(np.abs(x - y)) <= 1e-11 * np.abs(x).max()
+
+
+def test_detector_response_parity(gpu_ctx, oracle):
+    f = W.config1_grid()
+    d = dict(W.config1_source(), RA=2.0, DEC=-0.7, psi=1.3)
+    for det in ("Hanford", "Livingston", "Virgo", "Kagra", "ET1"):
+        a = oracle.detector_response(f, oracle.params_from_dict(d), det)
+        b = gpu_ctx.fourier_detector_response(f, det, "IMRPhenomD", G.gen_params(**d))
+        assert np.max(np.abs(a - b)) <= 1e-11 * np.abs(a).max()
+
+
+def test_log_likelihood_internal(gpu_ctx, oracle, network):
+    n = network
+    r = oracle.detector_response(n["f"], oracle.params_from_dict(n["src"]), "Hanford")
+    ref = oracle.lib().gwo_log_likelihood_internal(oracle._dp(n["data"][0]), oracle._dp(n["psd"][0]),
+                                                   oracle._dp(n["f"]), oracle._dp(r.view(np.float64).copy()),
+                                                   n["f"].size)
+    got = gpu_ctx.log_likelihood_internal(n["data"][0], n["psd"][0], n["f"], r)
+    assert abs(got - ref) <= FP64_RTOL * max(1, abs(ref))
+
+
+def test_plain_single_detector_config1(gpu_ctx, oracle, network):
+    """Config 1: single-detector IMRPhenomD, parameters perturbed by 1%."""
+    n = network
+    draws = W.perturbed(n["src"], 24, seed=5)
+    for d in draws:
+        ref = oracle.loglik(oracle.params_from_dict(d), n["f"], n["dets"][:1], n["data"][:1], n["psd"][:1])
+        got = gpu_ctx.mcmc_likelihood_extrinsic(G.gen_params(**d), "IMRPhenomD", n["handles"][:1], n["T"])
+        assert abs(got - ref) <= FP64_RTOL * max(1, abs(ref))
+
+
+def test_batched_forms_config2(gpu_ctx, oracle, network):
+    """Config 2: 512 requests, 3 detectors, prior draws."""
+    n = network
+    draws = [n["src"]] + W.prior_draws(511, 7)
+    ref = oracle.loglik_batch([oracle.params_from_dict(d) for d in draws], n["f"], n["dets"], n["data"], n["psd"])
+    fp64, st = gpu_ctx.loglik_batch(G.params_array(draws), G.IMRPhenomD, n["handles"], n["T"], G.PREC_FP64)
+    assert np.all(st == 0)
+    assert np.max(np.abs(fp64 - ref) / np.maximum(1, np.abs(ref))) <= FP64_RTOL
+    mixed, st = gpu_ctx.loglik_batch(G.params_array(draws), G.IMRPhenomD, n["handles"], n["T"], G.PREC_MIXED)
+    assert np.all(st == 0)
+    assert np.max(np.abs(mixed - ref)) <= MIXED_TOL
+
+
+def test_batched_pv2(gpu_ctx, oracle, network):
+    n = network
+    draws = W.prior_draws(96, 11, precessing=True)
+    ref = oracle.loglik_batch([oracle.params_from_dict(d) for d in draws], n["f"], n["dets"], n["data"], n["psd"],
+                              approximants=[1] * len(draws))
+    for prec, tol in ((G.PREC_FP64, None), (G.PREC_MIXED, MIXED_TOL)):
+        out, st = gpu_ctx.loglik_batch(G.params_array(draws), G.IMRPhenomPv2, n["handles"], n["T"], prec)
+        assert np.all(st == 0)
+        if tol is None:
+            assert np.max(np.abs(out - ref) / np.maximum(1, np.abs(ref))) <= FP64_RTOL
+        else:
+            assert np.max(np.abs(out - ref)) <= tol
+
+
+def test_mixed_approximants_in_one_batch(gpu_ctx, oracle, network):
+    n = network
+    dd = W.prior_draws(40, 21)
+    dp = W.prior_draws(40, 22, precessing=True)
+    draws = [x for pair in zip(dd, dp) for x in pair]
+    aps = [0, 1] * 40
+    ref = oracle.loglik_batch([oracle.params_from_dict(d) for d in draws], n["f"], n["dets"], n["data"], n["psd"],
+                              approximants=aps)
+    out, st = gpu_ctx.loglik_batch(G.params_array(draws), aps, n["handles"], n["T"], G.PREC_MIXED)
+    assert np.all(st == 0)
+    assert np.max(np.abs(out - ref)) <= MIXED_TOL
+
+
+def test_determinism(gpu_ctx, network):
+    n = network
+    draws = W.prior_draws(300, 31)
+    for prec in (G.PREC_FP64, G.PREC_MIXED):
+        a, _ = gpu_ctx.loglik_batch(G.params_array(draws), 0, n["handles"], n["T"], prec)
+        b, _ = gpu_ctx.loglik_batch(G.params_array(draws), 0, n["handles"], n["T"], prec)
+        assert np.array_equal(a, b)
+
+
+def test_same_result_alone_and_in_the_mix(gpu_ctx, network):
+    n = network
+    draws = W.prior_draws(200, 41)
+    many, _ = gpu_ctx.loglik_batch(G.params_array(draws), 0, n["handles"], n["T"], G.PREC_MIXED)
+    for i in (0, 57, 199):
+        one, _ = gpu_ctx.loglik_batch(G.params_array([draws[i]]), 0, n["handles"], n["T"], G.PREC_MIXED)
+        assert abs(one[0] - many[i]) <= 1e-9 * max(1, abs(many[i]))
+
+
+def test_bad_requests_flagged_rest_complete(gpu_ctx, oracle, network):
+    n = network
+    draws = W.prior_draws(8, 51)
+    bad = [dict(draws[0], mass1=float("nan")), dict(draws[1], mass2=-3.0)]
+    allp = draws[2:] + bad
+    ref = oracle.loglik_batch([oracle.params_from_dict(d) for d in draws[2:]], n["f"], n["dets"], n["data"], n["psd"])
+    for prec in (G.PREC_FP64, G.PREC_MIXED):
+        out, st = gpu_ctx.loglik_batch(G.params_array(allp), 0, n["handles"], n["T"], prec)
+        assert np.all(st[:6] == 0) and np.all(st[6:] != 0)
+        assert np.all(np.isnan(out[6:]))
+        assert np.max(np.abs(out[:6] - ref)) <= MIXED_TOL
+
+
+def test_uneven_grids_one_launch(gpu_ctx, oracle):
+    """Config 3 shape on a reduced band: requests on grids of different T."""
+    durations = [4, 8, 32]
+    grids, hs, datas, psds = {}, {}, {}, {}
+    for T in durations:
+        f = W.uniform_grid(20.0, 512.0, 1.0 / T)
+        grids[T] = f
+        datas[T] = [W.noise(f, 200 + T + i) for i in range(3)]
+        psds[T] = [W.analytic_psd(f)] * 3
+        hs[T] = [gpu_ctx.register_data(d, f, datas[T][i], psds[T][i]) for i, d in enumerate(W.DETECTORS3)]
+    draws = W.prior_draws(30, 61, precessing=True)
+    Ts = [durations[i % 3] for i in range(30)]
+    handles = np.array([hs[T] for T in Ts], dtype=np.int32)
+    for prec, tol in ((G.PREC_FP64, 1e-7), (G.PREC_MIXED, MIXED_TOL)):
+        # every grid in one launch; T_segment = 0 -> 1/df of each request's own grid
+        out, st = gpu_ctx.loglik_batch(G.params_array(draws), 1, handles, 0.0, prec)
+        assert np.all(st == 0)
+        for i in range(30):
+            T = Ts[i]
+            ref = oracle.loglik(oracle.params_from_dict(draws[i]), grids[T], list(W.DETECTORS3), datas[T], psds[T],
+                                approximant=1)
+            assert abs(out[i] - ref) <= tol * (max(1, abs(ref)) if tol < 1e-6 else 1), (i, out[i], ref)
+    for T in durations:
+        for h in hs[T]:
+            gpu_ctx.release_data(h)

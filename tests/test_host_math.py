@@ -74,3 +74,26 @@ def test_host_internals_match_oracle(oracle, hostcheck):
         oracle.lib().gwo_d_internals(ctypes.byref(p), oracle._dp(a))
         hostcheck.gwh_d_internals(ctypes.byref(p), oracle._dp(b))
         np.testing.assert_allclose(b[:21], a[:21], rtol=1e-13, atol=0)
+
+
+def test_host_batched_fisher_algebra_matches_oracle(oracle, hostcheck):
+    """Moment-form batched Fisher (amplitude/phase differences) against the
+    reference algorithm (complex central differences) in the oracle."""
+    dp = ctypes.POINTER(ctypes.c_double)
+    hostcheck.gwh_fisher_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int, dp, dp]
+    f = W.uniform_grid(10.0, 2048.0, 1 / 16.)
+    dets = list(W.DETECTORS3)
+    psd = [W.analytic_psd(f)] * 3
+    idx = (ctypes.c_int * 3)(*[oracle.detector_index(d) for d in dets])
+    for eps, mode, tol in ((1e-6, 1, 1e-5), (1e-8, 0, 1e-3)):
+        for d in W.prior_draws(3, 77):
+            p = oracle.params_from_dict(d)
+            ref = oracle.fisher_network(f, p, dets, psd, epsilon=eps, step_mode=mode)
+            out = np.zeros(121)
+            cov = np.zeros(121)
+            hostcheck.gwh_fisher_batch(ctypes.byref(p), 0, oracle._dp(f), f.size, 3, idx, oracle._ptr_array(psd), eps,
+                                       mode, oracle._dp(out), oracle._dp(cov))
+            G = out.reshape(11, 11)
+            rel = np.abs(G - ref) / np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
+            assert rel.max() <= tol, (eps, rel.max())
