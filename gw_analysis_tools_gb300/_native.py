@@ -13,6 +13,8 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 BUILDDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libgwgpu.so")
+DROPIN_SRC = os.path.join(HERE, "dropin", "gwat_dropin.cpp")
+DROPIN_LIB = os.path.join(LIBDIR, "libgwat_dropin.so")
 SOURCES = ["kernels.cu", "capi.cu", "batch.cu", "fisher.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
@@ -59,7 +61,22 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
+    build_dropin(force)
     return LIB
+
+
+def build_dropin(force=False):
+    """Compile the reference-signature C++ layer (libgwat_dropin.so) over libgwgpu.so."""
+    hdr = os.path.join(os.path.dirname(HERE), "include", "gwat_dropin.h")
+    newest = max(os.path.getmtime(x) for x in (DROPIN_SRC, hdr, LIB))
+    if not force and os.path.exists(DROPIN_LIB) and os.path.getmtime(DROPIN_LIB) >= newest:
+        return DROPIN_LIB
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", DROPIN_SRC, "-o", DROPIN_LIB,
+           "-L" + LIBDIR, "-lgwgpu", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("drop-in build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    return DROPIN_LIB
 
 
 _lib = None

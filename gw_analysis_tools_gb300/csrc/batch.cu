@@ -277,9 +277,11 @@ static int stage_io(gwgpu_context *c, gwb::Lane &L, size_t bytes) {
   return GWGPU_OK;
 }
 
+static size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
+
 static void statuses(const int *hs, int n, int *status) {
   if (!status) return;
-  for (int i = 0; i < n; i++) status[i] = hs[i] ? (hs[i] == 1 ? GWGPU_EINVAL : GWGPU_EDOMAIN) : GWGPU_OK;
+  for (int i = 0; i < n; i++) status[i] = gwk::status_code(hs[i]);
 }
 
 int gwgpu_loglik_batch(gwgpu_context *c, const gwgpu_gen_params *params, const int *approx, int n, const int *handles,
@@ -289,21 +291,24 @@ int gwgpu_loglik_batch(gwgpu_context *c, const gwgpu_gen_params *params, const i
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
   gwb::Lane &L = c->lane0();
-  size_t pb = sizeof(gwgpu_gen_params) * n, ab = sizeof(int) * n, ob = sizeof(double) * n, sb = sizeof(int) * n;
-  int st = stage_io(c, L, pb + ab + ob + sb + 64);
+  // params | approximants | log L | status, each on a 256-byte boundary
+  const size_t pb = sizeof(gwgpu_gen_params) * n, ab = sizeof(int) * n, ob = sizeof(double) * n,
+               sb = sizeof(int) * n;
+  const size_t o_ap = up256(pb), o_out = o_ap + up256(ab), o_st = o_out + up256(ob), total = o_st + up256(sb);
+  int st = stage_io(c, L, total);
   if (st) return st;
   char *hp = (char *)L.hio, *dp = (char *)L.dio;
   std::memcpy(hp, params, pb);
-  std::memcpy(hp + pb, approx, ab);
-  cudaMemcpyAsync(dp, hp, pb + ab, cudaMemcpyHostToDevice, L.stream);
-  st = gwb::enqueue_batch(c, L, (const gwgpu_gen_params *)dp, (const int *)(dp + pb), n, handles, ndet, T_segment,
-                          precision, (double *)(dp + pb + ab), (int *)(dp + pb + ab + ob), 0, c->use_graphs);
+  std::memcpy(hp + o_ap, approx, ab);
+  cudaMemcpyAsync(dp, hp, o_out, cudaMemcpyHostToDevice, L.stream);
+  st = gwb::enqueue_batch(c, L, (const gwgpu_gen_params *)dp, (const int *)(dp + o_ap), n, handles, ndet, T_segment,
+                          precision, (double *)(dp + o_out), (int *)(dp + o_st), 0, c->use_graphs);
   if (st) return st;
-  cudaMemcpyAsync(hp + pb + ab, dp + pb + ab, ob + sb, cudaMemcpyDeviceToHost, L.stream);
+  cudaMemcpyAsync(hp + o_out, dp + o_out, total - o_out, cudaMemcpyDeviceToHost, L.stream);
   cudaError_t e = cudaStreamSynchronize(L.stream);
   if (e != cudaSuccess) return c->fail(e, "batch");
-  std::memcpy(loglik, hp + pb + ab, ob);
-  statuses((const int *)(hp + pb + ab + ob), n, status);
+  std::memcpy(loglik, hp + o_out, ob);
+  statuses((const int *)(hp + o_st), n, status);
   return GWGPU_OK;
 }
 
@@ -315,28 +320,31 @@ int gwgpu_mcmc_loglik_batch(gwgpu_context *c, const double *theta, int dim, int 
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
   gwb::Lane &L = c->lane0();
-  size_t tb = sizeof(double) * (size_t)n * dim, pb = sizeof(gwgpu_gen_params) * n, ab = sizeof(int) * n,
-         ob = sizeof(double) * n, sb = sizeof(int) * n;
-  int st = stage_io(c, L, tb + pb + ab + ob + sb + 64);
+  // theta | params | approximants | log L | status, each on a 256-byte boundary
+  const size_t tb = sizeof(double) * (size_t)n * dim, pb = sizeof(gwgpu_gen_params) * n, ab = sizeof(int) * n,
+               ob = sizeof(double) * n, sb = sizeof(int) * n;
+  const size_t o_p = up256(tb), o_ap = o_p + up256(pb), o_out = o_ap + up256(ab), o_st = o_out + up256(ob),
+               total = o_st + up256(sb);
+  int st = stage_io(c, L, total);
   if (st) return st;
   char *hp = (char *)L.hio, *dp = (char *)L.dio;
   std::memcpy(hp, theta, tb);
   cudaMemcpyAsync(dp, hp, tb, cudaMemcpyHostToDevice, L.stream);
-  gwgpu_gen_params *dparams = (gwgpu_gen_params *)(dp + tb);
-  int *dapprox = (int *)(dp + tb + pb);
+  gwgpu_gen_params *dparams = (gwgpu_gen_params *)(dp + o_p);
+  int *dapprox = (int *)(dp + o_ap);
   cudaError_t e = gwk::launch_mcmc_repack((const double *)dp, dim, n, approximant, gmst, (gwt::GenParams *)dparams,
                                           dapprox, L.stream);
   if (e != cudaSuccess) return c->fail(e, "repack launch");
-  double *dout = (double *)(dp + tb + pb + ab);
-  int *dstat = (int *)(dp + tb + pb + ab + ob);
+  double *dout = (double *)(dp + o_out);
+  int *dstat = (int *)(dp + o_st);
   st = gwb::enqueue_batch(c, L, dparams, dapprox, n, handles, ndet, T_segment, precision, dout, dstat, 0,
                           c->use_graphs);
   if (st) return st;
-  cudaMemcpyAsync(hp + tb, dout, ob + sb, cudaMemcpyDeviceToHost, L.stream);
+  cudaMemcpyAsync(hp + o_out, dout, total - o_out, cudaMemcpyDeviceToHost, L.stream);
   e = cudaStreamSynchronize(L.stream);
   if (e != cudaSuccess) return c->fail(e, "mcmc batch");
-  std::memcpy(loglik, hp + tb, ob);
-  statuses((const int *)(hp + tb + ob), n, status);
+  std::memcpy(loglik, hp + o_out, ob);
+  statuses((const int *)(hp + o_st), n, status);
   return GWGPU_OK;
 }
 

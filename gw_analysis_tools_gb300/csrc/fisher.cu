@@ -33,6 +33,7 @@ using namespace gwt;
 using gwk::StreamDev;
 
 constexpr int kBlock = 128;
+constexpr int kStatusBounds = 0x100;  // set by a tile whose bins fall outside the tables
 
 // ------------------------------------------------------------- batched form
 __global__ void k_fisher_slots(const GenParams *__restrict__ params, int nsrc, int method, const int *__restrict__ dets,
@@ -60,6 +61,7 @@ struct FisherArgs {
   double df, fisher_df_ratio;  // (f1 - f0) / simpson_df
   gwt::Tables tab;
   const double *tm76d;
+  int tm76d_n;              // tm76d valid for n <= tm76d_n
   unsigned *item_counter, *src_done;
   double *partials;  // items * kMaxDet * kSums
   double *fisher, *cov;
@@ -90,7 +92,9 @@ __global__ void __launch_bounds__(kBlock) k_fisher_main(const FisherArgs a) {
 #pragma unroll
     for (int j = 0; j < NW * kSums; j++) acc[j] = KSum{0.f, 0.f};
     const int k0 = tile * a.tile, k1 = min(k0 + a.tile, a.N);
-    if (F.status == 0) {
+    const bool in_tables = a.n0 >= 1 && a.n0 + k1 - 1 <= a.tab.nmax && a.n0 + k1 - 1 <= a.tm76d_n;
+    if (!in_tables && tid == 0) atomicOr(a.status + src, kStatusBounds);
+    if (F.status == 0 && in_tables) {
       for (int k = k0 + tid; k < k1; k += blockDim.x) {
         const int n = a.n0 + k;
         float a0, qr[kIntr], qi[kIntr];
@@ -144,6 +148,7 @@ __global__ void __launch_bounds__(kBlock) k_fisher_main(const FisherArgs a) {
       fisher_assemble(F, Ssum, a.ndet, a.wslot, a.wscale, a.fisher_df_ratio, Gm);
       double *outF = a.fisher + (size_t)src * kDim * kDim;
       int st = F.status;
+      if (__ldcg(a.status + src) & kStatusBounds) st = 5;
       for (int j = 0; j < kDim * kDim; j++) outF[j] = st ? __longlong_as_double(0x7ff8000000000000ll) : Gm[j];
       if (a.cov) {
         double inv[kDim * kDim];
@@ -420,6 +425,7 @@ int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, 
   a.fisher_df_ratio = (s0->host_freqs[1] - s0->host_freqs[0]) / s0->dev.simpson_df;
   a.tab = c->tables;
   a.tm76d = c->tm76d;
+  a.tm76d_n = c->tm76d_n;
   static int grid_cache = 0;
   if (!grid_cache) {
     cudaDeviceProp pr;
@@ -464,7 +470,7 @@ int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, 
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return c->fail(e, "fisher batch");
     if (status)
-      for (int i = 0; i < m; i++) status[s0i + i] = hs[i] == 0 ? GWGPU_OK : (hs[i] == 9 ? GWGPU_EDOMAIN : GWGPU_EDOMAIN);
+      for (int i = 0; i < m; i++) status[s0i + i] = gwk::status_code(hs[i]);
   }
   return GWGPU_OK;
 }

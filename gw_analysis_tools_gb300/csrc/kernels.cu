@@ -245,6 +245,7 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
     }
   } else {
     st = 4;
+    if (want_mixed) mreq[i] = MixedReq{};
   }
   if (st && want_mixed) mreq[i].status = st;
   if (st && req) req[i].m.status = st;
@@ -310,6 +311,7 @@ cudaError_t launch_mcmc_repack(const double *theta, int dim, int n, int approxim
 
 // ---------------------------------------------------------- batched kernels
 constexpr int kBatchBlock = 256;
+constexpr int kStatusBounds = 0x100;  // set by an item whose bins fall outside the tables; finalize reports 5
 
 // Two-level compensated reduction of NV FP32 values per thread:
 // 16-element TwoSum columns, then FP64 across columns.  Result in res[0..NV).
@@ -387,7 +389,11 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch(const BatchArgs a) {
           dh[d] = s_st[d].dhat;
           wh[d] = s_st[d].what;
         }
-        const int kcut = min(kend, x.n_cut - n0 + 1);
+        int kcut = min(kend, x.n_cut - n0 + 1);
+        if (kcut > I.k0 && (n0 < 1 || n0 + kcut - 1 > a.tables.nmax)) {  // grid beyond the power tables
+          if (tid == 0) atomicOr(a.status + I.req, kStatusBounds);
+          kcut = I.k0;
+        }
         for (int k = I.k0 + tid; k < kcut; k += blockDim.x) {
           const int n = n0 + k;
           float dre[NDET], dim[NDET], w[NDET];
@@ -449,6 +455,7 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch(const BatchArgs a) {
           ll = fp64_finalize<NDET>(s, s_st);
           st = r.m.status;
         }
+        if (__ldcg(a.status + I.req) & kStatusBounds) st = 5;
         a.out[I.req] = st ? __longlong_as_double(0x7ff8000000000000ll) : ll;
         a.status[I.req] = st;
       }

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/gwgpu.h"
 #include "phenom_mixed.h"
 
 namespace gwk {
@@ -75,6 +76,18 @@ struct BatchArgs {
 cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int block, cudaStream_t s);
 int batch_block_size(int mixed);
 int batch_occupancy(int mixed, int ndet);  // resident blocks per SM
+
+// Per-request kernel status -> C ABI status: 0 ok, 1 invalid request (grids of
+// different lengths, grid unusable by the mixed form), 4 outside the model
+// domain, 5 grid beyond the per-bin power tables.
+inline int status_code(int kernel_status) {
+  switch (kernel_status) {
+    case 0: return GWGPU_OK;
+    case 1: return GWGPU_EINVAL;
+    case 5: return GWGPU_ETOOLARGE;
+    default: return GWGPU_EDOMAIN;
+  }
+}
 
 // Host-side helpers shared with the C API.
 void qnm_host_table(double *out5x1003);  // x, fring, fdamp, c_fring, c_fdamp

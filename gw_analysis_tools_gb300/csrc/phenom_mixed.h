@@ -89,36 +89,28 @@ struct WaveF64 {
   double tcl, fref, phic;         // linear phase: - tcl (f - fref) - phic
 };
 
+// First grid index n >= 0 with n df >= fb (strict: n df > fb), clamped to
+// 2e9 for NaN or out-of-range boundaries.  ceil(fb / df) is within a step of
+// the answer, so each correction loop runs at most a few times.
+GW_HD int grid_first(double fb, double df, bool strict) {
+  double q = ceil(fb / df);
+  if (!(q < 2.0e9)) return 2000000000;
+  int n = q > 0 ? (int)q : 0;
+  auto ok = [&](int m) { return strict ? (double)m * df > fb : (double)m * df >= fb; };
+  for (int it = 0; it < 4 && n > 0 && ok(n - 1); it++) n--;
+  for (int it = 0; it < 4 && !ok(n) && n < 2000000000; it++) n++;
+  return n;
+}
+
 GW_HDNI void wave64_prologue(const Request &r, double df, WaveF64 &x) {
   const ModelD &m = r.m;
   const Source &s = m.s;
   const double M = s.M, eta = s.eta, Mdf = M * df;
-  auto first_ge = [&](double fb) -> int {
-    double q = ceil(fb / df);
-    if (!(q < 2.0e9)) return 2000000000;
-    int n = (int)q;
-    if (n < 0) n = 0;
-    while (n > 0 && (double)(n - 1) * df >= fb) n--;
-    while ((double)n * df < fb) n++;
-    return n;
-  };
-  x.n_f1 = first_ge(s.f1);         // amp: f < f1 inspiral
-  x.n_f1p = first_ge(s.f1_phase);  // phase: f < f1_phase inspiral
-  {
-    int n = first_ge(s.f3);  // amp: f > f3 ringdown
-    while ((double)n * df <= s.f3) n++;
-    x.n_f3 = n;
-  }
-  {
-    int n = first_ge(s.f2_phase);
-    while ((double)n * df <= s.f2_phase) n++;
-    x.n_f2p = n;
-  }
-  {
-    int n = first_ge(m.fcut);  // last n with n df <= fcut
-    while (n > 0 && (double)n * df > m.fcut) n--;
-    x.n_cut = n;
-  }
+  x.n_f1 = grid_first(s.f1, df, false);          // amp: f < f1 inspiral
+  x.n_f1p = grid_first(s.f1_phase, df, false);   // phase: f < f1_phase inspiral
+  x.n_f3 = grid_first(s.f3, df, true);           // amp: f > f3 ringdown
+  x.n_f2p = grid_first(s.f2_phase, df, true);
+  x.n_cut = grid_first(m.fcut, df, true) - 1;    // last n with n df <= fcut
   const bool pv2 = (r.approximant == kPhenomPv2);
   x.A_scale = m.A0eff * pow(Mdf, -7. / 6.) * (pv2 ? 0.5 : 1.0);
   const double cu = cbrt(Mdf);
@@ -247,32 +239,11 @@ GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x) {
   x.status = m.status;
   x.ndet = r.ndet;
   // region starts in n: first n with n*df >= boundary (strict "<" tests of build_amp/build_phase)
-  auto first_ge = [&](double fb) -> int {
-    double q = ceil(fb / df);
-    if (!(q < 2.0e9)) return 2000000000;
-    int n = (int)q;
-    if (n < 0) n = 0;
-    while (n > 0 && (double)(n - 1) * df >= fb) n--;
-    while ((double)n * df < fb) n++;
-    return n;
-  };
-  x.n_f1 = first_ge(s.f1);          // amp: f < f1 inspiral
-  x.n_f1p = first_ge(s.f1_phase);   // phase: f < f1_phase inspiral
-  {                                 // amp: f > f3 ringdown -> first n with n*df > f3
-    int n = first_ge(s.f3);
-    while ((double)n * df <= s.f3) n++;
-    x.n_f3 = n;
-  }
-  {
-    int n = first_ge(s.f2_phase);
-    while ((double)n * df <= s.f2_phase) n++;
-    x.n_f2p = n;
-  }
-  {  // last n with n*df <= fcut
-    int n = first_ge(m.fcut);
-    while ((double)n * df > m.fcut) n--;
-    x.n_cut = n;
-  }
+  x.n_f1 = grid_first(s.f1, df, false);          // amp: f < f1 inspiral
+  x.n_f1p = grid_first(s.f1_phase, df, false);   // phase: f < f1_phase inspiral
+  x.n_f3 = grid_first(s.f3, df, true);           // amp: f > f3 ringdown
+  x.n_f2p = grid_first(s.f2_phase, df, true);
+  x.n_cut = grid_first(m.fcut, df, true) - 1;    // last n with n df <= fcut
   const bool pv2 = (r.approximant == kPhenomPv2);
   // amplitude scale: A0eff * (M df)^(-7/6) [* 1/2 for the Pv2 amp/2]
   x.A_scale = m.A0eff * pow(Mdf, -7. / 6.) * (pv2 ? 0.5 : 1.0);
@@ -557,7 +528,7 @@ GW_HD void mixed_bin(const MixedReq &x, int n, double t, double r, double lnn, d
   float ph_ = fmaf(fmaf(x.w[2], xx, x.w[1]), xx, x.w[0]);
   float pl_ = fmaf(fmaf(x.w_lo[2], xx, x.w_lo[1]), xx, x.w_lo[0]);
   float us = sround(fmaf(ph_, rs, x.w[3]), fmaf(pl_, rs, x.w_lo[3]), dither(n) ^ 0x9e3779b9u);  // 1/s
-  float cb = us / sqrtf(fmaf(us, us, 1.0f));  // cos beta = 1/sqrt(1 + s^2)
+  float cb = fabsf(us) / sqrtf(fmaf(us, us, 1.0f));  // cos beta = 1/sqrt(1 + s^2) >= 0, also when L + SL < 0
   float cbh = sqrtf((1.0f + cb) * 0.5f), sbh = sqrtf(fmaxf(1.0f - cb, 0.0f) * 0.5f);
   float c2 = cbh * cbh, s2 = sbh * sbh;
   float d2[5] = {s2 * s2, 2.f * cbh * s2 * sbh, 2.44948974278317788f * s2 * c2, 2.f * c2 * cbh * sbh, c2 * c2};

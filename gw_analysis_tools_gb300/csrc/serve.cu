@@ -85,6 +85,24 @@ size_t request_bytes(int precision, int N, int tile) {  // device scratch held b
          items * (sizeof(double) * gwk::kAcc + sizeof(gwk::Item)) + sizeof(gwgpu_gen_params) + 64;
 }
 
+// Layout of a lane's pinned and device I/O buffers for n requests: every
+// array starts on a 256-byte boundary (the log L array is read and written as
+// doubles by the kernels).
+struct IoLayout {
+  size_t params, approx, handles, out, status, total;
+};
+IoLayout io_layout(int n) {
+  auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  IoLayout o;
+  o.params = 0;
+  o.approx = up(sizeof(gwgpu_gen_params) * (size_t)n);
+  o.handles = o.approx + up(sizeof(int) * (size_t)n);
+  o.out = o.handles + up(sizeof(int) * (size_t)n * gwt::kMaxDet);
+  o.status = o.out + up(sizeof(double) * (size_t)n);
+  o.total = o.status + up(sizeof(int) * (size_t)n);
+  return o;
+}
+
 int lane_io(gwgpu_context *c, ServeLane &l, size_t bytes) {
   if (l.cap >= bytes) return GWGPU_OK;
   if (l.h) cudaFreeHost(l.h);
@@ -98,24 +116,32 @@ int lane_io(gwgpu_context *c, ServeLane &l, size_t bytes) {
   return GWGPU_OK;
 }
 
-void retire(gwgpu_server *s, ServeLane &l) {
+// Complete the lane's requests: with its results when cuda_error is 0, else
+// every request fails with GWGPU_ECUDA.
+void retire(gwgpu_server *s, ServeLane &l, int cuda_error) {
   const int n = (int)l.ids.size();
-  size_t pb = sizeof(gwgpu_gen_params) * n, ab = sizeof(int) * n, hb = sizeof(int) * (size_t)n * gwt::kMaxDet;
-  const double *out = (const double *)(l.h + pb + ab + hb);
-  const int *st = (const int *)(l.h + pb + ab + hb + sizeof(double) * n);
+  const IoLayout io = io_layout(n);
+  const double *out = (const double *)(l.h + io.out);
+  const int *st = (const int *)(l.h + io.status);
   double t = now_s();
   {
     std::lock_guard<std::mutex> lk(s->mu);
     for (int j = 0; j < n; j++) {
       Slot &sl = s->slots[l.ids[j]];
-      sl.ll = out[j];
-      sl.status = st[j] ? (st[j] == 1 ? GWGPU_EINVAL : GWGPU_EDOMAIN) : GWGPU_OK;
+      if (cuda_error) {
+        sl.ll = NAN;
+        sl.status = GWGPU_ECUDA;
+      } else {
+        sl.ll = out[j];
+        sl.status = gwk::status_code(st[j]);
+      }
       sl.t_done = t;
       sl.state = kDone;
       s->latency.push_back(t - sl.t_submit);
       s->completed++;
     }
     s->inflight_bytes -= l.reserved;
+    if (cuda_error) s->worker_error = GWGPU_ECUDA;
   }
   l.reserved = 0;
   l.ids.clear();
@@ -127,27 +153,26 @@ int launch(gwgpu_server *s, ServeLane &l) {
   gwgpu_context *c = s->ctx;
   const int n = (int)l.ids.size();
   const int ndet = s->slots[l.ids[0]].ndet;
-  size_t pb = sizeof(gwgpu_gen_params) * n, ab = sizeof(int) * n, hb = sizeof(int) * (size_t)n * gwt::kMaxDet,
-         ob = sizeof(double) * n, sb = sizeof(int) * n;
+  const IoLayout io = io_layout(n);
   std::lock_guard<std::mutex> ck(c->mu);
-  int st = lane_io(c, l, pb + ab + hb + ob + sb + 256);
+  int st = lane_io(c, l, io.total);
   if (st) return st;
-  gwgpu_gen_params *hp = (gwgpu_gen_params *)l.h;
-  int *ha = (int *)(l.h + pb);
-  int *hh = (int *)(l.h + pb + ab);
+  gwgpu_gen_params *hp = (gwgpu_gen_params *)(l.h + io.params);
+  int *ha = (int *)(l.h + io.approx);
+  int *hh = (int *)(l.h + io.handles);
   for (int j = 0; j < n; j++) {
     const Slot &sl = s->slots[l.ids[j]];
     hp[j] = sl.p;
     ha[j] = sl.approx;
     for (int d = 0; d < ndet; d++) hh[j * ndet + d] = sl.handles[d];
   }
-  cudaMemcpyAsync(l.d, l.h, pb + ab, cudaMemcpyHostToDevice, l.L.stream);
-  double *dout = (double *)(l.d + pb + ab + hb);
-  int *dst = (int *)(l.d + pb + ab + hb + ob);
-  st = gwb::enqueue_batch(c, l.L, (const gwgpu_gen_params *)l.d, (const int *)(l.d + pb), n, hh, ndet,
-                          s->cfg.T_segment, s->cfg.precision, dout, dst, 0, false);
+  cudaMemcpyAsync(l.d, l.h, io.handles, cudaMemcpyHostToDevice, l.L.stream);  // params + approximants
+  double *dout = (double *)(l.d + io.out);
+  int *dst = (int *)(l.d + io.status);
+  st = gwb::enqueue_batch(c, l.L, (const gwgpu_gen_params *)(l.d + io.params), (const int *)(l.d + io.approx), n,
+                          hh, ndet, s->cfg.T_segment, s->cfg.precision, dout, dst, 0, false);
   if (st) return st;
-  cudaMemcpyAsync(l.h + pb + ab + hb, dout, ob + sb, cudaMemcpyDeviceToHost, l.L.stream);
+  cudaMemcpyAsync(l.h + io.out, dout, io.total - io.out, cudaMemcpyDeviceToHost, l.L.stream);
   cudaError_t e = cudaEventRecord(l.ev, l.L.stream);
   if (e != cudaSuccess) return c->fail(e, "serve launch");
   l.busy = true;
@@ -163,10 +188,11 @@ void worker_loop(gwgpu_server *s) {
       if (!l.busy) continue;
       cudaError_t q = cudaEventQuery(l.ev);
       if (q == cudaSuccess) {
-        retire(s, l);
+        retire(s, l, 0);
         did = true;
-      } else if (q != cudaErrorNotReady) {
-        s->worker_error = GWGPU_ECUDA;
+      } else if (q != cudaErrorNotReady) {  // fail this lane's requests instead of waiting on it forever
+        retire(s, l, 1);
+        did = true;
       }
     }
     for (auto &l : s->lanes) {
@@ -357,45 +383,45 @@ int gwgpu_server_drive(gwgpu_server *s, const gwgpu_gen_params *params, const in
                        int ndet, const double *arrival_s, int n, double *loglik, int *status, double *latency_s,
                        double *wall_s) {
   if (!s || !params || !approx || !handles || !arrival_s || n < 1 || !loglik) return GWGPU_EINVAL;
-  std::vector<uint64_t> tickets(n);
-  std::vector<double> t_arr(n);
+  for (int i = 0; i < n * ndet; i++)
+    if (!s->ctx->get_stream(handles[i])) return GWGPU_ENOTFOUND;
+  std::vector<uint64_t> tickets(n, 0);
   double t0 = now_s();
+  // no completion for this long means the device or the worker stopped: give up
+  const double stall_limit_s = 120.0;
+  double last_progress = t0;
   int next_collect = 0;
   auto drain = [&](bool block) {
-    while (next_collect < n && next_collect < (int)tickets.size()) {
-      if (tickets[next_collect] == 0) break;
+    while (next_collect < n && tickets[next_collect] != 0) {
       int st;
       double ll;
-      int rc = block ? gwgpu_server_wait(s, tickets[next_collect], 60000, &ll, &st)
+      int rc = block ? gwgpu_server_wait(s, tickets[next_collect], 1000, &ll, &st)
                      : gwgpu_server_poll(s, tickets[next_collect], &ll, &st);
-      if (rc == GWGPU_EBUSY) return;
-      if (rc != GWGPU_OK) {
-        loglik[next_collect] = NAN;
-        if (status) status[next_collect] = rc;
-      } else {
-        loglik[next_collect] = ll;
-        if (status) status[next_collect] = st;
-      }
+      if (rc == GWGPU_EBUSY || (block && rc == GWGPU_ETIMEDOUT)) return false;
+      loglik[next_collect] = rc == GWGPU_OK ? ll : NAN;
+      if (status) status[next_collect] = rc == GWGPU_OK ? st : rc;
       next_collect++;
+      last_progress = now_s();
     }
+    return true;
   };
-  std::fill(tickets.begin(), tickets.end(), 0);
   for (int i = 0; i < n; i++) {
     double ta = t0 + arrival_s[i];
     while (now_s() < ta) {
       if (ta - now_s() > 2e-4) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
-    t_arr[i] = ta;
     for (;;) {
       int rc = submit_at(s, params + i, approx[i], handles + (size_t)i * ndet, ndet, ta, &tickets[i]);
       if (rc == GWGPU_OK) break;
       if (rc != GWGPU_EBUSY) return rc;
       drain(false);  // free slots
+      if (now_s() - last_progress > stall_limit_s) return GWGPU_ETIMEDOUT;
       std::this_thread::yield();
     }
     if ((i & 63) == 0) drain(false);
   }
-  drain(true);
+  while (!drain(true))
+    if (now_s() - last_progress > stall_limit_s) return GWGPU_ETIMEDOUT;
   if (wall_s) *wall_s = now_s() - t0;
   if (latency_s) {
     std::lock_guard<std::mutex> lk(s->mu);

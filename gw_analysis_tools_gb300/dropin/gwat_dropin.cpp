@@ -1,0 +1,254 @@
+// gwat_dropin.cpp -- definitions of the reference-signature entry points
+// (include/gwat_dropin.h) on top of the C ABI (include/gwgpu.h).
+//
+// One process-wide engine context.  The process-global data arrays of the
+// sampler (mcmc_data / mcmc_noise / mcmc_frequencies, mcmc_gw.cpp:1464-1476)
+// are registered on the device the first time a (pointer, length, content
+// fingerprint) triple is seen and reused afterwards, as the reference treats
+// them as read-only during sampling.  Callers on several threads are safe:
+// the engine serialises them, or, in "served" mode, coalesces them into
+// batched launches.
+#include "../../include/gwat_dropin.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "../../include/gwgpu.h"
+
+namespace gwat_dropin {
+
+struct Engine {
+  gwgpu_context *ctx = nullptr;
+  gwgpu_server *srv = nullptr;
+  double srv_T = 0;
+  bool served = false;
+  std::mutex mu;
+  std::map<std::tuple<const void *, const void *, const void *, int, int, uint64_t>, int> handles;
+};
+
+static Engine &engine() {
+  static Engine e;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const char *dev = std::getenv("GWGPU_DROPIN_DEVICE");
+    gwgpu_context_create(dev ? std::atoi(dev) : 0, 0, &e.ctx);
+    const char *mode = std::getenv("GWGPU_DROPIN_MODE");
+    e.served = mode && std::strcmp(mode, "served") == 0;
+  });
+  return e;
+}
+
+void set_mode(const char *mode) { engine().served = mode && std::strcmp(mode, "served") == 0; }
+
+static uint64_t fingerprint(const double *a, int n) {
+  uint64_t h = 1469598103934665603ull;
+  int step = n > 64 ? n / 64 : 1;
+  for (int i = 0; i < n; i += step) {
+    uint64_t v;
+    std::memcpy(&v, a + i, 8);
+    h = (h ^ v) * 1099511628211ull;
+  }
+  return h;
+}
+
+static void to_abi(const gen_params_base<double> *p, gwgpu_gen_params *o) {
+  gwgpu_default_params(o);
+  o->mass1 = p->mass1;
+  o->mass2 = p->mass2;
+  for (int i = 0; i < 3; i++) {
+    o->spin1[i] = p->spin1[i];
+    o->spin2[i] = p->spin2[i];
+  }
+  o->Luminosity_Distance = p->Luminosity_Distance;
+  o->incl_angle = p->incl_angle;
+  o->phiRef = p->phiRef;
+  o->f_ref = p->f_ref;
+  o->tc = p->tc;
+  o->RA = p->RA;
+  o->DEC = p->DEC;
+  o->psi = p->psi;
+  o->gmst = p->gmst;
+  o->chip = p->chip;
+  o->phip = p->phip;
+  o->shift_time = p->shift_time;
+  o->shift_phase = p->shift_phase;
+  o->sky_average = p->sky_average;
+  o->dep_postmerger = p->dep_postmerger;
+}
+
+static int handle_for(Engine &e, const std::string &det, const double *f, const std::complex<double> *d,
+                      const double *psd, int n) {
+  uint64_t fp = fingerprint(f, n) ^ (fingerprint((const double *)d, 2 * n) * 31) ^ (fingerprint(psd, n) * 131);
+  auto key = std::make_tuple((const void *)f, (const void *)d, (const void *)psd, n, (int)det.size() * 131 + det[0],
+                             fp);
+  auto it = e.handles.find(key);
+  if (it != e.handles.end()) return it->second;
+  int h = -1;
+  if (gwgpu_data_register(e.ctx, det.c_str(), f, n, (const double *)d, psd, &h) != GWGPU_OK) return -1;
+  e.handles[key] = h;
+  return h;
+}
+
+}  // namespace gwat_dropin
+
+using namespace gwat_dropin;
+
+template <class T>
+int fourier_waveform(T *frequencies, int length, waveform_polarizations<T> *wp, std::string generation_method,
+                     gen_params_base<T> *parameters) {
+  gwgpu_gen_params p;
+  to_abi(parameters, &p);
+  return gwgpu_fourier_waveform(engine().ctx, frequencies, length, (double *)wp->hplus, (double *)wp->hcross,
+                                generation_method.c_str(), &p);
+}
+template int fourier_waveform<double>(double *, int, waveform_polarizations<double> *, std::string,
+                                      gen_params_base<double> *);
+
+int fourier_waveform(double *frequencies, int length, std::complex<double> *waveform_plus,
+                     std::complex<double> *waveform_cross, std::string generation_method, gen_params *parameters) {
+  gwgpu_gen_params p;
+  to_abi(parameters, &p);
+  return gwgpu_fourier_waveform(engine().ctx, frequencies, length, (double *)waveform_plus, (double *)waveform_cross,
+                                generation_method.c_str(), &p);
+}
+
+template <class T>
+int fourier_detector_response(T *frequencies, int length, std::complex<T> *response, std::string detector,
+                              std::string generation_method, gen_params_base<T> *parameters, T *times) {
+  (void)times;
+  gwgpu_gen_params p;
+  to_abi(parameters, &p);
+  return gwgpu_fourier_detector_response(engine().ctx, frequencies, length, (double *)response, detector.c_str(),
+                                         generation_method.c_str(), &p);
+}
+template int fourier_detector_response<double>(double *, int, std::complex<double> *, std::string, std::string,
+                                               gen_params_base<double> *, double *);
+
+double Log_Likelihood_internal(std::complex<double> *data, double *psd, double *frequencies, double *weights,
+                               std::complex<double> *detector_response, int length, bool log10F,
+                               std::string integration_method) {
+  (void)weights;
+  (void)log10F;
+  if (integration_method != "SIMPSONS") return NAN;
+  double out = NAN;
+  gwgpu_log_likelihood_internal(engine().ctx, (const double *)data, psd, frequencies,
+                                (const double *)detector_response, length, &out);
+  return out;
+}
+
+double MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double> *parameters,
+                                 std::string generation_method, int *data_length, double **frequencies,
+                                 std::complex<double> **data, double **psd, double **weights,
+                                 std::string integration_method, bool log10F, std::string *detectors,
+                                 int num_detectors) {
+  (void)weights;
+  (void)log10F;
+  if (!save_waveform || integration_method != "SIMPSONS" || num_detectors < 1 || num_detectors > 4) return NAN;
+  Engine &e = engine();
+  // mcmc_gw.cpp:2466 forms T from frequencies[1] - frequencies[0] of the
+  // double** array, i.e. the distance between the first two detectors'
+  // frequency arrays; the same expression is used here so that a caller with
+  // the same arrays gets the same log L.  With one detector that expression
+  // reads past the array in the reference; 1/df of the grid is used instead.
+  double T = num_detectors > 1 ? 1. / (double)(frequencies[1] - frequencies[0])
+                               : 1. / (frequencies[0][1] - frequencies[0][0]);
+  double tc_ref = T - parameters->tc;  // mcmc_gw.cpp:2467-2473: the caller's params are mutated
+  int hs[4];
+  {
+    std::lock_guard<std::mutex> lk(e.mu);
+    for (int i = 0; i < num_detectors; i++) {
+      hs[i] = handle_for(e, detectors[i], frequencies[i], data[i], psd[i], data_length[i]);
+      if (hs[i] < 0) return NAN;
+    }
+  }
+  gwgpu_gen_params p;
+  to_abi(parameters, &p);
+  parameters->tc = tc_ref;
+  double ll = NAN;
+  const char *m = generation_method.c_str();
+  int approx = generation_method.find("Pv2") != std::string::npos ? GWGPU_IMRPHENOMPV2 : GWGPU_IMRPHENOMD;
+  if (e.served) {
+    {
+      std::lock_guard<std::mutex> lk(e.mu);
+      if (!e.srv || e.srv_T != T) {
+        if (e.srv) gwgpu_server_destroy(e.srv);
+        gwgpu_server_config cfg = {16384, 1024, 4, GWGPU_PREC_MIXED, T, 0};
+        gwgpu_server_create(e.ctx, &cfg, &e.srv);
+        e.srv_T = T;
+      }
+    }
+    uint64_t t;
+    int st;
+    while ((st = gwgpu_server_submit(e.srv, &p, approx, hs, num_detectors, &t)) == GWGPU_EBUSY) {
+    }
+    if (st != GWGPU_OK) return NAN;
+    gwgpu_server_wait(e.srv, t, 600000, &ll, &st);
+    return ll;
+  }
+  gwgpu_mcmc_likelihood_extrinsic(e.ctx, &p, m, hs, num_detectors, T, &ll);
+  return ll;
+}
+
+void fisher_numerical(double *frequency, int length, std::string generation_method, std::string detector,
+                      std::string reference_detector, double **output, int dimension,
+                      gen_params_base<double> *parameters, int order, int *amp_tapes, int *phase_tapes,
+                      double *noise) {
+  (void)amp_tapes;
+  (void)phase_tapes;
+  gwgpu_gen_params p;
+  to_abi(parameters, &p);
+  std::vector<double> out((size_t)dimension * dimension, NAN);
+  if (noise)
+    gwgpu_fisher_numerical(engine().ctx, frequency, length, generation_method.c_str(), detector.c_str(),
+                           reference_detector.c_str(), out.data(), dimension, &p, order, noise);
+  for (int i = 0; i < dimension; i++)
+    for (int j = 0; j < dimension; j++) output[i][j] = out[(size_t)i * dimension + j];
+}
+
+// ---- C entry points for the test suite (ctypes cannot call the C++ symbols)
+extern "C" double gwat_dropin_test_loglik(const double *f, int N, const double *const *data,
+                                          const double *const *psd, const char *const *dets, int ndet,
+                                          const gwgpu_gen_params *pp, int served, double *tc_after) {
+  gen_params_base<double> g;
+  g.mass1 = pp->mass1;
+  g.mass2 = pp->mass2;
+  for (int i = 0; i < 3; i++) {
+    g.spin1[i] = pp->spin1[i];
+    g.spin2[i] = pp->spin2[i];
+  }
+  g.Luminosity_Distance = pp->Luminosity_Distance;
+  g.incl_angle = pp->incl_angle;
+  g.phiRef = pp->phiRef;
+  g.f_ref = pp->f_ref;
+  g.tc = pp->tc;
+  g.RA = pp->RA;
+  g.DEC = pp->DEC;
+  g.psi = pp->psi;
+  g.gmst = pp->gmst;
+  set_mode(served ? "served" : "plain");
+  std::vector<int> len(ndet, N);
+  std::vector<double *> fs(ndet), ps(ndet), ws(ndet, nullptr);
+  std::vector<std::complex<double> *> ds(ndet);
+  std::vector<std::string> dn(ndet);
+  // one copy of the grid per detector, laid out back to back in one block,
+  // so that frequencies[1] - frequencies[0] is N elements
+  std::vector<double> fblock((size_t)ndet * N);
+  for (int i = 0; i < ndet; i++) {
+    std::copy(f, f + N, fblock.begin() + (size_t)i * N);
+    fs[i] = fblock.data() + (size_t)i * N;
+    ps[i] = const_cast<double *>(psd[i]);
+    ds[i] = (std::complex<double> *)data[i];
+    dn[i] = dets[i];
+  }
+  double ll = MCMC_likelihood_extrinsic(true, &g, "IMRPhenomD", len.data(), fs.data(), ds.data(), ps.data(),
+                                        ws.data(), "SIMPSONS", false, dn.data(), ndet);
+  if (tc_after) tc_after[0] = g.tc;
+  if (tc_after) tc_after[1] = ndet > 1 ? 1. / (double)(fs[1] - fs[0]) : 1. / (f[1] - f[0]);
+  return ll;
+}

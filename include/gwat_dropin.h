@@ -1,0 +1,73 @@
+// gwat_dropin.h -- the reference's C++ entry points of the likelihood path,
+// same signatures, running on the GB300 engine (include/gwgpu.h).
+//
+// A maintainer links libgwat_dropin.so in place of the CPU definitions of
+// these functions.  The parameter and polarisation types here are the subset
+// of the reference's gen_params_base<T> (include/gwat/util.h:121-378) and
+// waveform_polarizations<T> (include/gwat/waveform_generator.h:12-32) that the
+// path reads; in the reference build the reference's own headers replace
+// this block and the definitions in gwat_dropin.cpp are compiled against them.
+#ifndef GWAT_DROPIN_H
+#define GWAT_DROPIN_H
+
+#include <complex>
+#include <string>
+
+#ifndef GWAT_DROPIN_USE_REFERENCE_HEADERS
+template <class T>
+class gen_params_base {
+ public:
+  T mass1 = 0, mass2 = 0;
+  T spin1[3] = {0, 0, 0}, spin2[3] = {0, 0, 0};
+  T Luminosity_Distance = 0;
+  T incl_angle = 0, phiRef = 0, f_ref = 0, tc = 0;
+  T RA = 0, DEC = 0, psi = 0;
+  double gmst = 0;
+  T chip = -1, phip = -1;
+  bool shift_time = true, shift_phase = true, sky_average = false, dep_postmerger = false;
+  bool equatorial_orientation = false, horizon_coord = false;
+};
+class gen_params : public gen_params_base<double> {};
+template <class T>
+struct waveform_polarizations {
+  std::complex<T> *hplus = nullptr, *hcross = nullptr;
+};
+#endif
+
+// fourier_waveform (waveform_generator.h:43-49, waveform_generator.cpp:104)
+template <class T>
+int fourier_waveform(T *frequencies, int length, waveform_polarizations<T> *wp, std::string generation_method,
+                     gen_params_base<T> *parameters);
+// fourier_waveform complex overload (waveform_generator.h:70-74)
+int fourier_waveform(double *frequencies, int length, std::complex<double> *waveform_plus,
+                     std::complex<double> *waveform_cross, std::string generation_method, gen_params *parameters);
+// fourier_detector_response (waveform_util.h:190-197, waveform_util.cpp:1070)
+template <class T>
+int fourier_detector_response(T *frequencies, int length, std::complex<T> *response, std::string detector,
+                              std::string generation_method, gen_params_base<T> *parameters, T *times = nullptr);
+// Log_Likelihood_internal (mcmc_gw.h:276, mcmc_gw.cpp:801); SIMPSONS only
+double Log_Likelihood_internal(std::complex<double> *data, double *psd, double *frequencies, double *weights,
+                               std::complex<double> *detector_response, int length, bool log10F,
+                               std::string integration_method);
+// MCMC_likelihood_extrinsic (mcmc_gw.h:473, mcmc_gw.cpp:2374); SIMPSONS only,
+// save_waveform = true (one waveform for every detector, waveform_util.cpp:153)
+double MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double> *parameters,
+                                 std::string generation_method, int *data_length, double **frequencies,
+                                 std::complex<double> **data, double **psd, double **weights,
+                                 std::string integration_method, bool log10F, std::string *detectors,
+                                 int num_detectors);
+// fisher_numerical (fisher.h:35-48, fisher.cpp:81): "IMRPhenomD" / "MCMC_IMRPhenomD"
+void fisher_numerical(double *frequency, int length, std::string generation_method, std::string detector,
+                      std::string reference_detector, double **output, int dimension,
+                      gen_params_base<double> *parameters, int order, int *amp_tapes = nullptr,
+                      int *phase_tapes = nullptr, double *noise = nullptr);
+
+// Engine behind the drop-in: GWGPU_DROPIN_DEVICE (default 0) and
+// GWGPU_DROPIN_MODE = "plain" (default: one FP64 request per launch) or
+// "served" (concurrent callers coalesced by the continuous-batching server,
+// mixed precision).
+namespace gwat_dropin {
+void set_mode(const char *mode);
+}
+
+#endif

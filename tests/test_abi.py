@@ -27,3 +27,20 @@ def test_status_strings():
     L = _native.load()
     assert L.gwgpu_status_string(0) == b"ok"
     assert b"budget" in L.gwgpu_status_string(3)
+
+
+def test_dropin_library_exports_reference_signatures():
+    """libgwat_dropin.so loads and defines the reference-signature C++ entry
+    points declared in include/gwat_dropin.h."""
+    import shutil
+    import subprocess
+    _native.build()
+    L = ctypes.CDLL(_native.DROPIN_LIB)
+    assert hasattr(L, "gwat_dropin_test_loglik")
+    if shutil.which("nm") is None:
+        return
+    out = subprocess.run(["nm", "-DC", "--defined-only", _native.DROPIN_LIB], capture_output=True, text=True).stdout
+    for name in ("MCMC_likelihood_extrinsic(bool, gen_params_base<double>*", "Log_Likelihood_internal(",
+                 "fourier_waveform(double*, int, std::complex<double>*", "fourier_waveform<double>(",
+                 "fourier_detector_response<double>(", "fisher_numerical(double*, int"):
+        assert name in out, name

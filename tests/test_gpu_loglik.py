@@ -167,3 +167,34 @@ def test_uneven_grids_one_launch(gpu_ctx, oracle):
     for T in durations:
         for h in hs[T]:
             gpu_ctx.release_data(h)
+
+
+@pytest.mark.parametrize("n", [1, 3, 77])
+def test_odd_batch_sizes(gpu_ctx, oracle, network, n):
+    """Odd request counts: the per-request outputs of the host-buffer entry
+    points sit on their own aligned arrays."""
+    nw = network
+    draws = W.prior_draws(n, 300 + n)
+    ref = oracle.loglik_batch([oracle.params_from_dict(d) for d in draws], nw["f"], nw["dets"], nw["data"],
+                              nw["psd"])
+    for prec, tol in ((G.PREC_MIXED, MIXED_TOL), (G.PREC_FP64, None)):
+        out, st = gpu_ctx.loglik_batch(G.params_array(draws), 0, nw["handles"], nw["T"], prec)
+        assert np.all(st == 0)
+        err = np.abs(out - ref)
+        assert np.all(err <= (tol if tol else FP64_RTOL * np.maximum(1.0, np.abs(ref))))
+    # the sampler's 11-dimensional parameters (mcmc_gw.cpp:2492-2568)
+    theta = []
+    for d in draws:
+        m1, m2 = d["mass1"], d["mass2"]
+        mc = (m1 * m2) ** 0.6 / (m1 + m2) ** 0.2
+        eta = m1 * m2 / (m1 + m2) ** 2
+        theta.append([d["RA"], np.sin(d["DEC"]), d["psi"], np.cos(d["incl_angle"]), d["phiRef"], d["tc"],
+                      np.log(d["Luminosity_Distance"]), np.log(mc), eta, d["spin1"][2], d["spin2"][2]])
+    theta = np.array(theta)
+    ref = np.array([oracle.loglik(oracle.mcmc_repack(t, 0, W.GMST), nw["f"], nw["dets"], nw["data"], nw["psd"])
+                    for t in theta])
+    for prec, tol in ((G.PREC_MIXED, MIXED_TOL), (G.PREC_FP64, None)):
+        out, st = gpu_ctx.mcmc_loglik_batch(theta, 0, W.GMST, nw["handles"], nw["T"], prec)
+        assert np.all(st == 0)
+        err = np.abs(out - ref)
+        assert np.all(err <= (tol if tol else FP64_RTOL * np.maximum(1.0, np.abs(ref))))

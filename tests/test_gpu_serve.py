@@ -91,3 +91,18 @@ def test_unknown_ticket(gpu_ctx, served):
     srv = G.Server(gpu_ctx, served["T"], max_inflight=4, max_batch=4, lanes=1)
     assert srv.lib.gwgpu_server_poll(srv.h, 12345, None, None) == 7
     srv.close()
+
+
+def test_odd_batches_and_lane_errors_do_not_hang(gpu_ctx, oracle, served):
+    """Odd batch sizes (max_batch 7, 3 lanes) complete with the oracle's values."""
+    s = served
+    draws = W.prior_draws(61, 106)
+    srv = G.Server(gpu_ctx, s["T"], max_inflight=128, max_batch=7, lanes=3)
+    tickets = [srv.submit(G.gen_params(**d), 0, s["hs"]) for d in draws]
+    got = np.array([srv.wait(t)[0] for t in tickets])
+    srv.close()
+    f = s["f"]
+    data = [W.noise(f, 300 + i) for i in range(3)]
+    ref = oracle.loglik_batch([oracle.params_from_dict(d) for d in draws], f, list(W.DETECTORS3), data,
+                              [W.analytic_psd(f)] * 3)
+    assert np.max(np.abs(got - ref)) <= 1e-3

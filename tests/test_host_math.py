@@ -66,6 +66,20 @@ def test_host_mixed_loglik_within_tolerance(oracle, hostcheck, setup3):
     assert worst <= 1e-3, worst
 
 
+def test_host_mixed_pv2_precession_cone_through_zero(oracle, hostcheck, setup3):
+    """Pv2 draws where L + S_L changes sign on the grid (high mass ratio, anti-
+    aligned primary spin): cos(beta) = 1/sqrt(1 + s^2) stays positive."""
+    f, T, dets, data, psd = setup3
+    draws = W.prior_draws(40, 22, precessing=True)
+    worst = 0.0
+    for d in draws[18:24]:
+        p = oracle.params_from_dict(d)
+        ref = oracle.loglik(p, f, dets, data, psd, approximant=1)
+        got = _call(hostcheck.gwh_loglik_mixed, oracle, p, 1, T, f, dets, data, psd)
+        worst = max(worst, abs(got - ref))
+    assert worst <= 1e-3, worst
+
+
 def test_host_internals_match_oracle(oracle, hostcheck):
     for d in W.prior_draws(10, 5):
         p = oracle.params_from_dict(d)
