@@ -216,9 +216,9 @@ GW_HD double lambda_elem(const Source &s, int i) {  // IMRPhenomD.cpp:855-870
   const double *pl = GWT_T(gwt_lambda_fit)[i];
   double spin_coeff = s.chi_pn - 1;
   double eta = s.eta;
+  const double sc2 = spin_coeff * spin_coeff, sc3 = sc2 * spin_coeff;
   return pl[0] + pl[1] * eta + (spin_coeff) * (pl[2] + pl[3] * eta + pl[4] * eta * eta) +
-         pow(spin_coeff, 2) * (pl[5] + pl[6] * eta + pl[7] * eta * eta) +
-         pow(spin_coeff, 3) * (pl[8] + pl[9] * eta + pl[10] * eta * eta);
+         sc2 * (pl[5] + pl[6] * eta + pl[7] * eta * eta) + sc3 * (pl[8] + pl[9] * eta + pl[10] * eta * eta);
 }
 GW_HD void precalc_powers_ins(double f, double M, Pows &p) {  // IMRPhenomD.cpp:877-893
   double Mf = M * f;
@@ -400,12 +400,13 @@ GW_HD double phase_int(double f, const Source &s, const Lambda &l) {  // IMRPhen
   return (1. / s.eta) * (l.beta[0] + l.beta[1] * (Mf) + l.beta[2] * log(Mf) - l.beta[3] / 3. * 1. / Mf3);
 }
 GW_HD double Dphase_int(double f, const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1597-1607
-  return (1. / s.eta) * (l.beta[1] * (s.M) + l.beta[2] / f + l.beta[3] * pow(s.M, -3.) * pow(f, -4.));
+  const double M3 = s.M * s.M * s.M, f2 = f * f;
+  return (1. / s.eta) * (l.beta[1] * (s.M) + l.beta[2] / f + l.beta[3] / M3 / (f2 * f2));
 }
 GW_HD double Dphase_mr(double f, const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1539-1554
-  double M = s.M, fdamp = s.fdamp, fRD = s.fRD;
-  return (l.alpha[4] / (fdamp * (1. + pow(f - l.alpha[5] * fRD, 2.) / pow(fdamp, 2.))) + l.alpha[2] / (pow(f, 2.) * M) +
-          M * (l.alpha[1] + l.alpha[3] / pow(f * M, 0.25))) /
+  double M = s.M, fdamp = s.fdamp, fRD = s.fRD, u = f - l.alpha[5] * fRD;
+  return (l.alpha[4] / (fdamp * (1. + (u * u) / (fdamp * fdamp))) + l.alpha[2] / ((f * f) * M) +
+          M * (l.alpha[1] + l.alpha[3] / sqrt(sqrt(f * M)))) /
          s.eta;
 }
 GW_HD double build_amp(double f, const ModelD &m, const Pows &p) {  // IMRPhenomD.cpp:747-796

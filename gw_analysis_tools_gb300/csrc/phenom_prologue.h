@@ -8,19 +8,24 @@
 
 namespace gwt {
 
+// (pi M)^(i/3) f^(i/3 - 1) = (pi M f)^(i/3) / f and M^((7+i)/3) f^((7+i)/3 - 1)
+// = (M f)^((7+i)/3) / f: one cube root each instead of a pow per term.
 GW_HD double Damp_ins(double f, const ModelD &m) {  // IMRPhenomD.cpp:1407-1419
   const double *pn = m.pn_amp;
   double pn_amp = 0, M = m.s.M;
-  for (int i = 0; i < 7; i++) pn_amp += pn[i] * pow(kPi * (M), i / 3.) * pow(f, i / 3. - 1.) * (i / 3.);
-  double nr_amp = 0;
-  for (int i = 0; i < 3; i++) nr_amp += (m.l.rho[i]) * pow(M, (7. + i) / 3.) * pow(f, (7. + i) / 3. - 1.) * (7. + i) / 3.;
+  const double x = cbrt(kPi * M * f), y = cbrt(M * f), inv_f = 1. / f;
+  double xi = 1.0;
+  for (int i = 0; i < 7; i++, xi *= x) pn_amp += pn[i] * xi * inv_f * (i / 3.);
+  double nr_amp = 0, yi = y * y;
+  yi = yi * yi * yi * y;  // y^7
+  for (int i = 0; i < 3; i++, yi *= y) nr_amp += (m.l.rho[i]) * yi * inv_f * (7. + i) / 3.;
   return pn_amp + nr_amp;
 }
 GW_HD double Damp_mr(double f, const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1514-1532
   double g1 = l.gamma[0], g2 = l.gamma[1], g3 = l.gamma[2], fdamp = s.fdamp, fRD = s.fRD, M = s.M;
-  return -((exp(((-f + fRD) * g2) / (fdamp * g3)) * g1 *
-            (pow_int(f - fRD, 2) * g2 + 2 * fdamp * (f - fRD) * g3 + pow_int(fdamp, 2) * g2 * pow(g3, 2))) /
-           (pow(pow_int(f - fRD, 2) + pow_int(fdamp, 2) * pow_int(g3, 2), 2) * M));
+  double d = f - fRD, den = d * d + fdamp * fdamp * g3 * g3;
+  return -((exp(((-f + fRD) * g2) / (fdamp * g3)) * g1 * (d * d * g2 + 2 * fdamp * d * g3 + fdamp * fdamp * g2 * g3 * g3)) /
+           (den * den * M));
 }
 GW_HD double Dphase_ins(double f, const Source &s, double *pn, const Lambda &l) {  // IMRPhenomD.cpp:1427-1460
   double M = s.M, eta = s.eta;
@@ -29,69 +34,96 @@ GW_HD double Dphase_ins(double f, const Source &s, double *pn, const Lambda &l) 
                           s.delta_mass * (-732985. / 2268 - 140 * eta / 9) * s.chi_a +
                           (-732985. / 2268 + 24260 * eta / 81 + 340 * eta * eta / 9) * s.chi_s);  // :1067-1081
   double d1 = (-6848. * (1. / f) / 63);
+  // powers of v = (pi M f)^(1/3) and w = (M f)^(1/3) by products
+  const double v = cbrt(kPi * M * f), w = cbrt(M * f), inv_f = 1. / f;
+  double vp[9];
+  vp[0] = 1.0;
+  for (int i = 1; i < 9; i++) vp[i] = vp[i - 1] * v;
+  const double vm5 = 1. / (vp[5]);  // (pi M f)^(-5/3)
   double pn_phase = 0;
-  for (int i = 0; i < 8; i++) pn_phase += pn[i] * pow(kPi * M * f, i / 3.);
-  double phase_TF2 = +3. / (128 * eta) * pow(kPi * M, -5. / 3.) * (-5. / 3.) * pow(f, -5. / 3 - 1.) * pn_phase;
+  for (int i = 0; i < 8; i++) pn_phase += pn[i] * vp[i];
+  double phase_TF2 = +3. / (128 * eta) * vm5 * (-5. / 3.) * inv_f * pn_phase;
   double pn_phase_deriv = 0;
-  for (int i = 0; i < 8; i++) pn_phase_deriv += pn[i] * pow(kPi * M, i / 3.) * (i / 3.) * pow(f, i / 3. - 1.);
-  pn_phase_deriv += d0 * pow(kPi * M * f, 5. / 3) + d1 * pow(kPi * M * f, 6. / 3);
-  phase_TF2 += pn_phase_deriv * (3. / (128 * eta) * pow(kPi * M * f, -5. / 3));
-  return phase_TF2 + (1. / eta) * (l.sigma[1] * M + l.sigma[2] * pow(M, 4. / 3.) * pow(f, 1. / 3) +
-                                   l.sigma[3] * pow(M, 5. / 3.) * pow(f, 2. / 3) + l.sigma[4] * pow(M, 2.) * f);
+  for (int i = 0; i < 8; i++) pn_phase_deriv += pn[i] * vp[i] * (i / 3.) * inv_f;
+  pn_phase_deriv += d0 * vp[5] + d1 * vp[6];
+  phase_TF2 += pn_phase_deriv * (3. / (128 * eta) * vm5);
+  return phase_TF2 + (1. / eta) * (l.sigma[1] * M + l.sigma[2] * M * w + l.sigma[3] * M * w * w + l.sigma[4] * M * M * f);
 }
+// Integer powers of the three matching frequencies and of M used by the
+// intermediate-amplitude coefficients (products instead of pow calls).
+struct DeltaPowers {
+  double f1[6], f2[6], f3[6], m[5], d12_2, d13_3, d23_2;
+  GW_HD DeltaPowers(double a, double b, double c, double M) {
+    f1[0] = f2[0] = f3[0] = m[0] = 1.0;
+    for (int k = 1; k < 6; k++) {
+      f1[k] = f1[k - 1] * a;
+      f2[k] = f2[k - 1] * b;
+      f3[k] = f3[k - 1] * c;
+    }
+    for (int k = 1; k < 5; k++) m[k] = m[k - 1] * M;
+    d12_2 = (a - b) * (a - b);
+    d13_3 = (a - c) * (a - c) * (a - c);
+    d23_2 = (b - c) * (b - c);
+  }
+};
 /* calculate_delta_parameter_0..4 (IMRPhenomD.cpp:1709-1785) */
 GW_HD double delta0(double f1, double f2, double f3, double v1, double v2, double v3, double dd1, double dd3, double M) {
+  const DeltaPowers P(f1, f2, f3, M);
   (void)M;
-  return (-(dd3 * pow(f1, 2) * pow(f1 - f2, 2) * f2 * (f1 - f3) * (f2 - f3) * f3) +
-          dd1 * f1 * (f1 - f2) * f2 * (f1 - f3) * pow(f2 - f3, 2) * pow(f3, 2) - 4 * pow(f1, 2) * pow(f2, 3) * pow(f3, 2) * v1 +
-          3 * f1 * pow(f2, 4) * pow(f3, 2) * v1 + 8 * pow(f1, 2) * pow(f2, 2) * pow(f3, 3) * v1 -
-          4 * f1 * pow(f2, 3) * pow(f3, 3) * v1 - pow(f2, 4) * pow(f3, 3) * v1 - 4 * pow(f1, 2) * f2 * pow(f3, 4) * v1 -
-          f1 * pow(f2, 2) * pow(f3, 4) * v1 + 2 * pow(f2, 3) * pow(f3, 4) * v1 + 2 * f1 * f2 * pow(f3, 5) * v1 -
-          pow(f2, 2) * pow(f3, 5) * v1 + pow(f1, 5) * pow(f3, 2) * v2 - 3 * pow(f1, 4) * pow(f3, 3) * v2 +
-          3 * pow(f1, 3) * pow(f3, 4) * v2 - pow(f1, 2) * pow(f3, 5) * v2 + pow(f1, 5) * pow(f2, 2) * v3 -
-          2 * pow(f1, 4) * pow(f2, 3) * v3 + pow(f1, 3) * pow(f2, 4) * v3 - 2 * pow(f1, 5) * f2 * f3 * v3 +
-          pow(f1, 4) * pow(f2, 2) * f3 * v3 + 4 * pow(f1, 3) * pow(f2, 3) * f3 * v3 - 3 * pow(f1, 2) * pow(f2, 4) * f3 * v3 +
-          4 * pow(f1, 4) * f2 * pow(f3, 2) * v3 - 8 * pow(f1, 3) * pow(f2, 2) * pow(f3, 2) * v3 +
-          4 * pow(f1, 2) * pow(f2, 3) * pow(f3, 2) * v3) /
-         (pow(f1 - f2, 2) * pow(f1 - f3, 3) * pow(f2 - f3, 2));
+  return (-(dd3 * P.f1[2] * P.d12_2 * f2 * (f1 - f3) * (f2 - f3) * f3) +
+          dd1 * f1 * (f1 - f2) * f2 * (f1 - f3) * P.d23_2 * P.f3[2] - 4 * P.f1[2] * P.f2[3] * P.f3[2] * v1 +
+          3 * f1 * P.f2[4] * P.f3[2] * v1 + 8 * P.f1[2] * P.f2[2] * P.f3[3] * v1 -
+          4 * f1 * P.f2[3] * P.f3[3] * v1 - P.f2[4] * P.f3[3] * v1 - 4 * P.f1[2] * f2 * P.f3[4] * v1 -
+          f1 * P.f2[2] * P.f3[4] * v1 + 2 * P.f2[3] * P.f3[4] * v1 + 2 * f1 * f2 * P.f3[5] * v1 -
+          P.f2[2] * P.f3[5] * v1 + P.f1[5] * P.f3[2] * v2 - 3 * P.f1[4] * P.f3[3] * v2 +
+          3 * P.f1[3] * P.f3[4] * v2 - P.f1[2] * P.f3[5] * v2 + P.f1[5] * P.f2[2] * v3 -
+          2 * P.f1[4] * P.f2[3] * v3 + P.f1[3] * P.f2[4] * v3 - 2 * P.f1[5] * f2 * f3 * v3 +
+          P.f1[4] * P.f2[2] * f3 * v3 + 4 * P.f1[3] * P.f2[3] * f3 * v3 - 3 * P.f1[2] * P.f2[4] * f3 * v3 +
+          4 * P.f1[4] * f2 * P.f3[2] * v3 - 8 * P.f1[3] * P.f2[2] * P.f3[2] * v3 +
+          4 * P.f1[2] * P.f2[3] * P.f3[2] * v3) /
+         (P.d12_2 * P.d13_3 * P.d23_2);
 }
 GW_HD double delta1(double f1, double f2, double f3, double v1, double v2, double v3, double dd1, double dd3, double M) {
-  return (dd3 * f1 * pow(f1 - f2, 2) * (f1 - f3) * (f2 - f3) * (2 * f2 * f3 + f1 * (f2 + f3)) +
-          f3 * (-(dd1 * (f1 - f2) * (f1 - f3) * pow(f2 - f3, 2) * (f2 * f3 + f1 * (2 * f2 + f3))) -
+  const DeltaPowers P(f1, f2, f3, M);
+  return (dd3 * f1 * P.d12_2 * (f1 - f3) * (f2 - f3) * (2 * f2 * f3 + f1 * (f2 + f3)) +
+          f3 * (-(dd1 * (f1 - f2) * (f1 - f3) * P.d23_2 * (f2 * f3 + f1 * (2 * f2 + f3))) -
                 2 * f1 *
-                    (pow(f3, 4) * (v1 - v2) +
-                     f1 * (2 * pow(f3, 3) * (-v1 + v2) - 4 * pow(f2, 3) * (v1 - v3) + 6 * pow(f2, 2) * f3 * (v1 - v3)) +
-                     3 * pow(f2, 4) * (v1 - v3) + pow(f1, 4) * (v2 - v3) + 4 * pow(f2, 3) * f3 * (-v1 + v3) +
-                     2 * pow(f1, 3) * f3 * (-v2 + v3)))) /
-         (pow(f1 - f2, 2) * pow(f1 - f3, 3) * pow(f2 - f3, 2) * M);
+                    (P.f3[4] * (v1 - v2) +
+                     f1 * (2 * P.f3[3] * (-v1 + v2) - 4 * P.f2[3] * (v1 - v3) + 6 * P.f2[2] * f3 * (v1 - v3)) +
+                     3 * P.f2[4] * (v1 - v3) + P.f1[4] * (v2 - v3) + 4 * P.f2[3] * f3 * (-v1 + v3) +
+                     2 * P.f1[3] * f3 * (-v2 + v3)))) /
+         (P.d12_2 * P.d13_3 * P.d23_2 * M);
 }
 GW_HD double delta2(double f1, double f2, double f3, double v1, double v2, double v3, double dd1, double dd3, double M) {
-  return (-(dd3 * pow(f1 - f2, 2) * (f1 - f3) * (f2 - f3) * (pow(f1, 2) + f2 * f3 + 2. * f1 * (f2 + f3))) +
-          dd1 * (f1 - f3) * pow(f2 - f3, 2) * (-(f2 * f3 * (2 * f2 + f3)) + pow(f1, 2) * (f2 + 2 * f3) + f1 * (-pow(f2, 2) + pow(f3, 2))) -
-          4 * pow(f1, 2) * pow(f2, 3) * v1 + 3 * f1 * pow(f2, 4) * v1 - 4 * f1 * pow(f2, 3) * f3 * v1 + 3 * pow(f2, 4) * f3 * v1 +
-          12 * pow(f1, 2) * f2 * pow(f3, 2) * v1 - 4 * pow(f2, 3) * pow(f3, 2) * v1 - 8 * pow(f1, 2) * pow(f3, 3) * v1 +
-          f1 * pow(f3, 4) * v1 + pow(f3, 5) * v1 + pow(f1, 5) * v2 + pow(f1, 4) * f3 * v2 - 8 * pow(f1, 3) * pow(f3, 2) * v2 +
-          8 * pow(f1, 2) * pow(f3, 3) * v2 - f1 * pow(f3, 4) * v2 - pow(f3, 5) * v2 - pow(f1, 5) * v3 +
-          4 * pow(f1, 2) * pow(f2, 3) * v3 - 3 * f1 * pow(f2, 4) * v3 - pow(f1, 4) * f3 * v3 + 4 * f1 * pow(f2, 3) * f3 * v3 -
-          3 * pow(f2, 4) * f3 * v3 + 8 * pow(f1, 3) * pow(f3, 2) * v3 - 12 * pow(f1, 2) * f2 * pow(f3, 2) * v3 +
-          4 * pow(f2, 3) * pow(f3, 2) * v3) /
-         (pow(f1 - f2, 2) * pow(f1 - f3, 3) * pow(f2 - f3, 2) * pow(M, 2));
+  const DeltaPowers P(f1, f2, f3, M);
+  return (-(dd3 * P.d12_2 * (f1 - f3) * (f2 - f3) * (P.f1[2] + f2 * f3 + 2. * f1 * (f2 + f3))) +
+          dd1 * (f1 - f3) * P.d23_2 * (-(f2 * f3 * (2 * f2 + f3)) + P.f1[2] * (f2 + 2 * f3) + f1 * (-P.f2[2] + P.f3[2])) -
+          4 * P.f1[2] * P.f2[3] * v1 + 3 * f1 * P.f2[4] * v1 - 4 * f1 * P.f2[3] * f3 * v1 + 3 * P.f2[4] * f3 * v1 +
+          12 * P.f1[2] * f2 * P.f3[2] * v1 - 4 * P.f2[3] * P.f3[2] * v1 - 8 * P.f1[2] * P.f3[3] * v1 +
+          f1 * P.f3[4] * v1 + P.f3[5] * v1 + P.f1[5] * v2 + P.f1[4] * f3 * v2 - 8 * P.f1[3] * P.f3[2] * v2 +
+          8 * P.f1[2] * P.f3[3] * v2 - f1 * P.f3[4] * v2 - P.f3[5] * v2 - P.f1[5] * v3 +
+          4 * P.f1[2] * P.f2[3] * v3 - 3 * f1 * P.f2[4] * v3 - P.f1[4] * f3 * v3 + 4 * f1 * P.f2[3] * f3 * v3 -
+          3 * P.f2[4] * f3 * v3 + 8 * P.f1[3] * P.f3[2] * v3 - 12 * P.f1[2] * f2 * P.f3[2] * v3 +
+          4 * P.f2[3] * P.f3[2] * v3) /
+         (P.d12_2 * P.d13_3 * P.d23_2 * P.m[2]);
 }
 GW_HD double delta3(double f1, double f2, double f3, double v1, double v2, double v3, double dd1, double dd3, double M) {
-  return (dd3 * pow(f1 - f2, 2) * (f1 - f3) * (f2 - f3) * (2 * f1 + f2 + f3) -
-          dd1 * (f1 - f2) * (f1 - f3) * pow(f2 - f3, 2) * (f1 + f2 + 2 * f3) +
-          2 * (pow(f3, 4) * (-v1 + v2) + 2 * pow(f1, 2) * pow(f2 - f3, 2) * (v1 - v3) + 2 * pow(f2, 2) * pow(f3, 2) * (v1 - v3) +
-               2 * pow(f1, 3) * f3 * (v2 - v3) + pow(f2, 4) * (-v1 + v3) + pow(f1, 4) * (-v2 + v3) +
-               2 * f1 * f3 * (pow(f3, 2) * (v1 - v2) + pow(f2, 2) * (v1 - v3) + 2 * f2 * f3 * (-v1 + v3)))) /
-         (pow(f1 - f2, 2) * pow(f1 - f3, 3) * pow(f2 - f3, 2) * pow(M, 3));
+  const DeltaPowers P(f1, f2, f3, M);
+  return (dd3 * P.d12_2 * (f1 - f3) * (f2 - f3) * (2 * f1 + f2 + f3) -
+          dd1 * (f1 - f2) * (f1 - f3) * P.d23_2 * (f1 + f2 + 2 * f3) +
+          2 * (P.f3[4] * (-v1 + v2) + 2 * P.f1[2] * P.d23_2 * (v1 - v3) + 2 * P.f2[2] * P.f3[2] * (v1 - v3) +
+               2 * P.f1[3] * f3 * (v2 - v3) + P.f2[4] * (-v1 + v3) + P.f1[4] * (-v2 + v3) +
+               2 * f1 * f3 * (P.f3[2] * (v1 - v2) + P.f2[2] * (v1 - v3) + 2 * f2 * f3 * (-v1 + v3)))) /
+         (P.d12_2 * P.d13_3 * P.d23_2 * P.m[3]);
 }
 GW_HD double delta4(double f1, double f2, double f3, double v1, double v2, double v3, double dd1, double dd3, double M) {
-  return (-(dd3 * pow(f1 - f2, 2) * (f1 - f3) * (f2 - f3)) + dd1 * (f1 - f2) * (f1 - f3) * pow(f2 - f3, 2) -
-          3 * f1 * pow(f2, 2) * v1 + 2 * pow(f2, 3) * v1 + 6 * f1 * f2 * f3 * v1 - 3 * pow(f2, 2) * f3 * v1 -
-          3 * f1 * pow(f3, 2) * v1 + pow(f3, 3) * v1 + pow(f1, 3) * v2 - 3 * pow(f1, 2) * f3 * v2 + 3 * f1 * pow(f3, 2) * v2 -
-          pow(f3, 3) * v2 - pow(f1, 3) * v3 + 3 * f1 * pow(f2, 2) * v3 - 2 * pow(f2, 3) * v3 + 3 * pow(f1, 2) * f3 * v3 -
-          6 * f1 * f2 * f3 * v3 + 3 * pow(f2, 2) * f3 * v3) /
-         (pow(f1 - f2, 2) * pow(f1 - f3, 3) * pow(f2 - f3, 2) * pow(M, 4));
+  const DeltaPowers P(f1, f2, f3, M);
+  return (-(dd3 * P.d12_2 * (f1 - f3) * (f2 - f3)) + dd1 * (f1 - f2) * (f1 - f3) * P.d23_2 -
+          3 * f1 * P.f2[2] * v1 + 2 * P.f2[3] * v1 + 6 * f1 * f2 * f3 * v1 - 3 * P.f2[2] * f3 * v1 -
+          3 * f1 * P.f3[2] * v1 + P.f3[3] * v1 + P.f1[3] * v2 - 3 * P.f1[2] * f3 * v2 + 3 * f1 * P.f3[2] * v2 -
+          P.f3[3] * v2 - P.f1[3] * v3 + 3 * f1 * P.f2[2] * v3 - 2 * P.f2[3] * v3 + 3 * P.f1[2] * f3 * v3 -
+          6 * f1 * f2 * f3 * v3 + 3 * P.f2[2] * f3 * v3) /
+         (P.d12_2 * P.d13_3 * P.d23_2 * P.m[4]);
 }
 
 GW_HDNI void d_connections(ModelD &m) {
