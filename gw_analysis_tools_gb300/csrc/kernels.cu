@@ -311,6 +311,8 @@ cudaError_t launch_mcmc_repack(const double *theta, int dim, int n, int approxim
 
 // ---------------------------------------------------------- batched kernels
 constexpr int kBatchBlock = 256;
+static_assert(kBatchBlock == kSegBins, "one block pass covers one phase segment");
+constexpr int kMaxSegs = 64;  // segments per chunk of an item (shared buffers)
 constexpr int kStatusBounds = 0x100;  // set by an item whose bins fall outside the tables; finalize reports 5
 
 // Two-level compensated reduction of NV FP32 values per thread:
@@ -349,7 +351,7 @@ __device__ __forceinline__ void block_sum_mixed(const float (&v)[NV], float *sm,
 }
 
 template <int NDET, int MIXED>
-__global__ void __launch_bounds__(kBatchBlock) k_batch(const BatchArgs a) {
+__global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
   constexpr int NV = MIXED ? NDET * kAccPerDet : 2 * NDET;
   __shared__ int s_item;
   __shared__ __align__(16) unsigned char s_req[MIXED ? sizeof(MixedReq) : sizeof(Request)];
@@ -357,6 +359,10 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch(const BatchArgs a) {
   __shared__ double s_res[NV];
   __shared__ float s_red[MIXED ? NV * kBatchBlock : 1];
   __shared__ double s_dsm[32 * (MIXED ? 1 : NV)];
+  // mixed form: segment node values and fitted phase / alpha polynomials
+  constexpr int kSegBuf = MIXED ? kMaxSegs : 1;
+  __shared__ double s_node[kSegBuf * kSegEval], s_node_a[kSegBuf * kSegEval];
+  __shared__ SegPoly s_poly[kSegBuf], s_poly_a[kSegBuf];
   const int tid = threadIdx.x;
   for (;;) {
     if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
@@ -394,19 +400,61 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch(const BatchArgs a) {
           if (tid == 0) atomicOr(a.status + I.req, kStatusBounds);
           kcut = I.k0;
         }
-        for (int k = I.k0 + tid; k < kcut; k += blockDim.x) {
-          const int n = n0 + k;
-          float dre[NDET], dim[NDET], w[NDET];
-#pragma unroll
-          for (int d = 0; d < NDET; d++) {
-            float2 v = __ldg(((const float2 *)dh[d]) + k);
-            dre[d] = v.x;
-            dim[d] = v.y;
-            w[d] = __ldg(wh[d] + k);
+        const bool pv2 = x.approximant == kPhenomPv2;
+        const gwt::Tables &tb = a.tables;
+        // chunks of up to kMaxSegs segments (one segment = one pass of the block over kSegBins bins)
+        for (int c0 = I.k0; c0 < kcut; c0 += kMaxSegs * kSegBins) {
+          const int nseg = min(kMaxSegs, (kcut - c0 + kSegBins - 1) / kSegBins);
+          // (A) FP64 phase (and alpha) at the nodes of every usable segment
+          for (int e = tid; e < nseg * kSegEval; e += blockDim.x) {
+            const int sg = e / kSegEval, j = e - sg * kSegEval, kseg = c0 + sg * kSegBins;
+            double vp = 0.0, va = 0.0;
+            const int n = seg_node_n(n0, kseg, j);
+            if (seg_usable(x, n0, N, kseg) && n <= tb.nmax) {
+              const double t = __ldg(tb.t13 + n), r = __ldg(tb.tm53 + n), lnn = __ldg(tb.tln + n);
+              vp = mixed_phase_full(x, n, t, r, lnn, __ldg(tb.t34 + n), true);
+              if (pv2) va = mixed_pv2_alpha(x, n, t, r, lnn);
+            }
+            s_node[e] = vp;
+            s_node_a[e] = va;
           }
-          mixed_bin<NDET>(x, n, __ldg(a.tables.t13 + n), __ldg(a.tables.tm53 + n), __ldg(a.tables.tln + n),
-                          __ldg(a.tables.t34 + n), __ldg(a.tables.t13f + n), __ldg(a.tables.tm76f + n), dre, dim, w,
-                          acc);
+          __syncthreads();
+          // (B) fits: one thread per (segment, function)
+          for (int e = tid; e < nseg * 2; e += blockDim.x) {
+            const int sg = e >> 1, fn = e & 1, kseg = c0 + sg * kSegBins;
+            SegPoly &P = fn ? s_poly_a[sg] : s_poly[sg];
+            bool ok = seg_usable(x, n0, N, kseg) && seg_node_n(n0, kseg, 8) <= tb.nmax;
+            if (ok && (fn == 0 || pv2)) ok = seg_fit((fn ? s_node_a : s_node) + sg * kSegEval, P) == 0;
+            P.direct = ok ? 0 : 1;
+          }
+          __syncthreads();
+          // (C) bins: the block covers one segment per pass
+          for (int sg = 0; sg < nseg; sg++) {
+            const int kseg = c0 + sg * kSegBins, k = kseg + tid;
+            const bool direct = s_poly[sg].direct | (pv2 ? s_poly_a[sg].direct : 0);
+            if (k < kcut) {
+              const int n = n0 + k;
+              uint64_t ph, al = 0;
+              if (!direct) {
+                const int m = tid - kSegHalf;
+                ph = seg_eval(s_poly[sg], m);
+                if (pv2) al = seg_eval(s_poly_a[sg], m);
+              } else {
+                mixed_phase_direct(x, n, __ldg(tb.t13 + n), __ldg(tb.tm53 + n), __ldg(tb.tln + n),
+                                   __ldg(tb.t34 + n), ph, al);
+              }
+              float dre[NDET], dim[NDET], w[NDET];
+#pragma unroll
+              for (int d = 0; d < NDET; d++) {
+                float2 v = __ldg(((const float2 *)dh[d]) + k);
+                dre[d] = v.x;
+                dim[d] = v.y;
+                w[d] = __ldg(wh[d] + k);
+              }
+              mixed_bin_q<NDET>(x, n, ph, al, __ldg(tb.t13f + n), __ldg(tb.tm76f + n), dre, dim, w, acc);
+            }
+          }
+          __syncthreads();  // the node and fit buffers are reused by the next chunk
         }
       }
       float v[NV];

@@ -14,6 +14,7 @@
 #pragma once
 
 #include "phenom_bins.h"
+#include "segment_basis.h"
 
 #if !defined(__CUDA_ARCH__)
 #include <cmath>
@@ -391,6 +392,7 @@ GW_HD float __int_as_float_h(int i) { return __int_as_float(i); }
 GW_HD int __float_as_int_h(float f) { return __float_as_int(f); }
 GW_HD void gw_sincospif(float x, float *s, float *c) { sincospif(x, s, c); }
 GW_HD int64_t gw_llrint(double x) { return __double2ll_rn(x); }
+GW_HD int gw_f2i_rn(float x) { return __float2int_rn(x); }
 #else
 inline float __int_as_float_h(int i) {
   float f;
@@ -409,6 +411,7 @@ GW_HD void gw_sincospif(float x, float *s, float *c) {
   *c = (float)std::cos(a);
 }
 GW_HD int64_t gw_llrint(double x) { return (int64_t)std::llrint(x); }
+GW_HD int gw_f2i_rn(float x) { return (int)std::lrintf(x); }
 #endif
 
 // Kahan-compensated FP32 accumulator: value = s - c.
@@ -424,7 +427,10 @@ GW_HD void kadd(KSum &k, float v) {
 constexpr int kAccPerDet = 5;  // D uses 3 (hh, zr, zi); Pv2 uses 5 (spp, scc, spc, zp, zc)
 
 // Phase of the D model at bin n (FP64, radians), without the linear terms.
-GW_HD double mixed_phase_d(const MixedReq &x, int n, double t, double r, double lnn, double t34) {
+// exact_atan: the ringdown atan term in FP64 (segment nodes) instead of FP32
+// (per-bin path, where its small coefficient keeps the FP32 error below 1e-7 rad).
+GW_HD double mixed_phase_d(const MixedReq &x, int n, double t, double r, double lnn, double t34,
+                           bool exact_atan = false) {
   if (n < x.n_f1p) {
     const double *q = x.qi;
     double p = q[11];
@@ -433,8 +439,13 @@ GW_HD double mixed_phase_d(const MixedReq &x, int n, double t, double r, double 
   }
   double nd = (double)n;
   if (n >= x.n_f2p) {
-    float y = ((float)(n - x.n_c) - x.ncfrac) * x.inv_nw;
-    double at = (double)atanf(y);
+    double at;
+    if (exact_atan) {
+      at = atan(((double)(n - x.n_c) - (double)x.ncfrac) * (double)x.inv_nw);
+    } else {
+      float y = ((float)(n - x.n_c) - x.ncfrac) * x.inv_nw;
+      at = (double)atanf(y);
+    }
     return x.mA + x.mB * nd - x.mC * (r * t * t) + x.mD * t34 + x.mE * at;
   }
   return x.pA + x.pB * nd + x.pC * lnn - x.pD * (r * r * t);
@@ -492,15 +503,112 @@ GW_HD void q64_sincospi(uint64_t q, float *s, float *c) {
   gw_sincospif((float)hi * 4.656612873077393e-10f, s, c);  // 2^-31 half-turns
 }
 
-// One bin of the mixed form, accumulated into acc[d * kAccPerDet + j].
+// FP64 phase of bin n (radians; Pv2: phase + 2 epsilon) and the Pv2 Euler
+// angle alpha, from the per-bin power tables t = n^(1/3), r = n^(-5/3),
+// lnn = ln n, t34 = n^(3/4).
+GW_HD double mixed_pv2_alpha(const MixedReq &x, int n, double t, double r, double lnn) {
+  double nd = (double)n;
+  return r * (x.ea[0] * t * t + x.ea[1] * nd + x.ea[2] * nd * t) + x.ea[3] + x.ea[4] * t + x.ea[5] * lnn;
+}
+GW_HD double mixed_pv2_eps(const MixedReq &x, int n, double t, double r, double lnn) {
+  double nd = (double)n;
+  return r * (x.ee[0] * t * t + x.ee[1] * nd + x.ee[2] * nd * t) + x.ee[3] + x.ee[4] * t + x.ee[5] * lnn;
+}
+GW_HD double mixed_phase_full(const MixedReq &x, int n, double t, double r, double lnn, double t34,
+                              bool exact_atan = false) {
+  double ph = mixed_phase_d(x, n, t, r, lnn, t34, exact_atan);
+  if (x.approximant == kPhenomPv2) ph += 2.0 * mixed_pv2_eps(x, n, t, r, lnn);
+  return ph;
+}
+
+// ----------------------------------------------------- segment polynomials
+// Over a segment of kSegBins consecutive bins the FP64 phase (and the Pv2
+// angle alpha) is replaced by its degree-8 interpolant in u = m / 128,
+// m = n - n_c, through nine FP64 node values.  The coefficients of m^0..m^4
+// are carried as exact fixed-point turns (uint64, modulo one turn: integer m
+// keeps every product exact), those of u^5..u^8 in FP32; per bin this costs
+// integer multiply-adds and four FP32 FMAs instead of the FP64 series.  Two
+// check points between the outermost node pairs bound the interpolation
+// error; a segment that fails them, straddles a phase region boundary or
+// leaves the grid is evaluated per bin in FP64.
+constexpr int kSegBins = 256, kSegHalf = 128;
+constexpr int kSegNodes = GWT_SEG_NODES, kSegEval = GWT_SEG_NODES + GWT_SEG_CHECKS;
+constexpr int kSegQ = 5;                     // m^0 .. m^4 in fixed point
+constexpr int kSegF = kSegNodes - kSegQ;     // u^5 .. u^8 in FP32
+constexpr double kSegTolRad = 1e-8;          // interpolation error allowed at the check points
+constexpr float kSegFScale = 268435456.0f;   // FP32 part in turns * 2^28 (|part| < 4 turns)
+
+struct SegPoly {
+  uint64_t q[kSegQ];  // coefficient of m^j, turns * 2^64
+  float f[kSegF];     // coefficient of u^(kSegQ + j), turns * 2^28
+  int direct;         // 1: per-bin FP64 phase in this segment
+  int pad;
+};
+
+GW_HD int seg_offset(int j) { return GWT_T(gwt_seg_offsets)[j]; }
+
+// Fit one segment from its node values v[0..kSegEval) (radians; v[4] is the
+// centre).  Returns 0 when the polynomial meets the tolerance.
+GW_HD int seg_fit(const double *v, SegPoly &p) {
+  const double inv2pi = 1.0 / (2.0 * 3.14159265358979323846);
+  double c[kSegNodes];
+  c[0] = 0.0;
+  for (int j = 1; j < kSegNodes; j++) {
+    double s = 0.0;
+    for (int k = 0; k < kSegNodes; k++) s += GWT_T(gwt_seg_vinv)[j][k] * (v[k] - v[4]);
+    c[j] = s;
+  }
+  // interpolation error at the check points (FP64 Horner in u)
+  for (int k = kSegNodes; k < kSegEval; k++) {
+    double u = seg_offset(k) * (1.0 / kSegHalf), y = c[kSegNodes - 1];
+    for (int j = kSegNodes - 2; j >= 0; j--) y = y * u + c[j];
+    if (!(fabs(y - (v[k] - v[4])) <= kSegTolRad)) return 1;
+  }
+  double bound = 0.0, sc = 1.0;
+  for (int j = 0; j < kSegQ; j++, sc *= (1.0 / kSegHalf)) p.q[j] = turns_q64((j == 0 ? v[4] : c[j] * sc) * inv2pi);
+  for (int j = 0; j < kSegF; j++) {
+    double cf = c[kSegQ + j] * inv2pi;
+    bound += fabs(cf);
+    p.f[j] = (float)(cf * kSegFScale);
+  }
+  return bound < 3.0 ? 0 : 1;
+}
+
+// Whether the segment of bins [kseg, kseg + kSegBins) of a grid of N bins
+// (n = n0 + k) can carry a polynomial: inside the grid, below the cut, and
+// not across a phase region boundary.
+GW_HD bool seg_usable(const MixedReq &x, int n0, int N, int kseg) {
+  if (kseg < 0 || kseg + kSegBins > N) return false;
+  const int nlo = n0 + kseg, nhi = nlo + kSegBins - 1;
+  if (nlo > x.n_cut) return false;
+  if (nlo < x.n_f1p && nhi >= x.n_f1p) return false;
+  if (nlo < x.n_f2p && nhi >= x.n_f2p) return false;
+  return true;
+}
+// Bin n of node j of the segment starting at kseg.
+GW_HD int seg_node_n(int n0, int kseg, int j) { return n0 + kseg + kSegHalf + seg_offset(j); }
+
+// Phase of bin m of a fitted segment, turns * 2^64.
+GW_HD uint64_t seg_eval(const SegPoly &p, int m) {
+  const uint64_t mm = (uint64_t)(int64_t)m;
+  uint64_t acc = p.q[kSegQ - 1];
+#pragma unroll
+  for (int j = kSegQ - 2; j >= 0; j--) acc = acc * mm + p.q[j];
+  const float u = (float)m * (1.0f / kSegHalf), u2 = u * u;
+  float r = fmaf(fmaf(fmaf(p.f[3], u, p.f[2]), u, p.f[1]), u, p.f[0]);
+  r *= u2 * u2 * u;
+  return acc + ((uint64_t)(int64_t)gw_f2i_rn(r) << 36);
+}
+
+// One bin of the mixed form, accumulated into acc[d * kAccPerDet + j], with
+// the phase ph (Pv2: phase + 2 epsilon) and the Pv2 angle al in turns * 2^64.
 // dre/dim/w: the detector streams at this bin.
 template <int NDET>
-GW_HD void mixed_bin(const MixedReq &x, int n, double t, double r, double lnn, double t34, float tf, float m76,
-                     const float *dre, const float *dim, const float *w, KSum *acc) {
+GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float tf, float m76, const float *dre,
+                       const float *dim, const float *w, KSum *acc) {
   if (n > x.n_cut) return;
   float a = mixed_amp(x, n, tf, m76);
   if (x.approximant != kPhenomPv2) {
-    uint64_t ph = phase_q64(mixed_phase_d(x, n, t, r, lnn, t34));
     float aa = a * a;
 #pragma unroll
     for (int d = 0; d < NDET; d++) {
@@ -514,13 +622,9 @@ GW_HD void mixed_bin(const MixedReq &x, int n, double t, double r, double lnn, d
     }
     return;
   }
-  // Pv2: phase + 2 eps, Euler alpha (FP64), twist-up (FP32)
-  double nd = (double)n, t2 = t * t, nt = nd * t;
-  double alpha = r * (x.ea[0] * t2 + x.ea[1] * nd + x.ea[2] * nt) + x.ea[3] + x.ea[4] * t + x.ea[5] * lnn;
-  double eps = r * (x.ee[0] * t2 + x.ee[1] * nd + x.ee[2] * nt) + x.ee[3] + x.ee[4] * t + x.ee[5] * lnn;
-  uint64_t ph = phase_q64(mixed_phase_d(x, n, t, r, lnn, t34) + 2.0 * eps);
+  // Pv2: twist-up (FP32) with alpha from its fixed-point turns
   float sa, ca;
-  q64_sincospi(phase_q64(alpha), &sa, &ca);
+  q64_sincospi(al, &sa, &ca);
   // WignerD from L2PN (IMRPhenomP.cpp:665-693, 1214-1220)
   float tf2 = tf * tf;
   float xx = fmaf(x.x2c, tf2, x.x2c_lo * tf2);
@@ -563,6 +667,13 @@ GW_HD void mixed_bin(const MixedReq &x, int n, double t, double r, double lnn, d
     kadd(acc[d * kAccPerDet + 3], qr * hpr + qi * hpi);  // Re(q conj(hpf))
     kadd(acc[d * kAccPerDet + 4], qr * hcr + qi * hci);  // Re(q conj(hcf))
   }
+}
+
+// The per-bin FP64 path: phase and alpha of bin n in fixed-point turns.
+GW_HD void mixed_phase_direct(const MixedReq &x, int n, double t, double r, double lnn, double t34, uint64_t &ph,
+                              uint64_t &al) {
+  ph = phase_q64(mixed_phase_full(x, n, t, r, lnn, t34));
+  al = x.approximant == kPhenomPv2 ? phase_q64(mixed_pv2_alpha(x, n, t, r, lnn)) : 0;
 }
 
 // log L of one request from its FP64 accumulated sums s[d * kAccPerDet + j].

@@ -27,6 +27,8 @@ static const double *qnm() {
   return g_qnm.data();
 }
 
+static long g_seg_poly = 0, g_seg_total = 0;
+
 extern "C" {
 
 int gwh_waveform(const double *freqs, int N, double *hp, double *hc, int approx, const GenParams *p) {
@@ -123,29 +125,68 @@ double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, cons
       wh[d][k] = (float)(W[k] / wscale[d]);
     }
   }
-  double sums[kMaxDet * kAccPerDet] = {0};
-  for (int k = 0; k < N; k++) {
-    int n = n0 + k;
+  auto tables = [](int n, double &t, double &rr, double &lnn, double &t34) {
     double xn = (double)n;
-    double t = std::cbrt(xn), rr = std::pow(xn, -5. / 3.), lnn = std::log(xn), t34 = std::pow(xn, 0.75);
-    float tf = (float)std::cbrt(xn), m76 = (float)std::pow(xn, -7. / 6.);
-    float dre[kMaxDet], dim[kMaxDet], w[kMaxDet];
-    for (int d = 0; d < ndet; d++) {
-      dre[d] = dh[d][2 * k];
-      dim[d] = dh[d][2 * k + 1];
-      w[d] = wh[d][k];
+    t = std::cbrt(xn), rr = std::pow(xn, -5. / 3.), lnn = std::log(xn), t34 = std::pow(xn, 0.75);
+  };
+  double sums[kMaxDet * kAccPerDet] = {0};
+  const bool pv2 = x.approximant == kPhenomPv2;
+  for (int kseg = 0; kseg < N; kseg += kSegBins) {
+    // the kernel's segment plan: polynomial phase where usable and within tolerance
+    SegPoly sp{}, sa{};
+    bool poly = seg_usable(x, n0, N, kseg);
+    if (poly) {
+      double vp[kSegEval], va[kSegEval];
+      for (int j = 0; j < kSegEval; j++) {
+        int n = seg_node_n(n0, kseg, j);
+        double t, rr, lnn, t34;
+        tables(n, t, rr, lnn, t34);
+        vp[j] = mixed_phase_full(x, n, t, rr, lnn, t34, true);
+        va[j] = pv2 ? mixed_pv2_alpha(x, n, t, rr, lnn) : 0.0;
+      }
+      poly = seg_fit(vp, sp) == 0 && (!pv2 || seg_fit(va, sa) == 0);
     }
-    KSum acc[kMaxDet * kAccPerDet];
-    for (auto &a : acc) a = KSum{0.f, 0.f};
-    switch (ndet) {
-      case 1: mixed_bin<1>(x, n, t, rr, lnn, t34, tf, m76, dre, dim, w, acc); break;
-      case 2: mixed_bin<2>(x, n, t, rr, lnn, t34, tf, m76, dre, dim, w, acc); break;
-      case 3: mixed_bin<3>(x, n, t, rr, lnn, t34, tf, m76, dre, dim, w, acc); break;
-      default: mixed_bin<4>(x, n, t, rr, lnn, t34, tf, m76, dre, dim, w, acc); break;
+    g_seg_poly += poly ? 1 : 0;
+    g_seg_total += 1;
+    for (int k = kseg; k < std::min(N, kseg + kSegBins); k++) {
+      int n = n0 + k;
+      double xn = (double)n;
+      float tf = (float)std::cbrt(xn), m76 = (float)std::pow(xn, -7. / 6.);
+      uint64_t ph, al;
+      if (poly) {
+        int m = k - kseg - kSegHalf;
+        ph = seg_eval(sp, m);
+        al = pv2 ? seg_eval(sa, m) : 0;
+      } else {
+        double t, rr, lnn, t34;
+        tables(n, t, rr, lnn, t34);
+        mixed_phase_direct(x, n, t, rr, lnn, t34, ph, al);
+      }
+      float dre[kMaxDet], dim[kMaxDet], w[kMaxDet];
+      for (int d = 0; d < ndet; d++) {
+        dre[d] = dh[d][2 * k];
+        dim[d] = dh[d][2 * k + 1];
+        w[d] = wh[d][k];
+      }
+      KSum acc[kMaxDet * kAccPerDet];
+      for (auto &a : acc) a = KSum{0.f, 0.f};
+      switch (ndet) {
+        case 1: mixed_bin_q<1>(x, n, ph, al, tf, m76, dre, dim, w, acc); break;
+        case 2: mixed_bin_q<2>(x, n, ph, al, tf, m76, dre, dim, w, acc); break;
+        case 3: mixed_bin_q<3>(x, n, ph, al, tf, m76, dre, dim, w, acc); break;
+        default: mixed_bin_q<4>(x, n, ph, al, tf, m76, dre, dim, w, acc); break;
+      }
+      for (int j = 0; j < kMaxDet * kAccPerDet; j++) sums[j] += (double)(acc[j].s - acc[j].c);
     }
-    for (int j = 0; j < kMaxDet * kAccPerDet; j++) sums[j] += (double)(acc[j].s - acc[j].c);
   }
   return mixed_finalize(x, sums, dscale.data(), wscale.data());
+}
+
+// Segments that used the polynomial phase / all segments, since the last reset.
+void gwh_segment_stats(long *poly, long *total, int reset) {
+  *poly = g_seg_poly;
+  *total = g_seg_total;
+  if (reset) g_seg_poly = g_seg_total = 0;
 }
 
 }  // extern "C"
