@@ -139,9 +139,9 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   if (timing) cudaEventRecord(c->t_ev[0], L.stream);
   cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(unsigned) * (size_t)(n + 32), L.stream);
   if (e != cudaSuccess) return c->fail(e, "batch counters");
-  e = gwk::launch_prologue((const gwt::GenParams *)d_params, d_approx, n, pl.handles, ndet, T_segment, 1,
-                           c->streams_dev, c->qnm_dev, mixed ? nullptr : (gwt::Request *)reqs,
-                           mixed ? (gwt::MixedReq *)reqs : nullptr, mixed, d_status, L.stream);
+  e = (c->prologue_serial ? gwk::launch_prologue_serial : gwk::launch_prologue)(
+      (const gwt::GenParams *)d_params, d_approx, n, pl.handles, ndet, T_segment, 1, c->streams_dev, c->qnm_dev,
+      mixed ? nullptr : (gwt::Request *)reqs, mixed ? (gwt::MixedReq *)reqs : nullptr, mixed, d_status, L.stream);
   if (e != cudaSuccess) return c->fail(e, "prologue launch");
   if (timing) cudaEventRecord(c->t_ev[1], L.stream);
   gwk::BatchArgs a;

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -226,6 +227,10 @@ int gwgpu_context_create(int device, size_t budget, gwgpu_context **out) {
   gwgpu_context *c = new gwgpu_context();
   c->device = device;
   c->budget = budget;
+  // GWGPU_PROLOGUE=serial: one thread per request for the batched prologue
+  // (the reference's order of operations) instead of the cooperative kernel
+  const char *pro = std::getenv("GWGPU_PROLOGUE");
+  c->prologue_serial = pro && std::strcmp(pro, "serial") == 0;
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;

@@ -49,6 +49,7 @@ struct gwgpu_context {
   std::map<std::string, int> tuned;  // autotuned tile per (precision, detectors, grid length)
   int tile_override = 0;
   bool use_graphs = true;
+  bool prologue_serial = false;    // batched prologue: one thread per request instead of the cooperative kernel
   uint64_t streams_epoch = 0;      // bumped when the device stream table changes
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   bool timing = false;                                   // per-kernel events on context-stream batches

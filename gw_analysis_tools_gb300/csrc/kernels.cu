@@ -251,9 +251,151 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
   if (st && req) req[i].m.status = st;
   status[i] = st;
 }
+// Cooperative prologue: the same constants as k_prologue, with each request's
+// independent parts spread over the four warps of its block.  An FP64
+// instruction occupies a sub-partition's FP64 pipe for the same time whatever
+// the number of active lanes, so one request per lane leaves the model's
+// FP64 chain as the latency; running its independent parts on four
+// sub-partitions at once shortens that chain.  Lane j of every warp works on
+// request blockIdx.x * kCoopReq + j; shared memory holds the requests between
+// stages.  Stage plan (W0..W3 = warps):
+//   S0  W0 parameters, source;  W3 detector projections
+//   S1  W0 calibration fits;  W1 D: ringdown frequencies / Pv2: J-frame transform;  W2 PN coefficients
+//   S2  W0 Pv2: ringdown frequencies; matching frequencies
+//   S3  W0/W1 amplitude matching points;  W2 phase connection;  W3 Pv2: Euler and frame constants
+//   S4  W0/W1 amplitude deltas;  W2 D: phase/time shift / Pv2: time-shift nodes 0-4;  W3 Pv2: nodes 5-9
+//   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions;  W3 Pv2: time shift and mixed angles
+//   S6  W0 detector phases, outputs
+constexpr int kCoopWarps = 4, kCoopReq = 16;
+__global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
+    const GenParams *__restrict__ params, const int *__restrict__ approx, int n, const int *__restrict__ handles,
+    int ndet, double T_segment, int tc_from_segment, const StreamDev *__restrict__ streams,
+    const double *__restrict__ qnm, Request *req, MixedReq *mreq, int want_mixed, int *status) {
+  __shared__ Request s_r[kCoopReq];
+  __shared__ GenParams s_p[kCoopReq];
+  __shared__ AmpConn s_ac[kCoopReq];
+  __shared__ double s_shift[kCoopReq][kPv2ShiftNodes];
+  __shared__ double s_df[kCoopReq];
+  __shared__ int s_st[kCoopReq], s_bad[kCoopReq], s_uni[kCoopReq];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kCoopReq + lane;
+  const bool act = lane < kCoopReq && i < n;
+  Request &r = s_r[lane < kCoopReq ? lane : 0];
+  const GenParams &p = s_p[lane < kCoopReq ? lane : 0];
+  // S0
+  if (act && warp == 0) {
+    GenParams q = params[i];
+    const int ap = approx[i];
+    const StreamDev &s0 = streams[handles[i * ndet]];
+    // mcmc_gw.cpp:2466-2473; T_segment <= 0 selects 1/df of this request's grid
+    if (tc_from_segment) q.tc = (T_segment > 0 ? T_segment : 1.0 / s0.df) - q.tc;
+    int st = 0;
+    for (int d = 0; d < ndet; d++)
+      if (streams[handles[i * ndet + d]].N != s0.N) st = 1;
+    const bool bad = !(q.mass1 > 0) || !(q.mass2 > 0) || !(q.Luminosity_Distance > 0) || (ap != 0 && ap != 1);
+    s_p[lane] = q;
+    s_st[lane] = st;
+    s_bad[lane] = bad;
+    s_df[lane] = s0.df;
+    s_uni[lane] = s0.uniform_int;
+    r.approximant = ap;
+    r.ndet = ndet;
+    if (!bad) populate(r.m.s, q);
+  }
+  if (act && warp == 3) {  // projections need only the sky position
+    const GenParams &q = params[i];
+    SkyTrig tr;
+    sky_trig(q.RA, q.DEC, q.psi, q.gmst, tr);
+    const int d0 = streams[handles[i * ndet]].det;
+    for (int d = 0; d < ndet && d < kMaxDet; d++) {
+      const int dd = streams[handles[i * ndet + d]].det;
+      antenna_trig(dd, tr, r.det[d].fp, r.det[d].fc);
+      r.det[d].tau = -dtoa_trig(tr, d0, dd) * (2 * kPi);
+    }
+  }
+  __syncthreads();
+  const bool run = act && !s_bad[lane < kCoopReq ? lane : 0];
+  const bool pv2 = run && r.approximant == kPhenomPv2;
+  // S1
+  if (run) {
+    if (warp == 0) model_d_lambdas(r.m);
+    if (warp == 1) {
+      if (pv2) model_p_setup(r.m, r.p, p);
+      else post_merger(r.m.s, qnm);
+    }
+    if (warp == 2) model_d_pn(r.m);
+  }
+  __syncthreads();
+  // S2
+  if (run && warp == 0) {
+    if (pv2) post_merger(r.m.s, qnm);
+    model_d_freqs(r.m);
+  }
+  __syncthreads();
+  // S3
+  if (run) {
+    if (warp == 0) d_amp_conn_low(r.m, s_ac[lane]);
+    if (warp == 1) d_amp_conn_high(r.m, s_ac[lane]);
+    if (warp == 2) d_phase_conn(r.m);
+    if (warp == 3 && pv2) model_p_finish(r.m, r.p);
+  }
+  __syncthreads();
+  // S4
+  if (run) {
+    if (warp == 0) d_deltas(r.m, s_ac[lane], 0, 3);
+    if (warp == 1) d_deltas(r.m, s_ac[lane], 3, 5);
+    if (!pv2) {
+      if (warp == 2) model_d_finish(r.m);
+    } else if (r.m.s.shift_time && (warp == 2 || warp == 3)) {
+      for (int j = (warp - 2) * (kPv2ShiftNodes / 2); j < (warp - 1) * (kPv2ShiftNodes / 2); j++)
+        s_shift[lane][j] = pv2_shift_node(r.m, j);
+    }
+  }
+  __syncthreads();
+  // S5
+  if (run) {
+    if (warp == 3 && pv2) r.p.t_corr = r.m.s.shift_time ? pv2_shift_solve(r.m, s_shift[lane]) : 0.0;
+    if (want_mixed) {
+      MixedReq &x = mreq[i];
+      const double df = s_df[lane];
+      if (warp == 0) mixed_amp_coeffs(r, df, x);
+      if (warp == 1) mixed_phase_coeffs(r, df, x);
+      if (warp == 2) mixed_regions(r, df, x);
+      if (warp == 3 && pv2) mixed_pv2_coeffs(r, df, x);
+    }
+  }
+  __syncthreads();
+  // S6
+  if (act && warp == 0) {
+    int st = s_st[lane];
+    if (!s_bad[lane]) {
+      if (r.m.status) st = 4;
+      if (req) req[i] = r;
+      if (want_mixed) {
+        if (!s_uni[lane]) st = st ? st : 1;
+        mixed_det_coeffs(r, s_df[lane], mreq[i]);
+      }
+    } else {
+      st = 4;
+      if (want_mixed) mreq[i] = MixedReq{};
+    }
+    if (st && want_mixed) mreq[i].status = st;
+    if (st && req) req[i].m.status = st;
+    status[i] = st;
+  }
+}
+
 cudaError_t launch_prologue(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
                             double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
                             Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s) {
+  int grid = (n + kCoopReq - 1) / kCoopReq;
+  k_prologue_coop<<<grid, kCoopWarps * 32, 0, s>>>(params, approx, n, handles, ndet, T_segment, tc_from_segment,
+                                                   streams, qnm, req, mreq, want_mixed, status);
+  return cudaGetLastError();
+}
+cudaError_t launch_prologue_serial(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
+                                   double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
+                                   Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s) {
   int block = 32, grid = (n + block - 1) / block;
   k_prologue<<<grid, block, 0, s>>>(params, approx, n, handles, ndet, T_segment, tc_from_segment, streams, qnm, req,
                                     mreq, want_mixed, status);

@@ -53,6 +53,11 @@ int plain_blocks(int N);
 cudaError_t launch_prologue(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
                             double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
                             Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s);
+// One thread per request (the reference order of the prologue); kept to check
+// the cooperative kernel against.
+cudaError_t launch_prologue_serial(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
+                            double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
+                            Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s);
 cudaError_t launch_mcmc_repack(const double *theta, int dim, int n, int approximant, double gmst, GenParams *out,
                                int *approx_out, cudaStream_t s);
 struct BatchArgs {

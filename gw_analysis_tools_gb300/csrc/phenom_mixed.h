@@ -232,10 +232,13 @@ GW_HD uint64_t turns_q64(double turns) {  // frac(turns) * 2^64
 
 // Build the mixed constants of one request for a grid with spacing df and
 // integer offset (f_n = n df).  Returns the status of the prologue.
-GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x) {
+// The mixed constants in parts (regions and scale, phase, amplitude, Pv2
+// angles, detectors) so that the cooperative prologue can spread them over
+// warps; mixed_prologue runs them in order.
+GW_HD void mixed_regions(const Request &r, double df, MixedReq &x) {
   const ModelD &m = r.m;
   const Source &s = m.s;
-  const double M = s.M, eta = s.eta, Mdf = M * df;
+  const double Mdf = s.M * df;
   x.approximant = r.approximant;
   x.status = m.status;
   x.ndet = r.ndet;
@@ -248,6 +251,14 @@ GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x) {
   const bool pv2 = (r.approximant == kPhenomPv2);
   // amplitude scale: A0eff * (M df)^(-7/6) [* 1/2 for the Pv2 amp/2]
   x.A_scale = m.A0eff * pow(Mdf, -7. / 6.) * (pv2 ? 0.5 : 1.0);
+}
+GW_HD void mixed_phase_coeffs(const Request &r, double df, MixedReq &x) {
+  const ModelD &m = r.m;
+  const Source &s = m.s;
+  const double M = s.M, eta = s.eta, Mdf = M * df;
+  (void)M;
+  (void)eta;
+  (void)Mdf;
   // ---------------- inspiral phase: u = (M f)^(1/3) = cu t, t = n^(1/3)
   const double cu = cbrt(Mdf);
   const double K = 3. / (128. * eta) * m.pi.PIminus_5third;
@@ -291,6 +302,12 @@ GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x) {
     x.ncfrac = (float)(nc - nci);
     x.inv_nw = (float)(df / s.fdamp);
   }
+}
+GW_HD void mixed_amp_coeffs(const Request &r, double df, MixedReq &x) {
+  const ModelD &m = r.m;
+  const Source &s = m.s;
+  const double M = s.M, Mdf = M * df;
+  const double cu = cbrt(Mdf);
   // ---------------- inspiral amplitude: sum_i pn_i (pi M f)^(i/3) + rho (Mf)^(7..9)/3
   {
     const double *pa = m.pn_amp;
@@ -336,8 +353,16 @@ GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x) {
     split_f(g2 / w, x.mrExp, x.mrExp_lo);
     split_f(w * w, x.mrG2, x.mrG2_lo);
   }
+}
+GW_HD void mixed_pv2_coeffs(const Request &r, double df, MixedReq &x) {
+  const ModelD &m = r.m;
+  const Source &s = m.s;
+  const double M = s.M, eta = s.eta, Mdf = M * df;
+  (void)M;
+  (void)eta;
+  (void)Mdf;
   // ---------------- Pv2 angles
-  if (pv2) {
+  {
     double cw = cbrt(kPi * Mdf);  // omega^(1/3) = cw t
     const double *a = r.p.ac, *e = r.p.ec;
     double Lw = log(kPi * Mdf);
@@ -364,6 +389,11 @@ GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x) {
     split_f(s.SL / s.SP, x.w[3], x.w_lo[3]);
     split_f(cw * cw, x.x2c, x.x2c_lo);  // L2PN x = (pi M f)^(2/3) = cw^2 t^2
   }
+}
+GW_HD void mixed_det_coeffs(const Request &r, double df, MixedReq &x) {
+  const ModelD &m = r.m;
+  const Source &s = m.s;
+  const bool pv2 = (r.approximant == kPhenomPv2);
   // ---------------- linear phase per detector, in turns (f = n df):
   // D:   psi_d = phi(f) - tcl (f - fref) - phic - tau_d f
   // Pv2: psi_d = phi(f) + 2 eps(f) - tcl (f - fref) - phic + 2 pi t_corr f - tau_d f
@@ -383,6 +413,13 @@ GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x) {
       x.det[d].Gim = -r.det[d].fc * ci;
     }
   }
+}
+GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x) {
+  mixed_regions(r, df, x);
+  mixed_phase_coeffs(r, df, x);
+  mixed_amp_coeffs(r, df, x);
+  if (r.approximant == kPhenomPv2) mixed_pv2_coeffs(r, df, x);
+  mixed_det_coeffs(r, df, x);
   return x.status;
 }
 

@@ -126,27 +126,41 @@ GW_HD double delta4(double f1, double f2, double f3, double v1, double v2, doubl
          (P.d12_2 * P.d13_3 * P.d23_2 * P.m[4]);
 }
 
-GW_HDNI void d_connections(ModelD &m) {
+// amp_connection_coeffs (IMRPhenomD.cpp:1679-1702), in three parts so that the
+// cooperative prologue can run them on different warps: the inspiral side
+// (v1, dd1 at f1), the ringdown side (v3, dd3 at f3), then the deltas.
+struct AmpConn {
+  double v1, v3, dd1, dd3;
+};
+GW_HD void d_amp_conn_low(const ModelD &m, AmpConn &a) {
+  Pows pw;
+  precalc_powers_ins(m.s.f1, m.s.M, pw);
+  a.v1 = amp_ins(m.s.f1, m, pw);
+  a.dd1 = Damp_ins(m.s.f1, m);
+}
+GW_HD void d_amp_conn_high(const ModelD &m, AmpConn &a) {
+  a.v3 = amp_mr(m.s.f3, m.s, m.l);
+  a.dd3 = Damp_mr(m.s.f3, m.s, m.l);
+}
+GW_HD void d_deltas(ModelD &m, const AmpConn &a, int j0, int j1) {
+  const Source &s = m.s;
+  const double M = s.M, f1 = s.f1, f3 = s.f3, f2 = (f1 + f3) / 2., v2 = m.l.v2;
+  for (int j = j0; j < j1; j++) {
+    double d;
+    switch (j) {
+      case 0: d = delta0(f1, f2, f3, a.v1, v2, a.v3, a.dd1, a.dd3, M); break;
+      case 1: d = delta1(f1, f2, f3, a.v1, v2, a.v3, a.dd1, a.dd3, M); break;
+      case 2: d = delta2(f1, f2, f3, a.v1, v2, a.v3, a.dd1, a.dd3, M); break;
+      case 3: d = delta3(f1, f2, f3, a.v1, v2, a.v3, a.dd1, a.dd3, M); break;
+      default: d = delta4(f1, f2, f3, a.v1, v2, a.v3, a.dd1, a.dd3, M); break;
+    }
+    m.deltas[j] = d;
+  }
+}
+// phase_connection_coefficients (IMRPhenomD.cpp:1614-1674)
+GW_HD void d_phase_conn(ModelD &m) {
   Source &s = m.s;
   Lambda &l = m.l;
-  // amp_connection_coeffs (IMRPhenomD.cpp:1679-1702)
-  {
-    double M = s.M, f1 = s.f1, f3 = s.f3;
-    Pows pw;
-    precalc_powers_ins(f1, M, pw);
-    double f2 = (f1 + f3) / 2.;
-    double v1 = amp_ins(f1, m, pw);
-    double v2 = l.v2;
-    double v3 = amp_mr(f3, s, l);
-    double dd1 = Damp_ins(f1, m);
-    double dd3 = Damp_mr(f3, s, l);
-    m.deltas[0] = delta0(f1, f2, f3, v1, v2, v3, dd1, dd3, M);
-    m.deltas[1] = delta1(f1, f2, f3, v1, v2, v3, dd1, dd3, M);
-    m.deltas[2] = delta2(f1, f2, f3, v1, v2, v3, dd1, dd3, M);
-    m.deltas[3] = delta3(f1, f2, f3, v1, v2, v3, dd1, dd3, M);
-    m.deltas[4] = delta4(f1, f2, f3, v1, v2, v3, dd1, dd3, M);
-  }
-  // phase_connection_coefficients (IMRPhenomD.cpp:1614-1674)
   l.beta[0] = 0;
   l.beta[1] = 0;
   l.alpha[0] = 0;
@@ -179,10 +193,19 @@ GW_HDNI void d_connections(ModelD &m) {
     l.alpha[0] = (eta)*intval - eta * mr;
   }
 }
+GW_HDNI void d_connections(ModelD &m) {
+  AmpConn a;
+  d_amp_conn_low(m, a);
+  d_amp_conn_high(m, a);
+  d_deltas(m, a, 0, 5);
+  d_phase_conn(m);
+}
 
-// Model setup shared by D and Pv2 (IMRPhenomD.cpp:410-432).
-GW_HDNI int model_d_prologue(ModelD &m, const double *qnm) {
-  Source &s = m.s;
+// Model setup shared by D and Pv2 (IMRPhenomD.cpp:410-432), in stages:
+// calibration fits, ringdown frequencies (post_merger), matching frequencies,
+// PN coefficients, connection coefficients.
+GW_HD void model_d_lambdas(ModelD &m) {
+  const Source &s = m.s;
   Lambda &l = m.l;
   for (int i = 0; i < 4; i++) l.rho[i] = 0, l.gamma[i] = 0;
   for (int i = 0; i < 5; i++) l.sigma[i] = 0, l.beta[i] = 0;
@@ -193,19 +216,30 @@ GW_HDNI int model_d_prologue(ModelD &m, const double *qnm) {
   for (int i = 0; i < 4; i++) l.sigma[i + 1] = lambda_elem(s, i + 7);
   for (int i = 0; i < 3; i++) l.beta[i + 1] = lambda_elem(s, i + 11);
   for (int i = 0; i < 5; i++) l.alpha[i + 1] = lambda_elem(s, i + 14);
-  post_merger(s, qnm);
+}
+// needs the fits and post_merger
+GW_HD void model_d_freqs(ModelD &m) {
+  Source &s = m.s;
   s.f1_phase = 0.018 / (s.M);
   s.f2_phase = s.fRD / 2.;
   s.f1 = 0.014 / (s.M);
-  s.f3 = fpeak(s, l);
+  s.f3 = fpeak(s, m.l);
   precalc_powers_PI(m.pi);
   for (int i = 0; i < 5; i++) m.deltas[i] = 0;
-  pn_amp_coeff(s, m.pn_amp);
-  pn_phase_coeff_static(s, m.pn_phase);
-  d_connections(m);
   m.fcut = .2 / s.M;
   m.status = kModelOK;
   if (!(s.eta > 0 && s.eta <= 0.25 + 1e-12) || !(s.fRD > 0) || !(s.fdamp > 0) || !(s.M > 0)) m.status |= kModelQnmRange;
+}
+GW_HD void model_d_pn(ModelD &m) {
+  pn_amp_coeff(m.s, m.pn_amp);
+  pn_phase_coeff_static(m.s, m.pn_phase);
+}
+GW_HDNI int model_d_prologue(ModelD &m, const double *qnm) {
+  model_d_lambdas(m);
+  post_merger(m.s, qnm);
+  model_d_freqs(m);
+  model_d_pn(m);
+  d_connections(m);
   return m.status;
 }
 
@@ -369,24 +403,36 @@ GW_HD void pv2_euler_angles(double &alpha, double &eps, double MFthird, double P
 }
 // calculate_time_shift (IMRPhenomP.cpp:551-606): d/df of a 10-node natural
 // spline of -phi(f) over [0.8, 1.2] fRD, at fRD, over 2 pi.
-GW_HDNI double pv2_time_shift(const ModelD &m) {
-  const Source &s = m.s;
-  double M = s.M, f_final = s.fRD;
-  double ff[10], ph[10], cc[10], work[60];
+// Node j of the spline: -phi(f_j), f_j = 0.8 fRD + j (0.4 fRD / 9).
+constexpr int kPv2ShiftNodes = 10;
+GW_HD double pv2_shift_freq(const ModelD &m, int j) {
+  double fs = .8 * (m.s.fRD), fe = 1.2 * (m.s.fRD);
+  return fs + j * ((fe - fs) / (kPv2ShiftNodes - 1));
+}
+GW_HD double pv2_shift_node(const ModelD &m, int j) {
   double pn[12];
   for (int i = 0; i < 12; i++) pn[i] = m.pn_phase[i];
-  double fs = .8 * (f_final), fe = 1.2 * (f_final);
-  double dfx = (fe - fs) / (10 - 1);
+  double f = pv2_shift_freq(m, j);
+  Pows pw;
+  precalc_powers_ins(f, m.s.M, pw);
+  return -build_phase(f, m, pn, pw);
+}
+GW_HD double pv2_shift_solve(const ModelD &m, const double *ph) {
+  double ff[kPv2ShiftNodes], cc[kPv2ShiftNodes], work[6 * kPv2ShiftNodes];
+  double fs = .8 * (m.s.fRD), fe = 1.2 * (m.s.fRD);
+  double dfx = (fe - fs) / (kPv2ShiftNodes - 1);
   if (dfx != dfx || dfx <= 0) return 0;
-  for (int j = 0; j < 10; j++) ff[j] = fs + j * dfx;
-  for (int j = 0; j < 10; j++) {
-    double f = ff[j];
-    Pows pw;
-    precalc_powers_ins(f, M, pw);
-    ph[j] = -build_phase(f, m, pn, pw);
-  }
-  cspline_coeffs(ff, ph, 10, cc, work);
-  return cspline_eval(ff, ph, cc, 10, f_final, 1) / (2. * kPi);
+  for (int j = 0; j < kPv2ShiftNodes; j++) ff[j] = pv2_shift_freq(m, j);
+  cspline_coeffs(ff, ph, kPv2ShiftNodes, cc, work);
+  return cspline_eval(ff, ph, cc, kPv2ShiftNodes, m.s.fRD, 1) / (2. * kPi);
+}
+GW_HDNI double pv2_time_shift(const ModelD &m) {
+  double fs = .8 * (m.s.fRD), fe = 1.2 * (m.s.fRD);
+  double dfx = (fe - fs) / (kPv2ShiftNodes - 1);
+  if (dfx != dfx || dfx <= 0) return 0;
+  double ph[kPv2ShiftNodes];
+  for (int j = 0; j < kPv2ShiftNodes; j++) ph[j] = pv2_shift_node(m, j);
+  return pv2_shift_solve(m, ph);
 }
 GW_HD double swsh_2m2(double theta, int m) {  // XLALSpinWeightedSphericalHarmonic s=-2 l=2 (util.cpp:1953-2333)
   switch (m) {
@@ -400,7 +446,10 @@ GW_HD double swsh_2m2(double theta, int m) {  // XLALSpinWeightedSphericalHarmon
 
 // Full Pv2 per-request setup: transform, D model, Euler/harmonic constants,
 // time shift (IMRPhenomP.cpp:195-262, 345-351; waveform_generator.cpp:1272-1281).
-GW_HDNI int model_p_prologue(ModelD &m, ModelP &pm, const GenParams &in, const double *qnm) {
+// Pv2 stages: the J-frame transform and harmonics (before the D model, whose
+// final spin uses chi_p), and the constants that need the D model's matching
+// frequencies (before the time shift, which needs its full phase).
+GW_HD void model_p_setup(ModelD &m, ModelP &pm, const GenParams &in) {
   Source &s = m.s;
   s.pv2 = 1;
   if ((in.chip + 1) > kCompThresh) {
@@ -413,7 +462,9 @@ GW_HDNI int model_p_prologue(ModelD &m, ModelP &pm, const GenParams &in, const d
     pv2_transform(s, 0);
   }
   for (int k = 0; k < 5; k++) pm.Y[k] = swsh_2m2(s.thetaJN, k - 2);
-  model_d_prologue(m, qnm);
+}
+GW_HDNI void model_p_finish(ModelD &m, ModelP &pm) {
+  Source &s = m.s;
   m.fref = s.f_ref;
   m.phic = 2 * s.phi_aligned;
   m.tcl = 2 * kPi * s.tc;
@@ -425,20 +476,32 @@ GW_HDNI int model_p_prologue(ModelD &m, ModelP &pm, const GenParams &in, const d
   pv2_euler_angles(aoff, eoff, MFthird, m.pi.PIthird, pm.ac, pm.ec);
   pm.alpha_shift = s.alpha0 - aoff;
   pm.eps_off = eoff;
-  pm.t_corr = s.shift_time ? pv2_time_shift(m) : 0.0;
   pm.c2z = cos(2. * s.zeta_polariz);
   pm.s2z = sin(2. * s.zeta_polariz);
   if (!(s.f_ref > 0)) m.status |= kModelBadInput;
+}
+GW_HDNI int model_p_prologue(ModelD &m, ModelP &pm, const GenParams &in, const double *qnm) {
+  model_p_setup(m, pm, in);
+  model_d_prologue(m, qnm);
+  model_p_finish(m, pm);
+  pm.t_corr = m.s.shift_time ? pv2_time_shift(m) : 0.0;
   return m.status;
 }
 
 // ------------------------------------------------------------- detectors
-GW_HD void antenna(int det, double ra, double dec, double psi, double gmst, double &fp, double &fc) {
+// Sky-position trigonometry shared by every detector of a request.
+struct SkyTrig {
+  double cg, sg, cd, sd, cp, sp;  // cos/sin of the hour angle gmst - RA, of DEC and of psi
+};
+GW_HD void sky_trig(double ra, double dec, double psi, double gmst, SkyTrig &t) {
+  double gha = gmst - ra;
+  t.cg = cos(gha), t.sg = sin(gha), t.cd = cos(dec), t.sd = sin(dec), t.cp = cos(psi), t.sp = sin(psi);
+}
+GW_HD void antenna_trig(int det, const SkyTrig &t, double &fp, double &fc) {
   // detector_util.cpp:901-1015, geometric factor detector_util.cpp:1158-1160
   const double *D = GWT_T(gwt_det_tensor)[det];
   double X[3], Y[3];
-  double gha = gmst - ra;
-  double cg = cos(gha), sg = sin(gha), cd = cos(dec), sd = sin(dec), cp = cos(psi), sp = sin(psi);
+  const double cg = t.cg, sg = t.sg, cd = t.cd, sd = t.sd, cp = t.cp, sp = t.sp;
   X[0] = -cp * sg - sp * cg * sd;
   X[1] = -cp * cg + sp * sg * sd;
   X[2] = sp * cd;
@@ -456,11 +519,20 @@ GW_HD void antenna(int det, double ra, double dec, double psi, double gmst, doub
   fp *= GWT_T(gwt_det_geometric)[det];
   fc *= GWT_T(gwt_det_geometric)[det];
 }
-GW_HD double dtoa(double RA, double DEC, double gmst, int d1, int d2) {  // detector_util.cpp:760-780
+GW_HD void antenna(int det, double ra, double dec, double psi, double gmst, double &fp, double &fc) {
+  SkyTrig t;
+  sky_trig(ra, dec, psi, gmst, t);
+  antenna_trig(det, t, fp, fc);
+}
+GW_HD double dtoa_trig(const SkyTrig &t, int d1, int d2) {  // detector_util.cpp:760-780
   const double *l1 = GWT_T(gwt_det_location)[d1], *l2 = GWT_T(gwt_det_location)[d2];
-  double hour_angle = gmst - RA;
-  double e0 = cos(DEC) * cos(hour_angle), e1 = cos(DEC) * -sin(hour_angle), e2 = sin(DEC);
+  double e0 = t.cd * t.cg, e1 = t.cd * -t.sg, e2 = t.sd;
   return ((l1[0] - l2[0]) * e0 + (l1[1] - l2[1]) * e1 + (l1[2] - l2[2]) * e2) / kC;
+}
+GW_HD double dtoa(double RA, double DEC, double gmst, int d1, int d2) {
+  SkyTrig t;
+  sky_trig(RA, DEC, 0.0, gmst, t);
+  return dtoa_trig(t, d1, d2);
 }
 
 // Everything one likelihood request needs.
@@ -486,9 +558,11 @@ GW_HDNI int request_prologue(Request &r, const GenParams &in, int approximant, c
     model_d_finish(r.m);
     st = r.m.status;
   }
+  SkyTrig tr;
+  sky_trig(in.RA, in.DEC, in.psi, in.gmst, tr);
   for (int i = 0; i < ndet && i < kMaxDet; i++) {
-    antenna(dets[i], in.RA, in.DEC, in.psi, in.gmst, r.det[i].fp, r.det[i].fc);
-    double DTOA = dtoa(in.RA, in.DEC, in.gmst, dets[0], dets[i]);
+    antenna_trig(dets[i], tr, r.det[i].fp, r.det[i].fc);
+    double DTOA = dtoa_trig(tr, dets[0], dets[i]);
     double tc = -DTOA;
     tc *= 2 * kPi;
     r.det[i].tau = tc;

@@ -198,3 +198,28 @@ def test_odd_batch_sizes(gpu_ctx, oracle, network, n):
         assert np.all(st == 0)
         err = np.abs(out - ref)
         assert np.all(err <= (tol if tol else FP64_RTOL * np.maximum(1.0, np.abs(ref))))
+
+
+def test_cooperative_prologue_matches_serial(gpu_ctx, network):
+    """The batched prologue spread over four warps gives the constants of the
+    one-thread-per-request prologue (GWGPU_PROLOGUE=serial)."""
+    import os
+    n = network
+    dd = W.prior_draws(48, 401)
+    dp = W.prior_draws(48, 402, precessing=True)
+    draws = [x for pair in zip(dd, dp) for x in pair]
+    aps = [0, 1] * 48
+    os.environ["GWGPU_PROLOGUE"] = "serial"
+    try:
+        ser = G.Context(0)
+    finally:
+        del os.environ["GWGPU_PROLOGUE"]
+    try:
+        hs = [ser.register_data(d, n["f"], n["data"][i], n["psd"][i]) for i, d in enumerate(n["dets"])]
+        for prec, tol in ((G.PREC_FP64, 1e-11), (G.PREC_MIXED, 1e-6)):
+            a, sa = gpu_ctx.loglik_batch(G.params_array(draws), aps, n["handles"], n["T"], prec)
+            b, sb = ser.loglik_batch(G.params_array(draws), aps, hs, n["T"], prec)
+            assert np.array_equal(sa, sb)
+            assert np.max(np.abs(a - b) / np.maximum(1.0, np.abs(b))) <= tol
+    finally:
+        ser.close()
