@@ -454,7 +454,7 @@ cudaError_t launch_mcmc_repack(const double *theta, int dim, int n, int approxim
 // ---------------------------------------------------------- batched kernels
 constexpr int kBatchBlock = 256;
 static_assert(kBatchBlock == kSegBins, "one block pass covers one phase segment");
-constexpr int kMaxSegs = 64;  // segments per chunk of an item (shared buffers)
+constexpr int kMaxSegs = 32;  // segments per chunk of an item (shared buffers)
 constexpr int kStatusBounds = 0x100;  // set by an item whose bins fall outside the tables; finalize reports 5
 
 // Two-level compensated reduction of NV FP32 values per thread:
@@ -505,6 +505,7 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
   constexpr int kSegBuf = MIXED ? kMaxSegs : 1;
   __shared__ double s_node[kSegBuf * kSegEval], s_node_a[kSegBuf * kSegEval];
   __shared__ SegPoly s_poly[kSegBuf], s_poly_a[kSegBuf];
+  __shared__ double s_coef[kSegBuf * 2 * kSegNodes];
   const int tid = threadIdx.x;
   for (;;) {
     if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
@@ -547,6 +548,7 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
         // chunks of up to kMaxSegs segments (one segment = one pass of the block over kSegBins bins)
         for (int c0 = I.k0; c0 < kcut; c0 += kMaxSegs * kSegBins) {
           const int nseg = min(kMaxSegs, (kcut - c0 + kSegBins - 1) / kSegBins);
+          const int nfn = pv2 ? 2 : 1;  // phase, and alpha for Pv2
           // (A) FP64 phase (and alpha) at the nodes of every usable segment
           for (int e = tid; e < nseg * kSegEval; e += blockDim.x) {
             const int sg = e / kSegEval, j = e - sg * kSegEval, kseg = c0 + sg * kSegBins;
@@ -554,20 +556,35 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
             const int n = seg_node_n(n0, kseg, j);
             if (seg_usable(x, n0, N, kseg) && n <= tb.nmax) {
               const double t = __ldg(tb.t13 + n), r = __ldg(tb.tm53 + n), lnn = __ldg(tb.tln + n);
-              vp = mixed_phase_full(x, n, t, r, lnn, __ldg(tb.t34 + n), true);
+              vp = mixed_phase_full(x, n, t, r, lnn, __ldg(tb.t34 + n), false);
               if (pv2) va = mixed_pv2_alpha(x, n, t, r, lnn);
             }
             s_node[e] = vp;
             s_node_a[e] = va;
           }
           __syncthreads();
-          // (B) fits: one thread per (segment, function)
+          // (B1) polynomial coefficients, one thread per (segment, function, coefficient)
+          for (int e = tid; e < nseg * nfn * kSegNodes; e += blockDim.x) {
+            const int j = e % kSegNodes, q = e / kSegNodes, sg = q / nfn, fn = q - sg * nfn;
+            s_coef[(sg * 2 + fn) * kSegNodes + j] = seg_coef((fn ? s_node_a : s_node) + sg * kSegEval, j);
+          }
+          __syncthreads();
+          // (B2) acceptance per (segment, function)
           for (int e = tid; e < nseg * 2; e += blockDim.x) {
             const int sg = e >> 1, fn = e & 1, kseg = c0 + sg * kSegBins;
             SegPoly &P = fn ? s_poly_a[sg] : s_poly[sg];
             bool ok = seg_usable(x, n0, N, kseg) && seg_node_n(n0, kseg, 8) <= tb.nmax;
-            if (ok && (fn == 0 || pv2)) ok = seg_fit((fn ? s_node_a : s_node) + sg * kSegEval, P) == 0;
+            if (ok && (fn == 0 || pv2))
+              ok = seg_check((fn ? s_node_a : s_node) + sg * kSegEval, s_coef + (sg * 2 + fn) * kSegNodes) == 0;
             P.direct = ok ? 0 : 1;
+          }
+          __syncthreads();
+          // (B3) stored coefficients of the accepted segments
+          for (int e = tid; e < nseg * nfn * kSegNodes; e += blockDim.x) {
+            const int j = e % kSegNodes, q = e / kSegNodes, sg = q / nfn, fn = q - sg * nfn;
+            SegPoly &P = fn ? s_poly_a[sg] : s_poly[sg];
+            if (!P.direct)
+              seg_store((fn ? s_node_a : s_node) + sg * kSegEval, s_coef + (sg * 2 + fn) * kSegNodes, j, P);
           }
           __syncthreads();
           // (C) bins: the block covers one segment per pass
@@ -579,7 +596,7 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
               uint64_t ph, al = 0;
               if (!direct) {
                 const int m = tid - kSegHalf;
-                ph = seg_eval(s_poly[sg], m);
+                ph = seg_eval(s_poly[sg], m, n0 + kseg >= x.n_f2p ? seg_atan_extra(x, n) : 0.0f);
                 if (pv2) al = seg_eval(s_poly_a[sg], m);
               } else {
                 mixed_phase_direct(x, n, __ldg(tb.t13 + n), __ldg(tb.tm53 + n), __ldg(tb.tln + n),

@@ -464,10 +464,14 @@ GW_HD void kadd(KSum &k, float v) {
 constexpr int kAccPerDet = 5;  // D uses 3 (hh, zr, zi); Pv2 uses 5 (spp, scc, spc, zp, zc)
 
 // Phase of the D model at bin n (FP64, radians), without the linear terms.
-// exact_atan: the ringdown atan term in FP64 (segment nodes) instead of FP32
-// (per-bin path, where its small coefficient keeps the FP32 error below 1e-7 rad).
+// with_atan: include the ringdown atan term, evaluated in FP32 (its
+// coefficient is about 1 rad, so the FP32 error stays near 1e-7 rad); the
+// segment nodes leave it out and the bins add it in FP32.
+GW_HD float mixed_atan(const MixedReq &x, int n) {
+  return atanf(((float)(n - x.n_c) - x.ncfrac) * x.inv_nw);
+}
 GW_HD double mixed_phase_d(const MixedReq &x, int n, double t, double r, double lnn, double t34,
-                           bool exact_atan = false) {
+                           bool with_atan = true) {
   if (n < x.n_f1p) {
     const double *q = x.qi;
     double p = q[11];
@@ -476,14 +480,8 @@ GW_HD double mixed_phase_d(const MixedReq &x, int n, double t, double r, double 
   }
   double nd = (double)n;
   if (n >= x.n_f2p) {
-    double at;
-    if (exact_atan) {
-      at = atan(((double)(n - x.n_c) - (double)x.ncfrac) * (double)x.inv_nw);
-    } else {
-      float y = ((float)(n - x.n_c) - x.ncfrac) * x.inv_nw;
-      at = (double)atanf(y);
-    }
-    return x.mA + x.mB * nd - x.mC * (r * t * t) + x.mD * t34 + x.mE * at;
+    double ph = x.mA + x.mB * nd - x.mC * (r * t * t) + x.mD * t34;
+    return with_atan ? ph + x.mE * (double)mixed_atan(x, n) : ph;
   }
   return x.pA + x.pB * nd + x.pC * lnn - x.pD * (r * r * t);
 }
@@ -552,8 +550,8 @@ GW_HD double mixed_pv2_eps(const MixedReq &x, int n, double t, double r, double 
   return r * (x.ee[0] * t * t + x.ee[1] * nd + x.ee[2] * nd * t) + x.ee[3] + x.ee[4] * t + x.ee[5] * lnn;
 }
 GW_HD double mixed_phase_full(const MixedReq &x, int n, double t, double r, double lnn, double t34,
-                              bool exact_atan = false) {
-  double ph = mixed_phase_d(x, n, t, r, lnn, t34, exact_atan);
+                              bool with_atan = true) {
+  double ph = mixed_phase_d(x, n, t, r, lnn, t34, with_atan);
   if (x.approximant == kPhenomPv2) ph += 2.0 * mixed_pv2_eps(x, n, t, r, lnn);
   return ph;
 }
@@ -566,14 +564,17 @@ GW_HD double mixed_phase_full(const MixedReq &x, int n, double t, double r, doub
 // keeps every product exact), those of u^5..u^8 in FP32; per bin this costs
 // integer multiply-adds and four FP32 FMAs instead of the FP64 series.  Two
 // check points between the outermost node pairs bound the interpolation
-// error; a segment that fails them, straddles a phase region boundary or
-// leaves the grid is evaluated per bin in FP64.
+// error; a segment that fails them, whose FP32 part is not small enough to
+// keep FP32 rounding near 1e-9 rad, that straddles a phase region boundary or
+// leaves the grid is evaluated per bin in FP64.  The ringdown atan term is
+// not part of the nodes; the bins add it in FP32 (mixed_atan).
 constexpr int kSegBins = 256, kSegHalf = 128;
 constexpr int kSegNodes = GWT_SEG_NODES, kSegEval = GWT_SEG_NODES + GWT_SEG_CHECKS;
 constexpr int kSegQ = 5;                     // m^0 .. m^4 in fixed point
 constexpr int kSegF = kSegNodes - kSegQ;     // u^5 .. u^8 in FP32
 constexpr double kSegTolRad = 1e-8;          // interpolation error allowed at the check points
-constexpr float kSegFScale = 268435456.0f;   // FP32 part in turns * 2^28 (|part| < 4 turns)
+constexpr double kSegFMaxTurns = 0.02;       // bound on the FP32 part (sum of |coefficients|)
+constexpr float kSegFScale = 268435456.0f;   // FP32 part in turns * 2^28
 
 struct SegPoly {
   uint64_t q[kSegQ];  // coefficient of m^j, turns * 2^64
@@ -584,31 +585,44 @@ struct SegPoly {
 
 GW_HD int seg_offset(int j) { return GWT_T(gwt_seg_offsets)[j]; }
 
-// Fit one segment from its node values v[0..kSegEval) (radians; v[4] is the
-// centre).  Returns 0 when the polynomial meets the tolerance.
-GW_HD int seg_fit(const double *v, SegPoly &p) {
-  const double inv2pi = 1.0 / (2.0 * 3.14159265358979323846);
-  double c[kSegNodes];
-  c[0] = 0.0;
-  for (int j = 1; j < kSegNodes; j++) {
-    double s = 0.0;
-    for (int k = 0; k < kSegNodes; k++) s += GWT_T(gwt_seg_vinv)[j][k] * (v[k] - v[4]);
-    c[j] = s;
-  }
-  // interpolation error at the check points (FP64 Horner in u)
+// The fit in three steps, each parallel over (segment, coefficient) or
+// segments in the kernel: (1) coefficient j >= 1 of u^j (radians) from the
+// node values v[0..kSegEval) (v[4] is the centre; coefficient 0 is v[4]);
+GW_HD double seg_coef(const double *v, int j) {
+  if (j == 0) return 0.0;
+  double s = 0.0;
+  for (int k = 0; k < kSegNodes; k++) s += GWT_T(gwt_seg_vinv)[j][k] * (v[k] - v[4]);
+  return s;
+}
+// (2) the acceptance test (check points, size of the FP32 part): 0 when usable;
+GW_HD int seg_check(const double *v, const double *c) {
   for (int k = kSegNodes; k < kSegEval; k++) {
     double u = seg_offset(k) * (1.0 / kSegHalf), y = c[kSegNodes - 1];
     for (int j = kSegNodes - 2; j >= 0; j--) y = y * u + c[j];
     if (!(fabs(y - (v[k] - v[4])) <= kSegTolRad)) return 1;
   }
-  double bound = 0.0, sc = 1.0;
-  for (int j = 0; j < kSegQ; j++, sc *= (1.0 / kSegHalf)) p.q[j] = turns_q64((j == 0 ? v[4] : c[j] * sc) * inv2pi);
-  for (int j = 0; j < kSegF; j++) {
-    double cf = c[kSegQ + j] * inv2pi;
-    bound += fabs(cf);
-    p.f[j] = (float)(cf * kSegFScale);
+  double bound = 0.0;
+  for (int j = kSegQ; j < kSegNodes; j++) bound += fabs(c[j]);
+  return bound * (1.0 / (2.0 * 3.14159265358979323846)) < kSegFMaxTurns ? 0 : 1;
+}
+// (3) coefficient j in its stored form.
+GW_HD void seg_store(const double *v, const double *c, int j, SegPoly &p) {
+  const double inv2pi = 1.0 / (2.0 * 3.14159265358979323846);
+  if (j < kSegQ) {
+    double sc = 1.0;
+    for (int i = 0; i < j; i++) sc *= (1.0 / kSegHalf);
+    p.q[j] = turns_q64((j == 0 ? v[4] : c[j] * sc) * inv2pi);
+  } else {
+    p.f[j - kSegQ] = (float)(c[j] * inv2pi * kSegFScale);
   }
-  return bound < 3.0 ? 0 : 1;
+}
+// Whole fit of one segment (host use); returns 0 when usable.
+GW_HD int seg_fit(const double *v, SegPoly &p) {
+  double c[kSegNodes];
+  for (int j = 0; j < kSegNodes; j++) c[j] = seg_coef(v, j);
+  if (seg_check(v, c)) return 1;
+  for (int j = 0; j < kSegNodes; j++) seg_store(v, c, j, p);
+  return 0;
 }
 
 // Whether the segment of bins [kseg, kseg + kSegBins) of a grid of N bins
@@ -625,16 +639,21 @@ GW_HD bool seg_usable(const MixedReq &x, int n0, int N, int kseg) {
 // Bin n of node j of the segment starting at kseg.
 GW_HD int seg_node_n(int n0, int kseg, int j) { return n0 + kseg + kSegHalf + seg_offset(j); }
 
-// Phase of bin m of a fitted segment, turns * 2^64.
-GW_HD uint64_t seg_eval(const SegPoly &p, int m) {
+// Phase of bin m of a fitted segment, turns * 2^64; extra (turns * 2^28) is
+// added to the FP32 part before its conversion.
+GW_HD uint64_t seg_eval(const SegPoly &p, int m, float extra = 0.0f) {
   const uint64_t mm = (uint64_t)(int64_t)m;
   uint64_t acc = p.q[kSegQ - 1];
 #pragma unroll
   for (int j = kSegQ - 2; j >= 0; j--) acc = acc * mm + p.q[j];
   const float u = (float)m * (1.0f / kSegHalf), u2 = u * u;
   float r = fmaf(fmaf(fmaf(p.f[3], u, p.f[2]), u, p.f[1]), u, p.f[0]);
-  r *= u2 * u2 * u;
+  r = fmaf(r, u2 * u2 * u, extra);
   return acc + ((uint64_t)(int64_t)gw_f2i_rn(r) << 36);
+}
+// The FP32 ringdown atan term of bin n in the units of seg_eval's extra.
+GW_HD float seg_atan_extra(const MixedReq &x, int n) {
+  return (float)(x.mE * (1.0 / (2.0 * 3.14159265358979323846)) * kSegFScale) * mixed_atan(x, n);
 }
 
 // One bin of the mixed form, accumulated into acc[d * kAccPerDet + j], with

@@ -141,7 +141,7 @@ double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, cons
         int n = seg_node_n(n0, kseg, j);
         double t, rr, lnn, t34;
         tables(n, t, rr, lnn, t34);
-        vp[j] = mixed_phase_full(x, n, t, rr, lnn, t34, true);
+        vp[j] = mixed_phase_full(x, n, t, rr, lnn, t34, false);
         va[j] = pv2 ? mixed_pv2_alpha(x, n, t, rr, lnn) : 0.0;
       }
       poly = seg_fit(vp, sp) == 0 && (!pv2 || seg_fit(va, sa) == 0);
@@ -155,7 +155,7 @@ double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, cons
       uint64_t ph, al;
       if (poly) {
         int m = k - kseg - kSegHalf;
-        ph = seg_eval(sp, m);
+        ph = seg_eval(sp, m, n0 + kseg >= x.n_f2p ? seg_atan_extra(x, n) : 0.0f);
         al = pv2 ? seg_eval(sa, m) : 0;
       } else {
         double t, rr, lnn, t34;
