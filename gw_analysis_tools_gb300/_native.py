@@ -15,7 +15,7 @@ BUILDDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libgwgpu.so")
 DROPIN_SRC = os.path.join(HERE, "dropin", "gwat_dropin.cpp")
 DROPIN_LIB = os.path.join(LIBDIR, "libgwat_dropin.so")
-SOURCES = ["kernels.cu", "capi.cu", "batch.cu", "fisher.cu", "serve.cu"]
+SOURCES = ["kernels.cu", "capi.cu", "batch.cu", "fisher.cu", "serve.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
 
@@ -129,6 +129,8 @@ def _declare(L):
         "gwgpu_batch_last_timing": (c_int, [c_void_p, P(ctypes.c_float), P(ctypes.c_float)]),
         "gwgpu_batch_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_int, ip, c_int, c_double, c_int, c_void_p,
                                          c_void_p, ip, P(ctypes.c_float)]),
+        "gwgpu_mcmc_likelihood_extrinsic_noalloc": (c_int, [c_void_p, c_void_p, c_char_p, ip, c_int, c_double,
+                                                            c_void_p, c_void_p]),
     }
     for name, (res, args) in list(sig.items()) + list(optional.items()):
         fn = getattr(L, name, None)

@@ -195,6 +195,14 @@ __global__ void __launch_bounds__(128) k_plain(const __grid_constant__ Request r
     }
   }
 }
+cudaError_t plain_preload() {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, k_plain<1>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_plain<2>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_plain<3>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_plain<4>);
+  return e;
+}
 int plain_blocks(int N) {
   int g = (N + 127) / 128;
   return g < 1 ? 1 : g;

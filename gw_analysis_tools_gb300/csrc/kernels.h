@@ -48,6 +48,7 @@ cudaError_t launch_inner_product(const double *data, const double *psd, const do
 cudaError_t launch_plain(const Request &r, const StreamDev *streams, int ndet, double *partials, unsigned *counter,
                          double *out, int *status, cudaStream_t s);
 int plain_blocks(int N);
+cudaError_t plain_preload();  // loads the plain kernels' module (function-attribute query)
 
 // Batched: prologue (one thread per request) then the fused bin kernel.
 cudaError_t launch_prologue(const GenParams *params, const int *approx, int n, const int *handles, int ndet,

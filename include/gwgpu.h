@@ -111,6 +111,22 @@ int gwgpu_mcmc_likelihood_extrinsic(gwgpu_context *ctx, const gwgpu_gen_params *
                                     const char *generation_method, const int *handles, int num_detectors,
                                     double T_segment, double *loglik);
 
+/* No counterpart in the reference.  The same plain FP64 likelihood for callers
+ * that may not allocate memory while it runs (inside CUDA stream capture, or
+ * under a fixed memory budget): it allocates nothing, enqueues one launch on
+ * `stream` (0: the legacy default stream) and writes log L to the device
+ * pointer d_loglik without synchronising.  Its scratch is one fixed device
+ * array sized for grids of up to 524,288 bins (4,096 blocks of 128 bins);
+ * longer grids return GWGPU_ETOOLARGE.  The first call on a device sets up
+ * that array (cudaGetSymbolAddress, module load), so make one call before any
+ * stream capture that later calls belong to.  Calls share the array:
+ * overlapping calls (several host threads, or work in flight on several
+ * streams) race, so issue them in order on one stream.  A request outside the
+ * model domain returns GWGPU_EDOMAIN without a launch. */
+int gwgpu_mcmc_likelihood_extrinsic_noalloc(gwgpu_context *ctx, const gwgpu_gen_params *params,
+                                            const char *generation_method, const int *handles,
+                                            int num_detectors, double T_segment, double *d_loglik, void *stream);
+
 /* ---- batched form: n requests, one fused launch per step ---- */
 /* n independent MCMC_likelihood_extrinsic evaluations (the sampler calls
  * mcmc_step -> sampler->ll once per chain, mcmc_sampler_internals.cpp:98).
