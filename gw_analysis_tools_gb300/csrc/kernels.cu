@@ -249,7 +249,12 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
     if (req) req[i] = r;
     if (want_mixed) {
       if (!s0.uniform_int) st = st ? st : 1;
-      mixed_prologue(r, s0.df, mreq[i]);
+      double ds[kMaxDet], ws[kMaxDet];
+      for (int d = 0; d < ndet; d++) {
+        ds[d] = streams[handles[i * ndet + d]].dscale;
+        ws[d] = streams[handles[i * ndet + d]].wscale;
+      }
+      mixed_prologue(r, s0.df, mreq[i], ds, ws);
     }
   } else {
     st = 4;
@@ -381,7 +386,12 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
       if (req) req[i] = r;
       if (want_mixed) {
         if (!s_uni[lane]) st = st ? st : 1;
-        mixed_det_coeffs(r, s_df[lane], mreq[i]);
+        double ds[kMaxDet], ws[kMaxDet];
+        for (int d = 0; d < ndet; d++) {
+          ds[d] = streams[handles[i * ndet + d]].dscale;
+          ws[d] = streams[handles[i * ndet + d]].wscale;
+        }
+        mixed_det_coeffs(r, s_df[lane], mreq[i], ds, ws);
       }
     } else {
       st = 4;
@@ -492,10 +502,15 @@ __device__ __forceinline__ void block_sum_mixed(const float (&v)[NV], float *sm,
     s_lo[j * kCols + c] = lo;
   }
   __syncthreads();
-  if (tid < NV) {
-    double acc = 0.0;
-    for (int c = 0; c < kCols; c++) acc += (double)s_hi[tid * kCols + c] + (double)s_lo[tid * kCols + c];
-    res[tid] = acc;
+  if (tid < NV) {  // the column pairs with TwoSum in FP32, one conversion to FP64 at the end
+    float hi = s_hi[tid * kCols], lo = s_lo[tid * kCols];
+    for (int c = 1; c < kCols; c++) {
+      float a = s_hi[tid * kCols + c];
+      float sum = hi + a, bp = sum - hi;
+      lo += ((hi - (sum - bp)) + (a - bp)) + s_lo[tid * kCols + c];
+      hi = sum;
+    }
+    res[tid] = (double)hi + (double)lo;
   }
   __syncthreads();
 }
@@ -574,7 +589,8 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
           // (B1) polynomial coefficients, one thread per (segment, function, coefficient)
           for (int e = tid; e < nseg * nfn * kSegNodes; e += blockDim.x) {
             const int j = e % kSegNodes, q = e / kSegNodes, sg = q / nfn, fn = q - sg * nfn;
-            s_coef[(sg * 2 + fn) * kSegNodes + j] = seg_coef((fn ? s_node_a : s_node) + sg * kSegEval, j);
+            s_coef[(sg * 2 + fn) * kSegNodes + j] =
+                seg_usable(x, n0, N, c0 + sg * kSegBins) ? seg_coef((fn ? s_node_a : s_node) + sg * kSegEval, j) : 0.0;
           }
           __syncthreads();
           // (B2) acceptance per (segment, function)
@@ -644,7 +660,27 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
     if (tid < NV) a.partials[(size_t)it * kAcc + tid] = s_res[tid];
     // last item of this request: fixed-order FP64 sum and log L
     if (arrive_last(a.req_done + I.req, (unsigned)a.item_count[I.req])) {
-      if (tid == 0) {
+      if constexpr (MIXED) {
+        // lane j of warp 0: sum j over the request's items, times its factor;
+        // then a fixed-order warp sum
+        if (tid < 32) {
+          const MixedReq &x = *(const MixedReq *)s_req;
+          const int i0 = a.item_start[I.req], ic = a.item_count[I.req];
+          double v = 0.0;
+          if (tid < NV) {
+            for (int q = 0; q < ic; q++) v += __ldcg(&a.partials[(size_t)(i0 + q) * kAcc + tid]);
+            v *= x.fc[tid];
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          if (tid == 0) {
+            int st = x.status;
+            if (__ldcg(a.status + I.req) & kStatusBounds) st = 5;
+            a.out[I.req] = st ? __longlong_as_double(0x7ff8000000000000ll) : v;
+            a.status[I.req] = st;
+          }
+        }
+      } else if (tid == 0) {
         double s[NV];
 #pragma unroll
         for (int j = 0; j < NV; j++) s[j] = 0.0;
@@ -654,18 +690,7 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
           for (int j = 0; j < NV; j++) s[j] += __ldcg(&a.partials[(size_t)(i0 + q) * kAcc + j]);
         double ll;
         int st;
-        if constexpr (MIXED) {
-          const MixedReq &x = *(const MixedReq *)s_req;
-          double ds[kMaxDet], ws[kMaxDet];
-          for (int d = 0; d < NDET; d++) {
-            ds[d] = s_st[d].dscale;
-            ws[d] = s_st[d].wscale;
-          }
-          double full[kAcc];
-          for (int j = 0; j < kAcc; j++) full[j] = j < NV ? s[j] : 0.0;
-          ll = mixed_finalize(x, full, ds, ws);
-          st = x.status;
-        } else {
+        {
           const Request &r = *(const Request *)s_req;
           ll = fp64_finalize<NDET>(s, s_st);
           st = r.m.status;

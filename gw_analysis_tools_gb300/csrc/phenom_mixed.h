@@ -47,6 +47,7 @@ struct MixedDet {
   double Gre, Gim;   // D: F+ (1+c^2)/2, -Fx c ; Pv2: P_d, Q_d (real); applied in FP64 at the end
 };
 
+constexpr int kAccPerDet = 5;  // D uses 3 (hh, zr, zi); Pv2 uses 5 (spp, scc, spc, zp, zc)
 struct MixedReq {
   int approximant, status, ndet, pad;
   int n_f1, n_f3, n_f1p, n_f2p, n_cut;  // region starts (first n in region) and last non-zero n
@@ -72,6 +73,9 @@ struct MixedReq {
   float w[4], w_lo[4];
   float x2c, x2c_lo;
   MixedDet det[kMaxDet];
+  // log L = sum_j fc[j] * S[j] over the accumulated sums S[d * kAccPerDet + j]
+  // (the FP64 amplitude scale, projection and whitening factors of each detector)
+  double fc[kMaxDet * kAccPerDet];
 };
 
 // FP64 coefficients of the amplitude and phase of one request on a grid
@@ -390,7 +394,7 @@ GW_HD void mixed_pv2_coeffs(const Request &r, double df, MixedReq &x) {
     split_f(cw * cw, x.x2c, x.x2c_lo);  // L2PN x = (pi M f)^(2/3) = cw^2 t^2
   }
 }
-GW_HD void mixed_det_coeffs(const Request &r, double df, MixedReq &x) {
+GW_HD void mixed_det_coeffs(const Request &r, double df, MixedReq &x, const double *dscale, const double *wscale) {
   const ModelD &m = r.m;
   const Source &s = m.s;
   const bool pv2 = (r.approximant == kPhenomPv2);
@@ -412,14 +416,32 @@ GW_HD void mixed_det_coeffs(const Request &r, double df, MixedReq &x) {
       x.det[d].Gre = r.det[d].fp * .5 * (1 + ci * ci);
       x.det[d].Gim = -r.det[d].fc * ci;
     }
+    // HH = A^2 w |G h|^2 sums, DH = A d Re(G ...) sums; log L = -HH/2 + DH
+    const double A = x.A_scale, G1 = x.det[d].Gre, G2 = x.det[d].Gim, w = wscale[d], ds = dscale[d];
+    double *f = x.fc + d * kAccPerDet;
+    if (pv2) {
+      f[0] = -0.5 * A * A * w * G1 * G1;
+      f[1] = -0.5 * A * A * w * G2 * G2;
+      f[2] = -A * A * w * G1 * G2;
+      f[3] = A * ds * G1;
+      f[4] = A * ds * G2;
+    } else {
+      f[0] = -0.5 * A * A * w * (G1 * G1 + G2 * G2);
+      f[1] = A * ds * G1;
+      f[2] = A * ds * G2;
+      f[3] = 0.0;
+      f[4] = 0.0;
+    }
   }
+  for (int d = r.ndet; d < kMaxDet; d++)
+    for (int j = 0; j < kAccPerDet; j++) x.fc[d * kAccPerDet + j] = 0.0;
 }
-GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x) {
+GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x, const double *dscale, const double *wscale) {
   mixed_regions(r, df, x);
   mixed_phase_coeffs(r, df, x);
   mixed_amp_coeffs(r, df, x);
   if (r.approximant == kPhenomPv2) mixed_pv2_coeffs(r, df, x);
-  mixed_det_coeffs(r, df, x);
+  mixed_det_coeffs(r, df, x, dscale, wscale);
   return x.status;
 }
 
@@ -461,7 +483,6 @@ GW_HD void kadd(KSum &k, float v) {
   k.c = (t - k.s) - y;
   k.s = t;
 }
-constexpr int kAccPerDet = 5;  // D uses 3 (hh, zr, zi); Pv2 uses 5 (spp, scc, spc, zp, zc)
 
 // Phase of the D model at bin n (FP64, radians), without the linear terms.
 // with_atan: include the ringdown atan term, evaluated in FP32 (its
@@ -733,21 +754,9 @@ GW_HD void mixed_phase_direct(const MixedReq &x, int n, double t, double r, doub
 }
 
 // log L of one request from its FP64 accumulated sums s[d * kAccPerDet + j].
-GW_HD double mixed_finalize(const MixedReq &x, const double *s, const double *dscale, const double *wscale) {
+GW_HD double mixed_finalize(const MixedReq &x, const double *s) {
   double ll = 0;
-  double A = x.A_scale;
-  for (int d = 0; d < x.ndet; d++) {
-    const double *v = s + d * kAccPerDet;
-    double G1 = x.det[d].Gre, G2 = x.det[d].Gim, HH, DH;
-    if (x.approximant != kPhenomPv2) {
-      HH = A * A * wscale[d] * (G1 * G1 + G2 * G2) * v[0];
-      DH = A * dscale[d] * (G1 * v[1] + G2 * v[2]);
-    } else {
-      HH = A * A * wscale[d] * (G1 * G1 * v[0] + G2 * G2 * v[1] + 2.0 * G1 * G2 * v[2]);
-      DH = A * dscale[d] * (G1 * v[3] + G2 * v[4]);
-    }
-    ll += -0.5 * (HH - 2 * DH);
-  }
+  for (int j = 0; j < kMaxDet * kAccPerDet; j++) ll += x.fc[j] * s[j];
   return ll;
 }
 

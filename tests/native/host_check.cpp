@@ -101,8 +101,6 @@ double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, cons
   int n0 = (int)std::llround(freqs[0] / df);
   MixedReq x;
   std::memset(&x, 0, sizeof(x));
-  mixed_prologue(r, df, x);
-  if (x.status) return NAN;
   double sdf = freqs[N / 2] - freqs[N / 2 - 1];
   std::vector<std::vector<float>> dh(ndet), wh(ndet);
   std::vector<double> dscale(ndet), wscale(ndet);
@@ -125,6 +123,8 @@ double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, cons
       wh[d][k] = (float)(W[k] / wscale[d]);
     }
   }
+  mixed_prologue(r, df, x, dscale.data(), wscale.data());
+  if (x.status) return NAN;
   auto tables = [](int n, double &t, double &rr, double &lnn, double &t34) {
     double xn = (double)n;
     t = std::cbrt(xn), rr = std::pow(xn, -5. / 3.), lnn = std::log(xn), t34 = std::pow(xn, 0.75);
@@ -179,7 +179,7 @@ double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, cons
       for (int j = 0; j < kMaxDet * kAccPerDet; j++) sums[j] += (double)(acc[j].s - acc[j].c);
     }
   }
-  return mixed_finalize(x, sums, dscale.data(), wscale.data());
+  return mixed_finalize(x, sums);
 }
 
 // Segments that used the polynomial phase / all segments, since the last reset.
