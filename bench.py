@@ -519,13 +519,16 @@ def main():
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    # roofline of the fused bin kernel: FP64 pipe (the path is neither HBM- nor tensor-bound)
-    fp64_ops_per_bin = float(os.environ.get("GWGPU_FP64_OPS_PER_BIN", "0")) or FP64_OPS_PER_BIN
-    units = N_REQ * 32128
-    flops = 2.0 * fp64_ops_per_bin * units  # FMA-equivalent ops x 2
-    achieved = flops / (res["kernel_ms"] / 1e3) / 1e12
-    log("fp64 peak")
-    fp64_peak = measure_fp64_peak()
+    # roofline of the fused bin kernel: the reference algorithm's work of one
+    # step (flops counted on the reference's model code) per kernel time,
+    # against the FP32 peak -- the pipe that carries most of the mixed form
+    units_wave = N_REQ * 32128
+    algo_flops = units_wave * REF_FLOPS_PER_WAVE_BIN + 3 * units_wave * REF_FLOPS_PER_DET_BIN
+    kernel_s = res["kernel_ms"] / 1e3
+    achieved = algo_flops / kernel_s / 1e12
+    log("fp32/fp64 peaks")
+    fp32_peak = measure_peak("float32")
+    fp64_peak = measure_peak("float64")
     ex = res.get("extras", {})
     fisher_worst = fisher_err(ex.pop("_fisher_sample")) if "_fisher_sample" in ex else None
     line = {
@@ -539,13 +542,20 @@ def main():
                 "d2h_bytes_per_step": res["d2h"]},
         "gpu_launches": res["gpu_launches"],
         "clocks": res["clocks"],
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp64_peak if fp64_peak else None, "traffic": TRAFFIC_PER_LAUNCH,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak if fp32_peak else None, "traffic": TRAFFIC_PER_LAUNCH,
                      "kernel": "k_batch<3,1> (fused mixed bin kernel)", "kernel_ms": res["kernel_ms"],
-                     "prologue_ms": res["prologue_ms"],
-                     "peak_source": "measured live: cuBLAS DGEMM 4096^3 in this run",
-                     "hbm": {"achieved_gbs": (TRAFFIC_PER_LAUNCH or 0) / (res["kernel_ms"] / 1e3) / 1e9,
-                             "peak_gbs": peaks.get("hbm_gbs"), "peak_source": "MEASURED_PEAKS.json"}},
+                     "prologue_ms": res["prologue_ms"], "algorithmic_flops_per_launch": algo_flops,
+                     "algorithm": "reference flops per waveform-bin %.2f and per detector-bin %.1f "
+                                  "(oracle/op_counts.json)" % (REF_FLOPS_PER_WAVE_BIN, REF_FLOPS_PER_DET_BIN),
+                     "peak_source": "measured in this run: FP32 GEMM 8192^3 without TF32 (FMA pipe)",
+                     "fp64": {"achieved_tflops": FP64_FLOP_PER_LAUNCH / kernel_s / 1e12, "peak_tflops": fp64_peak,
+                              "frac": FP64_FLOP_PER_LAUNCH / kernel_s / 1e12 / fp64_peak if fp64_peak else None,
+                              "flop_per_launch": FP64_FLOP_PER_LAUNCH,
+                              "peak_source": "measured in this run: FP64 GEMM 4096^3"},
+                     "hbm": {"achieved_gbs": TRAFFIC_PER_LAUNCH / kernel_s / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
+                             "frac": TRAFFIC_PER_LAUNCH / kernel_s / 1e9 / peaks["hbm_gbs"]
+                             if peaks.get("hbm_gbs") else None, "peak_source": "MEASURED_PEAKS.json"}},
         "cpu_baseline": base,
         "parity": dict(parity, tolerance=1e-3, status_ok=res["stat_ok"]),
     }
@@ -564,17 +574,26 @@ def main():
     print(json.dumps(line))
 
 
-# FP64 operations per bin of the fused mixed kernel (ncu: FP64 FMA-equivalent
-# thread instructions of k_batch<3,1> on this workload / bins processed), and
-# the DRAM bytes of one launch (ncu dram__bytes_read + write); see profiles/.
-FP64_OPS_PER_BIN = 13.0
-TRAFFIC_PER_LAUNCH = None
+# Work of the 512-request IMRPhenomD step: reference flops per unit, counted
+# by oracle/count_ops.py on the reference's own model code (oracle/op_counts.json);
+# and, from one ncu capture of k_batch<3,1> on this workload
+# (profiles/k_batch_mixed_ptstep512.md), its DRAM bytes and FP64 flops per launch.
+REF_FLOPS_PER_WAVE_BIN = 66.56
+REF_FLOPS_PER_DET_BIN = 33.0
+TRAFFIC_PER_LAUNCH = 2.74e6
+FP64_FLOP_PER_LAUNCH = 3.30e7
 
 
-def measure_fp64_peak():
+def measure_peak(dtype):
+    """Dense GEMM throughput (TFLOP/s) on this GPU: FP32 without TF32 (8192^3),
+    FP64 (4096^3); best of 5."""
     import torch
-    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
-    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192 if dtype == "float32" else 4096
+    dt = getattr(torch, dtype)
+    a = torch.randn(n, n, dtype=dt, device="cuda")
+    b = torch.randn(n, n, dtype=dt, device="cuda")
     for _ in range(2):
         a @ b
     torch.cuda.synchronize()
@@ -585,7 +604,9 @@ def measure_fp64_peak():
         a @ b
         e1.record()
         torch.cuda.synchronize()
-        best = max(best, 2 * 4096 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b
     return best
 
 

@@ -615,6 +615,13 @@ GW_HD double seg_coef(const double *v, int j) {
   for (int k = 0; k < kSegNodes; k++) s += GWT_T(gwt_seg_vinv)[j][k] * (v[k] - v[4]);
   return s;
 }
+// the same from node values already taken relative to the centre (dv[4] = 0)
+GW_HD double seg_coef_rel(const double *dv, int j) {
+  if (j == 0) return 0.0;
+  double s = 0.0;
+  for (int k = 0; k < kSegNodes; k++) s += GWT_T(gwt_seg_vinv)[j][k] * dv[k];
+  return s;
+}
 // (2) the acceptance test (check points, size of the FP32 part): 0 when usable;
 GW_HD int seg_check(const double *v, const double *c) {
   for (int k = kSegNodes; k < kSegEval; k++) {
