@@ -580,8 +580,8 @@ def main():
 # (profiles/k_batch_mixed_ptstep512.md), its DRAM bytes and FP64 flops per launch.
 REF_FLOPS_PER_WAVE_BIN = 66.56
 REF_FLOPS_PER_DET_BIN = 33.0
-TRAFFIC_PER_LAUNCH = 2.74e6
-FP64_FLOP_PER_LAUNCH = 3.30e7
+TRAFFIC_PER_LAUNCH = 2.72e6
+FP64_FLOP_PER_LAUNCH = 3.15e7
 
 
 def measure_peak(dtype):

@@ -277,8 +277,8 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 //   S2  W0 Pv2: ringdown frequencies; matching frequencies
 //   S3  W0/W1 amplitude matching points;  W2 phase connection;  W3 Pv2: Euler and frame constants
 //   S4  W0/W1 amplitude deltas;  W2 D: phase/time shift / Pv2: time-shift nodes 0-4;  W3 Pv2: nodes 5-9
-//   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions;  W3 Pv2: time shift and mixed angles
-//   S6  W0 detector phases, outputs
+//   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions;  W3 D: detector phases / Pv2: time shift, angles
+//   S6  W0 Pv2: detector phases; finalize factors, outputs
 constexpr int kCoopWarps = 4, kCoopReq = 16;
 __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     const GenParams *__restrict__ params, const int *__restrict__ approx, int n, const int *__restrict__ handles,
@@ -374,7 +374,10 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
       if (warp == 0) mixed_amp_coeffs(r, df, x);
       if (warp == 1) mixed_phase_coeffs(r, df, x);
       if (warp == 2) mixed_regions(r, df, x);
-      if (warp == 3 && pv2) mixed_pv2_coeffs(r, df, x);
+      if (warp == 3) {
+        if (pv2) mixed_pv2_coeffs(r, df, x);
+        else mixed_det_phase(r, df, x);
+      }
     }
   }
   __syncthreads();
@@ -391,7 +394,8 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
           ds[d] = streams[handles[i * ndet + d]].dscale;
           ws[d] = streams[handles[i * ndet + d]].wscale;
         }
-        mixed_det_coeffs(r, s_df[lane], mreq[i], ds, ws);
+        if (r.approximant == kPhenomPv2) mixed_det_phase(r, s_df[lane], mreq[i]);
+        mixed_det_factors(r, mreq[i], ds, ws);
       }
     } else {
       st = 4;

@@ -394,7 +394,9 @@ GW_HD void mixed_pv2_coeffs(const Request &r, double df, MixedReq &x) {
     split_f(cw * cw, x.x2c, x.x2c_lo);  // L2PN x = (pi M f)^(2/3) = cw^2 t^2
   }
 }
-GW_HD void mixed_det_coeffs(const Request &r, double df, MixedReq &x, const double *dscale, const double *wscale) {
+// Detectors in two parts: the linear phases and projections (needs the time
+// shift), then the finalize factors (needs the amplitude scale).
+GW_HD void mixed_det_phase(const Request &r, double df, MixedReq &x) {
   const ModelD &m = r.m;
   const Source &s = m.s;
   const bool pv2 = (r.approximant == kPhenomPv2);
@@ -416,6 +418,11 @@ GW_HD void mixed_det_coeffs(const Request &r, double df, MixedReq &x, const doub
       x.det[d].Gre = r.det[d].fp * .5 * (1 + ci * ci);
       x.det[d].Gim = -r.det[d].fc * ci;
     }
+  }
+}
+GW_HD void mixed_det_factors(const Request &r, MixedReq &x, const double *dscale, const double *wscale) {
+  const bool pv2 = (r.approximant == kPhenomPv2);
+  for (int d = 0; d < r.ndet; d++) {
     // HH = A^2 w |G h|^2 sums, DH = A d Re(G ...) sums; log L = -HH/2 + DH
     const double A = x.A_scale, G1 = x.det[d].Gre, G2 = x.det[d].Gim, w = wscale[d], ds = dscale[d];
     double *f = x.fc + d * kAccPerDet;
@@ -435,6 +442,10 @@ GW_HD void mixed_det_coeffs(const Request &r, double df, MixedReq &x, const doub
   }
   for (int d = r.ndet; d < kMaxDet; d++)
     for (int j = 0; j < kAccPerDet; j++) x.fc[d * kAccPerDet + j] = 0.0;
+}
+GW_HD void mixed_det_coeffs(const Request &r, double df, MixedReq &x, const double *dscale, const double *wscale) {
+  mixed_det_phase(r, df, x);
+  mixed_det_factors(r, x, dscale, wscale);
 }
 GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x, const double *dscale, const double *wscale) {
   mixed_regions(r, df, x);

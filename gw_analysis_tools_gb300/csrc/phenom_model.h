@@ -196,14 +196,40 @@ GW_HD void cspline_coeffs(const double *x, const double *y, int n, double *c, do
     for (int i = N - 2; i >= 0; i--) c[1 + i] = z[i] - gam[i] * c[2 + i];
   }
 }
-GW_HD double cspline_eval(const double *x, const double *y, const double *c, int n, double xv, int deriv) {
-  if (!(xv >= x[0] && xv <= x[n - 1])) return NAN;
+// Interval of xv in the knots x[0..n): the last ilo <= n - 2 with x[ilo] <= xv
+// (what a bisection finds), or -1 outside [x[0], x[n-1]].
+GW_HD int cspline_locate(const double *x, int n, double xv) {
+  if (!(xv >= x[0] && xv <= x[n - 1])) return -1;
   int ilo = 0, ihi = n - 1;
   while (ihi > ilo + 1) {
     int i = (ihi + ilo) / 2;
     if (x[i] > xv) ihi = i;
     else ilo = i;
   }
+  return ilo;
+}
+// The same interval on a knot array that is nearly uniform with spacing h:
+// a guess from the spacing corrected by a short walk (bounded by n).
+GW_HD int cspline_locate_near_uniform(const double *x, int n, double xv, double h) {
+  if (!(xv >= x[0] && xv <= x[n - 1])) return -1;
+  int g = (int)((xv - x[0]) / h);
+  if (g < 0) g = 0;
+  if (g > n - 2) g = n - 2;
+  for (int it = 0; it < n && g > 0 && x[g] > xv; it++) g--;
+  for (int it = 0; it < n && g < n - 2 && x[g + 1] <= xv; it++) g++;
+  return g;
+}
+GW_HD double cspline_eval_at(const double *x, const double *y, const double *c, int ilo, double xv, int deriv) {
+  if (ilo < 0) return NAN;
+  double x_lo = x[ilo], dx = x[ilo + 1] - x_lo, y_lo = y[ilo], dy = y[ilo + 1] - y_lo, delx = xv - x_lo;
+  double c_i = c[ilo], c_ip1 = c[ilo + 1];
+  double b_i = (dy / dx) - dx * (c_ip1 + 2.0 * c_i) / 3.0, d_i = (c_ip1 - c_i) / (3.0 * dx);
+  if (deriv) return b_i + delx * (2.0 * c_i + 3.0 * d_i * delx);
+  return y_lo + delx * (b_i + delx * (c_i + delx * d_i));
+}
+GW_HD double cspline_eval(const double *x, const double *y, const double *c, int n, double xv, int deriv) {
+  if (!(xv >= x[0] && xv <= x[n - 1])) return NAN;
+  int ilo = cspline_locate(x, n, xv);
   double x_lo = x[ilo], dx = x[ilo + 1] - x_lo, y_lo = y[ilo], dy = y[ilo + 1] - y_lo, delx = xv - x_lo;
   double c_i = c[ilo], c_ip1 = c[ilo + 1];
   double b_i = (dy / dx) - dx * (c_ip1 + 2.0 * c_i) / 3.0, d_i = (c_ip1 - c_i) / (3.0 * dx);
@@ -346,8 +372,10 @@ GW_HD void post_merger(Source &s, const double *qnm) {  // IMRPhenomD.cpp:1091-1
                *cd = qnm + 4 * kQnmLen;
   double finspin = final_spin(s);
   double Erad = EradRational0815(s.eta, s.spin1z, s.spin2z);
-  s.fRD = cspline_eval(a, yr, cr, kQnmLen, finspin, 0) / (1.0 - Erad) / s.M;
-  s.fdamp = cspline_eval(a, yd, cd, kQnmLen, finspin, 0) / (1.0 - Erad) / s.M;
+  // both splines share the knots (spacing 0.002 inside, 0.001 at the ends)
+  const int ilo = cspline_locate_near_uniform(a, kQnmLen, finspin, 0.002);
+  s.fRD = cspline_eval_at(a, yr, cr, ilo, finspin, 0) / (1.0 - Erad) / s.M;
+  s.fdamp = cspline_eval_at(a, yd, cd, ilo, finspin, 0) / (1.0 - Erad) / s.M;
 }
 GW_HD double fpeak(const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1312-1326
   double fRD = s.fRD, fdamp = s.fdamp, g3 = l.gamma[2], g2 = l.gamma[1];
