@@ -1,7 +1,7 @@
 // noalloc.cu -- gwgpu_mcmc_likelihood_extrinsic_noalloc: the plain FP64
 // likelihood (one request, one launch of the plain kernel) for callers that
-// may not allocate memory while it runs, e.g. inside CUDA stream capture or
-// under a fixed memory budget.  It allocates nothing: the plain kernel's
+// may not allocate memory while it runs (a fixed memory budget, or code that
+// must not call an allocator on this path).  It allocates nothing: the plain kernel's
 // scratch (block partial sums and the block-arrival counter) lives in one
 // file-scope device array, the log-likelihood goes to a device pointer the
 // caller owns, and the call only enqueues on the caller's stream.

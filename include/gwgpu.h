@@ -112,8 +112,8 @@ int gwgpu_mcmc_likelihood_extrinsic(gwgpu_context *ctx, const gwgpu_gen_params *
                                     double T_segment, double *loglik);
 
 /* No counterpart in the reference.  The same plain FP64 likelihood for callers
- * that may not allocate memory while it runs (inside CUDA stream capture, or
- * under a fixed memory budget): it allocates nothing, enqueues one launch on
+ * that may not allocate memory while it runs (a fixed memory budget, or code
+ * that must not call an allocator on this path): it allocates nothing, enqueues one launch on
  * `stream` (0: the legacy default stream) and writes log L to the device
  * pointer d_loglik without synchronising.  Its scratch is one fixed device
  * array sized for grids of up to 524,288 bins (4,096 blocks of 128 bins);
