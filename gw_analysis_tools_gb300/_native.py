@@ -103,6 +103,8 @@ def _declare(L):
         "gwgpu_fourier_detector_response": (c_int, [c_void_p, dp, c_int, dp, c_char_p, c_char_p, c_void_p]),
         "gwgpu_data_register": (c_int, [c_void_p, c_char_p, dp, c_int, dp, dp, ip]),
         "gwgpu_data_release": (c_int, [c_void_p, c_int]),
+        "gwgpu_data_register_weighted": (c_int, [c_void_p, c_char_p, dp, c_int, dp, dp, dp, c_int, ip]),
+        "gwgpu_log_likelihood_internal_weighted": (c_int, [c_void_p, dp, dp, dp, dp, dp, c_int, c_int, dp]),
         "gwgpu_log_likelihood_internal": (c_int, [c_void_p, dp, dp, dp, dp, c_int, dp]),
         "gwgpu_mcmc_likelihood_extrinsic": (c_int, [c_void_p, c_void_p, c_char_p, ip, c_int, c_double, dp]),
         "gwgpu_loglik_batch": (c_int, [c_void_p, c_void_p, ip, c_int, ip, c_int, c_double, c_int, dp, ip]),

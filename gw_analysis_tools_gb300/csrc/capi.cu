@@ -279,8 +279,9 @@ void *gwgpu_context_stream(gwgpu_context *c) { return c ? (void *)c->stream : nu
 size_t gwgpu_context_bytes_in_use(gwgpu_context *c) { return c ? c->in_use : 0; }
 
 // ------------------------------------------------------------ data registry
-int gwgpu_data_register(gwgpu_context *c, const char *detector, const double *freqs, int N, const double *data,
-                        const double *psd, int *handle) {
+// One detector stream; weights (GAUSSLEG) or null (Simpson's rule).
+static int register_stream(gwgpu_context *c, const char *detector, const double *freqs, int N, const double *data,
+                           const double *psd, const double *weights, int log10F, int *handle) {
   if (!c || !freqs || !data || !psd || !handle || N < 2) return GWGPU_EINVAL;
   int det = det_index(detector);
   if (det < 0) {
@@ -303,13 +304,18 @@ int gwgpu_data_register(gwgpu_context *c, const char *detector, const double *fr
   double n0f = freqs[0] / d.df;
   d.n0 = (int)std::llround(n0f);
   d.uniform_int = uniform && d.n0 >= 1 && std::fabs(n0f - d.n0) < 1e-6 && (d.n0 + (double)N) < 1.5e9;
-  // Simpson-weighted whitening for the mixed form: W_k = (4 df/3) s_k / S_k
-  std::vector<double> W(N);
+  // integration weights: Simpson's rule, (4 df/3) s_k (util.h:844-856), or the
+  // GAUSSLEG branch, 4 w_k (times f_k ln 10 for log10F) (mcmc_gw.cpp:820-862);
+  // whitening for the mixed form W_k = weight_k / S_k
+  std::vector<double> iw(N), W(N);
   double c3 = 4. * d.simpson_df / 3.;
-  double wmax = 0, dmax = 0;
   for (int k = 0; k < N; k++) {
     double sw = (k == 0 || k == N - 1) ? 1.0 : ((k & 1) ? 4.0 : 2.0);
-    W[k] = c3 * sw / psd[k];
+    iw[k] = weights ? 4.0 * weights[k] * (log10F ? freqs[k] * std::log(10.) : 1.0) : c3 * sw;
+  }
+  double wmax = 0, dmax = 0;
+  for (int k = 0; k < N; k++) {
+    W[k] = iw[k] / psd[k];
     if (std::isfinite(W[k])) wmax = std::max(wmax, std::fabs(W[k]));
     double m = std::fabs(W[k] * data[2 * k]) + std::fabs(W[k] * data[2 * k + 1]);
     if (std::isfinite(m)) dmax = std::max(dmax, m);
@@ -323,11 +329,13 @@ int gwgpu_data_register(gwgpu_context *c, const char *detector, const double *fr
     wh[k] = (float)(W[k] / d.wscale);
   }
   int st;
-  void *pf, *pd, *pp, *pdh, *pwh;
+  void *pf, *pd, *pp, *pdh, *pwh, *piw = nullptr;
   if ((st = c->dalloc(&pf, 8 * (size_t)N, "freqs")) || (st = c->dalloc(&pd, 16 * (size_t)N, "data")) ||
       (st = c->dalloc(&pp, 8 * (size_t)N, "psd")) || (st = c->dalloc(&pdh, 8 * (size_t)N, "dhat")) ||
-      (st = c->dalloc(&pwh, 4 * (size_t)N, "what")))
+      (st = c->dalloc(&pwh, 4 * (size_t)N, "what")) ||
+      (weights && (st = c->dalloc(&piw, 8 * (size_t)N, "integration weights"))))
     return st;
+  if (piw) cudaMemcpyAsync(piw, iw.data(), 8 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(pf, freqs, 8 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(pd, data, 16 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(pp, psd, 8 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
@@ -340,12 +348,18 @@ int gwgpu_data_register(gwgpu_context *c, const char *detector, const double *fr
   d.psd = (const double *)pp;
   d.dhat = (const float *)pdh;
   d.what = (const float *)pwh;
+  d.iw = (const double *)piw;
   s.live = true;
   s.mem = {pf, pd, pp, pdh, pwh};
+  if (piw) s.mem.push_back(piw);
   s.host_freqs.assign(freqs, freqs + N);
   uint64_t hsh = 1469598103934665603ull;
   const unsigned char *pb = (const unsigned char *)psd;
   for (size_t i = 0; i < 8 * (size_t)N; i++) hsh = (hsh ^ pb[i]) * 1099511628211ull;
+  if (weights) {
+    const unsigned char *wb = (const unsigned char *)iw.data();
+    for (size_t i = 0; i < 8 * (size_t)N; i++) hsh = (hsh ^ wb[i]) * 1099511628211ull;
+  }
   s.psd_hash = hsh ^ (uint64_t)N;
   if (d.uniform_int) {
     st = c->ensure_tables(d.n0 + N);
@@ -354,6 +368,18 @@ int gwgpu_data_register(gwgpu_context *c, const char *detector, const double *fr
   c->streams.push_back(s);
   *handle = (int)c->streams.size() - 1;
   return c->sync_streams_table();
+}
+
+int gwgpu_data_register(gwgpu_context *c, const char *detector, const double *freqs, int N, const double *data,
+                        const double *psd, int *handle) {
+  return register_stream(c, detector, freqs, N, data, psd, nullptr, 0, handle);
+}
+
+int gwgpu_data_register_weighted(gwgpu_context *c, const char *detector, const double *freqs, int N,
+                                 const double *data, const double *psd, const double *weights, int log10F,
+                                 int *handle) {
+  if (!weights) return GWGPU_EINVAL;
+  return register_stream(c, detector, freqs, N, data, psd, weights, log10F, handle);
 }
 
 int gwgpu_data_release(gwgpu_context *c, int handle) {
@@ -427,6 +453,37 @@ int gwgpu_log_likelihood_internal(gwgpu_context *c, const double *data, const do
   cudaMemcpyAsync(dp, psd, 8 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
   double sdf = freqs[N / 2] - freqs[N / 2 - 1];
   cudaError_t e = gwk::launch_inner_product(dd, dp, dr, N, sdf, part, cnt, res, c->stream);
+  if (e != cudaSuccess) return c->fail(e, "inner product launch");
+  cudaMemcpyAsync(out, res, 8, cudaMemcpyDeviceToHost, c->stream);
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return c->fail(e, "inner product");
+  return GWGPU_OK;
+}
+
+int gwgpu_log_likelihood_internal_weighted(gwgpu_context *c, const double *data, const double *psd,
+                                           const double *freqs, const double *weights, const double *resp, int N,
+                                           int log10F, double *out) {
+  if (!c || !data || !psd || !freqs || !weights || !resp || !out || N < 1) return GWGPU_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  // integration weights of the GAUSSLEG branch (mcmc_gw.cpp:820-833, 843-862)
+  double *iwh;
+  int st = c->pinned(gwgpu_context::kHwsInner, 8 * (size_t)N, (void **)&iwh);
+  if (st) return st;
+  for (int k = 0; k < N; k++) iwh[k] = 4.0 * weights[k] * (log10F ? freqs[k] * std::log(10.) : 1.0);
+  void *dev;
+  size_t nb = 16 * (size_t)N * 2 + 8 * (size_t)N * 2 + 8 * 2048 + 64;
+  st = c->workspace(gwgpu_context::kWsInner, nb, &dev);
+  if (st) return st;
+  double *dd = (double *)dev, *dr = dd + 2 * (size_t)N, *dp = dr + 2 * (size_t)N, *diw = dp + N, *part = diw + N,
+         *res = part + 2048;
+  unsigned *cnt = c->counter(0);
+  if (!cnt) return GWGPU_ECUDA;
+  cudaMemcpyAsync(dd, data, 16 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(dr, resp, 16 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(dp, psd, 8 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(diw, iwh, 8 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
+  cudaError_t e = gwk::launch_inner_product_weighted(dd, dp, dr, diw, N, part, cnt, res, c->stream);
   if (e != cudaSuccess) return c->fail(e, "inner product launch");
   cudaMemcpyAsync(out, res, 8, cudaMemcpyDeviceToHost, c->stream);
   e = cudaStreamSynchronize(c->stream);

@@ -26,7 +26,7 @@ struct gwgpu_context {
     uint64_t psd_hash = 0;  // FNV-1a of the PSD bytes: detectors with equal PSDs share weights
   };
   enum { kWsWave = 0, kWsInner, kWsPlain, kWsBatch, kWsBatchItems, kWsFisher, kWsServe };
-  enum { kHwsPlain = 0, kHwsBatch, kHwsFisher };
+  enum { kHwsPlain = 0, kHwsBatch, kHwsFisher, kHwsInner };
 
   int device = 0;
   size_t budget = 0, in_use = 0;

@@ -344,8 +344,8 @@ int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, 
   cudaSetDevice(c->device);
   const gwgpu_context::Stream *s0 = c->get_stream(handles[0]);
   if (!s0) return GWGPU_ENOTFOUND;
-  if (!s0->dev.uniform_int) {
-    c->last_error = "fisher_batch needs a uniform grid with f0 a multiple of df";
+  if (!s0->dev.uniform_int || s0->dev.iw) {
+    c->last_error = "fisher_batch needs Simpson streams on a uniform grid with f0 a multiple of df";
     return GWGPU_EINVAL;
   }
   FisherArgs a;
@@ -357,7 +357,7 @@ int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, 
   for (int d = 0; d < ndet; d++) {
     const gwgpu_context::Stream *s = c->get_stream(handles[d]);
     if (!s) return GWGPU_ENOTFOUND;
-    if (s->dev.N != s0->dev.N || s->dev.n0 != s0->dev.n0) return GWGPU_EINVAL;
+    if (s->dev.N != s0->dev.N || s->dev.n0 != s0->dev.n0 || s->dev.iw) return GWGPU_EINVAL;
     dets[d] = s->dev.det;
     int found = -1;
     for (int w = 0; w < nw; w++) {  // same PSD and grid -> same weight stream

@@ -99,13 +99,14 @@ __device__ __forceinline__ bool arrive_last(unsigned *counter, unsigned expected
 }
 
 // ------------------------------------------------------ Simpson inner product
+// iw: GAUSSLEG integration weights (null: Simpson's rule).
 __global__ void k_inner(const double2 *__restrict__ data, const double *__restrict__ psd,
-                        const double2 *__restrict__ resp, int N, double simpson_df, double *partials,
-                        unsigned *counter, double *out) {
+                        const double2 *__restrict__ resp, const double *__restrict__ iw, int N, double simpson_df,
+                        double *partials, unsigned *counter, double *out) {
   __shared__ double smem[32 * 2];
   double v[2] = {0.0, 0.0};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
-    double w = simpson_weight(k, N);
+    double w = iw ? iw[k] : simpson_weight(k, N);
     double2 r = resp[k], d = data[k];
     double S = psd[k];
     v[0] += w * ((r.x * r.x + r.y * r.y) / S);
@@ -123,7 +124,7 @@ __global__ void k_inner(const double2 *__restrict__ data, const double *__restri
         hh += __ldcg(&partials[b * 2 + 0]);
         dh += __ldcg(&partials[b * 2 + 1]);
       }
-      double c = 4. * simpson_df / 3.;
+      double c = iw ? 1.0 : 4. * simpson_df / 3.;
       out[0] = -0.5 * (c * hh - 2 * c * dh);
       *counter = 0;
     }
@@ -133,7 +134,15 @@ cudaError_t launch_inner_product(const double *data, const double *psd, const do
                                  double *partials, unsigned *counter, double *out, cudaStream_t s) {
   int block = 256, grid = (N + block - 1) / block;
   if (grid > 1024) grid = 1024;
-  k_inner<<<grid, block, 0, s>>>((const double2 *)data, psd, (const double2 *)resp, N, simpson_df, partials, counter,
+  k_inner<<<grid, block, 0, s>>>((const double2 *)data, psd, (const double2 *)resp, nullptr, N, simpson_df, partials,
+                                 counter, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_inner_product_weighted(const double *data, const double *psd, const double *resp, const double *iw,
+                                          int N, double *partials, unsigned *counter, double *out, cudaStream_t s) {
+  int block = 256, grid = (N + block - 1) / block;
+  if (grid > 1024) grid = 1024;
+  k_inner<<<grid, block, 0, s>>>((const double2 *)data, psd, (const double2 *)resp, iw, N, 0.0, partials, counter,
                                  out);
   return cudaGetLastError();
 }
@@ -146,12 +155,13 @@ __device__ __forceinline__ void fp64_bin(const Request &r, const StreamDev *st, 
   const double f = st[0].freqs[k];
   cd hp, hc;
   wave_bin(r, f, hp, hc);
-  const double w = simpson_weight(k, N);
+  const double ws = simpson_weight(k, N);
 #pragma unroll
   for (int d = 0; d < NDET; d++) {
     cd x = response_bin(r.det[d], hp, hc, f, r.det[d].tau != 0.0);
     double2 dd = ((const double2 *)st[d].data)[k];
     double S = st[d].psd[k];
+    const double w = st[d].iw ? st[d].iw[k] : ws;
     v[2 * d] += w * ((x.re * x.re + x.im * x.im) / S);
     v[2 * d + 1] += w * ((dd.x * x.re + dd.y * x.im) / S);
   }
@@ -161,7 +171,7 @@ __device__ __forceinline__ double fp64_finalize(const double *s, const StreamDev
   double ll = 0;
 #pragma unroll
   for (int d = 0; d < NDET; d++) {
-    double c = 4. * st[d].simpson_df / 3.;
+    double c = st[d].iw ? 1.0 : 4. * st[d].simpson_df / 3.;
     ll += -0.5 * (c * s[2 * d] - 2 * c * s[2 * d + 1]);
   }
   return ll;

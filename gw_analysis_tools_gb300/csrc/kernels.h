@@ -24,6 +24,9 @@ struct StreamDev {
   const double *freqs, *data, *psd;  // FP64 originals (data interleaved complex)
   const float *dhat, *what;          // mixed-form streams (interleaved complex, real)
   double dscale, wscale;
+  // integration weights of the GAUSSLEG branch (mcmc_gw.cpp:820-862), times 4
+  // and f ln 10 for log10F; null for Simpson's rule (util.h:844-856)
+  const double *iw;
 };
 
 struct Item {
@@ -44,6 +47,9 @@ cudaError_t launch_response(const Request &r, int det_slot, int apply_shift, con
 // Simpson inner product of given response/data/psd arrays (Log_Likelihood_internal).
 cudaError_t launch_inner_product(const double *data, const double *psd, const double *resp, int N, double simpson_df,
                                  double *partials, unsigned *counter, double *out, cudaStream_t s);
+// The same with integration weights iw (4 w_i, times f_i ln 10 for log10F).
+cudaError_t launch_inner_product_weighted(const double *data, const double *psd, const double *resp, const double *iw,
+                                          int N, double *partials, unsigned *counter, double *out, cudaStream_t s);
 // Plain form: one request, FP64, one launch.  out[0] = log L.
 cudaError_t launch_plain(const Request &r, const StreamDev *streams, int ndet, double *partials, unsigned *counter,
                          double *out, int *status, cudaStream_t s);

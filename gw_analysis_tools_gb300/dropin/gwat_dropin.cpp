@@ -29,7 +29,7 @@ struct Engine {
   double srv_T = 0;
   bool served = false;
   std::mutex mu;
-  std::map<std::tuple<const void *, const void *, const void *, int, int, uint64_t>, int> handles;
+  std::map<std::tuple<const void *, const void *, const void *, const void *, int, int, uint64_t>, int> handles;
 };
 
 static Engine &engine() {
@@ -82,15 +82,20 @@ static void to_abi(const gen_params_base<double> *p, gwgpu_gen_params *o) {
   o->dep_postmerger = p->dep_postmerger;
 }
 
+// weights: the GAUSSLEG integration (null: Simpson's rule); log10F as the reference's flag
 static int handle_for(Engine &e, const std::string &det, const double *f, const std::complex<double> *d,
-                      const double *psd, int n) {
+                      const double *psd, const double *weights, bool log10F, int n) {
   uint64_t fp = fingerprint(f, n) ^ (fingerprint((const double *)d, 2 * n) * 31) ^ (fingerprint(psd, n) * 131);
-  auto key = std::make_tuple((const void *)f, (const void *)d, (const void *)psd, n, (int)det.size() * 131 + det[0],
-                             fp);
+  if (weights) fp ^= fingerprint(weights, n) * 1031 + (log10F ? 7 : 3);
+  auto key = std::make_tuple((const void *)f, (const void *)d, (const void *)psd, (const void *)weights, n,
+                             (int)det.size() * 131 + det[0], fp);
   auto it = e.handles.find(key);
   if (it != e.handles.end()) return it->second;
   int h = -1;
-  if (gwgpu_data_register(e.ctx, det.c_str(), f, n, (const double *)d, psd, &h) != GWGPU_OK) return -1;
+  int st = weights ? gwgpu_data_register_weighted(e.ctx, det.c_str(), f, n, (const double *)d, psd, weights,
+                                                  log10F ? 1 : 0, &h)
+                   : gwgpu_data_register(e.ctx, det.c_str(), f, n, (const double *)d, psd, &h);
+  if (st != GWGPU_OK) return -1;
   e.handles[key] = h;
   return h;
 }
@@ -133,12 +138,13 @@ template int fourier_detector_response<double>(double *, int, std::complex<doubl
 double Log_Likelihood_internal(std::complex<double> *data, double *psd, double *frequencies, double *weights,
                                std::complex<double> *detector_response, int length, bool log10F,
                                std::string integration_method) {
-  (void)weights;
-  (void)log10F;
-  if (integration_method != "SIMPSONS") return NAN;
   double out = NAN;
-  gwgpu_log_likelihood_internal(engine().ctx, (const double *)data, psd, frequencies,
-                                (const double *)detector_response, length, &out);
+  if (integration_method == "SIMPSONS")
+    gwgpu_log_likelihood_internal(engine().ctx, (const double *)data, psd, frequencies,
+                                  (const double *)detector_response, length, &out);
+  else if (integration_method == "GAUSSLEG" && weights)
+    gwgpu_log_likelihood_internal_weighted(engine().ctx, (const double *)data, psd, frequencies, weights,
+                                           (const double *)detector_response, length, log10F ? 1 : 0, &out);
   return out;
 }
 
@@ -147,9 +153,10 @@ double MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double> *pa
                                  std::complex<double> **data, double **psd, double **weights,
                                  std::string integration_method, bool log10F, std::string *detectors,
                                  int num_detectors) {
-  (void)weights;
-  (void)log10F;
-  if (!save_waveform || integration_method != "SIMPSONS" || num_detectors < 1 || num_detectors > 4) return NAN;
+  const bool gauss = integration_method == "GAUSSLEG";
+  if (!save_waveform || !(gauss || integration_method == "SIMPSONS") || num_detectors < 1 || num_detectors > 4)
+    return NAN;
+  if (gauss && !weights) return NAN;
   Engine &e = engine();
   // mcmc_gw.cpp:2466 forms T from frequencies[1] - frequencies[0] of the
   // double** array, i.e. the distance between the first two detectors'
@@ -163,7 +170,8 @@ double MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double> *pa
   {
     std::lock_guard<std::mutex> lk(e.mu);
     for (int i = 0; i < num_detectors; i++) {
-      hs[i] = handle_for(e, detectors[i], frequencies[i], data[i], psd[i], data_length[i]);
+      hs[i] = handle_for(e, detectors[i], frequencies[i], data[i], psd[i], gauss ? weights[i] : nullptr, log10F,
+                         data_length[i]);
       if (hs[i] < 0) return NAN;
     }
   }
@@ -173,7 +181,7 @@ double MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double> *pa
   double ll = NAN;
   const char *m = generation_method.c_str();
   int approx = generation_method.find("Pv2") != std::string::npos ? GWGPU_IMRPHENOMPV2 : GWGPU_IMRPHENOMD;
-  if (e.served) {
+  if (e.served && !gauss) {  // the served (mixed) form wants uniform grids; Gauss-Legendre grids run plain
     {
       std::lock_guard<std::mutex> lk(e.mu);
       if (!e.srv || e.srv_T != T) {
@@ -212,6 +220,10 @@ void fisher_numerical(double *frequency, int length, std::string generation_meth
 }
 
 // ---- C entry points for the test suite (ctypes cannot call the C++ symbols)
+extern "C" double gwat_dropin_test_loglik_gl(const double *f, int N, const double *const *data,
+                                             const double *const *psd, const double *const *weights, int log10F,
+                                             const char *const *dets, int ndet, const gwgpu_gen_params *pp,
+                                             double *tc_after);
 extern "C" double gwat_dropin_test_loglik(const double *f, int N, const double *const *data,
                                           const double *const *psd, const char *const *dets, int ndet,
                                           const gwgpu_gen_params *pp, int served, double *tc_after) {
@@ -248,6 +260,48 @@ extern "C" double gwat_dropin_test_loglik(const double *f, int N, const double *
   }
   double ll = MCMC_likelihood_extrinsic(true, &g, "IMRPhenomD", len.data(), fs.data(), ds.data(), ps.data(),
                                         ws.data(), "SIMPSONS", false, dn.data(), ndet);
+  if (tc_after) tc_after[0] = g.tc;
+  if (tc_after) tc_after[1] = ndet > 1 ? 1. / (double)(fs[1] - fs[0]) : 1. / (f[1] - f[0]);
+  return ll;
+}
+
+// The same with the GAUSSLEG integration (weights per detector), plain mode.
+extern "C" double gwat_dropin_test_loglik_gl(const double *f, int N, const double *const *data,
+                                             const double *const *psd, const double *const *weights, int log10F,
+                                             const char *const *dets, int ndet, const gwgpu_gen_params *pp,
+                                             double *tc_after) {
+  gen_params_base<double> g;
+  g.mass1 = pp->mass1;
+  g.mass2 = pp->mass2;
+  for (int i = 0; i < 3; i++) {
+    g.spin1[i] = pp->spin1[i];
+    g.spin2[i] = pp->spin2[i];
+  }
+  g.Luminosity_Distance = pp->Luminosity_Distance;
+  g.incl_angle = pp->incl_angle;
+  g.phiRef = pp->phiRef;
+  g.f_ref = pp->f_ref;
+  g.tc = pp->tc;
+  g.RA = pp->RA;
+  g.DEC = pp->DEC;
+  g.psi = pp->psi;
+  g.gmst = pp->gmst;
+  set_mode("plain");
+  std::vector<int> len(ndet, N);
+  std::vector<double *> fs(ndet), ps(ndet), ws(ndet);
+  std::vector<std::complex<double> *> ds(ndet);
+  std::vector<std::string> dn(ndet);
+  std::vector<double> fblock((size_t)ndet * N);
+  for (int i = 0; i < ndet; i++) {
+    std::copy(f, f + N, fblock.begin() + (size_t)i * N);
+    fs[i] = fblock.data() + (size_t)i * N;
+    ps[i] = const_cast<double *>(psd[i]);
+    ws[i] = const_cast<double *>(weights[i]);
+    ds[i] = (std::complex<double> *)data[i];
+    dn[i] = dets[i];
+  }
+  double ll = MCMC_likelihood_extrinsic(true, &g, "IMRPhenomD", len.data(), fs.data(), ds.data(), ps.data(),
+                                        ws.data(), "GAUSSLEG", log10F != 0, dn.data(), ndet);
   if (tc_after) tc_after[0] = g.tc;
   if (tc_after) tc_after[1] = ndet > 1 ? 1. / (double)(fs[1] - fs[0]) : 1. / (f[1] - f[0]);
   return ll;

@@ -138,12 +138,21 @@ class Context:
         return r
 
     # ---------------------------------------------------------------- data
-    def register_data(self, detector, freqs, data, psd):
+    def register_data(self, detector, freqs, data, psd, weights=None, log10F=False):
+        """One detector's grid, data and PSD on the device.  With weights, the
+        stream integrates by the GAUSSLEG rule (mcmc_gw.cpp:820-862) instead of
+        Simpson's."""
         f = np.ascontiguousarray(freqs, dtype=np.float64)
         d = np.ascontiguousarray(data, dtype=np.complex128)
         s = np.ascontiguousarray(psd, dtype=np.float64)
         h = ctypes.c_int()
-        st = self.lib.gwgpu_data_register(self.h, detector.encode(), _dp(f), f.size, _dp(d), _dp(s), ctypes.byref(h))
+        if weights is None:
+            st = self.lib.gwgpu_data_register(self.h, detector.encode(), _dp(f), f.size, _dp(d), _dp(s),
+                                              ctypes.byref(h))
+        else:
+            w = np.ascontiguousarray(weights, dtype=np.float64)
+            st = self.lib.gwgpu_data_register_weighted(self.h, detector.encode(), _dp(f), f.size, _dp(d), _dp(s),
+                                                       _dp(w), int(bool(log10F)), ctypes.byref(h))
         self._check(st, "data_register")
         self._data[h.value] = (detector, f.size)
         return h.value
@@ -153,14 +162,19 @@ class Context:
         self._data.pop(handle, None)
 
     # ---------------------------------------------------------- likelihood
-    def log_likelihood_internal(self, data, psd, freqs, response):
+    def log_likelihood_internal(self, data, psd, freqs, response, weights=None, log10F=False):
         d = np.ascontiguousarray(data, dtype=np.complex128)
         s = np.ascontiguousarray(psd, dtype=np.float64)
         f = np.ascontiguousarray(freqs, dtype=np.float64)
         r = np.ascontiguousarray(response, dtype=np.complex128)
         out = ctypes.c_double()
-        st = self.lib.gwgpu_log_likelihood_internal(self.h, _dp(d), _dp(s), _dp(f), _dp(r), f.size,
-                                                    ctypes.byref(out))
+        if weights is None:
+            st = self.lib.gwgpu_log_likelihood_internal(self.h, _dp(d), _dp(s), _dp(f), _dp(r), f.size,
+                                                        ctypes.byref(out))
+        else:
+            w = np.ascontiguousarray(weights, dtype=np.float64)
+            st = self.lib.gwgpu_log_likelihood_internal_weighted(self.h, _dp(d), _dp(s), _dp(f), _dp(w), _dp(r),
+                                                                 f.size, int(bool(log10F)), ctypes.byref(out))
         self._check(st, "log_likelihood_internal")
         return out.value
 

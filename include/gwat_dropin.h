@@ -45,12 +45,13 @@ int fourier_waveform(double *frequencies, int length, std::complex<double> *wave
 template <class T>
 int fourier_detector_response(T *frequencies, int length, std::complex<T> *response, std::string detector,
                               std::string generation_method, gen_params_base<T> *parameters, T *times = nullptr);
-// Log_Likelihood_internal (mcmc_gw.h:276, mcmc_gw.cpp:801); SIMPSONS only
+// Log_Likelihood_internal (mcmc_gw.h:276, mcmc_gw.cpp:801); SIMPSONS and GAUSSLEG
 double Log_Likelihood_internal(std::complex<double> *data, double *psd, double *frequencies, double *weights,
                                std::complex<double> *detector_response, int length, bool log10F,
                                std::string integration_method);
-// MCMC_likelihood_extrinsic (mcmc_gw.h:473, mcmc_gw.cpp:2374); SIMPSONS only,
-// save_waveform = true (one waveform for every detector, waveform_util.cpp:153)
+// MCMC_likelihood_extrinsic (mcmc_gw.h:473, mcmc_gw.cpp:2374); SIMPSONS and
+// GAUSSLEG, save_waveform = true (one waveform for every detector,
+// waveform_util.cpp:153)
 double MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double> *parameters,
                                  std::string generation_method, int *data_length, double **frequencies,
                                  std::complex<double> **data, double **psd, double **weights,

@@ -92,6 +92,14 @@ int gwgpu_fourier_detector_response(gwgpu_context *ctx, const double *frequencie
  * mcmc_frequencies pointers set at mcmc_gw.cpp:1464-1476) ---- */
 int gwgpu_data_register(gwgpu_context *ctx, const char *detector, const double *frequencies, int length,
                         const double *data, const double *psd, int *handle);
+/* The same for the "GAUSSLEG" integration of Log_Likelihood_internal
+ * (mcmc_gw.cpp:820-833, 843-862): integral = 4 sum_i weights[i] integrand[i],
+ * times frequencies[i] ln 10 when log10F (the sampler's GAUSS_QUAD option,
+ * mcmc_gw.cpp:2608-2610).  Every form integrates such a stream with its
+ * weights; the mixed form still needs a uniform grid with f0 a multiple of df. */
+int gwgpu_data_register_weighted(gwgpu_context *ctx, const char *detector, const double *frequencies, int length,
+                                 const double *data, const double *psd, const double *weights, int log10F,
+                                 int *handle);
 int gwgpu_data_release(gwgpu_context *ctx, int handle);
 
 /* ---- plain form: FP64, one request per launch (the drop-in) ---- */
@@ -100,6 +108,11 @@ int gwgpu_data_release(gwgpu_context *ctx, int handle);
  * std::string "SIMPSONS")  (mcmc_gw.h:276, mcmc_gw.cpp:801-873). */
 int gwgpu_log_likelihood_internal(gwgpu_context *ctx, const double *data, const double *psd,
                                   const double *frequencies, const double *response, int length, double *out);
+/* The "GAUSSLEG" branch of Log_Likelihood_internal (mcmc_gw.cpp:820-833,
+ * 843-862): weights[i], times frequencies[i] ln 10 when log10F. */
+int gwgpu_log_likelihood_internal_weighted(gwgpu_context *ctx, const double *data, const double *psd,
+                                           const double *frequencies, const double *weights, const double *response,
+                                           int length, int log10F, double *out);
 
 /* MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double>*, std::string
  * method, int* lengths, double** freqs, std::complex<double>** data, double** psd,

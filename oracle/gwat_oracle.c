@@ -1066,6 +1066,7 @@ static double simpsons_sum(double delta_x, int length, const double *x) { /* uti
 
 double gwo_log_likelihood_internal(const double *data, const double *psd, const double *freqs, const double *response,
                                    int length) { /* mcmc_gw.cpp:801-873, SIMPSONS */
+  if (length < 2) return 0.0;
   const double complex *d = (const double complex *)data, *r = (const double complex *)response;
   double delta_f = freqs[length / 2] - freqs[length / 2 - 1];
   double *integrand = (double *)malloc(sizeof(double) * (size_t)length);
@@ -1075,6 +1076,53 @@ double gwo_log_likelihood_internal(const double *data, const double *psd, const 
   double DH = 4. * simpsons_sum(delta_f, length, integrand);
   free(integrand);
   return -0.5 * (HH - 2 * DH);
+}
+
+/* GAUSSLEG branch of Log_Likelihood_internal (mcmc_gw.cpp:820-833, 843-862):
+ * integral = 4 sum_i w_i integrand_i, times f_i ln 10 when log10F. */
+static double gauss_sum(const double *w, const double *freqs, int log10F, int length, const double *x) {
+  double integral = 0;
+  if (log10F) {
+    for (int i = 0; i < length; i++) integral += w[i] * x[i] * freqs[i] * log(10.); /* LOG10, util.h:75 */
+  } else {
+    for (int i = 0; i < length; i++) integral += w[i] * x[i];
+  }
+  return integral * 4;
+}
+double gwo_log_likelihood_internal_gl(const double *data, const double *psd, const double *freqs,
+                                      const double *weights, const double *response, int length, int log10F) {
+  if (length < 1) return 0.0;
+  const double complex *d = (const double complex *)data, *r = (const double complex *)response;
+  double *integrand = (double *)malloc(sizeof(double) * (size_t)length);
+  for (int i = 0; i < length; i++) integrand[i] = creal(r[i] * conj(r[i])) / psd[i];
+  double HH = gauss_sum(weights, freqs, log10F, length, integrand);
+  for (int i = 0; i < length; i++) integrand[i] = creal(d[i] * conj(r[i])) / psd[i];
+  double DH = gauss_sum(weights, freqs, log10F, length, integrand);
+  free(integrand);
+  return -0.5 * (HH - 2 * DH);
+}
+
+double gwo_loglik_extrinsic_gl(const gwo_gen_params *pin, int approximant, double T_segment, const double *freqs,
+                               int length, int ndet, const int *dets, const double *const *data,
+                               const double *const *psd, const double *const *weights, int log10F) {
+  gwo_gen_params p = *pin;
+  p.tc = T_segment - p.tc; /* mcmc_gw.cpp:2466-2473 */
+  size_t n = (size_t)(length > 0 ? length : 1);
+  double complex *hp = (double complex *)malloc(sizeof(double complex) * n * 3);
+  double complex *hc = hp + n, *r = hc + n;
+  gwo_fourier_waveform(freqs, length, (double *)hp, (double *)hc, approximant, &p);
+  double ll = 0;
+  for (int i = 0; i < ndet; i++) {
+    double tc = -gwo_dtoa(p.RA, p.DEC, p.gmst, dets[0], dets[i]);
+    tc *= 2 * GWO_PI;
+    double fp, fc;
+    gwo_antenna(dets[i], p.RA, p.DEC, p.psi, p.gmst, &fp, &fc);
+    project(hp, hc, length, fp, fc, r);
+    for (int j = 0; j < length; j++) r[j] *= cexp(CMPLX(0, tc * freqs[j]));
+    ll += gwo_log_likelihood_internal_gl(data[i], psd[i], freqs, weights[i], (const double *)r, length, log10F);
+  }
+  free(hp);
+  return ll;
 }
 
 double gwo_loglik_extrinsic(const gwo_gen_params *pin, int approximant, double T_segment, const double *freqs,

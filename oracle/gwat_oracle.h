@@ -59,6 +59,14 @@ int gwo_fourier_detector_response(const double *freqs, int length, double *respo
 double gwo_log_likelihood_internal(const double *data, const double *psd, const double *freqs,
                                    const double *response, int length);
 
+/* The GAUSSLEG branch (mcmc_gw.cpp:820-833, 843-862): weights w_i, log10F
+ * multiplies each term by f_i ln 10. */
+double gwo_log_likelihood_internal_gl(const double *data, const double *psd, const double *freqs,
+                                      const double *weights, const double *response, int length, int log10F);
+double gwo_loglik_extrinsic_gl(const gwo_gen_params *p, int approximant, double T_segment, const double *freqs,
+                               int length, int ndet, const int *dets, const double *const *data,
+                               const double *const *psd, const double *const *weights, int log10F);
+
 /* MCMC_likelihood_extrinsic (mcmc_gw.cpp:2374-2487) with save_waveform=true.
  * T_segment is the value the reference forms at mcmc_gw.cpp:2466 before
  * t_c <- T_segment - t_c; p is copied, not mutated.  data/psd are per detector,

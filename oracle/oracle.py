@@ -85,6 +85,12 @@ def lib():
         L.gwo_loglik_extrinsic.argtypes = [gp, ctypes.c_int, ctypes.c_double, dp, ctypes.c_int, ctypes.c_int, ip,
                                            ctypes.POINTER(dp), ctypes.POINTER(dp)]
         L.gwo_loglik_extrinsic.restype = ctypes.c_double
+        L.gwo_log_likelihood_internal_gl.argtypes = [dp, dp, dp, dp, dp, ctypes.c_int, ctypes.c_int]
+        L.gwo_log_likelihood_internal_gl.restype = ctypes.c_double
+        L.gwo_loglik_extrinsic_gl.argtypes = [gp, ctypes.c_int, ctypes.c_double, dp, ctypes.c_int, ctypes.c_int, ip,
+                                              ctypes.POINTER(dp), ctypes.POINTER(dp), ctypes.POINTER(dp),
+                                              ctypes.c_int]
+        L.gwo_loglik_extrinsic_gl.restype = ctypes.c_double
         L.gwo_loglik_batch.argtypes = [gp, ctypes.c_int, ip, ctypes.c_double, dp, ctypes.c_int, ctypes.c_int, ip,
                                        ctypes.POINTER(dp), ctypes.POINTER(dp), dp, ctypes.c_int]
         L.gwo_mcmc_repack.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, gp]
@@ -177,6 +183,18 @@ def loglik(params, freqs, detectors, data, psd, approximant=IMRPhenomD, T_segmen
     psd = [np.ascontiguousarray(s, dtype=np.float64) for s in psd]
     return lib().gwo_loglik_extrinsic(ctypes.byref(params), approximant, T_segment, _dp(freqs), freqs.size,
                                       len(detectors), dets, _ptr_array(data), _ptr_array(psd))
+
+
+def loglik_gl(params, freqs, detectors, data, psd, weights, log10F=False, approximant=IMRPhenomD, T_segment=1.0):
+    """MCMC_likelihood_extrinsic with GAUSSLEG integration (weights per detector)."""
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    dets = (ctypes.c_int * len(detectors))(*[detector_index(d) for d in detectors])
+    data = [np.ascontiguousarray(d, dtype=np.complex128) for d in data]
+    psd = [np.ascontiguousarray(s, dtype=np.float64) for s in psd]
+    weights = [np.ascontiguousarray(w, dtype=np.float64) for w in weights]
+    return lib().gwo_loglik_extrinsic_gl(ctypes.byref(params), approximant, T_segment, _dp(freqs), freqs.size,
+                                         len(detectors), dets, _ptr_array(data), _ptr_array(psd),
+                                         _ptr_array(weights), int(log10F))
 
 
 def loglik_batch(params_list, freqs, detectors, data, psd, approximants=None, T_segment=None, nthreads=0):
