@@ -15,7 +15,7 @@ BUILDDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libgwgpu.so")
 DROPIN_SRC = os.path.join(HERE, "dropin", "gwat_dropin.cpp")
 DROPIN_LIB = os.path.join(LIBDIR, "libgwat_dropin.so")
-SOURCES = ["kernels.cu", "capi.cu", "batch.cu", "fisher.cu", "serve.cu", "noalloc.cu"]
+SOURCES = ["kernels.cu", "capi.cu", "batch.cu", "fisher.cu", "serve.cu", "noalloc.cu", "maxll.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
 
@@ -57,7 +57,7 @@ def build(force=False, verbose=False):
     with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(compile_one, srcs))
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cmd = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
@@ -133,6 +133,8 @@ def _declare(L):
                                          c_void_p, ip, P(ctypes.c_float)]),
         "gwgpu_mcmc_likelihood_extrinsic_noalloc": (c_int, [c_void_p, c_void_p, c_char_p, ip, c_int, c_double,
                                                             c_void_p, c_void_p]),
+        "gwgpu_maximized_log_likelihood_internal": (c_int, [c_void_p, dp, dp, dp, dp, c_int, dp]),
+        "gwgpu_maximized_loglik_batch": (c_int, [c_void_p, c_void_p, c_int, ip, c_int, dp, ip]),
     }
     for name, (res, args) in list(sig.items()) + list(optional.items()):
         fn = getattr(L, name, None)

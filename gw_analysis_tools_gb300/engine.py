@@ -178,6 +178,32 @@ class Context:
         self._check(st, "log_likelihood_internal")
         return out.value
 
+    def maximized_log_likelihood_internal(self, data, psd, freqs, response):
+        """maximized_Log_Likelihood_aligned_spin_internal (mcmc_gw.cpp:595-658)."""
+        d = np.ascontiguousarray(data, dtype=np.complex128)
+        s = np.ascontiguousarray(psd, dtype=np.float64)
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        r = np.ascontiguousarray(response, dtype=np.complex128)
+        out = ctypes.c_double()
+        st = self.lib.gwgpu_maximized_log_likelihood_internal(self.h, _dp(d), _dp(s), _dp(f), _dp(r), f.size,
+                                                              ctypes.byref(out))
+        self._check(st, "maximized_log_likelihood_internal")
+        return out.value
+
+    def maximized_loglik_batch(self, params, handles):
+        """The sampler's intrinsic mode over registered data (mcmc_gw.cpp:2611-2631)."""
+        parr = params if isinstance(params, ctypes.Array) else params_array(params)
+        n = len(parr)
+        hs = np.asarray(handles, dtype=np.int32)
+        if hs.ndim == 1:
+            hs = np.broadcast_to(hs, (n, hs.size))
+        hs = np.ascontiguousarray(hs, dtype=np.int32)
+        out = np.zeros(n)
+        status = np.zeros(n, dtype=np.int32)
+        st = self.lib.gwgpu_maximized_loglik_batch(self.h, parr, n, _ip(hs), hs.shape[1], _dp(out), _ip(status))
+        self._check(st, "maximized_loglik_batch")
+        return out, status
+
     def mcmc_likelihood_extrinsic(self, params, method, handles, T_segment):
         hs = np.ascontiguousarray(handles, dtype=np.int32)
         out = ctypes.c_double()

@@ -140,6 +140,23 @@ int gwgpu_mcmc_likelihood_extrinsic_noalloc(gwgpu_context *ctx, const gwgpu_gen_
                                             const char *generation_method, const int *handles,
                                             int num_detectors, double T_segment, double *d_loglik, void *stream);
 
+/* ---- likelihood maximised over arrival time and phase ---- */
+/* maximized_Log_Likelihood_aligned_spin_internal(std::complex<double>* data,
+ * double* psd, double* frequencies, std::complex<double>* response, size_t length,
+ * fftw_outline* plan)  (mcmc_gw.h, mcmc_gw.cpp:595-658): 1/2 max_t |DFT(4 d* r / S)|^2
+ * df^2 / HH, HH = 4 S(|r|^2 / S) by Simpson's rule.  Uniform grid. */
+int gwgpu_maximized_log_likelihood_internal(gwgpu_context *ctx, const double *data, const double *psd,
+                                            const double *frequencies, const double *response, int length,
+                                            double *out);
+/* The sampler's intrinsic mode (MCMC_likelihood_wrapper, mcmc_gw.cpp:2611-2631):
+ * for each request, IMRPhenomD with the extrinsic parameters fixed as there
+ * (horizon frame theta = phi = psi = 0, inclination 0, phiRef 1, f_ref 10,
+ * tc 1) and the maximised likelihood above summed over its detectors.  One
+ * grid length for the whole batch (handles[i*num_detectors + d]).  status[i]:
+ * GWGPU_OK or GWGPU_EDOMAIN. */
+int gwgpu_maximized_loglik_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, const int *handles,
+                                 int num_detectors, double *loglik, int *status);
+
 /* ---- batched form: n requests, one fused launch per step ---- */
 /* n independent MCMC_likelihood_extrinsic evaluations (the sampler calls
  * mcmc_step -> sampler->ll once per chain, mcmc_sampler_internals.cpp:98).

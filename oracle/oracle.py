@@ -197,6 +197,36 @@ def loglik_gl(params, freqs, detectors, data, psd, weights, log10F=False, approx
                                          _ptr_array(weights), int(log10F))
 
 
+def simpsons_sum(delta_x, x):
+    """util.h:844-856: (dx/3)[x0 + 4x1 + 2x2 + ... + x_{N-1}], the odd/even
+    pattern applied for any N."""
+    x = np.asarray(x, dtype=np.float64)
+    w = np.where(np.arange(x.size) % 2 == 0, 2.0, 4.0)
+    w[0] = w[-1] = 1.0
+    return float(np.sum(w * x) * delta_x / 3)
+
+
+def maximized_loglik_internal(data, psd, freqs, response):
+    """maximized_Log_Likelihood_aligned_spin_internal (mcmc_gw.cpp:595-658),
+    with numpy's DFT in place of FFTW's."""
+    freqs = np.asarray(freqs, dtype=np.float64)
+    n = freqs.size
+    delta_f = freqs[1] - freqs[0]
+    hh = 4.0 * simpsons_sum(delta_f, (response * np.conj(response)).real / psd)
+    g = 4.0 * np.conj(data) * response / psd
+    G = np.fft.fft(g)
+    return 0.5 * np.max(G.real ** 2 + G.imag ** 2) * delta_f * delta_f / hh
+
+
+def maximized_loglik_intrinsic(params_dict, freqs, data_list, psd_list):
+    """The sampler's intrinsic mode (mcmc_gw.cpp:2611-2631): IMRPhenomD with
+    the extrinsic parameters fixed (horizon frame theta = phi = psi = 0,
+    inclination 0: the response is h+), summed over detectors."""
+    d = dict(params_dict, RA=0.0, DEC=0.0, psi=0.0, phiRef=1.0, f_ref=10.0, incl_angle=0.0, tc=1.0)
+    hp, _ = fourier_waveform(freqs, params_from_dict(d), IMRPhenomD)
+    return sum(maximized_loglik_internal(dd, s, freqs, hp) for dd, s in zip(data_list, psd_list))
+
+
 def loglik_batch(params_list, freqs, detectors, data, psd, approximants=None, T_segment=None, nthreads=0):
     freqs = np.ascontiguousarray(freqs, dtype=np.float64)
     if T_segment is None:
