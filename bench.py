@@ -396,8 +396,24 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
                         "ok": int((fst == 0).sum())}
         ex["_fisher_sample"] = (pf, fish[:4].copy(), ff, psd_f)
 
+    def maximized():
+        # the sampler's intrinsic mode: likelihood maximised over t_c and phi_c
+        # (one batched FFT per step), IMRPhenomD and IMRPhenomPv2, same network
+        out = {}
+        for name, ap, draws in (("D", G.IMRPhenomD, host_params[1][:N_REQ]),
+                                ("Pv2", G.IMRPhenomPv2, W.prior_draws(N_REQ, 15, precessing=True))):
+            parr = G.params_array(draws)
+            ctx.maximized_loglik_batch(parr, handles, approximant=ap)
+            reps = 3
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                _, st = ctx.maximized_loglik_batch(parr, handles, approximant=ap)
+            dt = (time.perf_counter() - t0) / reps
+            out[name] = {"evals_per_s": N_REQ / dt, "ms_per_step": dt * 1e3, "ok": int((st == 0).sum())}
+        ex["maximized"] = dict(out, requests=N_REQ, bins=int(f.size), transforms_per_step=N_REQ * len(handles))
+
     for name, fn in (("plain", plain), ("batched_fp64", batched_fp64), ("served", served), ("uneven", uneven),
-                     ("fisher", fisher)):
+                     ("fisher", fisher), ("maximized", maximized)):
         log(name)
         try:
             fn()
@@ -562,7 +578,7 @@ def main():
     if ex:
         plain = ex.get("plain_fp64_evals_per_s")
         for k in ("plain_fp64_evals_per_s", "plain_fp64_p50_ms", "batched_fp64_evals_per_s", "served", "uneven_pv2",
-                  "errors"):
+                  "maximized", "errors"):
             if k in ex:
                 line[k] = ex[k]
         if plain:

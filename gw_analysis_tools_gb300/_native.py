@@ -134,7 +134,8 @@ def _declare(L):
         "gwgpu_mcmc_likelihood_extrinsic_noalloc": (c_int, [c_void_p, c_void_p, c_char_p, ip, c_int, c_double,
                                                             c_void_p, c_void_p]),
         "gwgpu_maximized_log_likelihood_internal": (c_int, [c_void_p, dp, dp, dp, dp, c_int, dp]),
-        "gwgpu_maximized_loglik_batch": (c_int, [c_void_p, c_void_p, c_int, ip, c_int, dp, ip]),
+        "gwgpu_maximized_log_likelihood_unaligned_internal": (c_int, [c_void_p, dp, dp, dp, dp, dp, c_int, dp]),
+        "gwgpu_maximized_loglik_batch": (c_int, [c_void_p, c_void_p, c_int, c_int, ip, c_int, dp, ip]),
     }
     for name, (res, args) in list(sig.items()) + list(optional.items()):
         fn = getattr(L, name, None)

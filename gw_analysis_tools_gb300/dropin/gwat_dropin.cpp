@@ -219,7 +219,40 @@ void fisher_numerical(double *frequency, int length, std::string generation_meth
     for (int j = 0; j < dimension; j++) output[i][j] = out[(size_t)i * dimension + j];
 }
 
+double maximized_Log_Likelihood_aligned_spin_internal(std::complex<double> *data, double *psd, double *frequencies,
+                                                      std::complex<double> *detector_response, size_t length,
+                                                      fftw_outline *plan) {
+  (void)plan;
+  double out = NAN;
+  gwgpu_maximized_log_likelihood_internal(engine().ctx, (const double *)data, psd, frequencies,
+                                          (const double *)detector_response, (int)length, &out);
+  return out;
+}
+
+double maximized_Log_Likelihood_unaligned_spin_internal(std::complex<double> *data, double *psd, double *frequencies,
+                                                        std::complex<double> *hplus, std::complex<double> *hcross,
+                                                        size_t length, fftw_outline *plan) {
+  (void)plan;
+  double out = NAN;
+  gwgpu_maximized_log_likelihood_unaligned_internal(engine().ctx, (const double *)data, psd, frequencies,
+                                                    (const double *)hplus, (const double *)hcross, (int)length,
+                                                    &out);
+  return out;
+}
+
 // ---- C entry points for the test suite (ctypes cannot call the C++ symbols)
+// The maximised likelihood through the reference signatures (hc null: aligned).
+extern "C" double gwat_dropin_test_maxll(const double *data, const double *psd, const double *f, const double *hp,
+                                         const double *hc, int N) {
+  auto *d = (std::complex<double> *)data;
+  auto *p = (std::complex<double> *)hp;
+  if (!hc)
+    return maximized_Log_Likelihood_aligned_spin_internal(d, const_cast<double *>(psd), const_cast<double *>(f), p,
+                                                          (size_t)N, nullptr);
+  return maximized_Log_Likelihood_unaligned_spin_internal(d, const_cast<double *>(psd), const_cast<double *>(f), p,
+                                                          (std::complex<double> *)hc, (size_t)N, nullptr);
+}
+
 extern "C" double gwat_dropin_test_loglik_gl(const double *f, int N, const double *const *data,
                                              const double *const *psd, const double *const *weights, int log10F,
                                              const char *const *dets, int ndet, const gwgpu_gen_params *pp,

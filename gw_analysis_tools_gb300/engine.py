@@ -190,8 +190,21 @@ class Context:
         self._check(st, "maximized_log_likelihood_internal")
         return out.value
 
-    def maximized_loglik_batch(self, params, handles):
-        """The sampler's intrinsic mode over registered data (mcmc_gw.cpp:2611-2631)."""
+    def maximized_log_likelihood_unaligned_internal(self, data, psd, freqs, hplus, hcross):
+        """maximized_Log_Likelihood_unaligned_spin_internal (mcmc_gw.cpp:660-800)."""
+        d = np.ascontiguousarray(data, dtype=np.complex128)
+        s = np.ascontiguousarray(psd, dtype=np.float64)
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        hp = np.ascontiguousarray(hplus, dtype=np.complex128)
+        hc = np.ascontiguousarray(hcross, dtype=np.complex128)
+        out = ctypes.c_double()
+        st = self.lib.gwgpu_maximized_log_likelihood_unaligned_internal(self.h, _dp(d), _dp(s), _dp(f), _dp(hp),
+                                                                        _dp(hc), f.size, ctypes.byref(out))
+        self._check(st, "maximized_log_likelihood_unaligned_internal")
+        return out.value
+
+    def maximized_loglik_batch(self, params, handles, approximant=IMRPhenomD):
+        """The sampler's intrinsic mode over registered data (mcmc_gw.cpp:2611-2720)."""
         parr = params if isinstance(params, ctypes.Array) else params_array(params)
         n = len(parr)
         hs = np.asarray(handles, dtype=np.int32)
@@ -200,7 +213,8 @@ class Context:
         hs = np.ascontiguousarray(hs, dtype=np.int32)
         out = np.zeros(n)
         status = np.zeros(n, dtype=np.int32)
-        st = self.lib.gwgpu_maximized_loglik_batch(self.h, parr, n, _ip(hs), hs.shape[1], _dp(out), _ip(status))
+        st = self.lib.gwgpu_maximized_loglik_batch(self.h, parr, n, approximant, _ip(hs), hs.shape[1], _dp(out),
+                                                   _ip(status))
         self._check(st, "maximized_loglik_batch")
         return out, status
 

@@ -32,6 +32,7 @@ template <class T>
 struct waveform_polarizations {
   std::complex<T> *hplus = nullptr, *hcross = nullptr;
 };
+struct fftw_outline;  // the reference's FFTW plan holder (util.h:90); unused here
 #endif
 
 // fourier_waveform (waveform_generator.h:43-49, waveform_generator.cpp:104)
@@ -57,6 +58,16 @@ double MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double> *pa
                                  std::complex<double> **data, double **psd, double **weights,
                                  std::string integration_method, bool log10F, std::string *detectors,
                                  int num_detectors);
+// maximized_Log_Likelihood_aligned_spin_internal (mcmc_gw.h:203-209,
+// mcmc_gw.cpp:595) and maximized_Log_Likelihood_unaligned_spin_internal
+// (mcmc_gw.h:219-226, mcmc_gw.cpp:660): the transform runs on the device, the
+// plan argument is not used
+double maximized_Log_Likelihood_aligned_spin_internal(std::complex<double> *data, double *psd, double *frequencies,
+                                                      std::complex<double> *detector_response, size_t length,
+                                                      fftw_outline *plan);
+double maximized_Log_Likelihood_unaligned_spin_internal(std::complex<double> *data, double *psd, double *frequencies,
+                                                        std::complex<double> *hplus, std::complex<double> *hcross,
+                                                        size_t length, fftw_outline *plan);
 // fisher_numerical (fisher.h:35-48, fisher.cpp:81): "IMRPhenomD" / "MCMC_IMRPhenomD"
 void fisher_numerical(double *frequency, int length, std::string generation_method, std::string detector,
                       std::string reference_detector, double **output, int dimension,

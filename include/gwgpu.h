@@ -148,14 +148,25 @@ int gwgpu_mcmc_likelihood_extrinsic_noalloc(gwgpu_context *ctx, const gwgpu_gen_
 int gwgpu_maximized_log_likelihood_internal(gwgpu_context *ctx, const double *data, const double *psd,
                                             const double *frequencies, const double *response, int length,
                                             double *out);
-/* The sampler's intrinsic mode (MCMC_likelihood_wrapper, mcmc_gw.cpp:2611-2631):
- * for each request, IMRPhenomD with the extrinsic parameters fixed as there
- * (horizon frame theta = phi = psi = 0, inclination 0, phiRef 1, f_ref 10,
- * tc 1) and the maximised likelihood above summed over its detectors.  One
- * grid length for the whole batch (handles[i*num_detectors + d]).  status[i]:
- * GWGPU_OK or GWGPU_EDOMAIN. */
-int gwgpu_maximized_loglik_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, const int *handles,
-                                 int num_detectors, double *loglik, int *status);
+/* maximized_Log_Likelihood_unaligned_spin_internal(std::complex<double>* data,
+ * double* psd, double* frequencies, std::complex<double>* hplus,
+ * std::complex<double>* hcross, size_t length, fftw_outline* plan)
+ * (mcmc_gw.cpp:660-800): the maximum over arrival time, phase and polarisation
+ * of 1/4 lambda built from the normalised h+ and hx transforms and their
+ * overlap.  Uniform grid. */
+int gwgpu_maximized_log_likelihood_unaligned_internal(gwgpu_context *ctx, const double *data, const double *psd,
+                                                      const double *frequencies, const double *hplus,
+                                                      const double *hcross, int length, double *out);
+/* The sampler's intrinsic mode (MCMC_likelihood_wrapper, mcmc_gw.cpp:2611-2720):
+ * for each request, the waveform with the extrinsic parameters fixed as there
+ * (horizon frame theta = phi = psi = 0, inclination 0, phiRef 1, tc 1; f_ref
+ * 10 for IMRPhenomD, 20 for IMRPhenomPv2), evaluated on the grid of the
+ * request's first detector, and summed over its detectors: the aligned form
+ * with r = h+ for GWGPU_IMRPHENOMD, the unaligned form for GWGPU_IMRPHENOMPV2.
+ * One grid length for the whole batch (handles[i*num_detectors + d]).
+ * status[i]: GWGPU_OK or GWGPU_EDOMAIN (loglik[i] NaN). */
+int gwgpu_maximized_loglik_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, int approximant,
+                                 const int *handles, int num_detectors, double *loglik, int *status);
 
 /* ---- batched form: n requests, one fused launch per step ---- */
 /* n independent MCMC_likelihood_extrinsic evaluations (the sampler calls

@@ -218,12 +218,37 @@ def maximized_loglik_internal(data, psd, freqs, response):
     return 0.5 * np.max(G.real ** 2 + G.imag ** 2) * delta_f * delta_f / hh
 
 
-def maximized_loglik_intrinsic(params_dict, freqs, data_list, psd_list):
-    """The sampler's intrinsic mode (mcmc_gw.cpp:2611-2631): IMRPhenomD with
+def maximized_loglik_unaligned_internal(data, psd, freqs, hplus, hcross):
+    """maximized_Log_Likelihood_unaligned_spin_internal (mcmc_gw.cpp:660-800),
+    with numpy's DFT in place of FFTW's."""
+    freqs = np.asarray(freqs, dtype=np.float64)
+    delta_f = freqs[1] - freqs[0]
+    hp_root = np.sqrt(4.0 * simpsons_sum(delta_f, (hplus * np.conj(hplus)).real / psd))
+    hc_root = np.sqrt(4.0 * simpsons_sum(delta_f, (hcross * np.conj(hcross)).real / psd))
+    hpn = hplus / hp_root
+    hcn = hcross / hc_root
+    rho_p = delta_f * np.fft.fft(4.0 * np.conj(data) * hpn / psd)
+    rho_c = delta_f * np.fft.fft(4.0 * np.conj(data) * hcn / psd)
+    rp2 = rho_p.real ** 2 + rho_p.imag ** 2
+    rc2 = rho_c.real ** 2 + rho_c.imag ** 2
+    gam = (rho_p * np.conj(rho_c)).real
+    ipc = 4.0 * simpsons_sum(delta_f, (hpn * np.conj(hcn)).real / psd)
+    lam = (rp2 + rc2 - 2 * gam * ipc + np.sqrt((rp2 - rc2) ** 2 + 4.0 * (ipc * rp2 - gam) * (ipc * rc2 - gam))) \
+        / (1.0 - ipc * ipc)
+    return 0.25 * np.max(lam)
+
+
+def maximized_loglik_intrinsic(params_dict, freqs, data_list, psd_list, approximant=IMRPhenomD):
+    """The sampler's intrinsic mode (mcmc_gw.cpp:2611-2720): the waveform with
     the extrinsic parameters fixed (horizon frame theta = phi = psi = 0,
-    inclination 0: the response is h+), summed over detectors."""
-    d = dict(params_dict, RA=0.0, DEC=0.0, psi=0.0, phiRef=1.0, f_ref=10.0, incl_angle=0.0, tc=1.0)
-    hp, _ = fourier_waveform(freqs, params_from_dict(d), IMRPhenomD)
+    inclination 0: F+ = 1, Fx = 0; f_ref 10 for IMRPhenomD, 20 for
+    IMRPhenomPv2), summed over detectors; IMRPhenomD uses the aligned form with
+    r = h+, IMRPhenomPv2 the unaligned form with h+ and hx."""
+    d = dict(params_dict, RA=0.0, DEC=0.0, psi=0.0, phiRef=1.0, incl_angle=0.0, tc=1.0,
+             f_ref=20.0 if approximant == IMRPhenomPv2 else 10.0)
+    hp, hc = fourier_waveform(freqs, params_from_dict(d), approximant)
+    if approximant == IMRPhenomPv2:
+        return sum(maximized_loglik_unaligned_internal(dd, s, freqs, hp, hc) for dd, s in zip(data_list, psd_list))
     return sum(maximized_loglik_internal(dd, s, freqs, hp) for dd, s in zip(data_list, psd_list))
 
 

@@ -42,5 +42,7 @@ def test_dropin_library_exports_reference_signatures():
     out = subprocess.run(["nm", "-DC", "--defined-only", _native.DROPIN_LIB], capture_output=True, text=True).stdout
     for name in ("MCMC_likelihood_extrinsic(bool, gen_params_base<double>*", "Log_Likelihood_internal(",
                  "fourier_waveform(double*, int, std::complex<double>*", "fourier_waveform<double>(",
-                 "fourier_detector_response<double>(", "fisher_numerical(double*, int"):
+                 "fourier_detector_response<double>(", "fisher_numerical(double*, int",
+                 "maximized_Log_Likelihood_aligned_spin_internal(std::complex<double>*",
+                 "maximized_Log_Likelihood_unaligned_spin_internal(std::complex<double>*"):
         assert name in out, name

@@ -42,3 +42,55 @@ def test_maximized_intrinsic_batch(gpu_ctx, oracle, setup):
     assert np.all(np.abs(out - ref) <= RTOL * np.maximum(1.0, np.abs(ref))), np.max(np.abs(out - ref) / np.abs(ref))
     # the injected source is the best of the draws
     assert np.argmax(out) == 0
+
+
+def test_maximized_unaligned_internal(gpu_ctx, oracle, setup):
+    s = setup
+    for d in W.prior_draws(5, 83, precessing=True):
+        hp, hc = oracle.fourier_waveform(s["f"], oracle.params_from_dict(d), oracle.IMRPhenomPv2)
+        ref = oracle.maximized_loglik_unaligned_internal(s["data"][0], s["psd"], s["f"], hp, hc)
+        got = gpu_ctx.maximized_log_likelihood_unaligned_internal(s["data"][0], s["psd"], s["f"], hp, hc)
+        assert abs(got - ref) <= RTOL * max(1.0, abs(ref)), (got, ref)
+
+
+def test_maximized_intrinsic_batch_pv2(gpu_ctx, oracle, setup):
+    s = setup
+    hs = [gpu_ctx.register_data(d, s["f"], s["data"][i], s["psd"]) for i, d in enumerate(s["dets"])]
+    draws = W.prior_draws(33, 84, precessing=True)
+    out, st = gpu_ctx.maximized_loglik_batch(G.params_array(draws), hs, approximant=G.IMRPhenomPv2)
+    assert np.all(st == 0)
+    ref = np.array([oracle.maximized_loglik_intrinsic(d, s["f"], s["data"], [s["psd"]] * 3, oracle.IMRPhenomPv2)
+                    for d in draws])
+    assert np.all(np.abs(out - ref) <= RTOL * np.maximum(1.0, np.abs(ref))), np.max(np.abs(out - ref) / np.abs(ref))
+
+
+def test_maximized_batch_bad_request(gpu_ctx, oracle, setup):
+    s = setup
+    hs = [gpu_ctx.register_data(d, s["f"], s["data"][i], s["psd"]) for i, d in enumerate(s["dets"])]
+    draws = W.prior_draws(3, 85)
+    draws[1] = dict(draws[1], mass1=float("nan"))   # outside the model domain
+    out, st = gpu_ctx.maximized_loglik_batch(G.params_array(draws), hs)
+    assert st[0] == 0 and st[2] == 0 and st[1] != 0
+    assert np.isnan(out[1]) and np.all(np.isfinite(out[[0, 2]]))
+
+
+def test_maximized_through_reference_signatures(oracle, setup):
+    """maximized_Log_Likelihood_{aligned,unaligned}_spin_internal of the C++
+    drop-in (the reference's argument lists; the FFTW plan argument unused)."""
+    import ctypes
+    from gw_analysis_tools_gb300 import _native
+    _native.build()
+    L = ctypes.CDLL(_native.DROPIN_LIB)
+    fn = L.gwat_dropin_test_maxll
+    fn.restype = ctypes.c_double
+    fn.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int]
+    s = setup
+    d = W.prior_draws(1, 86, precessing=True)[0]
+    hp, hc = oracle.fourier_waveform(s["f"], oracle.params_from_dict(d), oracle.IMRPhenomPv2)
+    hp, hc = np.ascontiguousarray(hp), np.ascontiguousarray(hc)
+    data, psd, f = s["data"][2], s["psd"], s["f"]
+    got_a = fn(data.ctypes.data, psd.ctypes.data, f.ctypes.data, hp.ctypes.data, None, f.size)
+    got_u = fn(data.ctypes.data, psd.ctypes.data, f.ctypes.data, hp.ctypes.data, hc.ctypes.data, f.size)
+    ref_a = oracle.maximized_loglik_internal(data, psd, f, hp)
+    ref_u = oracle.maximized_loglik_unaligned_internal(data, psd, f, hp, hc)
+    assert abs(got_a - ref_a) <= RTOL * abs(ref_a) and abs(got_u - ref_u) <= RTOL * abs(ref_u)
