@@ -412,8 +412,49 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
             out[name] = {"evals_per_s": N_REQ / dt, "ms_per_step": dt * 1e3, "ok": int((st == 0).sum())}
         ex["maximized"] = dict(out, requests=N_REQ, bins=int(f.size), transforms_per_step=N_REQ * len(handles))
 
+    def ingest():
+        # strain text files (GWOSC layout, 3 detectors x 128 s x 4096 Hz) and a
+        # PSD table (T_obs 32 s) -> windowed, transformed, band-limited spectra
+        import tempfile
+        fs_i, dur_i, t0_i, nd_i = 4096, 128, 1126259446, 3
+        rng = np.random.default_rng(17)
+        tmp = tempfile.mkdtemp(prefix="gwgpu_ingest_")
+        files, nbytes = [], 0
+        series = rng.normal(0, 1e-21, (nd_i, fs_i * dur_i))
+        for d in range(nd_i):
+            p = os.path.join(tmp, "strain%d.txt" % d)
+            with open(p, "w") as fh:
+                fh.write("# synthetic strain\n# This file has %d samples per second\n# starting GPS %d duration %d\n"
+                         % (fs_i, t0_i, dur_i))
+                fh.write("\n".join(map(repr, series[d].tolist())) + "\n")
+            nbytes += os.path.getsize(p)
+            files.append(p)
+        fpsd = np.arange(20.0, 2048.0, 1.0 / 32)
+        psd_path = os.path.join(tmp, "psd.txt")
+        with open(psd_path, "w") as fh:
+            fh.write("# freq H1 L1 V1\n")
+            fh.write("".join("%r %r %r %r\n" % (x, 1e-46, 1e-46, 2e-46) for x in fpsd.tolist()))
+        npsd = G.count_lines_losc_psd_file(psd_path)
+        ndata = G.count_lines_losc_data_file(files[0])
+        ctx.allocate_losc_data(files, psd_path, npsd, ndata, t0_i + 64.0, 2.0)  # warm-up (plans)
+        t0 = time.perf_counter()
+        ctx.allocate_losc_data(files, psd_path, npsd, ndata, t0_i + 64.0, 2.0)
+        t_files = time.perf_counter() - t0
+        tab = np.column_stack([fpsd] + [np.full(fpsd.size, 1e-46)] * nd_i)
+        t0 = time.perf_counter()
+        reps = 5
+        for _ in range(reps):
+            ctx.losc_prepare(series, float(t0_i), float(dur_i), float(fs_i), tab, t0_i + 64.0, 2.0)
+        t_mem = (time.perf_counter() - t0) / reps
+        ex["ingest"] = {"detectors": nd_i, "samples_per_detector": fs_i * dur_i, "text_bytes": nbytes,
+                        "files_to_spectra_s": t_files, "text_mb_per_s": nbytes / t_files / 1e6,
+                        "transform_from_memory_ms": t_mem * 1e3, "bins": int(npsd), "host_threads": os.cpu_count()}
+        for p in files + [psd_path]:
+            os.remove(p)
+        os.rmdir(tmp)
+
     for name, fn in (("plain", plain), ("batched_fp64", batched_fp64), ("served", served), ("uneven", uneven),
-                     ("fisher", fisher), ("maximized", maximized)):
+                     ("fisher", fisher), ("maximized", maximized), ("ingest", ingest)):
         log(name)
         try:
             fn()
@@ -578,7 +619,7 @@ def main():
     if ex:
         plain = ex.get("plain_fp64_evals_per_s")
         for k in ("plain_fp64_evals_per_s", "plain_fp64_p50_ms", "batched_fp64_evals_per_s", "served", "uneven_pv2",
-                  "maximized", "errors"):
+                  "maximized", "ingest", "errors"):
             if k in ex:
                 line[k] = ex[k]
         if plain:

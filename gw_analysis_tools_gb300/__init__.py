@@ -6,7 +6,9 @@ log-likelihood, plus the numerical Fisher matrix, as sm_103a CUDA kernels
 behind a C ABI (include/gwgpu.h).  See engine.Context.
 """
 from .engine import (IMRPhenomD, IMRPhenomPv2, PREC_FP64, PREC_MIXED, Context, GenParams, GwGpuError, Server,
-                     gen_params, params_array)
+                     count_lines_data_file, count_lines_losc_data_file, count_lines_losc_psd_file, gen_params,
+                     params_array, populate_noise, read_losc_data_file, read_losc_psd_file)
 
 __all__ = ["Context", "Server", "GenParams", "gen_params", "params_array", "GwGpuError", "IMRPhenomD",
-           "IMRPhenomPv2", "PREC_FP64", "PREC_MIXED"]
+           "IMRPhenomPv2", "PREC_FP64", "PREC_MIXED", "count_lines_data_file", "count_lines_losc_data_file",
+           "count_lines_losc_psd_file", "read_losc_data_file", "read_losc_psd_file", "populate_noise"]

@@ -15,9 +15,10 @@ BUILDDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libgwgpu.so")
 DROPIN_SRC = os.path.join(HERE, "dropin", "gwat_dropin.cpp")
 DROPIN_LIB = os.path.join(LIBDIR, "libgwat_dropin.so")
-SOURCES = ["kernels.cu", "capi.cu", "batch.cu", "fisher.cu", "serve.cu", "noalloc.cu", "maxll.cu"]
+SOURCES = ["kernels.cu", "capi.cu", "batch.cu", "fisher.cu", "serve.cu", "noalloc.cu", "maxll.cu", "cufft_rt.cu", "ingest.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
+# host code: no multiply-add contraction, so that it rounds the same on x86 and Arm hosts
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "--expt-relaxed-constexpr"]
 
 
 def _nvcc():
@@ -71,7 +72,8 @@ def build_dropin(force=False):
     newest = max(os.path.getmtime(x) for x in (DROPIN_SRC, hdr, LIB))
     if not force and os.path.exists(DROPIN_LIB) and os.path.getmtime(DROPIN_LIB) >= newest:
         return DROPIN_LIB
-    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", DROPIN_SRC, "-o", DROPIN_LIB,
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-ffp-contract=off", "-std=c++17", "-fPIC", "-shared", DROPIN_SRC,
+           "-o", DROPIN_LIB,
            "-L" + LIBDIR, "-lgwgpu", "-Wl,-rpath,$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -91,6 +93,8 @@ def _declare(L):
     P = ctypes.POINTER
     dp = P(c_double)
     ip = P(c_int)
+    c_longlong = ctypes.c_longlong
+    llp = P(c_longlong)
     sig = {
         "gwgpu_default_params": (None, [c_void_p]),
         "gwgpu_status_string": (c_char_p, [c_int]),
@@ -134,6 +138,16 @@ def _declare(L):
         "gwgpu_mcmc_likelihood_extrinsic_noalloc": (c_int, [c_void_p, c_void_p, c_char_p, ip, c_int, c_double,
                                                             c_void_p, c_void_p]),
         "gwgpu_maximized_log_likelihood_internal": (c_int, [c_void_p, dp, dp, dp, dp, c_int, dp]),
+        "gwgpu_count_lines_data_file": (c_int, [c_char_p, ip]),
+        "gwgpu_count_lines_losc_data_file": (c_int, [c_char_p, ip]),
+        "gwgpu_count_lines_losc_psd_file": (c_int, [c_char_p, ip]),
+        "gwgpu_read_losc_data_file": (c_int, [c_char_p, dp, c_longlong, llp, dp, dp, dp]),
+        "gwgpu_read_losc_psd_file": (c_int, [c_char_p, dp, c_int, c_int]),
+        "gwgpu_populate_noise": (c_int, [dp, c_char_p, dp, c_int, c_double, c_char_p]),
+        "gwgpu_losc_prepare": (c_int, [c_void_p, dp, c_int, c_longlong, c_double, c_double, c_double, dp, c_int,
+                                       c_double, c_double, dp, dp, dp, ip]),
+        "gwgpu_allocate_losc_data": (c_int, [c_void_p, c_void_p, c_char_p, c_int, c_int, c_int, c_double, c_double,
+                                             dp, dp, dp]),
         "gwgpu_maximized_log_likelihood_unaligned_internal": (c_int, [c_void_p, dp, dp, dp, dp, dp, c_int, dp]),
         "gwgpu_maximized_loglik_batch": (c_int, [c_void_p, c_void_p, c_int, c_int, ip, c_int, dp, ip]),
     }

@@ -18,6 +18,7 @@
 
 #include "../../include/gwgpu.h"
 #include "capi_internal.h"
+#include "cufft_rt.h"
 #include "kernels.h"
 
 using gwk::StreamDev;
@@ -259,6 +260,7 @@ int gwgpu_context_destroy(gwgpu_context *c) {
   if (!c) return GWGPU_EINVAL;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  gwfft::release(c);
   for (auto &kv : c->sizes) cudaFree(kv.first);
   for (auto &w : c->hws)
     if (w.second.ptr) cudaFreeHost(w.second.ptr);

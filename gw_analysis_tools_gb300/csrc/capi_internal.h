@@ -25,7 +25,7 @@ struct gwgpu_context {
     std::vector<double> host_freqs;
     uint64_t psd_hash = 0;  // FNV-1a of the PSD bytes: detectors with equal PSDs share weights
   };
-  enum { kWsWave = 0, kWsInner, kWsPlain, kWsBatch, kWsBatchItems, kWsFisher, kWsServe, kWsMaxll };
+  enum { kWsWave = 0, kWsInner, kWsPlain, kWsBatch, kWsBatchItems, kWsFisher, kWsServe, kWsMaxll, kWsIngest, kWsChirp };
   enum { kHwsPlain = 0, kHwsBatch, kHwsFisher, kHwsInner };
 
   int device = 0;
@@ -49,6 +49,7 @@ struct gwgpu_context {
   std::map<std::string, int> tuned;  // autotuned tile per (precision, detectors, grid length)
   int tile_override = 0;
   bool use_graphs = true;
+  int chirp_n = 0;                 // grid length whose Bluestein kernel the kWsChirp workspace holds
   bool prologue_serial = false;    // batched prologue: one thread per request instead of the cooperative kernel
   uint64_t streams_epoch = 0;      // bumped when the device stream table changes
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;

@@ -1,18 +1,27 @@
 // maxll.cu -- the likelihood maximised over arrival time and phase,
-// maximized_Log_Likelihood_aligned_spin_internal (mcmc_gw.cpp:595-658), and
-// the sampler's intrinsic mode that sums it over detectors
-// (MCMC_likelihood_wrapper, mcmc_gw.cpp:2611-2631).
+// maximized_Log_Likelihood_aligned_spin_internal (mcmc_gw.cpp:595-658) and
+// maximized_Log_Likelihood_unaligned_spin_internal (:660-800), and the
+// sampler's intrinsic mode that sums them over detectors
+// (MCMC_likelihood_wrapper, mcmc_gw.cpp:2611-2720).
 //
 // Per (request, detector): HH = 4 S(|r|^2 / S_n) by Simpson's rule,
-// g_k = 4 conj(d_k) r_k / S_n,k, G = DFT(g), and
+// g_k = 4 conj(d_k) r_k / S_n,k, G = DFT_N(g), and
 // log L = 1/2 max_j |G_j|^2 df^2 / HH.  The products and sums are fused in
-// hand-written kernels (FP64); the length-N transforms of all pairs run as one
-// batched cuFFT double-complex plan (a library transform, loaded at run time
-// so that the engine builds and runs without it: the entry points then return
-// GWGPU_ECUDA with a message).
+// hand-written FP64 kernels; the transforms of all pairs run as batched cuFFT
+// double-complex plans (cufft_rt.h).
+//
+// Grid lengths N with a prime factor above 7 (32128 = 2^7 * 251 is typical)
+// use Bluestein's identity nk = (n^2 + k^2 - (k - n)^2) / 2 with power-of-two
+// transforms of length M >= 2N - 1:
+//   G_k = e^{-i pi k^2/N} sum_n [g_n e^{-i pi n^2/N}] e^{i pi (k-n)^2/N},
+// a cyclic convolution of a_n = g_n e^{-i pi n^2/N} with b_m = e^{i pi m^2/N}
+// (FFT_M, a pointwise product with the transform of b, inverse FFT_M).  The
+// outer factor e^{-i pi k^2/N} is never applied: every quantity taken from G
+// (|G_k|^2, Re(G+_k conj(Gx_k))) is invariant to a phase common to the pair.
+// The chirp phases use n^2 mod 2N in integers, so they are exact to FP64.
 #include <cuda_runtime.h>
-#include <dlfcn.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -22,6 +31,7 @@
 
 #include "../../include/gwgpu.h"
 #include "capi_internal.h"
+#include "cufft_rt.h"
 #include "kernels.h"
 
 namespace {
@@ -29,139 +39,120 @@ namespace {
 using gwk::StreamDev;
 using gwt::Request;
 
-// ------------------------------------------------------------- cuFFT loader
-struct CuFft {
-  typedef int (*PlanMany)(int *, int, int *, int *, int, int, int *, int, int, int, int);
-  typedef int (*ExecZ2Z)(int, void *, void *, int);
-  typedef int (*SetStream)(int, cudaStream_t);
-  typedef int (*Destroy)(int);
-  void *lib = nullptr;
-  PlanMany plan_many = nullptr;
-  ExecZ2Z exec_z2z = nullptr;
-  SetStream set_stream = nullptr;
-  Destroy destroy = nullptr;
-  bool ok = false;
-};
-constexpr int kCufftZ2Z = 0x69, kCufftForward = -1;  // cufftType CUFFT_Z2Z, CUFFT_FORWARD
-
-CuFft &cufft() {
-  static CuFft f;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    const char *names[] = {"libcufft.so.12", "libcufft.so.13", "libcufft.so", "/usr/local/cuda/lib64/libcufft.so.12",
-                           "/usr/local/cuda/lib64/libcufft.so"};
-    for (const char *nm : names)
-      if ((f.lib = dlopen(nm, RTLD_NOW | RTLD_LOCAL))) break;
-    if (!f.lib) return;
-    f.plan_many = (CuFft::PlanMany)dlsym(f.lib, "cufftPlanMany");
-    f.exec_z2z = (CuFft::ExecZ2Z)dlsym(f.lib, "cufftExecZ2Z");
-    f.set_stream = (CuFft::SetStream)dlsym(f.lib, "cufftSetStream");
-    f.destroy = (CuFft::Destroy)dlsym(f.lib, "cufftDestroy");
-    f.ok = f.plan_many && f.exec_z2z && f.set_stream && f.destroy;
-  });
-  return f;
-}
-
-// One plan per (length, batch) and context, kept for reuse.
-struct Plans {
-  std::map<std::pair<int, int>, int> plans;
-};
-std::mutex g_plans_mu;
-std::map<gwgpu_context *, Plans> g_plans;
-
-int plan_for(gwgpu_context *c, int N, int batch, int *plan) {
-  CuFft &f = cufft();
-  if (!f.ok) {
-    c->last_error = "cuFFT library not found";
-    return GWGPU_ECUDA;
-  }
-  std::lock_guard<std::mutex> lk(g_plans_mu);
-  auto &m = g_plans[c].plans;
-  auto it = m.find({N, batch});
-  if (it != m.end()) {
-    *plan = it->second;
-    return GWGPU_OK;
-  }
-  int p = 0, n = N;
-  if (f.plan_many(&p, 1, &n, nullptr, 1, N, nullptr, 1, N, kCufftZ2Z, batch) != 0) {
-    c->last_error = "cuFFT plan";
-    return GWGPU_ECUDA;
-  }
-  m[{N, batch}] = p;
-  *plan = p;
-  return GWGPU_OK;
-}
-
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
 
+// e^{sign i pi m^2 / N}, the phase reduced exactly (m^2 mod 2N in integers).
+__device__ __forceinline__ double2 chirp(long long m, int N, double sign) {
+  const long long t = (m * m) % (2LL * N);
+  double sn, cs;
+  sincospi((double)t / (double)N, &sn, &cs);
+  return make_double2(cs, sign * sn);
+}
+
 // ------------------------------------------------------------------ kernels
-// Pair q = blockIdx.y is (request q / ndet, detector q % ndet).
+// Block (x, r): bins x*256.. of request r, for each of its detectors d (pair
+// q = r*ndet + d); rows of g have stride ld (N, or M for Bluestein, the bins
+// N..M-1 zero).  The waveform is evaluated once per bin and request, on the
+// grid of the request's first detector (the reference evaluates it once on
+// local_freqs[0], mcmc_gw.cpp:2651-2653, 2697-2701).
 //
-// Aligned (UN = false): g = 4 conj(d) h / S into g[q], and the block partial
+// Aligned (UN = false): g = 4 conj(d) h / S into row q, and the block partial
 // sums of w_k |h|^2 / S (Simpson weights w).  h is the model's h+ (the
 // horizon frame at theta = phi = psi = 0 and inclination 0 that the sampler's
-// intrinsic mode uses gives F+ = 1, Fx = 0), or a given response.
-// Unaligned (UN = true): the same for h+ and hx into g[2q] and g[2q+1], and
+// intrinsic mode uses gives F+ = 1, Fx = 0), or a given response per pair.
+// Unaligned (UN = true): the same for h+ and hx into rows 2q and 2q+1, and
 // partial sums of |h+|^2/S, |hx|^2/S and Re(h+ conj(hx))/S.  The
 // normalisation by sqrt(<h+|h+>) and sqrt(<hx|hx>) is applied after the
-// transform (it is linear).
-// The waveform of request r is evaluated on the grid of its first detector
-// (the reference evaluates it once on local_freqs[0], mcmc_gw.cpp:2651-2653,
-// 2697-2701).
+// transform (it is linear).  With Bluestein, g is multiplied by
+// e^{-i pi k^2/N}.
 template <bool UN>
 __global__ void k_maxll_prep(const Request *__restrict__ req, const double2 *__restrict__ resp_p,
                              const double2 *__restrict__ resp_c, int ndet, const StreamDev *__restrict__ streams,
-                             const int *__restrict__ handles, int N, double2 *__restrict__ g,
+                             const int *__restrict__ handles, int N, int ld, int blue, double2 *__restrict__ g,
                              double *__restrict__ part) {
   constexpr int NS = UN ? 3 : 1, NP = UN ? 2 : 1;
   __shared__ double s_red[NS][kWarps];
-  const int q = blockIdx.y, r = q / ndet;
-  const StreamDev &st = streams[handles[q]];
+  const int r = blockIdx.y;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[NS];
+  // a request outside the model domain contributes zeros (its result is NaN)
+  double2 hp = make_double2(0.0, 0.0), hc = make_double2(0.0, 0.0);
+  if (req && k < N && !req[r].m.status) {
+    gwt::cd p, c;
+    gwt::wave_bin(req[r], streams[handles[(size_t)r * ndet]].freqs[k], p, c);
+    hp = make_double2(p.re, p.im);
+    hc = make_double2(c.re, c.im);
+  }
+  const double2 ch = (blue && k < N) ? chirp(k, N, -1.0) : make_double2(1.0, 0.0);
+  for (int dd = 0; dd < ndet; dd++) {
+    const int q = r * ndet + dd;
+    const StreamDev &st = streams[handles[q]];
+    double acc[NS];
 #pragma unroll
-  for (int j = 0; j < NS; j++) acc[j] = 0.0;
-  if (k < N) {
-    // a request outside the model domain contributes zeros (its result is NaN)
-    double2 hp = make_double2(0.0, 0.0), hc = make_double2(0.0, 0.0);
-    if (req) {
-      if (!req[r].m.status) {
-        gwt::cd p, c;
-        gwt::wave_bin(req[r], streams[handles[(size_t)r * ndet]].freqs[k], p, c);
-        hp = make_double2(p.re, p.im);
-        hc = make_double2(c.re, c.im);
+    for (int j = 0; j < NS; j++) acc[j] = 0.0;
+    if (k < N) {
+      if (!req) {
+        hp = resp_p[(size_t)q * N + k];
+        if (UN) hc = resp_c[(size_t)q * N + k];
       }
-    } else {
-      hp = resp_p[(size_t)q * N + k];
-      if (UN) hc = resp_c[(size_t)q * N + k];
+      const double2 d = ((const double2 *)st.data)[k];
+      const double S = st.psd[k], w = gwt::simpson_weight(k, N);
+      // 4 conj(d) h / S, then the Bluestein chirp
+      double2 v = make_double2(4.0 * (d.x * hp.x + d.y * hp.y) / S, 4.0 * (d.x * hp.y - d.y * hp.x) / S);
+      g[((size_t)q * NP) * ld + k] = make_double2(v.x * ch.x - v.y * ch.y, v.x * ch.y + v.y * ch.x);
+      acc[0] = w * ((hp.x * hp.x + hp.y * hp.y) / S);
+      if (UN) {
+        v = make_double2(4.0 * (d.x * hc.x + d.y * hc.y) / S, 4.0 * (d.x * hc.y - d.y * hc.x) / S);
+        g[((size_t)q * NP + 1) * ld + k] = make_double2(v.x * ch.x - v.y * ch.y, v.x * ch.y + v.y * ch.x);
+        acc[1] = w * ((hc.x * hc.x + hc.y * hc.y) / S);
+        acc[2] = w * ((hp.x * hc.x + hp.y * hc.y) / S);
+      }
+    } else if (k < ld) {
+      g[((size_t)q * NP) * ld + k] = make_double2(0.0, 0.0);
+      if (UN) g[((size_t)q * NP + 1) * ld + k] = make_double2(0.0, 0.0);
     }
-    const double2 d = ((const double2 *)st.data)[k];
-    const double S = st.psd[k], w = gwt::simpson_weight(k, N);
-    // 4 conj(d) h / S
-    g[((size_t)q * NP) * N + k] =
-        make_double2(4.0 * (d.x * hp.x + d.y * hp.y) / S, 4.0 * (d.x * hp.y - d.y * hp.x) / S);
-    acc[0] = w * ((hp.x * hp.x + hp.y * hp.y) / S);
-    if (UN) {
-      g[((size_t)q * NP + 1) * N + k] =
-          make_double2(4.0 * (d.x * hc.x + d.y * hc.y) / S, 4.0 * (d.x * hc.y - d.y * hc.x) / S);
-      acc[1] = w * ((hc.x * hc.x + hc.y * hc.y) / S);
-      acc[2] = w * ((hp.x * hc.x + hp.y * hc.y) / S);
+#pragma unroll
+    for (int j = 0; j < NS; j++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+    }
+    __syncthreads();  // the previous detector's partials have been read
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+      for (int j = 0; j < NS; j++) s_red[j][threadIdx.x >> 5] = acc[j];
+    __syncthreads();
+    if (threadIdx.x < NS) {
+      double t = 0.0;
+      for (int w = 0; w < kWarps; w++) t += s_red[threadIdx.x][w];
+      part[((size_t)q * NS + threadIdx.x) * gridDim.x + blockIdx.x] = t;
     }
   }
-#pragma unroll
-  for (int j = 0; j < NS; j++) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+}
+
+// The Bluestein kernel: B = FFT_M(b) / M is made from b_m = e^{i pi m^2/N} at
+// index m (0 <= m < N) and M - m (0 < m < N), zero elsewhere.
+__global__ void k_chirp_fill(double2 *__restrict__ b, int N, int M) {
+  const double inv = 1.0 / (double)M;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+    long long m = -1;
+    if (i < N) m = i;
+    else if (i > M - N) m = M - i;
+    double2 v = make_double2(0.0, 0.0);
+    if (m >= 0) {
+      v = chirp(m, N, 1.0);
+      v.x *= inv;
+      v.y *= inv;
+    }
+    b[i] = v;
   }
-  if ((threadIdx.x & 31) == 0)
-#pragma unroll
-    for (int j = 0; j < NS; j++) s_red[j][threadIdx.x >> 5] = acc[j];
-  __syncthreads();
-  if (threadIdx.x < NS) {
-    double t = 0.0;
-    for (int w = 0; w < kWarps; w++) t += s_red[threadIdx.x][w];
-    part[((size_t)q * NS + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+}
+
+// g[row][i] *= B[i] over all rows (the convolution's pointwise product).
+__global__ void k_chirp_mul(double2 *__restrict__ g, const double2 *__restrict__ B, int M, long long total) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double2 a = g[i], c = B[i % M];
+    g[i] = make_double2(a.x * c.x - a.y * c.y, a.x * c.y + a.y * c.x);
   }
 }
 
@@ -178,8 +169,8 @@ __device__ double block_sum(double v, double *s_tmp) {
 }
 
 // One block per pair: the Simpson sums from the partials, then the maximum
-// over the transform and log L of the pair; the last block of each request
-// sums its detectors in order.
+// over the transform (rows of stride ld, the first N entries) and log L of the
+// pair; the last block of each request sums its detectors in order.
 //   aligned   (mcmc_gw.cpp:595-658): 1/2 max|G|^2 df^2 / <h|h>
 //   unaligned (mcmc_gw.cpp:660-800): 1/4 max lambda, with
 //     rho+ = df G+ / sqrt(<h+|h+>), rhox = df Gx / sqrt(<hx|hx>),
@@ -188,9 +179,10 @@ __device__ double block_sum(double v, double *s_tmp) {
 //              + 4 (I |rho+|^2 - gamma)(I |rhox|^2 - gamma))) / (1 - I^2).
 template <bool UN>
 __global__ void k_maxll_reduce(const double2 *__restrict__ G, const double *__restrict__ part, int nblk, int N,
-                               int ndet, const StreamDev *__restrict__ streams, const int *__restrict__ handles,
-                               const int *__restrict__ req_status, double *__restrict__ ll_pair,
-                               unsigned *__restrict__ done, double *__restrict__ out, int *__restrict__ status) {
+                               int ld, int ndet, const StreamDev *__restrict__ streams,
+                               const int *__restrict__ handles, const int *__restrict__ req_status,
+                               double *__restrict__ ll_pair, unsigned *__restrict__ done, double *__restrict__ out,
+                               int *__restrict__ status) {
   constexpr int NS = UN ? 3 : 1, NP = UN ? 2 : 1;
   __shared__ double s_tmp[kWarps];
   __shared__ bool s_last;
@@ -207,7 +199,7 @@ __global__ void k_maxll_reduce(const double2 *__restrict__ G, const double *__re
   double m = 0.0;
   if (!UN) {
     for (int k = threadIdx.x; k < N; k += blockDim.x) {
-      const double2 v = G[(size_t)q * N + k];
+      const double2 v = G[(size_t)q * ld + k];
       m = fmax(m, v.x * v.x + v.y * v.y);
     }
   } else {
@@ -215,7 +207,7 @@ __global__ void k_maxll_reduce(const double2 *__restrict__ G, const double *__re
     const double I = sums[2] / (sqrt(sums[0]) * sqrt(sums[1]));
     m = -HUGE_VAL;
     for (int k = threadIdx.x; k < N; k += blockDim.x) {
-      const double2 a = G[((size_t)q * NP) * N + k], c = G[((size_t)q * NP + 1) * N + k];
+      const double2 a = G[((size_t)q * NP) * ld + k], c = G[((size_t)q * NP + 1) * ld + k];
       const double rpx = ap * a.x, rpy = ap * a.y, rcx = ac * c.x, rcy = ac * c.y;
       const double p2 = rpx * rpx + rpy * rpy, c2 = rcx * rcx + rcy * rcy;
       const double gam = rpx * rcx + rpy * rcy;
@@ -249,6 +241,54 @@ __global__ void k_maxll_reduce(const double2 *__restrict__ G, const double *__re
 
 size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// ------------------------------------------------------------ the transform
+// Length-N DFTs of `rows` rows: cuFFT directly when N has no prime factor
+// above 7, else Bluestein with a power-of-two M (the kernel B cached in the
+// context per N).
+struct Xform {
+  int N = 0, ld = 0, blue = 0, plan = 0;
+  const double2 *B = nullptr;
+};
+
+bool smooth7(int n) {
+  for (int p : {2, 3, 5, 7})
+    while (n % p == 0) n /= p;
+  return n == 1;
+}
+
+int xform_setup(gwgpu_context *c, int N, int rows, Xform &x) {
+  x.N = N;
+  x.blue = !smooth7(N);
+  x.ld = N;
+  if (x.blue) {
+    x.ld = 1;
+    while (x.ld < 2 * N - 1) x.ld <<= 1;
+  }
+  int st = gwfft::plan(c, gwfft::kZ2Z, x.ld, rows, &x.plan);
+  if (st || !x.blue) return st;
+  void *kb;
+  if ((st = c->workspace(gwgpu_context::kWsChirp, 16 * (size_t)x.ld, &kb))) return st;
+  x.B = (const double2 *)kb;
+  if (c->chirp_n != N) {
+    int p1;
+    if ((st = gwfft::plan(c, gwfft::kZ2Z, x.ld, 1, &p1))) return st;
+    const int gb = std::min((x.ld + kBlock - 1) / kBlock, 1024);
+    k_chirp_fill<<<gb, kBlock, 0, c->stream>>>((double2 *)kb, N, x.ld);
+    if ((st = gwfft::exec_z2z(c, p1, (double2 *)kb, (double2 *)kb, gwfft::kForward, c->stream))) return st;
+    c->chirp_n = N;
+  }
+  return GWGPU_OK;
+}
+
+int xform_run(gwgpu_context *c, const Xform &x, double2 *g, int rows) {
+  int st = gwfft::exec_z2z(c, x.plan, g, g, gwfft::kForward, c->stream);
+  if (st || !x.blue) return st;
+  const long long total = (long long)rows * x.ld;
+  const int gb = (int)std::min<long long>((total + kBlock - 1) / kBlock, 152 * 16);
+  k_chirp_mul<<<gb, kBlock, 0, c->stream>>>(g, x.B, x.ld, total);
+  return gwfft::exec_z2z(c, x.plan, g, g, gwfft::kInverse, c->stream);
+}
+
 // One pair from host arrays: hp (and hc when unaligned) given.
 int maximized_single(gwgpu_context *c, const double *data, const double *psd, const double *freqs, const double *hp,
                      const double *hc, int N, double *out) {
@@ -256,13 +296,13 @@ int maximized_single(gwgpu_context *c, const double *data, const double *psd, co
   const int np = un ? 2 : 1, ns = un ? 3 : 1;
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
-  int plan;
-  int st = plan_for(c, N, np, &plan);
+  Xform x;
+  int st = xform_setup(c, N, np, x);
   if (st) return st;
-  const int nblk = (N + kBlock - 1) / kBlock;
+  const int nblk = (x.ld + kBlock - 1) / kBlock;
   const size_t o_f = 0, o_d = up256(8 * (size_t)N), o_s = o_d + up256(16 * (size_t)N),
                o_rp = o_s + up256(8 * (size_t)N), o_rc = o_rp + up256(16 * (size_t)N),
-               o_g = o_rc + up256(16 * (size_t)N), o_h = o_g + up256(16 * (size_t)N * np),
+               o_g = o_rc + up256(16 * (size_t)N), o_h = o_g + up256(16 * (size_t)x.ld * np),
                o_sd = o_h + up256(8 * (size_t)nblk * ns), o_misc = o_sd + up256(sizeof(StreamDev)),
                total = o_misc + 256;
   void *dev;
@@ -289,22 +329,19 @@ int maximized_single(gwgpu_context *c, const double *data, const double *psd, co
   double2 *g = (double2 *)(b + o_g);
   const StreamDev *sdd = (const StreamDev *)(b + o_sd);
   const double2 *rp = (const double2 *)(b + o_rp), *rc = (const double2 *)(b + o_rc);
+  double *hh = (double *)(b + o_h);
   if (un)
-    k_maxll_prep<true><<<dim3(nblk, 1), kBlock, 0, c->stream>>>(nullptr, rp, rc, 1, sdd, dh, N, g, (double *)(b + o_h));
+    k_maxll_prep<true><<<dim3(nblk, 1), kBlock, 0, c->stream>>>(nullptr, rp, rc, 1, sdd, dh, N, x.ld, x.blue, g, hh);
   else
-    k_maxll_prep<false><<<dim3(nblk, 1), kBlock, 0, c->stream>>>(nullptr, rp, nullptr, 1, sdd, dh, N, g,
-                                                                (double *)(b + o_h));
-  CuFft &f = cufft();
-  if (f.set_stream(plan, c->stream) != 0 || f.exec_z2z(plan, g, g, kCufftForward) != 0) {
-    c->last_error = "cuFFT exec";
-    return GWGPU_ECUDA;
-  }
+    k_maxll_prep<false><<<dim3(nblk, 1), kBlock, 0, c->stream>>>(nullptr, rp, nullptr, 1, sdd, dh, N, x.ld, x.blue,
+                                                                g, hh);
+  if ((st = xform_run(c, x, g, np))) return st;
   if (un)
-    k_maxll_reduce<true><<<1, kBlock, 0, c->stream>>>(g, (const double *)(b + o_h), nblk, N, 1, sdd, dh, nullptr,
-                                                      ll_pair, done, res, nullptr);
+    k_maxll_reduce<true><<<1, kBlock, 0, c->stream>>>(g, hh, nblk, N, x.ld, 1, sdd, dh, nullptr, ll_pair, done, res,
+                                                      nullptr);
   else
-    k_maxll_reduce<false><<<1, kBlock, 0, c->stream>>>(g, (const double *)(b + o_h), nblk, N, 1, sdd, dh, nullptr,
-                                                       ll_pair, done, res, nullptr);
+    k_maxll_reduce<false><<<1, kBlock, 0, c->stream>>>(g, hh, nblk, N, x.ld, 1, sdd, dh, nullptr, ll_pair, done,
+                                                       res, nullptr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return c->fail(e, "maximised likelihood launch");
   cudaMemcpyAsync(out, res, 8, cudaMemcpyDeviceToHost, c->stream);
@@ -350,15 +387,16 @@ int gwgpu_maximized_loglik_batch(gwgpu_context *c, const gwgpu_gen_params *param
     }
   }
   const int pairs = n * ndet;
-  int plan;
-  int st = plan_for(c, N, pairs * np, &plan);
+  Xform x;
+  int st = xform_setup(c, N, pairs * np, x);
   if (st) return st;
-  const int nblk = (N + kBlock - 1) / kBlock;
+  const int nblk = (x.ld + kBlock - 1) / kBlock;
   const size_t o_p = 0, o_a = up256(sizeof(gwgpu_gen_params) * n), o_h = o_a + up256(4 * (size_t)n),
                o_req = o_h + up256(4 * (size_t)pairs), o_g = o_req + up256(sizeof(Request) * n),
-               o_hh = o_g + up256(16 * (size_t)pairs * np * N), o_ll = o_hh + up256(8 * (size_t)pairs * ns * nblk),
-               o_out = o_ll + up256(8 * (size_t)pairs), o_st = o_out + up256(8 * (size_t)n),
-               o_done = o_st + up256(4 * (size_t)n), total = o_done + up256(4 * (size_t)n);
+               o_hh = o_g + up256(16 * (size_t)pairs * np * x.ld),
+               o_ll = o_hh + up256(8 * (size_t)pairs * ns * nblk), o_out = o_ll + up256(8 * (size_t)pairs),
+               o_st = o_out + up256(8 * (size_t)n), o_done = o_st + up256(4 * (size_t)n),
+               total = o_done + up256(4 * (size_t)n);
   void *dev;
   if ((st = c->workspace(gwgpu_context::kWsMaxll, total, &dev))) return st;
   char *b = (char *)dev;
@@ -386,23 +424,19 @@ int gwgpu_maximized_loglik_batch(gwgpu_context *c, const gwgpu_gen_params *param
   const int *hd = (const int *)(b + o_h);
   double *hh = (double *)(b + o_hh);
   if (un)
-    k_maxll_prep<true><<<dim3(nblk, pairs), kBlock, 0, c->stream>>>(rq, nullptr, nullptr, ndet, c->streams_dev, hd,
-                                                                   N, g, hh);
+    k_maxll_prep<true><<<dim3(nblk, n), kBlock, 0, c->stream>>>(rq, nullptr, nullptr, ndet, c->streams_dev, hd, N,
+                                                                   x.ld, x.blue, g, hh);
   else
-    k_maxll_prep<false><<<dim3(nblk, pairs), kBlock, 0, c->stream>>>(rq, nullptr, nullptr, ndet, c->streams_dev, hd,
-                                                                    N, g, hh);
-  CuFft &f = cufft();
-  if (f.set_stream(plan, c->stream) != 0 || f.exec_z2z(plan, g, g, kCufftForward) != 0) {
-    c->last_error = "cuFFT exec";
-    return GWGPU_ECUDA;
-  }
+    k_maxll_prep<false><<<dim3(nblk, n), kBlock, 0, c->stream>>>(rq, nullptr, nullptr, ndet, c->streams_dev, hd, N,
+                                                                    x.ld, x.blue, g, hh);
+  if ((st = xform_run(c, x, g, pairs * np))) return st;
   int *dst = (int *)(b + o_st);
   if (un)
-    k_maxll_reduce<true><<<pairs, kBlock, 0, c->stream>>>(g, hh, nblk, N, ndet, c->streams_dev, hd, dst,
+    k_maxll_reduce<true><<<pairs, kBlock, 0, c->stream>>>(g, hh, nblk, N, x.ld, ndet, c->streams_dev, hd, dst,
                                                           (double *)(b + o_ll), (unsigned *)(b + o_done),
                                                           (double *)(b + o_out), dst);
   else
-    k_maxll_reduce<false><<<pairs, kBlock, 0, c->stream>>>(g, hh, nblk, N, ndet, c->streams_dev, hd, dst,
+    k_maxll_reduce<false><<<pairs, kBlock, 0, c->stream>>>(g, hh, nblk, N, x.ld, ndet, c->streams_dev, hd, dst,
                                                            (double *)(b + o_ll), (unsigned *)(b + o_done),
                                                            (double *)(b + o_out), dst);
   e = cudaGetLastError();

@@ -11,7 +11,10 @@
 #include "../../include/gwat_dropin.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
+#include <cstdio>
+#include <stdexcept>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -240,7 +243,105 @@ double maximized_Log_Likelihood_unaligned_spin_internal(std::complex<double> *da
   return out;
 }
 
+// ---- data and noise ingestion
+static void io_fail(int st, const std::string &file) {
+  if (st == GWGPU_ENOTFOUND) {
+    std::printf("ERROR -- File %s not found\n", file.c_str());
+    std::exit(1);
+  }
+  if (st == GWGPU_EINVAL) throw std::invalid_argument("stod: " + file);
+}
+
+void read_LOSC_data_file(std::string filename, double *output, double *data_start_time, double *duration,
+                         double *fs) {
+  long long n = 0;
+  int st = gwgpu_read_losc_data_file(filename.c_str(), output, LLONG_MAX, &n, data_start_time, duration, fs);
+  if (st) io_fail(st, filename);
+}
+
+void read_LOSC_PSD_file(std::string filename, double **output, int rows, int cols) {
+  std::vector<double> flat((size_t)rows * cols);
+  int st = gwgpu_read_losc_psd_file(filename.c_str(), flat.data(), rows, cols);
+  if (st) io_fail(st, filename);
+  for (int i = 0; i < rows; i++)
+    for (int j = 0; j < cols; j++) output[i][j] = flat[(size_t)i * cols + j];
+}
+
+void allocate_LOSC_data(std::string *data_files, std::string psd_file, int num_detectors, int psd_length,
+                        int data_file_length, double trigger_time, double post_merger_duration,
+                        std::complex<double> **data, double **psds, double **freqs) {
+  std::vector<const char *> names(num_detectors);
+  for (int i = 0; i < num_detectors; i++) names[i] = data_files[i].c_str();
+  const size_t n = (size_t)num_detectors * psd_length;
+  std::vector<double> d(2 * n), p(n), f(n);
+  int st = gwgpu_allocate_losc_data(engine().ctx, names.data(), psd_file.c_str(), num_detectors, psd_length,
+                                    data_file_length, trigger_time, post_merger_duration, d.data(), p.data(),
+                                    f.data());
+  if (st == GWGPU_ENOTFOUND || st == GWGPU_EINVAL) io_fail(st, psd_file);
+  if (st != GWGPU_OK && st != GWGPU_EDOMAIN) return;
+  for (int i = 0; i < num_detectors; i++)
+    for (int j = 0; j < psd_length; j++) {
+      psds[i][j] = p[(size_t)i * psd_length + j];
+      freqs[i][j] = f[(size_t)i * psd_length + j];
+    }
+  if (st == GWGPU_EDOMAIN) return;  // the trigger window is outside the file: data untouched
+  for (int i = 0; i < num_detectors; i++)
+    for (int j = 0; j < psd_length; j++) {
+      const size_t k = 2 * ((size_t)i * psd_length + j);
+      data[i][j] = std::complex<double>(d[k], d[k + 1]);
+    }
+}
+
+int count_lines_data_file(std::string file, int *count) {
+  if (gwgpu_count_lines_data_file(file.c_str(), count) != GWGPU_OK) {
+    *count = 0;
+    std::printf("ERROR -- could not open file\n");
+    return 1;
+  }
+  return 0;
+}
+
+int count_lines_LOSC_PSD_file(std::string file, int *count) {
+  count_lines_data_file(file, count);
+  *count -= 1;
+  return 0;
+}
+
+int count_lines_LOSC_data_file(std::string file, int *count) {
+  count_lines_data_file(file, count);
+  *count -= 3;
+  return 0;
+}
+
+void populate_noise(double *frequencies, std::string detector, double *noise_root, int length,
+                    double integration_time) {
+  std::string dir;
+  if (const char *e = std::getenv("GWGPU_NOISE_DIR")) dir = e;
+#ifdef GWAT_SHARE_DIR
+  else dir = std::string(GWAT_SHARE_DIR) + "noise_data/";
+#endif
+  int st = gwgpu_populate_noise(frequencies, detector.c_str(), noise_root, length, integration_time,
+                                dir.empty() ? nullptr : dir.c_str());
+  if (st == GWGPU_ENOTFOUND) std::printf("Detector %s not supported\n", detector.c_str());
+}
+
 // ---- C entry points for the test suite (ctypes cannot call the C++ symbols)
+// allocate_LOSC_data through the reference signature: outputs flat like the C ABI.
+extern "C" void gwat_dropin_test_losc(const char *const *files, int nd, const char *psd_file, int psd_length,
+                                      int data_file_length, double trigger, double post, double *data, double *psds,
+                                      double *freqs) {
+  std::vector<std::string> names(files, files + nd);
+  std::vector<std::complex<double> *> dr(nd);
+  std::vector<double *> pr(nd), fr(nd);
+  for (int i = 0; i < nd; i++) {
+    dr[i] = (std::complex<double> *)(data + 2 * (size_t)i * psd_length);
+    pr[i] = psds + (size_t)i * psd_length;
+    fr[i] = freqs + (size_t)i * psd_length;
+  }
+  allocate_LOSC_data(names.data(), psd_file, nd, psd_length, data_file_length, trigger, post, dr.data(), pr.data(),
+                     fr.data());
+}
+
 // The maximised likelihood through the reference signatures (hc null: aligned).
 extern "C" double gwat_dropin_test_maxll(const double *data, const double *psd, const double *f, const double *hp,
                                          const double *hc, int N) {

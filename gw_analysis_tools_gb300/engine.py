@@ -15,6 +15,7 @@ data registry.  Functions mirror the reference's entry points:
 Every call goes to the CUDA library; there is no CPU fallback.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -80,6 +81,67 @@ def _ip(a):
 
 class GwGpuError(_native.GwGpuError):
     pass
+
+
+def _io_check(st, what):
+    if st != 0:
+        raise GwGpuError("%s: %s" % (what, STATUS.get(st, st)))
+
+
+def count_lines_data_file(path):
+    """count_lines_data_file (io_util.cpp:682-699)."""
+    n = ctypes.c_int()
+    _io_check(_native.load().gwgpu_count_lines_data_file(os.fsencode(path), ctypes.byref(n)), path)
+    return n.value
+
+
+def count_lines_losc_data_file(path):
+    """count_lines_LOSC_data_file (io_util.cpp:709-714): lines less the 3 header lines."""
+    n = ctypes.c_int()
+    _io_check(_native.load().gwgpu_count_lines_losc_data_file(os.fsencode(path), ctypes.byref(n)), path)
+    return n.value
+
+
+def count_lines_losc_psd_file(path):
+    """count_lines_LOSC_PSD_file (io_util.cpp:701-707): lines less the header line."""
+    n = ctypes.c_int()
+    _io_check(_native.load().gwgpu_count_lines_losc_psd_file(os.fsencode(path), ctypes.byref(n)), path)
+    return n.value
+
+
+def read_losc_data_file(path, capacity=None):
+    """read_LOSC_data_file (io_util.cpp:403-464) -> (samples, start, duration, fs)."""
+    L = _native.load()
+    n = ctypes.c_longlong()
+    start, duration, fs = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    cap = capacity if capacity is not None else max(count_lines_losc_data_file(path), 1)
+    for _ in range(2):
+        out = np.zeros(cap)
+        st = L.gwgpu_read_losc_data_file(os.fsencode(path), _dp(out), cap, ctypes.byref(n), ctypes.byref(start),
+                                         ctypes.byref(duration), ctypes.byref(fs))
+        if st != 8 or capacity is not None:
+            break
+        cap = n.value  # more than one value on some lines
+    _io_check(st, path)
+    return out[:n.value].copy(), start.value, duration.value, fs.value
+
+
+def read_losc_psd_file(path, rows, cols):
+    """read_LOSC_PSD_file (io_util.cpp:466-500) -> array [rows][cols]."""
+    out = np.zeros((rows, cols))
+    _io_check(_native.load().gwgpu_read_losc_psd_file(os.fsencode(path), _dp(out), rows, cols), path)
+    return out
+
+
+def populate_noise(frequencies, detector, noise_dir=None, integration_time=48.0):
+    """populate_noise (detector_util.cpp:86-283) for the ground-detector
+    curves: the amplitude spectral density at each frequency."""
+    f = np.ascontiguousarray(frequencies, dtype=np.float64)
+    out = np.zeros(f.size)
+    st = _native.load().gwgpu_populate_noise(_dp(f), detector.encode(), _dp(out), f.size, float(integration_time),
+                                             os.fsencode(noise_dir) if noise_dir else None)
+    _io_check(st, "populate_noise(%s)" % detector)
+    return out
 
 
 class Context:
@@ -177,6 +239,39 @@ class Context:
                                                                  f.size, int(bool(log10F)), ctypes.byref(out))
         self._check(st, "log_likelihood_internal")
         return out.value
+
+    def losc_prepare(self, series, file_start, duration, fs, psd_table, trigger_time, post_merger_duration):
+        """The transform step of allocate_LOSC_data (io_util.cpp:550-651) on the
+        device.  Returns (data [ndet][psd_length] complex, psds, freqs, bins)."""
+        x = np.ascontiguousarray(series, dtype=np.float64)
+        if x.ndim == 1:
+            x = x[None, :]
+        tab = np.ascontiguousarray(psd_table, dtype=np.float64)
+        nd, n = x.shape
+        pl = tab.shape[0]
+        data = np.zeros((nd, pl), dtype=np.complex128)
+        psds = np.zeros((nd, pl))
+        freqs = np.zeros((nd, pl))
+        bins = ctypes.c_int(0)
+        st = self.lib.gwgpu_losc_prepare(self.h, _dp(x), nd, n, float(file_start), float(duration), float(fs),
+                                         _dp(tab), pl, float(trigger_time), float(post_merger_duration), _dp(data),
+                                         _dp(psds), _dp(freqs), ctypes.byref(bins))
+        self._check(st, "losc_prepare")
+        return data, psds, freqs, bins.value
+
+    def allocate_losc_data(self, data_files, psd_file, psd_length, data_file_length, trigger_time,
+                           post_merger_duration):
+        """allocate_LOSC_data (io_util.cpp:523-664): files in, (data, psds, freqs) out."""
+        nd = len(data_files)
+        names = (ctypes.c_char_p * nd)(*[os.fsencode(f) for f in data_files])
+        data = np.zeros((nd, psd_length), dtype=np.complex128)
+        psds = np.zeros((nd, psd_length))
+        freqs = np.zeros((nd, psd_length))
+        st = self.lib.gwgpu_allocate_losc_data(self.h, names, os.fsencode(psd_file), nd, psd_length,
+                                               data_file_length, float(trigger_time), float(post_merger_duration),
+                                               _dp(data), _dp(psds), _dp(freqs))
+        self._check(st, "allocate_losc_data")
+        return data, psds, freqs
 
     def maximized_log_likelihood_internal(self, data, psd, freqs, response):
         """maximized_Log_Likelihood_aligned_spin_internal (mcmc_gw.cpp:595-658)."""

@@ -68,6 +68,23 @@ double maximized_Log_Likelihood_aligned_spin_internal(std::complex<double> *data
 double maximized_Log_Likelihood_unaligned_spin_internal(std::complex<double> *data, double *psd, double *frequencies,
                                                         std::complex<double> *hplus, std::complex<double> *hcross,
                                                         size_t length, fftw_outline *plan);
+// Data and noise ingestion (io_util.h:27-58, detector_util.h:168).  File
+// errors keep the reference's behaviour: a missing file prints a message and
+// exits, a value that does not parse throws std::invalid_argument.
+void read_LOSC_data_file(std::string filename, double *output, double *data_start_time, double *duration,
+                         double *fs);
+void read_LOSC_PSD_file(std::string filename, double **output, int rows, int cols);
+void allocate_LOSC_data(std::string *data_files, std::string psd_file, int num_detectors, int psd_length,
+                        int data_file_length, double trigger_time, double post_merger_duration,
+                        std::complex<double> **data, double **psds, double **freqs);
+int count_lines_data_file(std::string file, int *count);
+int count_lines_LOSC_PSD_file(std::string file, int *count);
+int count_lines_LOSC_data_file(std::string file, int *count);
+// populate_noise for the ground-detector curves; the tabulated curves are read
+// from $GWGPU_NOISE_DIR (else GWAT_SHARE_DIR "noise_data/" when defined at
+// build time, as the reference does)
+void populate_noise(double *frequencies, std::string detector, double *noise_root, int length,
+                    double integration_time = 48);
 // fisher_numerical (fisher.h:35-48, fisher.cpp:81): "IMRPhenomD" / "MCMC_IMRPhenomD"
 void fisher_numerical(double *frequency, int length, std::string generation_method, std::string detector,
                       std::string reference_detector, double **output, int dimension,

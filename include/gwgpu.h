@@ -168,6 +168,62 @@ int gwgpu_maximized_log_likelihood_unaligned_internal(gwgpu_context *ctx, const 
 int gwgpu_maximized_loglik_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, int approximant,
                                  const int *handles, int num_detectors, double *loglik, int *status);
 
+/* ---- data and noise ingestion (the formats feeding the registered streams) ---- */
+/* count_lines_data_file / count_lines_LOSC_data_file / count_lines_LOSC_PSD_file
+ * (io_util.h:56-58, io_util.cpp:682-714): the file's line count as
+ * std::getline yields lines, less the 3 (strain) or 1 (PSD) header lines.
+ * GWGPU_ENOTFOUND when the file cannot be read. */
+int gwgpu_count_lines_data_file(const char *path, int *count);
+int gwgpu_count_lines_losc_data_file(const char *path, int *count);
+int gwgpu_count_lines_losc_psd_file(const char *path, int *count);
+/* read_LOSC_data_file(std::string filename, double* output, double*
+ * data_start_time, double* duration, double* fs)  (io_util.h:27,
+ * io_util.cpp:403-464): line 1's digit-led tokens give fs, line 2's the GPS
+ * start and the duration, the comma-separated values from line 3 on are the
+ * samples.  *count (may be null) gets the number of samples; capacity
+ * bounds output (GWGPU_ETOOLARGE beyond it, with *count set).  GWGPU_EINVAL where a value does not parse (the
+ * reference throws). */
+int gwgpu_read_losc_data_file(const char *path, double *output, long long capacity, long long *count,
+                              double *data_start_time, double *duration, double *fs);
+/* read_LOSC_PSD_file(std::string filename, double** output, int rows, int cols)
+ * (io_util.h:33, io_util.cpp:466-500): the first line skipped, then
+ * white-space separated values into output[rows*cols] (row-major); rows the
+ * file does not fill are zero. */
+int gwgpu_read_losc_psd_file(const char *path, double *output, int rows, int cols);
+/* populate_noise(double* frequencies, std::string detector, double*
+ * noise_root, int length, double integration_time)  (detector_util.h:168,
+ * detector_util.cpp:86-283) for the ground-detector curves: "aLIGO_analytic",
+ * "Hanford_O1_fitted", and the tabulated curves ("AdLIGODesign", "CE2",
+ * "ET-D", ... the reference's interp_PSD_models names) interpolated linearly
+ * from their CSV file in noise_dir (the reference's share/noise_data).  The
+ * LISA curves are not part of this library.  Frequencies outside a table give
+ * NaN and GWGPU_EDOMAIN (the reference's GSL error). */
+int gwgpu_populate_noise(const double *frequencies, const char *detector, double *noise_root, int length,
+                         double integration_time, const char *noise_dir);
+/* allocate_LOSC_data(std::string* data_files, std::string psd_file, int
+ * num_detectors, int psd_length, int data_file_length, double trigger_time,
+ * double post_merger_duration, std::complex<double>** data, double** psds,
+ * double** freqs)  (io_util.h:38, io_util.cpp:523-664): the strain files are
+ * parsed in parallel, then as gwgpu_losc_prepare.  Outputs flat:
+ * data[num_detectors][psd_length] complex (interleaved), psds and freqs
+ * [num_detectors][psd_length]. */
+int gwgpu_allocate_losc_data(gwgpu_context *ctx, const char *const *data_files, const char *psd_file,
+                             int num_detectors, int psd_length, int data_file_length, double trigger_time,
+                             double post_merger_duration, double *data, double *psds, double *freqs);
+/* The transform step of allocate_LOSC_data from strain already in memory:
+ * series[num_detectors][series_length], psd_table[psd_length][num_detectors+1]
+ * (frequency, then one PSD column per detector).  T_obs = 1/(f_1 - f_0) of the
+ * table; the samples with trigger - (T_obs - post) < t <= trigger + post are
+ * Tukey-windowed (alpha = 0.8/T_obs), transformed on the device (forward DFT,
+ * times dt) and the bins k/T_obs inside the table's band kept.  psds and freqs
+ * are filled first; GWGPU_EDOMAIN when the window does not fit in the file.
+ * *bins_out (may be null) gets the number of data bins filled; the rest are
+ * zero. */
+int gwgpu_losc_prepare(gwgpu_context *ctx, const double *series, int num_detectors, long long series_length,
+                       double file_start, double duration, double fs, const double *psd_table, int psd_length,
+                       double trigger_time, double post_merger_duration, double *data, double *psds,
+                       double *freqs, int *bins_out);
+
 /* ---- batched form: n requests, one fused launch per step ---- */
 /* n independent MCMC_likelihood_extrinsic evaluations (the sampler calls
  * mcmc_step -> sampler->ll once per chain, mcmc_sampler_internals.cpp:98).

@@ -44,5 +44,7 @@ def test_dropin_library_exports_reference_signatures():
                  "fourier_waveform(double*, int, std::complex<double>*", "fourier_waveform<double>(",
                  "fourier_detector_response<double>(", "fisher_numerical(double*, int",
                  "maximized_Log_Likelihood_aligned_spin_internal(std::complex<double>*",
-                 "maximized_Log_Likelihood_unaligned_spin_internal(std::complex<double>*"):
+                 "maximized_Log_Likelihood_unaligned_spin_internal(std::complex<double>*",
+                 "allocate_LOSC_data(std::", "read_LOSC_data_file(std::", "read_LOSC_PSD_file(std::",
+                 "populate_noise(double*", "count_lines_LOSC_data_file(std::"):
         assert name in out, name

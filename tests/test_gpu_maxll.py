@@ -94,3 +94,21 @@ def test_maximized_through_reference_signatures(oracle, setup):
     ref_a = oracle.maximized_loglik_internal(data, psd, f, hp)
     ref_u = oracle.maximized_loglik_unaligned_internal(data, psd, f, hp, hc)
     assert abs(got_a - ref_a) <= RTOL * abs(ref_a) and abs(got_u - ref_u) <= RTOL * abs(ref_u)
+
+
+@pytest.mark.parametrize("nbins", [4000, 4096, 2 * 3 * 5 * 7 * 11])
+def test_maximized_transform_paths(gpu_ctx, oracle, nbins):
+    """Grid lengths with only factors up to 7 go through cuFFT directly, others
+    (here 2310 = 2*3*5*7*11; the fixture's 3937 = 31*127) through Bluestein."""
+    f = 20.0 + np.arange(nbins) / 8.0
+    psd = W.analytic_psd(f)
+    d = W.prior_draws(2, 87)
+    data = oracle.detector_response(f, oracle.params_from_dict(d[0]), "Hanford") + W.noise(f, 88)
+    r = oracle.detector_response(f, oracle.params_from_dict(d[1]), "Hanford")
+    hp, hc = oracle.fourier_waveform(f, oracle.params_from_dict(d[1]), oracle.IMRPhenomD)
+    ref = oracle.maximized_loglik_internal(data, psd, f, r)
+    got = gpu_ctx.maximized_log_likelihood_internal(data, psd, f, r)
+    assert abs(got - ref) <= RTOL * max(1.0, abs(ref)), (got, ref)
+    ref = oracle.maximized_loglik_unaligned_internal(data, psd, f, hp, hc * (1 + 0.3j))
+    got = gpu_ctx.maximized_log_likelihood_unaligned_internal(data, psd, f, hp, hc * (1 + 0.3j))
+    assert abs(got - ref) <= RTOL * max(1.0, abs(ref)), (got, ref)
