@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the secondary forms")
+    ap.add_argument("--forms", default="", help="comma-separated secondary forms to run (default: all)")
     return ap.parse_args()
 
 
@@ -455,6 +456,8 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
 
     for name, fn in (("plain", plain), ("batched_fp64", batched_fp64), ("served", served), ("uneven", uneven),
                      ("fisher", fisher), ("maximized", maximized), ("ingest", ingest)):
+        if args.forms and name not in args.forms.split(","):
+            continue
         log(name)
         try:
             fn()

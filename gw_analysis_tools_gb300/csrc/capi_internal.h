@@ -25,7 +25,7 @@ struct gwgpu_context {
     std::vector<double> host_freqs;
     uint64_t psd_hash = 0;  // FNV-1a of the PSD bytes: detectors with equal PSDs share weights
   };
-  enum { kWsWave = 0, kWsInner, kWsPlain, kWsBatch, kWsBatchItems, kWsFisher, kWsServe, kWsMaxll, kWsIngest, kWsChirp };
+  enum { kWsWave = 0, kWsInner, kWsPlain, kWsBatch, kWsBatchItems, kWsFisher, kWsServe, kWsMaxll, kWsIngest, kWsChirp, kWsChirp32, kWsMaxllRun };
   enum { kHwsPlain = 0, kHwsBatch, kHwsFisher, kHwsInner };
 
   int device = 0;
@@ -50,6 +50,8 @@ struct gwgpu_context {
   int tile_override = 0;
   bool use_graphs = true;
   int chirp_n = 0;                 // grid length whose Bluestein kernel the kWsChirp workspace holds
+  double chirp_kscale = 0;         // M max|B| of that kernel (the FP32 search's error scale)
+  bool maxll_fp64 = false;         // maximised likelihood: FP64 transforms only (no FP32 search)
   bool prologue_serial = false;    // batched prologue: one thread per request instead of the cooperative kernel
   uint64_t streams_epoch = 0;      // bumped when the device stream table changes
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;

@@ -15,12 +15,14 @@ namespace {
 struct Lib {
   typedef int (*PlanMany)(int *, int, int *, int *, int, int, int *, int, int, int, int);
   typedef int (*ExecZ2Z)(int, void *, void *, int);
+  typedef int (*ExecC2C)(int, void *, void *, int);
   typedef int (*ExecD2Z)(int, void *, void *);
   typedef int (*SetStream)(int, cudaStream_t);
   typedef int (*Destroy)(int);
   void *h = nullptr;
   PlanMany plan_many = nullptr;
   ExecZ2Z z2z = nullptr;
+  ExecC2C c2c = nullptr;
   ExecD2Z d2z = nullptr;
   SetStream set_stream = nullptr;
   Destroy destroy = nullptr;
@@ -39,9 +41,10 @@ Lib &lib() {
     f.plan_many = (Lib::PlanMany)dlsym(f.h, "cufftPlanMany");
     f.z2z = (Lib::ExecZ2Z)dlsym(f.h, "cufftExecZ2Z");
     f.d2z = (Lib::ExecD2Z)dlsym(f.h, "cufftExecD2Z");
+    f.c2c = (Lib::ExecC2C)dlsym(f.h, "cufftExecC2C");
     f.set_stream = (Lib::SetStream)dlsym(f.h, "cufftSetStream");
     f.destroy = (Lib::Destroy)dlsym(f.h, "cufftDestroy");
-    f.ok = f.plan_many && f.z2z && f.d2z && f.set_stream && f.destroy;
+    f.ok = f.plan_many && f.z2z && f.d2z && f.c2c && f.set_stream && f.destroy;
   });
   return f;
 }
@@ -79,6 +82,15 @@ int plan(gwgpu_context *c, Type type, int N, int batch, int *out) {
 int exec_z2z(gwgpu_context *c, int p, double2 *in, double2 *out, int direction, cudaStream_t s) {
   Lib &f = lib();
   if (f.set_stream(p, s) != 0 || f.z2z(p, in, out, direction) != 0) {
+    c->last_error = "cuFFT exec";
+    return GWGPU_ECUDA;
+  }
+  return GWGPU_OK;
+}
+
+int exec_c2c(gwgpu_context *c, int p, float2 *in, float2 *out, int direction, cudaStream_t s) {
+  Lib &f = lib();
+  if (f.set_stream(p, s) != 0 || f.c2c(p, in, out, direction) != 0) {
     c->last_error = "cuFFT exec";
     return GWGPU_ECUDA;
   }

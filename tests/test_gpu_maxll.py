@@ -112,3 +112,37 @@ def test_maximized_transform_paths(gpu_ctx, oracle, nbins):
     ref = oracle.maximized_loglik_unaligned_internal(data, psd, f, hp, hc * (1 + 0.3j))
     got = gpu_ctx.maximized_log_likelihood_unaligned_internal(data, psd, f, hp, hc * (1 + 0.3j))
     assert abs(got - ref) <= RTOL * max(1.0, abs(ref)), (got, ref)
+
+
+@pytest.fixture(scope="module")
+def fp64_ctx():
+    """A context whose maximised likelihood uses FP64 transforms only."""
+    import os
+    old = os.environ.get("GWGPU_MAXLL")
+    os.environ["GWGPU_MAXLL"] = "fp64"
+    try:
+        ctx = G.Context(0)
+    finally:
+        if old is None:
+            del os.environ["GWGPU_MAXLL"]
+        else:
+            os.environ["GWGPU_MAXLL"] = old
+    yield ctx
+    ctx.close()
+
+
+@pytest.mark.parametrize("approx", [G.IMRPhenomD, G.IMRPhenomPv2])
+def test_search_path_matches_fp64_transforms(gpu_ctx, fp64_ctx, setup, approx):
+    """The FP32 search with FP64 refinement gives the maximum of the FP64
+    transforms: same values, draws near the injection and far from it."""
+    s = setup
+    prec = approx == G.IMRPhenomPv2
+    draws = [dict(s["src"], spin1=(0.1, 0.0, 0.2), spin2=(0.0, 0.1, 0.1)) if prec else s["src"]]
+    draws += W.perturbed(draws[0], 20, 89, frac=0.002) + W.prior_draws(43, 90, precessing=prec)
+    outs = []
+    for ctx in (gpu_ctx, fp64_ctx):
+        hs = [ctx.register_data(d, s["f"], s["data"][i], s["psd"]) for i, d in enumerate(s["dets"])]
+        out, st = ctx.maximized_loglik_batch(G.params_array(draws), hs, approximant=approx)
+        assert np.all(st == 0)
+        outs.append(out)
+    assert np.all(np.abs(outs[0] - outs[1]) <= 1e-10 * np.abs(outs[1])), np.max(np.abs(outs[0] - outs[1]) / np.abs(outs[1]))
