@@ -285,10 +285,13 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 //   S0  W0 parameters, source;  W3 detector projections
 //   S1  W0 calibration fits;  W1 D: ringdown frequencies / Pv2: J-frame transform;  W2 PN coefficients
 //   S2  W0 Pv2: ringdown frequencies; matching frequencies
-//   S3  W0/W1 amplitude matching points;  W2 phase connection;  W3 Pv2: Euler and frame constants
-//   S4  W0/W1 amplitude deltas;  W2 D: phase/time shift / Pv2: time-shift nodes 0-4;  W3 Pv2: nodes 5-9
-//   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions;  W3 D: detector phases / Pv2: time shift, angles
-//   S6  W0 Pv2: detector phases; finalize factors, outputs
+//   S3  W0/W1 amplitude matching points;  D: W2/W3 phase connection, inspiral / other parts;
+//       Pv2: W2 phase connection, W3 Euler and frame constants
+//   S4  W0/W1 amplitude deltas;  W2 D: phase connection constants, phase/time shift /
+//       Pv2: time-shift nodes 0-4;  W3 Pv2: nodes 5-9
+//   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions;  W3 D: detector phases and factors /
+//       Pv2: time shift, angles
+//   S6  W0 Pv2: detector phases and factors; outputs
 constexpr int kCoopWarps = 4, kCoopReq = 16;
 __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     const GenParams *__restrict__ params, const int *__restrict__ approx, int n, const int *__restrict__ handles,
@@ -297,6 +300,8 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   __shared__ Request s_r[kCoopReq];
   __shared__ GenParams s_p[kCoopReq];
   __shared__ AmpConn s_ac[kCoopReq];
+  __shared__ PhaseConnParts s_pc[kCoopReq];
+  __shared__ double s_ds[kCoopReq][kMaxDet], s_ws[kCoopReq][kMaxDet];  // stream scales of the mixed form
   __shared__ double s_shift[kCoopReq][kPv2ShiftNodes];
   __shared__ double s_df[kCoopReq];
   __shared__ int s_st[kCoopReq], s_bad[kCoopReq], s_uni[kCoopReq];
@@ -331,7 +336,10 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     sky_trig(q.RA, q.DEC, q.psi, q.gmst, tr);
     const int d0 = streams[handles[i * ndet]].det;
     for (int d = 0; d < ndet && d < kMaxDet; d++) {
-      const int dd = streams[handles[i * ndet + d]].det;
+      const StreamDev &sd = streams[handles[i * ndet + d]];
+      const int dd = sd.det;
+      s_ds[lane][d] = sd.dscale;
+      s_ws[lane][d] = sd.wscale;
       antenna_trig(dd, tr, r.det[d].fp, r.det[d].fc);
       r.det[d].tau = -dtoa_trig(tr, d0, dd) * (2 * kPi);
     }
@@ -359,8 +367,13 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   if (run) {
     if (warp == 0) d_amp_conn_low(r.m, s_ac[lane]);
     if (warp == 1) d_amp_conn_high(r.m, s_ac[lane]);
-    if (warp == 2) d_phase_conn(r.m);
-    if (warp == 3 && pv2) model_p_finish(r.m, r.p);
+    if (pv2) {
+      if (warp == 2) d_phase_conn(r.m);
+      if (warp == 3) model_p_finish(r.m, r.p);
+    } else {
+      if (warp == 2) phase_conn_ins(r.m, s_pc[lane]);
+      if (warp == 3) phase_conn_imr(r.m, s_pc[lane]);
+    }
   }
   __syncthreads();
   // S4
@@ -368,7 +381,10 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     if (warp == 0) d_deltas(r.m, s_ac[lane], 0, 3);
     if (warp == 1) d_deltas(r.m, s_ac[lane], 3, 5);
     if (!pv2) {
-      if (warp == 2) model_d_finish(r.m);
+      if (warp == 2) {
+        phase_conn_combine(r.m, s_pc[lane]);
+        model_d_finish(r.m);
+      }
     } else if (r.m.s.shift_time && (warp == 2 || warp == 3)) {
       for (int j = (warp - 2) * (kPv2ShiftNodes / 2); j < (warp - 1) * (kPv2ShiftNodes / 2); j++)
         s_shift[lane][j] = pv2_shift_node(r.m, j);
@@ -385,8 +401,12 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
       if (warp == 1) mixed_phase_coeffs(r, df, x);
       if (warp == 2) mixed_regions(r, df, x);
       if (warp == 3) {
-        if (pv2) mixed_pv2_coeffs(r, df, x);
-        else mixed_det_phase(r, df, x);
+        if (pv2) {
+          mixed_pv2_coeffs(r, df, x);
+        } else {
+          mixed_det_phase(r, df, x);
+          mixed_det_factors_a(r, x, mixed_a_scale(r, df), s_ds[lane], s_ws[lane]);
+        }
       }
     }
   }
@@ -399,13 +419,10 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
       if (req) req[i] = r;
       if (want_mixed) {
         if (!s_uni[lane]) st = st ? st : 1;
-        double ds[kMaxDet], ws[kMaxDet];
-        for (int d = 0; d < ndet; d++) {
-          ds[d] = streams[handles[i * ndet + d]].dscale;
-          ws[d] = streams[handles[i * ndet + d]].wscale;
+        if (r.approximant == kPhenomPv2) {  // needs the time shift of S5
+          mixed_det_phase(r, s_df[lane], mreq[i]);
+          mixed_det_factors(r, mreq[i], s_ds[lane], s_ws[lane]);
         }
-        if (r.approximant == kPhenomPv2) mixed_det_phase(r, s_df[lane], mreq[i]);
-        mixed_det_factors(r, mreq[i], ds, ws);
       }
     } else {
       st = 4;

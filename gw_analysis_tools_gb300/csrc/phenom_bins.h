@@ -53,7 +53,7 @@ GW_HD void d_bin(const ModelD &m, double f, cd &hp, cd &hc) {
   if (f < m.s.f1_phase) {
     precalc_powers_ins(f, M, p);
   } else {
-    p.MFsixth = pow(M * f, 1. / 6.);
+    p.MFsixth = sqrt(cbrt(M * f));
     p.MF7sixth = pow_int(p.MFsixth, 7);
   }
   double amp = (m.A0eff * build_amp(f, m, p));
@@ -62,9 +62,9 @@ GW_HD void d_bin(const ModelD &m, double f, cd &hp, cd &hc) {
   double sn, cs;
   sincos(phase, &sn, &cs);
   cd h{amp * cs, -(amp * sn)};
-  double ci = cos(m.s.incl_angle);
+  const double ci = m.s.cos_incl;
   hc = cd{h.im * ci, -h.re * ci};  // (-i h) cos(iota)
-  double fac = .5 * (1 + ci * ci);
+  const double fac = m.s.fac_incl;
   hp = cd{h.re * fac, h.im * fac};
 }
 

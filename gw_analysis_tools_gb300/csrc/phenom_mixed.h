@@ -117,7 +117,7 @@ GW_HDNI void wave64_prologue(const Request &r, double df, WaveF64 &x) {
   x.n_f2p = grid_first(s.f2_phase, df, true);
   x.n_cut = grid_first(m.fcut, df, true) - 1;    // last n with n df <= fcut
   const bool pv2 = (r.approximant == kPhenomPv2);
-  x.A_scale = m.A0eff * pow(Mdf, -7. / 6.) * (pv2 ? 0.5 : 1.0);
+  x.A_scale = m.A0eff * pow_m7_6(Mdf) * (pv2 ? 0.5 : 1.0);
   const double cu = cbrt(Mdf);
   const double K = 3. / (128. * eta) * m.pi.PIminus_5third;
   const double *pn = m.pn_phase;
@@ -135,21 +135,21 @@ GW_HDNI void wave64_prologue(const Request &r, double df, WaveF64 &x) {
   q[9] = (3. / 4.) * m.l.sigma[2] / eta;
   q[10] = (3. / 5.) * m.l.sigma[3] / eta;
   q[11] = (1. / 2.) * m.l.sigma[4] / eta;
-  double cp = pow(cu, -5.);
+  double cp = 1.0 / ((cu * cu) * (cu * cu) * cu);  // cu^-5
   for (int j = 0; j < 12; j++) {
     x.qi[j] = q[j] * cp;
     cp *= cu;
   }
   x.bi0 = K * m.pi.PI5third * pn[9];
   x.bi1 = -K * m.pi.PIsquare * pn[11] * cu;
-  x.pA = (m.l.beta[0] + m.l.beta[2] * log(Mdf)) / eta;
+  x.pA = (m.l.beta[0] + m.l.beta[2] * (Lc - kLnPi)) / eta;  // ln(M df)
   x.pB = m.l.beta[1] * Mdf / eta;
   x.pC = m.l.beta[2] / eta;
   x.pD = m.l.beta[3] / (3. * eta * Mdf * Mdf * Mdf);
   x.mA = m.l.alpha[0] / eta;
   x.mB = m.l.alpha[1] * Mdf / eta;
   x.mC = m.l.alpha[2] / (eta * Mdf);
-  x.mD = (4. / 3.) * m.l.alpha[3] * pow(Mdf, 0.75) / eta;
+  x.mD = (4. / 3.) * m.l.alpha[3] * sqrt(Mdf * sqrt(Mdf)) / eta;
   x.mE = m.l.alpha[4] / eta;
   x.nc = m.l.alpha[5] * s.fRD / df;
   x.inv_nw = df / s.fdamp;
@@ -239,10 +239,13 @@ GW_HD uint64_t turns_q64(double turns) {  // frac(turns) * 2^64
 // The mixed constants in parts (regions and scale, phase, amplitude, Pv2
 // angles, detectors) so that the cooperative prologue can spread them over
 // warps; mixed_prologue runs them in order.
+// amplitude scale: A0eff * (M df)^(-7/6) [* 1/2 for the Pv2 amp/2]
+GW_HD double mixed_a_scale(const Request &r, double df) {
+  return r.m.A0eff * pow_m7_6(r.m.s.M * df) * (r.approximant == kPhenomPv2 ? 0.5 : 1.0);
+}
 GW_HD void mixed_regions(const Request &r, double df, MixedReq &x) {
   const ModelD &m = r.m;
   const Source &s = m.s;
-  const double Mdf = s.M * df;
   x.approximant = r.approximant;
   x.status = m.status;
   x.ndet = r.ndet;
@@ -252,9 +255,7 @@ GW_HD void mixed_regions(const Request &r, double df, MixedReq &x) {
   x.n_f3 = grid_first(s.f3, df, true);           // amp: f > f3 ringdown
   x.n_f2p = grid_first(s.f2_phase, df, true);
   x.n_cut = grid_first(m.fcut, df, true) - 1;    // last n with n df <= fcut
-  const bool pv2 = (r.approximant == kPhenomPv2);
-  // amplitude scale: A0eff * (M df)^(-7/6) [* 1/2 for the Pv2 amp/2]
-  x.A_scale = m.A0eff * pow(Mdf, -7. / 6.) * (pv2 ? 0.5 : 1.0);
+  x.A_scale = mixed_a_scale(r, df);
 }
 GW_HD void mixed_phase_coeffs(const Request &r, double df, MixedReq &x) {
   const ModelD &m = r.m;
@@ -281,7 +282,7 @@ GW_HD void mixed_phase_coeffs(const Request &r, double df, MixedReq &x) {
   q[9] = (3. / 4.) * m.l.sigma[2] / eta;
   q[10] = (3. / 5.) * m.l.sigma[3] / eta;
   q[11] = (1. / 2.) * m.l.sigma[4] / eta;
-  double cp = pow(cu, -5.);
+  double cp = 1.0 / ((cu * cu) * (cu * cu) * cu);  // cu^-5
   for (int j = 0; j < 12; j++) {
     x.qi[j] = q[j] * cp;
     cp *= cu;
@@ -289,7 +290,7 @@ GW_HD void mixed_phase_coeffs(const Request &r, double df, MixedReq &x) {
   x.bi0 = K * m.pi.PI5third * pn[9];
   x.bi1 = -K * m.pi.PIsquare * pn[11] * cu;
   // ---------------- intermediate phase
-  x.pA = (m.l.beta[0] + m.l.beta[2] * log(Mdf)) / eta;
+  x.pA = (m.l.beta[0] + m.l.beta[2] * (Lc - kLnPi)) / eta;  // ln(M df)
   x.pB = m.l.beta[1] * Mdf / eta;
   x.pC = m.l.beta[2] / eta;
   x.pD = m.l.beta[3] / (3. * eta * Mdf * Mdf * Mdf);
@@ -297,7 +298,7 @@ GW_HD void mixed_phase_coeffs(const Request &r, double df, MixedReq &x) {
   x.mA = m.l.alpha[0] / eta;
   x.mB = m.l.alpha[1] * Mdf / eta;
   x.mC = m.l.alpha[2] / (eta * Mdf);
-  x.mD = (4. / 3.) * m.l.alpha[3] * pow(Mdf, 0.75) / eta;
+  x.mD = (4. / 3.) * m.l.alpha[3] * sqrt(Mdf * sqrt(Mdf)) / eta;
   x.mE = m.l.alpha[4] / eta;
   {
     double nc = m.l.alpha[5] * s.fRD / df;
@@ -407,7 +408,7 @@ GW_HD void mixed_det_phase(const Request &r, double df, MixedReq &x) {
   double c0 = (m.tcl * m.fref - m.phic) * inv2pi;
   double c1 = -m.tcl * df * inv2pi;
   if (pv2) c1 += r.p.t_corr * df;
-  double ci = cos(s.incl_angle);
+  double ci = s.cos_incl;
   for (int d = 0; d < r.ndet; d++) {
     x.det[d].L0 = turns_q64(c0);
     x.det[d].L1 = turns_q64(c1 - r.det[d].tau * df * inv2pi);
@@ -420,11 +421,13 @@ GW_HD void mixed_det_phase(const Request &r, double df, MixedReq &x) {
     }
   }
 }
-GW_HD void mixed_det_factors(const Request &r, MixedReq &x, const double *dscale, const double *wscale) {
+// A: the amplitude scale (x.A_scale, passed so that a caller that has just
+// computed it need not read it back).
+GW_HD void mixed_det_factors_a(const Request &r, MixedReq &x, double A, const double *dscale, const double *wscale) {
   const bool pv2 = (r.approximant == kPhenomPv2);
   for (int d = 0; d < r.ndet; d++) {
     // HH = A^2 w |G h|^2 sums, DH = A d Re(G ...) sums; log L = -HH/2 + DH
-    const double A = x.A_scale, G1 = x.det[d].Gre, G2 = x.det[d].Gim, w = wscale[d], ds = dscale[d];
+    const double G1 = x.det[d].Gre, G2 = x.det[d].Gim, w = wscale[d], ds = dscale[d];
     double *f = x.fc + d * kAccPerDet;
     if (pv2) {
       f[0] = -0.5 * A * A * w * G1 * G1;
@@ -442,6 +445,9 @@ GW_HD void mixed_det_factors(const Request &r, MixedReq &x, const double *dscale
   }
   for (int d = r.ndet; d < kMaxDet; d++)
     for (int j = 0; j < kAccPerDet; j++) x.fc[d * kAccPerDet + j] = 0.0;
+}
+GW_HD void mixed_det_factors(const Request &r, MixedReq &x, const double *dscale, const double *wscale) {
+  mixed_det_factors_a(r, x, x.A_scale, dscale, wscale);
 }
 GW_HD void mixed_det_coeffs(const Request &r, double df, MixedReq &x, const double *dscale, const double *wscale) {
   mixed_det_phase(r, df, x);

@@ -26,6 +26,7 @@
 namespace gwt {
 
 constexpr double kPi = 3.14159265358979323846;
+constexpr double kLnPi = 1.1447298858494002;  // ln(pi)
 constexpr double kGammaE = 0.5772156649015328606065120900824024310421;
 constexpr double kC = 299792458.;
 constexpr double kMsolSec = 4.925491025543575903411922162094833998e-6;
@@ -60,6 +61,7 @@ struct Source {
   int shift_time, shift_phase, sky_average, dep_postmerger, pv2;
   double fRD, fdamp, f1, f3, f1_phase, f2_phase;
   double chip, phip, chil, SP, SL, phi_aligned, alpha0, thetaJN, zeta_polariz, q;
+  double cos_incl, fac_incl;  // cos(incl_angle), (1 + cos^2) / 2
 };
 
 struct Lambda {
@@ -111,8 +113,12 @@ GW_HD double pow_int(double base, int power) {  // util.cpp:1585-1597
   if (power > 0) return prod;
   return 1. / prod;
 }
+// FP64 pow costs about as much as a log and an exp together; where the
+// exponent allows, products, sqrt and cbrt take its place (a few ulp apart).
 GW_HD double calc_chirpmass(double m1, double m2) { return pow(m1 * m2, 3. / 5) / pow(m1 + m2, 1. / 5); }
-GW_HD double calc_eta(double m1, double m2) { return (m1 * m2) / pow(m1 + m2, 2); }
+GW_HD double calc_eta(double m1, double m2) { return (m1 * m2) / ((m1 + m2) * (m1 + m2)); }
+GW_HD double pow_m7_6(double x) { return 1.0 / (x * sqrt(cbrt(x))); }  // x^(-7/6)
+GW_HD double pow_7_6(double x) { return x * sqrt(cbrt(x)); }           // x^(7/6)
 GW_HD double calc_mass1(double mc, double eta) {  // util.cpp:1516
   double etapow = pow(eta, 3. / 5);
   return 1. / 2 * (mc / etapow + sqrt(1. - 4 * eta) * mc / etapow);
@@ -135,9 +141,9 @@ GW_HD void populate(Source &s, const GenParams &in) {
   s.spin2z = in.spin2[2];
   s.chi_s = (1. / 2) * (s.spin1z + s.spin2z);
   s.chi_a = (1. / 2) * (s.spin1z - s.spin2z);
-  s.chirpmass = calc_chirpmass(s.mass1, s.mass2);
   s.eta = calc_eta(s.mass1, s.mass2);
   s.M = s.mass1 + s.mass2;
+  s.chirpmass = s.M * pow(s.eta, 3. / 5);  // (m1 m2)^(3/5) / M^(1/5)
   s.chi_eff = (s.mass1 * (s.spin1z) + s.mass2 * (s.spin2z)) / (s.M);
   s.chi_pn = s.chi_eff - (38 * s.eta / 113) * (2 * s.chi_s);
   s.DL = in.Luminosity_Distance * (kMpcSI / kC);
@@ -147,10 +153,12 @@ GW_HD void populate(Source &s, const GenParams &in) {
   s.sky_average = in.sky_average;
   // A0_from_DL (util.cpp:1271-1279)
   if (s.sky_average)
-    s.A0 = sqrt(kPi / 30) * s.chirpmass * s.chirpmass / s.DL * pow(kPi * s.chirpmass, -7. / 6);
+    s.A0 = sqrt(kPi / 30) * s.chirpmass * s.chirpmass / s.DL * pow_m7_6(kPi * s.chirpmass);
   else
-    s.A0 = sqrt(kPi * 40. / 192.) * s.chirpmass * s.chirpmass / s.DL * pow(kPi * s.chirpmass, -7. / 6);
+    s.A0 = sqrt(kPi * 40. / 192.) * s.chirpmass * s.chirpmass / s.DL * pow_m7_6(kPi * s.chirpmass);
   s.incl_angle = in.incl_angle;
+  s.cos_incl = cos(in.incl_angle);
+  s.fac_incl = .5 * (1 + s.cos_incl * s.cos_incl);
   s.f_ref = in.f_ref;
   s.shift_time = in.shift_time;
   s.shift_phase = in.shift_phase;
@@ -250,7 +258,7 @@ GW_HD void precalc_powers_ins(double f, double M, Pows &p) {  // IMRPhenomD.cpp:
   double Mf = M * f;
   p.MFsquare = Mf * Mf;
   p.MFcube = Mf * Mf * Mf;
-  p.MFsixth = pow(M * f, 1. / 6.);
+  p.MFsixth = sqrt(cbrt(Mf));
   p.MF7sixth = p.MFsixth * M * f;
   p.MFthird = p.MFsixth * p.MFsixth;
   p.MF2third = p.MFthird * p.MFthird;
@@ -263,7 +271,7 @@ GW_HD void precalc_powers_ins(double f, double M, Pows &p) {  // IMRPhenomD.cpp:
 GW_HD void precalc_powers_PI(Pows &p) {  // IMRPhenomD.cpp:937-950
   p.PIsquare = kPi * kPi;
   p.PIcube = kPi * kPi * kPi;
-  p.PIthird = pow(kPi, 1. / 3.);
+  p.PIthird = 1.4645918875615231;  // pow(pi, 1/3)
   p.PI2third = p.PIthird * p.PIthird;
   p.PI4third = p.PIthird * kPi;
   p.PI5third = p.PI2third * kPi;

@@ -158,40 +158,82 @@ GW_HD void d_deltas(ModelD &m, const AmpConn &a, int j0, int j1) {
   }
 }
 // phase_connection_coefficients (IMRPhenomD.cpp:1614-1674)
-GW_HD void d_phase_conn(ModelD &m) {
-  Source &s = m.s;
+// The C1 phase connection (IMRPhenomD.cpp: the beta0/beta1 and alpha0/alpha1
+// constants) in parts: the inspiral values at f1, and the intermediate and
+// merger-ringdown terms that do not involve the connection constants.  The
+// two parts are independent (the cooperative prologue runs them at once);
+// phase_conn_combine then forms the constants:
+//   beta1  = eta/M (Dins(f1) - Dint(f1)|beta0=beta1=0)
+//   beta0  = eta (ins(f1) - int(f1)|beta0=0)
+//   alpha1 = eta/M (Dint(f2) - Dmr(f2)|alpha0=alpha1=0)
+//   alpha0 = eta (int(f2) - mr(f2)|alpha0=0)
+struct PhaseConnParts {
+  double Dins1, ins1;      // inspiral derivative and phase at f1
+  double Dint1, P1, Q1;    // at f1: Dint with beta1 = 0; beta2 ln Mf1; beta3 / 3 / Mf1^3
+  double R2, S2, P2, Q2;   // at f2: beta2 / f2; beta3 / M^3 / f2^4; beta2 ln Mf2; beta3 / 3 / Mf2^3
+  double Dmr2, T1, T2, T3; // at f2: Dmr with alpha1 = 0; alpha2 / Mf2; 4/3 alpha3 Mf2^(3/4); alpha4 atan(..)
+};
+GW_HD void phase_conn_ins(const ModelD &m, PhaseConnParts &c) {
+  const Source &s = m.s;
+  const double f1 = s.f1_phase;
+  double pn[12];  // coefficients 5 and 6 are set at f1 by both calls
+  for (int j = 0; j < 12; j++) pn[j] = m.pn_phase[j];
+  c.Dins1 = Dphase_ins(f1, s, pn, m.l);
+  Pows pw;
+  precalc_powers_ins(f1, s.M, pw);
+  c.ins1 = phase_ins(f1, s, pn, m.l, m.pi, pw);
+}
+GW_HD void phase_conn_imr(const ModelD &m, PhaseConnParts &c) {
+  const Source &s = m.s;
+  const Lambda &l = m.l;
+  const double M = s.M, eta = s.eta, M3 = M * M * M;
+  {
+    const double f = s.f1_phase, ff = f * f, Mf = M * f, Mf3 = Mf * Mf * Mf;
+    c.Dint1 = (1. / eta) * (l.beta[2] / f + l.beta[3] / M3 / (ff * ff));
+    c.P1 = l.beta[2] * log(Mf);
+    c.Q1 = l.beta[3] / 3. * 1. / Mf3;
+  }
+  {
+    const double f = s.f2_phase, ff = f * f, Mf = M * f, Mf3 = Mf * Mf * Mf;
+    c.R2 = l.beta[2] / f;
+    c.S2 = l.beta[3] / M3 / (ff * ff);
+    c.P2 = l.beta[2] * log(Mf);
+    c.Q2 = l.beta[3] / 3. * 1. / Mf3;
+    const double u = f - l.alpha[5] * s.fRD;
+    c.Dmr2 = (l.alpha[4] / (s.fdamp * (1. + (u * u) / (s.fdamp * s.fdamp))) + l.alpha[2] / ((f * f) * M) +
+              M * (l.alpha[3] / sqrt(sqrt(f * M)))) /
+             eta;
+    c.T1 = l.alpha[2] * (1. / (Mf));
+    c.T2 = (4. / 3) * l.alpha[3] * sqrt(sqrt(Mf * Mf * Mf));
+    c.T3 = l.alpha[4] * atan((f - l.alpha[5] * s.fRD) / s.fdamp);
+  }
+}
+GW_HD void phase_conn_combine(ModelD &m, const PhaseConnParts &c) {
+  const Source &s = m.s;
   Lambda &l = m.l;
-  l.beta[0] = 0;
-  l.beta[1] = 0;
-  l.alpha[0] = 0;
-  l.alpha[1] = 0;
-  double M = s.M, eta = s.eta;
+  const double M = s.M, eta = s.eta;
+  l.beta[1] = (eta / M) * c.Dins1 - (eta / M) * c.Dint1;
   {
-    double f1 = s.f1_phase;
-    double Dins = Dphase_ins(f1, s, m.pn_phase, l);
-    double Dint = Dphase_int(f1, s, l);
-    l.beta[1] = (eta / M) * Dins - (eta / M) * Dint;
+    const double Mf = M * s.f1_phase;
+    const double intval = (1. / eta) * (l.beta[1] * Mf + c.P1 - c.Q1);
+    l.beta[0] = (eta)*c.ins1 - eta * intval;
   }
   {
-    double f1 = s.f1_phase;
-    Pows pw;
-    precalc_powers_ins(f1, M, pw);
-    double ins = phase_ins(f1, s, m.pn_phase, l, m.pi, pw);
-    double intval = phase_int(f1, s, l);
-    l.beta[0] = (eta)*ins - eta * intval;
+    const double Dint = (1. / eta) * (l.beta[1] * M + c.R2 + c.S2);
+    l.alpha[1] = (eta / M) * Dint - eta / M * c.Dmr2;
   }
   {
-    double f2 = s.f2_phase;
-    double Dint = Dphase_int(f2, s, l);
-    double Dmr = Dphase_mr(f2, s, l);
-    l.alpha[1] = (eta / M) * Dint - eta / M * Dmr;
-  }
-  {
-    double f2 = s.f2_phase;
-    double intval = phase_int(f2, s, l);
-    double mr = phase_mr(f2, s, l);
+    const double Mf = M * s.f2_phase;
+    const double intval = (1. / eta) * (l.beta[0] + l.beta[1] * Mf + c.P2 - c.Q2);
+    const double mr = (1. / eta) * (l.alpha[1] * Mf - c.T1 + c.T2 + c.T3);
     l.alpha[0] = (eta)*intval - eta * mr;
   }
+}
+GW_HD void d_phase_conn(ModelD &m) {
+  PhaseConnParts c;
+  phase_conn_ins(m, c);
+  phase_conn_imr(m, c);
+  phase_conn_combine(m, c);
 }
 GW_HDNI void d_connections(ModelD &m) {
   AmpConn a;
@@ -263,7 +305,7 @@ GW_HDNI void model_d_finish(ModelD &m) {
     tc_shift = Dphase_mr(s.f3, s, m.l) + (-m.l.alpha[1] + alpha1_offset) * s.M / s.eta;
   }
   m.tcl = 2 * kPi * s.tc + tc_shift;
-  m.A0eff = s.A0 * pow(M, 7. / 6.);
+  m.A0eff = s.A0 * pow_7_6(M);
 }
 
 // ------------------------------------------------------------- IMRPhenomPv2
@@ -468,10 +510,10 @@ GW_HDNI void model_p_finish(ModelD &m, ModelP &pm) {
   m.fref = s.f_ref;
   m.phic = 2 * s.phi_aligned;
   m.tcl = 2 * kPi * s.tc;
-  m.A0eff = s.A0 * pow(s.M, 7. / 6.) / (2. * sqrt(5. / (64. * kPi)));
+  m.A0eff = s.A0 * pow_7_6(s.M) / (2. * sqrt(5. / (64. * kPi)));
   s.q = s.mass1 / s.mass2;
   pv2_euler_coeffs(pm.ac, pm.ec, s);
-  double MFthird = pow(s.M * s.f_ref, 1. / 3.);
+  double MFthird = cbrt(s.M * s.f_ref);
   double aoff, eoff;
   pv2_euler_angles(aoff, eoff, MFthird, m.pi.PIthird, pm.ac, pm.ec);
   pm.alpha_shift = s.alpha0 - aoff;
