@@ -282,9 +282,10 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 // sub-partitions at once shortens that chain.  Lane j of every warp works on
 // request blockIdx.x * kCoopReq + j; shared memory holds the requests between
 // stages.  Stage plan (W0..W3 = warps):
-//   S0  W0 parameters, source;  W3 detector projections
-//   S1  W0 calibration fits;  W1 D: ringdown frequencies / Pv2: J-frame transform;  W2 PN coefficients
-//   S2  W0 Pv2: ringdown frequencies; matching frequencies
+//   S0  W0 parameters, source;  W1-W3 detector projections
+//   S1  W0/W3 calibration fits;  W1 D: ringdown frequencies / Pv2: J-frame transform;  W2 PN coefficients
+//   S2  W0 Pv2: ringdown frequencies; matching frequencies;  W1 D: phase at f_ref (inspiral);
+//       W2 D: ringdown-phase terms at f3
 //   S3  W0/W1 amplitude matching points;  D: W2/W3 phase connection, inspiral / other parts;
 //       Pv2: W2 phase connection, W3 Euler and frame constants
 //   S4  W0/W1 amplitude deltas;  W2 D: phase connection constants, phase/time shift /
@@ -330,12 +331,12 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     r.ndet = ndet;
     if (!bad) populate(r.m.s, q);
   }
-  if (act && warp == 3) {  // projections need only the sky position
+  if (act && warp >= 1) {  // projections need only the sky position: detectors over warps 1-3
     const GenParams &q = params[i];
     SkyTrig tr;
     sky_trig(q.RA, q.DEC, q.psi, q.gmst, tr);
     const int d0 = streams[handles[i * ndet]].det;
-    for (int d = 0; d < ndet && d < kMaxDet; d++) {
+    for (int d = warp - 1; d < ndet && d < kMaxDet; d += kCoopWarps - 1) {
       const StreamDev &sd = streams[handles[i * ndet + d]];
       const int dd = sd.det;
       s_ds[lane][d] = sd.dscale;
@@ -349,7 +350,8 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   const bool pv2 = run && r.approximant == kPhenomPv2;
   // S1
   if (run) {
-    if (warp == 0) model_d_lambdas(r.m);
+    if (warp == 0) model_d_lambdas_a(r.m);
+    if (warp == 3) model_d_lambdas_b(r.m);
     if (warp == 1) {
       if (pv2) model_p_setup(r.m, r.p, p);
       else post_merger(r.m.s, qnm);
@@ -362,6 +364,8 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     if (pv2) post_merger(r.m.s, qnm);
     model_d_freqs(r.m);
   }
+  if (run && warp == 1 && !pv2) finish_fref_phase(r.m, s_pc[lane]);
+  if (run && warp == 2 && !pv2) finish_f3_terms(r.m, fpeak(r.m.s, r.m.l), s_pc[lane]);
   __syncthreads();
   // S3
   if (run) {
@@ -383,7 +387,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     if (!pv2) {
       if (warp == 2) {
         phase_conn_combine(r.m, s_pc[lane]);
-        model_d_finish(r.m);
+        model_d_finish_parts(r.m, s_pc[lane]);
       }
     } else if (r.m.s.shift_time && (warp == 2 || warp == 3)) {
       for (int j = (warp - 2) * (kPv2ShiftNodes / 2); j < (warp - 1) * (kPv2ShiftNodes / 2); j++)

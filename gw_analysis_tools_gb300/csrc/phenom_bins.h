@@ -33,8 +33,8 @@ GW_HD double build_phase_bin(double f, const ModelD &m, const Pows &p) {
     double pn_phase = pn[0] + pn[1] * m.pi.PIthird * p.MFthird + pn[2] * m.pi.PI2third * p.MF2third +
                       pn[3] * kPi * M * f + pn[4] * m.pi.PI4third * p.MF4third + c5 * m.pi.PI5third * p.MF5third +
                       c6 * m.pi.PIsquare * p.MFsquare + pn[7] * m.pi.PI7third * p.MF7third;
-    double phase_TF2 = -kPi / 4. + 3. / (128. * eta) * m.pi.PIminus_5third * p.MFminus_5third * pn_phase;
-    return phase_TF2 + (1. / eta) * (0 + m.l.sigma[1] * M * f + (3. / 4.) * m.l.sigma[2] * p.MF4third +
+    double phase_TF2 = -kPi / 4. + s.k_tf2 * m.pi.PIminus_5third * p.MFminus_5third * pn_phase;
+    return phase_TF2 + s.inv_eta * (0 + m.l.sigma[1] * M * f + (3. / 4.) * m.l.sigma[2] * p.MF4third +
                                      (3. / 5) * m.l.sigma[3] * p.MF5third + (1. / 2.) * m.l.sigma[4] * p.MFsquare);
   }
   if (f > s.f2_phase) return phase_mr(f, s, m.l);

@@ -118,8 +118,8 @@ GW_HDNI void wave64_prologue(const Request &r, double df, WaveF64 &x) {
   x.n_cut = grid_first(m.fcut, df, true) - 1;    // last n with n df <= fcut
   const bool pv2 = (r.approximant == kPhenomPv2);
   x.A_scale = m.A0eff * pow_m7_6(Mdf) * (pv2 ? 0.5 : 1.0);
-  const double cu = cbrt(Mdf);
-  const double K = 3. / (128. * eta) * m.pi.PIminus_5third;
+  const double cu = cbrt(Mdf), iMdf = 1. / Mdf;
+  const double K = s.k_tf2 * m.pi.PIminus_5third;
   const double *pn = m.pn_phase;
   const double Lc = log(kPi * Mdf);
   double q[12];
@@ -131,10 +131,10 @@ GW_HDNI void wave64_prologue(const Request &r, double df, WaveF64 &x) {
   q[5] = K * m.pi.PI5third * (pn[8] + pn[9] * Lc) - kPi / 4.;
   q[6] = K * m.pi.PIsquare * (pn[10] - pn[11] * Lc);
   q[7] = K * pn[7] * m.pi.PI7third;
-  q[8] = m.l.sigma[1] / eta;
-  q[9] = (3. / 4.) * m.l.sigma[2] / eta;
-  q[10] = (3. / 5.) * m.l.sigma[3] / eta;
-  q[11] = (1. / 2.) * m.l.sigma[4] / eta;
+  q[8] = m.l.sigma[1] * s.inv_eta;
+  q[9] = (3. / 4.) * m.l.sigma[2] * s.inv_eta;
+  q[10] = (3. / 5.) * m.l.sigma[3] * s.inv_eta;
+  q[11] = (1. / 2.) * m.l.sigma[4] * s.inv_eta;
   double cp = 1.0 / ((cu * cu) * (cu * cu) * cu);  // cu^-5
   for (int j = 0; j < 12; j++) {
     x.qi[j] = q[j] * cp;
@@ -142,15 +142,15 @@ GW_HDNI void wave64_prologue(const Request &r, double df, WaveF64 &x) {
   }
   x.bi0 = K * m.pi.PI5third * pn[9];
   x.bi1 = -K * m.pi.PIsquare * pn[11] * cu;
-  x.pA = (m.l.beta[0] + m.l.beta[2] * (Lc - kLnPi)) / eta;  // ln(M df)
-  x.pB = m.l.beta[1] * Mdf / eta;
-  x.pC = m.l.beta[2] / eta;
-  x.pD = m.l.beta[3] / (3. * eta * Mdf * Mdf * Mdf);
-  x.mA = m.l.alpha[0] / eta;
-  x.mB = m.l.alpha[1] * Mdf / eta;
-  x.mC = m.l.alpha[2] / (eta * Mdf);
-  x.mD = (4. / 3.) * m.l.alpha[3] * sqrt(Mdf * sqrt(Mdf)) / eta;
-  x.mE = m.l.alpha[4] / eta;
+  x.pA = (m.l.beta[0] + m.l.beta[2] * (Lc - kLnPi)) * s.inv_eta;  // ln(M df)
+  x.pB = m.l.beta[1] * Mdf * s.inv_eta;
+  x.pC = m.l.beta[2] * s.inv_eta;
+  x.pD = m.l.beta[3] * s.inv_eta * ((1. / 3.) * (iMdf * iMdf * iMdf));
+  x.mA = m.l.alpha[0] * s.inv_eta;
+  x.mB = m.l.alpha[1] * Mdf * s.inv_eta;
+  x.mC = m.l.alpha[2] * s.inv_eta * iMdf;
+  x.mD = (4. / 3.) * m.l.alpha[3] * sqrt(Mdf * sqrt(Mdf)) * s.inv_eta;
+  x.mE = m.l.alpha[4] * s.inv_eta;
   x.nc = m.l.alpha[5] * s.fRD / df;
   x.inv_nw = df / s.fdamp;
   {
@@ -265,8 +265,8 @@ GW_HD void mixed_phase_coeffs(const Request &r, double df, MixedReq &x) {
   (void)eta;
   (void)Mdf;
   // ---------------- inspiral phase: u = (M f)^(1/3) = cu t, t = n^(1/3)
-  const double cu = cbrt(Mdf);
-  const double K = 3. / (128. * eta) * m.pi.PIminus_5third;
+  const double cu = cbrt(Mdf), iMdf = 1. / Mdf;
+  const double K = s.k_tf2 * m.pi.PIminus_5third;
   const double *pn = m.pn_phase;
   const double Lc = log(kPi * Mdf);  // ln(pi M f) = Lc + ln n
   double q[12];
@@ -278,10 +278,10 @@ GW_HD void mixed_phase_coeffs(const Request &r, double df, MixedReq &x) {
   q[5] = K * m.pi.PI5third * (pn[8] + pn[9] * Lc) - kPi / 4.;
   q[6] = K * m.pi.PIsquare * (pn[10] - pn[11] * Lc);
   q[7] = K * pn[7] * m.pi.PI7third;
-  q[8] = m.l.sigma[1] / eta;
-  q[9] = (3. / 4.) * m.l.sigma[2] / eta;
-  q[10] = (3. / 5.) * m.l.sigma[3] / eta;
-  q[11] = (1. / 2.) * m.l.sigma[4] / eta;
+  q[8] = m.l.sigma[1] * s.inv_eta;
+  q[9] = (3. / 4.) * m.l.sigma[2] * s.inv_eta;
+  q[10] = (3. / 5.) * m.l.sigma[3] * s.inv_eta;
+  q[11] = (1. / 2.) * m.l.sigma[4] * s.inv_eta;
   double cp = 1.0 / ((cu * cu) * (cu * cu) * cu);  // cu^-5
   for (int j = 0; j < 12; j++) {
     x.qi[j] = q[j] * cp;
@@ -290,16 +290,16 @@ GW_HD void mixed_phase_coeffs(const Request &r, double df, MixedReq &x) {
   x.bi0 = K * m.pi.PI5third * pn[9];
   x.bi1 = -K * m.pi.PIsquare * pn[11] * cu;
   // ---------------- intermediate phase
-  x.pA = (m.l.beta[0] + m.l.beta[2] * (Lc - kLnPi)) / eta;  // ln(M df)
-  x.pB = m.l.beta[1] * Mdf / eta;
-  x.pC = m.l.beta[2] / eta;
-  x.pD = m.l.beta[3] / (3. * eta * Mdf * Mdf * Mdf);
+  x.pA = (m.l.beta[0] + m.l.beta[2] * (Lc - kLnPi)) * s.inv_eta;  // ln(M df)
+  x.pB = m.l.beta[1] * Mdf * s.inv_eta;
+  x.pC = m.l.beta[2] * s.inv_eta;
+  x.pD = m.l.beta[3] * s.inv_eta * ((1. / 3.) * (iMdf * iMdf * iMdf));
   // ---------------- ringdown phase
-  x.mA = m.l.alpha[0] / eta;
-  x.mB = m.l.alpha[1] * Mdf / eta;
-  x.mC = m.l.alpha[2] / (eta * Mdf);
-  x.mD = (4. / 3.) * m.l.alpha[3] * sqrt(Mdf * sqrt(Mdf)) / eta;
-  x.mE = m.l.alpha[4] / eta;
+  x.mA = m.l.alpha[0] * s.inv_eta;
+  x.mB = m.l.alpha[1] * Mdf * s.inv_eta;
+  x.mC = m.l.alpha[2] * s.inv_eta * iMdf;
+  x.mD = (4. / 3.) * m.l.alpha[3] * sqrt(Mdf * sqrt(Mdf)) * s.inv_eta;
+  x.mE = m.l.alpha[4] * s.inv_eta;
   {
     double nc = m.l.alpha[5] * s.fRD / df;
     double nci = floor(nc);

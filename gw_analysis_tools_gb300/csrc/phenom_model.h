@@ -62,6 +62,7 @@ struct Source {
   double fRD, fdamp, f1, f3, f1_phase, f2_phase;
   double chip, phip, chil, SP, SL, phi_aligned, alpha0, thetaJN, zeta_polariz, q;
   double cos_incl, fac_incl;  // cos(incl_angle), (1 + cos^2) / 2
+  double inv_eta, k_tf2;      // 1 / eta and 3 / (128 eta), the divisions of the phase formulas
 };
 
 struct Lambda {
@@ -142,10 +143,12 @@ GW_HD void populate(Source &s, const GenParams &in) {
   s.chi_s = (1. / 2) * (s.spin1z + s.spin2z);
   s.chi_a = (1. / 2) * (s.spin1z - s.spin2z);
   s.eta = calc_eta(s.mass1, s.mass2);
+  s.inv_eta = 1. / s.eta;
+  s.k_tf2 = 3. / (128. * s.eta);
   s.M = s.mass1 + s.mass2;
   s.chirpmass = s.M * pow(s.eta, 3. / 5);  // (m1 m2)^(3/5) / M^(1/5)
   s.chi_eff = (s.mass1 * (s.spin1z) + s.mass2 * (s.spin2z)) / (s.M);
-  s.chi_pn = s.chi_eff - (38 * s.eta / 113) * (2 * s.chi_s);
+  s.chi_pn = s.chi_eff - ((38. / 113) * s.eta) * (2 * s.chi_s);
   s.DL = in.Luminosity_Distance * (kMpcSI / kC);
   s.delta_mass = sqrt(1. - 4 * s.eta);
   s.phiRef = in.phiRef;
@@ -278,44 +281,50 @@ GW_HD void precalc_powers_PI(Pows &p) {  // IMRPhenomD.cpp:937-950
   p.PI7third = p.PI4third * kPi;
   p.PIminus_5third = 1. / p.PI5third;
 }
+// The PN coefficients with every constant ratio folded (k * eta / n written
+// (k / n) * eta): a runtime FP64 division costs tens of instructions.
 GW_HD void pn_amp_coeff(const Source &s, double *coeff) {  // IMRPhenomD.cpp:955-986
   double md = s.delta_mass, eta = s.eta, ca = s.chi_a, cs = s.chi_s;
-  double eta2 = eta * eta, eta3 = eta2 * eta, cs2 = cs * cs, ca2 = ca * ca, pi2 = kPi * kPi;
+  double eta2 = eta * eta, eta3 = eta2 * eta, cs2 = cs * cs, ca2 = ca * ca;
+  constexpr double pi2 = kPi * kPi;
   coeff[0] = 1.;
   coeff[1] = 0.;
-  coeff[2] = (-323. / 224 + 451 * eta / 168);
-  coeff[3] = (27. * md * ca / 8 + (27. / 8 - 11. * eta / 6) * cs);
-  coeff[4] = (-27312085. / 8128512 - 1975055 * eta / 338688 + 105271 * eta2 / 24192 + (-81. / 32 + 8 * eta) * ca2 -
-              81 * md * ca * cs / 16 + (-81. / 32 + 17 * eta / 8) * cs2);
-  coeff[5] = 1. * (-85 * kPi / 64 + 85 * kPi * eta / 16 + md * (285197. / 16128 - 1579 * eta / 4032) * ca +
-                   (285197. / 16128 - 15317 * eta / 672 - 2227 * eta2 / 1008) * cs);
+  coeff[2] = (-323. / 224 + (451. / 168) * eta);
+  coeff[3] = ((27. / 8) * md * ca + (27. / 8 - (11. / 6) * eta) * cs);
+  coeff[4] = (-27312085. / 8128512 - (1975055. / 338688) * eta + (105271. / 24192) * eta2 +
+              (-81. / 32 + 8 * eta) * ca2 - (81. / 16) * md * ca * cs + (-81. / 32 + (17. / 8) * eta) * cs2);
+  coeff[5] = 1. * (-85 * kPi / 64 + (85 * kPi / 16) * eta + md * (285197. / 16128 - (1579. / 4032) * eta) * ca +
+                   (285197. / 16128 - (15317. / 672) * eta - (2227. / 1008) * eta2) * cs);
   coeff[6] = 1. * (-177520268561. / 8583708672 + (545384828789. / 5007163392 - 205 * pi2 / 48) * eta -
-                   3248849057 * eta2 / 178827264 + 34473079 * eta3 / 6386688 +
-                   (1614569. / 64512 - 1873643. * eta / 16128 + 2167 * eta2 / 42) * ca2 +
-                   (31 * kPi / 12 - 7 * kPi * eta / 3) * cs +
-                   (1614569. / 64512 - 61391 * eta / 1344 + 57451 * eta2 / 4032) * cs2 +
-                   md * ca * (31 * kPi / 12 + (1614569. / 32256 - 165961 * eta / 2688) * cs));
+                   (3248849057. / 178827264) * eta2 + (34473079. / 6386688) * eta3 +
+                   (1614569. / 64512 - (1873643. / 16128) * eta + (2167. / 42) * eta2) * ca2 +
+                   (31 * kPi / 12 - (7 * kPi / 3) * eta) * cs +
+                   (1614569. / 64512 - (61391. / 1344) * eta + (57451. / 4032) * eta2) * cs2 +
+                   md * ca * (31 * kPi / 12 + (1614569. / 32256 - (165961. / 2688) * eta) * cs));
 }
 GW_HD void pn_phase_coeff_static(const Source &s, double *coeff) {  // IMRPhenomD.cpp:992-1032
   double delta = s.delta_mass, eta = s.eta, ca = s.chi_a, cs = s.chi_s;
-  double eta2 = eta * eta, eta3 = eta2 * eta, cs2 = cs * cs, ca2 = ca * ca, pi2 = kPi * kPi;
+  double eta2 = eta * eta, eta3 = eta2 * eta, cs2 = cs * cs, ca2 = ca * ca;
+  constexpr double pi2 = kPi * kPi;
   coeff[0] = 1.;
   coeff[1] = 0.;
-  coeff[2] = 3715. / 756 + 55. * eta / 9;
-  coeff[3] = -16. * kPi + 113. * delta * ca / 3 + (113. / 3 - 76. * eta / 3) * cs;
-  coeff[4] = 15293365. / 508032 + 27145. * eta / 504 + 3085. * eta2 / 72 + (-405. / 8 + 200. * eta) * ca2 -
-             (405. / 4) * delta * ca * cs + (-405. / 8 + 5. * eta / 2) * cs2;
+  coeff[2] = 3715. / 756 + (55. / 9) * eta;
+  coeff[3] = -16. * kPi + (113. / 3) * delta * ca + (113. / 3 - (76. / 3) * eta) * cs;
+  coeff[4] = 15293365. / 508032 + (27145. / 504) * eta + (3085. / 72) * eta2 + (-405. / 8 + 200. * eta) * ca2 -
+             (405. / 4) * delta * ca * cs + (-405. / 8 + (5. / 2) * eta) * cs2;
   coeff[5] = 0.;
   coeff[6] = 0.;
-  coeff[7] = 77096675. * kPi / 254016 + 378515. * kPi * eta / 1512 - 74045. * kPi * eta2 / 756 +
-             delta * (-25150083775. / 3048192 + 26804935. * eta / 6048 - 1985. * eta2 / 48) * ca +
-             (-25150083775. / 3048192 + 10566655595. * eta / 762048 - 1042165. * eta2 / 3024 + 5345. * eta3 / 36) * cs;
-  coeff[8] = (38645. * kPi / 756 - 65. * kPi * eta / 9 + delta * (-732985. / 2268 - 140. * eta / 9) * ca +
-              (-732985. / 2268 + 24260. * eta / 81 + 340. * eta2 / 9) * cs);
+  coeff[7] = 77096675. * kPi / 254016 + (378515. * kPi / 1512) * eta - (74045. * kPi / 756) * eta2 +
+             delta * (-25150083775. / 3048192 + (26804935. / 6048) * eta - (1985. / 48) * eta2) * ca +
+             (-25150083775. / 3048192 + (10566655595. / 762048) * eta - (1042165. / 3024) * eta2 +
+              (5345. / 36) * eta3) *
+                 cs;
+  coeff[8] = (38645. * kPi / 756 - (65. * kPi / 9) * eta + delta * (-732985. / 2268 - (140. / 9) * eta) * ca +
+              (-732985. / 2268 + (24260. / 81) * eta + (340. / 9) * eta2) * cs);
   coeff[9] = coeff[8];
   coeff[10] = 11583231236531. / 4694215680 - 6848. * kGammaE / 21 - 640. * pi2 / 3 +
-              (-15737765635. / 3048192 + 2255. * pi2 / 12) * eta + 76055. * eta2 / 1728 - 127825. * eta3 / 1296 +
-              2270. * delta * ca * kPi / 3 + (2270. * kPi / 3 - 520. * kPi * eta) * cs - 6848. * (kLog64) / 63;
+              (-15737765635. / 3048192 + 2255. * pi2 / 12) * eta + (76055. / 1728) * eta2 - (127825. / 1296) * eta3 +
+              (2270. * kPi / 3) * delta * ca + (2270. * kPi / 3 - 520. * kPi * eta) * cs - 6848. * (kLog64) / 63;
   coeff[11] = 6848. / 63.;
 }
 GW_HD void pn_phase_coeff_nonstatic(const Source &s, double *coeff, double f) {  // IMRPhenomD.cpp:1040-1060
@@ -410,8 +419,8 @@ GW_HD double phase_ins(double f, const Source &s, double *pn, const Lambda &l, c
   double pn_phase = pn[0] + pn[1] * pi.PIthird * p.MFthird + pn[2] * pi.PI2third * p.MF2third + pn[3] * kPi * M * f +
                     pn[4] * pi.PI4third * p.MF4third + pn[5] * pi.PI5third * p.MF5third +
                     pn[6] * pi.PIsquare * p.MFsquare + pn[7] * pi.PI7third * p.MF7third;
-  double phase_TF2 = -kPi / 4. + 3. / (128. * eta) * pi.PIminus_5third * p.MFminus_5third * pn_phase;
-  return phase_TF2 + (1. / eta) * (0 + l.sigma[1] * M * f + (3. / 4.) * l.sigma[2] * p.MF4third +
+  double phase_TF2 = -kPi / 4. + s.k_tf2 * pi.PIminus_5third * p.MFminus_5third * pn_phase;
+  return phase_TF2 + s.inv_eta * (0 + l.sigma[1] * M * f + (3. / 4.) * l.sigma[2] * p.MF4third +
                                    (3. / 5) * l.sigma[3] * p.MF5third + (1. / 2.) * l.sigma[4] * p.MFsquare);
 }
 GW_HD double amp_mr(double f, const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1468-1478
@@ -423,7 +432,7 @@ GW_HD double amp_mr(double f, const Source &s, const Lambda &l) {  // IMRPhenomD
 }
 GW_HD double phase_mr(double f, const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1485-1503
   double M = s.M, eta = s.eta, Mf = M * f, Mfcube = Mf * Mf * Mf, Mf3fourths = sqrt(sqrt(Mfcube));
-  return (1. / eta) * (l.alpha[0] + l.alpha[1] * (Mf)-l.alpha[2] * (1. / (Mf)) + (4. / 3) * l.alpha[3] * Mf3fourths +
+  return s.inv_eta * (l.alpha[0] + l.alpha[1] * (Mf)-l.alpha[2] * (1. / (Mf)) + (4. / 3) * l.alpha[3] * Mf3fourths +
                        l.alpha[4] * atan((f - l.alpha[5] * s.fRD) / s.fdamp));
 }
 GW_HD double amp_int(double f, const ModelD &m) {  // IMRPhenomD.cpp:1560-1570
@@ -433,11 +442,11 @@ GW_HD double amp_int(double f, const ModelD &m) {  // IMRPhenomD.cpp:1560-1570
 }
 GW_HD double phase_int(double f, const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1577-1589
   double Mf = s.M * f, Mf3 = Mf * Mf * Mf;
-  return (1. / s.eta) * (l.beta[0] + l.beta[1] * (Mf) + l.beta[2] * log(Mf) - l.beta[3] / 3. * 1. / Mf3);
+  return s.inv_eta * (l.beta[0] + l.beta[1] * (Mf) + l.beta[2] * log(Mf) - l.beta[3] / 3. * 1. / Mf3);
 }
 GW_HD double Dphase_int(double f, const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1597-1607
   const double M3 = s.M * s.M * s.M, f2 = f * f;
-  return (1. / s.eta) * (l.beta[1] * (s.M) + l.beta[2] / f + l.beta[3] / M3 / (f2 * f2));
+  return s.inv_eta * (l.beta[1] * (s.M) + l.beta[2] / f + l.beta[3] / M3 / (f2 * f2));
 }
 GW_HD double Dphase_mr(double f, const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1539-1554
   double M = s.M, fdamp = s.fdamp, fRD = s.fRD, u = f - l.alpha[5] * fRD;

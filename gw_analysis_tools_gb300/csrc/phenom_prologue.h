@@ -42,12 +42,12 @@ GW_HD double Dphase_ins(double f, const Source &s, double *pn, const Lambda &l) 
   const double vm5 = 1. / (vp[5]);  // (pi M f)^(-5/3)
   double pn_phase = 0;
   for (int i = 0; i < 8; i++) pn_phase += pn[i] * vp[i];
-  double phase_TF2 = +3. / (128 * eta) * vm5 * (-5. / 3.) * inv_f * pn_phase;
+  double phase_TF2 = +s.k_tf2 * vm5 * (-5. / 3.) * inv_f * pn_phase;
   double pn_phase_deriv = 0;
   for (int i = 0; i < 8; i++) pn_phase_deriv += pn[i] * vp[i] * (i / 3.) * inv_f;
   pn_phase_deriv += d0 * vp[5] + d1 * vp[6];
-  phase_TF2 += pn_phase_deriv * (3. / (128 * eta) * vm5);
-  return phase_TF2 + (1. / eta) * (l.sigma[1] * M + l.sigma[2] * M * w + l.sigma[3] * M * w * w + l.sigma[4] * M * M * f);
+  phase_TF2 += pn_phase_deriv * (s.k_tf2 * vm5);
+  return phase_TF2 + s.inv_eta * (l.sigma[1] * M + l.sigma[2] * M * w + l.sigma[3] * M * w * w + l.sigma[4] * M * M * f);
 }
 // Integer powers of the three matching frequencies and of M used by the
 // intermediate-amplitude coefficients (products instead of pow calls).
@@ -172,6 +172,10 @@ struct PhaseConnParts {
   double Dint1, P1, Q1;    // at f1: Dint with beta1 = 0; beta2 ln Mf1; beta3 / 3 / Mf1^3
   double R2, S2, P2, Q2;   // at f2: beta2 / f2; beta3 / M^3 / f2^4; beta2 ln Mf2; beta3 / 3 / Mf2^3
   double Dmr2, T1, T2, T3; // at f2: Dmr with alpha1 = 0; alpha2 / Mf2; 4/3 alpha3 Mf2^(3/4); alpha4 atan(..)
+  // model_d_finish: the phase at f_ref when it lies in the inspiral (have_phi),
+  // the alpha1 fit, and the alpha1-free terms of Dphase_mr at f3
+  double phi_fref, a1fit, A3, B3;
+  int have_phi;
 };
 GW_HD void phase_conn_ins(const ModelD &m, PhaseConnParts &c) {
   const Source &s = m.s;
@@ -183,13 +187,36 @@ GW_HD void phase_conn_ins(const ModelD &m, PhaseConnParts &c) {
   precalc_powers_ins(f1, s.M, pw);
   c.ins1 = phase_ins(f1, s, pn, m.l, m.pi, pw);
 }
+// Dphase_mr(f3) (IMRPhenomD.cpp:1539-1554) = (A3 + M (alpha1 + B3)) / eta;
+// f3 = fpeak as model_d_freqs sets it (passed, so that this can run beside it).
+GW_HD void finish_f3_terms(const ModelD &m, double f3, PhaseConnParts &c) {
+  const Source &s = m.s;
+  const Lambda &l = m.l;
+  const double f = f3, M = s.M, u = f - l.alpha[5] * s.fRD;
+  c.A3 = l.alpha[4] / (s.fdamp * (1. + (u * u) / (s.fdamp * s.fdamp))) + l.alpha[2] / ((f * f) * M);
+  c.B3 = l.alpha[3] / sqrt(sqrt(f * M));
+}
+// The phase at f_ref when f_ref is in the inspiral part (the common case: it
+// needs neither the matching frequencies nor the connection constants).
+GW_HD void finish_fref_phase(const ModelD &m, PhaseConnParts &c) {
+  const Source &s = m.s;
+  c.have_phi = 0;
+  if (!s.shift_phase || !(s.f_ref < 0.018 / (s.M))) return;  // f1_phase = 0.018 / M
+  Pows pw;
+  precalc_powers_ins(s.f_ref, s.M, pw);
+  double pn[12];
+  for (int j = 0; j < 12; j++) pn[j] = m.pn_phase[j];
+  c.phi_fref = phase_ins(s.f_ref, s, pn, m.l, m.pi, pw);
+  c.have_phi = 1;
+}
 GW_HD void phase_conn_imr(const ModelD &m, PhaseConnParts &c) {
   const Source &s = m.s;
   const Lambda &l = m.l;
   const double M = s.M, eta = s.eta, M3 = M * M * M;
+  c.a1fit = l.alpha[1];  // still the fit: the connection replaces it
   {
     const double f = s.f1_phase, ff = f * f, Mf = M * f, Mf3 = Mf * Mf * Mf;
-    c.Dint1 = (1. / eta) * (l.beta[2] / f + l.beta[3] / M3 / (ff * ff));
+    c.Dint1 = s.inv_eta * (l.beta[2] / f + l.beta[3] / M3 / (ff * ff));
     c.P1 = l.beta[2] * log(Mf);
     c.Q1 = l.beta[3] / 3. * 1. / Mf3;
   }
@@ -215,17 +242,17 @@ GW_HD void phase_conn_combine(ModelD &m, const PhaseConnParts &c) {
   l.beta[1] = (eta / M) * c.Dins1 - (eta / M) * c.Dint1;
   {
     const double Mf = M * s.f1_phase;
-    const double intval = (1. / eta) * (l.beta[1] * Mf + c.P1 - c.Q1);
+    const double intval = s.inv_eta * (l.beta[1] * Mf + c.P1 - c.Q1);
     l.beta[0] = (eta)*c.ins1 - eta * intval;
   }
   {
-    const double Dint = (1. / eta) * (l.beta[1] * M + c.R2 + c.S2);
+    const double Dint = s.inv_eta * (l.beta[1] * M + c.R2 + c.S2);
     l.alpha[1] = (eta / M) * Dint - eta / M * c.Dmr2;
   }
   {
     const double Mf = M * s.f2_phase;
-    const double intval = (1. / eta) * (l.beta[0] + l.beta[1] * Mf + c.P2 - c.Q2);
-    const double mr = (1. / eta) * (l.alpha[1] * Mf - c.T1 + c.T2 + c.T3);
+    const double intval = s.inv_eta * (l.beta[0] + l.beta[1] * Mf + c.P2 - c.Q2);
+    const double mr = s.inv_eta * (l.alpha[1] * Mf - c.T1 + c.T2 + c.T3);
     l.alpha[0] = (eta)*intval - eta * mr;
   }
 }
@@ -246,18 +273,30 @@ GW_HDNI void d_connections(ModelD &m) {
 // Model setup shared by D and Pv2 (IMRPhenomD.cpp:410-432), in stages:
 // calibration fits, ringdown frequencies (post_merger), matching frequencies,
 // PN coefficients, connection coefficients.
-GW_HD void model_d_lambdas(ModelD &m) {
+// The fits in two independent halves (amplitude and inspiral; intermediate
+// and merger-ringdown phase), and the powers of pi.
+GW_HD void model_d_lambdas_a(ModelD &m) {
   const Source &s = m.s;
   Lambda &l = m.l;
   for (int i = 0; i < 4; i++) l.rho[i] = 0, l.gamma[i] = 0;
-  for (int i = 0; i < 5; i++) l.sigma[i] = 0, l.beta[i] = 0;
-  for (int i = 0; i < 7; i++) l.alpha[i] = 0;
+  for (int i = 0; i < 5; i++) l.sigma[i] = 0;
   for (int i = 0; i < 3; i++) l.rho[i] = lambda_elem(s, i);  // IMRPhenomD.cpp:833-852
   l.v2 = lambda_elem(s, 3);
   for (int i = 0; i < 3; i++) l.gamma[i] = lambda_elem(s, i + 4);
   for (int i = 0; i < 4; i++) l.sigma[i + 1] = lambda_elem(s, i + 7);
+  precalc_powers_PI(m.pi);
+}
+GW_HD void model_d_lambdas_b(ModelD &m) {
+  const Source &s = m.s;
+  Lambda &l = m.l;
+  for (int i = 0; i < 5; i++) l.beta[i] = 0;
+  for (int i = 0; i < 7; i++) l.alpha[i] = 0;
   for (int i = 0; i < 3; i++) l.beta[i + 1] = lambda_elem(s, i + 11);
   for (int i = 0; i < 5; i++) l.alpha[i + 1] = lambda_elem(s, i + 14);
+}
+GW_HD void model_d_lambdas(ModelD &m) {
+  model_d_lambdas_a(m);
+  model_d_lambdas_b(m);
 }
 // needs the fits and post_merger
 GW_HD void model_d_freqs(ModelD &m) {
@@ -266,7 +305,6 @@ GW_HD void model_d_freqs(ModelD &m) {
   s.f2_phase = s.fRD / 2.;
   s.f1 = 0.014 / (s.M);
   s.f3 = fpeak(s, m.l);
-  precalc_powers_PI(m.pi);
   for (int i = 0; i < 5; i++) m.deltas[i] = 0;
   m.fcut = .2 / s.M;
   m.status = kModelOK;
@@ -286,14 +324,21 @@ GW_HDNI int model_d_prologue(ModelD &m, const double *qnm) {
 }
 
 // D-specific phase/time shift and amplitude scale (IMRPhenomD.cpp:434-470)
-GW_HDNI void model_d_finish(ModelD &m) {
+GW_HD void model_d_finish_parts(ModelD &m, const PhaseConnParts &c) {
   Source &s = m.s;
   double M = s.M;
   if (s.shift_phase) {
     m.fref = s.f_ref;
-    Pows pw;
-    precalc_powers_ins(m.fref, M, pw);
-    double phi_shift = build_phase(m.fref, m, m.pn_phase, pw);
+    double phi_shift;
+    if (c.have_phi) {
+      phi_shift = c.phi_fref;
+    } else {
+      Pows pw;
+      precalc_powers_ins(m.fref, M, pw);
+      double pn[12];
+      for (int j = 0; j < 12; j++) pn[j] = m.pn_phase[j];
+      phi_shift = build_phase(m.fref, m, pn, pw);
+    }
     m.phic = 2 * s.phiRef + phi_shift;
   } else {
     m.fref = 0;
@@ -301,11 +346,18 @@ GW_HDNI void model_d_finish(ModelD &m) {
   }
   double tc_shift = 0;
   if (s.shift_time) {
-    double alpha1_offset = lambda_elem(s, 14);
-    tc_shift = Dphase_mr(s.f3, s, m.l) + (-m.l.alpha[1] + alpha1_offset) * s.M / s.eta;
+    const double Dmr = (c.A3 + M * (m.l.alpha[1] + c.B3)) / s.eta;
+    tc_shift = Dmr + (-m.l.alpha[1] + c.a1fit) * s.M / s.eta;
   }
   m.tcl = 2 * kPi * s.tc + tc_shift;
   m.A0eff = s.A0 * pow_7_6(M);
+}
+GW_HDNI void model_d_finish(ModelD &m) {
+  PhaseConnParts c;
+  finish_fref_phase(m, c);
+  finish_f3_terms(m, m.s.f3, c);
+  c.a1fit = lambda_elem(m.s, 14);
+  model_d_finish_parts(m, c);
 }
 
 // ------------------------------------------------------------- IMRPhenomPv2
@@ -537,7 +589,9 @@ struct SkyTrig {
 };
 GW_HD void sky_trig(double ra, double dec, double psi, double gmst, SkyTrig &t) {
   double gha = gmst - ra;
-  t.cg = cos(gha), t.sg = sin(gha), t.cd = cos(dec), t.sd = sin(dec), t.cp = cos(psi), t.sp = sin(psi);
+  sincos(gha, &t.sg, &t.cg);
+  sincos(dec, &t.sd, &t.cd);
+  sincos(psi, &t.sp, &t.cp);
 }
 GW_HD void antenna_trig(int det, const SkyTrig &t, double &fp, double &fc) {
   // detector_util.cpp:901-1015, geometric factor detector_util.cpp:1158-1160
