@@ -242,7 +242,7 @@ int gwgpu_context_create(int device, size_t budget, gwgpu_context **out) {
   }
   cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
-  std::vector<double> q(5 * gwt::kQnmLen);
+  std::vector<double> q(gwt::kQnmArrays * gwt::kQnmLen);
   gwk::qnm_host_table(q.data());
   c->qnm_host = q;
   int st = c->dalloc((void **)&c->qnm_dev, q.size() * sizeof(double), "qnm table");

@@ -282,7 +282,8 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 // sub-partitions at once shortens that chain.  Lane j of every warp works on
 // request blockIdx.x * kCoopReq + j; shared memory holds the requests between
 // stages.  Stage plan (W0..W3 = warps):
-//   S0  W0 parameters, source;  W1-W3 detector projections
+//   S0  W0 parameters, source;  W1/W2 detector projections, W2 inclination factors;
+//       W3 chirp mass and amplitude normalisation
 //   S1  W0/W3 calibration fits;  W1 D: ringdown frequencies / Pv2: J-frame transform;  W2 PN coefficients
 //   S2  W0 Pv2: ringdown frequencies; matching frequencies;  W1 D: phase at f_ref (inspiral);
 //       W2 D: ringdown-phase terms at f3
@@ -329,14 +330,16 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     s_uni[lane] = s0.uniform_int;
     r.approximant = ap;
     r.ndet = ndet;
-    if (!bad) populate(r.m.s, q);
+    if (!bad) populate_core(r.m.s, q);
   }
-  if (act && warp >= 1) {  // projections need only the sky position: detectors over warps 1-3
+  if (act && warp == 3) populate_amp(r.m.s, params[i]);
+  if (act && (warp == 1 || warp == 2)) {  // projections need only the sky position: detectors over warps 1, 2
     const GenParams &q = params[i];
+    if (warp == 2) populate_incl(r.m.s, q);
     SkyTrig tr;
     sky_trig(q.RA, q.DEC, q.psi, q.gmst, tr);
     const int d0 = streams[handles[i * ndet]].det;
-    for (int d = warp - 1; d < ndet && d < kMaxDet; d += kCoopWarps - 1) {
+    for (int d = warp - 1; d < ndet && d < kMaxDet; d += 2) {
       const StreamDev &sd = streams[handles[i * ndet + d]];
       const int dd = sd.det;
       s_ds[lane][d] = sd.dscale;
@@ -792,16 +795,6 @@ cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int block, cud
   return cudaGetLastError();
 }
 
-void qnm_host_table(double *o) {
-  const int n = kQnmLen;
-  for (int i = 0; i < n; i++) {
-    o[i] = gwt_qnm_a_h[i];
-    o[n + i] = gwt_qnm_fring_h[i];
-    o[2 * n + i] = gwt_qnm_fdamp_h[i];
-  }
-  double work[6 * kQnmLen];
-  cspline_coeffs(o, o + n, n, o + 3 * n, work);
-  cspline_coeffs(o, o + 2 * n, n, o + 4 * n, work);
-}
+void qnm_host_table(double *o) { qnm_fill(o, gwt_qnm_a_h, gwt_qnm_fring_h, gwt_qnm_fdamp_h); }
 
 }  // namespace gwk

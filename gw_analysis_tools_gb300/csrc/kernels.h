@@ -102,6 +102,6 @@ inline int status_code(int kernel_status) {
 }
 
 // Host-side helpers shared with the C API.
-void qnm_host_table(double *out5x1003);  // x, fring, fdamp, c_fring, c_fdamp
+void qnm_host_table(double *out);  // kQnmArrays x kQnmLen: x, fring, fdamp, c_fring, c_fdamp, b/d per interval
 
 }  // namespace gwk

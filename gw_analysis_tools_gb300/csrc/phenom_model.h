@@ -10,6 +10,7 @@
 #pragma once
 
 #include <cmath>
+#include <vector>
 #include <cstdint>
 #include <cstring>
 
@@ -131,7 +132,10 @@ GW_HD double calc_mass2(double mc, double eta) {  // util.cpp:1531
 
 // populate_source_parameters (util.cpp:997-1030) + prep_source_parameters
 // (waveform_generator.cpp:1255-1271)
-GW_HD void populate(Source &s, const GenParams &in) {
+// In three independent parts (the cooperative prologue runs them at once on
+// different warps): the masses, spins and ratios; the chirp mass and the
+// amplitude normalisation (a pow); the inclination factors.
+GW_HD void populate_core(Source &s, const GenParams &in) {
   s.mass1 = in.mass1 * kMsolSec;
   s.mass2 = in.mass2 * kMsolSec;
   s.spin1x = in.spin1[0];
@@ -146,7 +150,6 @@ GW_HD void populate(Source &s, const GenParams &in) {
   s.inv_eta = 1. / s.eta;
   s.k_tf2 = 3. / (128. * s.eta);
   s.M = s.mass1 + s.mass2;
-  s.chirpmass = s.M * pow(s.eta, 3. / 5);  // (m1 m2)^(3/5) / M^(1/5)
   s.chi_eff = (s.mass1 * (s.spin1z) + s.mass2 * (s.spin2z)) / (s.M);
   s.chi_pn = s.chi_eff - ((38. / 113) * s.eta) * (2 * s.chi_s);
   s.DL = in.Luminosity_Distance * (kMpcSI / kC);
@@ -154,14 +157,7 @@ GW_HD void populate(Source &s, const GenParams &in) {
   s.phiRef = in.phiRef;
   s.tc = in.tc;
   s.sky_average = in.sky_average;
-  // A0_from_DL (util.cpp:1271-1279)
-  if (s.sky_average)
-    s.A0 = sqrt(kPi / 30) * s.chirpmass * s.chirpmass / s.DL * pow_m7_6(kPi * s.chirpmass);
-  else
-    s.A0 = sqrt(kPi * 40. / 192.) * s.chirpmass * s.chirpmass / s.DL * pow_m7_6(kPi * s.chirpmass);
   s.incl_angle = in.incl_angle;
-  s.cos_incl = cos(in.incl_angle);
-  s.fac_incl = .5 * (1 + s.cos_incl * s.cos_incl);
   s.f_ref = in.f_ref;
   s.shift_time = in.shift_time;
   s.shift_phase = in.shift_phase;
@@ -169,6 +165,26 @@ GW_HD void populate(Source &s, const GenParams &in) {
   s.pv2 = 0;
   s.chip = in.chip;
   s.phip = in.phip;
+}
+GW_HD void populate_amp(Source &s, const GenParams &in) {
+  const double m1 = in.mass1 * kMsolSec, m2 = in.mass2 * kMsolSec;
+  const double M = m1 + m2, eta = calc_eta(m1, m2), DL = in.Luminosity_Distance * (kMpcSI / kC);
+  const double mc = M * pow(eta, 3. / 5);  // (m1 m2)^(3/5) / M^(1/5)
+  s.chirpmass = mc;
+  // A0_from_DL (util.cpp:1271-1279)
+  if (in.sky_average)
+    s.A0 = sqrt(kPi / 30) * mc * mc / DL * pow_m7_6(kPi * mc);
+  else
+    s.A0 = sqrt(kPi * 40. / 192.) * mc * mc / DL * pow_m7_6(kPi * mc);
+}
+GW_HD void populate_incl(Source &s, const GenParams &in) {
+  s.cos_incl = cos(in.incl_angle);
+  s.fac_incl = .5 * (1 + s.cos_incl * s.cos_incl);
+}
+GW_HD void populate(Source &s, const GenParams &in) {
+  populate_core(s, in);
+  populate_amp(s, in);
+  populate_incl(s, in);
 }
 
 // ------------------------------------------- natural cubic spline (QNM table)
@@ -223,12 +239,20 @@ GW_HD int cspline_locate(const double *x, int n, double xv) {
 // a guess from the spacing corrected by a short walk (bounded by n).
 GW_HD int cspline_locate_near_uniform(const double *x, int n, double xv, double h) {
   if (!(xv >= x[0] && xv <= x[n - 1])) return -1;
-  int g = (int)((xv - x[0]) / h);
+  int g = (int)((xv - x[0]) * (1.0 / h));  // a guess: the walk below corrects it
   if (g < 0) g = 0;
   if (g > n - 2) g = n - 2;
   for (int it = 0; it < n && g > 0 && x[g] > xv; it++) g--;
   for (int it = 0; it < n && g < n - 2 && x[g + 1] <= xv; it++) g++;
   return g;
+}
+// A knot interval's cubic from per-interval coefficients b, d prepared once
+// (the values cspline_eval_at forms on each call): no division per call.
+GW_HD double cspline_eval_pre(const double *x, const double *y, const double *b, const double *c, const double *d,
+                              int ilo, double xv) {
+  if (ilo < 0) return NAN;
+  const double delx = xv - x[ilo];
+  return y[ilo] + delx * (b[ilo] + delx * (c[ilo] + delx * d[ilo]));
 }
 GW_HD double cspline_eval_at(const double *x, const double *y, const double *c, int ilo, double xv, int deriv) {
   if (ilo < 0) return NAN;
@@ -386,13 +410,43 @@ GW_HD void post_merger(Source &s, const double *qnm) {  // IMRPhenomD.cpp:1091-1
     return;
   }
   const double *a = qnm, *yr = qnm + kQnmLen, *yd = qnm + 2 * kQnmLen, *cr = qnm + 3 * kQnmLen,
-               *cd = qnm + 4 * kQnmLen;
+               *cd = qnm + 4 * kQnmLen, *br = qnm + 5 * kQnmLen, *dr = qnm + 6 * kQnmLen,
+               *bd = qnm + 7 * kQnmLen, *dd = qnm + 8 * kQnmLen;
   double finspin = final_spin(s);
   double Erad = EradRational0815(s.eta, s.spin1z, s.spin2z);
   // both splines share the knots (spacing 0.002 inside, 0.001 at the ends)
   const int ilo = cspline_locate_near_uniform(a, kQnmLen, finspin, 0.002);
-  s.fRD = cspline_eval_at(a, yr, cr, ilo, finspin, 0) / (1.0 - Erad) / s.M;
-  s.fdamp = cspline_eval_at(a, yd, cd, ilo, finspin, 0) / (1.0 - Erad) / s.M;
+  const double sc = 1.0 / ((1.0 - Erad) * s.M);
+  s.fRD = cspline_eval_pre(a, yr, br, cr, dr, ilo, finspin) * sc;
+  s.fdamp = cspline_eval_pre(a, yd, bd, cd, dd, ilo, finspin) * sc;
+}
+// The QNM table: knots a, fring and fdamp, the natural cubic spline
+// coefficients c of both, then their per-interval b and d (kQnmArrays arrays
+// of kQnmLen).  Host code.
+constexpr int kQnmArrays = 9;
+inline void qnm_fill(double *o, const double *a_h, const double *fring_h, const double *fdamp_h) {
+  const int n = kQnmLen;
+  for (int i = 0; i < n; i++) {
+    o[i] = a_h[i];
+    o[n + i] = fring_h[i];
+    o[2 * n + i] = fdamp_h[i];
+  }
+  std::vector<double> work(6 * n);
+  cspline_coeffs(o, o + n, n, o + 3 * n, work.data());
+  cspline_coeffs(o, o + 2 * n, n, o + 4 * n, work.data());
+  for (int sp = 0; sp < 2; sp++) {
+    const double *x = o, *y = o + (1 + sp) * n, *c = o + (3 + sp) * n;
+    double *b = o + (5 + 2 * sp) * n, *d = o + (6 + 2 * sp) * n;
+    for (int i = 0; i < n; i++) {
+      if (i + 1 >= n) {
+        b[i] = d[i] = 0.0;
+        continue;
+      }
+      const double dx = x[i + 1] - x[i], dy = y[i + 1] - y[i];
+      b[i] = (dy / dx) - dx * (c[i + 1] + 2.0 * c[i]) / 3.0;
+      d[i] = (c[i + 1] - c[i]) / (3.0 * dx);
+    }
+  }
 }
 GW_HD double fpeak(const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1312-1326
   double fRD = s.fRD, fdamp = s.fdamp, g3 = l.gamma[2], g2 = l.gamma[1];

@@ -13,16 +13,8 @@ using namespace gwt;
 static std::vector<double> g_qnm;
 static const double *qnm() {
   if (g_qnm.empty()) {
-    const int n = kQnmLen;
-    g_qnm.resize(5 * n);
-    for (int i = 0; i < n; i++) {
-      g_qnm[i] = gwt_qnm_a_h[i];
-      g_qnm[n + i] = gwt_qnm_fring_h[i];
-      g_qnm[2 * n + i] = gwt_qnm_fdamp_h[i];
-    }
-    std::vector<double> work(6 * n);
-    cspline_coeffs(g_qnm.data(), g_qnm.data() + n, n, g_qnm.data() + 3 * n, work.data());
-    cspline_coeffs(g_qnm.data(), g_qnm.data() + 2 * n, n, g_qnm.data() + 4 * n, work.data());
+    g_qnm.resize(kQnmArrays * kQnmLen);
+    qnm_fill(g_qnm.data(), gwt_qnm_a_h, gwt_qnm_fring_h, gwt_qnm_fdamp_h);
   }
   return g_qnm.data();
 }
