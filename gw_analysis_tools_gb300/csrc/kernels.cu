@@ -287,8 +287,9 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 //   S1  W0/W3 calibration fits;  W1 D: ringdown frequencies / Pv2: J-frame transform;  W2 PN coefficients
 //   S2  W0 Pv2: ringdown frequencies; matching frequencies;  W1 D: phase at f_ref (inspiral);
 //       W2 D: ringdown-phase terms at f3
-//   S3  W0/W1 amplitude matching points;  D: W2/W3 phase connection, inspiral / other parts;
-//       Pv2: W2 phase connection, W3 Euler and frame constants
+//   S3  W0/W1 amplitude matching points;  W2 phase connection, inspiral part;  W3 D: phase
+//       connection, other parts / Pv2: Euler and frame constants (W1 then the other parts)
+//   S3b Pv2: W2 phase connection constants
 //   S4  W0/W1 amplitude deltas;  W2 D: phase connection constants, phase/time shift /
 //       Pv2: time-shift nodes 0-4;  W3 Pv2: nodes 5-9
 //   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions;  W3 D: detector phases and factors /
@@ -373,15 +374,19 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   // S3
   if (run) {
     if (warp == 0) d_amp_conn_low(r.m, s_ac[lane]);
-    if (warp == 1) d_amp_conn_high(r.m, s_ac[lane]);
-    if (pv2) {
-      if (warp == 2) d_phase_conn(r.m);
-      if (warp == 3) model_p_finish(r.m, r.p);
-    } else {
-      if (warp == 2) phase_conn_ins(r.m, s_pc[lane]);
-      if (warp == 3) phase_conn_imr(r.m, s_pc[lane]);
+    if (warp == 1) {
+      d_amp_conn_high(r.m, s_ac[lane]);
+      if (pv2) phase_conn_imr(r.m, s_pc[lane]);
+    }
+    if (warp == 2) phase_conn_ins(r.m, s_pc[lane]);
+    if (warp == 3) {
+      if (pv2) model_p_finish(r.m, r.p);
+      else phase_conn_imr(r.m, s_pc[lane]);
     }
   }
+  __syncthreads();
+  // S3b  Pv2: the phase connection constants (its time-shift nodes need them)
+  if (run && pv2 && warp == 2) phase_conn_combine(r.m, s_pc[lane]);
   __syncthreads();
   // S4
   if (run) {

@@ -365,16 +365,6 @@ GW_HD double L2PN(double eta, double MF2third, double PI2third) {  // IMRPhenomP
   double x = MF2third * PI2third, x2 = x * x, eta2 = eta * eta;
   return (eta * (1.0 + (1.5 + eta / 6.0) * x + (3.375 - (19.0 * eta) / 8. - eta2 / 24.0) * x2)) / sqrt(x);
 }
-#define GWT_ROTATEZ(angle, vx, vy, vz)       \
-  tmp1 = vx * cos(angle) - vy * sin(angle); \
-  tmp2 = vx * sin(angle) + vy * cos(angle); \
-  vx = tmp1;                                \
-  vy = tmp2
-#define GWT_ROTATEY(angle, vx, vy, vz)       \
-  tmp1 = vx * cos(angle) + vz * sin(angle); \
-  tmp2 = -vx * sin(angle) + vz * cos(angle);\
-  vx = tmp1;                                \
-  vz = tmp2
 // PhenomPv2_Param_Transform (IMRPhenomP.cpp:1082-1210) / _reduced (:822-938)
 GW_HDNI void pv2_transform(Source &s, int reduced) {
   double chi1_l = s.spin1z, chi2_l = s.spin2z;
@@ -403,48 +393,66 @@ GW_HDNI void pv2_transform(Source &s, int reduced) {
     J0x = m1_2 * s.spin1x + m2_2 * s.spin2x;
     J0y = m1_2 * s.spin1y + m2_2 * s.spin2y;
   } else {
-    J0x = m1_2 * s.chip * cos(s.phip);
-    J0y = m1_2 * s.chip * sin(s.phip);
+    double sp, cp;
+    sincos(s.phip, &sp, &cp);
+    J0x = m1_2 * s.chip * cp;
+    J0y = m1_2 * s.chip * sp;
   }
   J0z = L0 + m1_2 * s.spin1z + m2_2 * s.spin2z;
   double J0 = sqrt(J0x * J0x + J0y * J0y + J0z * J0z);
   double thetaJ_sf = acos(J0z / J0);
   double phiJ_sf = atan2(J0y, J0x);
   s.phi_aligned = -phiJ_sf;
-  double tmp1, tmp2;
+  // the reference's rotations (ROTATEZ / ROTATEY), each angle's sine and
+  // cosine evaluated once
   double incl = s.incl_angle, phiRef = s.phiRef;
-  double Nx_sf = sin(incl) * cos(kPi / 2. - phiRef), Ny_sf = sin(incl) * sin(kPi / 2. - phiRef), Nz_sf = cos(incl);
+  double si, ci, sq, cq, sr, cr, sA, cA, sB, cB, sK, cK;
+  sincos(incl, &si, &ci);
+  sincos(kPi / 2. - phiRef, &sq, &cq);
+  sincos(phiRef, &sr, &cr);
+  sincos(-phiJ_sf, &sA, &cA);
+  sincos(-thetaJ_sf, &sB, &cB);
+  auto rotz = [](double c, double sn, double &vx, double &vy) {
+    const double t1 = vx * c - vy * sn, t2 = vx * sn + vy * c;
+    vx = t1;
+    vy = t2;
+  };
+  auto roty = [](double c, double sn, double &vx, double &vz) {
+    const double t1 = vx * c + vz * sn, t2 = -vx * sn + vz * c;
+    vx = t1;
+    vz = t2;
+  };
+  double Nx_sf = si * cq, Ny_sf = si * sq, Nz_sf = ci;
   double tx = Nx_sf, ty = Ny_sf, tz = Nz_sf;
-  GWT_ROTATEZ(-phiJ_sf, tx, ty, tz);
-  GWT_ROTATEY(-thetaJ_sf, tx, ty, tz);
+  rotz(cA, sA, tx, ty);
+  roty(cB, sB, tx, tz);
   double kappa = -atan2(ty, tx);
+  sincos(kappa, &sK, &cK);
   tx = 0.;
   ty = 0.;
   tz = 1.;
-  GWT_ROTATEZ(-phiJ_sf, tx, ty, tz);
-  GWT_ROTATEY(-thetaJ_sf, tx, ty, tz);
-  GWT_ROTATEZ(kappa, tx, ty, tz);
+  rotz(cA, sA, tx, ty);
+  roty(cB, sB, tx, tz);
+  rotz(cK, sK, tx, ty);
   s.alpha0 = atan2(ty, tx);
   tx = Nx_sf;
   ty = Ny_sf;
   tz = Nz_sf;
-  GWT_ROTATEZ(-phiJ_sf, tx, ty, tz);
-  GWT_ROTATEY(-thetaJ_sf, tx, ty, tz);
-  GWT_ROTATEZ(kappa, tx, ty, tz);
+  rotz(cA, sA, tx, ty);
+  roty(cB, sB, tx, tz);
+  rotz(cK, sK, tx, ty);
   double Nx_Jf = tx, Nz_Jf = tz;
   s.thetaJN = acos(Nz_Jf);
-  tx = -cos(incl) * sin(phiRef);
-  ty = -cos(incl) * cos(phiRef);
-  tz = sin(incl);
-  GWT_ROTATEZ(-phiJ_sf, tx, ty, tz);
-  GWT_ROTATEY(-thetaJ_sf, tx, ty, tz);
-  GWT_ROTATEZ(kappa, tx, ty, tz);
+  tx = -ci * sr;
+  ty = -ci * cr;
+  tz = si;
+  rotz(cA, sA, tx, ty);
+  roty(cB, sB, tx, tz);
+  rotz(cK, sK, tx, ty);
   double XdotPArun = tx * 0. + ty * -1. + tz * 0.;
   double XdotQArun = tx * Nz_Jf + ty * 0. + tz * -Nx_Jf;
   s.zeta_polariz = atan2(XdotQArun, XdotPArun);
 }
-#undef GWT_ROTATEZ
-#undef GWT_ROTATEY
 
 GW_HDNI void pv2_euler_coeffs(double *a, double *e, const Source &s) {  // IMRPhenomP.cpp:65-144
   double m2 = s.q / (1. + s.q), m1 = 1. / (1. + s.q), dm = m1 - m2, mtot = 1.;
@@ -454,38 +462,45 @@ GW_HDNI void pv2_euler_coeffs(double *a, double *e, const Source &s) {  // IMRPh
   double dm2 = dm * dm, dm3 = dm2 * dm;
   double m2_2 = m2 * m2, m2_3 = m2_2 * m2, m2_4 = m2_3 * m2, m2_5 = m2_4 * m2, m2_6 = m2_5 * m2, m2_7 = m2_6 * m2,
          m2_8 = m2_7 * m2;
-  a[0] = (-0.18229166666666666 - (5 * dm) / (64. * m2));
-  a[1] = ((-15 * dm * m2 * chil) / (128. * mtot2 * eta) - (35 * m2_2 * chil) / (128. * mtot2 * eta));
-  a[2] = (-1.7952473958333333 - (4555 * dm) / (7168. * m2) - (15 * chip2 * dm * m2_3) / (128. * mtot4 * eta2) -
-          (35 * chip2 * m2_4) / (128. * mtot4 * eta2) - (515 * eta) / 384. - (15 * dm2 * eta) / (256. * m2_2) -
-          (175 * dm * eta) / (256. * m2));
-  a[3] = -(35 * kPi) / 48. - (5 * dm * kPi) / (16. * m2) + (5 * dm2 * chil) / (16. * mtot2) +
-         (5 * dm * m2 * chil) / (3. * mtot2) + (2545 * m2_2 * chil) / (1152. * mtot2) -
-         (5 * chip2 * dm * m2_5 * chil) / (128. * mtot6 * eta3) - (35 * chip2 * m2_6 * chil) / (384. * mtot6 * eta3) +
-         (2035 * dm * m2 * chil) / (21504. * mtot2 * eta) + (2995 * m2_2 * chil) / (9216. * mtot2 * eta);
-  a[4] = (4.318908476114694 + (27895885 * dm) / (2.1676032e7 * m2) - (15 * chip4 * dm * m2_7) / (512. * mtot8 * eta4) -
-          (35 * chip4 * m2_8) / (512. * mtot8 * eta4) - (485 * chip2 * dm * m2_3) / (14336. * mtot4 * eta2) +
-          (475 * chip2 * m2_4) / (6144. * mtot4 * eta2) + (15 * chip2 * dm2 * m2_2) / (256. * mtot4 * eta) +
-          (145 * chip2 * dm * m2_3) / (512. * mtot4 * eta) + (575 * chip2 * m2_4) / (1536. * mtot4 * eta) +
-          (39695 * eta) / 86016. + (1615 * dm2 * eta) / (28672. * m2_2) - (265 * dm * eta) / (14336. * m2) +
-          (955 * eta2) / 576. + (15 * dm3 * eta2) / (1024. * m2_3) + (35 * dm2 * eta2) / (256. * m2_2) +
-          (2725 * dm * eta2) / (3072. * m2) - (15 * dm * m2 * kPi * chil) / (16. * mtot2 * eta) -
-          (35 * m2_2 * kPi * chil) / (16. * mtot2 * eta) + (15 * chip2 * dm * m2_7 * chil2) / (128. * mtot8 * eta4) +
-          (35 * chip2 * m2_8 * chil2) / (128. * mtot8 * eta4) + (375 * dm2 * m2_2 * chil2) / (256. * mtot4 * eta) +
-          (1815 * dm * m2_3 * chil2) / (256. * mtot4 * eta) + (1645 * m2_4 * chil2) / (192. * mtot4 * eta));
-  e[0] = (-0.18229166666666666 - (5 * dm) / (64. * m2));
-  e[1] = ((-15 * dm * m2 * chil) / (128. * mtot2 * eta) - (35 * m2_2 * chil) / (128. * mtot2 * eta));
-  e[2] = (-1.7952473958333333 - (4555 * dm) / (7168. * m2) - (515 * eta) / 384. - (15 * dm2 * eta) / (256. * m2_2) -
-          (175 * dm * eta) / (256. * m2));
-  e[3] = -(35 * kPi) / 48. - (5 * dm * kPi) / (16. * m2) + (5 * dm2 * chil) / (16. * mtot2) +
-         (5 * dm * m2 * chil) / (3. * mtot2) + (2545 * m2_2 * chil) / (1152. * mtot2) +
-         (2035 * dm * m2 * chil) / (21504. * mtot2 * eta) + (2995 * m2_2 * chil) / (9216. * mtot2 * eta);
-  e[4] = (4.318908476114694 + (27895885 * dm) / (2.1676032e7 * m2) + (39695 * eta) / 86016. +
-          (1615 * dm2 * eta) / (28672. * m2_2) - (265 * dm * eta) / (14336. * m2) + (955 * eta2) / 576. +
-          (15 * dm3 * eta2) / (1024. * m2_3) + (35 * dm2 * eta2) / (256. * m2_2) + (2725 * dm * eta2) / (3072. * m2) -
-          (15 * dm * m2 * kPi * chil) / (16. * mtot2 * eta) - (35 * m2_2 * kPi * chil) / (16. * mtot2 * eta) +
-          (375 * dm2 * m2_2 * chil2) / (256. * mtot4 * eta) + (1815 * dm * m2_3 * chil2) / (256. * mtot4 * eta) +
-          (1645 * m2_4 * chil2) / (192. * mtot4 * eta));
+  // the reference's quotients as products with these inverses (mtot = 1), and
+  // constant denominators folded
+  const double im2 = 1. / m2, ieta = 1. / eta;
+  const double im2_2 = im2 * im2, im2_3 = im2_2 * im2, ieta2 = ieta * ieta, ieta3 = ieta2 * ieta, ieta4 = ieta3 * ieta;
+  (void)mtot4;
+  (void)mtot6;
+  (void)mtot8;
+  a[0] = (-0.18229166666666666 - ((5 * dm) * (1. / 64.) * im2));
+  a[1] = (((-15 * dm * m2 * chil) * (1. / 128.) * ieta) - ((35 * m2_2 * chil) * (1. / 128.) * ieta));
+  a[2] = (-1.7952473958333333 - ((4555 * dm) * (1. / 7168.) * im2) - ((15 * chip2 * dm * m2_3) * (1. / 128.) * ieta2) -
+          ((35 * chip2 * m2_4) * (1. / 128.) * ieta2) - ((515 * eta) * (1. / 384.)) - ((15 * dm2 * eta) * (1. / 256.) * im2_2) -
+          ((175 * dm * eta) * (1. / 256.) * im2));
+  a[3] = -((35 * kPi) * (1. / 48.)) - ((5 * dm * kPi) * (1. / 16.) * im2) + ((5 * dm2 * chil) * (1. / 16.)) +
+         ((5 * dm * m2 * chil) * (1. / 3.)) + ((2545 * m2_2 * chil) * (1. / 1152.)) -
+         ((5 * chip2 * dm * m2_5 * chil) * (1. / 128.) * ieta3) - ((35 * chip2 * m2_6 * chil) * (1. / 384.) * ieta3) +
+         ((2035 * dm * m2 * chil) * (1. / 21504.) * ieta) + ((2995 * m2_2 * chil) * (1. / 9216.) * ieta);
+  a[4] = (4.318908476114694 + ((27895885 * dm) * (1. / 2.1676032e7) * im2) - ((15 * chip4 * dm * m2_7) * (1. / 512.) * ieta4) -
+          ((35 * chip4 * m2_8) * (1. / 512.) * ieta4) - ((485 * chip2 * dm * m2_3) * (1. / 14336.) * ieta2) +
+          ((475 * chip2 * m2_4) * (1. / 6144.) * ieta2) + ((15 * chip2 * dm2 * m2_2) * (1. / 256.) * ieta) +
+          ((145 * chip2 * dm * m2_3) * (1. / 512.) * ieta) + ((575 * chip2 * m2_4) * (1. / 1536.) * ieta) +
+          ((39695 * eta) * (1. / 86016.)) + ((1615 * dm2 * eta) * (1. / 28672.) * im2_2) - ((265 * dm * eta) * (1. / 14336.) * im2) +
+          ((955 * eta2) * (1. / 576.)) + ((15 * dm3 * eta2) * (1. / 1024.) * im2_3) + ((35 * dm2 * eta2) * (1. / 256.) * im2_2) +
+          ((2725 * dm * eta2) * (1. / 3072.) * im2) - ((15 * dm * m2 * kPi * chil) * (1. / 16.) * ieta) -
+          ((35 * m2_2 * kPi * chil) * (1. / 16.) * ieta) + ((15 * chip2 * dm * m2_7 * chil2) * (1. / 128.) * ieta4) +
+          ((35 * chip2 * m2_8 * chil2) * (1. / 128.) * ieta4) + ((375 * dm2 * m2_2 * chil2) * (1. / 256.) * ieta) +
+          ((1815 * dm * m2_3 * chil2) * (1. / 256.) * ieta) + ((1645 * m2_4 * chil2) * (1. / 192.) * ieta));
+  e[0] = (-0.18229166666666666 - ((5 * dm) * (1. / 64.) * im2));
+  e[1] = (((-15 * dm * m2 * chil) * (1. / 128.) * ieta) - ((35 * m2_2 * chil) * (1. / 128.) * ieta));
+  e[2] = (-1.7952473958333333 - ((4555 * dm) * (1. / 7168.) * im2) - ((515 * eta) * (1. / 384.)) - ((15 * dm2 * eta) * (1. / 256.) * im2_2) -
+          ((175 * dm * eta) * (1. / 256.) * im2));
+  e[3] = -((35 * kPi) * (1. / 48.)) - ((5 * dm * kPi) * (1. / 16.) * im2) + ((5 * dm2 * chil) * (1. / 16.)) +
+         ((5 * dm * m2 * chil) * (1. / 3.)) + ((2545 * m2_2 * chil) * (1. / 1152.)) +
+         ((2035 * dm * m2 * chil) * (1. / 21504.) * ieta) + ((2995 * m2_2 * chil) * (1. / 9216.) * ieta);
+  e[4] = (4.318908476114694 + ((27895885 * dm) * (1. / 2.1676032e7) * im2) + ((39695 * eta) * (1. / 86016.)) +
+          ((1615 * dm2 * eta) * (1. / 28672.) * im2_2) - ((265 * dm * eta) * (1. / 14336.) * im2) + ((955 * eta2) * (1. / 576.)) +
+          ((15 * dm3 * eta2) * (1. / 1024.) * im2_3) + ((35 * dm2 * eta2) * (1. / 256.) * im2_2) + ((2725 * dm * eta2) * (1. / 3072.) * im2) -
+          ((15 * dm * m2 * kPi * chil) * (1. / 16.) * ieta) - ((35 * m2_2 * kPi * chil) * (1. / 16.) * ieta) +
+          ((375 * dm2 * m2_2 * chil2) * (1. / 256.) * ieta) + ((1815 * dm * m2_3 * chil2) * (1. / 256.) * ieta) +
+          ((1645 * m2_4 * chil2) * (1. / 192.) * ieta));
 }
 // calculate_euler_angles (IMRPhenomP.cpp:717-735) from MFthird
 GW_HD void pv2_euler_angles(double &alpha, double &eps, double MFthird, double PIthird, const double *a,
@@ -528,15 +543,6 @@ GW_HDNI double pv2_time_shift(const ModelD &m) {
   for (int j = 0; j < kPv2ShiftNodes; j++) ph[j] = pv2_shift_node(m, j);
   return pv2_shift_solve(m, ph);
 }
-GW_HD double swsh_2m2(double theta, int m) {  // XLALSpinWeightedSphericalHarmonic s=-2 l=2 (util.cpp:1953-2333)
-  switch (m) {
-    case -2: return sqrt(5.0 / (64.0 * kPi)) * (1.0 - cos(theta)) * (1.0 - cos(theta));
-    case -1: return sqrt(5.0 / (16.0 * kPi)) * sin(theta) * (1.0 - cos(theta));
-    case 0: return sqrt(15.0 / (32.0 * kPi)) * sin(theta) * sin(theta);
-    case 1: return sqrt(5.0 / (16.0 * kPi)) * sin(theta) * (1.0 + cos(theta));
-    default: return sqrt(5.0 / (64.0 * kPi)) * (1.0 + cos(theta)) * (1.0 + cos(theta));
-  }
-}
 
 // Full Pv2 per-request setup: transform, D model, Euler/harmonic constants,
 // time shift (IMRPhenomP.cpp:195-262, 345-351; waveform_generator.cpp:1272-1281).
@@ -555,7 +561,15 @@ GW_HD void model_p_setup(ModelD &m, ModelP &pm, const GenParams &in) {
   } else {
     pv2_transform(s, 0);
   }
-  for (int k = 0; k < 5; k++) pm.Y[k] = swsh_2m2(s.thetaJN, k - 2);
+  // the s = -2, l = 2 spin-weighted harmonics Y_2m(thetaJN, 0), m = -2..2
+  // (XLALSpinWeightedSphericalHarmonic, util.cpp:1953-2333), from one sincos
+  double st, ct;
+  sincos(s.thetaJN, &st, &ct);
+  pm.Y[0] = sqrt(5.0 / (64.0 * kPi)) * (1.0 - ct) * (1.0 - ct);
+  pm.Y[1] = sqrt(5.0 / (16.0 * kPi)) * st * (1.0 - ct);
+  pm.Y[2] = sqrt(15.0 / (32.0 * kPi)) * st * st;
+  pm.Y[3] = sqrt(5.0 / (16.0 * kPi)) * st * (1.0 + ct);
+  pm.Y[4] = sqrt(5.0 / (64.0 * kPi)) * (1.0 + ct) * (1.0 + ct);
 }
 GW_HDNI void model_p_finish(ModelD &m, ModelP &pm) {
   Source &s = m.s;
@@ -570,8 +584,7 @@ GW_HDNI void model_p_finish(ModelD &m, ModelP &pm) {
   pv2_euler_angles(aoff, eoff, MFthird, m.pi.PIthird, pm.ac, pm.ec);
   pm.alpha_shift = s.alpha0 - aoff;
   pm.eps_off = eoff;
-  pm.c2z = cos(2. * s.zeta_polariz);
-  pm.s2z = sin(2. * s.zeta_polariz);
+  sincos(2. * s.zeta_polariz, &pm.s2z, &pm.c2z);
   if (!(s.f_ref > 0)) m.status |= kModelBadInput;
 }
 GW_HDNI int model_p_prologue(ModelD &m, ModelP &pm, const GenParams &in, const double *qnm) {
