@@ -572,7 +572,6 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
   __shared__ double s_node[kSegBuf * kSegEval], s_node_a[kSegBuf * kSegEval];
   __shared__ SegPoly s_poly[kSegBuf], s_poly_a[kSegBuf];
   __shared__ double s_coef[kSegBuf * 2 * kSegNodes];
-  __shared__ double s_dnode[kSegBuf * kSegEval], s_dnode_a[kSegBuf * kSegEval];
   const int tid = threadIdx.x;
   for (;;) {
     if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
@@ -630,19 +629,16 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
             s_node_a[e] = va;
           }
           __syncthreads();
-          // (B0) node values relative to the segment centre (node 4)
-          for (int e = tid; e < nseg * kSegEval; e += blockDim.x) {
-            const int sg = e / kSegEval, j = e - sg * kSegEval;
-            s_dnode[e] = j == 4 ? 0.0 : s_node[e] - s_node[sg * kSegEval + 4];
-            s_dnode_a[e] = j == 4 ? 0.0 : s_node_a[e] - s_node_a[sg * kSegEval + 4];
-          }
-          __syncthreads();
-          // (B1) polynomial coefficients, one thread per (segment, function, coefficient)
+          // (B1) polynomial coefficients and their stored form, one thread per
+          // (segment, function, coefficient); a segment the check rejects below
+          // keeps unused stored coefficients
           for (int e = tid; e < nseg * nfn * kSegNodes; e += blockDim.x) {
             const int j = e % kSegNodes, q = e / kSegNodes, sg = q / nfn, fn = q - sg * nfn;
-            s_coef[(sg * 2 + fn) * kSegNodes + j] =
-                seg_usable(x, n0, N, c0 + sg * kSegBins) ? seg_coef_rel((fn ? s_dnode_a : s_dnode) + sg * kSegEval, j)
-                                                         : 0.0;
+            const double *v = (fn ? s_node_a : s_node) + sg * kSegEval;
+            double *cf = s_coef + (sg * 2 + fn) * kSegNodes;
+            const bool use = seg_usable(x, n0, N, c0 + sg * kSegBins);
+            cf[j] = use ? seg_coef(v, j) : 0.0;
+            if (use) seg_store(v, cf, j, fn ? s_poly_a[sg] : s_poly[sg]);
           }
           __syncthreads();
           // (B2) acceptance per (segment, function)
@@ -653,14 +649,6 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
             if (ok && (fn == 0 || pv2))
               ok = seg_check((fn ? s_node_a : s_node) + sg * kSegEval, s_coef + (sg * 2 + fn) * kSegNodes) == 0;
             P.direct = ok ? 0 : 1;
-          }
-          __syncthreads();
-          // (B3) stored coefficients of the accepted segments
-          for (int e = tid; e < nseg * nfn * kSegNodes; e += blockDim.x) {
-            const int j = e % kSegNodes, q = e / kSegNodes, sg = q / nfn, fn = q - sg * nfn;
-            SegPoly &P = fn ? s_poly_a[sg] : s_poly[sg];
-            if (!P.direct)
-              seg_store((fn ? s_node_a : s_node) + sg * kSegEval, s_coef + (sg * 2 + fn) * kSegNodes, j, P);
           }
           __syncthreads();
           // (C) bins: the block covers one segment per pass

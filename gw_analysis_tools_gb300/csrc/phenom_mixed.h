@@ -639,20 +639,13 @@ struct SegPoly {
 
 GW_HD int seg_offset(int j) { return GWT_T(gwt_seg_offsets)[j]; }
 
-// The fit in three steps, each parallel over (segment, coefficient) or
-// segments in the kernel: (1) coefficient j >= 1 of u^j (radians) from the
-// node values v[0..kSegEval) (v[4] is the centre; coefficient 0 is v[4]);
+// The fit in steps, parallel over (segment, coefficient) or segments in the
+// kernel: (1) coefficient j >= 1 of u^j (radians) from the node values
+// v[0..kSegEval) (v[4] is the centre; coefficient 0 is v[4]);
 GW_HD double seg_coef(const double *v, int j) {
   if (j == 0) return 0.0;
   double s = 0.0;
   for (int k = 0; k < kSegNodes; k++) s += GWT_T(gwt_seg_vinv)[j][k] * (v[k] - v[4]);
-  return s;
-}
-// the same from node values already taken relative to the centre (dv[4] = 0)
-GW_HD double seg_coef_rel(const double *dv, int j) {
-  if (j == 0) return 0.0;
-  double s = 0.0;
-  for (int k = 0; k < kSegNodes; k++) s += GWT_T(gwt_seg_vinv)[j][k] * dv[k];
   return s;
 }
 // (2) the acceptance test (check points, size of the FP32 part): 0 when usable;
