@@ -171,7 +171,7 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
 
 int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, const int *d_approx, int n,
                   const int *h_handles, int ndet, double T_segment, int precision, double *d_out, int *d_status,
-                  int tile, bool use_graph) {
+                  int tile, bool use_graph, const BatchCopies *io) {
   const int mixed = precision == GWGPU_PREC_MIXED;
   if (tile <= 0) {
     const gwgpu_context::Stream *s0 = c->get_stream(h_handles[0]);
@@ -207,17 +207,24 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
   double *partials = (double *)p;
   p = align256(p + sizeof(double) * (size_t)L.plan.nitems * gwk::kAcc);
   unsigned *cnt = (unsigned *)p;
-  if (!use_graph || c->timing)
-    return launch_sequence(c, L, d_params, d_approx, n, ndet, T_segment, mixed, d_out, d_status, reqs, partials, cnt);
-  char gk[256];
-  snprintf(gk, sizeof(gk), "%p|%p|%p|%p|%d|%.17g|%d", (const void *)d_params, (const void *)d_approx,
-           (const void *)d_out, (const void *)d_status, mixed, T_segment, n);
+  auto sequence = [&]() {
+    if (io) cudaMemcpyAsync(io->h2d_dst, io->h2d_src, io->h2d_bytes, cudaMemcpyHostToDevice, L.stream);
+    int r = launch_sequence(c, L, d_params, d_approx, n, ndet, T_segment, mixed, d_out, d_status, reqs, partials, cnt);
+    if (!r && io) cudaMemcpyAsync(io->d2h_dst, io->d2h_src, io->d2h_bytes, cudaMemcpyDeviceToHost, L.stream);
+    return r;
+  };
+  if (!use_graph || c->timing) return sequence();
+  char gk[320];
+  snprintf(gk, sizeof(gk), "%p|%p|%p|%p|%d|%.17g|%d|%p|%p|%zu|%p|%p|%zu", (const void *)d_params,
+           (const void *)d_approx, (const void *)d_out, (const void *)d_status, mixed, T_segment, n,
+           io ? io->h2d_src : nullptr, io ? io->h2d_dst : nullptr, io ? io->h2d_bytes : 0,
+           io ? io->d2h_dst : nullptr, io ? (const void *)io->d2h_src : nullptr, io ? io->d2h_bytes : 0);
   auto it = L.graphs.find(gk);
   if (it == L.graphs.end()) {
     cudaGraph_t g;
     cudaError_t e = cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return c->fail(e, "graph capture");
-    st = launch_sequence(c, L, d_params, d_approx, n, ndet, T_segment, mixed, d_out, d_status, reqs, partials, cnt);
+    st = sequence();
     e = cudaStreamEndCapture(L.stream, &g);
     if (st) return st;
     if (e != cudaSuccess) return c->fail(e, "graph capture end");
@@ -300,11 +307,11 @@ int gwgpu_loglik_batch(gwgpu_context *c, const gwgpu_gen_params *params, const i
   char *hp = (char *)L.hio, *dp = (char *)L.dio;
   std::memcpy(hp, params, pb);
   std::memcpy(hp + o_ap, approx, ab);
-  cudaMemcpyAsync(dp, hp, o_out, cudaMemcpyHostToDevice, L.stream);
+  // inputs in, outputs out: copies in the same graph as the kernels
+  const gwb::BatchCopies io{hp, dp, o_out, hp + o_out, dp + o_out, total - o_out};
   st = gwb::enqueue_batch(c, L, (const gwgpu_gen_params *)dp, (const int *)(dp + o_ap), n, handles, ndet, T_segment,
-                          precision, (double *)(dp + o_out), (int *)(dp + o_st), 0, c->use_graphs);
+                          precision, (double *)(dp + o_out), (int *)(dp + o_st), 0, c->use_graphs, &io);
   if (st) return st;
-  cudaMemcpyAsync(hp + o_out, dp + o_out, total - o_out, cudaMemcpyDeviceToHost, L.stream);
   cudaError_t e = cudaStreamSynchronize(L.stream);
   if (e != cudaSuccess) return c->fail(e, "batch");
   std::memcpy(loglik, hp + o_out, ob);

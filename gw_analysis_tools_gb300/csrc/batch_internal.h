@@ -42,11 +42,22 @@ int default_tile(int mixed);
 // (precision, detectors, grid length) class, else the default.
 int choose_tile(gwgpu_context *c, int mixed, int ndet, int N);
 int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, int tile);
+// Copies around a launch (pinned host buffers of the lane): before it, the
+// inputs host -> device; after it, the outputs device -> host.
+struct BatchCopies {
+  const void *h2d_src;
+  void *h2d_dst;
+  size_t h2d_bytes;
+  void *d2h_dst;
+  const void *d2h_src;
+  size_t d2h_bytes;
+};
 // Enqueue prologue + fused kernel of n requests on L.stream (device arrays).
-// use_graph: capture/replay the launch sequence for this exact shape.
+// use_graph: capture/replay the launch sequence for this exact shape, with
+// the copies of io (may be null) inside the same graph.
 int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, const int *d_approx, int n,
                   const int *h_handles, int ndet, double T_segment, int precision, double *d_out, int *d_status,
-                  int tile, bool use_graph);
+                  int tile, bool use_graph, const BatchCopies *io = nullptr);
 void lane_release(gwgpu_context *c, Lane &L);
 
 }  // namespace gwb

@@ -322,19 +322,44 @@ class Context:
             self._check(st, "mcmc_likelihood_extrinsic")
         return out.value
 
+    def _call_arrays(self, approximants, handles, n):
+        """The approximant and handle arrays of a call; the common shapes (one
+        approximant, handles shared by every request) are kept between calls."""
+        cache = self.__dict__.setdefault("_arrays", {})
+        akey = ("a", int(approximants), n) if np.ndim(approximants) == 0 else None
+        hkey = ("h", tuple(int(h) for h in handles), n) if np.ndim(handles) == 1 else None
+        ap = cache.get(akey) if akey else None
+        if ap is None:
+            ap = np.ascontiguousarray(np.broadcast_to(np.asarray(approximants, dtype=np.int32), (n,)))
+            if akey:
+                cache[akey] = ap
+        hs = cache.get(hkey) if hkey else None
+        if hs is None:
+            hs = np.asarray(handles, dtype=np.int32)
+            if hs.ndim == 1:
+                hs = np.broadcast_to(hs, (n, hs.size))
+            hs = np.ascontiguousarray(hs, dtype=np.int32)
+            if hkey:
+                if len(cache) > 64:
+                    cache.clear()
+                cache[hkey] = hs
+        return ap, hs
+
     def loglik_batch(self, params, approximants, handles, T_segment, precision=PREC_MIXED):
         """params: GenParams array or list; handles: (ndet,) shared or (n, ndet) per request."""
         parr = params if isinstance(params, ctypes.Array) else params_array(params)
         n = len(parr)
-        ap = np.ascontiguousarray(np.broadcast_to(np.asarray(approximants, dtype=np.int32), (n,)))
-        hs = np.asarray(handles, dtype=np.int32)
-        if hs.ndim == 1:
-            hs = np.broadcast_to(hs, (n, hs.size))
-        hs = np.ascontiguousarray(hs, dtype=np.int32)
-        out = np.zeros(n)
-        status = np.zeros(n, dtype=np.int32)
-        st = self.lib.gwgpu_loglik_batch(self.h, parr, _ip(ap), n, _ip(hs), hs.shape[1], float(T_segment), precision,
-                                         _dp(out), _ip(status))
+        ap, hs = self._call_arrays(approximants, handles, n)
+        out = np.empty(n)
+        status = np.empty(n, dtype=np.int32)
+        fn = self.__dict__.get("_lb_raw")
+        if fn is None:  # the same entry point with address arguments (no pointer objects per call)
+            v = ctypes.c_void_p
+            fn = ctypes.CFUNCTYPE(ctypes.c_int, v, v, v, ctypes.c_int, v, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                  v, v)(("gwgpu_loglik_batch", self.lib))
+            self._lb_raw = fn
+        st = fn(self.h, ctypes.addressof(parr), ap.ctypes.data, n, hs.ctypes.data, hs.shape[1], float(T_segment),
+                precision, out.ctypes.data, status.ctypes.data)
         self._check(st, "loglik_batch")
         return out, status
 
