@@ -572,6 +572,9 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
   __shared__ double s_node[kSegBuf * kSegEval], s_node_a[kSegBuf * kSegEval];
   __shared__ SegPoly s_poly[kSegBuf], s_poly_a[kSegBuf];
   __shared__ double s_coef[kSegBuf * 2 * kSegNodes];
+  // detector rotations: per segment pass (first bin) and per thread offset
+  __shared__ float2 s_rot_seg[kSegBuf * (MIXED ? NDET : 1)];
+  __shared__ float2 s_rot_off[(MIXED ? NDET : 1) * (MIXED ? kBatchBlock : 1)];
   const int tid = threadIdx.x;
   for (;;) {
     if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
@@ -611,6 +614,13 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
         }
         const bool pv2 = x.approximant == kPhenomPv2;
         const gwt::Tables &tb = a.tables;
+        // this thread's offset rotations (read back only by this thread)
+#pragma unroll
+        for (int d = 0; d < NDET; d++) {
+          float c, sn;
+          det_rot_off(x, d, tid, c, sn);
+          s_rot_off[d * kBatchBlock + tid] = make_float2(c, sn);
+        }
         // chunks of up to kMaxSegs segments (one segment = one pass of the block over kSegBins bins)
         for (int c0 = I.k0; c0 < kcut; c0 += kMaxSegs * kSegBins) {
           const int nseg = min(kMaxSegs, (kcut - c0 + kSegBins - 1) / kSegBins);
@@ -641,6 +651,13 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
             if (use) seg_store(v, cf, j, fn ? s_poly_a[sg] : s_poly[sg]);
           }
           __syncthreads();
+          // segment-pass rotations of the detectors
+          for (int e = tid; e < nseg * NDET; e += blockDim.x) {
+            const int sg = e / NDET, d = e - sg * NDET;
+            float c, sn;
+            det_rot_seg(x, d, n0 + c0 + sg * kSegBins, c, sn);
+            s_rot_seg[sg * NDET + d] = make_float2(c, sn);
+          }
           // (B2) acceptance per (segment, function)
           for (int e = tid; e < nseg * 2; e += blockDim.x) {
             const int sg = e >> 1, fn = e & 1, kseg = c0 + sg * kSegBins;
@@ -674,7 +691,13 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
                 dim[d] = v.y;
                 w[d] = __ldg(wh[d] + k);
               }
-              mixed_bin_q<NDET>(x, n, ph, al, __ldg(tb.t13f + n), __ldg(tb.tm76f + n), dre, dim, w, acc);
+              float rc[NDET], rs[NDET];
+#pragma unroll
+              for (int d = 0; d < NDET; d++) {
+                const float2 ra = s_rot_seg[sg * NDET + d], rb = s_rot_off[d * kBatchBlock + tid];
+                cmulf(ra.x, ra.y, rb.x, rb.y, rc[d], rs[d]);
+              }
+              mixed_bin_q<NDET>(x, n, ph, al, __ldg(tb.t13f + n), __ldg(tb.tm76f + n), dre, dim, w, rc, rs, acc);
             }
           }
           __syncthreads();  // the node and fit buffers are reused by the next chunk

@@ -710,21 +710,39 @@ GW_HD float seg_atan_extra(const MixedReq &x, int n) {
   return (float)(x.mE * (1.0 / (2.0 * 3.14159265358979323846)) * kSegFScale) * mixed_atan(x, n);
 }
 
+// The detector's linear phase (L0 + L1 n, turns * 2^64) as a rotation, in
+// two factors: at the first bin n_s of a segment pass (shared by the pass) and
+// at the offset j = n - n_s (shared by the item).  Each factor is exact to
+// FP32 (fixed-point reduction); their product adds one complex rounding.
+GW_HD void det_rot_seg(const MixedReq &x, int d, int n_s, float &c, float &s) {
+  q64_sincospi(x.det[d].L0 + x.det[d].L1 * (uint64_t)n_s, &s, &c);
+}
+GW_HD void det_rot_off(const MixedReq &x, int d, int j, float &c, float &s) {
+  q64_sincospi(x.det[d].L1 * (uint64_t)j, &s, &c);
+}
+GW_HD void cmulf(float ac, float as, float bc, float bs, float &c, float &s) {
+  c = ac * bc - as * bs;
+  s = as * bc + ac * bs;
+}
+
 // One bin of the mixed form, accumulated into acc[d * kAccPerDet + j], with
 // the phase ph (Pv2: phase + 2 epsilon) and the Pv2 angle al in turns * 2^64.
-// dre/dim/w: the detector streams at this bin.
+// dre/dim/w: the detector streams at this bin; rotc/rots: the detector's linear
+// phase rotation at this bin (cos, sin).  The detector phase is the angle sum
+// of ph and that rotation.
 template <int NDET>
 GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float tf, float m76, const float *dre,
-                       const float *dim, const float *w, KSum *acc) {
+                       const float *dim, const float *w, const float *rotc, const float *rots, KSum *acc) {
   if (n > x.n_cut) return;
   float a = mixed_amp(x, n, tf, m76);
+  float sp, cp;
+  q64_sincospi(ph, &sp, &cp);
   if (x.approximant != kPhenomPv2) {
     float aa = a * a;
 #pragma unroll
     for (int d = 0; d < NDET; d++) {
-      uint64_t psi = ph + x.det[d].L0 + x.det[d].L1 * (uint64_t)n;
       float sn, cs;
-      q64_sincospi(psi, &sn, &cs);
+      cmulf(cp, sp, rotc[d], rots[d], cs, sn);
       float ar = a * dre[d], ai = a * dim[d];
       kadd(acc[d * kAccPerDet + 0], w[d] * aa);
       kadd(acc[d * kAccPerDet + 1], ar * cs - ai * sn);
@@ -766,9 +784,8 @@ GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float
   float spp = aa * (hpr * hpr + hpi * hpi), scc = aa * (hcr * hcr + hci * hci), spc = aa * (hpr * hcr + hpi * hci);
 #pragma unroll
   for (int d = 0; d < NDET; d++) {
-    uint64_t psi = ph + x.det[d].L0 + x.det[d].L1 * (uint64_t)n;
     float sn, cs;
-    q64_sincospi(psi, &sn, &cs);
+    cmulf(cp, sp, rotc[d], rots[d], cs, sn);
     // a * dhat * exp(i psi)
     float qr = a * (dre[d] * cs - dim[d] * sn), qi = a * (dre[d] * sn + dim[d] * cs);
     kadd(acc[d * kAccPerDet + 0], w[d] * spp);

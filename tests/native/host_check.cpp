@@ -160,13 +160,21 @@ double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, cons
         dim[d] = dh[d][2 * k + 1];
         w[d] = wh[d][k];
       }
+      // the kernel's detector rotations: segment factor times offset factor
+      float rc[kMaxDet], rs[kMaxDet];
+      for (int d = 0; d < ndet; d++) {
+        float ac, as, bc, bs;
+        det_rot_seg(x, d, n0 + kseg, ac, as);
+        det_rot_off(x, d, k - kseg, bc, bs);
+        cmulf(ac, as, bc, bs, rc[d], rs[d]);
+      }
       KSum acc[kMaxDet * kAccPerDet];
       for (auto &a : acc) a = KSum{0.f, 0.f};
       switch (ndet) {
-        case 1: mixed_bin_q<1>(x, n, ph, al, tf, m76, dre, dim, w, acc); break;
-        case 2: mixed_bin_q<2>(x, n, ph, al, tf, m76, dre, dim, w, acc); break;
-        case 3: mixed_bin_q<3>(x, n, ph, al, tf, m76, dre, dim, w, acc); break;
-        default: mixed_bin_q<4>(x, n, ph, al, tf, m76, dre, dim, w, acc); break;
+        case 1: mixed_bin_q<1>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc); break;
+        case 2: mixed_bin_q<2>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc); break;
+        case 3: mixed_bin_q<3>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc); break;
+        default: mixed_bin_q<4>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc); break;
       }
       for (int j = 0; j < kMaxDet * kAccPerDet; j++) sums[j] += (double)(acc[j].s - acc[j].c);
     }
