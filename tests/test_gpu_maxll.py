@@ -146,3 +146,21 @@ def test_search_path_matches_fp64_transforms(gpu_ctx, fp64_ctx, setup, approx):
         assert np.all(st == 0)
         outs.append(out)
     assert np.all(np.abs(outs[0] - outs[1]) <= 1e-10 * np.abs(outs[1])), np.max(np.abs(outs[0] - outs[1]) / np.abs(outs[1]))
+
+
+def test_flat_spectrum_takes_the_fp64_transforms(gpu_ctx, oracle, setup):
+    """Zero data: every bin scores the same, so a pair has more candidates
+    than the FP32 search keeps and the batch goes to the FP64 transforms; the
+    result is the oracle's (zero) all the same, for both forms."""
+    s = setup
+    zero = np.zeros(s["f"].size, dtype=np.complex128)
+    d = W.prior_draws(1, 91, precessing=True)[0]
+    hp, hc = oracle.fourier_waveform(s["f"], oracle.params_from_dict(d), oracle.IMRPhenomPv2)
+    got = gpu_ctx.maximized_log_likelihood_internal(zero, s["psd"], s["f"], hp)
+    assert got == oracle.maximized_loglik_internal(zero, s["psd"], s["f"], hp) == 0.0
+    got_u = gpu_ctx.maximized_log_likelihood_unaligned_internal(zero, s["psd"], s["f"], hp, hc)
+    ref_u = oracle.maximized_loglik_unaligned_internal(zero, s["psd"], s["f"], hp, hc)
+    assert abs(got_u - ref_u) <= 1e-12 and abs(ref_u) <= 1e-12
+    hs = [gpu_ctx.register_data(det, s["f"], zero, s["psd"]) for det in s["dets"]]
+    out, st = gpu_ctx.maximized_loglik_batch(G.params_array(W.prior_draws(5, 92)), hs)
+    assert np.all(st == 0) and np.all(out == 0.0)
