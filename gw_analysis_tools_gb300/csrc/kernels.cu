@@ -287,11 +287,12 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 //   S1  W0/W3 calibration fits;  W1 D: ringdown frequencies / Pv2: J-frame transform;  W2 PN coefficients
 //   S2  W0 Pv2: ringdown frequencies; matching frequencies;  W1 D: phase at f_ref (inspiral);
 //       W2 D: ringdown-phase terms at f3
-//   S3  W0/W1 amplitude matching points;  W2 phase connection, inspiral part;  W3 D: phase
-//       connection, other parts / Pv2: Euler and frame constants (W1 then the other parts)
+//   S3  W0/W1 amplitude matching points;  D: phase connection in four pieces after them
+//       (W1 inspiral phase, W2 inspiral derivative and f1 terms, W3 f2 terms);
+//       Pv2: W2 inspiral part, W1 the other parts, W3 Euler and frame constants
 //   S3b Pv2: W2 phase connection constants
-//   S4  W0/W1 amplitude deltas;  W2 D: phase connection constants, phase/time shift /
-//       Pv2: time-shift nodes 0-4;  W3 Pv2: nodes 5-9
+//   S4  amplitude deltas (D: W0/W1/W3, Pv2: W0/W1);  W2 D: phase connection constants,
+//       phase/time shift / Pv2: time-shift nodes 0-4;  W3 Pv2: nodes 5-9
 //   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions;  W3 D: detector phases and factors /
 //       Pv2: time shift, angles
 //   S6  W0 Pv2: detector phases and factors; outputs
@@ -377,11 +378,19 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     if (warp == 1) {
       d_amp_conn_high(r.m, s_ac[lane]);
       if (pv2) phase_conn_imr(r.m, s_pc[lane]);
+      else phase_conn_phins(r.m, s_pc[lane]);
     }
-    if (warp == 2) phase_conn_ins(r.m, s_pc[lane]);
+    if (warp == 2) {
+      if (pv2) {
+        phase_conn_ins(r.m, s_pc[lane]);
+      } else {
+        phase_conn_dins(r.m, s_pc[lane]);
+        phase_conn_imr1(r.m, s_pc[lane]);
+      }
+    }
     if (warp == 3) {
       if (pv2) model_p_finish(r.m, r.p);
-      else phase_conn_imr(r.m, s_pc[lane]);
+      else phase_conn_imr2(r.m, s_pc[lane]);
     }
   }
   __syncthreads();
@@ -390,14 +399,19 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   __syncthreads();
   // S4
   if (run) {
-    if (warp == 0) d_deltas(r.m, s_ac[lane], 0, 3);
-    if (warp == 1) d_deltas(r.m, s_ac[lane], 3, 5);
     if (!pv2) {
+      if (warp == 0) d_deltas(r.m, s_ac[lane], 0, 2);
+      if (warp == 1) d_deltas(r.m, s_ac[lane], 2, 4);
+      if (warp == 3) d_deltas(r.m, s_ac[lane], 4, 5);
       if (warp == 2) {
         phase_conn_combine(r.m, s_pc[lane]);
         model_d_finish_parts(r.m, s_pc[lane]);
       }
-    } else if (r.m.s.shift_time && (warp == 2 || warp == 3)) {
+    } else {
+      if (warp == 0) d_deltas(r.m, s_ac[lane], 0, 3);
+      if (warp == 1) d_deltas(r.m, s_ac[lane], 3, 5);
+    }
+    if (pv2 && r.m.s.shift_time && (warp == 2 || warp == 3)) {
       for (int j = (warp - 2) * (kPv2ShiftNodes / 2); j < (warp - 1) * (kPv2ShiftNodes / 2); j++)
         s_shift[lane][j] = pv2_shift_node(r.m, j);
     }

@@ -177,15 +177,25 @@ struct PhaseConnParts {
   double phi_fref, a1fit, A3, B3;
   int have_phi;
 };
-GW_HD void phase_conn_ins(const ModelD &m, PhaseConnParts &c) {
+// The inspiral part in two halves (derivative, value), and the rest in two
+// (terms at f1, terms at f2): four pieces that can run on four warps.
+GW_HD void phase_conn_dins(const ModelD &m, PhaseConnParts &c) {
+  double pn[12];  // coefficients 5 and 6 are set at f1 by the call
+  for (int j = 0; j < 12; j++) pn[j] = m.pn_phase[j];
+  c.Dins1 = Dphase_ins(m.s.f1_phase, m.s, pn, m.l);
+}
+GW_HD void phase_conn_phins(const ModelD &m, PhaseConnParts &c) {
   const Source &s = m.s;
   const double f1 = s.f1_phase;
-  double pn[12];  // coefficients 5 and 6 are set at f1 by both calls
+  double pn[12];
   for (int j = 0; j < 12; j++) pn[j] = m.pn_phase[j];
-  c.Dins1 = Dphase_ins(f1, s, pn, m.l);
   Pows pw;
   precalc_powers_ins(f1, s.M, pw);
   c.ins1 = phase_ins(f1, s, pn, m.l, m.pi, pw);
+}
+GW_HD void phase_conn_ins(const ModelD &m, PhaseConnParts &c) {
+  phase_conn_dins(m, c);
+  phase_conn_phins(m, c);
 }
 // Dphase_mr(f3) (IMRPhenomD.cpp:1539-1554) = (A3 + M (alpha1 + B3)) / eta;
 // f3 = fpeak as model_d_freqs sets it (passed, so that this can run beside it).
@@ -209,10 +219,10 @@ GW_HD void finish_fref_phase(const ModelD &m, PhaseConnParts &c) {
   c.phi_fref = phase_ins(s.f_ref, s, pn, m.l, m.pi, pw);
   c.have_phi = 1;
 }
-GW_HD void phase_conn_imr(const ModelD &m, PhaseConnParts &c) {
+GW_HD void phase_conn_imr1(const ModelD &m, PhaseConnParts &c) {
   const Source &s = m.s;
   const Lambda &l = m.l;
-  const double M = s.M, eta = s.eta, M3 = M * M * M;
+  const double M = s.M, M3 = M * M * M;
   c.a1fit = l.alpha[1];  // still the fit: the connection replaces it
   {
     const double f = s.f1_phase, ff = f * f, Mf = M * f, Mf3 = Mf * Mf * Mf;
@@ -220,6 +230,11 @@ GW_HD void phase_conn_imr(const ModelD &m, PhaseConnParts &c) {
     c.P1 = l.beta[2] * log(Mf);
     c.Q1 = l.beta[3] / 3. * 1. / Mf3;
   }
+}
+GW_HD void phase_conn_imr2(const ModelD &m, PhaseConnParts &c) {
+  const Source &s = m.s;
+  const Lambda &l = m.l;
+  const double M = s.M, eta = s.eta, M3 = M * M * M;
   {
     const double f = s.f2_phase, ff = f * f, Mf = M * f, Mf3 = Mf * Mf * Mf;
     c.R2 = l.beta[2] / f;
@@ -234,6 +249,10 @@ GW_HD void phase_conn_imr(const ModelD &m, PhaseConnParts &c) {
     c.T2 = (4. / 3) * l.alpha[3] * sqrt(sqrt(Mf * Mf * Mf));
     c.T3 = l.alpha[4] * atan((f - l.alpha[5] * s.fRD) / s.fdamp);
   }
+}
+GW_HD void phase_conn_imr(const ModelD &m, PhaseConnParts &c) {
+  phase_conn_imr1(m, c);
+  phase_conn_imr2(m, c);
 }
 GW_HD void phase_conn_combine(ModelD &m, const PhaseConnParts &c) {
   const Source &s = m.s;
