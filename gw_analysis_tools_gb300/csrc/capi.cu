@@ -334,12 +334,15 @@ static int register_stream(gwgpu_context *c, const char *detector, const double 
     wh[k] = (float)(W[k] / d.wscale);
   }
   int st;
-  void *pf, *pd, *pp, *pdh, *pwh, *piw = nullptr;
+  void *pf, *pd, *pp, *pip, *pdh, *pwh, *piw = nullptr;
+  std::vector<double> ip(N);  // the reciprocal PSD: the FP64 kernels multiply instead of dividing
+  for (int k = 0; k < N; k++) ip[k] = 1.0 / psd[k];
   if ((st = c->dalloc(&pf, 8 * (size_t)N, "freqs")) || (st = c->dalloc(&pd, 16 * (size_t)N, "data")) ||
-      (st = c->dalloc(&pp, 8 * (size_t)N, "psd")) || (st = c->dalloc(&pdh, 8 * (size_t)N, "dhat")) ||
-      (st = c->dalloc(&pwh, 4 * (size_t)N, "what")) ||
+      (st = c->dalloc(&pp, 8 * (size_t)N, "psd")) || (st = c->dalloc(&pip, 8 * (size_t)N, "inverse psd")) ||
+      (st = c->dalloc(&pdh, 8 * (size_t)N, "dhat")) || (st = c->dalloc(&pwh, 4 * (size_t)N, "what")) ||
       (weights && (st = c->dalloc(&piw, 8 * (size_t)N, "integration weights"))))
     return st;
+  cudaMemcpyAsync(pip, ip.data(), 8 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
   if (piw) cudaMemcpyAsync(piw, iw.data(), 8 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(pf, freqs, 8 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(pd, data, 16 * (size_t)N, cudaMemcpyHostToDevice, c->stream);
@@ -351,11 +354,12 @@ static int register_stream(gwgpu_context *c, const char *detector, const double 
   d.freqs = (const double *)pf;
   d.data = (const double *)pd;
   d.psd = (const double *)pp;
+  d.ipsd = (const double *)pip;
   d.dhat = (const float *)pdh;
   d.what = (const float *)pwh;
   d.iw = (const double *)piw;
   s.live = true;
-  s.mem = {pf, pd, pp, pdh, pwh};
+  s.mem = {pf, pd, pp, pip, pdh, pwh};
   if (piw) s.mem.push_back(piw);
   s.host_freqs.assign(freqs, freqs + N);
   uint64_t hsh = 1469598103934665603ull;

@@ -160,10 +160,31 @@ __device__ __forceinline__ void fp64_bin(const Request &r, const StreamDev *st, 
   for (int d = 0; d < NDET; d++) {
     cd x = response_bin(r.det[d], hp, hc, f, r.det[d].tau != 0.0);
     double2 dd = ((const double2 *)st[d].data)[k];
-    double S = st[d].psd[k];
+    const double iS = st[d].ipsd ? st[d].ipsd[k] : 1.0 / st[d].psd[k];
     const double w = st[d].iw ? st[d].iw[k] : ws;
-    v[2 * d] += w * ((x.re * x.re + x.im * x.im) / S);
-    v[2 * d + 1] += w * ((dd.x * x.re + dd.y * x.im) / S);
+    v[2 * d] += w * ((x.re * x.re + x.im * x.im) * iS);
+    v[2 * d + 1] += w * ((dd.x * x.re + dd.y * x.im) * iS);
+  }
+}
+// The same with each detector's arrival-time rotation e^{i tau_d f} given
+// (rc, rs): the batched kernel builds it on uniform grids as the product of a
+// per-pass and a per-thread factor instead of one sincos per detector-bin.
+template <int NDET>
+__device__ __forceinline__ void fp64_bin_rot(const Request &r, const StreamDev *st, int k, int N, const double *rc,
+                                             const double *rs, double (&v)[2 * NDET]) {
+  const double f = st[0].freqs[k];
+  cd hp, hc;
+  wave_bin(r, f, hp, hc);
+  const double ws = simpson_weight(k, N);
+#pragma unroll
+  for (int d = 0; d < NDET; d++) {
+    const cd y = response_bin(r.det[d], hp, hc, f, false);
+    const cd x{y.re * rc[d] - y.im * rs[d], y.re * rs[d] + y.im * rc[d]};
+    double2 dd = ((const double2 *)st[d].data)[k];
+    const double iS = st[d].ipsd ? st[d].ipsd[k] : 1.0 / st[d].psd[k];
+    const double w = st[d].iw ? st[d].iw[k] : ws;
+    v[2 * d] += w * ((x.re * x.re + x.im * x.im) * iS);
+    v[2 * d + 1] += w * ((dd.x * x.re + dd.y * x.im) * iS);
   }
 }
 template <int NDET>
@@ -530,6 +551,7 @@ cudaError_t launch_mcmc_repack(const double *theta, int dim, int n, int approxim
 constexpr int kBatchBlock = 256;
 static_assert(kBatchBlock == kSegBins, "one block pass covers one phase segment");
 constexpr int kMaxSegs = 32;  // segments per chunk of an item (shared buffers)
+constexpr int kMaxTile = 16384;  // FP64 form: items up to this many bins use the rotation table
 constexpr int kStatusBounds = 0x100;  // set by an item whose bins fall outside the tables; finalize reports 5
 
 // Two-level compensated reduction of NV FP32 values per thread:
@@ -586,6 +608,9 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
   __shared__ double s_node[kSegBuf * kSegEval], s_node_a[kSegBuf * kSegEval];
   __shared__ SegPoly s_poly[kSegBuf], s_poly_a[kSegBuf];
   __shared__ double s_coef[kSegBuf * 2 * kSegNodes];
+  // FP64 form on uniform grids: each pass's arrival-time rotations
+  constexpr int kRotPasses = MIXED ? 1 : kMaxTile / kBatchBlock;
+  __shared__ double2 s_rot64[kRotPasses * NDET];
   // detector rotations: per segment pass (first bin) and per thread offset
   __shared__ float2 s_rot_seg[kSegBuf * (MIXED ? NDET : 1)];
   __shared__ float2 s_rot_off[(MIXED ? NDET : 1) * (MIXED ? kBatchBlock : 1)];
@@ -726,8 +751,39 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
       double v[NV];
 #pragma unroll
       for (int j = 0; j < NV; j++) v[j] = 0.0;
-      if (r.m.status == 0)
+      bool uniform = true;
+#pragma unroll
+      for (int d = 0; d < NDET; d++) uniform = uniform && s_st[d].uniform_int;
+      const int npass = (kend - I.k0 + kBatchBlock - 1) / kBatchBlock;
+      if (uniform && npass <= kRotPasses) {
+        // e^{i tau f_k} = e^{i tau f_(first bin of the pass)} e^{i tau (k - first) df}
+        for (int e = tid; e < npass * NDET; e += blockDim.x) {
+          const int pass = e / NDET, d = e - pass * NDET;
+          double sn, cs;
+          sincos(r.det[d].tau * s_st[0].freqs[I.k0 + pass * kBatchBlock], &sn, &cs);
+          s_rot64[e] = make_double2(cs, sn);
+        }
+        double oc[NDET], os[NDET];
+#pragma unroll
+        for (int d = 0; d < NDET; d++) sincos(r.det[d].tau * (tid * s_st[0].df), &os[d], &oc[d]);
+        __syncthreads();
+        if (r.m.status == 0) {
+          int pass = 0;
+          for (int k = I.k0 + tid; k < kend; k += blockDim.x, pass++) {
+            double rc[NDET], rs[NDET];
+#pragma unroll
+            for (int d = 0; d < NDET; d++) {
+              const double2 b = s_rot64[pass * NDET + d];
+              rc[d] = b.x * oc[d] - b.y * os[d];
+              rs[d] = b.y * oc[d] + b.x * os[d];
+            }
+            fp64_bin_rot<NDET>(r, s_st, k, N, rc, rs, v);
+          }
+        }
+        __syncthreads();  // s_rot64 is rewritten by the next item
+      } else if (r.m.status == 0) {
         for (int k = I.k0 + tid; k < kend; k += blockDim.x) fp64_bin<NDET>(r, s_st, k, N, v);
+      }
       block_sum<NV>(v, s_dsm);
       if (tid == 0)
 #pragma unroll

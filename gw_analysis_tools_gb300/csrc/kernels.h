@@ -22,6 +22,7 @@ struct StreamDev {
   double df;          // f[1] - f[0]
   double simpson_df;  // f[N/2] - f[N/2-1] (mcmc_gw.cpp:811)
   const double *freqs, *data, *psd;  // FP64 originals (data interleaved complex)
+  const double *ipsd;                // 1 / psd (null: divide per bin)
   const float *dhat, *what;          // mixed-form streams (interleaved complex, real)
   double dscale, wscale;
   // integration weights of the GAUSSLEG branch (mcmc_gw.cpp:820-862), times 4

@@ -106,7 +106,7 @@ __global__ void k_maxll_prep(const Request *__restrict__ req, const double2 *__r
         if (UN) hc = resp_c[(size_t)q * N + k];
       }
       const double2 d = ((const double2 *)st.data)[k];
-      const double iS = 1.0 / st.psd[k], w = gwt::simpson_weight(k, N), s4 = 4.0 * iS;
+      const double iS = st.ipsd ? st.ipsd[k] : 1.0 / st.psd[k], w = gwt::simpson_weight(k, N), s4 = 4.0 * iS;
       // 4 conj(d) h / S, then the Bluestein chirp
       double2 v = make_double2(s4 * (d.x * hp.x + d.y * hp.y), s4 * (d.x * hp.y - d.y * hp.x));
       g[((size_t)q * NP) * ld + k] = make_double2(v.x * ch.x - v.y * ch.y, v.x * ch.y + v.y * ch.x);
@@ -296,7 +296,7 @@ __global__ void k_mx_prep(const Request *__restrict__ req, const double2 *__rest
         if (UN) hc = resp_c[(size_t)q * N + k];
       }
       const double2 d = ((const double2 *)st.data)[k];
-      const double iS = 1.0 / st.psd[k], w = gwt::simpson_weight(k, N), s4 = 4.0 * iS;
+      const double iS = st.ipsd ? st.ipsd[k] : 1.0 / st.psd[k], w = gwt::simpson_weight(k, N), s4 = 4.0 * iS;
       const double2 v = make_double2(s4 * (d.x * hp.x + d.y * hp.y), s4 * (d.x * hp.y - d.y * hp.x));
       g64[((size_t)q * NP) * N + k] = v;
       const float vx = (float)v.x, vy = (float)v.y;
