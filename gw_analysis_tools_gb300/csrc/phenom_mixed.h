@@ -466,7 +466,6 @@ GW_HDNI int mixed_prologue(const Request &r, double df, MixedReq &x, const doubl
 #if defined(__CUDA_ARCH__)
 GW_HD float __int_as_float_h(int i) { return __int_as_float(i); }
 GW_HD int __float_as_int_h(float f) { return __float_as_int(f); }
-GW_HD void gw_sincospif(float x, float *s, float *c) { sincospif(x, s, c); }
 GW_HD int64_t gw_llrint(double x) { return __double2ll_rn(x); }
 GW_HD int gw_f2i_rn(float x) { return __float2int_rn(x); }
 #else
@@ -479,12 +478,6 @@ inline int __float_as_int_h(float f) {
   int i;
   std::memcpy(&i, &f, 4);
   return i;
-}
-inline float rsqrtf(float x) { return 1.0f / std::sqrt(x); }
-GW_HD void gw_sincospif(float x, float *s, float *c) {
-  double a = 3.14159265358979323846 * (double)x;
-  *s = (float)std::sin(a);
-  *c = (float)std::cos(a);
 }
 GW_HD int64_t gw_llrint(double x) { return (int64_t)std::llrint(x); }
 GW_HD int gw_f2i_rn(float x) { return (int)std::lrintf(x); }
