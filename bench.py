@@ -454,8 +454,26 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
             os.remove(p)
         os.rmdir(tmp)
 
+    def gaussleg():
+        # GAUSSLEG integration: a 3000-node Gauss-Legendre grid over 20-1024 Hz,
+        # weighted streams, batched FP64 (the mixed form needs uniform grids)
+        x, wq = np.polynomial.legendre.leggauss(3000)
+        h = 0.5 * (1024.0 - 20.0)
+        fg, wg = 20.0 + h * (x + 1.0), wq * h
+        psd_g = W.analytic_psd(fg)
+        hg = [ctx.register_data(d, fg, W.noise(fg, 700 + i), psd_g, weights=wg) for i, d in enumerate(W.DETECTORS3)]
+        parr = host_params[1]
+        ctx.loglik_batch(parr, 0, hg, 8.0, G.PREC_FP64)
+        reps = 5
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            _, st = ctx.loglik_batch(parr, 0, hg, 8.0, G.PREC_FP64)
+        dt = (time.perf_counter() - t0) / reps
+        ex["gaussleg_fp64"] = {"evals_per_s": N_REQ / dt, "ms_per_call": dt * 1e3, "nodes": int(fg.size),
+                               "ok": int((st == 0).sum())}
+
     for name, fn in (("plain", plain), ("batched_fp64", batched_fp64), ("served", served), ("uneven", uneven),
-                     ("fisher", fisher), ("maximized", maximized), ("ingest", ingest)):
+                     ("fisher", fisher), ("maximized", maximized), ("ingest", ingest), ("gaussleg", gaussleg)):
         if args.forms and name not in args.forms.split(","):
             continue
         log(name)
@@ -622,7 +640,7 @@ def main():
     if ex:
         plain = ex.get("plain_fp64_evals_per_s")
         for k in ("plain_fp64_evals_per_s", "plain_fp64_p50_ms", "batched_fp64_evals_per_s", "served", "uneven_pv2",
-                  "maximized", "ingest", "errors"):
+                  "maximized", "ingest", "gaussleg_fp64", "errors"):
             if k in ex:
                 line[k] = ex[k]
         if plain:
