@@ -358,6 +358,24 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         ex["served"] = {"evals_per_s": nserve / wall, "p50_ms": s["p50_s"] * 1e3, "p99_ms": s["p99_s"] * 1e3,
                         "offered_rate": 2e5, "requests": nserve, "launches": s["launches"], "ensembles": ens,
                         "ok": int((st == 0).sum())}
+        # the same mix offered faster than the engine serves it: its capacity
+        nsat = 200000
+        ds = W.prior_draws(nsat // 2, 503)
+        dq = W.prior_draws(nsat - nsat // 2, 504, precessing=True)
+        sp2 = [ds[i // 2] if i % 2 == 0 else dq[i // 2] for i in range(nsat)]
+        sa2 = [i % 2 for i in range(nsat)]
+        arr2 = np.cumsum(rng.exponential(1.0 / 5e6, nsat))
+        srv = G.Server(ctx, T, max_inflight=65536, max_batch=4096, lanes=4, hbm_budget=120 * 1024 ** 3)
+        try:
+            srv.drive(G.params_array(sp2[:8192]), sa2[:8192], handles, arr2[:8192] - arr2[0])  # warm-up
+            srv.reset_stats()
+            out, st, lat, wall = srv.drive(G.params_array(sp2), sa2, handles, arr2 - arr2[0])
+            s = srv.stats()
+        finally:
+            srv.close()
+        ex["served"]["saturated"] = {"evals_per_s": nsat / wall, "p50_ms": s["p50_s"] * 1e3,
+                                     "p99_ms": s["p99_s"] * 1e3, "offered_rate": 5e6, "requests": nsat,
+                                     "max_batch": 4096, "launches": s["launches"], "ok": int((st == 0).sum())}
 
     def uneven():
         # uneven Pv2 batch: T in {4, 8, 32, 128}, 20-2048 Hz, 1024 requests, one launch
