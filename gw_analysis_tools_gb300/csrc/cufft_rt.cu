@@ -49,6 +49,7 @@ Lib &lib() {
   return f;
 }
 
+constexpr size_t kMaxPlans = 16;  // per context
 std::mutex g_mu;
 std::map<gwgpu_context *, std::map<std::tuple<int, int, int>, int>> g_plans;
 
@@ -67,6 +68,10 @@ int plan(gwgpu_context *c, Type type, int N, int batch, int *out) {
   if (it != m.end()) {
     *out = it->second;
     return GWGPU_OK;
+  }
+  if (m.size() >= kMaxPlans) {  // plans hold device work areas: bounded, oldest shapes dropped wholesale
+    for (auto &kv : m) f.destroy(kv.second);
+    m.clear();
   }
   int p = 0, n = N;
   const int odist = type == kD2Z ? N / 2 + 1 : N;

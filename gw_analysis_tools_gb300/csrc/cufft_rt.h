@@ -16,7 +16,9 @@ constexpr int kForward = -1;             // CUFFT_FORWARD
 constexpr int kInverse = 1;              // CUFFT_INVERSE (unnormalised)
 
 // A plan of `batch` contiguous length-N transforms (input distance N, output
-// distance N for Z2Z and N/2 + 1 for D2Z), reused across calls.
+// distance N for Z2Z/C2C and N/2 + 1 for D2Z), reused across calls.  The cache
+// holds at most 16 plans per context; creating one more destroys the others,
+// so a caller fetches the plan it executes after any other plan it needs.
 int plan(gwgpu_context *c, Type type, int N, int batch, int *out);
 // Transforms on stream s (Z2Z / C2C in either direction, in place allowed; D2Z forward).
 int exec_z2z(gwgpu_context *c, int plan, double2 *in, double2 *out, int direction, cudaStream_t s);

@@ -640,12 +640,12 @@ int run_fp64(gwgpu_context *c, const MxIn &in, double *out, int *status) {
   const int np = in.un ? 2 : 1, ns = in.un ? 3 : 1, pairs = in.n * in.ndet, rows = pairs * np;
   int blue;
   const int ld = xform_len(in.N, &blue);
-  int plan;
-  int st = gwfft::plan(c, gwfft::kZ2Z, ld, rows, &plan);
-  if (st) return st;
   const double2 *B64 = nullptr;
   const float2 *B32 = nullptr;
-  if (blue && (st = ensure_chirp(c, in.N, ld, &B64, &B32))) return st;
+  int st = blue ? ensure_chirp(c, in.N, ld, &B64, &B32) : GWGPU_OK;
+  if (st) return st;
+  int plan;  // fetched last: a new plan may reset the cache (cufft_rt.cu)
+  if ((st = gwfft::plan(c, gwfft::kZ2Z, ld, rows, &plan))) return st;
   const int nblk = (ld + kBlock - 1) / kBlock;
   const size_t o_g = 0, o_h = up256(16 * (size_t)rows * ld), o_ll = o_h + up256(8 * (size_t)pairs * ns * nblk),
                o_done = o_ll + up256(8 * (size_t)pairs), total = o_done + up256(4 * (size_t)in.n);
@@ -687,16 +687,16 @@ int run_search(gwgpu_context *c, const MxIn &in, double *out, int *status, bool 
   *fallback = false;
   int blue;
   const int ld = xform_len(in.N, &blue);
-  int plan;
-  int st = gwfft::plan(c, gwfft::kC2C, ld, rows, &plan);
-  if (st) return st;
   const double2 *B64 = nullptr;
   const float2 *B32 = nullptr;
   double kscale = std::sqrt((double)in.N);
+  int st = GWGPU_OK;
   if (blue) {
     if ((st = ensure_chirp(c, in.N, ld, &B64, &B32))) return st;
     kscale = c->chirp_kscale;
   }
+  int plan;  // fetched last: a new plan may reset the cache (cufft_rt.cu)
+  if ((st = gwfft::plan(c, gwfft::kC2C, ld, rows, &plan))) return st;
   const int nblk = (ld + kBlock - 1) / kBlock;
   const size_t o_g = 0, o_a = up256(16 * (size_t)rows * in.N), o_h = o_a + up256(8 * (size_t)rows * ld),
                o_s = o_h + up256(8 * (size_t)pairs * ns * nblk), o_c = o_s + up256(8 * (size_t)pairs * ns),
