@@ -595,7 +595,7 @@ __device__ __forceinline__ void block_sum_mixed(const float (&v)[NV], float *sm,
 }
 
 template <int NDET, int MIXED>
-__global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const BatchArgs a) {
+__global__ void __launch_bounds__(kBatchBlock, MIXED ? 3 : 2) k_batch(const BatchArgs a) {
   constexpr int NV = MIXED ? NDET * kAccPerDet : 2 * NDET;
   __shared__ int s_item;
   __shared__ __align__(16) unsigned char s_req[MIXED ? sizeof(MixedReq) : sizeof(Request)];
