@@ -48,6 +48,8 @@ struct MixedDet {
 };
 
 constexpr int kAccPerDet = 5;  // D uses 3 (hh, zr, zi); Pv2 uses 5 (spp, scc, spc, zp, zc)
+constexpr float kSegFScale = 268435456.0f;  // FP32 part of a segment phase polynomial: turns * 2^28
+
 struct MixedReq {
   int approximant, status, ndet, pad;
   int n_f1, n_f3, n_f1p, n_f2p, n_cut;  // region starts (first n in region) and last non-zero n
@@ -64,7 +66,8 @@ struct MixedReq {
   float ai[10], ai_lo[10];              // inspiral: sum ai_j t^j
   float ei[5], ei_lo[5];                // intermediate: sum ei_j (n - n_mid)^j
   float mrK, mrK_lo, mrExp, mrExp_lo;   // ringdown: mrK exp(-mrExp x) / (x^2 + mrG2), x = n - n_rd - frac
-  float mrG2, mrG2_lo, mrRDfrac, pad3;
+  float mrG2, mrG2_lo, mrRDfrac;
+  float mEq;                            // mE in the segment polynomials' FP32 units (turns * 2^28)
   float ncfrac, inv_nw;                 // atan argument y = (n - n_c - ncfrac) * inv_nw
   // Pv2
   double ea[6], ee[6];                  // alpha/epsilon: r*(a0 t^2 + a1 n + a2 n t) + a3 + a4 t + a5 tln
@@ -300,6 +303,7 @@ GW_HD void mixed_phase_coeffs(const Request &r, double df, MixedReq &x) {
   x.mC = m.l.alpha[2] * s.inv_eta * iMdf;
   x.mD = (4. / 3.) * m.l.alpha[3] * sqrt(Mdf * sqrt(Mdf)) * s.inv_eta;
   x.mE = m.l.alpha[4] * s.inv_eta;
+  x.mEq = (float)(x.mE * (1.0 / (2.0 * 3.14159265358979323846)) * kSegFScale);
   {
     double nc = m.l.alpha[5] * s.fRD / df;
     double nci = floor(nc);
@@ -621,7 +625,6 @@ constexpr int kSegQ = 5;                     // m^0 .. m^4 in fixed point
 constexpr int kSegF = kSegNodes - kSegQ;     // u^5 .. u^8 in FP32
 constexpr double kSegTolRad = 1e-8;          // interpolation error allowed at the check points
 constexpr double kSegFMaxTurns = 0.02;       // bound on the FP32 part (sum of |coefficients|)
-constexpr float kSegFScale = 268435456.0f;   // FP32 part in turns * 2^28
 
 struct SegPoly {
   uint64_t q[kSegQ];  // coefficient of m^j, turns * 2^64
@@ -700,7 +703,7 @@ GW_HD uint64_t seg_eval(const SegPoly &p, int m, float extra = 0.0f) {
 }
 // The FP32 ringdown atan term of bin n in the units of seg_eval's extra.
 GW_HD float seg_atan_extra(const MixedReq &x, int n) {
-  return (float)(x.mE * (1.0 / (2.0 * 3.14159265358979323846)) * kSegFScale) * mixed_atan(x, n);
+  return x.mEq * mixed_atan(x, n);
 }
 
 // The detector's linear phase (L0 + L1 n, turns * 2^64) as a rotation, in
