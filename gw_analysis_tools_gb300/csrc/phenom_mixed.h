@@ -472,6 +472,7 @@ GW_HD float __int_as_float_h(int i) { return __int_as_float(i); }
 GW_HD int __float_as_int_h(float f) { return __float_as_int(f); }
 GW_HD int64_t gw_llrint(double x) { return __double2ll_rn(x); }
 GW_HD int gw_f2i_rn(float x) { return __float2int_rn(x); }
+GW_HD float gw_rsqrt_rn(float x) { return __frsqrt_rn(x); }  // 1/sqrt(x), correctly rounded
 #else
 inline float __int_as_float_h(int i) {
   float f;
@@ -485,6 +486,7 @@ inline int __float_as_int_h(float f) {
 }
 GW_HD int64_t gw_llrint(double x) { return (int64_t)std::llrint(x); }
 GW_HD int gw_f2i_rn(float x) { return (int)std::lrintf(x); }
+GW_HD float gw_rsqrt_rn(float x) { return (float)(1.0 / std::sqrt((double)x)); }
 #endif
 
 // Kahan-compensated FP32 accumulator: value = s - c.
@@ -525,10 +527,11 @@ GW_HD double mixed_phase_d(const MixedReq &x, int n, double t, double r, double 
 // so the lo parts of per-request coefficients are not lost to round-to-nearest.
 GW_HD float sround(float hi, float lo, uint32_t u) {
   float ahi = fabsf(hi);
-  float ulp = __int_as_float_h(__float_as_int_h(ahi) + 1) - ahi;
-  float p = fabsf(lo) / ulp;
-  float fu = (float)(u >> 8) * 5.9604644775390625e-08f;  // 2^-24
-  return (fu < p) ? hi + copysignf(ulp, lo) : hi;
+  float ulp = __int_as_float_h(__float_as_int_h(ahi) + 1) - ahi;  // a power of two
+  float fu = (float)(u >> 8) * 5.9604644775390625e-08f;            // 2^-24
+  // fu < |lo| / ulp without the division: fu * ulp is exact (24-bit fu times
+  // a power of two) for every amplitude above 2^-100
+  return (fu * ulp < fabsf(lo)) ? hi + copysignf(ulp, lo) : hi;
 }
 GW_HD uint32_t dither(int n) { return (uint32_t)n * 2654435769u; }  // Weyl sequence, golden ratio
 
@@ -547,10 +550,10 @@ GW_HD float mixed_amp(const MixedReq &x, int n, float tf, float m76) {
     }
   } else if (n >= x.n_f3) {
     float xx = (float)(n - x.n_rd) - x.mrRDfrac;
-    float den = fmaf(xx, xx, x.mrG2);
-    float e = expf(-x.mrExp * xx) / den;
+    float iden = 1.0f / fmaf(xx, xx, x.mrG2);
+    float e = expf(-x.mrExp * xx) * iden;
     hi = x.mrK * e;
-    lo = e * (x.mrK_lo - x.mrK * (x.mrExp_lo * xx + x.mrG2_lo / den));
+    lo = e * (x.mrK_lo - x.mrK * (x.mrExp_lo * xx + x.mrG2_lo * iden));
   } else {
     float h = (float)(n - x.n_mid);
     const float *e = x.ei, *el = x.ei_lo;
@@ -752,12 +755,17 @@ GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float
   // WignerD from L2PN (IMRPhenomP.cpp:665-693, 1214-1220)
   float tf2 = tf * tf;
   float xx = fmaf(x.x2c, tf2, x.x2c_lo * tf2);
-  float rs = 1.0f / sqrtf(xx);
+  float rs = gw_rsqrt_rn(xx);
   float ph_ = fmaf(fmaf(x.w[2], xx, x.w[1]), xx, x.w[0]);
   float pl_ = fmaf(fmaf(x.w_lo[2], xx, x.w_lo[1]), xx, x.w_lo[0]);
   float us = sround(fmaf(ph_, rs, x.w[3]), fmaf(pl_, rs, x.w_lo[3]), dither(n) ^ 0x9e3779b9u);  // 1/s
-  float cb = fabsf(us) / sqrtf(fmaf(us, us, 1.0f));  // cos beta = 1/sqrt(1 + s^2) >= 0, also when L + SL < 0
-  float cbh = sqrtf((1.0f + cb) * 0.5f), sbh = sqrtf(fmaxf(1.0f - cb, 0.0f) * 0.5f);
+  // sin beta = 1/sqrt(1 + us^2); cos beta = |us| sin beta >= 0, also when L + SL < 0
+  float sb = gw_rsqrt_rn(fmaf(us, us, 1.0f));
+  float cb = fabsf(us) * sb;
+  // half angles: sin(beta/2) = sin beta / (2 cos(beta/2)), without the
+  // cancellation of 1 - cos beta near beta = 0
+  float yh = (1.0f + cb) * 0.5f, rcbh = gw_rsqrt_rn(yh);
+  float cbh = yh * rcbh, sbh = 0.5f * sb * rcbh;
   float c2 = cbh * cbh, s2 = sbh * sbh;
   float d2[5] = {s2 * s2, 2.f * cbh * s2 * sbh, 2.44948974278317788f * s2 * c2, 2.f * c2 * cbh * sbh, c2 * c2};
   // exp(i m alpha), m = -2..2
