@@ -330,9 +330,14 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   __shared__ double s_shift[kCoopReq][kPv2ShiftNodes];
   __shared__ double s_df[kCoopReq];
   __shared__ int s_st[kCoopReq], s_bad[kCoopReq], s_uni[kCoopReq];
+  __shared__ double s_pm[kCoopReq][2];  // D: final spin and radiated energy, for post_merger in S1
+  static_assert(2 * kCoopReq == 32, "two half-warps per warp share the block's requests");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kCoopReq + lane;
   const bool act = lane < kCoopReq && i < n;
+  // half-warp form: lanes j and j + kCoopReq both serve request j
+  const int hl = lane & (kCoopReq - 1);
+  const bool hact = blockIdx.x * kCoopReq + hl < n;
   Request &r = s_r[lane < kCoopReq ? lane : 0];
   const GenParams &p = s_p[lane < kCoopReq ? lane : 0];
   // S0
@@ -354,33 +359,50 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     r.approximant = ap;
     r.ndet = ndet;
     if (!bad) populate_core(r.m.s, q);
+    if (!bad && ap == kPhenomD && !r.m.s.dep_postmerger) {
+      s_pm[lane][0] = final_spin(r.m.s);
+      s_pm[lane][1] = EradRational0815(r.m.s.eta, r.m.s.spin1z, r.m.s.spin2z);
+    }
   }
   if (act && warp == 3) populate_amp(r.m.s, params[i]);
-  if (act && (warp == 1 || warp == 2)) {  // projections need only the sky position: detectors over warps 1, 2
-    const GenParams &q = params[i];
-    if (warp == 2) populate_incl(r.m.s, q);
+  if (warp == 1 || warp == 2) {  // projections need only the sky position: detectors over warps 1, 2
+    // sky_trig with the hour angle's sincos on lanes j and the declination's
+    // on lanes j + kCoopReq at once
+    const GenParams &q = params[min(blockIdx.x * kCoopReq + hl, n - 1)];
+    double s1, c1, sps, cps;
+    sincos(lane < kCoopReq ? q.gmst - q.RA : q.DEC, &s1, &c1);
+    sincos(q.psi, &sps, &cps);
     SkyTrig tr;
-    sky_trig(q.RA, q.DEC, q.psi, q.gmst, tr);
-    const int d0 = streams[handles[i * ndet]].det;
-    for (int d = warp - 1; d < ndet && d < kMaxDet; d += 2) {
-      const StreamDev &sd = streams[handles[i * ndet + d]];
-      const int dd = sd.det;
-      s_ds[lane][d] = sd.dscale;
-      s_ws[lane][d] = sd.wscale;
-      antenna_trig(dd, tr, r.det[d].fp, r.det[d].fc);
-      r.det[d].tau = -dtoa_trig(tr, d0, dd) * (2 * kPi);
+    tr.sg = __shfl_sync(0xffffffffu, s1, hl);
+    tr.cg = __shfl_sync(0xffffffffu, c1, hl);
+    tr.sd = __shfl_sync(0xffffffffu, s1, hl + kCoopReq);
+    tr.cd = __shfl_sync(0xffffffffu, c1, hl + kCoopReq);
+    tr.sp = sps;
+    tr.cp = cps;
+    if (act) {
+      if (warp == 2) populate_incl(r.m.s, q);
+      const int d0 = streams[handles[i * ndet]].det;
+      for (int d = warp - 1; d < ndet && d < kMaxDet; d += 2) {
+        const StreamDev &sd = streams[handles[i * ndet + d]];
+        const int dd = sd.det;
+        s_ds[lane][d] = sd.dscale;
+        s_ws[lane][d] = sd.wscale;
+        antenna_trig(dd, tr, r.det[d].fp, r.det[d].fc);
+        r.det[d].tau = -dtoa_trig(tr, d0, dd) * (2 * kPi);
+      }
     }
   }
   __syncthreads();
   const bool run = act && !s_bad[lane < kCoopReq ? lane : 0];
   const bool pv2 = run && r.approximant == kPhenomPv2;
-  // S1
+  // S1: the calibration fits in four slots, the half-warps of warps 0 and 3
+  if ((warp == 0 || warp == 3) && hact && !s_bad[hl])
+    model_d_lambdas_slot(s_r[hl].m, (warp == 3 ? 2 : 0) + (lane >= kCoopReq ? 1 : 0));
   if (run) {
-    if (warp == 0) model_d_lambdas_a(r.m);
-    if (warp == 3) model_d_lambdas_b(r.m);
     if (warp == 1) {
       if (pv2) model_p_setup(r.m, r.p, p);
-      else post_merger(r.m.s, qnm);
+      else if (r.m.s.dep_postmerger) post_merger(r.m.s, qnm);
+      else post_merger_qnm(r.m.s, qnm, s_pm[lane][0], s_pm[lane][1]);
     }
     if (warp == 2) model_d_pn(r.m);
   }

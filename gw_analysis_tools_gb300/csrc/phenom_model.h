@@ -394,6 +394,17 @@ GW_HD double final_spin(const Source &s) {
   double sgn = sqrt(1.0 * 1.0 / (af_parallel * af_parallel)) * af_parallel;  // copysign_internal (util.cpp:566)
   return sgn * sqrt(Sperp * Sperp + af_parallel * af_parallel);
 }
+// The QNM part of post_merger, with the final spin and radiated energy given.
+GW_HD void post_merger_qnm(Source &s, const double *qnm, double finspin, double Erad) {
+  const double *a = qnm, *yr = qnm + kQnmLen, *yd = qnm + 2 * kQnmLen, *cr = qnm + 3 * kQnmLen,
+               *cd = qnm + 4 * kQnmLen, *br = qnm + 5 * kQnmLen, *dr = qnm + 6 * kQnmLen,
+               *bd = qnm + 7 * kQnmLen, *dd = qnm + 8 * kQnmLen;
+  // both splines share the knots (spacing 0.002 inside, 0.001 at the ends)
+  const int ilo = cspline_locate_near_uniform(a, kQnmLen, finspin, 0.002);
+  const double sc = 1.0 / ((1.0 - Erad) * s.M);
+  s.fRD = cspline_eval_pre(a, yr, br, cr, dr, ilo, finspin) * sc;
+  s.fdamp = cspline_eval_pre(a, yd, bd, cd, dd, ilo, finspin) * sc;
+}
 GW_HD void post_merger(Source &s, const double *qnm) {  // IMRPhenomD.cpp:1091-1217
   if (s.dep_postmerger) {  // _calc_fring / _calc_fdamp (IMRPhenomD.cpp:1113-1176)
     double eta = s.eta, eta2 = eta * eta, eta3 = eta2 * eta, eta4 = eta3 * eta, M = s.M;
@@ -409,16 +420,7 @@ GW_HD void post_merger(Source &s, const double *qnm) {  // IMRPhenomD.cpp:1091-1
     s.fdamp = (1. / (2 * kPi)) * (MWdamp) / (M * (1. - E_rad));
     return;
   }
-  const double *a = qnm, *yr = qnm + kQnmLen, *yd = qnm + 2 * kQnmLen, *cr = qnm + 3 * kQnmLen,
-               *cd = qnm + 4 * kQnmLen, *br = qnm + 5 * kQnmLen, *dr = qnm + 6 * kQnmLen,
-               *bd = qnm + 7 * kQnmLen, *dd = qnm + 8 * kQnmLen;
-  double finspin = final_spin(s);
-  double Erad = EradRational0815(s.eta, s.spin1z, s.spin2z);
-  // both splines share the knots (spacing 0.002 inside, 0.001 at the ends)
-  const int ilo = cspline_locate_near_uniform(a, kQnmLen, finspin, 0.002);
-  const double sc = 1.0 / ((1.0 - Erad) * s.M);
-  s.fRD = cspline_eval_pre(a, yr, br, cr, dr, ilo, finspin) * sc;
-  s.fdamp = cspline_eval_pre(a, yd, bd, cd, dd, ilo, finspin) * sc;
+  post_merger_qnm(s, qnm, final_spin(s), EradRational0815(s.eta, s.spin1z, s.spin2z));
 }
 // The QNM table: knots a, fring and fdamp, the natural cubic spline
 // coefficients c of both, then their per-interval b and d (kQnmArrays arrays

@@ -317,6 +317,24 @@ GW_HD void model_d_lambdas(ModelD &m) {
   model_d_lambdas_a(m);
   model_d_lambdas_b(m);
 }
+// The same fits in kLambdaSlots interleaved slots (fit i in slot i % 4), for
+// slots running the same instructions on different lanes: slot 0 also clears
+// the entries no fit sets and fills the powers of pi.
+constexpr int kLambdaFits = 19, kLambdaSlots = 4;
+GW_HD void model_d_lambdas_slot(ModelD &m, int slot) {
+  const Source &s = m.s;
+  Lambda &l = m.l;
+  if (slot == 0) {
+    l.rho[3] = l.gamma[3] = l.sigma[0] = l.beta[0] = l.beta[4] = l.alpha[0] = l.alpha[6] = 0;
+    precalc_powers_PI(m.pi);
+  }
+  for (int i = slot; i < kLambdaFits; i += kLambdaSlots) {
+    const double v = lambda_elem(s, i);  // IMRPhenomD.cpp:833-852
+    double *dst = i < 3 ? &l.rho[i] : i == 3 ? &l.v2 : i < 7 ? &l.gamma[i - 4] : i < 11 ? &l.sigma[i - 6]
+                : i < 14 ? &l.beta[i - 10] : &l.alpha[i - 13];
+    *dst = v;
+  }
+}
 // needs the fits and post_merger
 GW_HD void model_d_freqs(ModelD &m) {
   Source &s = m.s;
