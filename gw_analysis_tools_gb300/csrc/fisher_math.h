@@ -25,6 +25,7 @@ struct FisherSrc {
   WaveF64 w0, wp[kIntr], wm[kIntr];
   double sp[kIntr], sm[kIntr];  // A_scale(+/-) / A_scale(centre)
   double div[kDim];
+  double idiv[kIntr];  // 1 / div[7 + q]
   double v[kDim];
   int logf[kDim];
   double G0re[kMaxDet], G0im[kMaxDet];
@@ -127,6 +128,7 @@ GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsil
     double tmp[kDim];
     F.div[i] = fisher_perturb(F.v, i, 1, eps, tmp);
   }
+  for (int q = 0; q < kIntr; q++) F.idiv[q] = 1.0 / F.div[7 + q];
   F.w0 = S[0].w;
   const double A0 = S[0].w.A_scale;
   for (int k = 0; k < kIntr; k++) {
@@ -187,17 +189,14 @@ GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsil
 // accumulated for weight stream w with weight wh (Simpson-weighted 1/S).
 GW_HD bool fisher_bin_q(const FisherSrc &F, int n, double t, double r, double lnn, double t34, double m76, float &a0,
                         float *qr, float *qi) {
-  double amp0, phi0;
-  wave64_eval(F.w0, n, t, r, lnn, t34, m76, amp0, phi0);
+  const double amp0 = wave64_amp(F.w0, n, t, m76);  // the centre's phase is not needed
   if (amp0 == 0.0) return false;
   a0 = (float)amp0;
   for (int q = 0; q < kIntr; q++) {
-    double ap, pp, am, pm;
-    wave64_eval(F.wp[q], n, t, r, lnn, t34, m76, ap, pp);
-    wave64_eval(F.wm[q], n, t, r, lnn, t34, m76, am, pm);
-    double inv = 1.0 / F.div[7 + q];
+    const double ap = wave64_amp(F.wp[q], n, t, m76), am = wave64_amp(F.wm[q], n, t, m76);
+    const double inv = F.idiv[q];
     double dA = (ap * F.sp[q] - am * F.sm[q]) * inv;
-    double dP = ((pp - F.wp[q].phic) - (pm - F.wm[q].phic)) * inv;
+    double dP = wave64_phase_diff(F.wp[q], F.wm[q], n, t, r, lnn, t34) * inv;
     qr[q] = (float)dA;  // q = dA - i A dPhi
     qi[q] = (float)(-amp0 * dP);
   }

@@ -193,13 +193,9 @@ GW_HDNI void wave64_prologue(const Request &r, double df, WaveF64 &x) {
 
 // FP64 amplitude / A_scale and nonlinear phase at bin n (tables: t = n^(1/3),
 // r = n^(-5/3), lnn = ln n, t34 = n^(3/4), m76 = n^(-7/6)).
-GW_HD void wave64_eval(const WaveF64 &x, int n, double t, double r, double lnn, double t34, double m76, double &amp,
-                       double &phi) {
-  if (n > x.n_cut) {
-    amp = 0.0;
-    phi = 0.0;
-    return;
-  }
+// Amplitude of bin n alone (0 beyond the cut).
+GW_HD double wave64_amp(const WaveF64 &x, int n, double t, double m76) {
+  if (n > x.n_cut) return 0.0;
   double a;
   if (n < x.n_f1) {
     a = x.ai[9];
@@ -211,17 +207,46 @@ GW_HD void wave64_eval(const WaveF64 &x, int n, double t, double r, double lnn, 
     double h = (double)(n - x.n_mid);
     a = (((x.ei[4] * h + x.ei[3]) * h + x.ei[2]) * h + x.ei[1]) * h + x.ei[0];
   }
-  amp = a * m76;
+  return a * m76;
+}
+// Phase of bin n alone (0 beyond the cut).
+GW_HD double wave64_phase(const WaveF64 &x, int n, double t, double r, double lnn, double t34) {
+  if (n > x.n_cut) return 0.0;
   double nd = (double)n;
   if (n < x.n_f1p) {
     double p = x.qi[11];
     for (int j = 10; j >= 0; j--) p = p * t + x.qi[j];
-    phi = r * p + lnn * (x.bi0 + x.bi1 * t);
-  } else if (n >= x.n_f2p) {
-    phi = x.mA + x.mB * nd - x.mC * (r * t * t) + x.mD * t34 + x.mE * atan((nd - x.nc) * x.inv_nw);
-  } else {
-    phi = x.pA + x.pB * nd + x.pC * lnn - x.pD * (r * r * t);
+    return r * p + lnn * (x.bi0 + x.bi1 * t);
   }
+  if (n >= x.n_f2p) return x.mA + x.mB * nd - x.mC * (r * t * t) + x.mD * t34 + x.mE * atan((nd - x.nc) * x.inv_nw);
+  return x.pA + x.pB * nd + x.pC * lnn - x.pD * (r * r * t);
+}
+GW_HD void wave64_eval(const WaveF64 &x, int n, double t, double r, double lnn, double t34, double m76, double &amp,
+                       double &phi) {
+  amp = wave64_amp(x, n, t, m76);
+  phi = wave64_phase(x, n, t, r, lnn, t34);
+}
+// (phase+ - phic+) - (phase- - phic-) of the waveforms of a central
+// difference at bin n.  Where both are in the ringdown region their atan terms
+// are combined, mE+ atan(y+) - mE- atan(y-) = mE+ atan((y+ - y-)/(1 + y+ y-))
+// + (mE+ - mE-) atan(y-): one FP64 atan instead of two, the first by its
+// series (argument below 1e-3: y+ and y- differ by the step).
+GW_HD double wave64_phase_diff(const WaveF64 &p, const WaveF64 &m, int n, double t, double r, double lnn,
+                               double t34) {
+  if (n >= p.n_f2p && n >= m.n_f2p && n <= p.n_cut && n <= m.n_cut) {
+    const double nd = (double)n;
+    const double yp = (nd - p.nc) * p.inv_nw, ym = (nd - m.nc) * m.inv_nw;
+    const double z = (yp - ym) / (1.0 + yp * ym);
+    if (fabs(z) < 1e-3) {
+      const double z2 = z * z;
+      const double datan = z * (1.0 - z2 * ((1.0 / 3.0) - z2 * 0.2));  // atan z to z^5
+      const double rtt = r * t * t;
+      const double bp = p.mA + p.mB * nd - p.mC * rtt + p.mD * t34;
+      const double bm = m.mA + m.mB * nd - m.mC * rtt + m.mD * t34;
+      return ((bp - p.phic) - (bm - m.phic)) + (p.mE * datan + (p.mE - m.mE) * atan(ym));
+    }
+  }
+  return (wave64_phase(p, n, t, r, lnn, t34) - p.phic) - (wave64_phase(m, n, t, r, lnn, t34) - m.phic);
 }
 
 GW_HD void split_f(double v, float &hi, float &lo) {
