@@ -21,11 +21,23 @@ struct SlotOut {
   int status;
 };
 
+// Coefficient differences of the waveforms of one central difference pair
+// (+ minus -): the phase polynomials, and the amplitude polynomials times
+// their scales relative to the centre (the intermediate one re-centred on the
+// centre waveform's n_mid).  Where both waveforms are in the same region at a
+// bin, their difference is one polynomial in FP64 instead of two.
+struct WaveDiff {
+  double qi[12], bi0, bi1, pA, pB, pC, pD, mA, mB, mC, mD, phic;
+  double ai[10], ei[5];
+};
+
 struct FisherSrc {
   WaveF64 w0, wp[kIntr], wm[kIntr];
   double sp[kIntr], sm[kIntr];  // A_scale(+/-) / A_scale(centre)
   double div[kDim];
   double idiv[kIntr];  // 1 / div[7 + q]
+  double amp_lk[kIntr];  // ln(K+ sp / (K- sm)) of the ringdown amplitudes of pair q
+  WaveDiff wd[kIntr];
   double v[kDim];
   int logf[kDim];
   double G0re[kMaxDet], G0im[kMaxDet];
@@ -118,6 +130,40 @@ GW_HDNI void fisher_slot(const GenParams &in, int slot, int method, const int *d
 }
 
 // Combine the slots of one source into the constants of the Gram sums.
+// Intermediate amplitude coefficients about n_mid re-centred on H (exact
+// binomial shift by the integer H - n_mid).
+GW_HD void recentre_ei(const WaveF64 &x, int H, double *e) {
+  const double sh = (double)(H - x.n_mid);
+  for (int k = 0; k < 5; k++) {
+    double acc = 0.0, binom = 1.0, pw = 1.0;  // C(j, k) sh^(j - k) for j = k..4
+    for (int j = k; j < 5; j++) {
+      acc += binom * x.ei[j] * pw;
+      binom = binom * (j + 1) / (j + 1 - k);
+      pw *= sh;
+    }
+    e[k] = acc;
+  }
+}
+GW_HD void wave_diff(const WaveF64 &p, const WaveF64 &m, double sp, double sm, int H, WaveDiff &d) {
+  for (int j = 0; j < 12; j++) d.qi[j] = p.qi[j] - m.qi[j];
+  d.bi0 = p.bi0 - m.bi0;
+  d.bi1 = p.bi1 - m.bi1;
+  d.pA = p.pA - m.pA;
+  d.pB = p.pB - m.pB;
+  d.pC = p.pC - m.pC;
+  d.pD = p.pD - m.pD;
+  d.mA = p.mA - m.mA;
+  d.mB = p.mB - m.mB;
+  d.mC = p.mC - m.mC;
+  d.mD = p.mD - m.mD;
+  d.phic = p.phic - m.phic;
+  for (int j = 0; j < 10; j++) d.ai[j] = p.ai[j] * sp - m.ai[j] * sm;
+  double ep[5], em[5];
+  recentre_ei(p, H, ep);
+  recentre_ei(m, H, em);
+  for (int j = 0; j < 5; j++) d.ei[j] = ep[j] * sp - em[j] * sm;
+}
+
 GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsilon, int step_mode, const SlotOut *S,
                          FisherSrc &F) {
   fisher_unpack(in, method, F.v, F.logf);
@@ -137,6 +183,8 @@ GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsil
     F.wm[k] = S[2 + 2 * i].w;
     F.sp[k] = F.wp[k].A_scale / A0;
     F.sm[k] = F.wm[k].A_scale / A0;
+    F.amp_lk[k] = log((F.wp[k].mrK * F.sp[k]) / (F.wm[k].mrK * F.sm[k]));
+    wave_diff(F.wp[k], F.wm[k], F.sp[k], F.sm[k], F.w0.n_mid, F.wd[k]);
   }
   for (int d = 0; d < ndet; d++) {
     double g0r = S[0].Gre[d], g0i = S[0].Gim[d];
@@ -185,6 +233,44 @@ GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsil
 }
 
 
+// A+ s+ - A- s- of pair q at bin n: one polynomial of coefficient
+// differences where both waveforms are in the same inspiral or intermediate
+// region, the ringdown form of wave64_amp_diff, each waveform on its own at
+// the bins between their region boundaries.
+GW_HD double fisher_amp_diff(const FisherSrc &F, int q, int n, double t, double m76) {
+  const WaveF64 &p = F.wp[q], &m = F.wm[q];
+  const WaveDiff &d = F.wd[q];
+  if (n <= p.n_cut && n <= m.n_cut) {
+    if (n < p.n_f1 && n < m.n_f1) {
+      double a = d.ai[9];
+      for (int j = 8; j >= 0; j--) a = a * t + d.ai[j];
+      return a * m76;
+    }
+    if (n >= p.n_f1 && n >= m.n_f1 && n < p.n_f3 && n < m.n_f3) {
+      const double h = (double)(n - F.w0.n_mid);
+      return ((((d.ei[4] * h + d.ei[3]) * h + d.ei[2]) * h + d.ei[1]) * h + d.ei[0]) * m76;
+    }
+  }
+  return wave64_amp_diff(p, m, n, t, m76, F.sp[q], F.sm[q], F.amp_lk[q]);
+}
+// (phase+ - phic+) - (phase- - phic-) of pair q at bin n, the same way.
+GW_HD double fisher_phase_diff(const FisherSrc &F, int q, int n, double t, double r, double lnn, double t34) {
+  const WaveF64 &p = F.wp[q], &m = F.wm[q];
+  const WaveDiff &d = F.wd[q];
+  if (n <= p.n_cut && n <= m.n_cut) {
+    if (n < p.n_f1p && n < m.n_f1p) {
+      double s = d.qi[11];
+      for (int j = 10; j >= 0; j--) s = s * t + d.qi[j];
+      return (r * s + lnn * (d.bi0 + d.bi1 * t)) - d.phic;
+    }
+    if (n >= p.n_f1p && n >= m.n_f1p && n < p.n_f2p && n < m.n_f2p) {
+      const double nd = (double)n;
+      return (d.pA + d.pB * nd + d.pC * lnn - d.pD * (r * r * t)) - d.phic;
+    }
+  }
+  return wave64_phase_diff(p, m, n, t, r, lnn, t34);
+}
+
 // One bin: the intrinsic amplitude/phase differences and the moment sums,
 // accumulated for weight stream w with weight wh (Simpson-weighted 1/S).
 GW_HD bool fisher_bin_q(const FisherSrc &F, int n, double t, double r, double lnn, double t34, double m76, float &a0,
@@ -193,10 +279,9 @@ GW_HD bool fisher_bin_q(const FisherSrc &F, int n, double t, double r, double ln
   if (amp0 == 0.0) return false;
   a0 = (float)amp0;
   for (int q = 0; q < kIntr; q++) {
-    const double ap = wave64_amp(F.wp[q], n, t, m76), am = wave64_amp(F.wm[q], n, t, m76);
     const double inv = F.idiv[q];
-    double dA = (ap * F.sp[q] - am * F.sm[q]) * inv;
-    double dP = wave64_phase_diff(F.wp[q], F.wm[q], n, t, r, lnn, t34) * inv;
+    double dA = fisher_amp_diff(F, q, n, t, m76) * inv;
+    double dP = fisher_phase_diff(F, q, n, t, r, lnn, t34) * inv;
     qr[q] = (float)dA;  // q = dA - i A dPhi
     qi[q] = (float)(-amp0 * dP);
   }

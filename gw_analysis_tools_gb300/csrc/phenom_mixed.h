@@ -226,6 +226,27 @@ GW_HD void wave64_eval(const WaveF64 &x, int n, double t, double r, double lnn, 
   amp = wave64_amp(x, n, t, m76);
   phi = wave64_phase(x, n, t, r, lnn, t34);
 }
+// A+ s+ - A- s- of the waveforms of a central difference at bin n (s: the
+// amplitude scales relative to the centre).  Where both are in the ringdown
+// amplitude region the difference is A- s- expm1(L) with L = ln(A+ s+ / (A- s-))
+// = lk - (e+ x+ - e- x-) + ln(d- / d+) assembled from small differences
+// (lk = ln(K+ s+ / (K- s-)) per source, x = n - n_rd, d = x^2 + G): one FP64
+// exp and one division instead of two.
+GW_HD double wave64_amp_diff(const WaveF64 &p, const WaveF64 &m, int n, double t, double m76, double sp, double sm,
+                             double lk) {
+  if (n >= p.n_f3 && n >= m.n_f3 && n <= p.n_cut && n <= m.n_cut) {
+    const double xm = (double)n - m.nrd, xp = (double)n - p.nrd;
+    const double dm = xm * xm + m.mrG2, dp = xp * xp + p.mrG2;
+    const double u = ((p.nrd - m.nrd) * (xm + xp) + (m.mrG2 - p.mrG2)) / dp;  // (d- - d+) / d+
+    const double L = lk - (p.mrExp * (m.nrd - p.nrd) + (p.mrExp - m.mrExp) * xm) +
+                     u * (1.0 - u * (0.5 - u * (1.0 / 3.0)));  // log1p(u) to u^3
+    if (fabs(u) < 1e-4 && fabs(L) < 1e-4) {
+      const double am = m.mrK * exp(-m.mrExp * xm) / dm * m76;
+      return am * sm * (L * (1.0 + L * (0.5 + L * (1.0 / 6.0))));  // expm1(L) to L^3
+    }
+  }
+  return wave64_amp(p, n, t, m76) * sp - wave64_amp(m, n, t, m76) * sm;
+}
 // (phase+ - phic+) - (phase- - phic-) of the waveforms of a central
 // difference at bin n.  Where both are in the ringdown region their atan terms
 // are combined, mE+ atan(y+) - mE- atan(y-) = mE+ atan((y+ - y-)/(1 + y+ y-))
