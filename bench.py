@@ -411,8 +411,10 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         t0 = time.perf_counter()
         fish, cov, fst = ctx.fisher_batch(pf, 0, hf, epsilon=1e-6, step_mode=1)
         dt = time.perf_counter() - t0
+        codes, counts = np.unique(fst, return_counts=True)
         ex["fisher"] = {"fishers_per_s": nf / dt, "sources": nf, "bins": int(ff.size), "seconds": dt,
-                        "ok": int((fst == 0).sum())}
+                        "ok": int((fst == 0).sum()),
+                        "status_counts": {str(int(c)): int(k) for c, k in zip(codes, counts)}}
         ex["_fisher_sample"] = (pf, fish[:4].copy(), ff, psd_f)
 
     def maximized():

@@ -59,6 +59,7 @@ struct FisherArgs {
   double wscale[kMaxDet];
   int n0, N, tile, ntiles;
   double df, fisher_df_ratio;  // (f1 - f0) / simpson_df
+  float df_f;                  // df in FP32 (the bins' frequency in the moment sums)
   gwt::Tables tab;
   const double *tm76d;
   int tm76d_n;              // tm76d valid for n <= tm76d_n
@@ -69,7 +70,7 @@ struct FisherArgs {
 };
 
 template <int NW>
-__global__ void __launch_bounds__(kBlock) k_fisher_main(const FisherArgs a) {
+__global__ void __launch_bounds__(kBlock, 3) k_fisher_main(const FisherArgs a) {
   __shared__ int s_item;
   __shared__ __align__(16) unsigned char s_buf[sizeof(FisherSrc)];
   __shared__ double s_red[32 * 8];
@@ -98,9 +99,10 @@ __global__ void __launch_bounds__(kBlock) k_fisher_main(const FisherArgs a) {
       for (int k = k0 + tid; k < k1; k += blockDim.x) {
         const int n = a.n0 + k;
         float a0, qr[kIntr], qi[kIntr];
-        if (!fisher_bin_q(F, n, a.tab.t13[n], a.tab.tm53[n], a.tab.tln[n], a.tab.t34[n], a.tm76d[n], a0, qr, qi))
+        if (!fisher_bin_q(F, n, a.tab.t13[n], a.tab.tm53[n], a.tab.tln[n], a.tab.t34[n], a.tm76d[n], a.tab.tm76f[n], a0,
+                          qr, qi))
           continue;
-        const float fk = (float)((double)n * a.df);
+        const float fk = (float)n * a.df_f;
 #pragma unroll
         for (int w = 0; w < NW; w++) fisher_accumulate(a.what[w][k], a0, fk, qr, qi, acc + w * kSums);
       }
@@ -422,6 +424,7 @@ int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, 
   a.tile = tile;
   a.ntiles = ntiles;
   a.df = df;
+  a.df_f = (float)df;
   a.fisher_df_ratio = (s0->host_freqs[1] - s0->host_freqs[0]) / s0->dev.simpson_df;
   a.tab = c->tables;
   a.tm76d = c->tm76d;

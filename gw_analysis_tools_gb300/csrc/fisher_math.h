@@ -144,24 +144,25 @@ GW_HD void recentre_ei(const WaveF64 &x, int H, double *e) {
     e[k] = acc;
   }
 }
-GW_HD void wave_diff(const WaveF64 &p, const WaveF64 &m, double sp, double sm, int H, WaveDiff &d) {
-  for (int j = 0; j < 12; j++) d.qi[j] = p.qi[j] - m.qi[j];
-  d.bi0 = p.bi0 - m.bi0;
-  d.bi1 = p.bi1 - m.bi1;
-  d.pA = p.pA - m.pA;
-  d.pB = p.pB - m.pB;
-  d.pC = p.pC - m.pC;
-  d.pD = p.pD - m.pD;
-  d.mA = p.mA - m.mA;
-  d.mB = p.mB - m.mB;
-  d.mC = p.mC - m.mC;
-  d.mD = p.mD - m.mD;
-  d.phic = p.phic - m.phic;
-  for (int j = 0; j < 10; j++) d.ai[j] = p.ai[j] * sp - m.ai[j] * sm;
+// The differences, times inv = 1 / (the difference's divisor).
+GW_HD void wave_diff(const WaveF64 &p, const WaveF64 &m, double sp, double sm, int H, double inv, WaveDiff &d) {
+  for (int j = 0; j < 12; j++) d.qi[j] = (p.qi[j] - m.qi[j]) * inv;
+  d.bi0 = (p.bi0 - m.bi0) * inv;
+  d.bi1 = (p.bi1 - m.bi1) * inv;
+  d.pA = (p.pA - m.pA) * inv;
+  d.pB = (p.pB - m.pB) * inv;
+  d.pC = (p.pC - m.pC) * inv;
+  d.pD = (p.pD - m.pD) * inv;
+  d.mA = (p.mA - m.mA) * inv;
+  d.mB = (p.mB - m.mB) * inv;
+  d.mC = (p.mC - m.mC) * inv;
+  d.mD = (p.mD - m.mD) * inv;
+  d.phic = (p.phic - m.phic) * inv;
+  for (int j = 0; j < 10; j++) d.ai[j] = (p.ai[j] * sp - m.ai[j] * sm) * inv;
   double ep[5], em[5];
   recentre_ei(p, H, ep);
   recentre_ei(m, H, em);
-  for (int j = 0; j < 5; j++) d.ei[j] = ep[j] * sp - em[j] * sm;
+  for (int j = 0; j < 5; j++) d.ei[j] = (ep[j] * sp - em[j] * sm) * inv;
 }
 
 GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsilon, int step_mode, const SlotOut *S,
@@ -184,7 +185,7 @@ GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsil
     F.sp[k] = F.wp[k].A_scale / A0;
     F.sm[k] = F.wm[k].A_scale / A0;
     F.amp_lk[k] = log((F.wp[k].mrK * F.sp[k]) / (F.wm[k].mrK * F.sm[k]));
-    wave_diff(F.wp[k], F.wm[k], F.sp[k], F.sm[k], F.w0.n_mid, F.wd[k]);
+    wave_diff(F.wp[k], F.wm[k], F.sp[k], F.sm[k], F.w0.n_mid, F.idiv[k], F.wd[k]);
   }
   for (int d = 0; d < ndet; d++) {
     double g0r = S[0].Gre[d], g0i = S[0].Gim[d];
@@ -233,28 +234,29 @@ GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsil
 }
 
 
-// A+ s+ - A- s- of pair q at bin n: one polynomial of coefficient
+// (A+ s+ - A- s-) / divisor of pair q at bin n (FP32 result; the amplitude
+// power m76 applied in FP32): one polynomial of coefficient
 // differences where both waveforms are in the same inspiral or intermediate
 // region, the ringdown form of wave64_amp_diff, each waveform on its own at
 // the bins between their region boundaries.
-GW_HD double fisher_amp_diff(const FisherSrc &F, int q, int n, double t, double m76) {
+GW_HD float fisher_amp_deriv(const FisherSrc &F, int q, int n, double t, double m76, float m76f) {
   const WaveF64 &p = F.wp[q], &m = F.wm[q];
   const WaveDiff &d = F.wd[q];
   if (n <= p.n_cut && n <= m.n_cut) {
     if (n < p.n_f1 && n < m.n_f1) {
       double a = d.ai[9];
       for (int j = 8; j >= 0; j--) a = a * t + d.ai[j];
-      return a * m76;
+      return (float)a * m76f;
     }
     if (n >= p.n_f1 && n >= m.n_f1 && n < p.n_f3 && n < m.n_f3) {
       const double h = (double)(n - F.w0.n_mid);
-      return ((((d.ei[4] * h + d.ei[3]) * h + d.ei[2]) * h + d.ei[1]) * h + d.ei[0]) * m76;
+      return (float)((((d.ei[4] * h + d.ei[3]) * h + d.ei[2]) * h + d.ei[1]) * h + d.ei[0]) * m76f;
     }
   }
-  return wave64_amp_diff(p, m, n, t, m76, F.sp[q], F.sm[q], F.amp_lk[q]);
+  return (float)(wave64_amp_diff(p, m, n, t, m76, F.sp[q], F.sm[q], F.amp_lk[q]) * F.idiv[q]);
 }
-// (phase+ - phic+) - (phase- - phic-) of pair q at bin n, the same way.
-GW_HD double fisher_phase_diff(const FisherSrc &F, int q, int n, double t, double r, double lnn, double t34) {
+// ((phase+ - phic+) - (phase- - phic-)) / divisor of pair q at bin n, the same way.
+GW_HD double fisher_phase_deriv(const FisherSrc &F, int q, int n, double t, double r, double lnn, double t34) {
   const WaveF64 &p = F.wp[q], &m = F.wm[q];
   const WaveDiff &d = F.wd[q];
   if (n <= p.n_cut && n <= m.n_cut) {
@@ -268,22 +270,19 @@ GW_HD double fisher_phase_diff(const FisherSrc &F, int q, int n, double t, doubl
       return (d.pA + d.pB * nd + d.pC * lnn - d.pD * (r * r * t)) - d.phic;
     }
   }
-  return wave64_phase_diff(p, m, n, t, r, lnn, t34);
+  return wave64_phase_diff(p, m, n, t, r, lnn, t34) * F.idiv[q];
 }
 
 // One bin: the intrinsic amplitude/phase differences and the moment sums,
 // accumulated for weight stream w with weight wh (Simpson-weighted 1/S).
-GW_HD bool fisher_bin_q(const FisherSrc &F, int n, double t, double r, double lnn, double t34, double m76, float &a0,
-                        float *qr, float *qi) {
+GW_HD bool fisher_bin_q(const FisherSrc &F, int n, double t, double r, double lnn, double t34, double m76,
+                        float m76f, float &a0, float *qr, float *qi) {
   const double amp0 = wave64_amp(F.w0, n, t, m76);  // the centre's phase is not needed
   if (amp0 == 0.0) return false;
   a0 = (float)amp0;
   for (int q = 0; q < kIntr; q++) {
-    const double inv = F.idiv[q];
-    double dA = fisher_amp_diff(F, q, n, t, m76) * inv;
-    double dP = fisher_phase_diff(F, q, n, t, r, lnn, t34) * inv;
-    qr[q] = (float)dA;  // q = dA - i A dPhi
-    qi[q] = (float)(-amp0 * dP);
+    qr[q] = fisher_amp_deriv(F, q, n, t, m76, m76f);  // q = dA - i A dPhi
+    qi[q] = (float)(-amp0 * fisher_phase_deriv(F, q, n, t, r, lnn, t34));
   }
   return true;
 }

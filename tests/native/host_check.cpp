@@ -220,8 +220,9 @@ extern "C" int gwh_fisher_batch(const GenParams *p, int method, const double *fr
       int n = n0 + k;
       double x = n;
       float a0, qr[kIntr], qi[kIntr];
-      if (!fisher_bin_q(F, n, std::cbrt(x), std::pow(x, -5. / 3.), std::log(x), std::pow(x, 0.75),
-                        std::pow(x, -7. / 6.), a0, qr, qi))
+      const double m76 = std::pow(x, -7. / 6.);
+      if (!fisher_bin_q(F, n, std::cbrt(x), std::pow(x, -5. / 3.), std::log(x), std::pow(x, 0.75), m76,
+                        (float)m76, a0, qr, qi))
         continue;
       double sw = (k == 0 || k == N - 1) ? 1.0 : ((k & 1) ? 4.0 : 2.0);
       float wh = (float)(4. * sdf / 3. * sw / psd[d][k] / wmax);
