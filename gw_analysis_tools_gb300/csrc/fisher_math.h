@@ -269,6 +269,17 @@ GW_HD double fisher_phase_deriv(const FisherSrc &F, int q, int n, double t, doub
       const double nd = (double)n;
       return (d.pA + d.pB * nd + d.pC * lnn - d.pD * (r * r * t)) - d.phic;
     }
+    if (n >= p.n_f2p && n >= m.n_f2p) {  // ringdown: the atan pair as in wave64_phase_diff
+      const double nd = (double)n;
+      const double yp = (nd - p.nc) * p.inv_nw, ym = (nd - m.nc) * m.inv_nw;
+      const double z = (yp - ym) / (1.0 + yp * ym);
+      if (fabs(z) < 1e-3) {
+        const double z2 = z * z;
+        const double datan = z * (1.0 - z2 * ((1.0 / 3.0) - z2 * 0.2));  // atan z to z^5
+        return (d.mA + d.mB * nd - d.mC * (r * t * t) + d.mD * t34 - d.phic) +
+               (p.mE * datan + (p.mE - m.mE) * atan(ym)) * F.idiv[q];
+      }
+    }
   }
   return wave64_phase_diff(p, m, n, t, r, lnn, t34) * F.idiv[q];
 }
