@@ -14,7 +14,7 @@ layout:
     gw_analysis_tools_gb300/csrc/phenom_tables.h (used by the CUDA path)
 
 Run it only where the reference sources are present:
-    python oracle/gen_tables.py /root/reference
+    GWAT_REFERENCE_DIR=<reference checkout> python oracle/gen_tables.py
 The generated headers are committed; nothing at build or run time reads the
 reference.
 """
@@ -123,4 +123,4 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ["GWAT_REFERENCE_DIR"])

@@ -1042,8 +1042,75 @@ static void project(const double complex *hp, const double complex *hc, int leng
   for (int i = 0; i < length; i++) r[i] = cscale(hp[i], fp) + cscale(hc[i], fc);
 }
 
+/* terr_pol_iota_from_equat_sph (util.cpp:1362-1378): polarisation and
+ * inclination of a direction (thetaj, phij) seen from the sky position. */
+static void terr_pol_iota(double RA, double DEC, double thetaj, double phij, double *pol, double *iota) {
+  double t = atan(cos(DEC) * 1. / tan(thetaj) * 1. / sin(phij - RA) - 1. / tan(phij - RA) * sin(DEC));
+  *pol = GWO_PI / 2. - t;
+  *iota = acos(-(cos(thetaj) * sin(DEC)) - cos(DEC) * cos(phij - RA) * sin(thetaj));
+}
+
+/* equatorial_from_SF (util.cpp:1440-1485): a source-frame vector (L along z)
+ * rotated to equatorial Cartesian coordinates. */
+static void equatorial_from_sf(const double *v, double thetal, double phil, double thetas, double phis, double iota,
+                               double phi_ref, double *out) {
+  double cp = cos(GWO_PI / 2. - phi_ref), sp = sin(GWO_PI / 2. - phi_ref);
+  double ci = cos(iota), si = sin(iota);
+  double ctl = cos(thetal), stl = sin(thetal), cts = cos(thetas), sts = sin(thetas);
+  double cps = cos(phis), sps = sin(phis), cpl = cos(phil), spl = sin(phil);
+  double jx = v[0], jy = v[1], jz = v[2];
+  out[0] = (pow_int(cp, 2) * cpl * jz * si * stl - ci * cpl * (cp * jx + jy * sp) * stl -
+            cp * (cts * jy * spl * stl + cps * jx * sts - ctl * jy * sps * sts) +
+            sp * (cpl * jz * si * sp * stl + cts * jx * spl * stl - (cps * jy + ctl * jx * sps) * sts)) / si;
+  out[1] = (pow_int(cp, 2) * jz * si * spl * stl +
+            sp * (-(cpl * cts * jx * stl) - ci * jy * spl * stl + jz * si * sp * spl * stl + cps * ctl * jx * sts -
+                  jy * sps * sts) +
+            cp * (cpl * cts * jy * stl - ci * jx * spl * stl - (cps * ctl * jy + jx * sps) * sts)) / si;
+  out[2] = (ctl * jz * si - jx * (ci * cp * ctl + cp * cts + sp * (cps * spl - cpl * sps) * stl * sts) -
+            jy * (ci * ctl * sp + cts * sp + cp * (-(cps * spl) + cpl * sps) * stl * sts)) / si;
+}
+
+/* transform_orientation_coords (waveform_util.cpp:1523-1586), ground-detector
+ * branch: the inclination and polarisation from the equatorial direction
+ * (theta_l, phi_l) of the orbital angular momentum.  IMRPhenomD: both from
+ * terr_pol_iota_from_equat_sph of L.  IMRPhenomPv2: the inclination is the
+ * angle between N and L; the polarisation is that of the total angular
+ * momentum J, its source-frame direction from PhenomPv2_JSF_from_params
+ * (IMRPhenomP.cpp:776-816) rotated to equatorial coordinates. */
+void gwo_transform_orientation_coords(gwo_gen_params *p, int approximant) {
+  double theta_s = GWO_PI / 2. - p->DEC, phi_s = p->RA;
+  double N[3] = {-sin(theta_s) * cos(phi_s), -sin(theta_s) * sin(phi_s), -cos(theta_s)};
+  double L[3] = {sin(p->theta_l) * cos(p->phi_l), sin(p->theta_l) * sin(p->phi_l), cos(p->theta_l)};
+  p->incl_angle = acos(N[0] * L[0] + N[1] * L[1] + N[2] * L[2]);
+  if (approximant != GWO_IMRPHENOMPV2) {
+    terr_pol_iota(p->RA, p->DEC, p->theta_l, p->phi_l, &p->psi, &p->incl_angle);
+    return;
+  }
+  double chi1_l = p->spin1[2], chi2_l = p->spin2[2];
+  double eta = calc_eta(p->mass1, p->mass2);
+  double m1_2 = p->mass1 * p->mass1, m2_2 = p->mass2 * p->mass2;
+  pows_t pw;
+  memset(&pw, 0, sizeof(pw));
+  precalc_powers_PI(&pw);
+  precalc_powers_ins(p->f_ref, (p->mass1 + p->mass2) * GWO_MSOL_SEC, &pw);
+  double L0 = pow_int(p->mass1 + p->mass2, 2) * L2PN(eta, &pw);
+  double jx = m1_2 * p->chip * cos(p->phip), jy = m1_2 * p->chip * sin(p->phip);
+  double jz = L0 + m1_2 * chi1_l + m2_2 * chi2_l;
+  double j0 = sqrt(jx * jx + jy * jy + jz * jz);
+  double jsf[3] = {jx / j0, jy / j0, jz / j0}, jeq[3];
+  equatorial_from_sf(jsf, p->theta_l, p->phi_l, theta_s, phi_s, p->incl_angle, p->phiRef, jeq);
+  double r = sqrt(jeq[0] * jeq[0] + jeq[2] * jeq[2] + jeq[1] * jeq[1]); /* transform_cart_sph, util.cpp:1882-1891 */
+  double theta_j = acos(jeq[2] / r), phi_j = atan2(jeq[1], jeq[0]);
+  if (phi_j < 0) phi_j += 2 * GWO_PI;
+  double iota_j;
+  terr_pol_iota(p->RA, p->DEC, theta_j, phi_j, &p->psi, &iota_j);
+}
+
 int gwo_fourier_detector_response(const double *freqs, int length, double *response, int det, int approximant,
-                                  const gwo_gen_params *p) {
+                                  const gwo_gen_params *p_in) {
+  gwo_gen_params pc = *p_in;
+  const gwo_gen_params *p = &pc;
+  if (pc.equatorial_orientation) gwo_transform_orientation_coords(&pc, approximant); /* waveform_util.cpp:946-948 */
   double complex *hp = (double complex *)malloc(sizeof(double complex) * (size_t)(length > 0 ? length : 1) * 2);
   double complex *hc = hp + length;
   int st = gwo_fourier_waveform(freqs, length, (double *)hp, (double *)hc, approximant, p);

@@ -32,6 +32,10 @@ typedef struct {
   double RA, DEC, psi, gmst;
   double chip, phip;          /* reduced Pv2 spins; chip = -1 selects the full transform */
   int shift_time, shift_phase, sky_average, dep_postmerger;
+  /* equatorial spherical angles of the orbital angular momentum, read when
+   * equatorial_orientation is set (util.h:166-172) */
+  double theta_l, phi_l;
+  int equatorial_orientation, pad_;
 } gwo_gen_params;
 
 void gwo_default_params(gwo_gen_params *p);
@@ -50,8 +54,14 @@ void gwo_antenna(int det, double ra, double dec, double psi, double gmst, double
 /* DTOA_DETECTOR (detector_util.cpp:677-790). */
 double gwo_dtoa(double ra, double dec, double gmst, int det1, int det2);
 
-/* fourier_detector_response, equatorial, no orientation transform
- * (waveform_util.cpp:1070-1088 -> :936-985 -> :725-905). */
+/* transform_orientation_coords (waveform_util.cpp:1523-1586) for a ground
+ * detector: incl_angle and psi from theta_l, phi_l (and, for IMRPhenomPv2, the
+ * total angular momentum from chip, phip and the aligned spins). */
+void gwo_transform_orientation_coords(gwo_gen_params *p, int approximant);
+
+/* fourier_detector_response, equatorial (waveform_util.cpp:1070-1088 ->
+ * :936-985 -> :725-905); with equatorial_orientation set, the orientation
+ * transform is applied to a copy of p first. */
 int gwo_fourier_detector_response(const double *freqs, int length, double *response, int det,
                                   int approximant, const gwo_gen_params *p);
 

@@ -33,6 +33,8 @@ class GenParams(ctypes.Structure):
         ("chip", ctypes.c_double), ("phip", ctypes.c_double),
         ("shift_time", ctypes.c_int), ("shift_phase", ctypes.c_int),
         ("sky_average", ctypes.c_int), ("dep_postmerger", ctypes.c_int),
+        ("theta_l", ctypes.c_double), ("phi_l", ctypes.c_double),
+        ("equatorial_orientation", ctypes.c_int), ("pad_", ctypes.c_int),
     ]
 
 
@@ -58,11 +60,25 @@ _lib = None
 _ref = None
 
 
+def reference_dir():
+    """The reference checkout: GWAT_REFERENCE_DIR, else the one the pin
+    libraries were last built from (oracle/_ref/source_dir.txt); None where
+    neither exists on this machine."""
+    d = os.environ.get("GWAT_REFERENCE_DIR")
+    if not d:
+        rec = os.path.join(HERE, "_ref", "source_dir.txt")
+        d = open(rec).read().strip() if os.path.exists(rec) else None
+    return d if d and os.path.isdir(os.path.join(d, "src")) else None
+
+
 def build(ref_dir=None):
-    """Compile liboracle.so (and the reference pin library if ref_dir exists)."""
+    """Compile liboracle.so (and the reference pin libraries if ref_dir exists)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
     if ref_dir and os.path.isdir(os.path.join(ref_dir, "src")):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + ref_dir])
+        jobs = "-j%d" % max(1, min(16, os.cpu_count() or 1))
+        subprocess.check_call(["make", "-s", "-C", HERE, jobs, "ref", "full", "REF=" + ref_dir])
+        with open(os.path.join(HERE, "_ref", "source_dir.txt"), "w") as fh:
+            fh.write(os.path.abspath(ref_dir) + "\n")
 
 
 def lib():
@@ -103,6 +119,7 @@ def lib():
                                        ctypes.POINTER(dp), ctypes.c_double, ctypes.c_int, dp, ctypes.c_int]
         L.gwo_cholesky_invert.argtypes = [dp, dp, ctypes.c_int]
         L.gwo_cholesky_invert.restype = ctypes.c_int
+        L.gwo_transform_orientation_coords.argtypes = [gp, ctypes.c_int]
         L.gwo_analytic_psd.argtypes = [ctypes.c_double]
         L.gwo_analytic_psd.restype = ctypes.c_double
         L.gwo_cspline_coeffs.argtypes = [dp, dp, ctypes.c_int, dp]
@@ -124,6 +141,180 @@ def ref_lib():
         L.ref_fourier_waveform.argtypes = [dp, ctypes.c_int, dp, dp, ctypes.c_int, ctypes.POINTER(GenParams)]
         _ref = L
     return _ref
+
+
+_ref_full = None
+
+
+def ref_full_lib():
+    """The reference's own glue (oracle/_ref/libgwatref_full.so), or None where
+    it was not built."""
+    global _ref_full
+    if _ref_full is None:
+        path = os.path.join(HERE, "_ref", "libgwatref_full.so")
+        if not os.path.exists(path):
+            return None
+        L = ctypes.CDLL(path)
+        dp = ctypes.POINTER(ctypes.c_double)
+        pdp = ctypes.POINTER(dp)
+        ip = ctypes.POINTER(ctypes.c_int)
+        gp = ctypes.POINTER(GenParams)
+        cpp = ctypes.POINTER(ctypes.c_char_p)
+        c, d, i = ctypes.c_char_p, ctypes.c_double, ctypes.c_int
+        L.gwr_fourier_waveform.argtypes = [dp, i, dp, dp, c, gp]
+        L.gwr_fourier_detector_response.argtypes = [dp, i, dp, c, c, gp, gp]
+        L.gwr_transform_orientation_coords.argtypes = [gp, c, c, gp]
+        L.gwr_antenna.argtypes = [c, d, d, d, d, dp, dp]
+        L.gwr_dtoa.argtypes = [d, d, d, c, c]
+        L.gwr_dtoa.restype = d
+        L.gwr_log_likelihood_internal.argtypes = [dp, dp, dp, dp, dp, i, i, c]
+        L.gwr_log_likelihood_internal.restype = d
+        L.gwr_mcmc_likelihood_extrinsic.argtypes = [gp, c, ip, pdp, pdp, pdp, pdp, c, i, cpp, i, dp, dp]
+        L.gwr_mcmc_likelihood_extrinsic.restype = d
+        L.gwr_fisher_numerical.argtypes = [dp, i, c, c, c, dp, i, gp, i, dp]
+        L.gwr_maximized_aligned.argtypes = [dp, dp, dp, dp, i]
+        L.gwr_maximized_aligned.restype = d
+        L.gwr_maximized_unaligned.argtypes = [dp, dp, dp, dp, dp, i]
+        L.gwr_maximized_unaligned.restype = d
+        L.gwr_gps_to_gmst_radian.argtypes = [d]
+        L.gwr_gps_to_gmst_radian.restype = d
+        L.gwr_sampler_eval.argtypes = [c, i, i, cpp, pdp, pdp, pdp, ip, d, i, dp, dp, dp, i]
+        L.gwr_sampler_eval.restype = d
+        _ref_full = L
+    return _ref_full
+
+
+APPROX_NAMES = {IMRPhenomD: "IMRPhenomD", IMRPhenomPv2: "IMRPhenomPv2"}
+
+
+def _cstrs(names):
+    return (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+
+
+def ref_fourier_waveform(freqs, params, method="IMRPhenomD"):
+    """The reference's fourier_waveform (waveform_generator.cpp:104)."""
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    hp = np.zeros(freqs.size, dtype=np.complex128)
+    hc = np.zeros(freqs.size, dtype=np.complex128)
+    ref_full_lib().gwr_fourier_waveform(_dp(freqs), freqs.size, _dp(hp), _dp(hc), method.encode(),
+                                        ctypes.byref(params))
+    return hp, hc
+
+
+def ref_detector_response(freqs, params, detector, method="IMRPhenomD"):
+    """The reference's fourier_detector_response (waveform_util.cpp:1070);
+    returns the response and the parameters as the call left them."""
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    r = np.zeros(freqs.size, dtype=np.complex128)
+    after = GenParams()
+    ref_full_lib().gwr_fourier_detector_response(_dp(freqs), freqs.size, _dp(r), detector.encode(), method.encode(),
+                                                 ctypes.byref(params), ctypes.byref(after))
+    return r, after
+
+
+def ref_transform_orientation_coords(params, method="IMRPhenomD", detector="Hanford"):
+    out = GenParams()
+    ref_full_lib().gwr_transform_orientation_coords(ctypes.byref(params), method.encode(), detector.encode(),
+                                                    ctypes.byref(out))
+    return out
+
+
+def ref_antenna(detector, ra, dec, psi, gmst):
+    fp, fc = ctypes.c_double(), ctypes.c_double()
+    ref_full_lib().gwr_antenna(detector.encode(), ra, dec, psi, gmst, ctypes.byref(fp), ctypes.byref(fc))
+    return fp.value, fc.value
+
+
+def ref_dtoa(ra, dec, gmst, det1, det2):
+    return ref_full_lib().gwr_dtoa(ra, dec, gmst, det1.encode(), det2.encode())
+
+
+def ref_log_likelihood_internal(data, psd, freqs, response, weights=None, log10F=False):
+    data = np.ascontiguousarray(data, dtype=np.complex128)
+    psd = np.ascontiguousarray(psd, dtype=np.float64)
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    response = np.ascontiguousarray(response, dtype=np.complex128)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    return ref_full_lib().gwr_log_likelihood_internal(_dp(data), _dp(psd), _dp(freqs),
+                                                      None if w is None else _dp(w), _dp(response), freqs.size,
+                                                      int(log10F), b"SIMPSONS" if w is None else b"GAUSSLEG")
+
+
+def ref_mcmc_likelihood_extrinsic(params, freqs, detectors, data, psd, method="IMRPhenomD", weights=None,
+                                  log10F=False):
+    """The reference's MCMC_likelihood_extrinsic (mcmc_gw.cpp:2374) with every
+    detector on the grid freqs.  The detectors' frequency arrays are copies laid
+    out back to back, so the T the reference forms from frequencies[1] -
+    frequencies[0] (a pointer difference, mcmc_gw.cpp:2466) is 1/len(freqs).
+    Returns (log L, T used, t_c as the call left it)."""
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    n, nd = freqs.size, len(detectors)
+    block = np.ascontiguousarray(np.tile(freqs, nd))
+    fptrs = (ctypes.POINTER(ctypes.c_double) * nd)(
+        *[ctypes.cast(block.ctypes.data + 8 * n * k, ctypes.POINTER(ctypes.c_double)) for k in range(nd)])
+    data = [np.ascontiguousarray(x, dtype=np.complex128) for x in data]
+    psd = [np.ascontiguousarray(x, dtype=np.float64) for x in psd]
+    ws = [None] * nd if weights is None else [np.ascontiguousarray(x, dtype=np.float64) for x in weights]
+    wptr = (ctypes.POINTER(ctypes.c_double) * nd)(*[None if w is None else _dp(w) for w in ws])
+    lengths = (ctypes.c_int * nd)(*([n] * nd))
+    T, tc = ctypes.c_double(), ctypes.c_double()
+    ll = ref_full_lib().gwr_mcmc_likelihood_extrinsic(
+        ctypes.byref(params), method.encode(), lengths, fptrs, _ptr_array(data), _ptr_array(psd), wptr,
+        b"SIMPSONS" if weights is None else b"GAUSSLEG", int(log10F), _cstrs(detectors), nd, ctypes.byref(T),
+        ctypes.byref(tc))
+    return ll, T.value, tc.value
+
+
+def ref_fisher_numerical(freqs, params, detector, ref_detector, psd, method="IMRPhenomD", order=2, dim=11):
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    psd = np.ascontiguousarray(psd, dtype=np.float64)
+    out = np.zeros(dim * dim)
+    ref_full_lib().gwr_fisher_numerical(_dp(freqs), freqs.size, method.encode(), detector.encode(),
+                                        ref_detector.encode(), _dp(out), dim, ctypes.byref(params), order, _dp(psd))
+    return out.reshape(dim, dim)
+
+
+def ref_maximized_loglik(data, psd, freqs, hplus, hcross=None):
+    """The reference's maximised likelihoods (mcmc_gw.cpp:595-800), its FFTW
+    calls answered by a direct DFT (oracle/ref_fftw.cpp)."""
+    data = np.ascontiguousarray(data, dtype=np.complex128)
+    psd = np.ascontiguousarray(psd, dtype=np.float64)
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    hp = np.ascontiguousarray(hplus, dtype=np.complex128)
+    L = ref_full_lib()
+    if hcross is None:
+        return L.gwr_maximized_aligned(_dp(data), _dp(psd), _dp(freqs), _dp(hp), freqs.size)
+    hc = np.ascontiguousarray(hcross, dtype=np.complex128)
+    return L.gwr_maximized_unaligned(_dp(data), _dp(psd), _dp(freqs), _dp(hp), _dp(hc), freqs.size)
+
+
+def ref_gps_to_gmst(gps):
+    return ref_full_lib().gwr_gps_to_gmst_radian(gps)
+
+
+def ref_sampler_eval(method, positions, freqs, detectors, data, psd, gps_time, fisher=False, nthreads=1):
+    """MCMC_likelihood_wrapper (and MCMC_fisher_wrapper) of the reference at
+    each row of positions, after the reference's own sampler set-up
+    (PTMCMC_MH_dynamic_PT_alloc_uncorrelated_GW, mcmc_gw.cpp:1422) with the
+    detectors' frequency arrays laid out back to back (so the T of
+    mcmc_gw.cpp:2466 is 1/len(freqs)).  Returns (log L, Fisher or None,
+    seconds)."""
+    positions = np.ascontiguousarray(positions, dtype=np.float64)
+    npos, dim = positions.shape
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    n, nd = freqs.size, len(detectors)
+    block = np.ascontiguousarray(np.tile(freqs, nd))
+    fptrs = (ctypes.POINTER(ctypes.c_double) * nd)(
+        *[ctypes.cast(block.ctypes.data + 8 * n * k, ctypes.POINTER(ctypes.c_double)) for k in range(nd)])
+    data = [np.ascontiguousarray(x, dtype=np.complex128) for x in data]
+    psd = [np.ascontiguousarray(x, dtype=np.float64) for x in psd]
+    lengths = (ctypes.c_int * nd)(*([n] * nd))
+    ll = np.zeros(npos)
+    fo = np.zeros(npos * dim * dim) if fisher else None
+    secs = ref_full_lib().gwr_sampler_eval(method.encode(), dim, nd, _cstrs(detectors), fptrs, _ptr_array(data),
+                                           _ptr_array(psd), lengths, gps_time, npos, _dp(positions), _dp(ll),
+                                           None if fo is None else _dp(fo), nthreads)
+    return ll, (None if fo is None else fo.reshape(npos, dim, dim)), secs
 
 
 def _dp(a):
@@ -151,6 +342,15 @@ def detector_response(freqs, params, detector, approximant=IMRPhenomD):
     lib().gwo_fourier_detector_response(_dp(freqs), freqs.size, _dp(r), detector_index(detector), approximant,
                                         ctypes.byref(params))
     return r
+
+
+def transform_orientation_coords(params, approximant=IMRPhenomD):
+    """A copy of params with incl_angle and psi from theta_l, phi_l
+    (transform_orientation_coords, waveform_util.cpp:1523-1586)."""
+    out = GenParams()
+    ctypes.pointer(out)[0] = params
+    lib().gwo_transform_orientation_coords(ctypes.byref(out), approximant)
+    return out
 
 
 def antenna(detector, ra, dec, psi, gmst):

@@ -1,7 +1,14 @@
 #ifndef GWO_SHIM_DRIVERS_H
 #define GWO_SHIM_DRIVERS_H
+/* Test-only ADOL-C driver stand-ins (the autodiff Fisher is off the pinned
+ * path; these are never executed on the double path). */
 #include "../taping.h"
 inline int gradient(short, int, const double *, double *) { return -1; }
 inline int jacobian(short, int, int, const double *, double **) { return -1; }
 inline int hessian(short, int, double *, double **) { return -1; }
+inline int binomi(int, int) { return 1; }
+inline int tensor_eval(short, int, int, int, int, double *, double **, double **) { return -1; }
+inline int tensor_address(int, int *) { return 0; }
+inline double **myalloc2(int m, int n) { double **a = new double *[m]; for (int i = 0; i < m; i++) a[i] = new double[n]; return a; }
+inline void myfree2(double **) {}
 #endif

@@ -16,7 +16,7 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def oracle():
     import oracle as O
-    O.build(os.environ.get("GWAT_REFERENCE_DIR") if os.environ.get("GWAT_REFERENCE_DIR") else None)
+    O.build(O.reference_dir())
     return O
 
 

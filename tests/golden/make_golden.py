@@ -6,7 +6,7 @@ the reference sources against test-only shim headers (oracle/Makefile target
 stores a subsample of the bins.  The committed fixture lets the oracle be
 checked where the reference sources are absent.
 
-    python tests/golden/make_golden.py /root/reference
+    GWAT_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 """
 import os
 import sys
@@ -56,4 +56,4 @@ def main(ref_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ["GWAT_REFERENCE_DIR"])

@@ -9,7 +9,19 @@ import pytest
 
 import gw_analysis_tools_gb300 as G
 
-REFERENCE_NOISE_DIR = "/root/reference/data/noise_data/currently_supported"
+def _reference_noise_dir():
+    """The reference's tabulated noise curves, where its checkout is known
+    (GWAT_REFERENCE_DIR, or the checkout the oracle's pin libraries were built
+    from)."""
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(os.path.dirname(here), "oracle"))
+    import oracle
+    d = oracle.reference_dir()
+    return os.path.join(d, "data", "noise_data", "currently_supported") if d else ""
+
+
+REFERENCE_NOISE_DIR = _reference_noise_dir()
 
 
 @pytest.fixture(scope="module")
