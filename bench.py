@@ -358,6 +358,8 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         ex["served"] = {"evals_per_s": nserve / wall, "p50_ms": s["p50_s"] * 1e3, "p99_ms": s["p99_s"] * 1e3,
                         "offered_rate": 2e5, "requests": nserve, "launches": s["launches"], "ensembles": ens,
                         "ok": int((st == 0).sum())}
+        pick = np.arange(0, nserve, 29)  # a parity sample, both approximants
+        ex["_parity_served"] = ([sp[i] for i in pick], [sa[i] for i in pick], out[pick].copy())
         # the same mix offered faster than the engine serves it: its capacity
         nsat = 200000
         ds = W.prior_draws(nsat // 2, 503)
@@ -380,12 +382,13 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
     def uneven():
         # uneven Pv2 batch: T in {4, 8, 32, 128}, 20-2048 Hz, 1024 requests, one launch
         Ts = W.uneven_durations(1024, 9)
-        hmap = {}
+        hmap, udata = {}, {}
         for Tu in (4, 8, 32, 128):
             fu = W.uniform_grid(20.0, 2048.0, 1.0 / Tu)
             psd_u = W.analytic_psd(fu)
-            hmap[Tu] = [ctx.register_data(d, fu, W.noise(fu, 900 + Tu + i), psd_u)
-                        for i, d in enumerate(W.DETECTORS3)]
+            udata[Tu] = [uneven_injection(ctx, G, fu, Tu, d) + W.noise(fu, 900 + Tu + i)
+                         for i, d in enumerate(W.DETECTORS3)]
+            hmap[Tu] = [ctx.register_data(d, fu, udata[Tu][i], psd_u) for i, d in enumerate(W.DETECTORS3)]
         # T_segment = 0: each request uses 1/df of its own grid
         pu = W.prior_draws(1024, 11, precessing=True)
         hs = np.array([hmap[int(t)] for t in Ts], dtype=np.int32)
@@ -398,7 +401,10 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
             _, st = ctx.loglik_batch(parr, 1, hs, 0.0, G.PREC_MIXED)
         dt = (time.perf_counter() - t0) / reps
         ex["uneven_pv2"] = {"evals_per_s": 1024 / dt, "ms_per_launch": dt * 1e3, "bins_per_launch": bins,
-                            "grid_bins": sorted(set(int(2028 * t) for t in Ts)), "ok": int((st == 0).sum())}
+                            "grid_bins": sorted(set(int(2028 * t) for t in Ts)), "ok": int((st == 0).sum()),
+                            "data": "Pv2 injection (SNR ~ 50 on the 128 s grid) + seeded noise per grid"}
+        out_u, _ = ctx.loglik_batch(parr, 1, hs, 0.0, G.PREC_MIXED)
+        ex["_parity_uneven"] = (pu, [int(t) for t in Ts], udata, out_u.copy())
 
     def fisher():
         # batched Fisher: IMRPhenomD 3 detectors, 10-2048 Hz at df=1/16, step 1e-6 relative
@@ -414,8 +420,26 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         codes, counts = np.unique(fst, return_counts=True)
         ex["fisher"] = {"fishers_per_s": nf / dt, "sources": nf, "bins": int(ff.size), "seconds": dt,
                         "ok": int((fst == 0).sum()),
-                        "status_counts": {str(int(c)): int(k) for c, k in zip(codes, counts)}}
-        ex["_fisher_sample"] = (pf, fish[:4].copy(), ff, psd_f)
+                        "status_counts": {str(int(c)): int(k) for c, k in zip(codes, counts)},
+                        "form": "moment sums (FP64 waveform differences, FP32-compensated Gram), order 2; "
+                                "sources it cannot invert redone by the FP64 reference algorithm"}
+        # the reference algorithm in FP64 (orders 2 and 4) and the sampler's proposal
+        nr = 2048
+        pr = G.params_array(W.prior_draws(nr, 13))
+        for order in (2, 4):
+            ctx.fisher_batch_ex(G.params_array(W.prior_draws(64, 14)), 0, hf, order=order, epsilon=1e-6, step_mode=1)
+            t0 = time.perf_counter()
+            ctx.fisher_batch_ex(pr, 0, hf, order=order, epsilon=1e-6, step_mode=1)
+            ex["fisher"]["reference_algorithm_order%d_per_s" % order] = nr / (time.perf_counter() - t0)
+        theta = mcmc_theta(W.prior_draws(nr, 15))
+        ctx.mcmc_fisher_batch(theta[:64], hf, W.GMST)
+        t0 = time.perf_counter()
+        ctx.mcmc_fisher_batch(theta, hf, W.GMST)
+        ex["fisher"]["mcmc_proposal_per_s"] = nr / (time.perf_counter() - t0)
+        ns = 64  # parity sample: the moment form and the reference algorithm against the oracle
+        fr, cr, _ = ctx.fisher_batch_ex(G.params_array(W.prior_draws(ns, 13)), 0, hf, order=2, epsilon=1e-6,
+                                        step_mode=1)
+        ex["_fisher_sample"] = (pf, fish[:ns].copy(), cov[:ns].copy(), fr, cr, ff, psd_f)
 
     def maximized():
         # the sampler's intrinsic mode: likelihood maximised over t_c and phi_c
@@ -430,7 +454,9 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
             for _ in range(reps):
                 _, st = ctx.maximized_loglik_batch(parr, handles, approximant=ap)
             dt = (time.perf_counter() - t0) / reps
+            res_mx, _ = ctx.maximized_loglik_batch(parr, handles, approximant=ap)
             out[name] = {"evals_per_s": N_REQ / dt, "ms_per_step": dt * 1e3, "ok": int((st == 0).sum())}
+            ex.setdefault("_parity_maximized", {})[name] = (draws[:64], ap, res_mx[:64].copy())
         ex["maximized"] = dict(out, requests=N_REQ, bins=int(f.size), transforms_per_step=N_REQ * len(handles))
 
     def ingest():
@@ -481,7 +507,8 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         h = 0.5 * (1024.0 - 20.0)
         fg, wg = 20.0 + h * (x + 1.0), wq * h
         psd_g = W.analytic_psd(fg)
-        hg = [ctx.register_data(d, fg, W.noise(fg, 700 + i), psd_g, weights=wg) for i, d in enumerate(W.DETECTORS3)]
+        dg = [W.noise(fg, 700 + i) for i in range(3)]
+        hg = [ctx.register_data(d, fg, dg[i], psd_g, weights=wg) for i, d in enumerate(W.DETECTORS3)]
         parr = host_params[1]
         ctx.loglik_batch(parr, 0, hg, 8.0, G.PREC_FP64)
         reps = 5
@@ -489,8 +516,10 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         for _ in range(reps):
             _, st = ctx.loglik_batch(parr, 0, hg, 8.0, G.PREC_FP64)
         dt = (time.perf_counter() - t0) / reps
+        out_g, _ = ctx.loglik_batch(parr, 0, hg, 8.0, G.PREC_FP64)
         ex["gaussleg_fp64"] = {"evals_per_s": N_REQ / dt, "ms_per_call": dt * 1e3, "nodes": int(fg.size),
                                "ok": int((st == 0).sum())}
+        ex["_parity_gaussleg"] = (host_params[1], fg, wg, dg, psd_g, out_g.copy())
 
     for name, fn in (("plain", plain), ("batched_fp64", batched_fp64), ("served", served), ("uneven", uneven),
                      ("fisher", fisher), ("maximized", maximized), ("ingest", ingest), ("gaussleg", gaussleg)):
@@ -533,20 +562,115 @@ def cpu_baseline(res, seconds=10.0):
 
 
 def fisher_err(sample):
+    """The Fisher parity sample against the FP64 oracle: max normalised error
+    |dGamma_ij| / sqrt(Gamma_ii Gamma_jj) of the moment form and of the
+    reference algorithm, and of their inverses (normalised by the oracle's
+    inverse diagonal), with the condition numbers of the normalised matrices."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from gw_analysis_tools_gb300 import workloads as W
-    pf, fish, ff, psd = sample
-    worst = 0.0
+    pf, fish, cov, fr, cr, ff, psd = sample
+    plist = []
     for i in range(len(fish)):
-        p = pf[i]
         op = O.GenParams()
         for k, _ in O.GenParams._fields_:
-            setattr(op, k, getattr(p, k))
-        ref = O.fisher_network(ff, op, list(W.DETECTORS3), [psd] * 3, epsilon=1e-6, step_mode=1)
-        d = np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
-        worst = max(worst, float(np.max(np.abs(fish[i] - ref) / d)))
-    return worst
+            setattr(op, k, getattr(pf[i], k))
+        plist.append(op)
+    ref = O.fisher_batch(plist, ff, list(W.DETECTORS3), [psd] * 3, epsilon=1e-6, step_mode=1)
+
+    def nerr(a, b):
+        return float(np.max(np.abs(a - b) / np.sqrt(np.abs(np.outer(np.diag(b), np.diag(b))))))
+    e_m, e_r, c_m, c_r, conds = [], [], [], [], []
+    for i in range(len(fish)):
+        e_m.append(nerr(fish[i], ref[i]))
+        e_r.append(nerr(fr[i], ref[i]))
+        st, rinv = O.cholesky_invert(ref[i])
+        if st == 0:
+            c_m.append(nerr(cov[i], rinv))
+            c_r.append(nerr(cr[i], rinv))
+            conds.append(float(np.linalg.cond(ref[i] / np.sqrt(np.outer(np.diag(ref[i]), np.diag(ref[i]))))))
+    return {"sources": len(fish), "step": "1e-6 relative",
+            "max_normalized_err": max(e_m), "median_normalized_err": float(np.median(e_m)),
+            "max_normalized_err_inverse": max(c_m), "median_normalized_err_inverse": float(np.median(c_m)),
+            "reference_algorithm_max_normalized_err": max(e_r),
+            "reference_algorithm_max_normalized_err_inverse": max(c_r),
+            "median_condition_number": float(np.median(conds)), "max_condition_number": max(conds)}
+
+
+def parity_stats(got, ref, tol, rel=False):
+    err = np.abs(np.asarray(got) - np.asarray(ref))
+    if rel:
+        err = err / np.maximum(1.0, np.abs(np.asarray(ref)))
+    return {"max_abs_dlogL" if not rel else "max_rel_dlogL": float(err.max()),
+            "p99": float(np.percentile(err, 99)), "median": float(np.median(err)), "requests": int(err.size),
+            "tolerance": tol, "within": bool(err.max() <= tol)}
+
+
+def secondary_parity(ex, res):
+    """|dlogL| against the FP64 oracle for the secondary forms' samples."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from gw_analysis_tools_gb300 import workloads as W
+    dets = list(W.DETECTORS3)
+    out = {}
+    if "_parity_served" in ex:
+        sp, sa, got = ex.pop("_parity_served")
+        ref = O.loglik_batch([O.params_from_dict(d) for d in sp], res["f"], dets, res["data"], [res["psd"]] * 3,
+                             approximants=list(sa), T_segment=res["T"])
+        out["served"] = parity_stats(got, ref, 1e-3)
+    if "_parity_uneven" in ex:
+        pu, Ts, udata, got = ex.pop("_parity_uneven")
+        ref = np.zeros(len(pu))
+        for T in sorted(set(Ts)):
+            idx = [i for i in range(len(pu)) if Ts[i] == T]
+            fu = W.uniform_grid(20.0, 2048.0, 1.0 / T)
+            ref[idx] = O.loglik_batch([O.params_from_dict(pu[i]) for i in idx], fu, dets, udata[T],
+                                      [W.analytic_psd(fu)] * 3, approximants=[O.IMRPhenomPv2] * len(idx))
+        st = parity_stats(got, ref, 1e-3)
+        st["max_abs_dlogL_T128"] = float(np.max(np.abs(got - ref)[np.array(Ts) == 128]))
+        st["max_abs_logL"] = float(np.max(np.abs(ref)))
+        out["uneven_pv2"] = st
+    if "_parity_maximized" in ex:
+        for name, (draws, ap, got) in ex.pop("_parity_maximized").items():
+            ref = [O.maximized_loglik_intrinsic(d, res["f"], res["data"], [res["psd"]] * 3, ap) for d in draws]
+            out["maximized_" + name] = parity_stats(got, ref, 1e-9, rel=True)
+    if "_parity_gaussleg" in ex:
+        parr, fg, wg, dg, psd_g, got = ex.pop("_parity_gaussleg")
+        ref = []
+        for i in range(len(got)):
+            op = O.GenParams()
+            for k, _ in O.GenParams._fields_:
+                setattr(op, k, getattr(parr[i], k))
+            ref.append(O.loglik_gl(op, fg, dets, dg, [psd_g] * 3, [wg] * 3, T_segment=8.0))
+        out["gaussleg_fp64"] = parity_stats(got, ref, 1e-9, rel=True)
+    return out
+
+
+def mcmc_theta(draws):
+    """The sampler's 11-dim IMRPhenomD vectors of parameter dicts
+    (MCMC_prep_params order, mcmc_gw.cpp:2492-2568)."""
+    th = []
+    for d in draws:
+        m1, m2 = d["mass1"], d["mass2"]
+        th.append([d["RA"], np.sin(d["DEC"]), d["psi"], np.cos(d["incl_angle"]), d["phiRef"], d["tc"],
+                   np.log(d["Luminosity_Distance"]), np.log((m1 * m2) ** 0.6 / (m1 + m2) ** 0.2),
+                   m1 * m2 / (m1 + m2) ** 2, d["spin1"][2], d["spin2"][2]])
+    return np.array(th)
+
+
+def uneven_injection(ctx, G, f, T, det):
+    """The IMRPhenomPv2 injection of the uneven-grid workload on one detector's
+    grid of duration T (t_c <- T - t_c as the likelihood sees it), shifted by
+    the arrival time from Hanford; the engine's FP64 detector response, as for
+    the main workload."""
+    src = UNEVEN_INJECTION
+    r = ctx.fourier_detector_response(f, det, "IMRPhenomPv2", G.gen_params(**dict(src, tc=T - src["tc"])))
+    return r * np.exp(-2j * np.pi * _dtoa(src, "Hanford", det) * f)
+
+
+UNEVEN_INJECTION = dict(mass1=31.0, mass2=24.0, spin1=(0.35, -0.2, 0.3), spin2=(-0.25, 0.3, -0.2),
+                        Luminosity_Distance=900.0, incl_angle=0.7, phiRef=0.9, f_ref=20.0, tc=0.02, RA=2.2, DEC=-0.5,
+                        psi=0.8, gmst=1.2345)
 
 
 # ------------------------------------------------------------ reference arm
@@ -628,7 +752,9 @@ def main():
     fp32_peak = measure_peak("float32")
     fp64_peak = measure_peak("float64")
     ex = res.get("extras", {})
-    fisher_worst = fisher_err(ex.pop("_fisher_sample")) if "_fisher_sample" in ex else None
+    fisher_parity = fisher_err(ex.pop("_fisher_sample")) if "_fisher_sample" in ex else None
+    log("secondary parity")
+    sec_parity = secondary_parity(ex, res)
     line = {
         "metric": METRIC, "value": res["value"], "unit": "evals/s", "n_gpus": world, "steps": len(res["step_ms"]),
         "warmup": parse_warmup(), "ms_per_step": res["tot_ms"] / len(res["step_ms"]), "higher_is_better": True,
@@ -647,9 +773,14 @@ def main():
                      "algorithm": "reference flops per waveform-bin %.2f and per detector-bin %.1f "
                                   "(oracle/op_counts.json)" % (REF_FLOPS_PER_WAVE_BIN, REF_FLOPS_PER_DET_BIN),
                      "peak_source": "measured in this run: FP32 GEMM 8192^3 without TF32 (FMA pipe)",
+                     "note": "achieved counts add/mul/div of the reference algorithm; its elementary functions "
+                             "(3.9 per waveform-bin, 3 per detector-bin) are not in it",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
+                                       "kernel on this workload, " + PROFILE_SOURCE,
                      "fp64": {"achieved_tflops": FP64_FLOP_PER_LAUNCH / kernel_s / 1e12, "peak_tflops": fp64_peak,
                               "frac": FP64_FLOP_PER_LAUNCH / kernel_s / 1e12 / fp64_peak if fp64_peak else None,
                               "flop_per_launch": FP64_FLOP_PER_LAUNCH,
+                              "flop_source": "ncu DFMA x 2 + DMUL + DADD of one launch, " + PROFILE_SOURCE,
                               "peak_source": "measured in this run: FP64 GEMM 4096^3"},
                      "hbm": {"achieved_gbs": TRAFFIC_PER_LAUNCH / kernel_s / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
                              "frac": TRAFFIC_PER_LAUNCH / kernel_s / 1e9 / peaks["hbm_gbs"]
@@ -668,7 +799,13 @@ def main():
             if "served" in ex:
                 line["served"]["speedup_vs_plain_fp64"] = ex["served"]["evals_per_s"] / plain
         if "fisher" in ex:
-            line["fisher"] = dict(ex["fisher"], max_normalized_err_vs_oracle=fisher_worst)
+            line["fisher"] = dict(ex["fisher"], parity=fisher_parity)
+        for k, v in sec_parity.items():
+            key = k if k in line else ("maximized" if k.startswith("maximized") else k)
+            if k.startswith("maximized") and "maximized" in line:
+                line["maximized"].setdefault("parity", {})[k.split("_", 1)[1]] = v
+            elif key in line:
+                line[key]["parity"] = v
     print(json.dumps(line))
 
 
@@ -676,6 +813,7 @@ def main():
 # by oracle/count_ops.py on the reference's own model code (oracle/op_counts.json);
 # and, from one ncu capture of k_batch<3,1> on this workload
 # (profiles/k_batch_mixed_ptstep512.md), its DRAM bytes and FP64 flops per launch.
+PROFILE_SOURCE = "profiles/k_batch_mixed_ptstep512.md"
 REF_FLOPS_PER_WAVE_BIN = 66.56
 REF_FLOPS_PER_DET_BIN = 33.0
 TRAFFIC_PER_LAUNCH = 2.72e6

@@ -7,8 +7,10 @@ behind a C ABI (include/gwgpu.h).  See engine.Context.
 """
 from .engine import (IMRPhenomD, IMRPhenomPv2, PREC_FP64, PREC_MIXED, Context, GenParams, GwGpuError, Server,
                      count_lines_data_file, count_lines_losc_data_file, count_lines_losc_psd_file, gen_params,
-                     params_array, populate_noise, read_losc_data_file, read_losc_psd_file)
+                     params_array, populate_noise, read_losc_data_file, read_losc_psd_file,
+                     transform_orientation_coords)
 
 __all__ = ["Context", "Server", "GenParams", "gen_params", "params_array", "GwGpuError", "IMRPhenomD",
            "IMRPhenomPv2", "PREC_FP64", "PREC_MIXED", "count_lines_data_file", "count_lines_losc_data_file",
-           "count_lines_losc_psd_file", "read_losc_data_file", "read_losc_psd_file", "populate_noise"]
+           "count_lines_losc_psd_file", "read_losc_data_file", "read_losc_psd_file", "populate_noise",
+           "transform_orientation_coords"]

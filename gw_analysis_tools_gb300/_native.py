@@ -15,7 +15,7 @@ BUILDDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libgwgpu.so")
 DROPIN_SRC = os.path.join(HERE, "dropin", "gwat_dropin.cpp")
 DROPIN_LIB = os.path.join(LIBDIR, "libgwat_dropin.so")
-SOURCES = ["kernels.cu", "capi.cu", "batch.cu", "fisher.cu", "serve.cu", "noalloc.cu", "maxll.cu", "cufft_rt.cu", "ingest.cu"]
+SOURCES = ["kernels.cu", "capi.cu", "batch.cu", "fisher.cu", "fisher_ref.cu", "serve.cu", "noalloc.cu", "maxll.cu", "cufft_rt.cu", "ingest.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no multiply-add contraction, so that it rounds the same on x86 and Arm hosts
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "--expt-relaxed-constexpr"]
@@ -118,9 +118,12 @@ def _declare(L):
                                             dp, ip]),
     }
     optional = {
+        "gwgpu_transform_orientation_coords": (c_int, [c_void_p, c_char_p]),
         "gwgpu_fisher_numerical": (c_int, [c_void_p, dp, c_int, c_char_p, c_char_p, c_char_p, dp, c_int, c_void_p,
                                            c_int, dp]),
         "gwgpu_fisher_batch": (c_int, [c_void_p, c_void_p, c_int, c_int, ip, c_int, c_double, c_int, dp, dp, ip]),
+        "gwgpu_fisher_batch_ex": (c_int, [c_void_p, c_void_p, c_int, ip, c_int, c_void_p, dp, dp, ip]),
+        "gwgpu_mcmc_fisher_batch": (c_int, [c_void_p, dp, c_int, c_int, c_int, c_double, ip, c_int, dp, ip]),
         "gwgpu_server_create": (c_int, [c_void_p, c_void_p, P(c_void_p)]),
         "gwgpu_server_destroy": (c_int, [c_void_p]),
         "gwgpu_server_submit": (c_int, [c_void_p, c_void_p, c_int, ip, c_int, P(ctypes.c_uint64)]),

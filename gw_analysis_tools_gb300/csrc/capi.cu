@@ -216,6 +216,7 @@ const char *gwgpu_status_string(int s) {
     case GWGPU_EBUSY: return "busy";
     case GWGPU_ENOTFOUND: return "not found";
     case GWGPU_ETOOLARGE: return "size beyond the fixed maximum";
+    case GWGPU_ESINGULAR: return "Fisher matrix not positive definite";
   }
   return "unknown status";
 }
@@ -412,6 +413,7 @@ static int waveform_common(gwgpu_context *c, const double *freqs, int N, double 
   gwt::Request r;
   gwt::GenParams gp;
   std::memcpy(&gp, p, sizeof(gp));
+  if (det >= 0 && gp.equatorial_orientation) gwt::orientation_transform(gp, ap);  // waveform_util.cpp:946-948
   int dets[1] = {det < 0 ? 0 : det};
   gwt::request_prologue(r, gp, ap, dets, 1, c->qnm_host.data());
   void *dev;
@@ -434,6 +436,17 @@ int gwgpu_fourier_waveform(gwgpu_context *c, const double *freqs, int N, double 
                            const gwgpu_gen_params *p) {
   if (!hc) return 0;
   return waveform_common(c, freqs, N, hp, hc, method, p, -1, 0);
+}
+
+int gwgpu_transform_orientation_coords(gwgpu_gen_params *p, const char *method) {
+  int ap = method_approx(method);
+  if (!p || ap < 0) return GWGPU_EINVAL;
+  gwt::GenParams gp;
+  std::memcpy(&gp, p, sizeof(gp));
+  gwt::orientation_transform(gp, ap);
+  p->psi = gp.psi;
+  p->incl_angle = gp.incl_angle;
+  return GWGPU_OK;
 }
 
 int gwgpu_fourier_detector_response(gwgpu_context *c, const double *freqs, int N, double *resp, const char *detector,

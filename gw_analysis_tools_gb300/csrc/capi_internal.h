@@ -25,7 +25,8 @@ struct gwgpu_context {
     std::vector<double> host_freqs;
     uint64_t psd_hash = 0;  // FNV-1a of the PSD bytes: detectors with equal PSDs share weights
   };
-  enum { kWsWave = 0, kWsInner, kWsPlain, kWsBatch, kWsBatchItems, kWsFisher, kWsServe, kWsMaxll, kWsIngest, kWsChirp, kWsChirp32, kWsMaxllRun };
+  enum { kWsWave = 0, kWsInner, kWsPlain, kWsBatch, kWsBatchItems, kWsFisher, kWsServe, kWsMaxll, kWsIngest, kWsChirp, kWsChirp32, kWsMaxllRun,
+         kWsFisherRef = 40 };
   enum { kHwsPlain = 0, kHwsBatch, kHwsFisher, kHwsInner };
 
   int device = 0;

@@ -26,6 +26,7 @@
 #include "../../include/gwgpu.h"
 #include "capi_internal.h"
 #include "fisher_math.h"
+#include "fisher_ref.h"
 #include "kernels.h"
 
 namespace gwf {
@@ -472,8 +473,29 @@ int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, 
     cudaMemcpyAsync(hs.data(), dstat, sizeof(int) * m, cudaMemcpyDeviceToHost, c->stream);
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return c->fail(e, "fisher batch");
+    // Sources whose matrix the FP32-compensated sums leave indefinite (a
+    // normalised smallest eigenvalue below their ~1e-8 precision: equal masses,
+    // face-on orientations) are recomputed by the FP64 reference algorithm.
+    std::vector<int> redo;
+    for (int i = 0; i < m; i++)
+      if (hs[i] == 9) redo.push_back(i);
+    if (!redo.empty()) {
+      std::vector<GenParams> rp(redo.size());
+      for (size_t j = 0; j < redo.size(); j++) std::memcpy(&rp[j], params + s0i + redo[j], sizeof(GenParams));
+      std::vector<double> rf(redo.size() * kDim * kDim), rc(redo.size() * kDim * kDim);
+      std::vector<int> rs(redo.size());
+      st = gwf_ref_run(c, rp.data(), (int)redo.size(), method, 2, handles, ndet, epsilon, step_mode, 0, rf.data(),
+                       covariance ? rc.data() : nullptr, rs.data());
+      if (st) return st;
+      for (size_t j = 0; j < redo.size(); j++) {
+        const size_t o = (size_t)(s0i + redo[j]) * kDim * kDim;
+        std::memcpy(fisher + o, &rf[j * kDim * kDim], sizeof(double) * kDim * kDim);
+        if (covariance) std::memcpy(covariance + o, &rc[j * kDim * kDim], sizeof(double) * kDim * kDim);
+        hs[redo[j]] = rs[j];
+      }
+    }
     if (status)
-      for (int i = 0; i < m; i++) status[s0i + i] = gwk::status_code(hs[i]);
+      for (int i = 0; i < m; i++) status[s0i + i] = hs[i] == 9 ? GWGPU_ESINGULAR : gwk::status_code(hs[i]);
   }
   return GWGPU_OK;
 }

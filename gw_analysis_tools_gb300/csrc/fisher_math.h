@@ -42,6 +42,9 @@ struct FisherSrc {
   int logf[kDim];
   double G0re[kMaxDet], G0im[kMaxDet];
   double ar[kMaxDet][kCheap], ai[kMaxDet][kCheap], br[kMaxDet][kCheap], bi[kMaxDet][kCheap];
+  int onesided[kIntr];  // pair q is a one-sided difference (eta at 1/4): its + waveform is the centre
+  int exact[kIntr];     // pair q is taken as the difference of its two waveforms at every bin
+  int n_cut_any;        // the last bin where any of the centre and the perturbed waveforms is non-zero
   int status;
 };
 // ----------------------------------------------------- pivoted Cholesky inverse
@@ -175,8 +178,18 @@ GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsil
     double tmp[kDim];
     F.div[i] = fisher_perturb(F.v, i, 1, eps, tmp);
   }
-  for (int q = 0; q < kIntr; q++) F.idiv[q] = 1.0 / F.div[7 + q];
+  for (int q = 0; q < kIntr; q++) {
+    F.idiv[q] = 1.0 / F.div[7 + q];
+    F.onesided[q] = F.div[7 + q] == fisher_step(F.v, 7 + q, epsilon, step_mode);
+    // The waveform depends on eta through sqrt(1 - 4 eta) (the component
+    // masses): within a few thousand steps of eta = 1/4 the pair's mean phase
+    // and amplitude offsets are no longer second order in the step, and the
+    // difference is taken waveform by waveform.
+    F.exact[q] = q == 1 && (0.25 - F.v[8]) < 1000.0 * F.div[8];
+  }
   F.w0 = S[0].w;
+  F.n_cut_any = F.w0.n_cut;
+  for (int s = 1; s < kSlots; s++) F.n_cut_any = F.n_cut_any > S[s].w.n_cut ? F.n_cut_any : S[s].w.n_cut;
   const double A0 = S[0].w.A_scale;
   for (int k = 0; k < kIntr; k++) {
     int i = 7 + k;
@@ -284,16 +297,59 @@ GW_HD double fisher_phase_deriv(const FisherSrc &F, int q, int n, double t, doub
   return wave64_phase_diff(p, m, n, t, r, lnn, t34) * F.idiv[q];
 }
 
-// One bin: the intrinsic amplitude/phase differences and the moment sums,
-// accumulated for weight stream w with weight wh (Simpson-weighted 1/S).
+// The exact difference of pair q relative to the centre's phase, per unit
+// step: the sum over the non-zero waveforms of +-A s e^{-i delta},
+// delta = (Phi - phic) - (Phi0 - phic0).  Used at a bin where a waveform is
+// beyond its cut (f > 0.2/M, where the model is exactly zero: a finite
+// difference across the cut is a jump, which the series form below does not
+// describe) and for pairs flagged exact.
+GW_HD void fisher_q_exact(const FisherSrc &F, int q, int n, double t, double r, double lnn, double t34, double m76,
+                          float &qr, float &qi) {
+  const double phi0 = wave64_phase(F.w0, n, t, r, lnn, t34) - F.w0.phic;
+  double re = 0.0, im = 0.0;
+  for (int side = 0; side < 2; side++) {
+    const WaveF64 &w = side == 0 ? F.wp[q] : F.wm[q];
+    if (n > w.n_cut) continue;
+    const double a = wave64_amp(w, n, t, m76) * (side == 0 ? F.sp[q] : F.sm[q]) * (side == 0 ? 1.0 : -1.0);
+    double s, c;
+    sincos((wave64_phase(w, n, t, r, lnn, t34) - w.phic) - phi0, &s, &c);
+    re += a * c;
+    im -= a * s;
+  }
+  qr = (float)(re * F.idiv[q]);
+  qi = (float)(im * F.idiv[q]);
+}
+
+// One bin: the intrinsic differences q = (r+ - r-) e^{i Phi0} / (G divisor) of
+// the four waveform pairs, for the moment sums.  With h half the phase step
+// (Phi+ - Phi-) / 2 and the mean phase offset of the pair second order in the
+// step, a central pair is exactly (A+ - A-) cos h - i (A+ + A-) sin h; cos h and
+// sin h / h by their series (h stays below 1e-2 for the steps used).  A
+// one-sided pair (eta at 1/4, + the centre) is A0 - A- e^{2ih}.
 GW_HD bool fisher_bin_q(const FisherSrc &F, int n, double t, double r, double lnn, double t34, double m76,
                         float m76f, float &a0, float *qr, float *qi) {
-  const double amp0 = wave64_amp(F.w0, n, t, m76);  // the centre's phase is not needed
-  if (amp0 == 0.0) return false;
+  if (n > F.n_cut_any) return false;
+  const double amp0 = wave64_amp(F.w0, n, t, m76);
   a0 = (float)amp0;
   for (int q = 0; q < kIntr; q++) {
-    qr[q] = fisher_amp_deriv(F, q, n, t, m76, m76f);  // q = dA - i A dPhi
-    qi[q] = (float)(-amp0 * fisher_phase_deriv(F, q, n, t, r, lnn, t34));
+    if (F.exact[q] || amp0 == 0.0 || n > F.wp[q].n_cut || n > F.wm[q].n_cut) {
+      fisher_q_exact(F, q, n, t, r, lnn, t34, m76, qr[q], qi[q]);
+      continue;
+    }
+    const float damp = fisher_amp_deriv(F, q, n, t, m76, m76f);    // (A+ - A-) / divisor
+    const double dph = fisher_phase_deriv(F, q, n, t, r, lnn, t34);  // (Phi+ - Phi-) / divisor
+    const double h = 0.5 * dph * F.div[7 + q];
+    const double h2 = h * h;
+    if (!F.onesided[q]) {
+      qr[q] = damp * (float)(1.0 - h2 * (0.5 - h2 * (1.0 / 24.0)));
+      qi[q] = (float)(-amp0 * dph * (1.0 - h2 * ((1.0 / 6.0) - h2 * (1.0 / 120.0))));
+    } else {
+      const double am = amp0 - (double)damp * F.div[7 + q];
+      double s2, c2;
+      sincos(2.0 * h, &s2, &c2);
+      qr[q] = (float)((amp0 - am * c2) * F.idiv[q]);
+      qi[q] = (float)(-am * s2 * F.idiv[q]);
+    }
   }
   return true;
 }

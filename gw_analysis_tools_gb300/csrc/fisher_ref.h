@@ -1,0 +1,16 @@
+// fisher_ref.h -- the reference's Fisher algorithm on the device for many
+// sources (fisher_ref.cu), shared with the batched moment form (fisher.cu),
+// which hands it the sources whose matrices it cannot invert.
+#pragma once
+
+#include "phenom_model.h"
+
+struct gwgpu_context;
+
+// Fisher matrices (and, if cov != NULL, inverses) of n sources with host
+// parameters over the registered streams `handles` (reference detector =
+// handles[0]); fisher/cov are host arrays n x 11 x 11; kstatus[i] is 0, 4
+// (outside the model domain) or 9 (not invertible).  The caller holds the
+// context lock.
+int gwf_ref_run(gwgpu_context *c, const gwt::GenParams *params, int n, int method, int order, const int *handles,
+                int ndet, double epsilon, int step_mode, int add_prior, double *fisher, double *cov, int *kstatus);

@@ -525,40 +525,8 @@ __global__ void k_mcmc_repack(const double *__restrict__ theta, int dim, int n, 
                               GenParams *out, int *approx_out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double *th = theta + (size_t)i * dim;
   GenParams o;
-  o.spin1[0] = o.spin1[1] = o.spin1[2] = 0;
-  o.spin2[0] = o.spin2[1] = o.spin2[2] = 0;
-  o.chip = -1;
-  o.phip = -1;
-  o.sky_average = 0;
-  o.dep_postmerger = 0;
-  o.f_ref = 20;
-  o.shift_time = 1;
-  o.shift_phase = 1;
-  o.gmst = gmst;
-  o.mass1 = calc_mass1(exp(th[7]), th[8]);
-  o.mass2 = calc_mass2(exp(th[7]), th[8]);
-  o.Luminosity_Distance = exp(th[6]);
-  o.RA = th[0];
-  o.DEC = asin(th[1]);
-  o.psi = th[2];
-  o.incl_angle = acos(th[3]);
-  o.phiRef = th[4];
-  o.tc = th[5];
-  if (approximant == kPhenomPv2 && dim >= 15) {
-    double t1 = th[11] > 1 ? 0 : (th[11] < -1 ? kPi : acos(th[11]));
-    double t2 = th[12] > 1 ? 0 : (th[12] < -1 ? kPi : acos(th[12]));
-    o.spin1[0] = th[9] * sin(t1) * cos(th[13]);
-    o.spin1[1] = th[9] * sin(t1) * sin(th[13]);
-    o.spin1[2] = th[9] * cos(t1);
-    o.spin2[0] = th[10] * sin(t2) * cos(th[14]);
-    o.spin2[1] = th[10] * sin(t2) * sin(th[14]);
-    o.spin2[2] = th[10] * cos(t2);
-  } else {
-    o.spin1[2] = th[9];
-    o.spin2[2] = th[10];
-  }
+  mcmc_repack(theta + (size_t)i * dim, dim, approximant, gmst, o);
   out[i] = o;
   approx_out[i] = approximant;
 }

@@ -32,23 +32,25 @@ constexpr int kNoAllocPartials = kNoAllocMaxBlocks * 2 * gwt::kMaxDet;  // doubl
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocPartials + 32];
 
 constexpr int kMaxDevices = 64;
-double *g_scratch_ptr[kMaxDevices] = {nullptr};
+bool g_loaded[kMaxDevices] = {false};
 std::mutex g_setup_mu;
 
-// Once per device, on the first call: the scratch address and the plain
-// kernels' module (cudaGetSymbolAddress and a function-attribute query, which
-// may load the module).  That first call must therefore come before any
-// stream capture that later calls are part of.
+// The scratch address, looked up on every call with the device current
+// (cudaGetSymbolAddress allocates nothing and is cheap), so that it stays
+// right after a device reset.  On the first call per device, also the plain
+// kernels' module (a function-attribute query, which may load the module):
+// that first call must come before any stream capture that later calls are
+// part of.
 int setup(int device, double **out) {
   if (device < 0 || device >= kMaxDevices) return GWGPU_EINVAL;
   std::lock_guard<std::mutex> lk(g_setup_mu);
-  if (!g_scratch_ptr[device]) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return GWGPU_ECUDA;
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return GWGPU_ECUDA;
+  if (!g_loaded[device]) {
     if (gwk::plain_preload() != cudaSuccess) return GWGPU_ECUDA;
-    g_scratch_ptr[device] = (double *)p;
+    g_loaded[device] = true;
   }
-  *out = g_scratch_ptr[device];
+  *out = (double *)p;
   return GWGPU_OK;
 }
 

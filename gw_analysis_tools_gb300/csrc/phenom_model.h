@@ -52,6 +52,8 @@ struct GenParams {
   double RA, DEC, psi, gmst;
   double chip, phip;
   int32_t shift_time, shift_phase, sky_average, dep_postmerger;
+  double theta_l, phi_l;  // equatorial direction of L, read when equatorial_orientation is set
+  int32_t equatorial_orientation, reserved;
 };
 
 // source_parameters<double> subset (include/gwat/util.h:426-665)
@@ -188,40 +190,41 @@ GW_HD void populate(Source &s, const GenParams &in) {
 }
 
 // ------------------------------------------- natural cubic spline (QNM table)
-// Spline layout in one array: x[n], y1[n], y2[n], c1[n], c2[n].  c = half the
-// second derivative (GSL "cspline" convention), natural end conditions,
-// solved once on the host.
+// Spline layout in one array: x[n], y1[n], y2[n], c1[n], c2[n].
+// On [x_i, x_{i+1}], S(x) = y_i + b_i t + c_i t^2 + d_i t^3, t = x - x_i,
+// h_i = x_{i+1} - x_i; natural ends c_0 = c_{n-1} = 0 (c is half of S'').
+// Continuity of S' at the interior knots gives
+//   h_{i-1} c_{i-1} + 2 (h_{i-1} + h_i) c_i + h_i c_{i+1} = 3 (s_i - s_{i-1}),
+// s_i = (y_{i+1} - y_i) / h_i (Burden & Faires, Numerical Analysis, sec. 3.5):
+// a symmetric tridiagonal system, solved by its L D L^T factorisation -- one
+// forward sweep for the pivots, the multipliers and the reduced right-hand
+// side, then back substitution.  Solved once on the host (QNM table) or per
+// request (the 10-node Pv2 time shift).  work: 3 (n - 2) doubles.
 GW_HD void cspline_coeffs(const double *x, const double *y, int n, double *c, double *work) {
-  int max_index = n - 1, sys = max_index - 1;
-  double *diag = work, *off = work + sys, *g = work + 2 * sys, *gam = work + 3 * sys, *alp = work + 4 * sys,
-         *z = work + 5 * sys;
+  const int m = n - 2;  // unknowns: the interior knots 1..n-2
   c[0] = 0.0;
-  c[max_index] = 0.0;
-  for (int i = 0; i < sys; i++) {
-    double h_i = x[i + 1] - x[i], h_ip1 = x[i + 2] - x[i + 1];
-    double yd_i = y[i + 1] - y[i], yd_ip1 = y[i + 2] - y[i + 1];
-    double g_i = (h_i != 0.0) ? 1.0 / h_i : 0.0, g_ip1 = (h_ip1 != 0.0) ? 1.0 / h_ip1 : 0.0;
-    off[i] = h_ip1;
-    diag[i] = 2.0 * (h_ip1 + h_i);
-    g[i] = 3.0 * (yd_ip1 * g_ip1 - yd_i * g_i);
-  }
-  if (sys == 1) {
-    c[1] = g[0] / diag[0];
-  } else if (sys > 1) {
-    int N = sys;
-    alp[0] = diag[0];
-    gam[0] = off[0] / alp[0];
-    for (int i = 1; i < N - 1; i++) {
-      alp[i] = diag[i] - off[i - 1] * gam[i - 1];
-      gam[i] = off[i] / alp[i];
+  c[n - 1] = 0.0;
+  if (m < 1) return;
+  double *piv = work, *mul = work + m, *rhs = work + 2 * m;
+  double h_left = x[1] - x[0];
+  double s_left = (y[1] - y[0]) * (h_left != 0.0 ? 1.0 / h_left : 0.0);
+  for (int k = 0; k < m; k++) {
+    const double h_right = x[k + 2] - x[k + 1];
+    const double s_right = (y[k + 2] - y[k + 1]) * (h_right != 0.0 ? 1.0 / h_right : 0.0);
+    const double diag = 2.0 * (h_right + h_left), load = 3.0 * (s_right - s_left);
+    if (k == 0) {
+      piv[0] = diag;
+      rhs[0] = load;
+    } else {  // the row's sub-diagonal entry is the previous row's h_right = h_left here
+      piv[k] = diag - h_left * mul[k - 1];
+      rhs[k] = load - mul[k - 1] * rhs[k - 1];
     }
-    alp[N - 1] = diag[N - 1] - off[N - 2] * gam[N - 2];
-    z[0] = g[0];
-    for (int i = 1; i < N; i++) z[i] = g[i] - gam[i - 1] * z[i - 1];
-    for (int i = 0; i < N; i++) z[i] = z[i] / alp[i];
-    c[N] = z[N - 1];
-    for (int i = N - 2; i >= 0; i--) c[1 + i] = z[i] - gam[i] * c[2 + i];
+    if (k < m - 1) mul[k] = h_right / piv[k];
+    h_left = h_right;
+    s_left = s_right;
   }
+  c[m] = rhs[m - 1] / piv[m - 1];
+  for (int k = m - 2; k >= 0; k--) c[k + 1] = rhs[k] / piv[k] - mul[k] * c[k + 2];
 }
 // Interval of xv in the knots x[0..n): the last ilo <= n - 2 with x[ilo] <= xv
 // (what a bisection finds), or -1 outside [x[0], x[n-1]].
@@ -254,6 +257,8 @@ GW_HD double cspline_eval_pre(const double *x, const double *y, const double *b,
   const double delx = xv - x[ilo];
   return y[ilo] + delx * (b[ilo] + delx * (c[ilo] + delx * d[ilo]));
 }
+// S (deriv 0) or S' (deriv 1) on knot interval i:
+// b_i = s_i - h_i (c_{i+1} + 2 c_i) / 3, d_i = (c_{i+1} - c_i) / (3 h_i).
 GW_HD double cspline_eval_at(const double *x, const double *y, const double *c, int ilo, double xv, int deriv) {
   if (ilo < 0) return NAN;
   double x_lo = x[ilo], dx = x[ilo + 1] - x_lo, y_lo = y[ilo], dy = y[ilo + 1] - y_lo, delx = xv - x_lo;

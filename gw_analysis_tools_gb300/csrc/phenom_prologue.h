@@ -564,7 +564,7 @@ GW_HD double pv2_shift_node(const ModelD &m, int j) {
   return -build_phase(f, m, pn, pw);
 }
 GW_HD double pv2_shift_solve(const ModelD &m, const double *ph) {
-  double ff[kPv2ShiftNodes], cc[kPv2ShiftNodes], work[6 * kPv2ShiftNodes];
+  double ff[kPv2ShiftNodes], cc[kPv2ShiftNodes], work[3 * kPv2ShiftNodes];
   double fs = .8 * (m.s.fRD), fe = 1.2 * (m.s.fRD);
   double dfx = (fe - fs) / (kPv2ShiftNodes - 1);
   if (dfx != dfx || dfx <= 0) return 0;
@@ -733,8 +733,13 @@ GW_HD void fisher_unpack(const GenParams &p, int method, double *v, int *logf) {
   double mc = calc_chirpmass(p.mass1, p.mass2), eta = calc_eta(p.mass1, p.mass2);
   v[0] = p.RA;
   v[1] = mcmc ? sin(p.DEC) : p.DEC;
-  v[2] = p.psi;
-  v[3] = mcmc ? cos(p.incl_angle) : p.incl_angle;
+  if (p.equatorial_orientation) {  // L's equatorial angles stand for psi, iota (fisher.cpp:1916-1919, 1944-1947)
+    v[2] = p.theta_l;
+    v[3] = p.phi_l;
+  } else {
+    v[2] = p.psi;
+    v[3] = mcmc ? cos(p.incl_angle) : p.incl_angle;
+  }
   v[4] = p.phiRef;
   v[5] = p.tc;
   if (mcmc) {
@@ -751,6 +756,76 @@ GW_HD void fisher_unpack(const GenParams &p, int method, double *v, int *logf) {
   v[10] = p.spin2[2];
 }
 
+// ------------------------------------------------- equatorial orientation
+// Polarisation and inclination of a direction (th, ph) in equatorial
+// coordinates seen from the sky position (ra, dec): tan(pi/2 - psi) =
+// cos(dec) cot(th) / sin(ph - ra) - cot(ph - ra) sin(dec), and the angle to the
+// propagation direction -N (terr_pol_iota_from_equat_sph, util.cpp:1362-1378).
+GW_HD void pol_incl_of_direction(double ra, double dec, double th, double ph, double &pol, double &incl) {
+  const double cd = cos(dec), sd = sin(dec);
+  pol = kPi / 2. - atan(cd * 1. / tan(th) * 1. / sin(ph - ra) - 1. / tan(ph - ra) * sd);
+  incl = acos(-(cos(th) * sd) - cd * cos(ph - ra) * sin(th));
+}
+
+// transform_orientation_coords (waveform_util.cpp:1523-1586) for a ground
+// detector.  IMRPhenomD: inclination and polarisation of L itself.
+// IMRPhenomPv2: the inclination is the angle between L and the line of sight N;
+// the polarisation is that of the total angular momentum J.  J's direction in
+// the source frame (L along z) is J0 = (m1^2 chip cos phip, m1^2 chip sin phip,
+// L0 + m1^2 chi1z + m2^2 chi2z), L0 = M^2 L2PN at f_ref
+// (PhenomPv2_JSF_from_params, IMRPhenomP.cpp:776-816); it is carried to
+// equatorial coordinates by the rotation that takes the source frame's (L, N,
+// L x N) to their equatorial directions (equatorial_from_SF, util.cpp:1440-1485).
+GW_HD void orientation_transform(GenParams &p, int approx) {
+  const double ths = kPi / 2. - p.DEC, phs = p.RA;
+  const double n0 = -sin(ths) * cos(phs), n1 = -sin(ths) * sin(phs), n2 = -cos(ths);
+  const double l0 = sin(p.theta_l) * cos(p.phi_l), l1 = sin(p.theta_l) * sin(p.phi_l), l2 = cos(p.theta_l);
+  p.incl_angle = acos(n0 * l0 + n1 * l1 + n2 * l2);
+  if (approx != kPhenomPv2) {
+    pol_incl_of_direction(p.RA, p.DEC, p.theta_l, p.phi_l, p.psi, p.incl_angle);
+    return;
+  }
+  // J in the source frame
+  const double eta = calc_eta(p.mass1, p.mass2);
+  const double m1sq = p.mass1 * p.mass1, m2sq = p.mass2 * p.mass2;
+  Pows pw;
+  precalc_powers_PI(pw);
+  precalc_powers_ins(p.f_ref, (p.mass1 + p.mass2) * kMsolSec, pw);
+  const double Mt = p.mass1 + p.mass2;
+  const double Lz = Mt * Mt * L2PN(eta, pw.MF2third, pw.PI2third);
+  double jx = m1sq * p.chip * cos(p.phip), jy = m1sq * p.chip * sin(p.phip), jz = Lz + m1sq * p.spin1[2] +
+                                                                                  m2sq * p.spin2[2];
+  const double jn = sqrt(jx * jx + jy * jy + jz * jz);
+  jx /= jn;
+  jy /= jn;
+  jz /= jn;
+  // rotated to equatorial coordinates
+  const double cp = cos(kPi / 2. - p.phiRef), sp = sin(kPi / 2. - p.phiRef);
+  const double ci = cos(p.incl_angle), si = sin(p.incl_angle);
+  const double ctl = cos(p.theta_l), stl = sin(p.theta_l), cts = cos(ths), sts = sin(ths);
+  const double cps = cos(phs), sps = sin(phs), cpl = cos(p.phi_l), spl = sin(p.phi_l);
+  const double cp2 = cp * cp;
+  const double ex = (cp2 * cpl * jz * si * stl - ci * cpl * (cp * jx + jy * sp) * stl -
+                     cp * (cts * jy * spl * stl + cps * jx * sts - ctl * jy * sps * sts) +
+                     sp * (cpl * jz * si * sp * stl + cts * jx * spl * stl - (cps * jy + ctl * jx * sps) * sts)) /
+                    si;
+  const double ey = (cp2 * jz * si * spl * stl +
+                     sp * (-(cpl * cts * jx * stl) - ci * jy * spl * stl + jz * si * sp * spl * stl +
+                           cps * ctl * jx * sts - jy * sps * sts) +
+                     cp * (cpl * cts * jy * stl - ci * jx * spl * stl - (cps * ctl * jy + jx * sps) * sts)) /
+                    si;
+  const double ez = (ctl * jz * si - jx * (ci * cp * ctl + cp * cts + sp * (cps * spl - cpl * sps) * stl * sts) -
+                     jy * (ci * ctl * sp + cts * sp + cp * (-(cps * spl) + cpl * sps) * stl * sts)) /
+                    si;
+  // its spherical angles (transform_cart_sph, util.cpp:1882-1891)
+  const double r = sqrt(ex * ex + ez * ez + ey * ey);
+  const double thj = acos(ez / r);
+  double phj = atan2(ey, ex);
+  if (phj < 0) phj += 2 * kPi;
+  double incl_j;
+  pol_incl_of_direction(p.RA, p.DEC, thj, phj, p.psi, incl_j);
+}
+
 // repack_non_parameter_options (fisher.cpp:2514-2535) + repack_parameters
 GW_HD void fisher_repack(const double *v, const GenParams &in, int method, GenParams &o) {
   for (int k = 0; k < 3; k++) o.spin1[k] = o.spin2[k] = 0;
@@ -762,25 +837,77 @@ GW_HD void fisher_repack(const double *v, const GenParams &in, int method, GenPa
   o.shift_time = 0;
   o.shift_phase = in.shift_phase;
   o.dep_postmerger = in.dep_postmerger;
+  o.equatorial_orientation = in.equatorial_orientation;
+  o.theta_l = in.theta_l;
+  o.phi_l = in.phi_l;
+  o.reserved = 0;
   if (method == 1) {
     o.mass1 = calc_mass1(exp(v[7]), v[8]);
     o.mass2 = calc_mass2(exp(v[7]), v[8]);
     o.Luminosity_Distance = exp(v[6]);
     o.DEC = asin(v[1]);
-    o.incl_angle = acos(v[3]);
   } else {
     o.mass1 = calc_mass1(v[7], v[8]);
     o.mass2 = calc_mass2(v[7], v[8]);
     o.Luminosity_Distance = v[6];
     o.DEC = v[1];
-    o.incl_angle = v[3];
   }
   o.RA = v[0];
-  o.psi = v[2];
   o.phiRef = v[4];
   o.tc = v[5];
   o.spin1[2] = v[9];
   o.spin2[2] = v[10];
+  if (in.equatorial_orientation) {  // the response takes psi and iota from L (fisher.cpp:2242-2245)
+    o.theta_l = v[2];
+    o.phi_l = v[3];
+    orientation_transform(o, kPhenomD);
+  } else {
+    o.psi = v[2];
+    o.incl_angle = method == 1 ? acos(v[3]) : v[3];
+  }
+}
+
+// The sampler's parameter vector to the generation parameters: MCMC_prep_params
+// (mcmc_gw.cpp:2492-2510: f_ref 20, t_c and phase shifts on, the sampler's
+// GMST, no orientation transform) + repack_parameters, MCMC_IMRPhenomD 11-dim
+// and MCMC_IMRPhenomPv2 15-dim with spherical spins (fisher.cpp:2171-2284).
+GW_HD void mcmc_repack(const double *th, int dim, int approximant, double gmst, GenParams &o) {
+  o.spin1[0] = o.spin1[1] = o.spin1[2] = 0;
+  o.spin2[0] = o.spin2[1] = o.spin2[2] = 0;
+  o.chip = -1;
+  o.phip = -1;
+  o.sky_average = 0;
+  o.dep_postmerger = 0;
+  o.f_ref = 20;
+  o.shift_time = 1;
+  o.shift_phase = 1;
+  o.gmst = gmst;
+  o.theta_l = 0;
+  o.phi_l = 0;
+  o.equatorial_orientation = 0;
+  o.reserved = 0;
+  o.mass1 = calc_mass1(exp(th[7]), th[8]);
+  o.mass2 = calc_mass2(exp(th[7]), th[8]);
+  o.Luminosity_Distance = exp(th[6]);
+  o.RA = th[0];
+  o.DEC = asin(th[1]);
+  o.psi = th[2];
+  o.incl_angle = acos(th[3]);
+  o.phiRef = th[4];
+  o.tc = th[5];
+  if (approximant == kPhenomPv2 && dim >= 15) {
+    double t1 = th[11] > 1 ? 0 : (th[11] < -1 ? kPi : acos(th[11]));
+    double t2 = th[12] > 1 ? 0 : (th[12] < -1 ? kPi : acos(th[12]));
+    o.spin1[0] = th[9] * sin(t1) * cos(th[13]);
+    o.spin1[1] = th[9] * sin(t1) * sin(th[13]);
+    o.spin1[2] = th[9] * cos(t1);
+    o.spin2[0] = th[10] * sin(t2) * cos(th[14]);
+    o.spin2[1] = th[10] * sin(t2) * sin(th[14]);
+    o.spin2[2] = th[10] * cos(t2);
+  } else {
+    o.spin1[2] = th[9];
+    o.spin2[2] = th[10];
+  }
 }
 
 // The perturbed parameter vector of calculate_derivatives (fisher.cpp:361-375):

@@ -5,13 +5,21 @@
 // sampler (mcmc_data / mcmc_noise / mcmc_frequencies, mcmc_gw.cpp:1464-1476)
 // are registered on the device the first time a (pointer, length, content
 // fingerprint) triple is seen and reused afterwards, as the reference treats
-// them as read-only during sampling.  Callers on several threads are safe:
-// the engine serialises them, or, in "served" mode, coalesces them into
-// batched launches.
+// them as read-only during sampling.  The fingerprint reads 64 samples of each
+// of the frequency, data and PSD arrays (and the weights) on every likelihood
+// call: about 1 us of host time.  At most kMaxHandles registrations are kept;
+// the least recently used one is released when a new one would exceed that,
+// so a caller that refills or reallocates its arrays does not grow device
+// memory without bound.  Callers on several threads are safe: the engine
+// serialises them, or, in "served" mode, coalesces them into batched launches
+// (one server per segment length T, kept until the process exits).
 #include "../../include/gwat_dropin.h"
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
+#include <list>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <stdexcept>
@@ -26,13 +34,20 @@
 
 namespace gwat_dropin {
 
+constexpr size_t kMaxHandles = 64;
+
+using HandleKey = std::tuple<const void *, const void *, const void *, const void *, int, int, uint64_t>;
+
 struct Engine {
   gwgpu_context *ctx = nullptr;
-  gwgpu_server *srv = nullptr;
-  double srv_T = 0;
   bool served = false;
   std::mutex mu;
-  std::map<std::tuple<const void *, const void *, const void *, const void *, int, int, uint64_t>, int> handles;
+  // registered streams, most recently used first
+  std::list<std::pair<HandleKey, int>> lru;
+  std::map<HandleKey, std::list<std::pair<HandleKey, int>>::iterator> handles;
+  // one continuous-batching server per segment length T: never destroyed
+  // while the process runs, so no caller can be inside a server being freed
+  std::map<double, gwgpu_server *> servers;
 };
 
 static Engine &engine() {
@@ -83,6 +98,9 @@ static void to_abi(const gen_params_base<double> *p, gwgpu_gen_params *o) {
   o->shift_phase = p->shift_phase;
   o->sky_average = p->sky_average;
   o->dep_postmerger = p->dep_postmerger;
+  o->equatorial_orientation = p->equatorial_orientation;
+  o->theta_l = p->theta_l;
+  o->phi_l = p->phi_l;
 }
 
 // weights: the GAUSSLEG integration (null: Simpson's rule); log10F as the reference's flag
@@ -93,14 +111,37 @@ static int handle_for(Engine &e, const std::string &det, const double *f, const 
   auto key = std::make_tuple((const void *)f, (const void *)d, (const void *)psd, (const void *)weights, n,
                              (int)det.size() * 131 + det[0], fp);
   auto it = e.handles.find(key);
-  if (it != e.handles.end()) return it->second;
+  if (it != e.handles.end()) {
+    e.lru.splice(e.lru.begin(), e.lru, it->second);
+    return it->second->second;
+  }
   int h = -1;
   int st = weights ? gwgpu_data_register_weighted(e.ctx, det.c_str(), f, n, (const double *)d, psd, weights,
                                                   log10F ? 1 : 0, &h)
                    : gwgpu_data_register(e.ctx, det.c_str(), f, n, (const double *)d, psd, &h);
   if (st != GWGPU_OK) return -1;
-  e.handles[key] = h;
+  e.lru.emplace_front(key, h);
+  e.handles[key] = e.lru.begin();
   return h;
+}
+
+// Release the least recently used registrations beyond kMaxHandles, keeping
+// the `keep` handles of the call in progress.  Called with e.mu held, before
+// any launch of that call: a released stream is never read by work in flight
+// on the context stream, which the engine serialises.  In served mode the
+// server may still hold requests on older streams, so nothing is released
+// there while any server exists.
+static void evict(Engine &e, const int *keep, int nkeep) {
+  if (!e.servers.empty()) return;
+  while (e.lru.size() > kMaxHandles) {
+    auto last = std::prev(e.lru.end());
+    bool kept = false;
+    for (int i = 0; i < nkeep; i++) kept |= keep[i] == last->second;
+    if (kept) break;
+    gwgpu_data_release(e.ctx, last->second);
+    e.handles.erase(last->first);
+    e.lru.erase(last);
+  }
 }
 
 }  // namespace gwat_dropin
@@ -132,6 +173,11 @@ int fourier_detector_response(T *frequencies, int length, std::complex<T> *respo
   (void)times;
   gwgpu_gen_params p;
   to_abi(parameters, &p);
+  if (parameters->equatorial_orientation &&
+      gwgpu_transform_orientation_coords(&p, generation_method.c_str()) == GWGPU_OK) {
+    parameters->psi = p.psi;  // the reference rewrites the caller's psi and inclination (waveform_util.cpp:946-948)
+    parameters->incl_angle = p.incl_angle;
+  }
   return gwgpu_fourier_detector_response(engine().ctx, frequencies, length, (double *)response, detector.c_str(),
                                          generation_method.c_str(), &p);
 }
@@ -177,6 +223,7 @@ double MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double> *pa
                          data_length[i]);
       if (hs[i] < 0) return NAN;
     }
+    evict(e, hs, num_detectors);
   }
   gwgpu_gen_params p;
   to_abi(parameters, &p);
@@ -185,21 +232,31 @@ double MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double> *pa
   const char *m = generation_method.c_str();
   int approx = generation_method.find("Pv2") != std::string::npos ? GWGPU_IMRPHENOMPV2 : GWGPU_IMRPHENOMD;
   if (e.served && !gauss) {  // the served (mixed) form wants uniform grids; Gauss-Legendre grids run plain
+    gwgpu_server *srv = nullptr;
     {
       std::lock_guard<std::mutex> lk(e.mu);
-      if (!e.srv || e.srv_T != T) {
-        if (e.srv) gwgpu_server_destroy(e.srv);
+      auto it = e.servers.find(T);
+      if (it == e.servers.end()) {
         gwgpu_server_config cfg = {16384, 1024, 4, GWGPU_PREC_MIXED, T, 0};
-        gwgpu_server_create(e.ctx, &cfg, &e.srv);
-        e.srv_T = T;
+        if (gwgpu_server_create(e.ctx, &cfg, &srv) != GWGPU_OK || !srv) return NAN;
+        e.servers[T] = srv;
+      } else {
+        srv = it->second;
       }
     }
+    // every slot taken: back off and retry, for at most a minute
     uint64_t t;
     int st;
-    while ((st = gwgpu_server_submit(e.srv, &p, approx, hs, num_detectors, &t)) == GWGPU_EBUSY) {
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::seconds(60);
+    auto pause = std::chrono::microseconds(20);
+    while ((st = gwgpu_server_submit(srv, &p, approx, hs, num_detectors, &t)) == GWGPU_EBUSY) {
+      if (std::chrono::steady_clock::now() > deadline) return NAN;
+      std::this_thread::sleep_for(pause);
+      pause = std::min(pause * 2, std::chrono::microseconds(2000));
     }
     if (st != GWGPU_OK) return NAN;
-    gwgpu_server_wait(e.srv, t, 600000, &ll, &st);
+    int rst = GWGPU_OK;
+    if (gwgpu_server_wait(srv, t, 600000, &ll, &rst) != GWGPU_OK || rst != GWGPU_OK) return NAN;
     return ll;
   }
   gwgpu_mcmc_likelihood_extrinsic(e.ctx, &p, m, hs, num_detectors, T, &ll);

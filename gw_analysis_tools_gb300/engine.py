@@ -27,7 +27,7 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 METHODS = {"IMRPhenomD": IMRPhenomD, "IMRPhenomPv2": IMRPhenomPv2}
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "HBM budget exceeded", 4: "outside model domain",
-          5: "timed out", 6: "busy", 7: "not found", 8: "too large"}
+          5: "timed out", 6: "busy", 7: "not found", 8: "too large", 9: "Fisher matrix not positive definite"}
 
 
 class GenParams(ctypes.Structure):
@@ -44,6 +44,8 @@ class GenParams(ctypes.Structure):
         ("chip", ctypes.c_double), ("phip", ctypes.c_double),
         ("shift_time", ctypes.c_int32), ("shift_phase", ctypes.c_int32),
         ("sky_average", ctypes.c_int32), ("dep_postmerger", ctypes.c_int32),
+        ("theta_l", ctypes.c_double), ("phi_l", ctypes.c_double),
+        ("equatorial_orientation", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
 
 
@@ -57,11 +59,21 @@ def gen_params(**kw):
     for k, v in kw.items():
         if k in ("spin1", "spin2"):
             getattr(p, k)[:] = [float(x) for x in v]
-        elif k in ("shift_time", "shift_phase", "sky_average", "dep_postmerger"):
+        elif k in ("shift_time", "shift_phase", "sky_average", "dep_postmerger", "equatorial_orientation"):
             setattr(p, k, int(bool(v)))
         else:
             setattr(p, k, float(v))
     return p
+
+
+def transform_orientation_coords(params, generation_method="IMRPhenomD"):
+    """transform_orientation_coords (waveform_util.cpp:1523-1586), ground
+    detectors: a copy of params with incl_angle and psi from theta_l, phi_l."""
+    out = GenParams()
+    ctypes.pointer(out)[0] = params if isinstance(params, GenParams) else gen_params(**params)
+    _io_check(_native.load().gwgpu_transform_orientation_coords(ctypes.byref(out), generation_method.encode()),
+              "transform_orientation_coords")
+    return out
 
 
 def params_array(plist):
@@ -405,6 +417,44 @@ class Context:
                                          _dp(fish), _dp(cov) if cov is not None else None, _ip(status))
         self._check(st, "fisher_batch")
         return fish, cov, status
+
+    def fisher_batch_ex(self, params, method, handles, order=2, epsilon=1e-8, step_mode=0, precision=PREC_FP64,
+                        add_prior=False, covariance=True):
+        """fisher_numerical for many sources summed over the detectors of
+        handles (the first is the reference detector): precision PREC_FP64 runs
+        the reference algorithm (orders 2 and 4), PREC_MIXED the moment form."""
+        parr = params if isinstance(params, ctypes.Array) else params_array(params)
+        n = len(parr)
+        hs = np.ascontiguousarray(handles, dtype=np.int32)
+        fish = np.zeros((n, 11, 11))
+        cov = np.zeros((n, 11, 11)) if covariance else None
+        status = np.zeros(n, dtype=np.int32)
+        opt = FisherOptions(int(method), int(order), float(epsilon), int(step_mode), int(precision), int(add_prior))
+        st = self.lib.gwgpu_fisher_batch_ex(self.h, parr, n, _ip(hs), hs.size, ctypes.byref(opt), _dp(fish),
+                                            _dp(cov) if cov is not None else None, _ip(status))
+        self._check(st, "fisher_batch_ex")
+        return fish, cov, status
+
+    def mcmc_fisher_batch(self, theta, handles, gmst, approximant=IMRPhenomD):
+        """MCMC_fisher_wrapper (mcmc_gw.cpp:2230-2340) at each row of theta (the
+        11-dim MCMC_IMRPhenomD vector): the order-4 network Fisher plus the prior
+        diagonal."""
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        n, dim = th.shape
+        hs = np.ascontiguousarray(handles, dtype=np.int32)
+        fish = np.zeros((n, dim, dim))
+        status = np.zeros(n, dtype=np.int32)
+        st = self.lib.gwgpu_mcmc_fisher_batch(self.h, _dp(th), dim, n, int(approximant), float(gmst), _ip(hs), hs.size,
+                                              _dp(fish), _ip(status))
+        self._check(st, "mcmc_fisher_batch")
+        return fish, status
+
+
+class FisherOptions(ctypes.Structure):
+    """gwgpu_fisher_options."""
+
+    _fields_ = [("method", ctypes.c_int), ("order", ctypes.c_int), ("epsilon", ctypes.c_double),
+                ("step_mode", ctypes.c_int), ("precision", ctypes.c_int), ("add_prior", ctypes.c_int)]
 
 
 class ServerConfig(ctypes.Structure):

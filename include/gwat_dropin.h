@@ -26,6 +26,7 @@ class gen_params_base {
   T chip = -1, phip = -1;
   bool shift_time = true, shift_phase = true, sky_average = false, dep_postmerger = false;
   bool equatorial_orientation = false, horizon_coord = false;
+  T theta_l = 0, phi_l = 0;  // equatorial direction of L, read when equatorial_orientation is set
 };
 class gen_params : public gen_params_base<double> {};
 template <class T>

@@ -30,6 +30,7 @@ extern "C" {
 #define GWGPU_EBUSY 6       /* queue full / resource in use */
 #define GWGPU_ENOTFOUND 7   /* unknown handle or ticket */
 #define GWGPU_ETOOLARGE 8   /* size beyond a fixed maximum */
+#define GWGPU_ESINGULAR 9   /* Fisher matrix not positive definite in FP64: matrix returned, covariance NaN */
 
 /* ---- approximants and precision forms ---- */
 #define GWGPU_IMRPHENOMD 0
@@ -49,7 +50,11 @@ typedef struct gwgpu_server gwgpu_server;
 /* POD mirror of the gen_params_base<double> fields on the path
  * (include/gwat/util.h:121-378).  Solar masses, Mpc, seconds, radians, Hz.
  * chip = -1 selects the full in-plane-spin transform for Pv2
- * (waveform_generator.cpp:1272-1281). */
+ * (waveform_generator.cpp:1272-1281).  equatorial_orientation: the detector
+ * response and the Fisher entry points take the inclination and polarisation
+ * from theta_l, phi_l (the equatorial direction of the orbital angular
+ * momentum), as fourier_detector_response does (waveform_util.cpp:946-948);
+ * the likelihood entry points ignore it, as MCMC_likelihood_extrinsic does. */
 typedef struct {
   double mass1, mass2;
   double spin1[3], spin2[3];
@@ -58,6 +63,8 @@ typedef struct {
   double RA, DEC, psi, gmst;
   double chip, phip;
   int32_t shift_time, shift_phase, sky_average, dep_postmerger;
+  double theta_l, phi_l;
+  int32_t equatorial_orientation, reserved;
 } gwgpu_gen_params;
 
 void gwgpu_default_params(gwgpu_gen_params *p);
@@ -87,6 +94,13 @@ int gwgpu_fourier_waveform(gwgpu_context *ctx, const double *frequencies, int le
 int gwgpu_fourier_detector_response(gwgpu_context *ctx, const double *frequencies, int length, double *response,
                                     const char *detector, const char *generation_method,
                                     const gwgpu_gen_params *params);
+
+/* transform_orientation_coords(gen_params_base<T>*, std::string
+ * generation_method, std::string detector)  (waveform_util.h:229,
+ * waveform_util.cpp:1523-1586) for a ground detector: sets incl_angle and psi
+ * from theta_l, phi_l, RA, DEC (IMRPhenomPv2: psi of the total angular
+ * momentum from chip, phip and the aligned spins).  Host only, no launch. */
+int gwgpu_transform_orientation_coords(gwgpu_gen_params *params, const char *generation_method);
 
 /* ---- data registry (replaces the process-global mcmc_data/mcmc_noise/
  * mcmc_frequencies pointers set at mcmc_gw.cpp:1464-1476) ---- */
@@ -130,9 +144,11 @@ int gwgpu_mcmc_likelihood_extrinsic(gwgpu_context *ctx, const gwgpu_gen_params *
  * `stream` (0: the legacy default stream) and writes log L to the device
  * pointer d_loglik without synchronising.  Its scratch is one fixed device
  * array sized for grids of up to 524,288 bins (4,096 blocks of 128 bins);
- * longer grids return GWGPU_ETOOLARGE.  The first call on a device sets up
- * that array (cudaGetSymbolAddress, module load), so make one call before any
- * stream capture that later calls belong to.  Calls share the array:
+ * longer grids return GWGPU_ETOOLARGE.  Every call looks the array's device
+ * address up again (cudaGetSymbolAddress, which allocates nothing), so the
+ * entry point stays valid across a device reset; the first call on a device
+ * also loads the kernels' module, so make one call before any stream capture
+ * that later calls belong to.  Calls share the array:
  * overlapping calls (several host threads, or work in flight on several
  * streams) race, so issue them in order on one stream.  A request outside the
  * model domain returns GWGPU_EDOMAIN without a launch. */
@@ -277,10 +293,40 @@ int gwgpu_fisher_numerical(gwgpu_context *ctx, const double *frequencies, int le
 /* Batched network Fisher (MCMC_fisher_wrapper summing detectors,
  * mcmc_gw.cpp:2283-2317) for n sources over registered data: fisher[n][dim][dim]
  * and, if covariance != NULL, its FP64 inverse (gsl_cholesky_matrix_invert,
- * util.cpp:857-900).  status[i]: GWGPU_OK, GWGPU_EDOMAIN. */
+ * util.cpp:857-900).  Order 2, the moment form: FP64 waveform differences per
+ * bin, FP32-compensated Gram sums.  A source whose matrix that form cannot
+ * invert is recomputed with the FP64 reference algorithm
+ * (gwgpu_fisher_batch_ex, GWGPU_PREC_FP64).  status[i]: GWGPU_OK,
+ * GWGPU_EDOMAIN, GWGPU_ESINGULAR (not invertible in FP64 either). */
 int gwgpu_fisher_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, int method, const int *handles,
                        int num_detectors, double epsilon, int step_mode, double *fisher, double *covariance,
                        int *status);
+typedef struct {
+  int method;     /* GWGPU_FISHER_IMRPHENOMD or GWGPU_FISHER_MCMC_IMRPHENOMD */
+  int order;      /* 2 (central) or 4 (five-point, fisher.cpp:426-458) */
+  double epsilon; /* step (the reference: 1e-8) */
+  int step_mode;  /* GWGPU_FISHER_STEP_* */
+  int precision;  /* GWGPU_PREC_MIXED: the moment form (order 2 only); GWGPU_PREC_FP64: the reference algorithm */
+  int add_prior;  /* add MCMC_fisher_transformations' prior diagonal (mcmc_gw.cpp:2136-2160) */
+} gwgpu_fisher_options;
+/* fisher_numerical (fisher.h:35-48, fisher.cpp:81-557, 2704-2781) for n
+ * sources, summed over the detectors with the first as reference detector.
+ * GWGPU_PREC_FP64 runs the reference's algorithm itself on the device: every
+ * perturbed response in FP64 (including the constant phase the +-2 eps
+ * responses of the five-point rule carry at a non-reference detector,
+ * fisher.cpp:426-458), derivatives and Simpson Gram sums in FP64. */
+int gwgpu_fisher_batch_ex(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, const int *handles,
+                          int num_detectors, const gwgpu_fisher_options *options, double *fisher, double *covariance,
+                          int *status);
+/* MCMC_fisher_wrapper(double *param, double **output, mcmc_data_interface*,
+ * void*)  (mcmc_gw.h:486, mcmc_gw.cpp:2230-2340) for n sampler positions: the
+ * 11-dim MCMC_IMRPhenomD vector repacked as MCMC_prep_params does (f_ref 20,
+ * the given GMST), fisher_numerical("MCMC_IMRPhenomD", order 4 =
+ * mcmc_deriv_order, mcmc_gw.h:45, epsilon 1e-8) summed over the detectors with
+ * the first as reference, plus the prior diagonal of
+ * MCMC_fisher_transformations.  fisher[n][11][11]; status as above. */
+int gwgpu_mcmc_fisher_batch(gwgpu_context *ctx, const double *theta, int dim, int n, int approximant, double gmst,
+                            const int *handles, int num_detectors, double *fisher, int *status);
 
 /* ---- serving: continuous batching of log-likelihood requests ----
  * The reference serves one chain per host thread (mcmc_sampler.cpp:4585-4590,

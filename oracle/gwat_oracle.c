@@ -134,45 +134,49 @@ static void populate(src_t *s, const gwo_gen_params *in) {
   s->dep_postmerger = in->dep_postmerger;
 }
 
-/* ----------------------------------------------- natural cubic spline (GSL) */
-/* Tridiagonal system of the natural cubic spline, solved by the symmetric
- * LDL^T recurrence (the algorithm of gsl_linalg_solve_symm_tridiag).  c[] holds
- * half the second derivative at each node, c[0] = c[n-1] = 0. */
+/* ------------------------------------------------- natural cubic spline */
+/* The natural cubic spline the reference takes from GSL's "cspline"
+ * (IMRPhenomD.cpp:1190-1217, IMRPhenomP.cpp:595-602); GSL is not part of the
+ * reference, so this is the published algorithm (Burden & Faires, Numerical
+ * Analysis, sec. 3.5): c[i] = S''(x_i)/2, c[0] = c[n-1] = 0, and for the
+ * interior knots h_{i-1} c_{i-1} + 2 (h_{i-1} + h_i) c_i + h_i c_{i+1}
+ * = 3 (s_i - s_{i-1}), s_i the interval slopes.  The symmetric tridiagonal
+ * system is solved by its L D L^T factorisation: a forward sweep (pivots,
+ * multipliers, reduced right-hand side), then back substitution.  The same
+ * arithmetic, in the same order, as the test-only spline of oracle/shim that
+ * the reference's own model code is compiled against. */
 void gwo_cspline_coeffs(const double *x, const double *y, int n, double *c) {
-  int max_index = n - 1, sys = max_index - 1;
-  double *diag = (double *)malloc(sizeof(double) * (size_t)(sys > 0 ? sys : 1) * 6);
-  double *off = diag + sys, *g = off + sys, *gam = g + sys, *alp = gam + sys, *z = alp + sys;
+  const int m = n - 2;
   c[0] = 0.0;
-  c[max_index] = 0.0;
-  for (int i = 0; i < sys; i++) {
-    double h_i = x[i + 1] - x[i], h_ip1 = x[i + 2] - x[i + 1];
-    double yd_i = y[i + 1] - y[i], yd_ip1 = y[i + 2] - y[i + 1];
-    double g_i = (h_i != 0.0) ? 1.0 / h_i : 0.0;
-    double g_ip1 = (h_ip1 != 0.0) ? 1.0 / h_ip1 : 0.0;
-    off[i] = h_ip1;
-    diag[i] = 2.0 * (h_ip1 + h_i);
-    g[i] = 3.0 * (yd_ip1 * g_ip1 - yd_i * g_i);
-  }
-  if (sys == 1) {
-    c[1] = g[0] / diag[0];
-  } else if (sys > 1) {
-    int N = sys;
-    alp[0] = diag[0];
-    gam[0] = off[0] / alp[0];
-    for (int i = 1; i < N - 1; i++) {
-      alp[i] = diag[i] - off[i - 1] * gam[i - 1];
-      gam[i] = off[i] / alp[i];
+  c[n - 1] = 0.0;
+  if (m < 1) return;
+  double *piv = (double *)malloc(sizeof(double) * (size_t)m * 3);
+  double *mul = piv + m, *rhs = mul + m;
+  double h_left = x[1] - x[0];
+  double s_left = (y[1] - y[0]) * (h_left != 0.0 ? 1.0 / h_left : 0.0);
+  for (int k = 0; k < m; k++) {
+    const double h_right = x[k + 2] - x[k + 1];
+    const double s_right = (y[k + 2] - y[k + 1]) * (h_right != 0.0 ? 1.0 / h_right : 0.0);
+    const double diag = 2.0 * (h_right + h_left), load = 3.0 * (s_right - s_left);
+    if (k == 0) {
+      piv[0] = diag;
+      rhs[0] = load;
+    } else {
+      piv[k] = diag - h_left * mul[k - 1];
+      rhs[k] = load - mul[k - 1] * rhs[k - 1];
     }
-    alp[N - 1] = diag[N - 1] - off[N - 2] * gam[N - 2];
-    z[0] = g[0];
-    for (int i = 1; i < N; i++) z[i] = g[i] - gam[i - 1] * z[i - 1];
-    for (int i = 0; i < N; i++) z[i] = z[i] / alp[i];
-    c[1 + N - 1] = z[N - 1];
-    for (int i = N - 2; i >= 0; i--) c[1 + i] = z[i] - gam[i] * c[1 + i + 1];
+    if (k < m - 1) mul[k] = h_right / piv[k];
+    h_left = h_right;
+    s_left = s_right;
   }
-  free(diag);
+  c[m] = rhs[m - 1] / piv[m - 1];
+  for (int k = m - 2; k >= 0; k--) c[k + 1] = rhs[k] / piv[k] - mul[k] * c[k + 2];
+  free(piv);
 }
 
+/* S (deriv 0) or S' (deriv 1): on [x_i, x_{i+1}], S = y_i + b t + c_i t^2 + d t^3,
+ * b = s_i - h_i (c_{i+1} + 2 c_i)/3, d = (c_{i+1} - c_i)/(3 h_i); outside the
+ * knots NaN (GSL_EDOM). */
 double gwo_cspline_eval(const double *x, const double *y, const double *c, int n, double xv, int deriv) {
   if (!(xv >= x[0] && xv <= x[n - 1])) return NAN; /* GSL_EDOM */
   int ilo = 0, ihi = n - 1;
@@ -1276,8 +1280,13 @@ static int fisher_unpack(double *v, int *logf, const gwo_gen_params *p, int meth
   double mc = calc_chirpmass(p->mass1, p->mass2), eta = calc_eta(p->mass1, p->mass2);
   v[0] = p->RA;
   v[1] = mcmc ? sin(p->DEC) : p->DEC;
-  v[2] = p->psi;
-  v[3] = mcmc ? cos(p->incl_angle) : p->incl_angle;
+  if (p->equatorial_orientation) { /* L's equatorial angles in place of psi, iota (fisher.cpp:1916-1919, 1944-1947) */
+    v[2] = p->theta_l;
+    v[3] = p->phi_l;
+  } else {
+    v[2] = p->psi;
+    v[3] = mcmc ? cos(p->incl_angle) : p->incl_angle;
+  }
   v[4] = p->phiRef;
   v[5] = p->tc;
   if (mcmc) {
@@ -1329,22 +1338,27 @@ static void fisher_repack(const double *v, gwo_gen_params *o, const gwo_gen_para
   o->shift_time = 0;
   o->shift_phase = in->shift_phase;
   o->dep_postmerger = in->dep_postmerger;
+  o->equatorial_orientation = in->equatorial_orientation;
   int mcmc = (method == 1 || method == 3);
   if (mcmc) {
     o->mass1 = calc_mass1(exp(v[7]), v[8]);
     o->mass2 = calc_mass2(exp(v[7]), v[8]);
     o->Luminosity_Distance = exp(v[6]);
     o->DEC = asin(v[1]);
-    o->incl_angle = acos(v[3]);
   } else {
     o->mass1 = calc_mass1(v[7], v[8]);
     o->mass2 = calc_mass2(v[7], v[8]);
     o->Luminosity_Distance = v[6];
     o->DEC = v[1];
-    o->incl_angle = v[3];
+  }
+  if (in->equatorial_orientation) { /* psi and iota follow from the transform at the response (fisher.cpp:2242-2245) */
+    o->theta_l = v[2];
+    o->phi_l = v[3];
+  } else {
+    o->psi = v[2];
+    o->incl_angle = mcmc ? acos(v[3]) : v[3];
   }
   o->RA = v[0];
-  o->psi = v[2];
   o->phiRef = v[4];
   o->tc = v[5];
   if (method == 3) {

@@ -35,7 +35,7 @@ typedef struct {
   /* equatorial spherical angles of the orbital angular momentum, read when
    * equatorial_orientation is set (util.h:166-172) */
   double theta_l, phi_l;
-  int equatorial_orientation, pad_;
+  int equatorial_orientation, reserved;
 } gwo_gen_params;
 
 void gwo_default_params(gwo_gen_params *p);

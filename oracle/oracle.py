@@ -34,7 +34,7 @@ class GenParams(ctypes.Structure):
         ("shift_time", ctypes.c_int), ("shift_phase", ctypes.c_int),
         ("sky_average", ctypes.c_int), ("dep_postmerger", ctypes.c_int),
         ("theta_l", ctypes.c_double), ("phi_l", ctypes.c_double),
-        ("equatorial_orientation", ctypes.c_int), ("pad_", ctypes.c_int),
+        ("equatorial_orientation", ctypes.c_int), ("reserved", ctypes.c_int),
     ]
 
 

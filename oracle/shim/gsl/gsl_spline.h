@@ -14,34 +14,43 @@ static inline gsl_spline *gsl_spline_alloc(const gsl_interp_type *T, size_t n) {
   return s;
 }
 static inline void gsl_spline_free(gsl_spline *s) { if (!s) return; free(s->x); free(s->y); free(s->c); free(s); }
-/* natural spline: symmetric tridiagonal system, LDL^T recurrence */
+/* Natural cubic spline (Burden & Faires, Numerical Analysis, sec. 3.5):
+ * c[i] = S''(x_i)/2 with c[0] = c[n-1] = 0 from the symmetric tridiagonal
+ * system of the interior knots, h_{i-1} c_{i-1} + 2 (h_{i-1} + h_i) c_i +
+ * h_i c_{i+1} = 3 (s_i - s_{i-1}), solved by L D L^T: a forward sweep, then
+ * back substitution.  The same arithmetic, in the same order, as
+ * gwo_cspline_coeffs in oracle/gwat_oracle.c. */
 static inline int gsl_spline_init(gsl_spline *s, const double *xa, const double *ya, size_t n) {
-  memcpy(s->x, xa, n * sizeof(double)); memcpy(s->y, ya, n * sizeof(double));
+  memcpy(s->x, xa, n * sizeof(double));
+  memcpy(s->y, ya, n * sizeof(double));
   if (s->T->kind == 0) return 0;
-  size_t max_index = n - 1, sys = max_index - 1;
-  double *w = (double *)calloc(6 * (sys > 0 ? sys : 1), sizeof(double));
-  double *diag = w, *off = w + sys, *g = w + 2 * sys, *gam = w + 3 * sys, *alp = w + 4 * sys, *z = w + 5 * sys;
   double *c = s->c;
-  c[0] = 0.0; c[max_index] = 0.0;
-  for (size_t i = 0; i < sys; i++) {
-    double h_i = xa[i + 1] - xa[i], h_ip1 = xa[i + 2] - xa[i + 1];
-    double yd_i = ya[i + 1] - ya[i], yd_ip1 = ya[i + 2] - ya[i + 1];
-    double g_i = (h_i != 0.0) ? 1.0 / h_i : 0.0, g_ip1 = (h_ip1 != 0.0) ? 1.0 / h_ip1 : 0.0;
-    off[i] = h_ip1; diag[i] = 2.0 * (h_ip1 + h_i); g[i] = 3.0 * (yd_ip1 * g_ip1 - yd_i * g_i);
+  const long m = (long)n - 2;
+  c[0] = 0.0;
+  c[n - 1] = 0.0;
+  if (m < 1) return 0;
+  double *piv = (double *)calloc(3 * (size_t)m, sizeof(double));
+  double *mul = piv + m, *rhs = mul + m;
+  double h_left = xa[1] - xa[0];
+  double s_left = (ya[1] - ya[0]) * (h_left != 0.0 ? 1.0 / h_left : 0.0);
+  for (long k = 0; k < m; k++) {
+    const double h_right = xa[k + 2] - xa[k + 1];
+    const double s_right = (ya[k + 2] - ya[k + 1]) * (h_right != 0.0 ? 1.0 / h_right : 0.0);
+    const double diag = 2.0 * (h_right + h_left), load = 3.0 * (s_right - s_left);
+    if (k == 0) {
+      piv[0] = diag;
+      rhs[0] = load;
+    } else {
+      piv[k] = diag - h_left * mul[k - 1];
+      rhs[k] = load - mul[k - 1] * rhs[k - 1];
+    }
+    if (k < m - 1) mul[k] = h_right / piv[k];
+    h_left = h_right;
+    s_left = s_right;
   }
-  if (sys == 1) { c[1] = g[0] / diag[0]; }
-  else if (sys > 1) {
-    size_t N = sys;
-    alp[0] = diag[0]; gam[0] = off[0] / alp[0];
-    for (size_t i = 1; i < N - 1; i++) { alp[i] = diag[i] - off[i - 1] * gam[i - 1]; gam[i] = off[i] / alp[i]; }
-    alp[N - 1] = diag[N - 1] - off[N - 2] * gam[N - 2];
-    z[0] = g[0];
-    for (size_t i = 1; i < N; i++) z[i] = g[i] - gam[i - 1] * z[i - 1];
-    for (size_t i = 0; i < N; i++) z[i] = z[i] / alp[i];
-    c[N] = z[N - 1];
-    for (long i = (long)N - 2; i >= 0; i--) c[1 + i] = z[i] - gam[i] * c[1 + i + 1];
-  }
-  free(w);
+  c[m] = rhs[m - 1] / piv[m - 1];
+  for (long k = m - 2; k >= 0; k--) c[k + 1] = rhs[k] / piv[k] - mul[k] * c[k + 2];
+  free(piv);
   return 0;
 }
 static inline size_t gwo_bsearch(const double *x, double xv, size_t lo, size_t hi) {

@@ -234,3 +234,35 @@ extern "C" int gwh_fisher_batch(const GenParams *p, int method, const double *fr
   if (cov) return chol_invert(out, cov, kDim) ? 9 : 0;
   return 0;
 }
+
+// Each intrinsic pair's per-bin complex difference as fisher_bin_q forms it
+// (the polynomial-difference fast path, its series in the half phase step, the
+// one-sided and beyond-the-cut cases) against fisher_q_exact, which takes the
+// pair's two waveforms bin by bin.  maxerr[q] = max_k |q_fast - q_exact| /
+// max_k |q_exact| over every bin of the grid, region boundaries included.
+extern "C" int gwh_fisher_pair_check(const GenParams *p, int method, double df, int n0, int N, double epsilon,
+                                     int step_mode, double *maxerr) {
+  using namespace gwf;
+  int dets[1] = {0};
+  std::vector<SlotOut> slots(kSlots);
+  for (int s = 0; s < kSlots; s++) fisher_slot(*p, s, method, dets, 1, df, epsilon, step_mode, qnm(), slots[s]);
+  FisherSrc F;
+  int st = fisher_setup(*p, method, 1, epsilon, step_mode, slots.data(), F);
+  if (st) return st;
+  double emax[kIntr] = {0, 0, 0, 0}, qmax[kIntr] = {0, 0, 0, 0};
+  for (int k = 0; k < N; k++) {
+    const int n = n0 + k;
+    const double x = n, t = std::cbrt(x), r = std::pow(x, -5. / 3.), lnn = std::log(x), t34 = std::pow(x, 0.75);
+    const double m76 = std::pow(x, -7. / 6.);
+    float a0, qr[kIntr], qi[kIntr];
+    if (!fisher_bin_q(F, n, t, r, lnn, t34, m76, (float)m76, a0, qr, qi)) continue;
+    for (int q = 0; q < kIntr; q++) {
+      float er, ei;
+      fisher_q_exact(F, q, n, t, r, lnn, t34, m76, er, ei);
+      emax[q] = std::max(emax[q], std::hypot((double)qr[q] - er, (double)qi[q] - ei));
+      qmax[q] = std::max(qmax[q], std::hypot((double)er, (double)ei));
+    }
+  }
+  for (int q = 0; q < kIntr; q++) maxerr[q] = qmax[q] > 0 ? emax[q] / qmax[q] : 0.0;
+  return 0;
+}

@@ -48,3 +48,42 @@ def test_dropin_library_exports_reference_signatures():
                  "allocate_LOSC_data(std::", "read_LOSC_data_file(std::", "read_LOSC_PSD_file(std::",
                  "populate_noise(double*", "count_lines_LOSC_data_file(std::"):
         assert name in out, name
+
+
+def test_orientation_transform_host_code(oracle):
+    """gwgpu_transform_orientation_coords (host code, no launch) against the
+    oracle's transform_orientation_coords, which is pinned bit for bit to the
+    reference's (tests/test_oracle_pins.py)."""
+    import numpy as np
+    import gw_analysis_tools_gb300 as G
+    from gw_analysis_tools_gb300 import workloads as W
+    rng = np.random.Generator(np.random.PCG64(5))
+    for ap, name, prec in ((0, "IMRPhenomD", False), (1, "IMRPhenomPv2", True)):
+        for d in W.prior_draws(16, 6, precessing=prec):
+            d = dict(d, theta_l=float(np.arccos(rng.uniform(-1, 1))), phi_l=float(rng.uniform(0, 2 * np.pi)),
+                     equatorial_orientation=1)
+            if prec and rng.uniform() < 0.5:
+                d.update(chip=float(rng.uniform(0.1, 0.7)), phip=float(rng.uniform(0, 2 * np.pi)))
+            want = oracle.transform_orientation_coords(oracle.params_from_dict(d), ap)
+            got = G.transform_orientation_coords(G.gen_params(**d), name)
+            assert abs(got.psi - want.psi) <= 1e-12 and abs(got.incl_angle - want.incl_angle) <= 1e-12
+
+
+def test_dropin_compiles_against_reference_headers(oracle):
+    """gwat_dropin.cpp compiled with the reference's own headers
+    (GWAT_DROPIN_USE_REFERENCE_HEADERS) against oracle/shim: the drop-in's
+    definitions match the reference declarations they replace."""
+    import shutil
+    import subprocess
+    import pytest
+    ref = oracle.reference_dir()
+    if ref is None or shutil.which("g++") is None:
+        pytest.skip("reference headers not present")
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    src = os.path.join(root, "gw_analysis_tools_gb300", "dropin", "gwat_dropin.cpp")
+    cmd = ["g++", "-std=c++17", "-fsyntax-only", "-w", "-DGWAT_DROPIN_USE_REFERENCE_HEADERS",
+           "-include", "util.h", "-include", "waveform_generator.h", "-include", "mcmc_gw.h",
+           "-I", os.path.join(root, "oracle", "shim"), "-I", os.path.join(ref, "include", "gwat"), src]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]

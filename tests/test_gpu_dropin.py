@@ -58,3 +58,36 @@ def test_mcmc_likelihood_extrinsic_dropin(oracle, served):
             assert abs(ll - ref) <= MIXED_TOL, (ll, ref)
         else:
             assert abs(ll - ref) <= FP64_RTOL * max(1.0, abs(ref)), (ll, ref)
+
+
+def test_served_dropin_threads_two_segment_lengths(oracle):
+    """Concurrent callers in served mode with two grid lengths, so two values of
+    the reference's T: one server per T, none freed while another thread uses
+    it (the drop-in keeps every server until the process exits)."""
+    from concurrent.futures import ThreadPoolExecutor
+    fn = _dropin()
+    dets = list(workloads.DETECTORS3)
+    src = workloads.config1_source()
+    cases = []
+    for hi in (300.0, 400.0):
+        f = np.ascontiguousarray(workloads.uniform_grid(20.0, hi, 1.0 / 8.0))
+        injp = oracle.params_from_dict(dict(src, tc=8.0 - src["tc"]))
+        psd = [np.ascontiguousarray(workloads.analytic_psd(f))] * 3
+        data = [np.ascontiguousarray(oracle.detector_response(f, injp, d) + workloads.noise(f, 60 + i))
+                for i, d in enumerate(dets)]
+        cases.append((f, data, psd))
+    draws = workloads.perturbed(src, 24, seed=12)
+    jobs = [(k % 2, draws[k]) for k in range(len(draws))]
+
+    def run(job):
+        g, q = job
+        f, data, psd = cases[g]
+        return _call(fn, f, data, psd, dets, engine.gen_params(**q), 1)
+
+    with ThreadPoolExecutor(8) as ex:
+        got = list(ex.map(run, jobs * 3))
+    errs = []
+    for (g, q), (ll, tc) in zip(jobs * 3, got):
+        f, data, psd = cases[g]
+        errs.append(abs(ll - oracle.loglik(oracle.params_from_dict(q), f, dets, data, psd, T_segment=tc[1])))
+    assert max(errs) <= MIXED_TOL, max(errs)

@@ -24,7 +24,14 @@ def test_plain_fisher_numerical(gpu_ctx, oracle):
             assert _norm_err(got, ref) <= 1e-4
 
 
+def _inv_err(C, R):
+    return np.max(np.abs(C - R) / np.sqrt(np.abs(np.outer(np.diag(R), np.diag(R)))))
+
+
 def test_batched_fisher_network(gpu_ctx, oracle):
+    """The moment form (FP32-compensated Gram sums) against the FP64 oracle on
+    all 16 sources: the Fisher matrix and its inverse, each normalised by the
+    oracle's diagonal."""
     f = W.uniform_grid(10.0, 2048.0, 1 / 16.)
     dets = list(W.DETECTORS3)
     psd = W.analytic_psd(f)
@@ -32,13 +39,86 @@ def test_batched_fisher_network(gpu_ctx, oracle):
     draws = W.prior_draws(16, 83)
     fish, cov, st = gpu_ctx.fisher_batch(G.params_array(draws), 0, hs, epsilon=1e-6, step_mode=1)
     assert np.all(st == 0)
-    for i in range(4):
+    for i in range(len(draws)):
         ref = oracle.fisher_network(f, oracle.params_from_dict(draws[i]), dets, [psd] * 3, epsilon=1e-6,
                                     step_mode=1)
         assert _norm_err(fish[i], ref) <= 1e-5
         assert np.allclose(fish[i], fish[i].T)
-        # the inverse is the inverse of the returned matrix
-        ident = cov[i] @ fish[i]
-        assert np.max(np.abs(ident - np.eye(11))) < 1e-4
+        ist, rinv = oracle.cholesky_invert(ref)
+        assert ist == 0
+        # the inverse's error is the matrix's error in its weakest direction
+        # times the condition number of the normalised matrix (1e5-1e8 here)
+        cond = np.linalg.cond(ref / np.sqrt(np.outer(np.diag(ref), np.diag(ref))))
+        assert _inv_err(cov[i], rinv) <= 2e-9 * cond, (i, cond, _inv_err(cov[i], rinv))
+    for h in hs:
+        gpu_ctx.release_data(h)
+
+
+def test_batched_fisher_refines_singular_sources(gpu_ctx, oracle):
+    """Sources whose matrix the FP32-compensated sums leave indefinite (equal
+    masses, a face-on orientation) are recomputed by the FP64 reference
+    algorithm: status OK and the oracle's matrix."""
+    f = W.uniform_grid(10.0, 2048.0, 1 / 16.)
+    dets = list(W.DETECTORS3)
+    psd = W.analytic_psd(f)
+    hs = [gpu_ctx.register_data(d, f, np.zeros(f.size, complex), psd) for d in dets]
+    pool = W.prior_draws(10000, 13)
+    draws = [pool[i] for i in (228, 3139, 4213, 6593, 8425, 4968)] + W.prior_draws(6, 84)
+    fish, cov, st = gpu_ctx.fisher_batch(G.params_array(draws), 0, hs, epsilon=1e-6, step_mode=1)
+    for i, d in enumerate(draws):
+        ref = oracle.fisher_network(f, oracle.params_from_dict(d), dets, [psd] * 3, epsilon=1e-6, step_mode=1)
+        # near-degenerate sources: the FP64 rounding of two implementations,
+        # divided by steps of 1e-6 of parameters near zero
+        assert _norm_err(fish[i], ref) <= 1e-4, i
+        ist, _ = oracle.cholesky_invert(ref)
+        assert st[i] == (0 if ist == 0 else 9), (i, st[i], ist)
+    for h in hs:
+        gpu_ctx.release_data(h)
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_fisher_reference_algorithm(gpu_ctx, oracle, order):
+    """gwgpu_fisher_batch_ex in FP64: the reference algorithm on the device,
+    both parameterisations, orders 2 and 4 (the five-point rule keeps the
+    reference's constant phase on the +-2 eps responses of a non-reference
+    detector), against the oracle's network Fisher."""
+    f = W.uniform_grid(10.0, 1024.0, 1 / 8.)
+    dets = list(W.DETECTORS3)
+    psd = W.analytic_psd(f)
+    hs = [gpu_ctx.register_data(d, f, np.zeros(f.size, complex), psd) for d in dets]
+    draws = W.prior_draws(12, 85)
+    for method, name in ((0, "IMRPhenomD"), (1, "MCMC_IMRPhenomD")):
+        # FP64 rounding differences of two implementations, divided by the step
+        # (1e-6 relative: steps of parameters near zero -- sin DEC, cos iota,
+        # spins -- are far below 1e-6)
+        for eps, mode, tol in ((1e-6, 1, 1e-4), (1e-8, 0, 3e-4)):
+            fish, cov, st = gpu_ctx.fisher_batch_ex(G.params_array(draws), method, hs, order=order, epsilon=eps,
+                                                    step_mode=mode, precision=G.PREC_FP64)
+            for i, d in enumerate(draws):
+                ref = oracle.fisher_network(f, oracle.params_from_dict(d), dets, [psd] * 3, method=name, order=order,
+                                            epsilon=eps, step_mode=mode)
+                assert _norm_err(fish[i], ref) <= tol, (name, eps, i, _norm_err(fish[i], ref))
+                ist, rinv = oracle.cholesky_invert(ref)
+                assert st[i] == (0 if ist == 0 else 9)
+                if ist == 0 and eps == 1e-6:
+                    cond = np.linalg.cond(ref / np.sqrt(np.outer(np.diag(ref), np.diag(ref))))
+                    assert _inv_err(cov[i], rinv) <= 2e-11 * cond * (3 if order == 4 else 1), (i, cond)
+    for h in hs:
+        gpu_ctx.release_data(h)
+
+
+def test_mcmc_fisher_proposal_golden(gpu_ctx):
+    """gwgpu_mcmc_fisher_batch against the reference's own MCMC_fisher_wrapper
+    output (order 4, MCMC_IMRPhenomD, prior diagonal) stored in the golden
+    fixture, on the fixture's data and positions."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_glue.npz"))
+    f, psd = g["freqs"], g["psd"]
+    dets = list(W.DETECTORS3)
+    hs = [gpu_ctx.register_data(d, f, g["data"][i], psd) for i, d in enumerate(dets)]
+    fish, st = gpu_ctx.mcmc_fisher_batch(g["wrapper_pos_d"], hs, float(g["wrapper_gmst"]))
+    assert np.all(st == 0)
+    for got, want in zip(fish, g["wrapper_fisher_d"]):
+        assert _norm_err(got, want) <= 1e-4
     for h in hs:
         gpu_ctx.release_data(h)

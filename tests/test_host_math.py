@@ -114,3 +114,37 @@ def test_host_batched_fisher_algebra_matches_oracle(oracle, hostcheck):
             G = out.reshape(11, 11)
             rel = np.abs(G - ref) / np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
             assert rel.max() <= tol, (eps, rel.max())
+
+
+def test_fisher_pair_differences_every_bin(hostcheck):
+    """The batched Fisher's per-bin intrinsic differences (the
+    coefficient-difference polynomials, fisher_phase_deriv / fisher_amp_deriv
+    and their series in the half phase step) against the pair's two waveforms
+    taken bin by bin, over every bin of the benchmark grid: across the
+    inspiral / intermediate / ringdown boundaries of both waveforms, past the
+    cut f = 0.2/M, one-sided pairs at eta = 1/4, both step rules."""
+    import ctypes
+    import numpy as np
+    import gw_analysis_tools_gb300 as G
+    from gw_analysis_tools_gb300 import workloads as W
+    fn = hostcheck.gwh_fisher_pair_check
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                   ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    df, n0, N = 1.0 / 16, 160, 32608
+    pool = W.prior_draws(10000, 13)
+    draws = W.prior_draws(24, 91) + [pool[i] for i in (228, 284, 4213, 6931)]
+    draws.append(dict(W.config1_source(), mass1=30.0, mass2=30.0))  # eta = 1/4: one-sided pair
+    worst = {1: 0.0, 0: 0.0}
+    for d in draws:
+        for method in (0, 1):
+            for eps, mode in ((1e-6, 1), (1e-8, 0)):
+                e = (ctypes.c_double * 4)()
+                assert fn(ctypes.byref(G.gen_params(**d)), method, df, n0, N, eps, mode, e) == 0
+                worst[mode] = max(worst[mode], max(e))
+    # relative steps: FP32 results of FP64 differences, a few ulp of the
+    # pair's largest value.  The reference's 1e-8 absolute step moves M_c by
+    # ~3e-10 of itself, so the two-waveform difference used as the yardstick
+    # carries its own rounding, ~1e-16 |Phi| over a phase step of ~1e-6 rad.
+    assert worst[1] <= 3e-6, worst
+    assert worst[0] <= 2e-5, worst

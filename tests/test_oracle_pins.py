@@ -190,7 +190,9 @@ def test_glue_bit_exact_against_reference_build(oracle):
             got = oracle.loglik(oracle.params_from_dict(dict(d, equatorial_orientation=0)), f, dets, data, [psd] * 3,
                                 approximant=ap, T_segment=T)
             assert got == ll
-    for d in W.prior_draws(2, 43):
+    oriented = [dict(d, theta_l=0.4 + 0.3 * k, phi_l=1.0 + 1.7 * k, equatorial_orientation=1)
+                for k, d in enumerate(W.prior_draws(2, 44))]
+    for d in W.prior_draws(2, 43) + oriented:
         for method in ("IMRPhenomD", "MCMC_IMRPhenomD"):
             for order in (2, 4):
                 p = oracle.params_from_dict(d)
