@@ -627,12 +627,14 @@ def secondary_parity(ex, res):
             ref[idx] = O.loglik_batch([O.params_from_dict(pu[i]) for i in idx], fu, dets, udata[T],
                                       [W.analytic_psd(fu)] * 3, approximants=[O.IMRPhenomPv2] * len(idx))
         st = parity_stats(got, ref, 1e-3)
-        st["max_abs_dlogL_T128"] = float(np.max(np.abs(got - ref)[np.array(Ts) == 128]))
+        if 128 in Ts:
+            st["max_abs_dlogL_T128"] = float(np.max(np.abs(got - ref)[np.array(Ts) == 128]))
         st["max_abs_logL"] = float(np.max(np.abs(ref)))
         out["uneven_pv2"] = st
     if "_parity_maximized" in ex:
         for name, (draws, ap, got) in ex.pop("_parity_maximized").items():
-            ref = [O.maximized_loglik_intrinsic(d, res["f"], res["data"], [res["psd"]] * 3, ap) for d in draws]
+            ref = [O.maximized_loglik_intrinsic(params_dict(d), res["f"], res["data"], [res["psd"]] * 3, ap)
+                   for d in draws]
             out["maximized_" + name] = parity_stats(got, ref, 1e-9, rel=True)
     if "_parity_gaussleg" in ex:
         parr, fg, wg, dg, psd_g, got = ex.pop("_parity_gaussleg")
@@ -643,6 +645,17 @@ def secondary_parity(ex, res):
                 setattr(op, k, getattr(parr[i], k))
             ref.append(O.loglik_gl(op, fg, dets, dg, [psd_g] * 3, [wg] * 3, T_segment=8.0))
         out["gaussleg_fp64"] = parity_stats(got, ref, 1e-9, rel=True)
+    return out
+
+
+def params_dict(p):
+    """A parameter dict of a gen-params structure (or the dict itself)."""
+    if isinstance(p, dict):
+        return p
+    out = {}
+    for k, _ in p._fields_:
+        v = getattr(p, k)
+        out[k] = tuple(v) if k in ("spin1", "spin2") else v
     return out
 
 

@@ -371,6 +371,13 @@ static int register_stream(gwgpu_context *c, const char *detector, const double 
     for (size_t i = 0; i < 8 * (size_t)N; i++) hsh = (hsh ^ wb[i]) * 1099511628211ull;
   }
   s.psd_hash = hsh ^ (uint64_t)N;
+  {  // the weights follow from the PSD, the integration rule and the grid
+    uint64_t gk = s.psd_hash;
+    const double gv[3] = {d.simpson_df, d.df, (double)d.n0};
+    const unsigned char *gb = (const unsigned char *)gv;
+    for (size_t i = 0; i < sizeof(gv); i++) gk = (gk ^ gb[i]) * 1099511628211ull;
+    s.dev.wkey = gk;
+  }
   if (d.uniform_int) {
     st = c->ensure_tables(d.n0 + N);
     if (st) return st;

@@ -281,11 +281,14 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
     if (want_mixed) {
       if (!s0.uniform_int) st = st ? st : 1;
       double ds[kMaxDet], ws[kMaxDet];
+      unsigned long long wk[kMaxDet];
       for (int d = 0; d < ndet; d++) {
         ds[d] = streams[handles[i * ndet + d]].dscale;
         ws[d] = streams[handles[i * ndet + d]].wscale;
+        wk[d] = streams[handles[i * ndet + d]].wkey;
       }
       mixed_prologue(r, s0.df, mreq[i], ds, ws);
+      mixed_fold_shared_weights(mreq[i], wk, ndet);
     }
   } else {
     st = 4;
@@ -327,6 +330,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   __shared__ AmpConn s_ac[kCoopReq];
   __shared__ PhaseConnParts s_pc[kCoopReq];
   __shared__ double s_ds[kCoopReq][kMaxDet], s_ws[kCoopReq][kMaxDet];  // stream scales of the mixed form
+  __shared__ unsigned long long s_wk[kCoopReq][kMaxDet];                 // and weight keys
   __shared__ double s_shift[kCoopReq][kPv2ShiftNodes];
   __shared__ double s_df[kCoopReq];
   __shared__ int s_st[kCoopReq], s_bad[kCoopReq], s_uni[kCoopReq];
@@ -387,6 +391,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
         const int dd = sd.det;
         s_ds[lane][d] = sd.dscale;
         s_ws[lane][d] = sd.wscale;
+        s_wk[lane][d] = sd.wkey;
         antenna_trig(dd, tr, r.det[d].fp, r.det[d].fc);
         r.det[d].tau = -dtoa_trig(tr, d0, dd) * (2 * kPi);
       }
@@ -492,6 +497,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
           mixed_det_phase(r, s_df[lane], mreq[i]);
           mixed_det_factors(r, mreq[i], s_ds[lane], s_ws[lane]);
         }
+        mixed_fold_shared_weights(mreq[i], s_wk[lane], ndet);
       }
     } else {
       st = 4;
@@ -642,6 +648,7 @@ __global__ void __launch_bounds__(kBatchBlock, MIXED ? 3 : 2) k_batch(const Batc
           kcut = I.k0;
         }
         const bool pv2 = x.approximant == kPhenomPv2;
+        const bool wsh = x.wshared != 0;  // one weight stream for every detector
         const gwt::Tables &tb = a.tables;
         // this thread's offset rotations (read back only by this thread)
 #pragma unroll
@@ -718,7 +725,7 @@ __global__ void __launch_bounds__(kBatchBlock, MIXED ? 3 : 2) k_batch(const Batc
                 float2 v = __ldg(((const float2 *)dh[d]) + k);
                 dre[d] = v.x;
                 dim[d] = v.y;
-                w[d] = __ldg(wh[d] + k);
+                w[d] = (d == 0 || !wsh) ? __ldg(wh[d] + k) : 0.0f;
               }
               float rc[NDET], rs[NDET];
 #pragma unroll
@@ -726,7 +733,8 @@ __global__ void __launch_bounds__(kBatchBlock, MIXED ? 3 : 2) k_batch(const Batc
                 const float2 ra = s_rot_seg[sg * NDET + d], rb = s_rot_off[d * kBatchBlock + tid];
                 cmulf(ra.x, ra.y, rb.x, rb.y, rc[d], rs[d]);
               }
-              mixed_bin_q<NDET>(x, n, ph, al, __ldg(tb.t13f + n), __ldg(tb.tm76f + n), dre, dim, w, rc, rs, acc);
+              mixed_bin_q<NDET>(x, n, ph, al, __ldg(tb.t13f + n), __ldg(tb.tm76f + n), dre, dim, w, rc, rs, acc,
+                                wsh);
             }
           }
           __syncthreads();  // the node and fit buffers are reused by the next chunk

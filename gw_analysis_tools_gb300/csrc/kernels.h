@@ -28,6 +28,9 @@ struct StreamDev {
   // integration weights of the GAUSSLEG branch (mcmc_gw.cpp:820-862), times 4
   // and f ln 10 for log10F; null for Simpson's rule (util.h:844-856)
   const double *iw;
+  // content key of the whitening weights (what, wscale): streams with equal
+  // keys have identical weights (same grid, PSD and integration rule)
+  unsigned long long wkey;
 };
 
 struct Item {

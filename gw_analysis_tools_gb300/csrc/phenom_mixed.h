@@ -51,7 +51,8 @@ constexpr int kAccPerDet = 5;  // D uses 3 (hh, zr, zi); Pv2 uses 5 (spp, scc, s
 constexpr float kSegFScale = 268435456.0f;  // FP32 part of a segment phase polynomial: turns * 2^28
 
 struct MixedReq {
-  int approximant, status, ndet, pad;
+  int approximant, status, ndet;
+  int wshared;  // every detector has the same whitening weights: the weighted |h|^2 sums are kept for detector 0 only
   int n_f1, n_f3, n_f1p, n_f2p, n_cut;  // region starts (first n in region) and last non-zero n
   int n_mid, n_rd, n_c, pad2;
   double A_scale;                       // amplitude scale applied in FP64
@@ -496,6 +497,21 @@ GW_HD void mixed_det_factors_a(const Request &r, MixedReq &x, double A, const do
   for (int d = r.ndet; d < kMaxDet; d++)
     for (int j = 0; j < kAccPerDet; j++) x.fc[d * kAccPerDet + j] = 0.0;
 }
+// Detectors whose whitening weights are the same array (the same PSD on the
+// same grid) have the same weighted |h|^2 sums: their HH factors are added to
+// detector 0's and the bin kernels accumulate those sums once (wshared).
+GW_HD void mixed_fold_shared_weights(MixedReq &x, const unsigned long long *wkey, int ndet) {
+  bool same = ndet > 1;
+  for (int d = 1; d < ndet; d++) same = same && wkey[d] == wkey[0];
+  x.wshared = same ? 1 : 0;
+  if (!same) return;
+  const int nh = x.approximant == kPhenomPv2 ? 3 : 1;  // the weighted sums: D |h|^2; Pv2 |h+|^2, |hx|^2, h+ hx*
+  for (int d = 1; d < ndet; d++)
+    for (int j = 0; j < nh; j++) {
+      x.fc[j] += x.fc[d * kAccPerDet + j];
+      x.fc[d * kAccPerDet + j] = 0.0;
+    }
+}
 GW_HD void mixed_det_factors(const Request &r, MixedReq &x, const double *dscale, const double *wscale) {
   mixed_det_factors_a(r, x, x.A_scale, dscale, wscale);
 }
@@ -777,7 +793,8 @@ GW_HD void cmulf(float ac, float as, float bc, float bs, float &c, float &s) {
 // of ph and that rotation.
 template <int NDET>
 GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float tf, float m76, const float *dre,
-                       const float *dim, const float *w, const float *rotc, const float *rots, KSum *acc) {
+                       const float *dim, const float *w, const float *rotc, const float *rots, KSum *acc,
+                       bool wshared) {
   if (n > x.n_cut) return;
   float a = mixed_amp(x, n, tf, m76);
   float sp, cp;
@@ -789,7 +806,7 @@ GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float
       float sn, cs;
       cmulf(cp, sp, rotc[d], rots[d], cs, sn);
       float ar = a * dre[d], ai = a * dim[d];
-      kadd(acc[d * kAccPerDet + 0], w[d] * aa);
+      if (d == 0 || !wshared) kadd(acc[d * kAccPerDet + 0], w[d] * aa);
       kadd(acc[d * kAccPerDet + 1], ar * cs - ai * sn);
       kadd(acc[d * kAccPerDet + 2], ar * sn + ai * cs);
     }
@@ -838,9 +855,11 @@ GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float
     cmulf(cp, sp, rotc[d], rots[d], cs, sn);
     // a * dhat * exp(i psi)
     float qr = a * (dre[d] * cs - dim[d] * sn), qi = a * (dre[d] * sn + dim[d] * cs);
-    kadd(acc[d * kAccPerDet + 0], w[d] * spp);
-    kadd(acc[d * kAccPerDet + 1], w[d] * scc);
-    kadd(acc[d * kAccPerDet + 2], w[d] * spc);
+    if (d == 0 || !wshared) {
+      kadd(acc[d * kAccPerDet + 0], w[d] * spp);
+      kadd(acc[d * kAccPerDet + 1], w[d] * scc);
+      kadd(acc[d * kAccPerDet + 2], w[d] * spc);
+    }
     kadd(acc[d * kAccPerDet + 3], qr * hpr + qi * hpi);  // Re(q conj(hpf))
     kadd(acc[d * kAccPerDet + 4], qr * hcr + qi * hci);  // Re(q conj(hcf))
   }

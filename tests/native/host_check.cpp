@@ -116,6 +116,9 @@ double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, cons
     }
   }
   mixed_prologue(r, df, x, dscale.data(), wscale.data());
+  std::vector<unsigned long long> wk(ndet);  // detectors given the same PSD array share weights
+  for (int d = 0; d < ndet; d++) wk[d] = (unsigned long long)(uintptr_t)psd[d];
+  mixed_fold_shared_weights(x, wk.data(), ndet);
   if (x.status) return NAN;
   auto tables = [](int n, double &t, double &rr, double &lnn, double &t34) {
     double xn = (double)n;
@@ -171,10 +174,10 @@ double gwh_loglik_mixed(const GenParams *pin, int approx, double T_segment, cons
       KSum acc[kMaxDet * kAccPerDet];
       for (auto &a : acc) a = KSum{0.f, 0.f};
       switch (ndet) {
-        case 1: mixed_bin_q<1>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc); break;
-        case 2: mixed_bin_q<2>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc); break;
-        case 3: mixed_bin_q<3>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc); break;
-        default: mixed_bin_q<4>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc); break;
+        case 1: mixed_bin_q<1>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc, x.wshared != 0); break;
+        case 2: mixed_bin_q<2>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc, x.wshared != 0); break;
+        case 3: mixed_bin_q<3>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc, x.wshared != 0); break;
+        default: mixed_bin_q<4>(x, n, ph, al, tf, m76, dre, dim, w, rc, rs, acc, x.wshared != 0); break;
       }
       for (int j = 0; j < kMaxDet * kAccPerDet; j++) sums[j] += (double)(acc[j].s - acc[j].c);
     }
