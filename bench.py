@@ -378,6 +378,23 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         ex["served"]["saturated"] = {"evals_per_s": nsat / wall, "p50_ms": s["p50_s"] * 1e3,
                                      "p99_ms": s["p99_s"] * 1e3, "offered_rate": 5e6, "requests": nsat,
                                      "max_batch": 4096, "launches": s["launches"], "ok": int((st == 0).sum())}
+        # latency against offered load: the same mix, one server configuration
+        curve = []
+        srv = G.Server(ctx, T, max_inflight=65536, max_batch=2048, lanes=4, hbm_budget=120 * 1024 ** 3)
+        try:
+            srv.drive(G.params_array(sp2[:4096]), sa2[:4096], handles, arr2[:4096] - arr2[0])  # warm-up
+            for rate in (2e5, 5e5, 1e6, 2e6, 3e6):
+                nr = int(min(100000, max(20000, rate * 0.05)))
+                arr3 = np.cumsum(np.random.default_rng(int(rate)).exponential(1.0 / rate, nr))
+                srv.reset_stats()
+                _, st3, _, wall3 = srv.drive(G.params_array(sp2[:nr]), sa2[:nr], handles, arr3 - arr3[0])
+                s3 = srv.stats()
+                curve.append({"offered_rate": rate, "evals_per_s": nr / wall3, "p50_ms": s3["p50_s"] * 1e3,
+                              "p99_ms": s3["p99_s"] * 1e3, "requests": nr, "launches": s3["launches"],
+                              "ok": int((st3 == 0).sum())})
+        finally:
+            srv.close()
+        ex["served"]["load_curve"] = {"max_batch": 2048, "lanes": 4, "points": curve}
 
     def uneven():
         # uneven Pv2 batch: T in {4, 8, 32, 128}, 20-2048 Hz, 1024 requests, one launch

@@ -24,20 +24,35 @@ static int length_class(int N) {  // grid-length bucket of the tuning table
   return c;
 }
 
+std::string tune_key(int mixed, int ndet, int N) {
+  return std::to_string(mixed) + ":" + std::to_string(ndet) + ":" + std::to_string(length_class(N));
+}
+
 int choose_tile(gwgpu_context *c, int mixed, int ndet, int N) {
   if (c->tile_override > 0) return c->tile_override;
-  auto it = c->tuned.find(std::to_string(mixed) + ":" + std::to_string(ndet) + ":" + std::to_string(length_class(N)));
+  auto it = c->tuned.find(tune_key(mixed, ndet, N));
   if (it != c->tuned.end()) return it->second;
   return default_tile(mixed);
 }
 
-static int persistent_grid(int device, int mixed, int ndet) {
-  static int cache[2][gwt::kMaxDet + 1] = {{0}};
-  int &g = cache[mixed ? 1 : 0][ndet];
+// Resident blocks per SM of the fused kernel's launch shape: the autotuner's
+// candidate while it runs, else its choice for this batch class, else the
+// default.
+static int choose_occ(gwgpu_context *c, int mixed, int ndet, int N) {
+  if (!mixed) return gwk::batch_default_occ(0);
+  if (c->occ_override > 0) return c->occ_override;
+  auto it = c->tuned_occ.find(tune_key(mixed, ndet, N));
+  if (it != c->tuned_occ.end()) return it->second;
+  return gwk::batch_default_occ(1);
+}
+
+static int persistent_grid(int device, int mixed, int ndet, int occ) {
+  static int cache[2][gwt::kMaxDet + 1][5] = {{{0}}};
+  int &g = cache[mixed ? 1 : 0][ndet][occ & 3];
   if (g) return g;
   cudaDeviceProp p;
   cudaGetDeviceProperties(&p, device);
-  int per_sm = gwk::batch_occupancy(mixed, ndet);
+  int per_sm = gwk::batch_occupancy(mixed, ndet, occ);
   if (per_sm < 1) per_sm = 1;
   g = p.multiProcessorCount * per_sm;
   return g;
@@ -64,7 +79,7 @@ static int lane_alloc(gwgpu_context *c, Lane &L, void **p, size_t *cap, size_t b
 
 void lane_release(gwgpu_context *c, Lane &L) {
   if (L.stream) cudaStreamSynchronize(L.stream);
-  for (auto &g : L.graphs) cudaGraphExecDestroy(g.second);
+  for (auto &g : L.graphs) cudaGraphExecDestroy(g.second.exec);
   L.graphs.clear();
   c->dfree(L.plan.mem);
   c->dfree(L.work);
@@ -132,7 +147,7 @@ int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, i
 }
 
 static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, const int *d_approx, int n,
-                           int ndet, double T_segment, int mixed, double *d_out, int *d_status, void *reqs,
+                           int ndet, double T_segment, int mixed, int occ, double *d_out, int *d_status, void *reqs,
                            double *partials, unsigned *cnt) {
   const Plan &pl = L.plan;
   const bool timing = c->timing && &L == &c->lane;
@@ -161,9 +176,9 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   a.out = d_out;
   a.status = d_status;
   a.tables = c->tables;
-  int grid = std::min(pl.nitems, persistent_grid(c->device, mixed, ndet));
+  int grid = std::min(pl.nitems, persistent_grid(c->device, mixed, ndet, occ));
   if (grid < 1) grid = 1;
-  e = gwk::launch_batch(a, mixed, grid, 0, L.stream);
+  e = gwk::launch_batch(a, mixed, grid, occ, L.stream);
   if (e != cudaSuccess) return c->fail(e, "batch launch");
   if (timing) cudaEventRecord(c->t_ev[2], L.stream);
   return GWGPU_OK;
@@ -173,11 +188,10 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
                   const int *h_handles, int ndet, double T_segment, int precision, double *d_out, int *d_status,
                   int tile, bool use_graph, const BatchCopies *io) {
   const int mixed = precision == GWGPU_PREC_MIXED;
-  if (tile <= 0) {
-    const gwgpu_context::Stream *s0 = c->get_stream(h_handles[0]);
-    if (!s0) return GWGPU_ENOTFOUND;
-    tile = choose_tile(c, mixed, ndet, s0->dev.N);
-  }
+  const gwgpu_context::Stream *s0 = c->get_stream(h_handles[0]);
+  if (!s0) return GWGPU_ENOTFOUND;
+  if (tile <= 0) tile = choose_tile(c, mixed, ndet, s0->dev.N);
+  const int occ = choose_occ(c, mixed, ndet, s0->dev.N);
   std::string key((const char *)h_handles, (const char *)(h_handles + (size_t)n * ndet));
   key += "|" + std::to_string(n) + "|" + std::to_string(tile) + "|" + std::to_string(ndet) + "|" +
          std::to_string(c->streams_epoch);
@@ -198,7 +212,7 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
   int st = lane_alloc(c, L, &L.work, &L.work_cap, bytes, "batch scratch");
   if (st) return st;
   if (L.work != old || replanned) {  // captured graphs hold the old addresses
-    for (auto &g : L.graphs) cudaGraphExecDestroy(g.second);
+    for (auto &g : L.graphs) cudaGraphExecDestroy(g.second.exec);
     L.graphs.clear();
   }
   char *p = (char *)L.work;
@@ -209,18 +223,28 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
   unsigned *cnt = (unsigned *)p;
   auto sequence = [&]() {
     if (io) cudaMemcpyAsync(io->h2d_dst, io->h2d_src, io->h2d_bytes, cudaMemcpyHostToDevice, L.stream);
-    int r = launch_sequence(c, L, d_params, d_approx, n, ndet, T_segment, mixed, d_out, d_status, reqs, partials, cnt);
+    int r = launch_sequence(c, L, d_params, d_approx, n, ndet, T_segment, mixed, occ, d_out, d_status, reqs, partials,
+                            cnt);
     if (!r && io) cudaMemcpyAsync(io->d2h_dst, io->d2h_src, io->d2h_bytes, cudaMemcpyDeviceToHost, L.stream);
     return r;
   };
   if (!use_graph || c->timing) return sequence();
   char gk[320];
-  snprintf(gk, sizeof(gk), "%p|%p|%p|%p|%d|%.17g|%d|%p|%p|%zu|%p|%p|%zu", (const void *)d_params,
-           (const void *)d_approx, (const void *)d_out, (const void *)d_status, mixed, T_segment, n,
+  snprintf(gk, sizeof(gk), "%p|%p|%p|%p|%d|%d|%.17g|%d|%p|%p|%zu|%p|%p|%zu", (const void *)d_params,
+           (const void *)d_approx, (const void *)d_out, (const void *)d_status, mixed, occ, T_segment, n,
            io ? io->h2d_src : nullptr, io ? io->h2d_dst : nullptr, io ? io->h2d_bytes : 0,
            io ? io->d2h_dst : nullptr, io ? (const void *)io->d2h_src : nullptr, io ? io->d2h_bytes : 0);
   auto it = L.graphs.find(gk);
   if (it == L.graphs.end()) {
+    if (L.graphs.size() >= kMaxGraphs) {  // drop the least recently used one, after the work queued on it
+      auto lru = L.graphs.begin();
+      for (auto j = L.graphs.begin(); j != L.graphs.end(); ++j)
+        if (j->second.used < lru->second.used) lru = j;
+      cudaError_t e = cudaStreamSynchronize(L.stream);
+      if (e != cudaSuccess) return c->fail(e, "graph cache");
+      cudaGraphExecDestroy(lru->second.exec);
+      L.graphs.erase(lru);
+    }
     cudaGraph_t g;
     cudaError_t e = cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return c->fail(e, "graph capture");
@@ -232,9 +256,10 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
     e = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return c->fail(e, "graph instantiate");
-    it = L.graphs.emplace(gk, ge).first;
+    it = L.graphs.emplace(gk, Lane::Graph{ge, 0}).first;
   }
-  cudaError_t e = cudaGraphLaunch(it->second, L.stream);
+  it->second.used = ++L.graph_tick;
+  cudaError_t e = cudaGraphLaunch(it->second.exec, L.stream);
   if (e != cudaSuccess) return c->fail(e, "graph launch");
   return GWGPU_OK;
 }
@@ -279,7 +304,7 @@ static int stage_io(gwgpu_context *c, gwb::Lane &L, size_t bytes) {
   if (st) return st;
   L.io_cap = nb;
   L.bytes += nb;
-  for (auto &g : L.graphs) cudaGraphExecDestroy(g.second);
+  for (auto &g : L.graphs) cudaGraphExecDestroy(g.second.exec);
   L.graphs.clear();
   return GWGPU_OK;
 }
@@ -406,35 +431,49 @@ int gwgpu_batch_autotune(gwgpu_context *c, const gwgpu_gen_params *d_params, con
   if (!s0) return GWGPU_ENOTFOUND;
   static const int cand_mixed[] = {1024, 2048, 4096, 8192, 16384}, cand_fp64[] = {256, 512, 1024, 2048, 4096};
   const int *cand = mixed ? cand_mixed : cand_fp64;
+  // launch shapes: bin tile x resident blocks per SM of the fused kernel
+  // (the mixed form's register bound for 3 or 4 blocks of 256 threads)
+  const int occs_mixed[] = {3, 4}, occs_fp64[] = {0};
+  const int *occs = mixed ? occs_mixed : occs_fp64;
+  const int nocc = mixed ? 2 : 1;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  int best = 0;
+  int best = 0, best_occ = 0;
   float bms = 1e30f;
-  for (int i = 0; i < 5; i++) {
-    int tile = cand[i];
+  for (int ci = 0; ci < 5 * nocc; ci++) {
+    int tile = cand[ci / nocc];
+    c->occ_override = occs[ci % nocc];
     int st = gwb::enqueue_batch(c, L, d_params, d_approx, n, h_handles, ndet, T_segment, precision, d_out, d_status,
                                 tile, false);  // warm-up and plan
-    if (st) return st;
+    if (st) {
+      c->occ_override = 0;
+      return st;
+    }
     cudaEventRecord(e0, L.stream);
     for (int r = 0; r < 3; r++)
       gwb::enqueue_batch(c, L, d_params, d_approx, n, h_handles, ndet, T_segment, precision, d_out, d_status, tile,
                          false);
     cudaEventRecord(e1, L.stream);
     cudaError_t e = cudaEventSynchronize(e1);
-    if (e != cudaSuccess) return c->fail(e, "autotune");
+    if (e != cudaSuccess) {
+      c->occ_override = 0;
+      return c->fail(e, "autotune");
+    }
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     ms /= 3;
     if (ms < bms) {
       bms = ms;
       best = tile;
+      best_occ = c->occ_override;
     }
   }
+  c->occ_override = 0;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  c->tuned[std::to_string(mixed) + ":" + std::to_string(ndet) + ":" + std::to_string(gwb::length_class(s0->dev.N))] =
-      best;
+  c->tuned[gwb::tune_key(mixed, ndet, s0->dev.N)] = best;
+  if (mixed) c->tuned_occ[gwb::tune_key(mixed, ndet, s0->dev.N)] = best_occ;
   if (best_tile) *best_tile = best;
   if (best_ms) *best_ms = bms;
   return GWGPU_OK;

@@ -33,14 +33,26 @@ struct Lane {
   size_t work_cap = 0;
   void *hio = nullptr, *dio = nullptr;  // staging for the host-array entry points
   size_t io_cap = 0;
-  std::map<std::string, cudaGraphExec_t> graphs;
+  // captured launch sequences by (pointers, shape), least recently used ones
+  // dropped beyond kMaxGraphs: a caller rotating through many buffer sets
+  // keeps a bounded number of executable graphs
+  struct Graph {
+    cudaGraphExec_t exec;
+    uint64_t used;
+  };
+  std::map<std::string, Graph> graphs;
+  uint64_t graph_tick = 0;
   size_t bytes = 0;  // device bytes held (budget accounting)
 };
+
+constexpr size_t kMaxGraphs = 8;
 
 int default_tile(int mixed);
 // Tile for one launch: explicit override, else the autotuned choice for this
 // (precision, detectors, grid length) class, else the default.
 int choose_tile(gwgpu_context *c, int mixed, int ndet, int N);
+// Key of the tuning tables: (precision, detectors, grid-length class).
+std::string tune_key(int mixed, int ndet, int N);
 int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, int tile);
 // Copies around a launch (pinned host buffers of the lane): before it, the
 // inputs host -> device; after it, the outputs device -> host.

@@ -269,7 +269,7 @@ int gwgpu_context_destroy(gwgpu_context *c) {
   for (auto &w : c->hws)
     if (w.second.ptr) cudaFreeHost(w.second.ptr);
   c->lane.stream = c->stream;
-  for (auto &g : c->lane.graphs) cudaGraphExecDestroy(g.second);
+  for (auto &g : c->lane.graphs) cudaGraphExecDestroy(g.second.exec);
   if (c->lane.hio) cudaFreeHost(c->lane.hio);
   if (c->ev_in) cudaEventDestroy(c->ev_in);
   for (int i = 0; i < 3; i++)

@@ -47,8 +47,10 @@ struct gwgpu_context {
   size_t streams_dev_cap = 0;
   unsigned *counters = nullptr;
   gwb::Lane lane;                  // scratch of the context-stream batches
-  std::map<std::string, int> tuned;  // autotuned tile per (precision, detectors, grid length)
+  std::map<std::string, int> tuned;      // autotuned tile per (precision, detectors, grid length)
+  std::map<std::string, int> tuned_occ;  // and the fused kernel's resident blocks per SM
   int tile_override = 0;
+  int occ_override = 0;                  // set while the autotuner times a launch shape
   bool use_graphs = true;
   int chirp_n = 0;                 // grid length whose Bluestein kernel the kWsChirp workspace holds
   double chirp_kscale = 0;         // M max|B| of that kernel (the FP32 search's error scale)

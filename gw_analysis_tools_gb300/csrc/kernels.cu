@@ -590,8 +590,10 @@ __device__ __forceinline__ void block_sum_mixed(const float (&v)[NV], float *sm,
   __syncthreads();
 }
 
-template <int NDET, int MIXED>
-__global__ void __launch_bounds__(kBatchBlock, MIXED ? 3 : 2) k_batch(const BatchArgs a) {
+// OCC: the resident blocks per SM the register allocation is bounded for
+// (mixed form 3 or 4, a launch-shape choice of the autotuner; FP64 form 2).
+template <int NDET, int MIXED, int OCC>
+__global__ void __launch_bounds__(kBatchBlock, OCC) k_batch(const BatchArgs a) {
   constexpr int NV = MIXED ? NDET * kAccPerDet : 2 * NDET;
   __shared__ int s_item;
   __shared__ __align__(16) unsigned char s_req[MIXED ? sizeof(MixedReq) : sizeof(Request)];
@@ -837,46 +839,36 @@ __global__ void __launch_bounds__(kBatchBlock, MIXED ? 3 : 2) k_batch(const Batc
 
 int batch_block_size(int) { return kBatchBlock; }
 
-int batch_occupancy(int mixed, int ndet) {
-  int nb = 0;
-  const void *f = nullptr;
-  switch (ndet * 2 + (mixed ? 1 : 0)) {
-    case 2: f = (const void *)k_batch<1, 0>; break;
-    case 3: f = (const void *)k_batch<1, 1>; break;
-    case 4: f = (const void *)k_batch<2, 0>; break;
-    case 5: f = (const void *)k_batch<2, 1>; break;
-    case 6: f = (const void *)k_batch<3, 0>; break;
-    case 7: f = (const void *)k_batch<3, 1>; break;
-    case 8: f = (const void *)k_batch<4, 0>; break;
-    case 9: f = (const void *)k_batch<4, 1>; break;
-    default: return 1;
+template <int NDET>
+static const void *batch_fn(int mixed, int occ) {
+  if (!mixed) return (const void *)k_batch<NDET, 0, 2>;
+  return occ == 3 ? (const void *)k_batch<NDET, 1, 3> : (const void *)k_batch<NDET, 1, 4>;
+}
+static const void *batch_fn(int mixed, int ndet, int occ) {
+  switch (ndet) {
+    case 1: return batch_fn<1>(mixed, occ);
+    case 2: return batch_fn<2>(mixed, occ);
+    case 3: return batch_fn<3>(mixed, occ);
+    case 4: return batch_fn<4>(mixed, occ);
+    default: return nullptr;
   }
+}
+
+int batch_default_occ(int mixed) { return mixed ? 4 : 2; }
+
+int batch_occupancy(int mixed, int ndet, int occ) {
+  int nb = 0;
+  const void *f = batch_fn(mixed, ndet, occ);
+  if (!f) return 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, kBatchBlock, 0) != cudaSuccess) return 1;
   return nb;
 }
 
-cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int block, cudaStream_t s) {
-  (void)block;
-#define GWK_CASE(ND, MX) k_batch<ND, MX><<<grid, kBatchBlock, 0, s>>>(a)
-  if (mixed) {
-    switch (a.ndet) {
-      case 1: GWK_CASE(1, 1); break;
-      case 2: GWK_CASE(2, 1); break;
-      case 3: GWK_CASE(3, 1); break;
-      case 4: GWK_CASE(4, 1); break;
-      default: return cudaErrorInvalidValue;
-    }
-  } else {
-    switch (a.ndet) {
-      case 1: GWK_CASE(1, 0); break;
-      case 2: GWK_CASE(2, 0); break;
-      case 3: GWK_CASE(3, 0); break;
-      case 4: GWK_CASE(4, 0); break;
-      default: return cudaErrorInvalidValue;
-    }
-  }
-#undef GWK_CASE
-  return cudaGetLastError();
+cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s) {
+  const void *f = batch_fn(mixed, a.ndet, occ);
+  if (!f) return cudaErrorInvalidValue;
+  void *args[] = {(void *)&a};
+  return cudaLaunchKernel(f, dim3(grid), dim3(kBatchBlock), args, 0, s);
 }
 
 void qnm_host_table(double *o) { qnm_fill(o, gwt_qnm_a_h, gwt_qnm_fring_h, gwt_qnm_fdamp_h); }

@@ -89,9 +89,11 @@ struct BatchArgs {
   int *status;
   gwt::Tables tables;
 };
-cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int block, cudaStream_t s);
+// occ: the launch shape's resident blocks per SM (mixed 3 or 4, FP64 2)
+cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s);
+int batch_default_occ(int mixed);
 int batch_block_size(int mixed);
-int batch_occupancy(int mixed, int ndet);  // resident blocks per SM
+int batch_occupancy(int mixed, int ndet, int occ);  // resident blocks per SM
 
 // Per-request kernel status -> C ABI status: 0 ok, 1 invalid request (grids of
 // different lengths, grid unusable by the mixed form), 4 outside the model

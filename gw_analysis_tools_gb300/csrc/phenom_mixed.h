@@ -47,7 +47,7 @@ struct MixedDet {
   double Gre, Gim;   // D: F+ (1+c^2)/2, -Fx c ; Pv2: P_d, Q_d (real); applied in FP64 at the end
 };
 
-constexpr int kAccPerDet = 5;  // D uses 3 (hh, zr, zi); Pv2 uses 5 (spp, scc, spc, zp, zc)
+constexpr int kAccPerDet = 5;  // D uses 2 (hh, Re z); Pv2 uses 5 (spp, scc, spc, zp, zc)
 constexpr float kSegFScale = 268435456.0f;  // FP32 part of a segment phase polynomial: turns * 2^28
 
 struct MixedReq {
@@ -469,6 +469,10 @@ GW_HD void mixed_det_phase(const Request &r, double df, MixedReq &x) {
     } else {
       x.det[d].Gre = r.det[d].fp * .5 * (1 + ci * ci);
       x.det[d].Gim = -r.det[d].fc * ci;
+      // DH_d = A ds Re(conj(G) S) = A ds |G| Re(e^{-i arg G} S): the phase of
+      // conj(G) joins the detector's fixed-point linear phase, so the bins
+      // accumulate Re(S) only and |G| is applied in FP64 (mixed_det_factors_a)
+      x.det[d].L0 -= turns_q64(atan2(x.det[d].Gim, x.det[d].Gre) * inv2pi);
     }
   }
 }
@@ -486,10 +490,10 @@ GW_HD void mixed_det_factors_a(const Request &r, MixedReq &x, double A, const do
       f[2] = -A * A * w * G1 * G2;
       f[3] = A * ds * G1;
       f[4] = A * ds * G2;
-    } else {
+    } else {  // the phase of conj(G) is in the detector's linear phase (mixed_det_phase)
       f[0] = -0.5 * A * A * w * (G1 * G1 + G2 * G2);
-      f[1] = A * ds * G1;
-      f[2] = A * ds * G2;
+      f[1] = A * ds * sqrt(G1 * G1 + G2 * G2);
+      f[2] = 0.0;
       f[3] = 0.0;
       f[4] = 0.0;
     }
@@ -807,8 +811,7 @@ GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float
       cmulf(cp, sp, rotc[d], rots[d], cs, sn);
       float ar = a * dre[d], ai = a * dim[d];
       if (d == 0 || !wshared) kadd(acc[d * kAccPerDet + 0], w[d] * aa);
-      kadd(acc[d * kAccPerDet + 1], ar * cs - ai * sn);
-      kadd(acc[d * kAccPerDet + 2], ar * sn + ai * cs);
+      kadd(acc[d * kAccPerDet + 1], ar * cs - ai * sn);  // Re(a dhat e^{i (phase + linear phase - arg G)})
     }
     return;
   }

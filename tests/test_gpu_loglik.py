@@ -223,3 +223,40 @@ def test_cooperative_prologue_matches_serial(gpu_ctx, network):
             assert np.max(np.abs(a - b) / np.maximum(1.0, np.abs(b))) <= tol
     finally:
         ser.close()
+
+
+def test_device_batches_rotating_buffers_and_launch_shapes(gpu_ctx, oracle, network):
+    """gwgpu_loglik_batch_device over twelve buffer sets in turn (more than the
+    eight captured graphs the engine keeps: the least recently used are
+    dropped and captured again), before and after the autotuner has picked a
+    tile and a blocks-per-SM launch shape; every result against the oracle."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    n = network
+    nsets, m = 12, 40
+    draws = [W.prior_draws(m, 500 + s) for s in range(nsets)]
+    refs = [oracle.loglik_batch([oracle.params_from_dict(d) for d in dr], n["f"], n["dets"], n["data"], n["psd"])
+            for dr in draws]
+    pb = ctypes.sizeof(G.GenParams) * m
+    dev = torch.device("cuda", 0)
+    params = [torch.frombuffer(bytearray(G.params_array(dr)), dtype=torch.uint8).to(dev) for dr in draws]
+    approx = torch.zeros(m, dtype=torch.int32, device=dev)
+    outs = [torch.zeros(m, dtype=torch.float64, device=dev) for _ in range(nsets)]
+    stats = [torch.zeros(m, dtype=torch.int32, device=dev) for _ in range(nsets)]
+    assert params[0].numel() == pb
+
+    def run_all():
+        for rep in range(2):
+            for s in range(nsets):
+                gpu_ctx.loglik_batch_device(params[s].data_ptr(), approx.data_ptr(), m, n["handles"], n["T"],
+                                            G.PREC_MIXED, outs[s].data_ptr(), stats[s].data_ptr())
+        torch.cuda.synchronize()
+        for s in range(nsets):
+            assert np.all(stats[s].cpu().numpy() == 0)
+            assert np.max(np.abs(outs[s].cpu().numpy() - refs[s])) <= MIXED_TOL
+
+    run_all()
+    tile, ms = gpu_ctx.autotune(params[0].data_ptr(), approx.data_ptr(), m, n["handles"], n["T"], G.PREC_MIXED,
+                                outs[0].data_ptr(), stats[0].data_ptr())
+    assert tile in (1024, 2048, 4096, 8192, 16384) and ms > 0
+    run_all()
