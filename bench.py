@@ -440,6 +440,15 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
                         "status_counts": {str(int(c)): int(k) for c, k in zip(codes, counts)},
                         "form": "moment sums (FP64 waveform differences, FP32-compensated Gram), order 2; "
                                 "sources it cannot invert redone by the FP64 reference algorithm"}
+        # the moment form with FP64 differences and sums
+        ctx.fisher_batch_ex(G.params_array(W.prior_draws(64, 14)), 0, hf, epsilon=1e-6, step_mode=1,
+                            algorithm=G.FISHER_MOMENTS)
+        t0 = time.perf_counter()
+        f64, c64, st64 = ctx.fisher_batch_ex(pf, 0, hf, epsilon=1e-6, step_mode=1, algorithm=G.FISHER_MOMENTS)
+        dt64 = time.perf_counter() - t0
+        codes, counts = np.unique(st64, return_counts=True)
+        ex["fisher"]["fp64_sums"] = {"fishers_per_s": nf / dt64, "seconds": dt64, "ok": int((st64 == 0).sum()),
+                                     "status_counts": {str(int(c)): int(k) for c, k in zip(codes, counts)}}
         # the reference algorithm in FP64 (orders 2 and 4) and the sampler's proposal
         nr = 2048
         pr = G.params_array(W.prior_draws(nr, 13))
@@ -456,7 +465,8 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         ns = 64  # parity sample: the moment form and the reference algorithm against the oracle
         fr, cr, _ = ctx.fisher_batch_ex(G.params_array(W.prior_draws(ns, 13)), 0, hf, order=2, epsilon=1e-6,
                                         step_mode=1)
-        ex["_fisher_sample"] = (pf, fish[:ns].copy(), cov[:ns].copy(), fr, cr, ff, psd_f)
+        ex["_fisher_sample"] = (pf, fish[:ns].copy(), cov[:ns].copy(), fr, cr, ff, psd_f, f64[:ns].copy(),
+                                c64[:ns].copy())
 
     def maximized():
         # the sampler's intrinsic mode: likelihood maximised over t_c and phi_c
@@ -586,7 +596,7 @@ def fisher_err(sample):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from gw_analysis_tools_gb300 import workloads as W
-    pf, fish, cov, fr, cr, ff, psd = sample
+    pf, fish, cov, fr, cr, ff, psd, f64, c64 = sample
     plist = []
     for i in range(len(fish)):
         op = O.GenParams()
@@ -597,20 +607,23 @@ def fisher_err(sample):
 
     def nerr(a, b):
         return float(np.max(np.abs(a - b) / np.sqrt(np.abs(np.outer(np.diag(b), np.diag(b))))))
-    e_m, e_r, c_m, c_r, conds = [], [], [], [], []
+    e_m, e_r, e_6, c_m, c_r, c_6, conds = [], [], [], [], [], [], []
     for i in range(len(fish)):
         e_m.append(nerr(fish[i], ref[i]))
         e_r.append(nerr(fr[i], ref[i]))
+        e_6.append(nerr(f64[i], ref[i]))
         st, rinv = O.cholesky_invert(ref[i])
         if st == 0:
             c_m.append(nerr(cov[i], rinv))
             c_r.append(nerr(cr[i], rinv))
+            c_6.append(nerr(c64[i], rinv))
             conds.append(float(np.linalg.cond(ref[i] / np.sqrt(np.outer(np.diag(ref[i]), np.diag(ref[i]))))))
     return {"sources": len(fish), "step": "1e-6 relative",
             "max_normalized_err": max(e_m), "median_normalized_err": float(np.median(e_m)),
             "max_normalized_err_inverse": max(c_m), "median_normalized_err_inverse": float(np.median(c_m)),
             "reference_algorithm_max_normalized_err": max(e_r),
             "reference_algorithm_max_normalized_err_inverse": max(c_r),
+            "fp64_sums_max_normalized_err": max(e_6), "fp64_sums_max_normalized_err_inverse": max(c_6),
             "median_condition_number": float(np.median(conds)), "max_condition_number": max(conds)}
 
 

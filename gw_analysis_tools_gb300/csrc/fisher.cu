@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/gwgpu.h"
@@ -58,6 +59,12 @@ struct FisherArgs {
   const int *wslot;         // detector -> weight stream
   const float *what[kMaxDet];
   double wscale[kMaxDet];
+  // FP64 sums: the weight of bin k is c3 s_k / (S_k wscale) from the stream's
+  // FP64 reciprocal PSD (Simpson pattern s_k, c3 = 4 df_s / 3), or iw_k / (S_k
+  // wscale) for a stream registered with its own integration weights iw
+  const double *ipsd[kMaxDet];
+  const double *iw[kMaxDet];
+  double c3[kMaxDet];
   int n0, N, tile, ntiles;
   double df, fisher_df_ratio;  // (f1 - f0) / simpson_df
   float df_f;                  // df in FP32 (the bins' frequency in the moment sums)
@@ -70,7 +77,9 @@ struct FisherArgs {
   int *status;
 };
 
-template <int NW>
+// ACC64: the per-bin differences, weights and moment sums in FP64 instead of
+// FP32 values with compensated FP32 sums.
+template <int NW, bool ACC64>
 __global__ void __launch_bounds__(kBlock, 3) k_fisher_main(const FisherArgs a) {
   __shared__ int s_item;
   __shared__ __align__(16) unsigned char s_buf[sizeof(FisherSrc)];
@@ -90,22 +99,38 @@ __global__ void __launch_bounds__(kBlock, 3) k_fisher_main(const FisherArgs a) {
     }
     __syncthreads();
     const FisherSrc &F = *(const FisherSrc *)s_buf;
-    KSum acc[NW * kSums];
+    using Acc = typename std::conditional<ACC64, double, KSum>::type;
+    Acc acc[NW * kSums];
 #pragma unroll
-    for (int j = 0; j < NW * kSums; j++) acc[j] = KSum{0.f, 0.f};
+    for (int j = 0; j < NW * kSums; j++) {
+      if constexpr (ACC64) acc[j] = 0.0;
+      else acc[j] = KSum{0.f, 0.f};
+    }
     const int k0 = tile * a.tile, k1 = min(k0 + a.tile, a.N);
     const bool in_tables = a.n0 >= 1 && a.n0 + k1 - 1 <= a.tab.nmax && a.n0 + k1 - 1 <= a.tm76d_n;
     if (!in_tables && tid == 0) atomicOr(a.status + src, kStatusBounds);
     if (F.status == 0 && in_tables) {
       for (int k = k0 + tid; k < k1; k += blockDim.x) {
         const int n = a.n0 + k;
-        float a0, qr[kIntr], qi[kIntr];
-        if (!fisher_bin_q(F, n, a.tab.t13[n], a.tab.tm53[n], a.tab.tln[n], a.tab.t34[n], a.tm76d[n], a.tab.tm76f[n], a0,
-                          qr, qi))
-          continue;
-        const float fk = (float)n * a.df_f;
+        if constexpr (ACC64) {
+          double a0, qr[kIntr], qi[kIntr];
+          if (!fisher_bin_q(F, n, a.tab.t13[n], a.tab.tm53[n], a.tab.tln[n], a.tab.t34[n], a.tm76d[n],
+                            a.tab.tm76f[n], a0, qr, qi))
+            continue;
+          const double fk = (double)n * a.df, sw = simpson_weight(k, a.N);
 #pragma unroll
-        for (int w = 0; w < NW; w++) fisher_accumulate(a.what[w][k], a0, fk, qr, qi, acc + w * kSums);
+          for (int w = 0; w < NW; w++)
+            fisher_accumulate64((a.iw[w] ? a.iw[w][k] : a.c3[w] * sw) * a.ipsd[w][k] / a.wscale[w], a0, fk, qr, qi,
+                                acc + w * kSums);
+        } else {
+          float a0, qr[kIntr], qi[kIntr];
+          if (!fisher_bin_q(F, n, a.tab.t13[n], a.tab.tm53[n], a.tab.tln[n], a.tab.t34[n], a.tm76d[n],
+                            a.tab.tm76f[n], a0, qr, qi))
+            continue;
+          const float fk = (float)n * a.df_f;
+#pragma unroll
+          for (int w = 0; w < NW; w++) fisher_accumulate(a.what[w][k], a0, fk, qr, qi, acc + w * kSums);
+        }
       }
     }
     // block reduction in FP64, 8 values at a time
@@ -113,7 +138,11 @@ __global__ void __launch_bounds__(kBlock, 3) k_fisher_main(const FisherArgs a) {
     for (int base = 0; base < NW * kSums; base += 8) {
       double v[8];
 #pragma unroll
-      for (int j = 0; j < 8; j++) v[j] = (base + j < NW * kSums) ? (double)acc[base + j].s - (double)acc[base + j].c : 0.0;
+      for (int j = 0; j < 8; j++) {
+        if (base + j >= NW * kSums) v[j] = 0.0;
+        else if constexpr (ACC64) v[j] = acc[base + j];
+        else v[j] = (double)acc[base + j].s - (double)acc[base + j].c;
+      }
 #pragma unroll
       for (int j = 0; j < 8; j++)
 #pragma unroll
@@ -339,8 +368,11 @@ int gwgpu_fisher_numerical(gwgpu_context *c, const double *freqs, int N, const c
   return GWGPU_OK;
 }
 
-int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, int method, const int *handles,
-                       int ndet, double epsilon, int step_mode, double *fisher, double *covariance, int *status) {
+}  // extern "C"
+
+// The moment form for n sources; acc64 selects FP64 per-bin values and sums.
+int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int method, const int *handles, int ndet,
+                   double epsilon, int step_mode, double *fisher, double *covariance, int *status, bool acc64) {
   if (!c || !params || n < 1 || !handles || ndet < 1 || ndet > kMaxDet || !fisher || (method != 0 && method != 1))
     return GWGPU_EINVAL;
   std::lock_guard<std::mutex> lk(c->mu);
@@ -419,6 +451,9 @@ int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, 
   for (int w = 0; w < nw; w++) {
     a.what[w] = ws[w]->dev.what;
     a.wscale[w] = ws[w]->dev.wscale;
+    a.ipsd[w] = ws[w]->dev.ipsd;
+    a.iw[w] = ws[w]->dev.iw;
+    a.c3[w] = 4. * ws[w]->dev.simpson_df / 3.;
   }
   a.n0 = s0->dev.n0;
   a.N = N;
@@ -435,7 +470,7 @@ int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, 
     cudaDeviceProp pr;
     cudaGetDeviceProperties(&pr, c->device);
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fisher_main<1>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fisher_main<1, false>, kBlock, 0);
     grid_cache = pr.multiProcessorCount * std::max(per, 1);
   }
   for (int s0i = 0; s0i < n; s0i += chunk) {
@@ -457,10 +492,22 @@ int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, 
     a.status = dstat;
     int grid = std::min(m * ntiles, grid_cache);
     switch (nw) {
-      case 1: k_fisher_main<1><<<grid, kBlock, 0, c->stream>>>(a); break;
-      case 2: k_fisher_main<2><<<grid, kBlock, 0, c->stream>>>(a); break;
-      case 3: k_fisher_main<3><<<grid, kBlock, 0, c->stream>>>(a); break;
-      default: k_fisher_main<4><<<grid, kBlock, 0, c->stream>>>(a); break;
+      case 1:
+        if (acc64) k_fisher_main<1, true><<<grid, kBlock, 0, c->stream>>>(a);
+        else k_fisher_main<1, false><<<grid, kBlock, 0, c->stream>>>(a);
+        break;
+      case 2:
+        if (acc64) k_fisher_main<2, true><<<grid, kBlock, 0, c->stream>>>(a);
+        else k_fisher_main<2, false><<<grid, kBlock, 0, c->stream>>>(a);
+        break;
+      case 3:
+        if (acc64) k_fisher_main<3, true><<<grid, kBlock, 0, c->stream>>>(a);
+        else k_fisher_main<3, false><<<grid, kBlock, 0, c->stream>>>(a);
+        break;
+      default:
+        if (acc64) k_fisher_main<4, true><<<grid, kBlock, 0, c->stream>>>(a);
+        else k_fisher_main<4, false><<<grid, kBlock, 0, c->stream>>>(a);
+        break;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return c->fail(e, "fisher batch launch");
@@ -500,4 +547,8 @@ int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, 
   return GWGPU_OK;
 }
 
-}  // extern "C"
+extern "C" int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, int method,
+                                  const int *handles, int ndet, double epsilon, int step_mode, double *fisher,
+                                  double *covariance, int *status) {
+  return gwf_moment_run(c, params, n, method, handles, ndet, epsilon, step_mode, fisher, covariance, status, false);
+}

@@ -247,26 +247,30 @@ GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsil
 }
 
 
-// (A+ s+ - A- s-) / divisor of pair q at bin n (FP32 result; the amplitude
-// power m76 applied in FP32): one polynomial of coefficient
+// (A+ s+ - A- s-) / divisor of pair q at bin n (T = float: the amplitude power
+// m76 applied in FP32; T = double: all FP64): one polynomial of coefficient
 // differences where both waveforms are in the same inspiral or intermediate
 // region, the ringdown form of wave64_amp_diff, each waveform on its own at
 // the bins between their region boundaries.
-GW_HD float fisher_amp_deriv(const FisherSrc &F, int q, int n, double t, double m76, float m76f) {
+template <typename T>
+GW_HD T fisher_amp_deriv(const FisherSrc &F, int q, int n, double t, double m76, float m76f) {
   const WaveF64 &p = F.wp[q], &m = F.wm[q];
   const WaveDiff &d = F.wd[q];
   if (n <= p.n_cut && n <= m.n_cut) {
     if (n < p.n_f1 && n < m.n_f1) {
       double a = d.ai[9];
       for (int j = 8; j >= 0; j--) a = a * t + d.ai[j];
-      return (float)a * m76f;
+      if constexpr (sizeof(T) == sizeof(float)) return (float)a * m76f;
+      else return a * m76;
     }
     if (n >= p.n_f1 && n >= m.n_f1 && n < p.n_f3 && n < m.n_f3) {
       const double h = (double)(n - F.w0.n_mid);
-      return (float)((((d.ei[4] * h + d.ei[3]) * h + d.ei[2]) * h + d.ei[1]) * h + d.ei[0]) * m76f;
+      const double a = (((d.ei[4] * h + d.ei[3]) * h + d.ei[2]) * h + d.ei[1]) * h + d.ei[0];
+      if constexpr (sizeof(T) == sizeof(float)) return (float)a * m76f;
+      else return a * m76;
     }
   }
-  return (float)(wave64_amp_diff(p, m, n, t, m76, F.sp[q], F.sm[q], F.amp_lk[q]) * F.idiv[q]);
+  return (T)(wave64_amp_diff(p, m, n, t, m76, F.sp[q], F.sm[q], F.amp_lk[q]) * F.idiv[q]);
 }
 // ((phase+ - phic+) - (phase- - phic-)) / divisor of pair q at bin n, the same way.
 GW_HD double fisher_phase_deriv(const FisherSrc &F, int q, int n, double t, double r, double lnn, double t34) {
@@ -303,8 +307,9 @@ GW_HD double fisher_phase_deriv(const FisherSrc &F, int q, int n, double t, doub
 // beyond its cut (f > 0.2/M, where the model is exactly zero: a finite
 // difference across the cut is a jump, which the series form below does not
 // describe) and for pairs flagged exact.
+template <typename T>
 GW_HD void fisher_q_exact(const FisherSrc &F, int q, int n, double t, double r, double lnn, double t34, double m76,
-                          float &qr, float &qi) {
+                          T &qr, T &qi) {
   const double phi0 = wave64_phase(F.w0, n, t, r, lnn, t34) - F.w0.phic;
   double re = 0.0, im = 0.0;
   for (int side = 0; side < 2; side++) {
@@ -316,8 +321,8 @@ GW_HD void fisher_q_exact(const FisherSrc &F, int q, int n, double t, double r, 
     re += a * c;
     im -= a * s;
   }
-  qr = (float)(re * F.idiv[q]);
-  qi = (float)(im * F.idiv[q]);
+  qr = (T)(re * F.idiv[q]);
+  qi = (T)(im * F.idiv[q]);
 }
 
 // One bin: the intrinsic differences q = (r+ - r-) e^{i Phi0} / (G divisor) of
@@ -326,29 +331,30 @@ GW_HD void fisher_q_exact(const FisherSrc &F, int q, int n, double t, double r, 
 // step, a central pair is exactly (A+ - A-) cos h - i (A+ + A-) sin h; cos h and
 // sin h / h by their series (h stays below 1e-2 for the steps used).  A
 // one-sided pair (eta at 1/4, + the centre) is A0 - A- e^{2ih}.
+template <typename T>
 GW_HD bool fisher_bin_q(const FisherSrc &F, int n, double t, double r, double lnn, double t34, double m76,
-                        float m76f, float &a0, float *qr, float *qi) {
+                        float m76f, T &a0, T *qr, T *qi) {
   if (n > F.n_cut_any) return false;
   const double amp0 = wave64_amp(F.w0, n, t, m76);
-  a0 = (float)amp0;
+  a0 = (T)amp0;
   for (int q = 0; q < kIntr; q++) {
     if (F.exact[q] || amp0 == 0.0 || n > F.wp[q].n_cut || n > F.wm[q].n_cut) {
       fisher_q_exact(F, q, n, t, r, lnn, t34, m76, qr[q], qi[q]);
       continue;
     }
-    const float damp = fisher_amp_deriv(F, q, n, t, m76, m76f);    // (A+ - A-) / divisor
+    const T damp = fisher_amp_deriv<T>(F, q, n, t, m76, m76f);      // (A+ - A-) / divisor
     const double dph = fisher_phase_deriv(F, q, n, t, r, lnn, t34);  // (Phi+ - Phi-) / divisor
     const double h = 0.5 * dph * F.div[7 + q];
     const double h2 = h * h;
     if (!F.onesided[q]) {
-      qr[q] = damp * (float)(1.0 - h2 * (0.5 - h2 * (1.0 / 24.0)));
-      qi[q] = (float)(-amp0 * dph * (1.0 - h2 * ((1.0 / 6.0) - h2 * (1.0 / 120.0))));
+      qr[q] = damp * (T)(1.0 - h2 * (0.5 - h2 * (1.0 / 24.0)));
+      qi[q] = (T)(-amp0 * dph * (1.0 - h2 * ((1.0 / 6.0) - h2 * (1.0 / 120.0))));
     } else {
       const double am = amp0 - (double)damp * F.div[7 + q];
       double s2, c2;
       sincos(2.0 * h, &s2, &c2);
-      qr[q] = (float)((amp0 - am * c2) * F.idiv[q]);
-      qi[q] = (float)(-am * s2 * F.idiv[q]);
+      qr[q] = (T)((amp0 - am * c2) * F.idiv[q]);
+      qi[q] = (T)(-am * s2 * F.idiv[q]);
     }
   }
   return true;
@@ -367,6 +373,23 @@ GW_HD void fisher_accumulate(float wh, float a0, float fk, const float *qr, cons
     kadd(A[13 + 4 * i + 1], wa * qi[i]);
     kadd(A[13 + 4 * i + 2], wa * qr[i] * fk);
     kadd(A[13 + 4 * i + 3], wa * qi[i] * fk);
+  }
+}
+// The same moment sums in FP64 (weights, differences and sums all FP64).
+GW_HD void fisher_accumulate64(double wh, double a0, double fk, const double *qr, const double *qi, double *A) {
+  const double wa2 = wh * a0 * a0;
+  A[0] += wa2;
+  A[1] += wa2 * fk;
+  A[2] += wa2 * fk * fk;
+  int o = 3;
+  for (int i = 0; i < kIntr; i++)
+    for (int j = i; j < kIntr; j++) A[o++] += wh * (qr[i] * qr[j] + qi[i] * qi[j]);
+  const double wa = wh * a0;
+  for (int i = 0; i < kIntr; i++) {
+    A[13 + 4 * i + 0] += wa * qr[i];
+    A[13 + 4 * i + 1] += wa * qi[i];
+    A[13 + 4 * i + 2] += wa * qr[i] * fk;
+    A[13 + 4 * i + 3] += wa * qi[i] * fk;
   }
 }
 // FP64 assembly of Gamma from the moment sums Ssum[w * kSums + j] of each

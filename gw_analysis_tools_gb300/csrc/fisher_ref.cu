@@ -330,18 +330,19 @@ int gwgpu_fisher_batch_ex(gwgpu_context *c, const gwgpu_gen_params *params, int 
   if (!c || !params || n < 1 || !handles || ndet < 1 || ndet > kMaxDet || !fisher || !opt) return GWGPU_EINVAL;
   if (opt->method != GWGPU_FISHER_IMRPHENOMD && opt->method != GWGPU_FISHER_MCMC_IMRPHENOMD) return GWGPU_EINVAL;
   if (opt->order != 2 && opt->order != 4) return GWGPU_EINVAL;
-  if (opt->precision == GWGPU_PREC_MIXED) {
+  if (opt->precision != GWGPU_PREC_FP64 && opt->precision != GWGPU_PREC_MIXED) return GWGPU_EINVAL;
+  if (opt->algorithm == GWGPU_FISHER_MOMENTS) {
     if (opt->order != 2) {
-      c->last_error = "fisher: the mixed form is order 2; order 4 runs in FP64";
+      c->last_error = "fisher_batch_ex: the moment form is the central (order 2) rule";
       return GWGPU_EINVAL;
     }
-    int st = gwgpu_fisher_batch(c, params, n, opt->method, handles, ndet, opt->epsilon, opt->step_mode, fisher,
-                                covariance, status);
+    int st = gwf_moment_run(c, params, n, opt->method, handles, ndet, opt->epsilon, opt->step_mode, fisher, covariance,
+                            status, opt->precision == GWGPU_PREC_FP64);
     if (st || !opt->add_prior) return st;
+    double prior[kDim];
+    cudaMemcpyFromSymbol(prior, c_prior_diag, sizeof(prior));
     for (int i = 0; i < n; i++) {  // the prior diagonal, then the inverse again
       double *F = fisher + (size_t)i * kDim * kDim;
-      double prior[kDim];
-      cudaMemcpyFromSymbol(prior, c_prior_diag, sizeof(prior));
       for (int k = 0; k < kDim; k++) F[k * kDim + k] += prior[k];
       if (covariance) {
         double *C = covariance + (size_t)i * kDim * kDim;
@@ -356,6 +357,7 @@ int gwgpu_fisher_batch_ex(gwgpu_context *c, const gwgpu_gen_params *params, int 
     }
     return GWGPU_OK;
   }
+  if (opt->algorithm != GWGPU_FISHER_REFERENCE || opt->precision != GWGPU_PREC_FP64) return GWGPU_EINVAL;
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
   std::vector<int> ks(n);

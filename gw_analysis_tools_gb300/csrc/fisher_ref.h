@@ -3,9 +3,8 @@
 // which hands it the sources whose matrices it cannot invert.
 #pragma once
 
+#include "../../include/gwgpu.h"
 #include "phenom_model.h"
-
-struct gwgpu_context;
 
 // Fisher matrices (and, if cov != NULL, inverses) of n sources with host
 // parameters over the registered streams `handles` (reference detector =
@@ -14,3 +13,9 @@ struct gwgpu_context;
 // context lock.
 int gwf_ref_run(gwgpu_context *c, const gwt::GenParams *params, int n, int method, int order, const int *handles,
                 int ndet, double epsilon, int step_mode, int add_prior, double *fisher, double *cov, int *kstatus);
+
+// The moment form (fisher.cu) for n sources; acc64: FP64 per-bin differences,
+// weights and sums instead of FP32 values in compensated FP32 sums.  Takes the
+// context lock.  Sources it cannot invert are redone by gwf_ref_run.
+int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int method, const int *handles, int ndet,
+                   double epsilon, int step_mode, double *fisher, double *covariance, int *status, bool acc64);

@@ -25,6 +25,8 @@ IMRPhenomD = 0
 IMRPhenomPv2 = 1
 PREC_FP64 = 0
 PREC_MIXED = 1
+FISHER_REFERENCE = 0   # gwgpu_fisher_options.algorithm
+FISHER_MOMENTS = 1
 METHODS = {"IMRPhenomD": IMRPhenomD, "IMRPhenomPv2": IMRPhenomPv2}
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "HBM budget exceeded", 4: "outside model domain",
           5: "timed out", 6: "busy", 7: "not found", 8: "too large", 9: "Fisher matrix not positive definite"}
@@ -419,17 +421,20 @@ class Context:
         return fish, cov, status
 
     def fisher_batch_ex(self, params, method, handles, order=2, epsilon=1e-8, step_mode=0, precision=PREC_FP64,
-                        add_prior=False, covariance=True):
+                        add_prior=False, covariance=True, algorithm=FISHER_REFERENCE):
         """fisher_numerical for many sources summed over the detectors of
-        handles (the first is the reference detector): precision PREC_FP64 runs
-        the reference algorithm (orders 2 and 4), PREC_MIXED the moment form."""
+        handles (the first is the reference detector): FISHER_REFERENCE runs
+        the reference algorithm in FP64 (orders 2 and 4), FISHER_MOMENTS the
+        moment form (order 2) with FP64 (PREC_FP64) or compensated FP32
+        (PREC_MIXED) sums."""
         parr = params if isinstance(params, ctypes.Array) else params_array(params)
         n = len(parr)
         hs = np.ascontiguousarray(handles, dtype=np.int32)
         fish = np.zeros((n, 11, 11))
         cov = np.zeros((n, 11, 11)) if covariance else None
         status = np.zeros(n, dtype=np.int32)
-        opt = FisherOptions(int(method), int(order), float(epsilon), int(step_mode), int(precision), int(add_prior))
+        opt = FisherOptions(int(method), int(order), float(epsilon), int(step_mode), int(precision), int(add_prior),
+                            int(algorithm))
         st = self.lib.gwgpu_fisher_batch_ex(self.h, parr, n, _ip(hs), hs.size, ctypes.byref(opt), _dp(fish),
                                             _dp(cov) if cov is not None else None, _ip(status))
         self._check(st, "fisher_batch_ex")
@@ -454,7 +459,8 @@ class FisherOptions(ctypes.Structure):
     """gwgpu_fisher_options."""
 
     _fields_ = [("method", ctypes.c_int), ("order", ctypes.c_int), ("epsilon", ctypes.c_double),
-                ("step_mode", ctypes.c_int), ("precision", ctypes.c_int), ("add_prior", ctypes.c_int)]
+                ("step_mode", ctypes.c_int), ("precision", ctypes.c_int), ("add_prior", ctypes.c_int),
+                ("algorithm", ctypes.c_int)]
 
 
 class ServerConfig(ctypes.Structure):

@@ -301,20 +301,25 @@ int gwgpu_fisher_numerical(gwgpu_context *ctx, const double *frequencies, int le
 int gwgpu_fisher_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, int method, const int *handles,
                        int num_detectors, double epsilon, int step_mode, double *fisher, double *covariance,
                        int *status);
+#define GWGPU_FISHER_REFERENCE 0   /* the reference's algorithm: every perturbed response in FP64 (orders 2 and 4) */
+#define GWGPU_FISHER_MOMENTS 1     /* order 2: analytic extrinsic derivatives, per-bin waveform differences, moment sums */
 typedef struct {
   int method;     /* GWGPU_FISHER_IMRPHENOMD or GWGPU_FISHER_MCMC_IMRPHENOMD */
-  int order;      /* 2 (central) or 4 (five-point, fisher.cpp:426-458) */
+  int order;      /* 2 (central) or 4 (five-point, fisher.cpp:426-458; always GWGPU_FISHER_REFERENCE) */
   double epsilon; /* step (the reference: 1e-8) */
   int step_mode;  /* GWGPU_FISHER_STEP_* */
-  int precision;  /* GWGPU_PREC_MIXED: the moment form (order 2 only); GWGPU_PREC_FP64: the reference algorithm */
+  int precision;  /* GWGPU_PREC_FP64; the moment form also takes GWGPU_PREC_MIXED (FP32 values, compensated FP32 sums) */
   int add_prior;  /* add MCMC_fisher_transformations' prior diagonal (mcmc_gw.cpp:2136-2160) */
+  int algorithm;  /* GWGPU_FISHER_REFERENCE (0) or GWGPU_FISHER_MOMENTS */
 } gwgpu_fisher_options;
 /* fisher_numerical (fisher.h:35-48, fisher.cpp:81-557, 2704-2781) for n
  * sources, summed over the detectors with the first as reference detector.
- * GWGPU_PREC_FP64 runs the reference's algorithm itself on the device: every
- * perturbed response in FP64 (including the constant phase the +-2 eps
+ * GWGPU_FISHER_REFERENCE runs the reference's algorithm itself on the device:
+ * every perturbed response in FP64 (including the constant phase the +-2 eps
  * responses of the five-point rule carry at a non-reference detector,
- * fisher.cpp:426-458), derivatives and Simpson Gram sums in FP64. */
+ * fisher.cpp:426-458), derivatives and Simpson Gram sums in FP64.
+ * GWGPU_FISHER_MOMENTS is the form of gwgpu_fisher_batch, its sums in the
+ * given precision. */
 int gwgpu_fisher_batch_ex(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, const int *handles,
                           int num_detectors, const gwgpu_fisher_options *options, double *fisher, double *covariance,
                           int *status);

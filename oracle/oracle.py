@@ -516,6 +516,19 @@ def fisher_batch(params_list, freqs, detectors, psds, method="IMRPhenomD", epsil
     return out.reshape(n, dim, dim)
 
 
+def mcmc_fisher_prior_diag(dim=11):
+    """The diagonal MCMC_fisher_transformations adds to a non-intrinsic
+    sampler's Fisher matrix (mcmc_gw.cpp:2136-2160): RA, sin DEC, psi,
+    cos iota, phiRef, tc, eta, the two aligned spins, and for the 15-dim
+    precessing vector cos theta1, cos theta2, phi1, phi2; nothing on
+    ln D_L and ln Mc."""
+    tp = 1.0 / (4 * np.pi * np.pi)
+    d = [tp, 1 / 4., tp, 1 / 4., tp, 1 / .01, 0.0, 0.0, 1 / .25, 1 / 4., 1 / 4.]
+    if dim == 15:
+        d += [1 / 4., 1 / 4., tp, tp]
+    return np.array(d[:dim])
+
+
 def cholesky_invert(a):
     a = np.ascontiguousarray(a, dtype=np.float64)
     inv = np.zeros_like(a)

@@ -54,6 +54,54 @@ def test_batched_fisher_network(gpu_ctx, oracle):
         gpu_ctx.release_data(h)
 
 
+@pytest.mark.parametrize("add_prior", [False, True])
+def test_batched_fisher_fp64_sums(gpu_ctx, oracle, add_prior):
+    """The moment form with FP64 per-bin differences and sums
+    (gwgpu_fisher_batch_ex, FISHER_MOMENTS, PREC_FP64) on ordinary and
+    near-degenerate sources: the matrix and its inverse at the FP64 reference
+    algorithm's accuracy, the prior diagonal of MCMC_fisher_transformations
+    added on request."""
+    f = W.uniform_grid(10.0, 2048.0, 1 / 16.)
+    dets = list(W.DETECTORS3)
+    psd = W.analytic_psd(f)
+    hs = [gpu_ctx.register_data(d, f, np.zeros(f.size, complex), psd) for d in dets]
+    pool = W.prior_draws(10000, 13)
+    draws = [pool[i] for i in (228, 3139, 4213, 6593)] + W.prior_draws(12, 83)
+    # the sampler's parameterisation with its prior diagonal, or the plain one
+    method, name = (1, "MCMC_IMRPhenomD") if add_prior else (0, "IMRPhenomD")
+    fish, cov, st = gpu_ctx.fisher_batch_ex(G.params_array(draws), method, hs, order=2, epsilon=1e-6, step_mode=1,
+                                            precision=G.PREC_FP64, algorithm=G.FISHER_MOMENTS, add_prior=add_prior)
+    prior = np.diag(oracle.mcmc_fisher_prior_diag()) if add_prior else 0.0
+    for i, d in enumerate(draws):
+        ref = oracle.fisher_network(f, oracle.params_from_dict(d), dets, [psd] * 3, method=name, epsilon=1e-6,
+                                    step_mode=1) + prior
+        assert _norm_err(fish[i], ref) <= 1e-7, (i, _norm_err(fish[i], ref))
+        ist, rinv = oracle.cholesky_invert(ref)
+        assert st[i] == (0 if ist == 0 else 9), (i, st[i], ist)
+        if ist == 0:
+            cond = np.linalg.cond(ref / np.sqrt(np.outer(np.diag(ref), np.diag(ref))))
+            assert _inv_err(cov[i], rinv) <= 2e-11 * cond, (i, cond, _inv_err(cov[i], rinv))
+    # the FP32-compensated form of the same call
+    fm, _, stm = gpu_ctx.fisher_batch_ex(G.params_array(draws), method, hs, order=2, epsilon=1e-6, step_mode=1,
+                                         precision=G.PREC_MIXED, algorithm=G.FISHER_MOMENTS, add_prior=add_prior)
+    assert np.array_equal(stm, st)
+    for i in range(len(draws)):
+        assert _norm_err(fm[i], fish[i]) <= 1e-4
+    for h in hs:
+        gpu_ctx.release_data(h)
+
+
+def test_fisher_batch_ex_rejects_bad_options(gpu_ctx):
+    f = W.uniform_grid(10.0, 512.0, 1 / 4.)
+    h = gpu_ctx.register_data("Hanford", f, np.zeros(f.size, complex), W.analytic_psd(f))
+    p = G.params_array(W.prior_draws(1, 86))
+    for kw in (dict(order=4, algorithm=G.FISHER_MOMENTS), dict(precision=G.PREC_MIXED),
+               dict(algorithm=7), dict(order=3)):
+        with pytest.raises(G.GwGpuError):
+            gpu_ctx.fisher_batch_ex(p, 0, [h], **kw)
+    gpu_ctx.release_data(h)
+
+
 def test_batched_fisher_refines_singular_sources(gpu_ctx, oracle):
     """Sources whose matrix the FP32-compensated sums leave indefinite (equal
     masses, a face-on orientation) are recomputed by the FP64 reference
