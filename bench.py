@@ -583,9 +583,37 @@ def cpu_baseline(res, seconds=10.0):
     cores = os.cpu_count()
     err = np.abs(res["out_mixed"] - ref)
     return {"value": n / dt, "unit": "evals/s", "cores": cores, "kind": "port",
-            "sample": "%d requests of the 512-request step (prior draws), %.1f s on %d threads" % (n, dt, cores)}, \
+            "sample": "%d requests of the 512-request step (prior draws), %.1f s on %d threads" % (n, dt, cores),
+            "reference_code": reference_code_rate(O, f, dets, data, psd, plist)}, \
         {"max_abs_dlogL": float(err.max()), "p99_abs_dlogL": float(np.percentile(err, 99)),
          "median_abs_dlogL": float(np.median(err)), "requests": int(err.size)}
+
+
+def reference_code_rate(O, f, dets, data, psd, plist, seconds=6.0):
+    """The reference's own MCMC_likelihood_extrinsic (mcmc_gw.cpp:2374-2487,
+    compiled unmodified from its sources by oracle/Makefile target "full") on
+    one host thread, beside the C port on one thread over the same requests:
+    how the port's timing relates to the reference's code on the same cores.
+    Where the reference library was not built (its sources absent on this
+    host) it says so."""
+    if O.ref_full_lib() is None:
+        return {"unavailable": "oracle/_ref/libgwatref_full.so is not built on this host (the reference's sources "
+                               "are absent)"}
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        # the call rewrites t_c in place (mcmc_gw.cpp:2466-2473): a fresh copy each time
+        O.ref_mcmc_likelihood_extrinsic(O.GenParams.from_buffer_copy(plist[n % len(plist)]), f, dets, data, psd)
+        n += 1
+    ref_rate = n / (time.perf_counter() - t0)
+    m, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        O.loglik_batch(plist[:16], f, dets, data, psd, nthreads=1)
+        m += 16
+    port_rate = m / (time.perf_counter() - t0)
+    return {"value": ref_rate, "unit": "evals/s", "cores": 1, "kind": "reference", "port_value_1_core": port_rate,
+            "port_over_reference": port_rate / ref_rate,
+            "sample": "%d calls of MCMC_likelihood_extrinsic, 3 detectors x %d bins, %.0f s per arm" %
+                      (n, len(f), seconds)}
 
 
 def fisher_err(sample):
@@ -761,7 +789,8 @@ def run_reference(args, rank, world):
             "data": "synthetic", "config": {"workload": WORKLOAD, "global_batch": N_REQ},
             "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
                              "sample": "%d steps of %d of the 512 requests (prior draws), OpenMP over requests on "
-                                       "%d threads" % (args.steps, nsample, cores)},
+                                       "%d threads" % (args.steps, nsample, cores),
+                             "reference_code": reference_code_rate(O, f, dets, data, psd, plist)},
             "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     return line
 
