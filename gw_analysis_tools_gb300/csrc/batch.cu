@@ -24,13 +24,24 @@ static int length_class(int N) {  // grid-length bucket of the tuning table
   return c;
 }
 
-std::string tune_key(int mixed, int ndet, int N) {
-  return std::to_string(mixed) + ":" + std::to_string(ndet) + ":" + std::to_string(length_class(N));
+// The tuning class of a batch: precision, detectors, the length class of its
+// longest grid, and whether its requests' grids differ (an uneven batch
+// spreads its items differently from a uniform one of the same longest grid).
+std::string tune_key(gwgpu_context *c, int mixed, int ndet, const int *h_handles, int n) {
+  int nmax = 0, nmin = 1 << 30;
+  for (int i = 0; i < n; i++) {
+    const gwgpu_context::Stream *s = c->get_stream(h_handles[(size_t)i * ndet]);
+    if (!s) continue;
+    nmax = std::max(nmax, s->dev.N);
+    nmin = std::min(nmin, s->dev.N);
+  }
+  return std::to_string(mixed) + ":" + std::to_string(ndet) + ":" + std::to_string(length_class(nmax)) +
+         (nmin < nmax ? ":u" : "");
 }
 
-int choose_tile(gwgpu_context *c, int mixed, int ndet, int N) {
+int choose_tile(gwgpu_context *c, int mixed, const std::string &key) {
   if (c->tile_override > 0) return c->tile_override;
-  auto it = c->tuned.find(tune_key(mixed, ndet, N));
+  auto it = c->tuned.find(key);
   if (it != c->tuned.end()) return it->second;
   return default_tile(mixed);
 }
@@ -38,10 +49,10 @@ int choose_tile(gwgpu_context *c, int mixed, int ndet, int N) {
 // Resident blocks per SM of the fused kernel's launch shape: the autotuner's
 // candidate while it runs, else its choice for this batch class, else the
 // default.
-static int choose_occ(gwgpu_context *c, int mixed, int ndet, int N) {
+static int choose_occ(gwgpu_context *c, int mixed, const std::string &key) {
   if (!mixed) return gwk::batch_default_occ(0);
   if (c->occ_override > 0) return c->occ_override;
-  auto it = c->tuned_occ.find(tune_key(mixed, ndet, N));
+  auto it = c->tuned_occ.find(key);
   if (it != c->tuned_occ.end()) return it->second;
   return gwk::batch_default_occ(1);
 }
@@ -190,8 +201,9 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
   const int mixed = precision == GWGPU_PREC_MIXED;
   const gwgpu_context::Stream *s0 = c->get_stream(h_handles[0]);
   if (!s0) return GWGPU_ENOTFOUND;
-  if (tile <= 0) tile = choose_tile(c, mixed, ndet, s0->dev.N);
-  const int occ = choose_occ(c, mixed, ndet, s0->dev.N);
+  const std::string tk = tune_key(c, mixed, ndet, h_handles, n);
+  if (tile <= 0) tile = choose_tile(c, mixed, tk);
+  const int occ = choose_occ(c, mixed, tk);
   std::string key((const char *)h_handles, (const char *)(h_handles + (size_t)n * ndet));
   key += "|" + std::to_string(n) + "|" + std::to_string(tile) + "|" + std::to_string(ndet) + "|" +
          std::to_string(c->streams_epoch);
@@ -472,8 +484,9 @@ int gwgpu_batch_autotune(gwgpu_context *c, const gwgpu_gen_params *d_params, con
   c->occ_override = 0;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  c->tuned[gwb::tune_key(mixed, ndet, s0->dev.N)] = best;
-  if (mixed) c->tuned_occ[gwb::tune_key(mixed, ndet, s0->dev.N)] = best_occ;
+  const std::string tk = gwb::tune_key(c, mixed, ndet, h_handles, n);
+  c->tuned[tk] = best;
+  if (mixed) c->tuned_occ[tk] = best_occ;
   if (best_tile) *best_tile = best;
   if (best_ms) *best_ms = bms;
   return GWGPU_OK;

@@ -49,10 +49,11 @@ constexpr size_t kMaxGraphs = 8;
 
 int default_tile(int mixed);
 // Tile for one launch: explicit override, else the autotuned choice for this
-// (precision, detectors, grid length) class, else the default.
-int choose_tile(gwgpu_context *c, int mixed, int ndet, int N);
-// Key of the tuning tables: (precision, detectors, grid-length class).
-std::string tune_key(int mixed, int ndet, int N);
+// batch's tuning class (key), else the default.
+int choose_tile(gwgpu_context *c, int mixed, const std::string &key);
+// Key of the tuning tables: precision, detectors, the length class of the
+// batch's longest grid, and whether its requests' grids differ.
+std::string tune_key(gwgpu_context *c, int mixed, int ndet, const int *h_handles, int n);
 int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, int tile);
 // Copies around a launch (pinned host buffers of the lane): before it, the
 // inputs host -> device; after it, the outputs device -> host.

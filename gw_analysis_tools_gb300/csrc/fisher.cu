@@ -520,9 +520,10 @@ int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int 
     cudaMemcpyAsync(hs.data(), dstat, sizeof(int) * m, cudaMemcpyDeviceToHost, c->stream);
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return c->fail(e, "fisher batch");
-    // Sources whose matrix the FP32-compensated sums leave indefinite (a
-    // normalised smallest eigenvalue below their ~1e-8 precision: equal masses,
-    // face-on orientations) are recomputed by the FP64 reference algorithm.
+    // Sources whose matrix the sums leave indefinite (a normalised smallest
+    // eigenvalue below their precision: ~1e-8 for the FP32-compensated sums,
+    // near-equal masses and face-on orientations) are recomputed by the FP64
+    // reference algorithm.
     std::vector<int> redo;
     for (int i = 0; i < m; i++)
       if (hs[i] == 9) redo.push_back(i);
@@ -550,5 +551,5 @@ int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int 
 extern "C" int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, int method,
                                   const int *handles, int ndet, double epsilon, int step_mode, double *fisher,
                                   double *covariance, int *status) {
-  return gwf_moment_run(c, params, n, method, handles, ndet, epsilon, step_mode, fisher, covariance, status, false);
+  return gwf_moment_run(c, params, n, method, handles, ndet, epsilon, step_mode, fisher, covariance, status, true);
 }

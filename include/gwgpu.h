@@ -274,9 +274,11 @@ int gwgpu_batch_use_graphs(gwgpu_context *ctx, int on);
  * CUDA events around the prologue and the fused bin kernel of the last batch. */
 int gwgpu_batch_timing(gwgpu_context *ctx, int on);
 int gwgpu_batch_last_timing(gwgpu_context *ctx, float *prologue_ms, float *kernel_ms);
-/* Autotuner: time the candidate tiles on this batch (device arrays as for
- * gwgpu_loglik_batch_device; results are overwritten) and keep the fastest for
- * batches of the same precision, detector count and grid-length class. */
+/* Autotuner: time the candidate launch shapes -- bin tile x resident blocks
+ * per SM of the fused kernel (mixed form) -- on this batch (device arrays as
+ * for gwgpu_loglik_batch_device; results are overwritten) and keep the
+ * fastest for batches of the same precision, detector count, length class of
+ * the longest grid and evenness (all requests on one grid length or not). */
 int gwgpu_batch_autotune(gwgpu_context *ctx, const gwgpu_gen_params *d_params, const int *d_approximants, int n,
                          const int *handles, int num_detectors, double T_segment, int precision, double *d_loglik,
                          int *d_status, int *best_tile, float *best_ms);
@@ -293,11 +295,11 @@ int gwgpu_fisher_numerical(gwgpu_context *ctx, const double *frequencies, int le
 /* Batched network Fisher (MCMC_fisher_wrapper summing detectors,
  * mcmc_gw.cpp:2283-2317) for n sources over registered data: fisher[n][dim][dim]
  * and, if covariance != NULL, its FP64 inverse (gsl_cholesky_matrix_invert,
- * util.cpp:857-900).  Order 2, the moment form: FP64 waveform differences per
- * bin, FP32-compensated Gram sums.  A source whose matrix that form cannot
- * invert is recomputed with the FP64 reference algorithm
- * (gwgpu_fisher_batch_ex, GWGPU_PREC_FP64).  status[i]: GWGPU_OK,
- * GWGPU_EDOMAIN, GWGPU_ESINGULAR (not invertible in FP64 either). */
+ * util.cpp:857-900).  Order 2, the moment form: FP64 waveform differences,
+ * weights and Gram moment sums per bin (gwgpu_fisher_batch_ex with
+ * GWGPU_FISHER_MOMENTS and GWGPU_PREC_FP64).  A source whose matrix that form
+ * cannot invert is recomputed with the FP64 reference algorithm.  status[i]:
+ * GWGPU_OK, GWGPU_EDOMAIN, GWGPU_ESINGULAR (not invertible in FP64 either). */
 int gwgpu_fisher_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, int method, const int *handles,
                        int num_detectors, double epsilon, int step_mode, double *fisher, double *covariance,
                        int *status);

@@ -29,9 +29,9 @@ def _inv_err(C, R):
 
 
 def test_batched_fisher_network(gpu_ctx, oracle):
-    """The moment form (FP32-compensated Gram sums) against the FP64 oracle on
-    all 16 sources: the Fisher matrix and its inverse, each normalised by the
-    oracle's diagonal."""
+    """gwgpu_fisher_batch (the moment form, FP64 sums) against the FP64 oracle
+    on all 16 sources: the Fisher matrix and its inverse, each normalised by
+    the oracle's diagonal."""
     f = W.uniform_grid(10.0, 2048.0, 1 / 16.)
     dets = list(W.DETECTORS3)
     psd = W.analytic_psd(f)
@@ -49,7 +49,7 @@ def test_batched_fisher_network(gpu_ctx, oracle):
         # the inverse's error is the matrix's error in its weakest direction
         # times the condition number of the normalised matrix (1e5-1e8 here)
         cond = np.linalg.cond(ref / np.sqrt(np.outer(np.diag(ref), np.diag(ref))))
-        assert _inv_err(cov[i], rinv) <= 2e-9 * cond, (i, cond, _inv_err(cov[i], rinv))
+        assert _inv_err(cov[i], rinv) <= 2e-11 * cond, (i, cond, _inv_err(cov[i], rinv))
     for h in hs:
         gpu_ctx.release_data(h)
 
@@ -75,7 +75,10 @@ def test_batched_fisher_fp64_sums(gpu_ctx, oracle, add_prior):
     for i, d in enumerate(draws):
         ref = oracle.fisher_network(f, oracle.params_from_dict(d), dets, [psd] * 3, method=name, epsilon=1e-6,
                                     step_mode=1) + prior
-        assert _norm_err(fish[i], ref) <= 1e-7, (i, _norm_err(fish[i], ref))
+        # both sides FP64: the rounding differences of two implementations
+        # divided by the 1e-6 step (up to 2e-5 normalised on the four
+        # near-degenerate sources, normalised smallest eigenvalue 2e-10-4e-9)
+        assert _norm_err(fish[i], ref) <= (1e-4 if i < 4 else 1e-5), (i, _norm_err(fish[i], ref))
         ist, rinv = oracle.cholesky_invert(ref)
         assert st[i] == (0 if ist == 0 else 9), (i, st[i], ist)
         if ist == 0:
@@ -103,23 +106,32 @@ def test_fisher_batch_ex_rejects_bad_options(gpu_ctx):
 
 
 def test_batched_fisher_refines_singular_sources(gpu_ctx, oracle):
-    """Sources whose matrix the FP32-compensated sums leave indefinite (equal
-    masses, a face-on orientation) are recomputed by the FP64 reference
-    algorithm: status OK and the oracle's matrix."""
+    """Sources whose matrix the FP32-compensated sums (PREC_MIXED) leave
+    indefinite (equal masses, a face-on orientation) are recomputed by the FP64
+    reference algorithm: status OK and the oracle's matrix."""
     f = W.uniform_grid(10.0, 2048.0, 1 / 16.)
     dets = list(W.DETECTORS3)
     psd = W.analytic_psd(f)
     hs = [gpu_ctx.register_data(d, f, np.zeros(f.size, complex), psd) for d in dets]
     pool = W.prior_draws(10000, 13)
     draws = [pool[i] for i in (228, 3139, 4213, 6593, 8425, 4968)] + W.prior_draws(6, 84)
-    fish, cov, st = gpu_ctx.fisher_batch(G.params_array(draws), 0, hs, epsilon=1e-6, step_mode=1)
+    fish, cov, st = gpu_ctx.fisher_batch_ex(G.params_array(draws), 0, hs, epsilon=1e-6, step_mode=1,
+                                            precision=G.PREC_MIXED, algorithm=G.FISHER_MOMENTS)
     for i, d in enumerate(draws):
         ref = oracle.fisher_network(f, oracle.params_from_dict(d), dets, [psd] * 3, epsilon=1e-6, step_mode=1)
         # near-degenerate sources: the FP64 rounding of two implementations,
         # divided by steps of 1e-6 of parameters near zero
         assert _norm_err(fish[i], ref) <= 1e-4, i
         ist, _ = oracle.cholesky_invert(ref)
-        assert st[i] == (0 if ist == 0 else 9), (i, st[i], ist)
+        dn = np.sqrt(np.abs(np.diag(ref)))
+        if np.linalg.eigvalsh(ref / np.outer(dn, dn))[0] < 1e-13:
+            # singular to FP64 rounding (4968: within 3 degrees of face-on,
+            # normalised smallest eigenvalue 6e-15): whether a Cholesky
+            # factorisation succeeds is decided by the rounding of each
+            # implementation
+            assert st[i] in (0, 9)
+        else:
+            assert st[i] == (0 if ist == 0 else 9), (i, st[i], ist)
     for h in hs:
         gpu_ctx.release_data(h)
 
