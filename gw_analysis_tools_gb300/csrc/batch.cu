@@ -138,7 +138,8 @@ int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, i
     pos += count[r];
   }
   pl.nitems = (int)sorted.size();
-  size_t need = sizeof(gwk::Item) * sorted.size() + 256 + sizeof(int) * (size_t)n * (2 + ndet) + 256;
+  size_t need = sizeof(gwk::Item) * sorted.size() + 256 + sizeof(int) * (size_t)n * (2 + ndet) + 256 +
+                sizeof(int) * sorted.size() + 256;
   int st = lane_alloc(c, L, &pl.mem, &pl.cap, need, "batch plan");
   if (st) return st;
   char *p = (char *)pl.mem;
@@ -147,6 +148,7 @@ int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, i
   pl.item_start = (int *)p;
   pl.item_count = pl.item_start + n;
   pl.handles = pl.item_count + n;
+  pl.order = (int *)align256((char *)(pl.handles + (size_t)n * ndet));
   cudaMemcpyAsync(pl.items, sorted.data(), sizeof(gwk::Item) * sorted.size(), cudaMemcpyHostToDevice, L.stream);
   cudaMemcpyAsync(pl.item_start, nstart.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
   cudaMemcpyAsync(pl.item_count, count.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
@@ -169,7 +171,6 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
       (const gwt::GenParams *)d_params, d_approx, n, pl.handles, ndet, T_segment, 1, c->streams_dev, c->qnm_dev,
       mixed ? nullptr : (gwt::Request *)reqs, mixed ? (gwt::MixedReq *)reqs : nullptr, mixed, d_status, L.stream);
   if (e != cudaSuccess) return c->fail(e, "prologue launch");
-  if (timing) cudaEventRecord(c->t_ev[1], L.stream);
   gwk::BatchArgs a;
   a.req = mixed ? nullptr : (const gwt::Request *)reqs;
   a.mreq = mixed ? (const gwt::MixedReq *)reqs : nullptr;
@@ -177,6 +178,7 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   a.ndet = ndet;
   a.streams = c->streams_dev;
   a.items = pl.items;
+  a.order = nullptr;
   a.nitems = pl.nitems;
   a.item_start = pl.item_start;
   a.item_count = pl.item_count;
@@ -187,6 +189,13 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   a.out = d_out;
   a.status = d_status;
   a.tables = c->tables;
+  if (mixed && c->order_items) {
+    e = gwk::launch_order_items((const gwt::MixedReq *)reqs, pl.items, pl.nitems, pl.tile, pl.handles, ndet,
+                                c->streams_dev, pl.order, L.stream);
+    if (e != cudaSuccess) return c->fail(e, "item order launch");
+    a.order = pl.order;
+  }
+  if (timing) cudaEventRecord(c->t_ev[1], L.stream);  // prologue and item order | bin kernel
   int grid = std::min(pl.nitems, persistent_grid(c->device, mixed, ndet, occ));
   if (grid < 1) grid = 1;
   e = gwk::launch_batch(a, mixed, grid, occ, L.stream);

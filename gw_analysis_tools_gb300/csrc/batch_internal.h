@@ -21,6 +21,7 @@ struct Plan {
   size_t cap = 0;
   gwk::Item *items = nullptr;
   int *item_start = nullptr, *item_count = nullptr, *handles = nullptr;
+  int *order = nullptr;  // nitems: the execution order the mixed batch writes before each launch
 };
 
 // Scratch of one in-flight batch.  Owned by the context (lane 0, the context

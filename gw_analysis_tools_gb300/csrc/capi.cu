@@ -233,6 +233,10 @@ int gwgpu_context_create(int device, size_t budget, gwgpu_context **out) {
   // (the reference's order of operations) instead of the cooperative kernel
   const char *pro = std::getenv("GWGPU_PROLOGUE");
   c->prologue_serial = pro && std::strcmp(pro, "serial") == 0;
+  // GWGPU_ITEM_ORDER=listed: the mixed batch's items in plan order instead of
+  // most live bins first
+  const char *io = std::getenv("GWGPU_ITEM_ORDER");
+  c->order_items = !(io && std::strcmp(io, "listed") == 0);
   // GWGPU_MAXLL=fp64: the maximised likelihood with FP64 transforms only
   const char *mx = std::getenv("GWGPU_MAXLL");
   c->maxll_fp64 = mx && std::strcmp(mx, "fp64") == 0;

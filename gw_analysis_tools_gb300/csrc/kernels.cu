@@ -618,7 +618,8 @@ __global__ void __launch_bounds__(kBatchBlock, OCC) k_batch(const BatchArgs a) {
     __syncthreads();
     const int it = s_item;
     if (it >= a.nitems) break;
-    const Item I = a.items[it];
+    const int iid = a.order ? __ldg(a.order + it) : it;  // the item's own index: its partials' slot
+    const Item I = a.items[iid];
     // stage the request constants and its streams
     {
       const unsigned *src = MIXED ? (const unsigned *)(a.mreq + I.req) : (const unsigned *)(a.req + I.req);
@@ -790,7 +791,7 @@ __global__ void __launch_bounds__(kBatchBlock, OCC) k_batch(const BatchArgs a) {
         for (int j = 0; j < NV; j++) s_res[j] = v[j];
       __syncthreads();
     }
-    if (tid < NV) a.partials[(size_t)it * kAcc + tid] = s_res[tid];
+    if (tid < NV) a.partials[(size_t)iid * kAcc + tid] = s_res[tid];
     // last item of this request: fixed-order FP64 sum and log L
     if (arrive_last(a.req_done + I.req, (unsigned)a.item_count[I.req])) {
       if constexpr (MIXED) {
@@ -862,6 +863,53 @@ int batch_occupancy(int mixed, int ndet, int occ) {
   if (!f) return 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, kBatchBlock, 0) != cudaSuccess) return 1;
   return nb;
+}
+
+// Longest-processing-time-first order for the persistent mixed kernel: an
+// item's work is its live 256-bin passes (bins below the request's cut
+// f <= 0.2/M, where the model is non-zero; beyond it a pass costs nothing), and
+// requests of one batch differ several-fold in it.  A counting sort over the
+// number of live passes, most first, so that the grid drains on cheap items.
+// The order inside a bucket depends on atomics; results do not (partials are
+// indexed by item, and each request's finalize sums them in item order).
+constexpr int kOrderBlock = 1024, kOrderBuckets = 65;
+__global__ void __launch_bounds__(kOrderBlock) k_order_items(const MixedReq *__restrict__ mreq,
+                                                             const Item *__restrict__ items, int nitems, int tile,
+                                                             const int *__restrict__ handles, int ndet,
+                                                             const StreamDev *__restrict__ streams, int *order) {
+  __shared__ int hist[kOrderBuckets], off[kOrderBuckets];
+  const int tid = threadIdx.x;
+  const int npass = (tile + kSegBins - 1) / kSegBins;
+  auto bucket = [&](int i) {
+    const Item I = items[i];
+    int live = 0;
+    if (mreq[I.req].status == 0) {
+      const StreamDev &s = streams[handles[(size_t)I.req * ndet]];
+      const int kcut = min(s.N, mreq[I.req].n_cut - s.n0 + 1);
+      live = max(0, min(kcut, I.k0 + tile) - I.k0);
+    }
+    const int lp = min(npass, (live + kSegBins - 1) / kSegBins);
+    return (int)((long long)(npass - lp) * (kOrderBuckets - 1) / npass);  // 0: all passes live
+  };
+  for (int b = tid; b < kOrderBuckets; b += blockDim.x) hist[b] = 0;
+  __syncthreads();
+  for (int i = tid; i < nitems; i += blockDim.x) atomicAdd(&hist[bucket(i)], 1);
+  __syncthreads();
+  if (tid == 0) {
+    int sum = 0;
+    for (int b = 0; b < kOrderBuckets; b++) {
+      off[b] = sum;
+      sum += hist[b];
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < nitems; i += blockDim.x) order[atomicAdd(&off[bucket(i)], 1)] = i;
+}
+
+cudaError_t launch_order_items(const MixedReq *mreq, const Item *items, int nitems, int tile, const int *handles,
+                               int ndet, const StreamDev *streams, int *order, cudaStream_t s) {
+  k_order_items<<<1, kOrderBlock, 0, s>>>(mreq, items, nitems, tile, handles, ndet, streams, order);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s) {

@@ -78,6 +78,7 @@ struct BatchArgs {
   int ndet;
   const StreamDev *streams;
   const Item *items;
+  const int *order;  // execution order of the items (nullptr: as listed); partials stay indexed by item
   int nitems;
   const int *item_start;  // per request
   const int *item_count;
@@ -91,6 +92,10 @@ struct BatchArgs {
 };
 // occ: the launch shape's resident blocks per SM (mixed 3 or 4, FP64 2)
 cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s);
+// The mixed batch's items ordered by their live bins (below each request's
+// waveform cut), most first, into order[nitems]; one block.
+cudaError_t launch_order_items(const MixedReq *mreq, const Item *items, int nitems, int tile, const int *handles,
+                               int ndet, const StreamDev *streams, int *order, cudaStream_t s);
 int batch_default_occ(int mixed);
 int batch_block_size(int mixed);
 int batch_occupancy(int mixed, int ndet, int occ);  // resident blocks per SM
