@@ -190,8 +190,8 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   a.status = d_status;
   a.tables = c->tables;
   if (mixed && c->order_items) {
-    e = gwk::launch_order_items((const gwt::MixedReq *)reqs, pl.items, pl.nitems, pl.tile, pl.handles, ndet,
-                                c->streams_dev, pl.order, L.stream);
+    e = gwk::launch_order_items((const gwt::MixedReq *)reqs, n, pl.item_start, pl.item_count, pl.tile, pl.handles,
+                                ndet, c->streams_dev, pl.order, L.stream);
     if (e != cudaSuccess) return c->fail(e, "item order launch");
     a.order = pl.order;
   }
@@ -210,12 +210,16 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
   const int mixed = precision == GWGPU_PREC_MIXED;
   const gwgpu_context::Stream *s0 = c->get_stream(h_handles[0]);
   if (!s0) return GWGPU_ENOTFOUND;
-  const std::string tk = tune_key(c, mixed, ndet, h_handles, n);
-  if (tile <= 0) tile = choose_tile(c, mixed, tk);
-  const int occ = choose_occ(c, mixed, tk);
   std::string key((const char *)h_handles, (const char *)(h_handles + (size_t)n * ndet));
-  key += "|" + std::to_string(n) + "|" + std::to_string(tile) + "|" + std::to_string(ndet) + "|" +
-         std::to_string(c->streams_epoch);
+  key += "|" + std::to_string(n) + "|" + std::to_string(ndet) + "|" + std::to_string(c->streams_epoch) + "|" +
+         std::to_string(mixed);
+  if (L.tk_shape != key) {  // the tuning class follows from the handles: recomputed when they change
+    L.tk = tune_key(c, mixed, ndet, h_handles, n);
+    L.tk_shape = key;
+  }
+  if (tile <= 0) tile = choose_tile(c, mixed, L.tk);
+  const int occ = choose_occ(c, mixed, L.tk);
+  key += "|" + std::to_string(tile);
   bool replanned = false;
   if (L.plan.key != key) {
     int st = plan_batch(c, L, n, h_handles, ndet, tile);

@@ -44,6 +44,8 @@ struct Lane {
   std::map<std::string, Graph> graphs;
   uint64_t graph_tick = 0;
   size_t bytes = 0;  // device bytes held (budget accounting)
+  // tuning class of the last batch shape (handles, precision, registration epoch)
+  std::string tk_shape, tk;
 };
 
 constexpr size_t kMaxGraphs = 8;

@@ -873,27 +873,35 @@ int batch_occupancy(int mixed, int ndet, int occ) {
 // The order inside a bucket depends on atomics; results do not (partials are
 // indexed by item, and each request's finalize sums them in item order).
 constexpr int kOrderBlock = 1024, kOrderBuckets = 65;
-__global__ void __launch_bounds__(kOrderBlock) k_order_items(const MixedReq *__restrict__ mreq,
-                                                             const Item *__restrict__ items, int nitems, int tile,
+// Bucket of a tile with lp of its np passes live: 0 when all are live.
+__device__ __forceinline__ int order_bucket(int lp, int np) {
+  return (int)((long long)(np - lp) * (kOrderBuckets - 1) / np);
+}
+// Request r's items are item_start[r] + t (t = 0 .. item_count[r]) with first
+// bin t * tile; its live bins end at kcut (below the cut and the grid).
+__device__ __forceinline__ int order_kcut(const MixedReq *__restrict__ mreq, const int *__restrict__ handles,
+                                          int ndet, const StreamDev *__restrict__ streams, int r) {
+  if (mreq[r].status != 0) return 0;
+  const StreamDev &s = streams[handles[(size_t)r * ndet]];
+  return min(s.N, mreq[r].n_cut - s.n0 + 1);
+}
+__global__ void __launch_bounds__(kOrderBlock) k_order_items(const MixedReq *__restrict__ mreq, int n,
+                                                             const int *__restrict__ item_start,
+                                                             const int *__restrict__ item_count, int tile,
                                                              const int *__restrict__ handles, int ndet,
                                                              const StreamDev *__restrict__ streams, int *order) {
   __shared__ int hist[kOrderBuckets], off[kOrderBuckets];
   const int tid = threadIdx.x;
-  const int npass = (tile + kSegBins - 1) / kSegBins;
-  auto bucket = [&](int i) {
-    const Item I = items[i];
-    int live = 0;
-    if (mreq[I.req].status == 0) {
-      const StreamDev &s = streams[handles[(size_t)I.req * ndet]];
-      const int kcut = min(s.N, mreq[I.req].n_cut - s.n0 + 1);
-      live = max(0, min(kcut, I.k0 + tile) - I.k0);
-    }
-    const int lp = min(npass, (live + kSegBins - 1) / kSegBins);
-    return (int)((long long)(npass - lp) * (kOrderBuckets - 1) / npass);  // 0: all passes live
-  };
+  const int np = (tile + kSegBins - 1) / kSegBins;
   for (int b = tid; b < kOrderBuckets; b += blockDim.x) hist[b] = 0;
   __syncthreads();
-  for (int i = tid; i < nitems; i += blockDim.x) atomicAdd(&hist[bucket(i)], 1);
+  for (int r = tid; r < n; r += blockDim.x) {
+    const int kcut = order_kcut(mreq, handles, ndet, streams, r), nt = item_count[r];
+    for (int t = 0; t < nt; t++) {
+      const int live = max(0, min(kcut - t * tile, tile));
+      atomicAdd(&hist[order_bucket(min(np, (live + kSegBins - 1) / kSegBins), np)], 1);
+    }
+  }
   __syncthreads();
   if (tid == 0) {
     int sum = 0;
@@ -903,12 +911,18 @@ __global__ void __launch_bounds__(kOrderBlock) k_order_items(const MixedReq *__r
     }
   }
   __syncthreads();
-  for (int i = tid; i < nitems; i += blockDim.x) order[atomicAdd(&off[bucket(i)], 1)] = i;
+  for (int r = tid; r < n; r += blockDim.x) {
+    const int kcut = order_kcut(mreq, handles, ndet, streams, r), nt = item_count[r], i0 = item_start[r];
+    for (int t = 0; t < nt; t++) {
+      const int live = max(0, min(kcut - t * tile, tile));
+      order[atomicAdd(&off[order_bucket(min(np, (live + kSegBins - 1) / kSegBins), np)], 1)] = i0 + t;
+    }
+  }
 }
 
-cudaError_t launch_order_items(const MixedReq *mreq, const Item *items, int nitems, int tile, const int *handles,
-                               int ndet, const StreamDev *streams, int *order, cudaStream_t s) {
-  k_order_items<<<1, kOrderBlock, 0, s>>>(mreq, items, nitems, tile, handles, ndet, streams, order);
+cudaError_t launch_order_items(const MixedReq *mreq, int n, const int *item_start, const int *item_count, int tile,
+                               const int *handles, int ndet, const StreamDev *streams, int *order, cudaStream_t s) {
+  k_order_items<<<1, kOrderBlock, 0, s>>>(mreq, n, item_start, item_count, tile, handles, ndet, streams, order);
   return cudaGetLastError();
 }
 

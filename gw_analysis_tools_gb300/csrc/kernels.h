@@ -94,8 +94,8 @@ struct BatchArgs {
 cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s);
 // The mixed batch's items ordered by their live bins (below each request's
 // waveform cut), most first, into order[nitems]; one block.
-cudaError_t launch_order_items(const MixedReq *mreq, const Item *items, int nitems, int tile, const int *handles,
-                               int ndet, const StreamDev *streams, int *order, cudaStream_t s);
+cudaError_t launch_order_items(const MixedReq *mreq, int n, const int *item_start, const int *item_count, int tile,
+                               const int *handles, int ndet, const StreamDev *streams, int *order, cudaStream_t s);
 int batch_default_occ(int mixed);
 int batch_block_size(int mixed);
 int batch_occupancy(int mixed, int ndet, int occ);  // resident blocks per SM
