@@ -138,7 +138,7 @@ int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, i
     pos += count[r];
   }
   pl.nitems = (int)sorted.size();
-  size_t need = sizeof(gwk::Item) * sorted.size() + 256 + sizeof(int) * (size_t)n * (2 + ndet) + 256 +
+  size_t need = sizeof(gwk::Item) * sorted.size() + 256 + sizeof(int) * (size_t)n * (4 + ndet) + 256 +
                 sizeof(int) * sorted.size() + 256;
   int st = lane_alloc(c, L, &pl.mem, &pl.cap, need, "batch plan");
   if (st) return st;
@@ -148,7 +148,17 @@ int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, i
   pl.item_start = (int *)p;
   pl.item_count = pl.item_start + n;
   pl.handles = pl.item_count + n;
-  pl.order = (int *)align256((char *)(pl.handles + (size_t)n * ndet));
+  pl.req_n0 = pl.handles + (size_t)n * ndet;
+  pl.req_N = pl.req_n0 + n;
+  pl.order = (int *)align256((char *)(pl.req_N + n));
+  std::vector<int> rn0(n), rN(n);
+  for (int r = 0; r < n; r++) {
+    const gwgpu_context::Stream *s0 = c->get_stream(handles[r * ndet]);
+    rn0[r] = s0->dev.n0;
+    rN[r] = s0->dev.N;
+  }
+  cudaMemcpyAsync(pl.req_n0, rn0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
+  cudaMemcpyAsync(pl.req_N, rN.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
   cudaMemcpyAsync(pl.items, sorted.data(), sizeof(gwk::Item) * sorted.size(), cudaMemcpyHostToDevice, L.stream);
   cudaMemcpyAsync(pl.item_start, nstart.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
   cudaMemcpyAsync(pl.item_count, count.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
@@ -190,15 +200,15 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   a.status = d_status;
   a.tables = c->tables;
   if (mixed && c->order_items) {
-    e = gwk::launch_order_items((const gwt::MixedReq *)reqs, n, pl.item_start, pl.item_count, pl.tile, pl.handles,
-                                ndet, c->streams_dev, pl.order, L.stream);
+    e = gwk::launch_order_items((const gwt::MixedReq *)reqs, n, pl.item_start, pl.item_count, pl.tile, pl.req_n0,
+                                pl.req_N, pl.order, L.stream, c->pdl);
     if (e != cudaSuccess) return c->fail(e, "item order launch");
     a.order = pl.order;
   }
   if (timing) cudaEventRecord(c->t_ev[1], L.stream);  // prologue and item order | bin kernel
   int grid = std::min(pl.nitems, persistent_grid(c->device, mixed, ndet, occ));
   if (grid < 1) grid = 1;
-  e = gwk::launch_batch(a, mixed, grid, occ, L.stream);
+  e = gwk::launch_batch(a, mixed, grid, occ, L.stream, c->pdl);
   if (e != cudaSuccess) return c->fail(e, "batch launch");
   if (timing) cudaEventRecord(c->t_ev[2], L.stream);
   return GWGPU_OK;

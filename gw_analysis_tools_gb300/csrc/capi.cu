@@ -237,6 +237,9 @@ int gwgpu_context_create(int device, size_t budget, gwgpu_context **out) {
   // most live bins first
   const char *io = std::getenv("GWGPU_ITEM_ORDER");
   c->order_items = !(io && std::strcmp(io, "listed") == 0);
+  // GWGPU_PDL=0: the batch kernels launched as plain stream successors
+  const char *pd = std::getenv("GWGPU_PDL");
+  c->pdl = !(pd && std::strcmp(pd, "0") == 0);
   // GWGPU_MAXLL=fp64: the maximised likelihood with FP64 transforms only
   const char *mx = std::getenv("GWGPU_MAXLL");
   c->maxll_fp64 = mx && std::strcmp(mx, "fp64") == 0;

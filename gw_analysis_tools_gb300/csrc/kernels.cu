@@ -320,6 +320,14 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 //   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions;  W3 D: detector phases and factors /
 //       Pv2: time shift, angles
 //   S6  W0 Pv2: detector phases and factors; outputs
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream-serialisation attribute may start while the one before it on the
+// stream still runs; grid_dep_wait() returns once that kernel has completed
+// and its memory is visible, and grid_dep_trigger() lets the next kernel start
+// launching.  Without the attribute both are no-ops.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 constexpr int kCoopWarps = 4, kCoopReq = 16;
 __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     const GenParams *__restrict__ params, const int *__restrict__ approx, int n, const int *__restrict__ handles,
@@ -336,6 +344,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   __shared__ int s_st[kCoopReq], s_bad[kCoopReq], s_uni[kCoopReq];
   __shared__ double s_pm[kCoopReq][2];  // D: final spin and radiated energy, for post_merger in S1
   static_assert(2 * kCoopReq == 32, "two half-warps per warp share the block's requests");
+  grid_dep_trigger();  // the item order / bin kernel may launch and wait for this grid
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kCoopReq + lane;
   const bool act = lane < kCoopReq && i < n;
@@ -613,6 +622,7 @@ __global__ void __launch_bounds__(kBatchBlock, OCC) k_batch(const BatchArgs a) {
   __shared__ float2 s_rot_seg[kSegBuf * (MIXED ? NDET : 1)];
   __shared__ float2 s_rot_off[(MIXED ? NDET : 1) * (MIXED ? kBatchBlock : 1)];
   const int tid = threadIdx.x;
+  grid_dep_wait();  // the prologue's (and item order's) output
   for (;;) {
     if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
     __syncthreads();
@@ -878,41 +888,59 @@ __device__ __forceinline__ int order_bucket(int lp, int np) {
   return (int)((long long)(np - lp) * (kOrderBuckets - 1) / np);
 }
 // Request r's items are item_start[r] + t (t = 0 .. item_count[r]) with first
-// bin t * tile; its live bins end at kcut (below the cut and the grid).
-__device__ __forceinline__ int order_kcut(const MixedReq *__restrict__ mreq, const int *__restrict__ handles,
-                                          int ndet, const StreamDev *__restrict__ streams, int r) {
+// bin t * tile; its live bins end at kcut (below the cut and the grid of N
+// bins starting at n0).
+__device__ __forceinline__ int order_kcut(const MixedReq *__restrict__ mreq, const int *__restrict__ req_n0,
+                                          const int *__restrict__ req_N, int r) {
   if (mreq[r].status != 0) return 0;
-  const StreamDev &s = streams[handles[(size_t)r * ndet]];
-  return min(s.N, mreq[r].n_cut - s.n0 + 1);
+  return min(req_N[r], mreq[r].n_cut - req_n0[r] + 1);
 }
 __global__ void __launch_bounds__(kOrderBlock) k_order_items(const MixedReq *__restrict__ mreq, int n,
                                                              const int *__restrict__ item_start,
                                                              const int *__restrict__ item_count, int tile,
-                                                             const int *__restrict__ handles, int ndet,
-                                                             const StreamDev *__restrict__ streams, int *order) {
+                                                             const int *__restrict__ req_n0,
+                                                             const int *__restrict__ req_N, int *order) {
+  constexpr int kPerLane = (kOrderBuckets + 31) / 32;
   __shared__ int hist[kOrderBuckets], off[kOrderBuckets];
+  grid_dep_trigger();
+  grid_dep_wait();  // the prologue's request records
   const int tid = threadIdx.x;
   const int np = (tile + kSegBins - 1) / kSegBins;
   for (int b = tid; b < kOrderBuckets; b += blockDim.x) hist[b] = 0;
   __syncthreads();
   for (int r = tid; r < n; r += blockDim.x) {
-    const int kcut = order_kcut(mreq, handles, ndet, streams, r), nt = item_count[r];
+    const int kcut = order_kcut(mreq, req_n0, req_N, r), nt = item_count[r];
     for (int t = 0; t < nt; t++) {
       const int live = max(0, min(kcut - t * tile, tile));
       atomicAdd(&hist[order_bucket(min(np, (live + kSegBins - 1) / kSegBins), np)], 1);
     }
   }
   __syncthreads();
-  if (tid == 0) {
-    int sum = 0;
-    for (int b = 0; b < kOrderBuckets; b++) {
-      off[b] = sum;
-      sum += hist[b];
+  if (tid < 32) {  // exclusive prefix of the buckets: kPerLane consecutive buckets per lane, then a warp scan
+    int v[kPerLane], s = 0;
+#pragma unroll
+    for (int q = 0; q < kPerLane; q++) {
+      const int b = tid * kPerLane + q;
+      v[q] = b < kOrderBuckets ? hist[b] : 0;
+      s += v[q];
+    }
+    int incl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (tid >= o) incl += y;
+    }
+    int run = incl - s;
+#pragma unroll
+    for (int q = 0; q < kPerLane; q++) {
+      const int b = tid * kPerLane + q;
+      if (b < kOrderBuckets) off[b] = run;
+      run += v[q];
     }
   }
   __syncthreads();
   for (int r = tid; r < n; r += blockDim.x) {
-    const int kcut = order_kcut(mreq, handles, ndet, streams, r), nt = item_count[r], i0 = item_start[r];
+    const int kcut = order_kcut(mreq, req_n0, req_N, r), nt = item_count[r], i0 = item_start[r];
     for (int t = 0; t < nt; t++) {
       const int live = max(0, min(kcut - t * tile, tile));
       order[atomicAdd(&off[order_bucket(min(np, (live + kSegBins - 1) / kSegBins), np)], 1)] = i0 + t;
@@ -920,17 +948,32 @@ __global__ void __launch_bounds__(kOrderBlock) k_order_items(const MixedReq *__r
   }
 }
 
-cudaError_t launch_order_items(const MixedReq *mreq, int n, const int *item_start, const int *item_count, int tile,
-                               const int *handles, int ndet, const StreamDev *streams, int *order, cudaStream_t s) {
-  k_order_items<<<1, kOrderBlock, 0, s>>>(mreq, n, item_start, item_count, tile, handles, ndet, streams, order);
-  return cudaGetLastError();
+static cudaError_t launch_dependent(const void *f, dim3 grid, dim3 block, void **args, cudaStream_t s, bool pdl) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelExC(&cfg, f, args);
 }
 
-cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s) {
+cudaError_t launch_order_items(const MixedReq *mreq, int n, const int *item_start, const int *item_count, int tile,
+                               const int *req_n0, const int *req_N, int *order, cudaStream_t s, bool pdl) {
+  void *args[] = {(void *)&mreq, (void *)&n, (void *)&item_start, (void *)&item_count, (void *)&tile,
+                  (void *)&req_n0, (void *)&req_N, (void *)&order};
+  return launch_dependent((const void *)k_order_items, dim3(1), dim3(kOrderBlock), args, s, pdl);
+}
+
+cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s, bool pdl) {
   const void *f = batch_fn(mixed, a.ndet, occ);
   if (!f) return cudaErrorInvalidValue;
   void *args[] = {(void *)&a};
-  return cudaLaunchKernel(f, dim3(grid), dim3(kBatchBlock), args, 0, s);
+  return launch_dependent(f, dim3(grid), dim3(kBatchBlock), args, s, pdl);
 }
 
 void qnm_host_table(double *o) { qnm_fill(o, gwt_qnm_a_h, gwt_qnm_fring_h, gwt_qnm_fdamp_h); }

@@ -90,12 +90,14 @@ struct BatchArgs {
   int *status;
   gwt::Tables tables;
 };
-// occ: the launch shape's resident blocks per SM (mixed 3 or 4, FP64 2)
-cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s);
+// occ: the launch shape's resident blocks per SM (mixed 3 or 4, FP64 2);
+// pdl: launched as a programmatic dependent of the kernel before it on s
+// (it starts launching while that one runs and waits for its completion).
+cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s, bool pdl);
 // The mixed batch's items ordered by their live bins (below each request's
 // waveform cut), most first, into order[nitems]; one block.
 cudaError_t launch_order_items(const MixedReq *mreq, int n, const int *item_start, const int *item_count, int tile,
-                               const int *handles, int ndet, const StreamDev *streams, int *order, cudaStream_t s);
+                               const int *req_n0, const int *req_N, int *order, cudaStream_t s, bool pdl);
 int batch_default_occ(int mixed);
 int batch_block_size(int mixed);
 int batch_occupancy(int mixed, int ndet, int occ);  // resident blocks per SM
