@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the secondary forms")
     ap.add_argument("--forms", default="", help="comma-separated secondary forms to run (default: all)")
+    ap.add_argument("--tile", type=int, default=0, help="fixed bin tile of the headline step (0: autotuned)")
+    ap.add_argument("--blocks-per-sm", type=int, default=0,
+                    help="fixed resident blocks per SM of the headline step (0: autotuned)")
     return ap.parse_args()
 
 
@@ -193,13 +196,19 @@ def run_ours(args, rank, world, local, pg):
         ctx.loglik_batch_device(d_params[b].data_ptr(), d_approx.data_ptr(), N_REQ, handles, T, prec,
                                 d_out[b].data_ptr(), d_stat[b].data_ptr())
 
-    log("autotune")
-    # autotune the tile once on this workload, then warm up (graph capture)
-    tile, _ = ctx.autotune(d_params[0].data_ptr(), d_approx.data_ptr(), N_REQ, handles, T, G.PREC_MIXED,
-                           d_out[0].data_ptr(), d_stat[0].data_ptr())
+    if args.tile or args.blocks_per_sm:
+        # a fixed launch shape (profiling a given shape)
+        ctx.set_tile(args.tile)
+        ctx.set_blocks_per_sm(args.blocks_per_sm)
+    else:
+        log("autotune")
+        # autotune the launch shape once on this workload, then warm up (graph capture)
+        ctx.autotune(d_params[0].data_ptr(), d_approx.data_ptr(), N_REQ, handles, T, G.PREC_MIXED,
+                     d_out[0].data_ptr(), d_stat[0].data_ptr())
     for i in range(args.warmup):
         step(i % nbatch)
     torch.cuda.synchronize()
+    tile, blocks_per_sm, grid = ctx.last_launch_shape()
 
     log("timed steps")
     # ---------------- value: device-resident, CUDA events on the engine stream
@@ -262,6 +271,8 @@ def run_ours(args, rank, world, local, pg):
     res = {}
     res.update(dict(value=value, tot_ms=tot_ms, step_ms=step_ms, kernel_ms=kernel_ms, prologue_ms=prologue_ms,
                     e2e_value=e2e_value, h2d=h2d, d2h=d2h, clocks=clk.summary(), tile=tile,
+                    launch_shape={"tile": tile, "blocks_per_sm": blocks_per_sm, "grid": grid,
+                                  "chosen_by": "fixed" if (args.tile or args.blocks_per_sm) else "autotuner"},
                     gpu_launches=gpu_launches, stat_ok=int((stat0 == 0).sum())))
 
     if not args.quick and rank == 0:
@@ -847,6 +858,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (FP64 phase)", "data": "synthetic",
         "config": {"workload": WORKLOAD, "global_batch": N_REQ * world, "precision": "mixed",
                    "l2": "flushed before every step (256 MiB write)", "tile": res["tile"],
+                   "launch_shape": res["launch_shape"],
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": res["e2e_value"], "unit": "evals/s", "h2d_bytes_per_step": res["h2d"],
                 "d2h_bytes_per_step": res["d2h"]},

@@ -133,6 +133,8 @@ def _declare(L):
         "gwgpu_server_reset_stats": (c_int, [c_void_p]),
         "gwgpu_server_drive": (c_int, [c_void_p, c_void_p, ip, ip, c_int, dp, c_int, dp, ip, dp, dp]),
         "gwgpu_batch_set_tile": (c_int, [c_void_p, c_int]),
+        "gwgpu_batch_set_blocks_per_sm": (c_int, [c_void_p, c_int]),
+        "gwgpu_batch_last_launch_shape": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
         "gwgpu_batch_use_graphs": (c_int, [c_void_p, c_int]),
         "gwgpu_batch_timing": (c_int, [c_void_p, c_int]),
         "gwgpu_batch_last_timing": (c_int, [c_void_p, P(ctypes.c_float), P(ctypes.c_float)]),

@@ -52,6 +52,7 @@ int choose_tile(gwgpu_context *c, int mixed, const std::string &key) {
 static int choose_occ(gwgpu_context *c, int mixed, const std::string &key) {
   if (!mixed) return gwk::batch_default_occ(0);
   if (c->occ_override > 0) return c->occ_override;
+  if (c->occ_user > 0) return c->occ_user;
   auto it = c->tuned_occ.find(key);
   if (it != c->tuned_occ.end()) return it->second;
   return gwk::batch_default_occ(1);
@@ -209,6 +210,11 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   int grid = std::min(pl.nitems, persistent_grid(c->device, mixed, ndet, occ));
   if (grid < 1) grid = 1;
   e = gwk::launch_batch(a, mixed, grid, occ, L.stream, c->pdl);
+  if (&L == &c->lane) {
+    c->last_shape[0] = pl.tile;
+    c->last_shape[1] = occ;
+    c->last_shape[2] = grid;
+  }
   if (e != cudaSuccess) return c->fail(e, "batch launch");
   if (timing) cudaEventRecord(c->t_ev[2], L.stream);
   return GWGPU_OK;
@@ -422,6 +428,22 @@ int gwgpu_batch_set_tile(gwgpu_context *c, int tile) {
   return GWGPU_OK;
 }
 
+int gwgpu_batch_set_blocks_per_sm(gwgpu_context *c, int blocks) {
+  if (!c || (blocks != 0 && blocks != 3 && blocks != 4)) return GWGPU_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->occ_user = blocks;
+  return GWGPU_OK;
+}
+
+int gwgpu_batch_last_launch_shape(gwgpu_context *c, int *tile, int *blocks_per_sm, int *grid) {
+  if (!c) return GWGPU_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (tile) *tile = c->last_shape[0];
+  if (blocks_per_sm) *blocks_per_sm = c->last_shape[1];
+  if (grid) *grid = c->last_shape[2];
+  return GWGPU_OK;
+}
+
 int gwgpu_batch_timing(gwgpu_context *c, int on) {
   if (!c) return GWGPU_EINVAL;
   std::lock_guard<std::mutex> lk(c->mu);
@@ -485,19 +507,24 @@ int gwgpu_batch_autotune(gwgpu_context *c, const gwgpu_gen_params *d_params, con
       c->occ_override = 0;
       return st;
     }
-    cudaEventRecord(e0, L.stream);
-    for (int r = 0; r < 3; r++)
-      gwb::enqueue_batch(c, L, d_params, d_approx, n, h_handles, ndet, T_segment, precision, d_out, d_status, tile,
-                         false);
-    cudaEventRecord(e1, L.stream);
-    cudaError_t e = cudaEventSynchronize(e1);
-    if (e != cudaSuccess) {
-      c->occ_override = 0;
-      return c->fail(e, "autotune");
+    // the fastest of three timings of two launches each (a shared GPU's
+    // clocks and neighbours make single timings noisy)
+    float ms = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(e0, L.stream);
+      for (int r = 0; r < 2; r++)
+        gwb::enqueue_batch(c, L, d_params, d_approx, n, h_handles, ndet, T_segment, precision, d_out, d_status, tile,
+                           false);
+      cudaEventRecord(e1, L.stream);
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess) {
+        c->occ_override = 0;
+        return c->fail(e, "autotune");
+      }
+      float t = 0;
+      cudaEventElapsedTime(&t, e0, e1);
+      ms = std::min(ms, t / 2);
     }
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    ms /= 3;
     if (ms < bms) {
       bms = ms;
       best = tile;

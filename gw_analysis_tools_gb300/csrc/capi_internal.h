@@ -51,6 +51,8 @@ struct gwgpu_context {
   std::map<std::string, int> tuned_occ;  // and the fused kernel's resident blocks per SM
   int tile_override = 0;
   int occ_override = 0;                  // set while the autotuner times a launch shape
+  int occ_user = 0;                      // gwgpu_batch_set_blocks_per_sm (0: autotuned or default)
+  int last_shape[3] = {0, 0, 0};         // tile, blocks per SM, grid of the last context-stream batch
   bool use_graphs = true;
   int chirp_n = 0;                 // grid length whose Bluestein kernel the kWsChirp workspace holds
   double chirp_kscale = 0;         // M max|B| of that kernel (the FP32 search's error scale)

@@ -392,9 +392,19 @@ class Context:
         return out, status
 
     def set_tile(self, tile):
-        fn = getattr(self.lib, "gwgpu_batch_set_tile", None)
-        if fn is not None:
-            self._check(fn(self.h, int(tile)), "batch_set_tile")
+        self._check(self.lib.gwgpu_batch_set_tile(self.h, int(tile)), "batch_set_tile")
+
+    def set_blocks_per_sm(self, blocks):
+        """Launch shape of the mixed fused kernel: 3 or 4 resident blocks per
+        SM, 0 for the autotuned or default choice."""
+        self._check(self.lib.gwgpu_batch_set_blocks_per_sm(self.h, int(blocks)), "batch_set_blocks_per_sm")
+
+    def last_launch_shape(self):
+        """(tile, blocks per SM, grid) of the last batch on the context stream."""
+        t, b, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.gwgpu_batch_last_launch_shape(self.h, ctypes.byref(t), ctypes.byref(b), ctypes.byref(g)),
+                    "batch_last_launch_shape")
+        return t.value, b.value, g.value
 
     # --------------------------------------------------------------- Fisher
     def fisher_numerical(self, freqs, method, detector, reference_detector, params, noise, order=2, dimension=11):

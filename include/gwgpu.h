@@ -269,6 +269,12 @@ int gwgpu_mcmc_loglik_batch(gwgpu_context *ctx, const double *theta, int dim, in
  * batched kernels, and whether repeated batch shapes replay a captured CUDA
  * graph (default on). */
 int gwgpu_batch_set_tile(gwgpu_context *ctx, int tile);
+/* Resident blocks per SM of the mixed form's fused kernel (3 or 4; 0 =
+ * autotuned or default), the launch shape's second coordinate. */
+int gwgpu_batch_set_blocks_per_sm(gwgpu_context *ctx, int blocks);
+/* Launch shape of the last batch on the context stream: bin tile, resident
+ * blocks per SM and grid of the fused kernel. */
+int gwgpu_batch_last_launch_shape(gwgpu_context *ctx, int *tile, int *blocks_per_sm, int *grid);
 int gwgpu_batch_use_graphs(gwgpu_context *ctx, int on);
 /* Per-kernel timing of context-stream batches (graphs bypassed while on):
  * CUDA events around the prologue and the fused bin kernel of the last batch. */
