@@ -563,10 +563,8 @@ class Server:
 def _ctx_batch_device(self, d_params_ptr, d_approx_ptr, n, handles, T_segment, precision, d_out_ptr, d_status_ptr,
                       stream=None):
     """gwgpu_loglik_batch_device on raw device pointers (e.g. torch tensors' data_ptr())."""
-    hs = np.ascontiguousarray(handles, dtype=np.int32)
-    ndet = hs.shape[-1] if hs.ndim == 2 else hs.size
-    if hs.ndim == 1:
-        hs = np.ascontiguousarray(np.broadcast_to(hs, (n, ndet)))
+    _, hs = self._call_arrays(0, handles, n)
+    ndet = hs.shape[1]
     st = self.lib.gwgpu_loglik_batch_device(self.h, d_params_ptr, d_approx_ptr, n, _ip(hs), ndet, float(T_segment),
                                             precision, d_out_ptr, d_status_ptr, stream)
     self._check(st, "loglik_batch_device")
