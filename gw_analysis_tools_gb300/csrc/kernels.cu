@@ -895,6 +895,12 @@ __device__ __forceinline__ int order_kcut(const MixedReq *__restrict__ mreq, con
   if (mreq[r].status != 0) return 0;
   return min(req_N[r], mreq[r].n_cut - req_n0[r] + 1);
 }
+__device__ __forceinline__ int order_tile_bucket(int kcut, int t, int tile, int np) {
+  const int live = max(0, min(kcut - t * tile, tile));
+  return order_bucket(min(np, (live + kSegBins - 1) / kSegBins), np);
+}
+// Lanes that draw the same bucket add to it once (most tiles of a step fall in
+// the first bucket: one shared atomic per lane would serialise on it).
 __global__ void __launch_bounds__(kOrderBlock) k_order_items(const MixedReq *__restrict__ mreq, int n,
                                                              const int *__restrict__ item_start,
                                                              const int *__restrict__ item_count, int tile,
@@ -904,33 +910,38 @@ __global__ void __launch_bounds__(kOrderBlock) k_order_items(const MixedReq *__r
   __shared__ int hist[kOrderBuckets], off[kOrderBuckets];
   grid_dep_trigger();
   grid_dep_wait();  // the prologue's request records
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31;
   const int np = (tile + kSegBins - 1) / kSegBins;
   for (int b = tid; b < kOrderBuckets; b += blockDim.x) hist[b] = 0;
   __syncthreads();
-  for (int r = tid; r < n; r += blockDim.x) {
-    const int kcut = order_kcut(mreq, req_n0, req_N, r), nt = item_count[r];
-    for (int t = 0; t < nt; t++) {
-      const int live = max(0, min(kcut - t * tile, tile));
-      atomicAdd(&hist[order_bucket(min(np, (live + kSegBins - 1) / kSegBins), np)], 1);
+  // warp-uniform loops: lane l of a warp takes request rb + l
+  for (int rb = tid - lane; rb < n; rb += blockDim.x) {
+    const int r = rb + lane;
+    const bool on = r < n;
+    const int kcut = on ? order_kcut(mreq, req_n0, req_N, r) : 0, nt = on ? item_count[r] : 0;
+    const int ntmax = __reduce_max_sync(0xffffffffu, nt);
+    for (int t = 0; t < ntmax; t++) {
+      const int b = t < nt ? order_tile_bucket(kcut, t, tile, np) : -1;
+      const unsigned grp = __match_any_sync(0xffffffffu, b);
+      if (b >= 0 && lane == __ffs(grp) - 1) atomicAdd(&hist[b], __popc(grp));
     }
   }
   __syncthreads();
   if (tid < 32) {  // exclusive prefix of the buckets: kPerLane consecutive buckets per lane, then a warp scan
-    int v[kPerLane], s = 0;
+    int v[kPerLane], sum = 0;
 #pragma unroll
     for (int q = 0; q < kPerLane; q++) {
       const int b = tid * kPerLane + q;
       v[q] = b < kOrderBuckets ? hist[b] : 0;
-      s += v[q];
+      sum += v[q];
     }
-    int incl = s;
+    int incl = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int y = __shfl_up_sync(0xffffffffu, incl, o);
       if (tid >= o) incl += y;
     }
-    int run = incl - s;
+    int run = incl - sum;
 #pragma unroll
     for (int q = 0; q < kPerLane; q++) {
       const int b = tid * kPerLane + q;
@@ -939,11 +950,20 @@ __global__ void __launch_bounds__(kOrderBlock) k_order_items(const MixedReq *__r
     }
   }
   __syncthreads();
-  for (int r = tid; r < n; r += blockDim.x) {
-    const int kcut = order_kcut(mreq, req_n0, req_N, r), nt = item_count[r], i0 = item_start[r];
-    for (int t = 0; t < nt; t++) {
-      const int live = max(0, min(kcut - t * tile, tile));
-      order[atomicAdd(&off[order_bucket(min(np, (live + kSegBins - 1) / kSegBins), np)], 1)] = i0 + t;
+  for (int rb = tid - lane; rb < n; rb += blockDim.x) {
+    const int r = rb + lane;
+    const bool on = r < n;
+    const int kcut = on ? order_kcut(mreq, req_n0, req_N, r) : 0, nt = on ? item_count[r] : 0;
+    const int i0 = on ? item_start[r] : 0;
+    const int ntmax = __reduce_max_sync(0xffffffffu, nt);
+    for (int t = 0; t < ntmax; t++) {
+      const int b = t < nt ? order_tile_bucket(kcut, t, tile, np) : -1;
+      const unsigned grp = __match_any_sync(0xffffffffu, b);
+      const int leader = __ffs(grp) - 1;
+      int base = 0;
+      if (b >= 0 && lane == leader) base = atomicAdd(&off[b], __popc(grp));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (b >= 0) order[base + __popc(grp & ((1u << lane) - 1u))] = i0 + t;
     }
   }
 }
