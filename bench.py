@@ -228,9 +228,9 @@ def run_ours(args, rank, world, local, pg):
         torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in zip(e0, e1)]
     tot_ms, units, value = replica_aggregate(float(np.sum(step_ms)), N_REQ * args.steps, pg, "cuda")
-    # prologue, item order (unless GWGPU_ITEM_ORDER=listed) and fused bin kernel
-    # per step (the memset node is not ours)
-    gpu_launches = (2 if os.environ.get("GWGPU_ITEM_ORDER", "") == "listed" else 3) * args.steps
+    # prologue (which also writes the work order) and fused bin kernel per step
+    # (the memset node is not ours)
+    gpu_launches = 2 * args.steps
 
     # status and a parity sample for |dlogL| against the oracle (cpu_baseline leg below)
     out_mixed = d_out[0].cpu().numpy().copy()

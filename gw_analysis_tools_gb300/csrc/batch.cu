@@ -139,8 +139,8 @@ int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, i
     pos += count[r];
   }
   pl.nitems = (int)sorted.size();
-  size_t need = sizeof(gwk::Item) * sorted.size() + 256 + sizeof(int) * (size_t)n * (4 + ndet) + 256 +
-                sizeof(int) * sorted.size() + 256;
+  size_t need = sizeof(gwk::Item) * sorted.size() + 256 + sizeof(int) * (size_t)n * (2 + ndet) + 256 +
+                sizeof(int) * sorted.size() * gwk::kOrderBuckets + 256;
   int st = lane_alloc(c, L, &pl.mem, &pl.cap, need, "batch plan");
   if (st) return st;
   char *p = (char *)pl.mem;
@@ -149,17 +149,7 @@ int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, i
   pl.item_start = (int *)p;
   pl.item_count = pl.item_start + n;
   pl.handles = pl.item_count + n;
-  pl.req_n0 = pl.handles + (size_t)n * ndet;
-  pl.req_N = pl.req_n0 + n;
-  pl.order = (int *)align256((char *)(pl.req_N + n));
-  std::vector<int> rn0(n), rN(n);
-  for (int r = 0; r < n; r++) {
-    const gwgpu_context::Stream *s0 = c->get_stream(handles[r * ndet]);
-    rn0[r] = s0->dev.n0;
-    rN[r] = s0->dev.N;
-  }
-  cudaMemcpyAsync(pl.req_n0, rn0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
-  cudaMemcpyAsync(pl.req_N, rN.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
+  pl.order = (int *)align256((char *)(pl.handles + (size_t)n * ndet));
   cudaMemcpyAsync(pl.items, sorted.data(), sizeof(gwk::Item) * sorted.size(), cudaMemcpyHostToDevice, L.stream);
   cudaMemcpyAsync(pl.item_start, nstart.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
   cudaMemcpyAsync(pl.item_count, count.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.stream);
@@ -176,12 +166,29 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   const Plan &pl = L.plan;
   const bool timing = c->timing && &L == &c->lane;
   if (timing) cudaEventRecord(c->t_ev[0], L.stream);
-  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(unsigned) * (size_t)(n + 32), L.stream);
+  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(unsigned) * (size_t)(n + 32 + gwk::kOrderBuckets), L.stream);
   if (e != cudaSuccess) return c->fail(e, "batch counters");
-  e = (c->prologue_serial ? gwk::launch_prologue_serial : gwk::launch_prologue)(
-      (const gwt::GenParams *)d_params, d_approx, n, pl.handles, ndet, T_segment, 1, c->streams_dev, c->qnm_dev,
-      mixed ? nullptr : (gwt::Request *)reqs, mixed ? (gwt::MixedReq *)reqs : nullptr, mixed, d_status, L.stream);
+  // mixed form: the prologue writes the work order (most live bins first)
+  const bool ordered = mixed && c->order_items && !c->prologue_serial;
+  gwk::OrderArgs ord;
+  if (ordered) {
+    ord.fill = (int *)(cnt + n + 32);
+    ord.items = pl.order;
+    ord.item_start = pl.item_start;
+    ord.item_count = pl.item_count;
+    ord.nitems = pl.nitems;
+    ord.tile = pl.tile;
+  }
+  if (c->prologue_serial)
+    e = gwk::launch_prologue_serial((const gwt::GenParams *)d_params, d_approx, n, pl.handles, ndet, T_segment, 1,
+                                    c->streams_dev, c->qnm_dev, mixed ? nullptr : (gwt::Request *)reqs,
+                                    mixed ? (gwt::MixedReq *)reqs : nullptr, mixed, d_status, L.stream);
+  else
+    e = gwk::launch_prologue((const gwt::GenParams *)d_params, d_approx, n, pl.handles, ndet, T_segment, 1,
+                             c->streams_dev, c->qnm_dev, mixed ? nullptr : (gwt::Request *)reqs,
+                             mixed ? (gwt::MixedReq *)reqs : nullptr, mixed, d_status, L.stream, ord);
   if (e != cudaSuccess) return c->fail(e, "prologue launch");
+  if (timing) cudaEventRecord(c->t_ev[1], L.stream);
   gwk::BatchArgs a;
   a.req = mixed ? nullptr : (const gwt::Request *)reqs;
   a.mreq = mixed ? (const gwt::MixedReq *)reqs : nullptr;
@@ -189,7 +196,8 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   a.ndet = ndet;
   a.streams = c->streams_dev;
   a.items = pl.items;
-  a.order = nullptr;
+  a.bucket_fill = ordered ? ord.fill : nullptr;
+  a.bucket_items = ordered ? ord.items : nullptr;
   a.nitems = pl.nitems;
   a.item_start = pl.item_start;
   a.item_count = pl.item_count;
@@ -200,13 +208,6 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   a.out = d_out;
   a.status = d_status;
   a.tables = c->tables;
-  if (mixed && c->order_items) {
-    e = gwk::launch_order_items((const gwt::MixedReq *)reqs, n, pl.item_start, pl.item_count, pl.tile, pl.req_n0,
-                                pl.req_N, pl.order, L.stream, c->pdl);
-    if (e != cudaSuccess) return c->fail(e, "item order launch");
-    a.order = pl.order;
-  }
-  if (timing) cudaEventRecord(c->t_ev[1], L.stream);  // prologue and item order | bin kernel
   int grid = std::min(pl.nitems, persistent_grid(c->device, mixed, ndet, occ));
   if (grid < 1) grid = 1;
   e = gwk::launch_batch(a, mixed, grid, occ, L.stream, c->pdl);
@@ -248,7 +249,7 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
   }
   size_t rq = mixed ? sizeof(gwt::MixedReq) : sizeof(gwt::Request);
   size_t bytes = rq * n + 256 + sizeof(double) * (size_t)L.plan.nitems * gwk::kAcc + 256 +
-                 sizeof(unsigned) * (size_t)(n + 32);
+                 sizeof(unsigned) * (size_t)(n + 32 + gwk::kOrderBuckets);
   void *old = L.work;
   int st = lane_alloc(c, L, &L.work, &L.work_cap, bytes, "batch scratch");
   if (st) return st;

@@ -21,8 +21,7 @@ struct Plan {
   size_t cap = 0;
   gwk::Item *items = nullptr;
   int *item_start = nullptr, *item_count = nullptr, *handles = nullptr;
-  int *req_n0 = nullptr, *req_N = nullptr;  // per request: first bin index and length of its grid
-  int *order = nullptr;  // nitems: the execution order the mixed batch writes before each launch
+  int *order = nullptr;  // kOrderBuckets x nitems: the work order the prologue writes for each launch
 };
 
 // Scratch of one in-flight batch.  Owned by the context (lane 0, the context

@@ -328,11 +328,42 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void grid_dep_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// Longest-processing-time-first order for the persistent mixed kernel: an
+// item's work is its live 256-bin passes (bins below the request's cut
+// f <= 0.2/M, where the model is non-zero; beyond it a pass costs nothing), and
+// the requests of one batch differ several-fold in it.  Items are bucketed by
+// their number of live passes, most first, so that the grid drains on cheap
+// items.  The order inside a bucket depends on atomics; results do not
+// (partials are indexed by item, and each request's finalize sums them in
+// item order).
+__device__ __forceinline__ int order_bucket(int kcut, int t, int tile) {
+  const int np = (tile + kSegBins - 1) / kSegBins;
+  const int live = max(0, min(kcut - t * tile, tile));
+  const int lp = min(np, (live + kSegBins - 1) / kSegBins);
+  return (int)((long long)(np - lp) * (kOrderBuckets - 1) / np);  // 0: all passes live
+}
+// Warp-wide: lane l appends the items of its request (kcut: end of its live
+// bins, nt items from i0) to their buckets.  Lanes that draw the same bucket
+// add to it once.  Every lane of the warp calls this (nt = 0 for none).
+__device__ __forceinline__ void order_append(const OrderArgs &o, int kcut, int nt, int i0) {
+  const int lane = threadIdx.x & 31;
+  const int ntmax = __reduce_max_sync(0xffffffffu, nt);
+  for (int t = 0; t < ntmax; t++) {
+    const int b = t < nt ? order_bucket(kcut, t, o.tile) : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, b);
+    const int leader = __ffs(grp) - 1;
+    int base = 0;
+    if (b >= 0 && lane == leader) base = atomicAdd(o.fill + b, __popc(grp));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (b >= 0) o.items[(size_t)b * o.nitems + base + __popc(grp & ((1u << lane) - 1u))] = i0 + t;
+  }
+}
+
 constexpr int kCoopWarps = 4, kCoopReq = 16;
 __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     const GenParams *__restrict__ params, const int *__restrict__ approx, int n, const int *__restrict__ handles,
     int ndet, double T_segment, int tc_from_segment, const StreamDev *__restrict__ streams,
-    const double *__restrict__ qnm, Request *req, MixedReq *mreq, int want_mixed, int *status) {
+    const double *__restrict__ qnm, Request *req, MixedReq *mreq, int want_mixed, int *status, const OrderArgs ord) {
   __shared__ Request s_r[kCoopReq];
   __shared__ GenParams s_p[kCoopReq];
   __shared__ AmpConn s_ac[kCoopReq];
@@ -344,7 +375,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   __shared__ int s_st[kCoopReq], s_bad[kCoopReq], s_uni[kCoopReq];
   __shared__ double s_pm[kCoopReq][2];  // D: final spin and radiated energy, for post_merger in S1
   static_assert(2 * kCoopReq == 32, "two half-warps per warp share the block's requests");
-  grid_dep_trigger();  // the item order / bin kernel may launch and wait for this grid
+  grid_dep_trigger();  // the bin kernel may launch and wait for this grid
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kCoopReq + lane;
   const bool act = lane < kCoopReq && i < n;
@@ -516,14 +547,28 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     if (st && req) req[i].m.status = st;
     status[i] = st;
   }
+  if (warp == 0 && ord.fill && want_mixed) {  // this block's requests into the work order
+    int kcut = 0, nt = 0, i0 = 0;
+    if (act) {
+      const MixedReq &x = mreq[i];
+      if (x.status == 0) {
+        const StreamDev &s0 = streams[handles[i * ndet]];
+        kcut = min(s0.N, x.n_cut - s0.n0 + 1);
+      }
+      nt = ord.item_count[i];
+      i0 = ord.item_start[i];
+    }
+    order_append(ord, kcut, nt, i0);
+  }
 }
 
 cudaError_t launch_prologue(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
                             double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
-                            Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s) {
+                            Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s,
+                            const OrderArgs &ord) {
   int grid = (n + kCoopReq - 1) / kCoopReq;
   k_prologue_coop<<<grid, kCoopWarps * 32, 0, s>>>(params, approx, n, handles, ndet, T_segment, tc_from_segment,
-                                                   streams, qnm, req, mreq, want_mixed, status);
+                                                   streams, qnm, req, mreq, want_mixed, status, ord);
   return cudaGetLastError();
 }
 cudaError_t launch_prologue_serial(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
@@ -621,14 +666,53 @@ __global__ void __launch_bounds__(kBatchBlock, OCC) k_batch(const BatchArgs a) {
   // detector rotations: per segment pass (first bin) and per thread offset
   __shared__ float2 s_rot_seg[kSegBuf * (MIXED ? NDET : 1)];
   __shared__ float2 s_rot_off[(MIXED ? NDET : 1) * (MIXED ? kBatchBlock : 1)];
+  __shared__ int s_iid, s_bstart[kOrderBuckets];
   const int tid = threadIdx.x;
-  grid_dep_wait();  // the prologue's (and item order's) output
+  grid_dep_wait();  // the prologue's output
+  if (a.bucket_fill && tid < 32) {  // first position of each bucket in the work order
+    constexpr int kPerLane = (kOrderBuckets + 31) / 32;
+    int v[kPerLane], sum = 0;
+#pragma unroll
+    for (int q = 0; q < kPerLane; q++) {
+      const int b = tid * kPerLane + q;
+      v[q] = b < kOrderBuckets ? __ldcg(a.bucket_fill + b) : 0;
+      sum += v[q];
+    }
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (tid >= o) incl += y;
+    }
+    int run = incl - sum;
+#pragma unroll
+    for (int q = 0; q < kPerLane; q++) {
+      const int b = tid * kPerLane + q;
+      if (b < kOrderBuckets) s_bstart[b] = run;
+      run += v[q];
+    }
+  }
+  __syncthreads();
   for (;;) {
-    if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
+    if (tid == 0) {
+      const int it = (int)atomicAdd(a.item_counter, 1u);
+      int iid = it;
+      if (a.bucket_fill && it < a.nitems) {  // the bucket holding position it: the last start <= it
+        int lo = 0, hi = kOrderBuckets - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (s_bstart[mid] <= it) lo = mid;
+          else hi = mid - 1;
+        }
+        iid = __ldcg(a.bucket_items + (size_t)lo * a.nitems + (it - s_bstart[lo]));
+      }
+      s_item = it;
+      s_iid = iid;
+    }
     __syncthreads();
     const int it = s_item;
     if (it >= a.nitems) break;
-    const int iid = a.order ? __ldg(a.order + it) : it;  // the item's own index: its partials' slot
+    const int iid = s_iid;  // the item's own index: its partials' slot
     const Item I = a.items[iid];
     // stage the request constants and its streams
     {
@@ -875,99 +959,6 @@ int batch_occupancy(int mixed, int ndet, int occ) {
   return nb;
 }
 
-// Longest-processing-time-first order for the persistent mixed kernel: an
-// item's work is its live 256-bin passes (bins below the request's cut
-// f <= 0.2/M, where the model is non-zero; beyond it a pass costs nothing), and
-// requests of one batch differ several-fold in it.  A counting sort over the
-// number of live passes, most first, so that the grid drains on cheap items.
-// The order inside a bucket depends on atomics; results do not (partials are
-// indexed by item, and each request's finalize sums them in item order).
-constexpr int kOrderBlock = 1024, kOrderBuckets = 65;
-// Bucket of a tile with lp of its np passes live: 0 when all are live.
-__device__ __forceinline__ int order_bucket(int lp, int np) {
-  return (int)((long long)(np - lp) * (kOrderBuckets - 1) / np);
-}
-// Request r's items are item_start[r] + t (t = 0 .. item_count[r]) with first
-// bin t * tile; its live bins end at kcut (below the cut and the grid of N
-// bins starting at n0).
-__device__ __forceinline__ int order_kcut(const MixedReq *__restrict__ mreq, const int *__restrict__ req_n0,
-                                          const int *__restrict__ req_N, int r) {
-  if (mreq[r].status != 0) return 0;
-  return min(req_N[r], mreq[r].n_cut - req_n0[r] + 1);
-}
-__device__ __forceinline__ int order_tile_bucket(int kcut, int t, int tile, int np) {
-  const int live = max(0, min(kcut - t * tile, tile));
-  return order_bucket(min(np, (live + kSegBins - 1) / kSegBins), np);
-}
-// Lanes that draw the same bucket add to it once (most tiles of a step fall in
-// the first bucket: one shared atomic per lane would serialise on it).
-__global__ void __launch_bounds__(kOrderBlock) k_order_items(const MixedReq *__restrict__ mreq, int n,
-                                                             const int *__restrict__ item_start,
-                                                             const int *__restrict__ item_count, int tile,
-                                                             const int *__restrict__ req_n0,
-                                                             const int *__restrict__ req_N, int *order) {
-  constexpr int kPerLane = (kOrderBuckets + 31) / 32;
-  __shared__ int hist[kOrderBuckets], off[kOrderBuckets];
-  grid_dep_trigger();
-  grid_dep_wait();  // the prologue's request records
-  const int tid = threadIdx.x, lane = tid & 31;
-  const int np = (tile + kSegBins - 1) / kSegBins;
-  for (int b = tid; b < kOrderBuckets; b += blockDim.x) hist[b] = 0;
-  __syncthreads();
-  // warp-uniform loops: lane l of a warp takes request rb + l
-  for (int rb = tid - lane; rb < n; rb += blockDim.x) {
-    const int r = rb + lane;
-    const bool on = r < n;
-    const int kcut = on ? order_kcut(mreq, req_n0, req_N, r) : 0, nt = on ? item_count[r] : 0;
-    const int ntmax = __reduce_max_sync(0xffffffffu, nt);
-    for (int t = 0; t < ntmax; t++) {
-      const int b = t < nt ? order_tile_bucket(kcut, t, tile, np) : -1;
-      const unsigned grp = __match_any_sync(0xffffffffu, b);
-      if (b >= 0 && lane == __ffs(grp) - 1) atomicAdd(&hist[b], __popc(grp));
-    }
-  }
-  __syncthreads();
-  if (tid < 32) {  // exclusive prefix of the buckets: kPerLane consecutive buckets per lane, then a warp scan
-    int v[kPerLane], sum = 0;
-#pragma unroll
-    for (int q = 0; q < kPerLane; q++) {
-      const int b = tid * kPerLane + q;
-      v[q] = b < kOrderBuckets ? hist[b] : 0;
-      sum += v[q];
-    }
-    int incl = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (tid >= o) incl += y;
-    }
-    int run = incl - sum;
-#pragma unroll
-    for (int q = 0; q < kPerLane; q++) {
-      const int b = tid * kPerLane + q;
-      if (b < kOrderBuckets) off[b] = run;
-      run += v[q];
-    }
-  }
-  __syncthreads();
-  for (int rb = tid - lane; rb < n; rb += blockDim.x) {
-    const int r = rb + lane;
-    const bool on = r < n;
-    const int kcut = on ? order_kcut(mreq, req_n0, req_N, r) : 0, nt = on ? item_count[r] : 0;
-    const int i0 = on ? item_start[r] : 0;
-    const int ntmax = __reduce_max_sync(0xffffffffu, nt);
-    for (int t = 0; t < ntmax; t++) {
-      const int b = t < nt ? order_tile_bucket(kcut, t, tile, np) : -1;
-      const unsigned grp = __match_any_sync(0xffffffffu, b);
-      const int leader = __ffs(grp) - 1;
-      int base = 0;
-      if (b >= 0 && lane == leader) base = atomicAdd(&off[b], __popc(grp));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (b >= 0) order[base + __popc(grp & ((1u << lane) - 1u))] = i0 + t;
-    }
-  }
-}
-
 static cudaError_t launch_dependent(const void *f, dim3 grid, dim3 block, void **args, cudaStream_t s, bool pdl) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
@@ -980,13 +971,6 @@ static cudaError_t launch_dependent(const void *f, dim3 grid, dim3 block, void *
   cfg.attrs = at;
   cfg.numAttrs = pdl ? 1 : 0;
   return cudaLaunchKernelExC(&cfg, f, args);
-}
-
-cudaError_t launch_order_items(const MixedReq *mreq, int n, const int *item_start, const int *item_count, int tile,
-                               const int *req_n0, const int *req_N, int *order, cudaStream_t s, bool pdl) {
-  void *args[] = {(void *)&mreq, (void *)&n, (void *)&item_start, (void *)&item_count, (void *)&tile,
-                  (void *)&req_n0, (void *)&req_N, (void *)&order};
-  return launch_dependent((const void *)k_order_items, dim3(1), dim3(kOrderBlock), args, s, pdl);
 }
 
 cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s, bool pdl) {

@@ -60,10 +60,21 @@ cudaError_t launch_plain(const Request &r, const StreamDev *streams, int ndet, d
 int plain_blocks(int N);
 cudaError_t plain_preload();  // loads the plain kernels' module (function-attribute query)
 
+// Work order of a mixed batch: the prologue appends each request's items to
+// the bucket of their live 256-bin passes (bucket 0: all live) as soon as it
+// knows the request's cut; the bin kernel takes items bucket by bucket.
+constexpr int kOrderBuckets = 65;
+struct OrderArgs {
+  int *fill = nullptr;          // kOrderBuckets counters (zeroed before the prologue); nullptr: no ordering
+  int *items = nullptr;         // bucket b's items at items[b * nitems ...]
+  const int *item_start = nullptr, *item_count = nullptr;  // per request: first item, number of items
+  int nitems = 0, tile = 0;
+};
 // Batched: prologue (one thread per request) then the fused bin kernel.
 cudaError_t launch_prologue(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
                             double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
-                            Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s);
+                            Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s,
+                            const OrderArgs &ord = OrderArgs());
 // One thread per request (the reference order of the prologue); kept to check
 // the cooperative kernel against.
 cudaError_t launch_prologue_serial(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
@@ -78,7 +89,8 @@ struct BatchArgs {
   int ndet;
   const StreamDev *streams;
   const Item *items;
-  const int *order;  // execution order of the items (nullptr: as listed); partials stay indexed by item
+  const int *bucket_fill;   // work order written by the prologue (nullptr: items as listed);
+  const int *bucket_items;  // partials stay indexed by item
   int nitems;
   const int *item_start;  // per request
   const int *item_count;
@@ -94,10 +106,7 @@ struct BatchArgs {
 // pdl: launched as a programmatic dependent of the kernel before it on s
 // (it starts launching while that one runs and waits for its completion).
 cudaError_t launch_batch(const BatchArgs &a, int mixed, int grid, int occ, cudaStream_t s, bool pdl);
-// The mixed batch's items ordered by their live bins (below each request's
-// waveform cut), most first, into order[nitems]; one block.
-cudaError_t launch_order_items(const MixedReq *mreq, int n, const int *item_start, const int *item_count, int tile,
-                               const int *req_n0, const int *req_N, int *order, cudaStream_t s, bool pdl);
+
 int batch_default_occ(int mixed);
 int batch_block_size(int mixed);
 int batch_occupancy(int mixed, int ndet, int occ);  // resident blocks per SM
