@@ -866,7 +866,8 @@ def main():
         "clocks": res["clocks"],
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak if fp32_peak else None, "traffic": TRAFFIC_PER_LAUNCH,
-                     "kernel": "k_batch<3,1> (fused mixed bin kernel)", "kernel_ms": res["kernel_ms"],
+                     "kernel": "k_batch<3,1,%d> (fused mixed bin kernel)" % res["launch_shape"]["blocks_per_sm"],
+                     "kernel_ms": res["kernel_ms"],
                      "prologue_ms": res["prologue_ms"], "algorithmic_flops_per_launch": algo_flops,
                      "algorithm": "reference flops per waveform-bin %.2f and per detector-bin %.1f "
                                   "(oracle/op_counts.json)" % (REF_FLOPS_PER_WAVE_BIN, REF_FLOPS_PER_DET_BIN),
@@ -914,8 +915,8 @@ def main():
 PROFILE_SOURCE = "profiles/k_batch_mixed_ptstep512.md"
 REF_FLOPS_PER_WAVE_BIN = 66.56
 REF_FLOPS_PER_DET_BIN = 33.0
-TRAFFIC_PER_LAUNCH = 2.72e6
-FP64_FLOP_PER_LAUNCH = 3.15e7
+TRAFFIC_PER_LAUNCH = 2.48e6
+FP64_FLOP_PER_LAUNCH = 1.98e7
 
 
 def measure_peak(dtype):
