@@ -260,3 +260,57 @@ def test_device_batches_rotating_buffers_and_launch_shapes(gpu_ctx, oracle, netw
                                 outs[0].data_ptr(), stats[0].data_ptr())
     assert tile in (1024, 2048, 4096, 8192, 16384) and ms > 0
     run_all()
+
+
+def test_work_order_and_launch_shape_leave_results_unchanged(gpu_ctx, oracle, monkeypatch):
+    """The mixed batch's items run in work order (most live bins first,
+    written by the prologue) or in plan order (GWGPU_ITEM_ORDER=listed), with 3
+    or 4 blocks per SM: each item writes its own partials and each request's
+    finalize sums them in item order, so the results are the same to the last
+    bit.  An uneven D/Pv2 batch with two requests outside the model domain."""
+    durations = [4, 8, 16]
+    grids, datas, psds = {}, {}, {}
+    for T in durations:
+        f = W.uniform_grid(20.0, 1024.0, 1.0 / T)
+        grids[T] = f
+        datas[T] = [W.noise(f, 700 + T + i) for i in range(3)]
+        psds[T] = [W.analytic_psd(f)] * 3
+    draws = W.prior_draws(24, 71) + W.prior_draws(24, 72, precessing=True)
+    draws[5] = dict(draws[5], mass1=-1.0)
+    draws[30] = dict(draws[30], mass2=0.0)
+    aps = np.array([0] * 24 + [1] * 24, dtype=np.int32)
+    Ts = [durations[i % 3] for i in range(len(draws))]
+    monkeypatch.setenv("GWGPU_ITEM_ORDER", "listed")
+    listed = G.Context(0)
+    monkeypatch.delenv("GWGPU_ITEM_ORDER")
+    results = []
+    for ctx in (gpu_ctx, listed):
+        hs = {T: [ctx.register_data(d, grids[T], datas[T][i], psds[T][i]) for i, d in enumerate(W.DETECTORS3)]
+              for T in durations}
+        handles = np.array([hs[T] for T in Ts], dtype=np.int32)
+        ctx.set_tile(2048)
+        for blocks in (3, 4):
+            ctx.set_blocks_per_sm(blocks)
+            out, st = ctx.loglik_batch(G.params_array(draws), aps, handles, 0.0, G.PREC_MIXED)
+            assert ctx.last_launch_shape()[:2] == (2048, blocks)
+            results.append((out.copy(), st.copy()))
+        ctx.set_tile(0)
+        ctx.set_blocks_per_sm(0)
+        for T in durations:
+            for h in hs[T]:
+                ctx.release_data(h)
+    listed.close()
+    out0, st0 = results[0]
+    assert st0[5] == 4 and st0[30] == 4 and np.count_nonzero(st0) == 2
+    for out, st in results[1:]:
+        assert np.array_equal(st, st0)
+        assert np.array_equal(out, out0, equal_nan=True)
+    for i in range(len(draws)):
+        if st0[i]:
+            continue
+        T = Ts[i]
+        ref = oracle.loglik(oracle.params_from_dict(draws[i]), grids[T], list(W.DETECTORS3), datas[T], psds[T],
+                            approximant=int(aps[i]))
+        assert abs(out0[i] - ref) <= MIXED_TOL, (i, out0[i], ref)
+    with pytest.raises(G.GwGpuError):
+        gpu_ctx.set_blocks_per_sm(5)
