@@ -312,14 +312,16 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 //   S2  W0 Pv2: ringdown frequencies; matching frequencies;  W1 D: phase at f_ref (inspiral);
 //       W2 D: ringdown-phase terms at f3
 //   S3  W0/W1 amplitude matching points;  D: phase connection in four pieces after them
-//       (W1 inspiral phase, W2 inspiral derivative and f1 terms, W3 f2 terms);
+//       (W0 f1 terms, W1 inspiral phase, W2 inspiral derivative, W3 f2 terms);
 //       Pv2: W2 inspiral part, W1 the other parts, W3 Euler and frame constants
 //   S3b Pv2: W2 phase connection constants
 //   S4  amplitude deltas (D: W0/W1/W3, Pv2: W0/W1);  W2 D: phase connection constants,
 //       phase/time shift / Pv2: time-shift nodes 0-4;  W3 Pv2: nodes 5-9
-//   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions;  W3 D: detector phases and factors /
-//       Pv2: time shift, angles
-//   S6  W0 Pv2: detector phases and factors; outputs
+//   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions, D: detector factors;
+//       W3 D: detector phases / Pv2: time shift, angles
+//   S6  W0 Pv2: detector phases and factors; outputs;  W1-W3 the bin kernel's work order
+// (per-warp clock stamps of each stage guided the split: IMRPhenomD, warm,
+// before this split S3 20.2k / S5 22.2k / S6 13.0k cycles on the longest warp)
 // Programmatic dependent launch: a kernel launched with the programmatic
 // stream-serialisation attribute may start while the one before it on the
 // stream still runs; grid_dep_wait() returns once that kernel has completed
@@ -342,13 +344,14 @@ __device__ __forceinline__ int order_bucket(int kcut, int t, int tile) {
   const int lp = min(np, (live + kSegBins - 1) / kSegBins);
   return (int)((long long)(np - lp) * (kOrderBuckets - 1) / np);  // 0: all passes live
 }
-// Warp-wide: lane l appends the items of its request (kcut: end of its live
-// bins, nt items from i0) to their buckets.  Lanes that draw the same bucket
-// add to it once.  Every lane of the warp calls this (nt = 0 for none).
-__device__ __forceinline__ void order_append(const OrderArgs &o, int kcut, int nt, int i0) {
+// Warp-wide: lane l appends the items t = t0, t0 + dt, ... of its request
+// (kcut: end of its live bins, nt items from i0) to their buckets.  Lanes that
+// draw the same bucket add to it once.  Every lane of the warp calls this
+// (nt = 0 for none).
+__device__ __forceinline__ void order_append(const OrderArgs &o, int kcut, int nt, int i0, int t0, int dt) {
   const int lane = threadIdx.x & 31;
   const int ntmax = __reduce_max_sync(0xffffffffu, nt);
-  for (int t = 0; t < ntmax; t++) {
+  for (int t = t0; t < ntmax; t += dt) {
     const int b = t < nt ? order_bucket(kcut, t, o.tile) : -1;
     const unsigned grp = __match_any_sync(0xffffffffu, b);
     const int leader = __ffs(grp) - 1;
@@ -462,7 +465,10 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   __syncthreads();
   // S3
   if (run) {
-    if (warp == 0) d_amp_conn_low(r.m, s_ac[lane]);
+    if (warp == 0) {
+      d_amp_conn_low(r.m, s_ac[lane]);
+      if (!pv2) phase_conn_imr1(r.m, s_pc[lane]);
+    }
     if (warp == 1) {
       d_amp_conn_high(r.m, s_ac[lane]);
       if (pv2) phase_conn_imr(r.m, s_pc[lane]);
@@ -473,7 +479,6 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
         phase_conn_ins(r.m, s_pc[lane]);
       } else {
         phase_conn_dins(r.m, s_pc[lane]);
-        phase_conn_imr1(r.m, s_pc[lane]);
       }
     }
     if (warp == 3) {
@@ -513,14 +518,13 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
       const double df = s_df[lane];
       if (warp == 0) mixed_amp_coeffs(r, df, x);
       if (warp == 1) mixed_phase_coeffs(r, df, x);
-      if (warp == 2) mixed_regions(r, df, x);
+      if (warp == 2) {
+        mixed_regions(r, df, x);  // sets x.A_scale
+        if (!pv2) mixed_det_factors_a(r, x, x.A_scale, s_ds[lane], s_ws[lane]);
+      }
       if (warp == 3) {
-        if (pv2) {
-          mixed_pv2_coeffs(r, df, x);
-        } else {
-          mixed_det_phase(r, df, x);
-          mixed_det_factors_a(r, x, mixed_a_scale(r, df), s_ds[lane], s_ws[lane]);
-        }
+        if (pv2) mixed_pv2_coeffs(r, df, x);
+        else mixed_det_phase(r, df, x);
       }
     }
   }
@@ -547,18 +551,20 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     if (st && req) req[i].m.status = st;
     status[i] = st;
   }
-  if (warp == 0 && ord.fill && want_mixed) {  // this block's requests into the work order
+  if (warp >= 1 && ord.fill && want_mixed) {
+    // this block's requests into the work order, on the warps idle in S6 (warp
+    // w takes the tiles t = w - 1 mod 3); a request is live when S6's status
+    // will be 0: valid parameters, model status 0, one uniform grid length
     int kcut = 0, nt = 0, i0 = 0;
     if (act) {
-      const MixedReq &x = mreq[i];
-      if (x.status == 0) {
+      if (!s_bad[lane] && r.m.status == 0 && s_st[lane] == 0 && s_uni[lane]) {
         const StreamDev &s0 = streams[handles[i * ndet]];
-        kcut = min(s0.N, x.n_cut - s0.n0 + 1);
+        kcut = min(s0.N, mreq[i].n_cut - s0.n0 + 1);  // n_cut: written in S5
       }
       nt = ord.item_count[i];
       i0 = ord.item_start[i];
     }
-    order_append(ord, kcut, nt, i0);
+    order_append(ord, kcut, nt, i0, warp - 1, kCoopWarps - 1);
   }
 }
 

@@ -446,11 +446,23 @@ GW_HD void mixed_pv2_coeffs(const Request &r, double df, MixedReq &x) {
     split_f(cw * cw, x.x2c, x.x2c_lo);  // L2PN x = (pi M f)^(2/3) = cw^2 t^2
   }
 }
-// Detectors in two parts: the linear phases and projections (needs the time
-// shift), then the finalize factors (needs the amplitude scale).
+// The complex antenna factor G_d of the response r_d = G_d h (D: the
+// inclination factors of h+ and hx folded in; Pv2: the 2 zeta rotation).
+GW_HD void mixed_det_G(const Request &r, int d, double &Gre, double &Gim) {
+  if (r.approximant == kPhenomPv2) {
+    Gre = r.det[d].fp * r.p.c2z - r.det[d].fc * r.p.s2z;
+    Gim = r.det[d].fp * r.p.s2z + r.det[d].fc * r.p.c2z;
+  } else {
+    const double ci = r.m.s.cos_incl;
+    Gre = r.det[d].fp * .5 * (1 + ci * ci);
+    Gim = -r.det[d].fc * ci;
+  }
+}
+// Detectors in two independent parts: the linear phases and projections
+// (needs the time shift), and the finalize factors (needs the amplitude
+// scale).
 GW_HD void mixed_det_phase(const Request &r, double df, MixedReq &x) {
   const ModelD &m = r.m;
-  const Source &s = m.s;
   const bool pv2 = (r.approximant == kPhenomPv2);
   // ---------------- linear phase per detector, in turns (f = n df):
   // D:   psi_d = phi(f) - tcl (f - fref) - phic - tau_d f
@@ -459,21 +471,14 @@ GW_HD void mixed_det_phase(const Request &r, double df, MixedReq &x) {
   double c0 = (m.tcl * m.fref - m.phic) * inv2pi;
   double c1 = -m.tcl * df * inv2pi;
   if (pv2) c1 += r.p.t_corr * df;
-  double ci = s.cos_incl;
   for (int d = 0; d < r.ndet; d++) {
     x.det[d].L0 = turns_q64(c0);
     x.det[d].L1 = turns_q64(c1 - r.det[d].tau * df * inv2pi);
-    if (pv2) {
-      x.det[d].Gre = r.det[d].fp * r.p.c2z - r.det[d].fc * r.p.s2z;
-      x.det[d].Gim = r.det[d].fp * r.p.s2z + r.det[d].fc * r.p.c2z;
-    } else {
-      x.det[d].Gre = r.det[d].fp * .5 * (1 + ci * ci);
-      x.det[d].Gim = -r.det[d].fc * ci;
-      // DH_d = A ds Re(conj(G) S) = A ds |G| Re(e^{-i arg G} S): the phase of
-      // conj(G) joins the detector's fixed-point linear phase, so the bins
-      // accumulate Re(S) only and |G| is applied in FP64 (mixed_det_factors_a)
-      x.det[d].L0 -= turns_q64(atan2(x.det[d].Gim, x.det[d].Gre) * inv2pi);
-    }
+    mixed_det_G(r, d, x.det[d].Gre, x.det[d].Gim);
+    // D: DH_d = A ds Re(conj(G) S) = A ds |G| Re(e^{-i arg G} S): the phase of
+    // conj(G) joins the detector's fixed-point linear phase, so the bins
+    // accumulate Re(S) only and |G| is applied in FP64 (mixed_det_factors_a)
+    if (!pv2) x.det[d].L0 -= turns_q64(atan2(x.det[d].Gim, x.det[d].Gre) * inv2pi);
   }
 }
 // A: the amplitude scale (x.A_scale, passed so that a caller that has just
@@ -482,7 +487,9 @@ GW_HD void mixed_det_factors_a(const Request &r, MixedReq &x, double A, const do
   const bool pv2 = (r.approximant == kPhenomPv2);
   for (int d = 0; d < r.ndet; d++) {
     // HH = A^2 w |G h|^2 sums, DH = A d Re(G ...) sums; log L = -HH/2 + DH
-    const double G1 = x.det[d].Gre, G2 = x.det[d].Gim, w = wscale[d], ds = dscale[d];
+    double G1, G2;
+    mixed_det_G(r, d, G1, G2);
+    const double w = wscale[d], ds = dscale[d];
     double *f = x.fc + d * kAccPerDet;
     if (pv2) {
       f[0] = -0.5 * A * A * w * G1 * G1;
