@@ -883,7 +883,8 @@ def main():
                               "peak_source": "measured in this run: FP64 GEMM 4096^3"},
                      "hbm": {"achieved_gbs": TRAFFIC_PER_LAUNCH / kernel_s / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
                              "frac": TRAFFIC_PER_LAUNCH / kernel_s / 1e9 / peaks["hbm_gbs"]
-                             if peaks.get("hbm_gbs") else None, "peak_source": "MEASURED_PEAKS.json"}},
+                             if peaks.get("hbm_gbs") else None, "peak_source": "MEASURED_PEAKS.json"},
+                     "issue": issue_roofline(kernel_s, res["clocks"])},
         "cpu_baseline": base,
         "parity": dict(parity, tolerance=1e-3, status_ok=res["stat_ok"]),
     }
@@ -911,12 +912,31 @@ def main():
 # Work of the 512-request IMRPhenomD step: reference flops per unit, counted
 # by oracle/count_ops.py on the reference's own model code (oracle/op_counts.json);
 # and, from one ncu capture of k_batch<3,1> on this workload
-# (profiles/k_batch_mixed_ptstep512.md), its DRAM bytes and FP64 flops per launch.
+# (profiles/k_batch_mixed_ptstep512.md), its DRAM bytes, FP64 flops and warp
+# instructions per launch.
 PROFILE_SOURCE = "profiles/k_batch_mixed_ptstep512.md"
 REF_FLOPS_PER_WAVE_BIN = 66.56
 REF_FLOPS_PER_DET_BIN = 33.0
 TRAFFIC_PER_LAUNCH = 2.48e6
 FP64_FLOP_PER_LAUNCH = 1.98e7
+INST_PER_LAUNCH = 8.92e7
+
+
+def issue_roofline(kernel_s, clocks):
+    """The bin kernel against the instruction-issue limit (it is issue-bound:
+    no pipe saturates): warp instructions per launch (ncu) / event-timed
+    duration, against 4 issue slots per SM per cycle at the SM clock seen
+    under load."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    if not mhz:
+        return None
+    peak = sms * 4 * mhz * 1e6
+    achieved = INST_PER_LAUNCH / kernel_s
+    return {"achieved_warp_inst_per_s": achieved, "peak_warp_inst_per_s": peak, "frac": achieved / peak,
+            "inst_per_launch": INST_PER_LAUNCH, "inst_source": "ncu smsp__inst_executed.sum of one launch, " +
+            PROFILE_SOURCE, "peak_source": "%d SMs x 4 schedulers x %.0f MHz (clocks under load)" % (sms, mhz)}
 
 
 def measure_peak(dtype):
