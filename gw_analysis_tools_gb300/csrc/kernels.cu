@@ -316,9 +316,10 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 //       Pv2: W2 inspiral part, W1 the other parts, W3 Euler and frame constants
 //   S3b Pv2: W2 phase connection constants
 //   S4  amplitude deltas (D: W0/W1/W3, Pv2: W0/W1);  W2 D: phase connection constants,
-//       phase/time shift / Pv2: time-shift nodes 0-4;  W3 Pv2: nodes 5-9
-//   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions, D: detector factors;
-//       W3 D: detector phases / Pv2: time shift, angles
+//       phase/time shift / Pv2: time-shift nodes 0-4;  W3 Pv2: nodes 5-9 (two
+//       nodes at a time on the half-warps)
+//   S5  W0 mixed amplitude;  W1 mixed phase;  W2 regions, D: detector factors / Pv2:
+//       angles;  W3 D: detector phases / Pv2: time shift
 //   S6  W0 Pv2: detector phases and factors; outputs;  W1-W3 the bin kernel's work order
 // (per-warp clock stamps of each stage guided the split: IMRPhenomD, warm,
 // before this split S3 20.2k / S5 22.2k / S6 13.0k cycles on the longest warp)
@@ -504,9 +505,13 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
       if (warp == 0) d_deltas(r.m, s_ac[lane], 0, 3);
       if (warp == 1) d_deltas(r.m, s_ac[lane], 3, 5);
     }
-    if (pv2 && r.m.s.shift_time && (warp == 2 || warp == 3)) {
-      for (int j = (warp - 2) * (kPv2ShiftNodes / 2); j < (warp - 1) * (kPv2ShiftNodes / 2); j++)
-        s_shift[lane][j] = pv2_shift_node(r.m, j);
+  }
+  if (warp == 2 || warp == 3) {  // Pv2 time-shift nodes: both half-warps, lanes j and j + kCoopReq on request j
+    const Request &rh = s_r[hl];
+    if (hact && !s_bad[hl] && rh.approximant == kPhenomPv2 && rh.m.s.shift_time) {
+      const int j1 = (warp - 1) * (kPv2ShiftNodes / 2);
+      for (int j = (warp - 2) * (kPv2ShiftNodes / 2) + (lane >= kCoopReq ? 1 : 0); j < j1; j += 2)
+        s_shift[hl][j] = pv2_shift_node(rh.m, j);
     }
   }
   __syncthreads();
@@ -520,12 +525,10 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
       if (warp == 1) mixed_phase_coeffs(r, df, x);
       if (warp == 2) {
         mixed_regions(r, df, x);  // sets x.A_scale
-        if (!pv2) mixed_det_factors_a(r, x, x.A_scale, s_ds[lane], s_ws[lane]);
-      }
-      if (warp == 3) {
         if (pv2) mixed_pv2_coeffs(r, df, x);
-        else mixed_det_phase(r, df, x);
+        else mixed_det_factors_a(r, x, x.A_scale, s_ds[lane], s_ws[lane]);
       }
+      if (warp == 3 && !pv2) mixed_det_phase(r, df, x);
     }
   }
   __syncthreads();
