@@ -551,15 +551,18 @@ int gwgpu_mcmc_likelihood_extrinsic(gwgpu_context *c, const gwgpu_gen_params *p,
   int nblk = gwk::plain_blocks(sd[0].N);
   int st = c->workspace(gwgpu_context::kWsPlain, sizeof(double) * ((size_t)nblk * 2 * gwt::kMaxDet + 8), &dev);
   if (st) return st;
-  double *part = (double *)dev, *res = part + (size_t)nblk * 2 * gwt::kMaxDet;
+  double *part = (double *)dev;
   unsigned *cnt = c->counter(1);
   if (!cnt) return GWGPU_ECUDA;
-  cudaError_t e = gwk::launch_plain(r, sd, ndet, part, cnt, res, nullptr, c->stream);
-  if (e != cudaSuccess) return c->fail(e, "plain launch");
-  double *h;
+  // the last block writes log L straight into pinned host memory (mapped:
+  // no copy after the kernel)
+  double *h, *hd;
   st = c->pinned(gwgpu_context::kHwsPlain, 64, (void **)&h);
   if (st) return st;
-  cudaMemcpyAsync(h, res, 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaHostGetDevicePointer((void **)&hd, h, 0);
+  if (e != cudaSuccess) return c->fail(e, "plain result mapping");
+  e = gwk::launch_plain(r, sd, ndet, part, cnt, hd, nullptr, c->stream);
+  if (e != cudaSuccess) return c->fail(e, "plain launch");
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return c->fail(e, "plain");
   *loglik = r.m.status ? NAN : h[0];
