@@ -797,31 +797,36 @@ GW_HD void cmulf(float ac, float as, float bc, float bs, float &c, float &s) {
   s = as * bc + ac * bs;
 }
 
-// One bin of the mixed form, accumulated into acc[d * kAccPerDet + j], with
-// the phase ph (Pv2: phase + 2 epsilon) and the Pv2 angle al in turns * 2^64.
-// dre/dim/w: the detector streams at this bin; rotc/rots: the detector's linear
-// phase rotation at this bin (cos, sin).  The detector phase is the angle sum
-// of ph and that rotation.
+// IMRPhenomD bin: two sums per detector at acc[d * STRIDE + 0] (weighted
+// |h|^2; once for all detectors when they share a weight stream) and
+// acc[d * STRIDE + 1] (Re d* h e^{i phi_d}).
+template <int NDET, int STRIDE>
+GW_HD void mixed_bin_d(const MixedReq &x, int n, uint64_t ph, float tf, float m76, const float *dre, const float *dim,
+                       const float *w, const float *rotc, const float *rots, KSum *acc, bool wshared) {
+  if (n > x.n_cut) return;
+  const float a = mixed_amp(x, n, tf, m76);
+  float sp, cp;
+  q64_sincospi(ph, &sp, &cp);
+  const float aa = a * a;
+#pragma unroll
+  for (int d = 0; d < NDET; d++) {
+    float sn, cs;
+    cmulf(cp, sp, rotc[d], rots[d], cs, sn);
+    float ar = a * dre[d], ai = a * dim[d];
+    if (d == 0 || !wshared) kadd(acc[d * STRIDE + 0], w[d] * aa);
+    kadd(acc[d * STRIDE + 1], ar * cs - ai * sn);  // Re(a dhat e^{i (phase + linear phase - arg G)})
+  }
+}
+// IMRPhenomPv2 bin: five sums per detector at acc[d * kAccPerDet + j], with
+// the Euler angle alpha in fixed-point turns.
 template <int NDET>
-GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float tf, float m76, const float *dre,
+GW_HD void mixed_bin_p(const MixedReq &x, int n, uint64_t ph, uint64_t al, float tf, float m76, const float *dre,
                        const float *dim, const float *w, const float *rotc, const float *rots, KSum *acc,
                        bool wshared) {
   if (n > x.n_cut) return;
   float a = mixed_amp(x, n, tf, m76);
   float sp, cp;
   q64_sincospi(ph, &sp, &cp);
-  if (x.approximant != kPhenomPv2) {
-    float aa = a * a;
-#pragma unroll
-    for (int d = 0; d < NDET; d++) {
-      float sn, cs;
-      cmulf(cp, sp, rotc[d], rots[d], cs, sn);
-      float ar = a * dre[d], ai = a * dim[d];
-      if (d == 0 || !wshared) kadd(acc[d * kAccPerDet + 0], w[d] * aa);
-      kadd(acc[d * kAccPerDet + 1], ar * cs - ai * sn);  // Re(a dhat e^{i (phase + linear phase - arg G)})
-    }
-    return;
-  }
   // Pv2: twist-up (FP32) with alpha from its fixed-point turns
   float sa, ca;
   q64_sincospi(al, &sa, &ca);
@@ -873,6 +878,21 @@ GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float
     kadd(acc[d * kAccPerDet + 3], qr * hpr + qi * hpi);  // Re(q conj(hpf))
     kadd(acc[d * kAccPerDet + 4], qr * hcr + qi * hci);  // Re(q conj(hcf))
   }
+}
+
+// One bin of the mixed form, accumulated into acc[d * kAccPerDet + j], with
+// the phase ph (Pv2: phase + 2 epsilon) and the Pv2 angle al in turns * 2^64.
+// dre/dim/w: the detector streams at this bin; rotc/rots: the detector's linear
+// phase rotation at this bin (cos, sin).  The detector phase is the angle sum
+// of ph and that rotation.
+template <int NDET>
+GW_HD void mixed_bin_q(const MixedReq &x, int n, uint64_t ph, uint64_t al, float tf, float m76, const float *dre,
+                       const float *dim, const float *w, const float *rotc, const float *rots, KSum *acc,
+                       bool wshared) {
+  if (x.approximant != kPhenomPv2)
+    mixed_bin_d<NDET, kAccPerDet>(x, n, ph, tf, m76, dre, dim, w, rotc, rots, acc, wshared);
+  else
+    mixed_bin_p<NDET>(x, n, ph, al, tf, m76, dre, dim, w, rotc, rots, acc, wshared);
 }
 
 // The per-bin FP64 path: phase and alpha of bin n in fixed-point turns.
