@@ -653,6 +653,136 @@ __device__ __forceinline__ void block_sum_mixed(const float (&v)[NV], float *sm,
   __syncthreads();
 }
 
+// One item of the mixed form for one approximant class, its sums into
+// v[d * kAccPerDet + j]: IMRPhenomD keeps two sums per detector live through
+// the item (twelve registers for three detectors instead of thirty), Pv2 five.
+template <int NDET, bool PV2>
+__device__ __forceinline__ void mixed_item(const BatchArgs &a, const MixedReq &x, const StreamDev *s_st, const Item &I,
+                                           int N, int kend, double *s_node, double *s_node_a, SegPoly *s_poly,
+                                           SegPoly *s_poly_a, double *s_coef, float2 *s_rot_seg, float2 *s_rot_off,
+                                           float (&v)[NDET * kAccPerDet]) {
+  const int tid = threadIdx.x;
+  constexpr int NA = PV2 ? kAccPerDet : 2;  // sums per detector: Pv2 five, D two
+  KSum acc[NDET * NA];
+#pragma unroll
+  for (int j = 0; j < NDET * NA; j++) acc[j] = KSum{0.f, 0.f};
+  if (x.status == 0) {
+    const int n0 = s_st[0].n0;
+    const float *dh[NDET];
+    const float *wh[NDET];
+#pragma unroll
+    for (int d = 0; d < NDET; d++) {
+      dh[d] = s_st[d].dhat;
+      wh[d] = s_st[d].what;
+    }
+    int kcut = min(kend, x.n_cut - n0 + 1);
+    if (kcut > I.k0 && (n0 < 1 || n0 + kcut - 1 > a.tables.nmax)) {  // grid beyond the power tables
+      if (tid == 0) atomicOr(a.status + I.req, kStatusBounds);
+      kcut = I.k0;
+    }
+    constexpr bool pv2 = PV2;
+    const bool wsh = x.wshared != 0;  // one weight stream for every detector
+    const gwt::Tables &tb = a.tables;
+    // this thread's offset rotations (read back only by this thread)
+#pragma unroll
+    for (int d = 0; d < NDET; d++) {
+      float c, sn;
+      det_rot_off(x, d, tid, c, sn);
+      s_rot_off[d * kBatchBlock + tid] = make_float2(c, sn);
+    }
+    // chunks of up to kMaxSegs segments (one segment = one pass of the block over kSegBins bins)
+    for (int c0 = I.k0; c0 < kcut; c0 += kMaxSegs * kSegBins) {
+      const int nseg = min(kMaxSegs, (kcut - c0 + kSegBins - 1) / kSegBins);
+      const int nfn = pv2 ? 2 : 1;  // phase, and alpha for Pv2
+      // (A) FP64 phase (and alpha) at the nodes of every usable segment
+      for (int e = tid; e < nseg * kSegEval; e += blockDim.x) {
+        const int sg = e / kSegEval, j = e - sg * kSegEval, kseg = c0 + sg * kSegBins;
+        double vp = 0.0, va = 0.0;
+        const int n = seg_node_n(n0, kseg, j);
+        if (seg_usable(x, n0, N, kseg) && n <= tb.nmax) {
+          const double t = __ldg(tb.t13 + n), r = __ldg(tb.tm53 + n), lnn = __ldg(tb.tln + n);
+          vp = mixed_phase_full(x, n, t, r, lnn, __ldg(tb.t34 + n), false);
+          if (pv2) va = mixed_pv2_alpha(x, n, t, r, lnn);
+        }
+        s_node[e] = vp;
+        s_node_a[e] = va;
+      }
+      __syncthreads();
+      // (B1) polynomial coefficients and their stored form, one thread per
+      // (segment, function, coefficient); a segment the check rejects below
+      // keeps unused stored coefficients
+      for (int e = tid; e < nseg * nfn * kSegNodes; e += blockDim.x) {
+        const int j = e % kSegNodes, q = e / kSegNodes, sg = q / nfn, fn = q - sg * nfn;
+        const double *v = (fn ? s_node_a : s_node) + sg * kSegEval;
+        double *cf = s_coef + (sg * 2 + fn) * kSegNodes;
+        const bool use = seg_usable(x, n0, N, c0 + sg * kSegBins);
+        cf[j] = use ? seg_coef(v, j) : 0.0;
+        if (use) seg_store(v, cf, j, fn ? s_poly_a[sg] : s_poly[sg]);
+      }
+      __syncthreads();
+      // segment-pass rotations of the detectors
+      for (int e = tid; e < nseg * NDET; e += blockDim.x) {
+        const int sg = e / NDET, d = e - sg * NDET;
+        float c, sn;
+        det_rot_seg(x, d, n0 + c0 + sg * kSegBins, c, sn);
+        s_rot_seg[sg * NDET + d] = make_float2(c, sn);
+      }
+      // (B2) acceptance per (segment, function)
+      for (int e = tid; e < nseg * 2; e += blockDim.x) {
+        const int sg = e >> 1, fn = e & 1, kseg = c0 + sg * kSegBins;
+        SegPoly &P = fn ? s_poly_a[sg] : s_poly[sg];
+        bool ok = seg_usable(x, n0, N, kseg) && seg_node_n(n0, kseg, 8) <= tb.nmax;
+        if (ok && (fn == 0 || pv2))
+          ok = seg_check((fn ? s_node_a : s_node) + sg * kSegEval, s_coef + (sg * 2 + fn) * kSegNodes) == 0;
+        P.direct = ok ? 0 : 1;
+      }
+      __syncthreads();
+      // (C) bins: the block covers one segment per pass
+      for (int sg = 0; sg < nseg; sg++) {
+        const int kseg = c0 + sg * kSegBins, k = kseg + tid;
+        const bool direct = s_poly[sg].direct | (pv2 ? s_poly_a[sg].direct : 0);
+        if (k < kcut) {
+          const int n = n0 + k;
+          uint64_t ph, al = 0;
+          if (!direct) {
+            const int m = tid - kSegHalf;
+            ph = seg_eval(s_poly[sg], m, n0 + kseg >= x.n_f2p ? seg_atan_extra(x, n) : 0.0f);
+            if (pv2) al = seg_eval(s_poly_a[sg], m);
+          } else {
+            mixed_phase_direct(x, n, __ldg(tb.t13 + n), __ldg(tb.tm53 + n), __ldg(tb.tln + n),
+                               __ldg(tb.t34 + n), ph, al);
+          }
+          float dre[NDET], dim[NDET], w[NDET];
+#pragma unroll
+          for (int d = 0; d < NDET; d++) {
+            float2 v = __ldg(((const float2 *)dh[d]) + k);
+            dre[d] = v.x;
+            dim[d] = v.y;
+            w[d] = (d == 0 || !wsh) ? __ldg(wh[d] + k) : 0.0f;
+          }
+          float rc[NDET], rs[NDET];
+#pragma unroll
+          for (int d = 0; d < NDET; d++) {
+            const float2 ra = s_rot_seg[sg * NDET + d], rb = s_rot_off[d * kBatchBlock + tid];
+            cmulf(ra.x, ra.y, rb.x, rb.y, rc[d], rs[d]);
+          }
+          if constexpr (PV2)
+            mixed_bin_p<NDET>(x, n, ph, al, __ldg(tb.t13f + n), __ldg(tb.tm76f + n), dre, dim, w, rc, rs, acc,
+                              wsh);
+          else
+            mixed_bin_d<NDET, 2>(x, n, ph, __ldg(tb.t13f + n), __ldg(tb.tm76f + n), dre, dim, w, rc, rs, acc,
+                                 wsh);
+        }
+      }
+      __syncthreads();  // the node and fit buffers are reused by the next chunk
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < NDET; d++)
+#pragma unroll
+    for (int j = 0; j < kAccPerDet; j++) v[d * kAccPerDet + j] = j < NA ? acc[d * NA + j].s - acc[d * NA + j].c : 0.f;
+}
+
 // OCC: the resident blocks per SM the register allocation is bounded for
 // (mixed form 3 or 4, a launch-shape choice of the autotuner; FP64 form 2).
 template <int NDET, int MIXED, int OCC>
@@ -736,119 +866,13 @@ __global__ void __launch_bounds__(kBatchBlock, OCC) k_batch(const BatchArgs a) {
     const int kend = min(I.k0 + a.tile, N);
     if constexpr (MIXED) {
       const MixedReq &x = *(const MixedReq *)s_req;
-      KSum acc[NV];
-#pragma unroll
-      for (int j = 0; j < NV; j++) acc[j] = KSum{0.f, 0.f};
-      if (x.status == 0) {
-        const int n0 = s_st[0].n0;
-        const float *dh[NDET];
-        const float *wh[NDET];
-#pragma unroll
-        for (int d = 0; d < NDET; d++) {
-          dh[d] = s_st[d].dhat;
-          wh[d] = s_st[d].what;
-        }
-        int kcut = min(kend, x.n_cut - n0 + 1);
-        if (kcut > I.k0 && (n0 < 1 || n0 + kcut - 1 > a.tables.nmax)) {  // grid beyond the power tables
-          if (tid == 0) atomicOr(a.status + I.req, kStatusBounds);
-          kcut = I.k0;
-        }
-        const bool pv2 = x.approximant == kPhenomPv2;
-        const bool wsh = x.wshared != 0;  // one weight stream for every detector
-        const gwt::Tables &tb = a.tables;
-        // this thread's offset rotations (read back only by this thread)
-#pragma unroll
-        for (int d = 0; d < NDET; d++) {
-          float c, sn;
-          det_rot_off(x, d, tid, c, sn);
-          s_rot_off[d * kBatchBlock + tid] = make_float2(c, sn);
-        }
-        // chunks of up to kMaxSegs segments (one segment = one pass of the block over kSegBins bins)
-        for (int c0 = I.k0; c0 < kcut; c0 += kMaxSegs * kSegBins) {
-          const int nseg = min(kMaxSegs, (kcut - c0 + kSegBins - 1) / kSegBins);
-          const int nfn = pv2 ? 2 : 1;  // phase, and alpha for Pv2
-          // (A) FP64 phase (and alpha) at the nodes of every usable segment
-          for (int e = tid; e < nseg * kSegEval; e += blockDim.x) {
-            const int sg = e / kSegEval, j = e - sg * kSegEval, kseg = c0 + sg * kSegBins;
-            double vp = 0.0, va = 0.0;
-            const int n = seg_node_n(n0, kseg, j);
-            if (seg_usable(x, n0, N, kseg) && n <= tb.nmax) {
-              const double t = __ldg(tb.t13 + n), r = __ldg(tb.tm53 + n), lnn = __ldg(tb.tln + n);
-              vp = mixed_phase_full(x, n, t, r, lnn, __ldg(tb.t34 + n), false);
-              if (pv2) va = mixed_pv2_alpha(x, n, t, r, lnn);
-            }
-            s_node[e] = vp;
-            s_node_a[e] = va;
-          }
-          __syncthreads();
-          // (B1) polynomial coefficients and their stored form, one thread per
-          // (segment, function, coefficient); a segment the check rejects below
-          // keeps unused stored coefficients
-          for (int e = tid; e < nseg * nfn * kSegNodes; e += blockDim.x) {
-            const int j = e % kSegNodes, q = e / kSegNodes, sg = q / nfn, fn = q - sg * nfn;
-            const double *v = (fn ? s_node_a : s_node) + sg * kSegEval;
-            double *cf = s_coef + (sg * 2 + fn) * kSegNodes;
-            const bool use = seg_usable(x, n0, N, c0 + sg * kSegBins);
-            cf[j] = use ? seg_coef(v, j) : 0.0;
-            if (use) seg_store(v, cf, j, fn ? s_poly_a[sg] : s_poly[sg]);
-          }
-          __syncthreads();
-          // segment-pass rotations of the detectors
-          for (int e = tid; e < nseg * NDET; e += blockDim.x) {
-            const int sg = e / NDET, d = e - sg * NDET;
-            float c, sn;
-            det_rot_seg(x, d, n0 + c0 + sg * kSegBins, c, sn);
-            s_rot_seg[sg * NDET + d] = make_float2(c, sn);
-          }
-          // (B2) acceptance per (segment, function)
-          for (int e = tid; e < nseg * 2; e += blockDim.x) {
-            const int sg = e >> 1, fn = e & 1, kseg = c0 + sg * kSegBins;
-            SegPoly &P = fn ? s_poly_a[sg] : s_poly[sg];
-            bool ok = seg_usable(x, n0, N, kseg) && seg_node_n(n0, kseg, 8) <= tb.nmax;
-            if (ok && (fn == 0 || pv2))
-              ok = seg_check((fn ? s_node_a : s_node) + sg * kSegEval, s_coef + (sg * 2 + fn) * kSegNodes) == 0;
-            P.direct = ok ? 0 : 1;
-          }
-          __syncthreads();
-          // (C) bins: the block covers one segment per pass
-          for (int sg = 0; sg < nseg; sg++) {
-            const int kseg = c0 + sg * kSegBins, k = kseg + tid;
-            const bool direct = s_poly[sg].direct | (pv2 ? s_poly_a[sg].direct : 0);
-            if (k < kcut) {
-              const int n = n0 + k;
-              uint64_t ph, al = 0;
-              if (!direct) {
-                const int m = tid - kSegHalf;
-                ph = seg_eval(s_poly[sg], m, n0 + kseg >= x.n_f2p ? seg_atan_extra(x, n) : 0.0f);
-                if (pv2) al = seg_eval(s_poly_a[sg], m);
-              } else {
-                mixed_phase_direct(x, n, __ldg(tb.t13 + n), __ldg(tb.tm53 + n), __ldg(tb.tln + n),
-                                   __ldg(tb.t34 + n), ph, al);
-              }
-              float dre[NDET], dim[NDET], w[NDET];
-#pragma unroll
-              for (int d = 0; d < NDET; d++) {
-                float2 v = __ldg(((const float2 *)dh[d]) + k);
-                dre[d] = v.x;
-                dim[d] = v.y;
-                w[d] = (d == 0 || !wsh) ? __ldg(wh[d] + k) : 0.0f;
-              }
-              float rc[NDET], rs[NDET];
-#pragma unroll
-              for (int d = 0; d < NDET; d++) {
-                const float2 ra = s_rot_seg[sg * NDET + d], rb = s_rot_off[d * kBatchBlock + tid];
-                cmulf(ra.x, ra.y, rb.x, rb.y, rc[d], rs[d]);
-              }
-              mixed_bin_q<NDET>(x, n, ph, al, __ldg(tb.t13f + n), __ldg(tb.tm76f + n), dre, dim, w, rc, rs, acc,
-                                wsh);
-            }
-          }
-          __syncthreads();  // the node and fit buffers are reused by the next chunk
-        }
-      }
       float v[NV];
-#pragma unroll
-      for (int j = 0; j < NV; j++) v[j] = acc[j].s - acc[j].c;
+      if (x.approximant == kPhenomPv2)
+        mixed_item<NDET, true>(a, x, s_st, I, N, kend, s_node, s_node_a, s_poly, s_poly_a, s_coef, s_rot_seg,
+                               s_rot_off, v);
+      else
+        mixed_item<NDET, false>(a, x, s_st, I, N, kend, s_node, s_node_a, s_poly, s_poly_a, s_coef, s_rot_seg,
+                                s_rot_off, v);
       block_sum_mixed<NV>(v, s_red, s_res);
     } else {
       const Request &r = *(const Request *)s_req;
