@@ -340,8 +340,10 @@ class Context:
         """The approximant and handle arrays of a call; the common shapes (one
         approximant, handles shared by every request) are kept between calls."""
         cache = self.__dict__.setdefault("_arrays", {})
-        akey = ("a", int(approximants), n) if np.ndim(approximants) == 0 else None
-        hkey = ("h", tuple(int(h) for h in handles), n) if np.ndim(handles) == 1 else None
+        akey = ("a", int(approximants), n) if isinstance(approximants, (int, np.integer)) else None
+        hkey = (("h", tuple(int(h) for h in handles), n)
+                if isinstance(handles, (list, tuple)) or (isinstance(handles, np.ndarray) and handles.ndim == 1)
+                else None)
         ap = cache.get(akey) if akey else None
         if ap is None:
             ap = np.ascontiguousarray(np.broadcast_to(np.asarray(approximants, dtype=np.int32), (n,)))
@@ -359,22 +361,45 @@ class Context:
                 cache[hkey] = hs
         return ap, hs
 
+    def _call_ptrs(self, approximants, handles, n):
+        """(approximants address, handles address, detectors) of a call: the
+        arrays of _call_arrays, their addresses kept beside them for the
+        common shapes (the address lookup costs a microsecond each)."""
+        key = None
+        if isinstance(approximants, (int, np.integer)) and isinstance(handles, (list, tuple)):
+            key = (int(approximants), tuple(handles), n)
+            hit = self.__dict__.get("_ptrs", {}).get(key)
+            if hit is not None:
+                return hit
+        ap, hs = self._call_arrays(approximants, handles, n)
+        res = (ap.ctypes.data, hs.ctypes.data, hs.shape[1], ap, hs)
+        if key is not None:
+            ptrs = self.__dict__.setdefault("_ptrs", {})
+            if len(ptrs) > 64:
+                ptrs.clear()
+            ptrs[key] = res
+        return res
+
     def loglik_batch(self, params, approximants, handles, T_segment, precision=PREC_MIXED):
         """params: GenParams array or list; handles: (ndet,) shared or (n, ndet) per request."""
         parr = params if isinstance(params, ctypes.Array) else params_array(params)
         n = len(parr)
-        ap, hs = self._call_arrays(approximants, handles, n)
-        out = np.empty(n)
-        status = np.empty(n, dtype=np.int32)
+        ap_ptr, hs_ptr, ndet, _, _ = self._call_ptrs(approximants, handles, n)
+        # log L (n doubles) then status (n int32) in one allocation: one address lookup
+        buf = np.empty(12 * n, dtype=np.uint8)
+        base = buf.ctypes.data
+        out = buf[:8 * n].view(np.float64)
+        status = buf[8 * n:].view(np.int32)
         fn = self.__dict__.get("_lb_raw")
         if fn is None:  # the same entry point with address arguments (no pointer objects per call)
             v = ctypes.c_void_p
             fn = ctypes.CFUNCTYPE(ctypes.c_int, v, v, v, ctypes.c_int, v, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                   v, v)(("gwgpu_loglik_batch", self.lib))
             self._lb_raw = fn
-        st = fn(self.h, ctypes.addressof(parr), ap.ctypes.data, n, hs.ctypes.data, hs.shape[1], float(T_segment),
-                precision, out.ctypes.data, status.ctypes.data)
-        self._check(st, "loglik_batch")
+        st = fn(self.h, ctypes.addressof(parr), ap_ptr, n, hs_ptr, ndet, float(T_segment), precision, base,
+                base + 8 * n)
+        if st:
+            self._check(st, "loglik_batch")
         return out, status
 
     def mcmc_loglik_batch(self, theta, approximant, gmst, handles, T_segment, precision=PREC_MIXED):
@@ -563,11 +588,17 @@ class Server:
 def _ctx_batch_device(self, d_params_ptr, d_approx_ptr, n, handles, T_segment, precision, d_out_ptr, d_status_ptr,
                       stream=None):
     """gwgpu_loglik_batch_device on raw device pointers (e.g. torch tensors' data_ptr())."""
-    _, hs = self._call_arrays(0, handles, n)
-    ndet = hs.shape[1]
-    st = self.lib.gwgpu_loglik_batch_device(self.h, d_params_ptr, d_approx_ptr, n, _ip(hs), ndet, float(T_segment),
-                                            precision, d_out_ptr, d_status_ptr, stream)
-    self._check(st, "loglik_batch_device")
+    _, hs_ptr, ndet, _, _ = self._call_ptrs(0, handles, n)
+    fn = self.__dict__.get("_lbd_raw")
+    if fn is None:  # the entry point with address arguments
+        v = ctypes.c_void_p
+        fn = ctypes.CFUNCTYPE(ctypes.c_int, v, v, v, ctypes.c_int, v, ctypes.c_int, ctypes.c_double, ctypes.c_int, v, v,
+                              v)(("gwgpu_loglik_batch_device", self.lib))
+        self._lbd_raw = fn
+    st = fn(self.h, d_params_ptr, d_approx_ptr, n, hs_ptr, ndet, float(T_segment), precision, d_out_ptr, d_status_ptr,
+            stream)
+    if st:
+        self._check(st, "loglik_batch_device")
 
 
 def _ctx_autotune(self, d_params_ptr, d_approx_ptr, n, handles, T_segment, precision, d_out_ptr, d_status_ptr):
