@@ -227,24 +227,31 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
   const int mixed = precision == GWGPU_PREC_MIXED;
   const gwgpu_context::Stream *s0 = c->get_stream(h_handles[0]);
   if (!s0) return GWGPU_ENOTFOUND;
-  std::string key((const char *)h_handles, (const char *)(h_handles + (size_t)n * ndet));
-  key += "|" + std::to_string(n) + "|" + std::to_string(ndet) + "|" + std::to_string(c->streams_epoch) + "|" +
-         std::to_string(mixed);
-  if (L.tk_shape != key) {  // the tuning class follows from the handles: recomputed when they change
+  // the batch shape (handles, sizes, registrations, precision) of the last
+  // call on this lane: the tuning class and the plan follow from it and are
+  // recomputed only when it changes (one comparison of the handle array)
+  const size_t nh = (size_t)n * ndet;
+  const bool same = L.shape.n == n && L.shape.ndet == ndet && L.shape.epoch == c->streams_epoch &&
+                    L.shape.mixed == mixed && L.shape.handles.size() == nh &&
+                    std::memcmp(L.shape.handles.data(), h_handles, sizeof(int) * nh) == 0;
+  if (!same) {
     L.tk = tune_key(c, mixed, ndet, h_handles, n);
-    L.tk_shape = key;
+    L.shape.handles.assign(h_handles, h_handles + nh);
+    L.shape.n = n;
+    L.shape.ndet = ndet;
+    L.shape.epoch = c->streams_epoch;
+    L.shape.mixed = mixed;
   }
   if (tile <= 0) tile = choose_tile(c, mixed, L.tk);
   const int occ = choose_occ(c, mixed, L.tk);
-  key += "|" + std::to_string(tile);
   bool replanned = false;
-  if (L.plan.key != key) {
+  if (!same || !L.plan.valid || L.plan.tile != tile) {
     int st = plan_batch(c, L, n, h_handles, ndet, tile);
     if (st) {
-      L.plan.key.clear();
+      L.plan.valid = false;
       return st;
     }
-    L.plan.key = key;
+    L.plan.valid = true;
     replanned = true;
   }
   size_t rq = mixed ? sizeof(gwt::MixedReq) : sizeof(gwt::Request);

@@ -5,8 +5,10 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <map>
 #include <string>
+#include <vector>
 
 #include "kernels.h"
 
@@ -15,7 +17,7 @@ struct gwgpu_context;
 namespace gwb {
 
 struct Plan {
-  std::string key;
+  bool valid = false;  // built for the lane's current batch shape and tile
   int n = 0, ndet = 0, tile = 0, nitems = 0;
   void *mem = nullptr;
   size_t cap = 0;
@@ -44,8 +46,14 @@ struct Lane {
   std::map<std::string, Graph> graphs;
   uint64_t graph_tick = 0;
   size_t bytes = 0;  // device bytes held (budget accounting)
-  // tuning class of the last batch shape (handles, precision, registration epoch)
-  std::string tk_shape, tk;
+  // the last batch shape (handles, sizes, registration epoch, precision) and
+  // its tuning class
+  struct Shape {
+    std::vector<int> handles;
+    int n = -1, ndet = -1, mixed = -1;
+    uint64_t epoch = ~0ull;
+  } shape;
+  std::string tk;
 };
 
 constexpr size_t kMaxGraphs = 8;
