@@ -917,9 +917,9 @@ def main():
 PROFILE_SOURCE = "profiles/k_batch_mixed_ptstep512.md"
 REF_FLOPS_PER_WAVE_BIN = 66.56
 REF_FLOPS_PER_DET_BIN = 33.0
-TRAFFIC_PER_LAUNCH = 2.48e6
+TRAFFIC_PER_LAUNCH = 2.39e6
 FP64_FLOP_PER_LAUNCH = 1.98e7
-INST_PER_LAUNCH = 8.92e7
+INST_PER_LAUNCH = 8.17e7
 
 
 def issue_roofline(kernel_s, clocks):
