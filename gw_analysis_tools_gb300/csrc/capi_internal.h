@@ -58,7 +58,7 @@ struct gwgpu_context {
   double chirp_kscale = 0;         // M max|B| of that kernel (the FP32 search's error scale)
   bool maxll_fp64 = false;         // maximised likelihood: FP64 transforms only (no FP32 search)
   bool prologue_serial = false;    // batched prologue: one thread per request instead of the cooperative kernel
-  bool order_items = true;         // mixed batch: items in live-work order (k_order_items) instead of as listed
+  bool order_items = true;         // mixed batch: items in work order (written by the prologue) instead of as listed
   bool pdl = true;                 // batch kernels as programmatic dependents of the prologue
   uint64_t streams_epoch = 0;      // bumped when the device stream table changes
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
