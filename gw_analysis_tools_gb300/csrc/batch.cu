@@ -161,8 +161,8 @@ int plan_batch(gwgpu_context *c, Lane &L, int n, const int *handles, int ndet, i
 }
 
 static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, const int *d_approx, int n,
-                           int ndet, double T_segment, int mixed, int occ, double *d_out, int *d_status, void *reqs,
-                           double *partials, unsigned *cnt) {
+                           int ndet, double T_segment, int mixed, int occ, double *d_out, int *d_status,
+                           int *status_out, void *reqs, double *partials, unsigned *cnt) {
   const Plan &pl = L.plan;
   const bool timing = c->timing && &L == &c->lane;
   if (timing) cudaEventRecord(c->t_ev[0], L.stream);
@@ -207,6 +207,7 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   a.partials = partials;
   a.out = d_out;
   a.status = d_status;
+  a.status_out = status_out ? status_out : d_status;
   a.tables = c->tables;
   int grid = std::min(pl.nitems, persistent_grid(c->device, mixed, ndet, occ));
   if (grid < 1) grid = 1;
@@ -223,7 +224,7 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
 
 int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, const int *d_approx, int n,
                   const int *h_handles, int ndet, double T_segment, int precision, double *d_out, int *d_status,
-                  int tile, bool use_graph, const BatchCopies *io) {
+                  int tile, bool use_graph, const BatchCopies *io, int *status_out) {
   const int mixed = precision == GWGPU_PREC_MIXED;
   const gwgpu_context::Stream *s0 = c->get_stream(h_handles[0]);
   if (!s0) return GWGPU_ENOTFOUND;
@@ -272,15 +273,16 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
   unsigned *cnt = (unsigned *)p;
   auto sequence = [&]() {
     if (io) cudaMemcpyAsync(io->h2d_dst, io->h2d_src, io->h2d_bytes, cudaMemcpyHostToDevice, L.stream);
-    int r = launch_sequence(c, L, d_params, d_approx, n, ndet, T_segment, mixed, occ, d_out, d_status, reqs, partials,
-                            cnt);
+    int r = launch_sequence(c, L, d_params, d_approx, n, ndet, T_segment, mixed, occ, d_out, d_status, status_out,
+                            reqs, partials, cnt);
     if (!r && io) cudaMemcpyAsync(io->d2h_dst, io->d2h_src, io->d2h_bytes, cudaMemcpyDeviceToHost, L.stream);
     return r;
   };
   if (!use_graph || c->timing) return sequence();
   char gk[320];
-  snprintf(gk, sizeof(gk), "%p|%p|%p|%p|%d|%d|%.17g|%d|%p|%p|%zu|%p|%p|%zu", (const void *)d_params,
-           (const void *)d_approx, (const void *)d_out, (const void *)d_status, mixed, occ, T_segment, n,
+  snprintf(gk, sizeof(gk), "%p|%p|%p|%p|%p|%d|%d|%.17g|%d|%p|%p|%zu|%p|%p|%zu", (const void *)d_params,
+           (const void *)d_approx, (const void *)d_out, (const void *)d_status, (const void *)status_out, mixed, occ,
+           T_segment, n,
            io ? io->h2d_src : nullptr, io ? io->h2d_dst : nullptr, io ? io->h2d_bytes : 0,
            io ? io->d2h_dst : nullptr, io ? (const void *)io->d2h_src : nullptr, io ? io->d2h_bytes : 0);
   auto it = L.graphs.find(gk);
@@ -378,15 +380,20 @@ int gwgpu_loglik_batch(gwgpu_context *c, const gwgpu_gen_params *params, const i
   const size_t o_ap = up256(pb), o_out = o_ap + up256(ab), o_st = o_out + up256(ob), total = o_st + up256(sb);
   int st = stage_io(c, L, total);
   if (st) return st;
-  char *hp = (char *)L.hio, *dp = (char *)L.dio;
+  char *hp = (char *)L.hio, *dp = (char *)L.dio, *hm = nullptr;
   std::memcpy(hp, params, pb);
   std::memcpy(hp + o_ap, approx, ab);
-  // inputs in, outputs out: copies in the same graph as the kernels
-  const gwb::BatchCopies io{hp, dp, o_out, hp + o_out, dp + o_out, total - o_out};
-  st = gwb::enqueue_batch(c, L, (const gwgpu_gen_params *)dp, (const int *)(dp + o_ap), n, handles, ndet, T_segment,
-                          precision, (double *)(dp + o_out), (int *)(dp + o_st), 0, c->use_graphs, &io);
+  // The kernels read the parameters from, and write log L and the status
+  // into, the pinned staging buffer (mapped: the transfers cross the
+  // host-device link inside the kernels, with no copy nodes); the working
+  // status, which items flag atomically, stays in device memory.
+  cudaError_t e = cudaHostGetDevicePointer((void **)&hm, hp, 0);
+  if (e != cudaSuccess) return c->fail(e, "batch staging mapping");
+  st = gwb::enqueue_batch(c, L, (const gwgpu_gen_params *)hm, (const int *)(hm + o_ap), n, handles, ndet, T_segment,
+                          precision, (double *)(hm + o_out), (int *)(dp + o_st), 0, c->use_graphs, nullptr,
+                          (int *)(hm + o_st));
   if (st) return st;
-  cudaError_t e = cudaStreamSynchronize(L.stream);
+  e = cudaStreamSynchronize(L.stream);
   if (e != cudaSuccess) return c->fail(e, "batch");
   std::memcpy(loglik, hp + o_out, ob);
   statuses((const int *)(hp + o_st), n, status);

@@ -78,10 +78,12 @@ struct BatchCopies {
 };
 // Enqueue prologue + fused kernel of n requests on L.stream (device arrays).
 // use_graph: capture/replay the launch sequence for this exact shape, with
-// the copies of io (may be null) inside the same graph.
+// the copies of io (may be null) inside the same graph.  status_out (null:
+// d_status) receives each request's final status; d_status is the working
+// array the items flag atomically and must be device memory.
 int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, const int *d_approx, int n,
                   const int *h_handles, int ndet, double T_segment, int precision, double *d_out, int *d_status,
-                  int tile, bool use_graph, const BatchCopies *io = nullptr);
+                  int tile, bool use_graph, const BatchCopies *io = nullptr, int *status_out = nullptr);
 void lane_release(gwgpu_context *c, Lane &L);
 
 }  // namespace gwb

@@ -938,7 +938,7 @@ __global__ void __launch_bounds__(kBatchBlock, OCC) k_batch(const BatchArgs a) {
             int st = x.status;
             if (__ldcg(a.status + I.req) & kStatusBounds) st = 5;
             a.out[I.req] = st ? __longlong_as_double(0x7ff8000000000000ll) : v;
-            a.status[I.req] = st;
+            a.status_out[I.req] = st;
           }
         }
       } else if (tid == 0) {
@@ -958,7 +958,7 @@ __global__ void __launch_bounds__(kBatchBlock, OCC) k_batch(const BatchArgs a) {
         }
         if (__ldcg(a.status + I.req) & kStatusBounds) st = 5;
         a.out[I.req] = st ? __longlong_as_double(0x7ff8000000000000ll) : ll;
-        a.status[I.req] = st;
+        a.status_out[I.req] = st;
       }
     }
     __syncthreads();

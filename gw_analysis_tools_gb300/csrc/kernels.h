@@ -99,7 +99,8 @@ struct BatchArgs {
   unsigned *req_done;      // per request finished-item counters (zeroed before launch)
   double *partials;        // nitems * kAcc
   double *out;
-  int *status;
+  int *status;      // per-request working status (device memory: the bounds flag is set atomically)
+  int *status_out;  // where the finalize writes each request's status (status itself, or mapped host memory)
   gwt::Tables tables;
 };
 // occ: the launch shape's resident blocks per SM (mixed 3 or 4, FP64 2);
