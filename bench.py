@@ -11,8 +11,10 @@ A step is one pass of the hot path over one batch of 512 requests.
           the device, CUDA events on the engine stream; L2 flushed (256 MiB
           write) before every step, outside the events.
   e2e     the same through the C ABI entry point gwgpu_loglik_batch with host
-          buffers: H2D of the parameters and D2H of log L + status inside the
-          timed region (wall clock per step), L2 flushed before every step.
+          buffers: the parameters host -> device and log L + status device ->
+          host inside the timed region (the kernels read and write the pinned
+          staging buffer over the host-device link), wall clock per step, L2
+          flushed before every step.
 
 Beside them: the plain FP64 one-request-per-launch form, the batched FP64
 form, the served form (Poisson arrivals, mixed D/Pv2, p50/p99), the uneven

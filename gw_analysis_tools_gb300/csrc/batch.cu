@@ -415,20 +415,20 @@ int gwgpu_mcmc_loglik_batch(gwgpu_context *c, const double *theta, int dim, int 
                total = o_st + up256(sb);
   int st = stage_io(c, L, total);
   if (st) return st;
-  char *hp = (char *)L.hio, *dp = (char *)L.dio;
+  char *hp = (char *)L.hio, *dp = (char *)L.dio, *hm = nullptr;
   std::memcpy(hp, theta, tb);
-  cudaMemcpyAsync(dp, hp, tb, cudaMemcpyHostToDevice, L.stream);
+  // the repack reads theta from the mapped staging buffer and the finalize
+  // writes log L and the status back into it (no copy nodes)
+  cudaError_t e = cudaHostGetDevicePointer((void **)&hm, hp, 0);
+  if (e != cudaSuccess) return c->fail(e, "batch staging mapping");
   gwgpu_gen_params *dparams = (gwgpu_gen_params *)(dp + o_p);
   int *dapprox = (int *)(dp + o_ap);
-  cudaError_t e = gwk::launch_mcmc_repack((const double *)dp, dim, n, approximant, gmst, (gwt::GenParams *)dparams,
-                                          dapprox, L.stream);
+  e = gwk::launch_mcmc_repack((const double *)hm, dim, n, approximant, gmst, (gwt::GenParams *)dparams, dapprox,
+                              L.stream);
   if (e != cudaSuccess) return c->fail(e, "repack launch");
-  double *dout = (double *)(dp + o_out);
-  int *dstat = (int *)(dp + o_st);
-  st = gwb::enqueue_batch(c, L, dparams, dapprox, n, handles, ndet, T_segment, precision, dout, dstat, 0,
-                          c->use_graphs);
+  st = gwb::enqueue_batch(c, L, dparams, dapprox, n, handles, ndet, T_segment, precision, (double *)(hm + o_out),
+                          (int *)(dp + o_st), 0, c->use_graphs, nullptr, (int *)(hm + o_st));
   if (st) return st;
-  cudaMemcpyAsync(hp + o_out, dout, total - o_out, cudaMemcpyDeviceToHost, L.stream);
   e = cudaStreamSynchronize(L.stream);
   if (e != cudaSuccess) return c->fail(e, "mcmc batch");
   std::memcpy(loglik, hp + o_out, ob);
