@@ -166,14 +166,16 @@ int launch(gwgpu_server *s, ServeLane &l) {
     ha[j] = sl.approx;
     for (int d = 0; d < ndet; d++) hh[j * ndet + d] = sl.handles[d];
   }
-  cudaMemcpyAsync(l.d, l.h, io.handles, cudaMemcpyHostToDevice, l.L.stream);  // params + approximants
-  double *dout = (double *)(l.d + io.out);
-  int *dst = (int *)(l.d + io.status);
-  st = gwb::enqueue_batch(c, l.L, (const gwgpu_gen_params *)(l.d + io.params), (const int *)(l.d + io.approx), n,
-                          hh, ndet, s->cfg.T_segment, s->cfg.precision, dout, dst, 0, false);
+  // the kernels read the parameters from, and write log L and the status
+  // into, the lane's mapped pinned buffer; the working status stays on the device
+  char *hm = nullptr;
+  cudaError_t e = cudaHostGetDevicePointer((void **)&hm, l.h, 0);
+  if (e != cudaSuccess) return c->fail(e, "serve staging mapping");
+  st = gwb::enqueue_batch(c, l.L, (const gwgpu_gen_params *)(hm + io.params), (const int *)(hm + io.approx), n, hh,
+                          ndet, s->cfg.T_segment, s->cfg.precision, (double *)(hm + io.out),
+                          (int *)(l.d + io.status), 0, false, nullptr, (int *)(hm + io.status));
   if (st) return st;
-  cudaMemcpyAsync(l.h + io.out, dout, io.total - io.out, cudaMemcpyDeviceToHost, l.L.stream);
-  cudaError_t e = cudaEventRecord(l.ev, l.L.stream);
+  e = cudaEventRecord(l.ev, l.L.stream);
   if (e != cudaSuccess) return c->fail(e, "serve launch");
   l.busy = true;
   s->launches++;
