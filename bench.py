@@ -327,6 +327,26 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
                 times.append(time.perf_counter() - t0)
         ex["plain_fp64_evals_per_s"] = len(times) / float(np.sum(times))
         ex["plain_fp64_p50_ms"] = float(np.median(times) * 1e3)
+        # the plain workload itself: Hanford only, 1000 calls at the injection
+        # scaled by 1 + 0.01 N(0,1) per parameter, FP64, L2 flushed before each
+        h1 = handles[:1]
+        c1 = W.perturbed(W.config1_source(), 1000, 21, frac=0.01)
+        c1p = [G.gen_params(**d) for d in c1]
+        t1, o1 = [], []
+        for i in range(len(c1p) + 8):
+            with torch.cuda.stream(stream):
+                flush_l2(flush)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            v = ctx.mcmc_likelihood_extrinsic(c1p[i % len(c1p)], "IMRPhenomD", h1, T)
+            if i >= 8:
+                t1.append(time.perf_counter() - t0)
+                o1.append(v)
+        ex["plain_config1"] = {"evals_per_s": len(t1) / float(np.sum(t1)), "p50_ms": float(np.median(t1) * 1e3),
+                               "p99_ms": float(np.percentile(t1, 99) * 1e3), "calls": len(t1),
+                               "workload": "IMRPhenomD, Hanford only, 32128 bins, the injection scaled by "
+                                           "1 + 0.01 N(0,1) per parameter, FP64, one call per request"}
+        ex["_parity_plain1"] = (c1[:200], np.array(o1[:200]))
 
     def batched_fp64():
         # batched FP64 (device resident)
@@ -608,9 +628,14 @@ def cpu_baseline(res, seconds=10.0):
     dt = time.perf_counter() - t0
     cores = os.cpu_count()
     err = np.abs(res["out_mixed"] - ref)
+    m, t1 = 0, time.perf_counter()  # the same port on one thread
+    while time.perf_counter() - t1 < 4.0:
+        O.loglik_batch(plist[:16], f, dets, data, [psd] * 3, nthreads=1)
+        m += 16
+    one = m / (time.perf_counter() - t1)
     return {"value": n / dt, "unit": "evals/s", "cores": cores, "kind": "port",
             "sample": "%d requests of the 512-request step (prior draws), %.1f s on %d threads" % (n, dt, cores),
-            "reference_code": reference_code_rate(O, f, dets, data, psd, plist)}, \
+            "value_1_core": one, "reference_code": reference_code_rate(O, f, dets, data, psd, plist)}, \
         {"max_abs_dlogL": float(err.max()), "p99_abs_dlogL": float(np.percentile(err, 99)),
          "median_abs_dlogL": float(np.median(err)), "requests": int(err.size)}
 
@@ -698,6 +723,11 @@ def secondary_parity(ex, res):
     from gw_analysis_tools_gb300 import workloads as W
     dets = list(W.DETECTORS3)
     out = {}
+    if "_parity_plain1" in ex:
+        pp, got = ex.pop("_parity_plain1")
+        # one detector: the plain call's T is 1/df of the grid, as the oracle's
+        ref = O.loglik_batch([O.params_from_dict(d) for d in pp], res["f"], dets[:1], res["data"][:1], [res["psd"]])
+        out["plain_config1"] = parity_stats(got, ref, 1e-9, rel=True)
     if "_parity_served" in ex:
         sp, sa, got = ex.pop("_parity_served")
         ref = O.loglik_batch([O.params_from_dict(d) for d in sp], res["f"], dets, res["data"], [res["psd"]] * 3,
@@ -892,8 +922,8 @@ def main():
     }
     if ex:
         plain = ex.get("plain_fp64_evals_per_s")
-        for k in ("plain_fp64_evals_per_s", "plain_fp64_p50_ms", "batched_fp64_evals_per_s", "served", "uneven_pv2",
-                  "maximized", "ingest", "gaussleg_fp64", "errors"):
+        for k in ("plain_fp64_evals_per_s", "plain_fp64_p50_ms", "plain_config1", "batched_fp64_evals_per_s", "served",
+                  "uneven_pv2", "maximized", "ingest", "gaussleg_fp64", "errors"):
             if k in ex:
                 line[k] = ex[k]
         if plain:
