@@ -332,21 +332,21 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         h1 = handles[:1]
         c1 = W.perturbed(W.config1_source(), 1000, 21, frac=0.01)
         c1p = [G.gen_params(**d) for d in c1]
-        t1, o1 = [], []
-        for i in range(len(c1p) + 8):
+        t1, o1 = [], np.zeros(len(c1p))
+        for i in range(-8, len(c1p)):  # 8 warm-up calls, then each request once
             with torch.cuda.stream(stream):
                 flush_l2(flush)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             v = ctx.mcmc_likelihood_extrinsic(c1p[i % len(c1p)], "IMRPhenomD", h1, T)
-            if i >= 8:
+            if i >= 0:
                 t1.append(time.perf_counter() - t0)
-                o1.append(v)
+                o1[i] = v
         ex["plain_config1"] = {"evals_per_s": len(t1) / float(np.sum(t1)), "p50_ms": float(np.median(t1) * 1e3),
                                "p99_ms": float(np.percentile(t1, 99) * 1e3), "calls": len(t1),
                                "workload": "IMRPhenomD, Hanford only, 32128 bins, the injection scaled by "
                                            "1 + 0.01 N(0,1) per parameter, FP64, one call per request"}
-        ex["_parity_plain1"] = (c1[:200], np.array(o1[:200]))
+        ex["_parity_plain1"] = (c1[:200], o1[:200].copy())
 
     def batched_fp64():
         # batched FP64 (device resident)
