@@ -36,6 +36,7 @@ using gwk::StreamDev;
 
 constexpr int kBlock = 128;
 constexpr int kStatusBounds = 0x100;  // set by a tile whose bins fall outside the tables
+constexpr int kStatusRedo = 10;       // five-point source left to the reference algorithm (never returned)
 
 // ------------------------------------------------------------- batched form
 __global__ void k_fisher_slots(const GenParams *__restrict__ params, int nsrc, int method, const int *__restrict__ dets,
@@ -47,10 +48,12 @@ __global__ void k_fisher_slots(const GenParams *__restrict__ params, int nsrc, i
 }
 
 __global__ void k_fisher_setup(const GenParams *__restrict__ params, int nsrc, int method, int ndet, double epsilon,
-                               int step_mode, const SlotOut *__restrict__ slots, FisherSrc *out, int *status) {
+                               int step_mode, int order, const SlotOut *__restrict__ slots, FisherSrc *out,
+                               int *status) {
   int src = blockIdx.x * blockDim.x + threadIdx.x;
   if (src >= nsrc) return;
-  status[src] = fisher_setup(params[src], method, ndet, epsilon, step_mode, slots + (size_t)src * kSlots, out[src]);
+  status[src] =
+      fisher_setup(params[src], method, ndet, epsilon, step_mode, order, slots + (size_t)src * kSlots, out[src]);
 }
 
 struct FisherArgs {
@@ -189,6 +192,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fisher_main(const FisherArgs a) {
         for (int j = 0; j < kDim * kDim; j++) outC[j] = cs ? __longlong_as_double(0x7ff8000000000000ll) : inv[j];
         if (!st && cs) st = 9;  // inversion failed
       }
+      if (!st && F.needs_ref) st = kStatusRedo;
       a.status[src] = st;
     }
     __syncthreads();
@@ -371,9 +375,11 @@ int gwgpu_fisher_numerical(gwgpu_context *c, const double *freqs, int N, const c
 }  // extern "C"
 
 // The moment form for n sources; acc64 selects FP64 per-bin values and sums.
-int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int method, const int *handles, int ndet,
-                   double epsilon, int step_mode, double *fisher, double *covariance, int *status, bool acc64) {
-  if (!c || !params || n < 1 || !handles || ndet < 1 || ndet > kMaxDet || !fisher || (method != 0 && method != 1))
+int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int method, int order, const int *handles,
+                   int ndet, double epsilon, int step_mode, double *fisher, double *covariance, int *status,
+                   bool acc64) {
+  if (!c || !params || n < 1 || !handles || ndet < 1 || ndet > kMaxDet || !fisher || (method != 0 && method != 1) ||
+      (order != 2 && order != 4))
     return GWGPU_EINVAL;
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
@@ -480,8 +486,8 @@ int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int 
     int tot = m * kSlots;
     k_fisher_slots<<<(tot + 63) / 64, 64, 0, c->stream>>>(dparams, m, method, ddets, ndet, df, epsilon, step_mode,
                                                           c->qnm_dev, slots);
-    k_fisher_setup<<<(m + 63) / 64, 64, 0, c->stream>>>(dparams, m, method, ndet, epsilon, step_mode, slots, srcs,
-                                                        dstat);
+    k_fisher_setup<<<(m + 63) / 64, 64, 0, c->stream>>>(dparams, m, method, ndet, epsilon, step_mode, order, slots,
+                                                        srcs, dstat);
     a.src = srcs;
     a.nsrc = m;
     a.item_counter = cnt + m;
@@ -526,13 +532,13 @@ int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int 
     // reference algorithm.
     std::vector<int> redo;
     for (int i = 0; i < m; i++)
-      if (hs[i] == 9) redo.push_back(i);
+      if (hs[i] == 9 || hs[i] == kStatusRedo) redo.push_back(i);
     if (!redo.empty()) {
       std::vector<GenParams> rp(redo.size());
       for (size_t j = 0; j < redo.size(); j++) std::memcpy(&rp[j], params + s0i + redo[j], sizeof(GenParams));
       std::vector<double> rf(redo.size() * kDim * kDim), rc(redo.size() * kDim * kDim);
       std::vector<int> rs(redo.size());
-      st = gwf_ref_run(c, rp.data(), (int)redo.size(), method, 2, handles, ndet, epsilon, step_mode, 0, rf.data(),
+      st = gwf_ref_run(c, rp.data(), (int)redo.size(), method, order, handles, ndet, epsilon, step_mode, 0, rf.data(),
                        covariance ? rc.data() : nullptr, rs.data());
       if (st) return st;
       for (size_t j = 0; j < redo.size(); j++) {
@@ -551,5 +557,5 @@ int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int 
 extern "C" int gwgpu_fisher_batch(gwgpu_context *c, const gwgpu_gen_params *params, int n, int method,
                                   const int *handles, int ndet, double epsilon, int step_mode, double *fisher,
                                   double *covariance, int *status) {
-  return gwf_moment_run(c, params, n, method, handles, ndet, epsilon, step_mode, fisher, covariance, status, true);
+  return gwf_moment_run(c, params, n, method, 2, handles, ndet, epsilon, step_mode, fisher, covariance, status, true);
 }

@@ -45,6 +45,7 @@ struct FisherSrc {
   int onesided[kIntr];  // pair q is a one-sided difference (eta at 1/4): its + waveform is the centre
   int exact[kIntr];     // pair q is taken as the difference of its two waveforms at every bin
   int n_cut_any;        // the last bin where any of the centre and the perturbed waveforms is non-zero
+  int needs_ref;        // five-point rule and a pair taken bin by bin: left to the reference algorithm
   int status;
 };
 // ----------------------------------------------------- pivoted Cholesky inverse
@@ -168,8 +169,8 @@ GW_HD void wave_diff(const WaveF64 &p, const WaveF64 &m, double sp, double sm, i
   for (int j = 0; j < 5; j++) d.ei[j] = (ep[j] * sp - em[j] * sm) * inv;
 }
 
-GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsilon, int step_mode, const SlotOut *S,
-                         FisherSrc &F) {
+GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsilon, int step_mode, int order,
+                         const SlotOut *S, FisherSrc &F) {
   fisher_unpack(in, method, F.v, F.logf);
   int st = 0;
   for (int s = 0; s < kSlots; s++) st |= S[s].status;
@@ -236,11 +237,51 @@ GW_HDNI int fisher_setup(const GenParams &in, int method, int ndet, double epsil
         br *= F.v[i];
         bi *= F.v[i];
       }
+      if (order == 4) {
+        // Five-point rule (fisher.cpp:426-458): the reference shifts t_c by
+        // the detector's arrival time at the +-2 eps steps instead of
+        // rotating by e^{-2 pi i DTOA f}, so those two responses carry the
+        // extra constant phase phq = -tau f_ref.  To second order in the step
+        // the five-point difference is then kappa r' + c r with
+        // kappa = (4 - e^{i phq}) / 3 and c = -(i/3) e^{i phq} d(phq)/d(theta)
+        // = (i/3) e^{i phq} f_ref dtau (the sky position only); kappa = 1 and
+        // c = 0 at the reference detector (tau = 0).  Here a' = kappa a + c G0
+        // and b' = kappa b; the intrinsic rows take kappa G0 below.
+        const double phq = -S[0].tau[d] * S[0].w.fref;
+        double sq, cq;
+        sincos(phq, &sq, &cq);
+        const double kr = (4.0 - cq) / 3.0, ki = -sq / 3.0;
+        double dt = i <= 3 ? (P.tau[d] - Mn.tau[d]) / dv : 0.0;
+        if (F.logf[i]) dt *= F.v[i];
+        const double cr = -sq * S[0].w.fref * dt / 3.0, ci = cq * S[0].w.fref * dt / 3.0;
+        const double ar2 = kr * ar - ki * ai + (cr * g0r - ci * g0i), ai2 = kr * ai + ki * ar + (cr * g0i + ci * g0r);
+        const double br2 = kr * br - ki * bi, bi2 = kr * bi + ki * br;
+        ar = ar2;
+        ai = ai2;
+        br = br2;
+        bi = bi2;
+      }
       F.ar[d][i] = ar;
       F.ai[d][i] = ai;
       F.br[d][i] = br;
       F.bi[d][i] = bi;
     }
+    if (order == 4) {  // the intrinsic derivatives: kappa G0 q
+      const double phq = -S[0].tau[d] * S[0].w.fref;
+      double sq, cq;
+      sincos(phq, &sq, &cq);
+      const double kr = (4.0 - cq) / 3.0, ki = -sq / 3.0;
+      F.G0re[d] = kr * g0r - ki * g0i;
+      F.G0im[d] = kr * g0i + ki * g0r;
+    }
+  }
+  // The five-point rule's +-2 eps waveforms are not among the slots: a pair
+  // that the moment form takes bin by bin (eta at 1/4, a waveform's cut inside
+  // the pair) is left to the reference algorithm.
+  F.needs_ref = 0;
+  if (order == 4) {
+    for (int q = 0; q < kIntr; q++)
+      if (F.onesided[q] || F.exact[q] || F.wp[q].n_cut != F.w0.n_cut || F.wm[q].n_cut != F.w0.n_cut) F.needs_ref = 1;
   }
   F.status = st;
   return st;

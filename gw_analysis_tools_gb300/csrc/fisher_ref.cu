@@ -332,12 +332,8 @@ int gwgpu_fisher_batch_ex(gwgpu_context *c, const gwgpu_gen_params *params, int 
   if (opt->order != 2 && opt->order != 4) return GWGPU_EINVAL;
   if (opt->precision != GWGPU_PREC_FP64 && opt->precision != GWGPU_PREC_MIXED) return GWGPU_EINVAL;
   if (opt->algorithm == GWGPU_FISHER_MOMENTS) {
-    if (opt->order != 2) {
-      c->last_error = "fisher_batch_ex: the moment form is the central (order 2) rule";
-      return GWGPU_EINVAL;
-    }
-    int st = gwf_moment_run(c, params, n, opt->method, handles, ndet, opt->epsilon, opt->step_mode, fisher, covariance,
-                            status, opt->precision == GWGPU_PREC_FP64);
+    int st = gwf_moment_run(c, params, n, opt->method, opt->order, handles, ndet, opt->epsilon, opt->step_mode, fisher,
+                            covariance, status, opt->precision == GWGPU_PREC_FP64);
     if (st || !opt->add_prior) return st;
     double prior[kDim];
     cudaMemcpyFromSymbol(prior, c_prior_diag, sizeof(prior));
@@ -380,16 +376,26 @@ int gwgpu_mcmc_fisher_batch(gwgpu_context *c, const double *theta, int dim, int 
   }
   std::vector<GenParams> hp(n);
   for (int i = 0; i < n; i++) mcmc_repack(theta + (size_t)i * dim, dim, kPhenomD, gmst, hp[i]);
-  std::lock_guard<std::mutex> lk(c->mu);
-  cudaSetDevice(c->device);
-  std::vector<int> ks(n);
   // MCMC_fisher_wrapper: fisher_numerical("MCMC_" + method, order mcmc_deriv_order = 4,
-  // epsilon 1e-8 absolute) summed over the detectors, plus the prior diagonal
-  int st = gwf_ref_run(c, hp.data(), n, GWGPU_FISHER_MCMC_IMRPHENOMD, 4, handles, ndet, 1e-8,
-                       GWGPU_FISHER_STEP_ABSOLUTE, 1, fisher, nullptr, ks.data());
+  // epsilon 1e-8 absolute) summed over the detectors, plus the prior diagonal.
+  // The moment form with FP64 sums at order 4 (the reference algorithm for the
+  // sources it leaves to it)
+  std::vector<int> ks(n);
+  static_assert(sizeof(GenParams) == sizeof(gwgpu_gen_params), "one parameter layout");
+  int st = gwf_moment_run(c, (const gwgpu_gen_params *)hp.data(), n, GWGPU_FISHER_MCMC_IMRPHENOMD, 4, handles, ndet,
+                          1e-8, GWGPU_FISHER_STEP_ABSOLUTE, fisher, nullptr, ks.data(), true);
   if (st) return st;
+  double prior[kDim];
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaMemcpyFromSymbol(prior, c_prior_diag, sizeof(prior));
+    if (e != cudaSuccess) return c->fail(e, "prior diagonal");
+  }
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < kDim; k++) fisher[(size_t)i * kDim * kDim + k * kDim + k] += prior[k];
   if (status)
-    for (int i = 0; i < n; i++) status[i] = fisher_status_code(ks[i]);
+    for (int i = 0; i < n; i++) status[i] = ks[i];
   return GWGPU_OK;
 }
 

@@ -14,8 +14,12 @@
 int gwf_ref_run(gwgpu_context *c, const gwt::GenParams *params, int n, int method, int order, const int *handles,
                 int ndet, double epsilon, int step_mode, int add_prior, double *fisher, double *cov, int *kstatus);
 
-// The moment form (fisher.cu) for n sources; acc64: FP64 per-bin differences,
-// weights and sums instead of FP32 values in compensated FP32 sums.  Takes the
-// context lock.  Sources it cannot invert are redone by gwf_ref_run.
-int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int method, const int *handles, int ndet,
-                   double epsilon, int step_mode, double *fisher, double *covariance, int *status, bool acc64);
+// The moment form (fisher.cu) for n sources, order 2 or 4 (the five-point
+// rule, with the reference's constant phase on the +-2 eps responses of a
+// non-reference detector); acc64: FP64 per-bin differences, weights and sums
+// instead of FP32 values in compensated FP32 sums.  Takes the context lock.
+// Sources it cannot invert, and five-point sources with a pair taken bin by
+// bin, are redone by gwf_ref_run.
+int gwf_moment_run(gwgpu_context *c, const gwgpu_gen_params *params, int n, int method, int order, const int *handles,
+                   int ndet, double epsilon, int step_mode, double *fisher, double *covariance, int *status,
+                   bool acc64);

@@ -460,7 +460,7 @@ class Context:
         """fisher_numerical for many sources summed over the detectors of
         handles (the first is the reference detector): FISHER_REFERENCE runs
         the reference algorithm in FP64 (orders 2 and 4), FISHER_MOMENTS the
-        moment form (order 2) with FP64 (PREC_FP64) or compensated FP32
+        moment form (orders 2 and 4) with FP64 (PREC_FP64) or compensated FP32
         (PREC_MIXED) sums."""
         parr = params if isinstance(params, ctypes.Array) else params_array(params)
         n = len(parr)

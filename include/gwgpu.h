@@ -313,7 +313,7 @@ int gwgpu_fisher_batch(gwgpu_context *ctx, const gwgpu_gen_params *params, int n
 #define GWGPU_FISHER_MOMENTS 1     /* order 2: analytic extrinsic derivatives, per-bin waveform differences, moment sums */
 typedef struct {
   int method;     /* GWGPU_FISHER_IMRPHENOMD or GWGPU_FISHER_MCMC_IMRPHENOMD */
-  int order;      /* 2 (central) or 4 (five-point, fisher.cpp:426-458; always GWGPU_FISHER_REFERENCE) */
+  int order;      /* 2 (central) or 4 (five-point, fisher.cpp:426-458) */
   double epsilon; /* step (the reference: 1e-8) */
   int step_mode;  /* GWGPU_FISHER_STEP_* */
   int precision;  /* GWGPU_PREC_FP64; the moment form also takes GWGPU_PREC_MIXED (FP32 values, compensated FP32 sums) */
@@ -327,7 +327,12 @@ typedef struct {
  * responses of the five-point rule carry at a non-reference detector,
  * fisher.cpp:426-458), derivatives and Simpson Gram sums in FP64.
  * GWGPU_FISHER_MOMENTS is the form of gwgpu_fisher_batch, its sums in the
- * given precision. */
+ * given precision; at order 4 it takes the five-point rule with that constant
+ * phase analytically (each derivative at a non-reference detector becomes
+ * kappa r' + c r, kappa = (4 - e^{i phq}) / 3, phq = 2 pi DTOA f_ref, c from
+ * the sky position's change of phq), and a source with a pair it takes bin by
+ * bin (eta at 1/4, a waveform's cut between the steps) is computed with the
+ * reference algorithm. */
 int gwgpu_fisher_batch_ex(gwgpu_context *ctx, const gwgpu_gen_params *params, int n, const int *handles,
                           int num_detectors, const gwgpu_fisher_options *options, double *fisher, double *covariance,
                           int *status);
@@ -337,7 +342,9 @@ int gwgpu_fisher_batch_ex(gwgpu_context *ctx, const gwgpu_gen_params *params, in
  * the given GMST), fisher_numerical("MCMC_IMRPhenomD", order 4 =
  * mcmc_deriv_order, mcmc_gw.h:45, epsilon 1e-8) summed over the detectors with
  * the first as reference, plus the prior diagonal of
- * MCMC_fisher_transformations.  fisher[n][11][11]; status as above. */
+ * MCMC_fisher_transformations, in the moment form with FP64 sums at order 4
+ * (gwgpu_fisher_batch_ex, GWGPU_FISHER_MOMENTS).  fisher[n][11][11]; status
+ * as above. */
 int gwgpu_mcmc_fisher_batch(gwgpu_context *ctx, const double *theta, int dim, int n, int approximant, double gmst,
                             const int *handles, int num_detectors, double *fisher, int *status);
 

@@ -204,7 +204,7 @@ extern "C" int gwh_fisher_batch(const GenParams *p, int method, const double *fr
   std::vector<SlotOut> slots(kSlots);
   for (int s = 0; s < kSlots; s++) fisher_slot(*p, s, method, dets, ndet, df, epsilon, step_mode, qnm(), slots[s]);
   FisherSrc F;
-  int st = fisher_setup(*p, method, ndet, epsilon, step_mode, slots.data(), F);
+  int st = fisher_setup(*p, method, ndet, epsilon, step_mode, 2, slots.data(), F);
   if (st) return st;
   double sdf = freqs[N / 2] - freqs[N / 2 - 1];
   std::vector<double> Ssum(kMaxDet * kSums, 0.0);
@@ -250,7 +250,7 @@ extern "C" int gwh_fisher_pair_check(const GenParams *p, int method, double df, 
   std::vector<SlotOut> slots(kSlots);
   for (int s = 0; s < kSlots; s++) fisher_slot(*p, s, method, dets, 1, df, epsilon, step_mode, qnm(), slots[s]);
   FisherSrc F;
-  int st = fisher_setup(*p, method, 1, epsilon, step_mode, slots.data(), F);
+  int st = fisher_setup(*p, method, 1, epsilon, step_mode, 2, slots.data(), F);
   if (st) return st;
   double emax[kIntr] = {0, 0, 0, 0}, qmax[kIntr] = {0, 0, 0, 0};
   for (int k = 0; k < N; k++) {

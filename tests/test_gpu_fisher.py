@@ -100,7 +100,7 @@ def test_fisher_batch_ex_rejects_bad_options(gpu_ctx):
     f = W.uniform_grid(10.0, 512.0, 1 / 4.)
     h = gpu_ctx.register_data("Hanford", f, np.zeros(f.size, complex), W.analytic_psd(f))
     p = G.params_array(W.prior_draws(1, 86))
-    for kw in (dict(order=4, algorithm=G.FISHER_MOMENTS), dict(precision=G.PREC_MIXED),
+    for kw in (dict(order=3, algorithm=G.FISHER_MOMENTS), dict(precision=G.PREC_MIXED),
                dict(algorithm=7), dict(order=3)):
         with pytest.raises(G.GwGpuError):
             gpu_ctx.fisher_batch_ex(p, 0, [h], **kw)
@@ -182,5 +182,36 @@ def test_mcmc_fisher_proposal_golden(gpu_ctx):
     assert np.all(st == 0)
     for got, want in zip(fish, g["wrapper_fisher_d"]):
         assert _norm_err(got, want) <= 1e-4
+    for h in hs:
+        gpu_ctx.release_data(h)
+
+
+@pytest.mark.parametrize("method,name", [(0, "IMRPhenomD"), (1, "MCMC_IMRPhenomD")])
+def test_moment_form_five_point(gpu_ctx, oracle, method, name):
+    """The moment form at order 4 (gwgpu_fisher_batch_ex, FISHER_MOMENTS):
+    the five-point rule with the reference's constant phase on the +-2 eps
+    responses of the non-reference detectors (fisher.cpp:426-458), taken
+    analytically, against the oracle's network Fisher at order 4; among the
+    sources, one within 1000 steps of eta = 1/4 (left to the reference
+    algorithm).  Both step rules."""
+    f = W.uniform_grid(10.0, 1024.0, 1 / 8.)
+    dets = list(W.DETECTORS3)
+    psd = W.analytic_psd(f)
+    hs = [gpu_ctx.register_data(d, f, np.zeros(f.size, complex), psd) for d in dets]
+    draws = W.prior_draws(10, 87) + [dict(W.prior_draws(1, 88)[0], mass1=30.0, mass2=30.0 * (1 - 1e-5))]
+    for eps, mode, tol in ((1e-6, 1, 1e-4), (1e-8, 0, 3e-4)):
+        fish, cov, st = gpu_ctx.fisher_batch_ex(G.params_array(draws), method, hs, order=4, epsilon=eps,
+                                                step_mode=mode, precision=G.PREC_FP64, algorithm=G.FISHER_MOMENTS)
+        for i, d in enumerate(draws):
+            ref = oracle.fisher_network(f, oracle.params_from_dict(d), dets, [psd] * 3, method=name, order=4,
+                                        epsilon=eps, step_mode=mode)
+            # the FP64 rounding of the reference's own differences, divided by
+            # the step, against the analytic form
+            assert _norm_err(fish[i], ref) <= tol, (name, eps, i, _norm_err(fish[i], ref))
+            ist, _ = oracle.cholesky_invert(ref)
+            if ist != 0:
+                assert st[i] in (0, 9)
+            else:
+                assert st[i] == 0, (i, st[i])
     for h in hs:
         gpu_ctx.release_data(h)
