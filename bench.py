@@ -508,6 +508,8 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         t0 = time.perf_counter()
         ctx.mcmc_fisher_batch(theta, hf, W.GMST)
         ex["fisher"]["mcmc_proposal_per_s"] = nr / (time.perf_counter() - t0)
+        ex["fisher"]["mcmc_proposal_form"] = ("moment form at order 4 (five-point rule with the reference's constant "
+                                              "phase), epsilon 1e-8 absolute, prior diagonal")
         ns = 64  # parity sample: the moment form and the reference algorithm against the oracle
         fr, cr, _ = ctx.fisher_batch_ex(G.params_array(W.prior_draws(ns, 13)), 0, hf, order=2, epsilon=1e-6,
                                         step_mode=1)
