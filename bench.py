@@ -515,6 +515,10 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
                                         step_mode=1)
         ex["_fisher_sample"] = (pf, fish[:ns].copy(), cov[:ns].copy(), fr, cr, ff, psd_f, f32[:ns].copy(),
                                 c32[:ns].copy())
+        # the five-point rule in the moment form, on 16 of them
+        f4, _, _ = ctx.fisher_batch_ex(G.params_array(W.prior_draws(16, 13)), 0, hf, order=4, epsilon=1e-6,
+                                       step_mode=1, algorithm=G.FISHER_MOMENTS)
+        ex["_fisher_sample4"] = (W.prior_draws(16, 13), f4, ff, psd_f)
 
     def maximized():
         # the sampler's intrinsic mode: likelihood maximised over t_c and phi_c
@@ -709,6 +713,21 @@ def fisher_err(sample):
             "median_condition_number": float(np.median(conds)), "max_condition_number": max(conds)}
 
 
+def fisher_err4(sample):
+    """The moment form at order 4 against the oracle's five-point network
+    Fisher (with the reference's constant phase on the +-2 eps responses)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from gw_analysis_tools_gb300 import workloads as W
+    draws, f4, ff, psd = sample
+    errs = []
+    for i, d in enumerate(draws):
+        ref = O.fisher_network(ff, O.params_from_dict(d), list(W.DETECTORS3), [psd] * 3, order=4, epsilon=1e-6,
+                               step_mode=1)
+        errs.append(float(np.max(np.abs(f4[i] - ref) / np.sqrt(np.abs(np.outer(np.diag(ref), np.diag(ref)))))))
+    return {"sources": len(draws), "max_normalized_err": max(errs), "median_normalized_err": float(np.median(errs))}
+
+
 def parity_stats(got, ref, tol, rel=False):
     err = np.abs(np.asarray(got) - np.asarray(ref))
     if rel:
@@ -884,6 +903,8 @@ def main():
     fp64_peak = measure_peak("float64")
     ex = res.get("extras", {})
     fisher_parity = fisher_err(ex.pop("_fisher_sample")) if "_fisher_sample" in ex else None
+    if fisher_parity is not None and "_fisher_sample4" in ex:
+        fisher_parity["moment_order4"] = fisher_err4(ex.pop("_fisher_sample4"))
     log("secondary parity")
     sec_parity = secondary_parity(ex, res)
     line = {
