@@ -196,16 +196,20 @@ void gwh_segment_stats(long *poly, long *total, int reset) {
 
 #include "../../gw_analysis_tools_gb300/csrc/fisher_math.h"
 
-extern "C" int gwh_fisher_batch(const GenParams *p, int method, const double *freqs, int N, int ndet, const int *dets,
-                                const double *const *psd, double epsilon, int step_mode, double *out, double *cov) {
+// The moment form on the host at order 2 or 4; returns 10 for a five-point
+// source the product leaves to the reference algorithm.
+extern "C" int gwh_fisher_batch_order(const GenParams *p, int method, int order, const double *freqs, int N, int ndet,
+                                      const int *dets, const double *const *psd, double epsilon, int step_mode,
+                                      double *out, double *cov) {
   using namespace gwf;
   double df = freqs[1] - freqs[0];
   int n0 = (int)std::llround(freqs[0] / df);
   std::vector<SlotOut> slots(kSlots);
   for (int s = 0; s < kSlots; s++) fisher_slot(*p, s, method, dets, ndet, df, epsilon, step_mode, qnm(), slots[s]);
   FisherSrc F;
-  int st = fisher_setup(*p, method, ndet, epsilon, step_mode, 2, slots.data(), F);
+  int st = fisher_setup(*p, method, ndet, epsilon, step_mode, order, slots.data(), F);
   if (st) return st;
+  if (F.needs_ref) return 10;
   double sdf = freqs[N / 2] - freqs[N / 2 - 1];
   std::vector<double> Ssum(kMaxDet * kSums, 0.0);
   std::vector<int> wslot(ndet);
@@ -236,6 +240,10 @@ extern "C" int gwh_fisher_batch(const GenParams *p, int method, const double *fr
   fisher_assemble(F, Ssum.data(), ndet, wslot.data(), wscale.data(), df / sdf, out);
   if (cov) return chol_invert(out, cov, kDim) ? 9 : 0;
   return 0;
+}
+extern "C" int gwh_fisher_batch(const GenParams *p, int method, const double *freqs, int N, int ndet, const int *dets,
+                                const double *const *psd, double epsilon, int step_mode, double *out, double *cov) {
+  return gwh_fisher_batch_order(p, method, 2, freqs, N, ndet, dets, psd, epsilon, step_mode, out, cov);
 }
 
 // Each intrinsic pair's per-bin complex difference as fisher_bin_q forms it

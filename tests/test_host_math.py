@@ -116,6 +116,39 @@ def test_host_batched_fisher_algebra_matches_oracle(oracle, hostcheck):
             assert rel.max() <= tol, (eps, rel.max())
 
 
+def test_host_five_point_moment_form_matches_oracle(oracle, hostcheck):
+    """The moment form at order 4 on the host (the product's fisher_setup
+    with the five-point coefficients kappa a + c G, kappa b, kappa G) against
+    the oracle's order-4 network Fisher, which evaluates the +-2 eps responses
+    with the reference's constant phase at the non-reference detectors;
+    both parameterisations and both step rules."""
+    dp = ctypes.POINTER(ctypes.c_double)
+    fn = hostcheck.gwh_fisher_batch_order
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                   ctypes.c_void_p, ctypes.c_double, ctypes.c_int, dp, dp]
+    f = W.uniform_grid(10.0, 512.0, 1 / 8.)
+    dets = list(W.DETECTORS3)
+    psd = [W.analytic_psd(f)] * 3
+    idx = (ctypes.c_int * 3)(*[oracle.detector_index(d) for d in dets])
+    checked = 0
+    for method, name in ((0, "IMRPhenomD"), (1, "MCMC_IMRPhenomD")):
+        for eps, mode, tol in ((1e-6, 1, 2e-5), (1e-8, 0, 1e-3)):
+            for d in W.prior_draws(3, 79):
+                p = oracle.params_from_dict(d)
+                out = np.zeros(121)
+                st = fn(ctypes.byref(p), method, 4, oracle._dp(f), f.size, 3, idx, oracle._ptr_array(psd), eps, mode,
+                        oracle._dp(out), None)
+                if st == 10:  # left to the reference algorithm
+                    continue
+                assert st == 0
+                ref = oracle.fisher_network(f, p, dets, psd, method=name, order=4, epsilon=eps, step_mode=mode)
+                G = out.reshape(11, 11)
+                rel = np.abs(G - ref) / np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
+                assert rel.max() <= tol, (name, eps, rel.max())
+                checked += 1
+    assert checked >= 10
+
+
 def test_fisher_pair_differences_every_bin(hostcheck):
     """The batched Fisher's per-bin intrinsic differences (the
     coefficient-difference polynomials, fisher_phase_deriv / fisher_amp_deriv
