@@ -306,8 +306,9 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 // sub-partitions at once shortens that chain.  Lane j of every warp works on
 // request blockIdx.x * kCoopReq + j; shared memory holds the requests between
 // stages.  Stage plan (W0..W3 = warps):
-//   S0  W0 parameters, source;  W1/W2 detector projections, W2 inclination factors;
-//       W3 chirp mass and amplitude normalisation
+//   S0  W0 parameters, source;  W1/W2 detector projections (a detector per half-warp),
+//       W1 D final spin and radiated energy, W2 inclination factors;  W3 chirp mass and
+//       amplitude normalisation
 //   S1  W0/W3 calibration fits;  W1 D: ringdown frequencies / Pv2: J-frame transform;  W2 PN coefficients
 //   S2  W0 Pv2: ringdown frequencies; matching frequencies;  W1 D: phase at f_ref (inspiral);
 //       W2 D: ringdown-phase terms at f3
@@ -407,16 +408,13 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     r.approximant = ap;
     r.ndet = ndet;
     if (!bad) populate_core(r.m.s, q);
-    if (!bad && ap == kPhenomD && !r.m.s.dep_postmerger) {
-      s_pm[lane][0] = final_spin(r.m.s);
-      s_pm[lane][1] = EradRational0815(r.m.s.eta, r.m.s.spin1z, r.m.s.spin2z);
-    }
   }
   if (act && warp == 3) populate_amp(r.m.s, params[i]);
-  if (warp == 1 || warp == 2) {  // projections need only the sky position: detectors over warps 1, 2
+  if (warp == 1 || warp == 2) {  // projections need only the sky position: detectors over the half-warps of warps 1, 2
     // sky_trig with the hour angle's sincos on lanes j and the declination's
     // on lanes j + kCoopReq at once
-    const GenParams &q = params[min(blockIdx.x * kCoopReq + hl, n - 1)];
+    const int ih = blockIdx.x * kCoopReq + hl;
+    const GenParams &q = params[min(ih, n - 1)];
     double s1, c1, sps, cps;
     sincos(lane < kCoopReq ? q.gmst - q.RA : q.DEC, &s1, &c1);
     sincos(q.psi, &sps, &cps);
@@ -427,17 +425,29 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     tr.cd = __shfl_sync(0xffffffffu, c1, hl + kCoopReq);
     tr.sp = sps;
     tr.cp = cps;
-    if (act) {
-      if (warp == 2) populate_incl(r.m.s, q);
-      const int d0 = streams[handles[i * ndet]].det;
-      for (int d = warp - 1; d < ndet && d < kMaxDet; d += 2) {
-        const StreamDev &sd = streams[handles[i * ndet + d]];
+    if (hact) {  // request hl: warp 1 detectors 0, 2 (+4k), warp 2 detectors 1, 3, half-warp by half-warp
+      Request &rh = s_r[hl];
+      if (warp == 2 && lane < kCoopReq) populate_incl(rh.m.s, q);
+      const int d0 = streams[handles[ih * ndet]].det;
+      for (int d = (warp - 1) + (lane >= kCoopReq ? 2 : 0); d < ndet && d < kMaxDet; d += 4) {
+        const StreamDev &sd = streams[handles[ih * ndet + d]];
         const int dd = sd.det;
-        s_ds[lane][d] = sd.dscale;
-        s_ws[lane][d] = sd.wscale;
-        s_wk[lane][d] = sd.wkey;
-        antenna_trig(dd, tr, r.det[d].fp, r.det[d].fc);
-        r.det[d].tau = -dtoa_trig(tr, d0, dd) * (2 * kPi);
+        s_ds[hl][d] = sd.dscale;
+        s_ws[hl][d] = sd.wscale;
+        s_wk[hl][d] = sd.wkey;
+        antenna_trig(dd, tr, rh.det[d].fp, rh.det[d].fc);
+        rh.det[d].tau = -dtoa_trig(tr, d0, dd) * (2 * kPi);
+      }
+      // D: the final spin and radiated energy for S1 from the parameters (eta
+      // formed as populate_core forms it), on the lower half of warp 1
+      if (warp == 1 && lane < kCoopReq) {
+        const int ap = approx[ih];
+        const bool bad = !(q.mass1 > 0) || !(q.mass2 > 0) || !(q.Luminosity_Distance > 0) || (ap != 0 && ap != 1);
+        if (!bad && ap == kPhenomD && !q.dep_postmerger) {
+          const double eta = calc_eta(q.mass1 * kMsolSec, q.mass2 * kMsolSec);
+          s_pm[hl][0] = FinalSpin0815(eta, q.spin1[2], q.spin2[2]);
+          s_pm[hl][1] = EradRational0815(eta, q.spin1[2], q.spin2[2]);
+        }
       }
     }
   }
