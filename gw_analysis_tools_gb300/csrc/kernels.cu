@@ -307,9 +307,9 @@ __global__ void k_prologue(const GenParams *__restrict__ params, const int *__re
 // request blockIdx.x * kCoopReq + j; shared memory holds the requests between
 // stages.  Stage plan (W0..W3 = warps):
 //   S0  W0 parameters, source;  W1/W2 detector projections (a detector per half-warp),
-//       W1 D final spin and radiated energy, W2 inclination factors;  W3 chirp mass and
-//       amplitude normalisation
-//   S1  W0/W3 calibration fits;  W1 D: ringdown frequencies / Pv2: J-frame transform;  W2 PN coefficients
+//       W2 inclination factors;  W3 chirp mass and amplitude normalisation
+//   S1  W0/W3 calibration fits;  W1 D: final spin, radiated energy, ringdown frequencies /
+//       Pv2: J-frame transform;  W2 PN coefficients
 //   S2  W0 Pv2: ringdown frequencies; matching frequencies;  W1 D: phase at f_ref (inspiral);
 //       W2 D: ringdown-phase terms at f3
 //   S3  W0/W1 amplitude matching points;  D: phase connection in four pieces after them
@@ -378,7 +378,6 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   __shared__ double s_shift[kCoopReq][kPv2ShiftNodes];
   __shared__ double s_df[kCoopReq];
   __shared__ int s_st[kCoopReq], s_bad[kCoopReq], s_uni[kCoopReq];
-  __shared__ double s_pm[kCoopReq][2];  // D: final spin and radiated energy, for post_merger in S1
   static_assert(2 * kCoopReq == 32, "two half-warps per warp share the block's requests");
   grid_dep_trigger();  // the bin kernel may launch and wait for this grid
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -438,17 +437,6 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
         antenna_trig(dd, tr, rh.det[d].fp, rh.det[d].fc);
         rh.det[d].tau = -dtoa_trig(tr, d0, dd) * (2 * kPi);
       }
-      // D: the final spin and radiated energy for S1 from the parameters (eta
-      // formed as populate_core forms it), on the lower half of warp 1
-      if (warp == 1 && lane < kCoopReq) {
-        const int ap = approx[ih];
-        const bool bad = !(q.mass1 > 0) || !(q.mass2 > 0) || !(q.Luminosity_Distance > 0) || (ap != 0 && ap != 1);
-        if (!bad && ap == kPhenomD && !q.dep_postmerger) {
-          const double eta = calc_eta(q.mass1 * kMsolSec, q.mass2 * kMsolSec);
-          s_pm[hl][0] = FinalSpin0815(eta, q.spin1[2], q.spin2[2]);
-          s_pm[hl][1] = EradRational0815(eta, q.spin1[2], q.spin2[2]);
-        }
-      }
     }
   }
   __syncthreads();
@@ -461,7 +449,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     if (warp == 1) {
       if (pv2) model_p_setup(r.m, r.p, p);
       else if (r.m.s.dep_postmerger) post_merger(r.m.s, qnm);
-      else post_merger_qnm(r.m.s, qnm, s_pm[lane][0], s_pm[lane][1]);
+      else post_merger_qnm(r.m.s, qnm, final_spin(r.m.s), EradRational0815(r.m.s.eta, r.m.s.spin1z, r.m.s.spin2z));
     }
     if (warp == 2) model_d_pn(r.m);
   }
