@@ -324,7 +324,6 @@ int gwgpu_fisher_numerical(gwgpu_context *c, const double *freqs, int N, const c
   FDReq *h;
   st = c->pinned(gwgpu_context::kHwsFisher, sizeof(FDReq) * dim, (void **)&h);
   if (st) return st;
-  int dets[2] = {det, ref};
   for (int i = 0; i < dim; i++) {
     double eps = epsilon, pv[kDim];
     GenParams q;
@@ -352,7 +351,6 @@ int gwgpu_fisher_numerical(gwgpu_context *c, const double *freqs, int N, const c
       if (ref != det) q.tc -= dtoa(q.RA, q.DEC, q.gmst, ref, det);
       request_prologue(h[i].rmm, q, kPhenomD, dd, 1, c->qnm_host.data());
     }
-    (void)dets;
     double divisor = order >= 4 ? d4 : div;
     double logscale = logf[i] ? v[i] : 1.0;
     cudaMemcpyAsync(dreq, &h[i], sizeof(FDReq), cudaMemcpyHostToDevice, c->stream);

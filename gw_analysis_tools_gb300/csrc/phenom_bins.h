@@ -26,7 +26,7 @@ GW_HD double build_phase_bin(double f, const ModelD &m, const Pows &p) {
   const Source &s = m.s;
   if (f < s.f1_phase) {
     const double *pn = m.pn_phase;
-    double M = s.M, eta = s.eta;
+    double M = s.M;
     double logF = log(kPi * (s.mass1 + s.mass2) * f);
     double c5 = pn[8] + logF * pn[9];
     double c6 = pn[10] - pn[11] * (logF);

@@ -114,7 +114,7 @@ GW_HD int grid_first(double fb, double df, bool strict) {
 GW_HDNI void wave64_prologue(const Request &r, double df, WaveF64 &x) {
   const ModelD &m = r.m;
   const Source &s = m.s;
-  const double M = s.M, eta = s.eta, Mdf = M * df;
+  const double M = s.M, Mdf = M * df;
   x.n_f1 = grid_first(s.f1, df, false);          // amp: f < f1 inspiral
   x.n_f1p = grid_first(s.f1_phase, df, false);   // phase: f < f1_phase inspiral
   x.n_f3 = grid_first(s.f3, df, true);           // amp: f > f3 ringdown

@@ -475,7 +475,7 @@ GW_HD double amp_ins(double f, const ModelD &m, const Pows &p) {  // IMRPhenomD.
 }
 GW_HD double phase_ins(double f, const Source &s, double *pn, const Lambda &l, const Pows &pi, const Pows &p) {
   // IMRPhenomD.cpp:1365-1399
-  double M = s.M, eta = s.eta;
+  double M = s.M;
   pn_phase_coeff_nonstatic(s, pn, f);
   double pn_phase = pn[0] + pn[1] * pi.PIthird * p.MFthird + pn[2] * pi.PI2third * p.MF2third + pn[3] * kPi * M * f +
                     pn[4] * pi.PI4third * p.MF4third + pn[5] * pi.PI5third * p.MF5third +
@@ -492,7 +492,7 @@ GW_HD double amp_mr(double f, const Source &s, const Lambda &l) {  // IMRPhenomD
   return numerator / denominator;
 }
 GW_HD double phase_mr(double f, const Source &s, const Lambda &l) {  // IMRPhenomD.cpp:1485-1503
-  double M = s.M, eta = s.eta, Mf = M * f, Mfcube = Mf * Mf * Mf, Mf3fourths = sqrt(sqrt(Mfcube));
+  double M = s.M, Mf = M * f, Mfcube = Mf * Mf * Mf, Mf3fourths = sqrt(sqrt(Mfcube));
   return s.inv_eta * (l.alpha[0] + l.alpha[1] * (Mf)-l.alpha[2] * (1. / (Mf)) + (4. / 3) * l.alpha[3] * Mf3fourths +
                        l.alpha[4] * atan((f - l.alpha[5] * s.fRD) / s.fdamp));
 }

@@ -492,9 +492,8 @@ GW_HDNI void pv2_transform(Source &s, int reduced) {
 }
 
 GW_HDNI void pv2_euler_coeffs(double *a, double *e, const Source &s) {  // IMRPhenomP.cpp:65-144
-  double m2 = s.q / (1. + s.q), m1 = 1. / (1. + s.q), dm = m1 - m2, mtot = 1.;
-  double eta = m1 * m2, eta2 = eta * eta, eta3 = eta2 * eta, eta4 = eta3 * eta;
-  double mtot2 = mtot * mtot, mtot4 = mtot2 * mtot2, mtot6 = mtot4 * mtot2, mtot8 = mtot6 * mtot2;
+  double m2 = s.q / (1. + s.q), m1 = 1. / (1. + s.q), dm = m1 - m2;
+  double eta = m1 * m2, eta2 = eta * eta;
   double chil = s.chil, chil2 = chil * chil, chip2 = s.chip * s.chip, chip4 = chip2 * chip2;
   double dm2 = dm * dm, dm3 = dm2 * dm;
   double m2_2 = m2 * m2, m2_3 = m2_2 * m2, m2_4 = m2_3 * m2, m2_5 = m2_4 * m2, m2_6 = m2_5 * m2, m2_7 = m2_6 * m2,
@@ -503,9 +502,6 @@ GW_HDNI void pv2_euler_coeffs(double *a, double *e, const Source &s) {  // IMRPh
   // constant denominators folded
   const double im2 = 1. / m2, ieta = 1. / eta;
   const double im2_2 = im2 * im2, im2_3 = im2_2 * im2, ieta2 = ieta * ieta, ieta3 = ieta2 * ieta, ieta4 = ieta3 * ieta;
-  (void)mtot4;
-  (void)mtot6;
-  (void)mtot8;
   a[0] = (-0.18229166666666666 - ((5 * dm) * (1. / 64.) * im2));
   a[1] = (((-15 * dm * m2 * chil) * (1. / 128.) * ieta) - ((35 * m2_2 * chil) * (1. / 128.) * ieta));
   a[2] = (-1.7952473958333333 - ((4555 * dm) * (1. / 7168.) * im2) - ((15 * chip2 * dm * m2_3) * (1. / 128.) * ieta2) -
