@@ -17,9 +17,11 @@ A step is one pass of the hot path over one batch of 512 requests.
           flushed before every step.
 
 Beside them: the plain FP64 one-request-per-launch form, the batched FP64
-form, the served form (Poisson arrivals, mixed D/Pv2, p50/p99), the uneven
-Pv2 batch and the batched Fisher, a roofline of the fused bin kernel, and
-the CPU oracle timed on the host cores.
+form, the served form (the device-resident request loop under Poisson
+arrivals, mixed D/Pv2, p50/p99, saturation and latency against offered load,
+with the host scheduler's numbers beside it), the uneven Pv2 batch and the
+batched Fisher, a roofline of the fused bin kernel, and the CPU oracle timed
+on the host cores.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -382,19 +384,7 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
                 sp.append(dp[i // 2])
                 sa.append(1)
         arrivals = np.cumsum(rng.exponential(1.0 / 2e5, nserve))
-        srv = G.Server(ctx, T, max_inflight=16384, max_batch=1024, lanes=4, hbm_budget=120 * 1024 ** 3)
-        try:
-            srv.drive(G.params_array(sp[:2000]), sa[:2000], handles, arrivals[:2000] - arrivals[0])  # warm-up
-            srv.reset_stats()
-            out, st, lat, wall = srv.drive(G.params_array(sp), sa, handles, arrivals - arrivals[0])
-            s = srv.stats()
-        finally:
-            srv.close()
-        ex["served"] = {"evals_per_s": nserve / wall, "p50_ms": s["p50_s"] * 1e3, "p99_ms": s["p99_s"] * 1e3,
-                        "offered_rate": 2e5, "requests": nserve, "launches": s["launches"], "ensembles": ens,
-                        "ok": int((st == 0).sum())}
         pick = np.arange(0, nserve, 29)  # a parity sample, both approximants
-        ex["_parity_served"] = ([sp[i] for i in pick], [sa[i] for i in pick], out[pick].copy())
         # the same mix offered faster than the engine serves it: its capacity
         nsat = 200000
         ds = W.prior_draws(nsat // 2, 503)
@@ -402,23 +392,24 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         sp2 = [ds[i // 2] if i % 2 == 0 else dq[i // 2] for i in range(nsat)]
         sa2 = [i % 2 for i in range(nsat)]
         arr2 = np.cumsum(rng.exponential(1.0 / 5e6, nsat))
-        srv = G.Server(ctx, T, max_inflight=65536, max_batch=4096, lanes=4, hbm_budget=120 * 1024 ** 3)
-        try:
-            srv.drive(G.params_array(sp2[:8192]), sa2[:8192], handles, arr2[:8192] - arr2[0])  # warm-up
+
+        def run(srv):
+            """2e5/s, saturation (5e6/s offered) and latency against offered load."""
+            srv.drive(G.params_array(sp[:2000]), sa[:2000], handles, arrivals[:2000] - arrivals[0])  # warm-up
             srv.reset_stats()
-            out, st, lat, wall = srv.drive(G.params_array(sp2), sa2, handles, arr2 - arr2[0])
+            out, st, lat, wall = srv.drive(G.params_array(sp), sa, handles, arrivals - arrivals[0])
             s = srv.stats()
-        finally:
-            srv.close()
-        ex["served"]["saturated"] = {"evals_per_s": nsat / wall, "p50_ms": s["p50_s"] * 1e3,
-                                     "p99_ms": s["p99_s"] * 1e3, "offered_rate": 5e6, "requests": nsat,
-                                     "max_batch": 4096, "launches": s["launches"], "ok": int((st == 0).sum())}
-        # latency against offered load: the same mix, one server configuration
-        curve = []
-        srv = G.Server(ctx, T, max_inflight=65536, max_batch=2048, lanes=4, hbm_budget=120 * 1024 ** 3)
-        try:
-            srv.drive(G.params_array(sp2[:4096]), sa2[:4096], handles, arr2[:4096] - arr2[0])  # warm-up
-            for rate in (2e5, 5e5, 1e6, 2e6, 3e6):
+            r = {"evals_per_s": nserve / wall, "p50_ms": s["p50_s"] * 1e3, "p99_ms": s["p99_s"] * 1e3,
+                 "offered_rate": 2e5, "requests": nserve, "launches": s["launches"], "ok": int((st == 0).sum())}
+            got = out[pick].copy()
+            srv.reset_stats()
+            _, st2, _, wall2 = srv.drive(G.params_array(sp2), sa2, handles, arr2 - arr2[0])
+            s2 = srv.stats()
+            r["saturated"] = {"evals_per_s": nsat / wall2, "p50_ms": s2["p50_s"] * 1e3, "p99_ms": s2["p99_s"] * 1e3,
+                              "offered_rate": 5e6, "requests": nsat, "launches": s2["launches"],
+                              "ok": int((st2 == 0).sum())}
+            curve = []
+            for rate in (5e5, 1e6, 2e6, 3e6):
                 nr = int(min(100000, max(20000, rate * 0.05)))
                 arr3 = np.cumsum(np.random.default_rng(int(rate)).exponential(1.0 / rate, nr))
                 srv.reset_stats()
@@ -427,9 +418,29 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
                 curve.append({"offered_rate": rate, "evals_per_s": nr / wall3, "p50_ms": s3["p50_s"] * 1e3,
                               "p99_ms": s3["p99_s"] * 1e3, "requests": nr, "launches": s3["launches"],
                               "ok": int((st3 == 0).sum())})
+            r["load_curve"] = curve
+            return r, got
+
+        # the device-resident request loop (the served form)
+        srv = G.Server(ctx, T, max_inflight=65536, device_loop=True, hbm_budget=120 * 1024 ** 3)
+        try:
+            r, got = run(srv)
+            li = srv.loop_info()
         finally:
             srv.close()
-        ex["served"]["load_curve"] = {"max_batch": 2048, "lanes": 4, "points": curve}
+        r.update({"form": "device-resident request loop", "ensembles": ens,
+                  "loop": {k: li[k] for k in ("ring_slots", "tile", "max_items", "blocks", "launches")}})
+        ex["served"] = r
+        ex["_parity_served"] = ([sp[i] for i in pick], [sa[i] for i in pick], got)
+        # the host scheduler: fused batches on 4 stream lanes
+        srv = G.Server(ctx, T, max_inflight=65536, max_batch=2048, lanes=4, hbm_budget=120 * 1024 ** 3)
+        try:
+            r2, got2 = run(srv)
+        finally:
+            srv.close()
+        r2.update({"form": "host scheduler, batches up to 2048 on 4 lanes"})
+        ex["served"]["host_scheduler"] = r2
+        ex["_parity_served_host"] = got2
 
     def uneven():
         # uneven Pv2 batch: T in {4, 8, 32, 128}, 20-2048 Hz, 1024 requests, one launch
@@ -754,6 +765,8 @@ def secondary_parity(ex, res):
         ref = O.loglik_batch([O.params_from_dict(d) for d in sp], res["f"], dets, res["data"], [res["psd"]] * 3,
                              approximants=list(sa), T_segment=res["T"])
         out["served"] = parity_stats(got, ref, 1e-3)
+        if "_parity_served_host" in ex:  # the same sample through the host scheduler
+            out["served_host_scheduler"] = parity_stats(ex.pop("_parity_served_host"), ref, 1e-3)
     if "_parity_uneven" in ex:
         pu, Ts, udata, got = ex.pop("_parity_uneven")
         ref = np.zeros(len(pu))
@@ -955,6 +968,8 @@ def main():
                 line["served"]["speedup_vs_plain_fp64"] = ex["served"]["evals_per_s"] / plain
         if "fisher" in ex:
             line["fisher"] = dict(ex["fisher"], parity=fisher_parity)
+        if "served_host_scheduler" in sec_parity and "served" in line:
+            line["served"]["host_scheduler"]["parity"] = sec_parity.pop("served_host_scheduler")
         for k, v in sec_parity.items():
             key = k if k in line else ("maximized" if k.startswith("maximized") else k)
             if k.startswith("maximized") and "maximized" in line:

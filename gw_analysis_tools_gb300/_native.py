@@ -131,6 +131,7 @@ def _declare(L):
         "gwgpu_server_wait": (c_int, [c_void_p, ctypes.c_uint64, c_int, dp, ip]),
         "gwgpu_server_stats": (c_int, [c_void_p, dp, dp, P(ctypes.c_uint64), P(ctypes.c_uint64)]),
         "gwgpu_server_reset_stats": (c_int, [c_void_p]),
+        "gwgpu_server_loop_info": (c_int, [c_void_p, P(ctypes.c_longlong)]),
         "gwgpu_server_drive": (c_int, [c_void_p, c_void_p, ip, ip, c_int, dp, c_int, dp, ip, dp, dp]),
         "gwgpu_batch_set_tile": (c_int, [c_void_p, c_int]),
         "gwgpu_batch_set_blocks_per_sm": (c_int, [c_void_p, c_int]),

@@ -365,27 +365,48 @@ __device__ __forceinline__ void order_append(const OrderArgs &o, int kcut, int n
 }
 
 constexpr int kCoopWarps = 4, kCoopReq = 16;
-__global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
-    const GenParams *__restrict__ params, const int *__restrict__ approx, int n, const int *__restrict__ handles,
-    int ndet, double T_segment, int tc_from_segment, const StreamDev *__restrict__ streams,
-    const double *__restrict__ qnm, Request *req, MixedReq *mreq, int want_mixed, int *status, const OrderArgs ord) {
-  __shared__ Request s_r[kCoopReq];
-  __shared__ GenParams s_p[kCoopReq];
-  __shared__ AmpConn s_ac[kCoopReq];
-  __shared__ PhaseConnParts s_pc[kCoopReq];
-  __shared__ double s_ds[kCoopReq][kMaxDet], s_ws[kCoopReq][kMaxDet];  // stream scales of the mixed form
-  __shared__ unsigned long long s_wk[kCoopReq][kMaxDet];                 // and weight keys
-  __shared__ double s_shift[kCoopReq][kPv2ShiftNodes];
-  __shared__ double s_df[kCoopReq];
-  __shared__ int s_st[kCoopReq], s_bad[kCoopReq], s_uni[kCoopReq];
-  static_assert(2 * kCoopReq == 32, "two half-warps per warp share the block's requests");
-  grid_dep_trigger();  // the bin kernel may launch and wait for this grid
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * kCoopReq + lane;
+// Shared state of one group of kCoopWarps warps serving kCoopReq requests.
+struct CoopSmem {
+  Request r[kCoopReq];
+  GenParams p[kCoopReq];
+  AmpConn ac[kCoopReq];
+  PhaseConnParts pc[kCoopReq];
+  double ds[kCoopReq][kMaxDet], ws[kCoopReq][kMaxDet];  // stream scales of the mixed form
+  unsigned long long wk[kCoopReq][kMaxDet];              // and weight keys
+  double shift[kCoopReq][kPv2ShiftNodes];
+  double df[kCoopReq];
+  int st[kCoopReq], bad[kCoopReq], uni[kCoopReq];
+};
+// The cooperative prologue of requests base .. base + kCoopReq - 1 (those
+// below n) on one group of kCoopWarps warps: warp (0..3) and lane are the
+// thread's place in the group, sync() the group's barrier.  In S6, while warp
+// 0 stores the results, warps 1-3 call tail(warp, lane, act, i, kcut) with
+// kcut the end of request i's live bins (0 when it will not be evaluated);
+// tail is warp-collective.
+template <class Sync, class Tail>
+__device__ __forceinline__ void prologue_coop_body(CoopSmem &sm, int base, int warp, int lane,
+                                                   const GenParams *__restrict__ params,
+                                                   const int *__restrict__ approx, int n,
+                                                   const int *__restrict__ handles, int ndet, double T_segment,
+                                                   int tc_from_segment, const StreamDev *__restrict__ streams,
+                                                   const double *__restrict__ qnm, Request *req, MixedReq *mreq,
+                                                   int want_mixed, int *status, Sync sync, Tail tail) {
+  Request *s_r = sm.r;
+  GenParams *s_p = sm.p;
+  AmpConn *s_ac = sm.ac;
+  PhaseConnParts *s_pc = sm.pc;
+  double(*s_ds)[kMaxDet] = sm.ds;
+  double(*s_ws)[kMaxDet] = sm.ws;
+  unsigned long long(*s_wk)[kMaxDet] = sm.wk;
+  double(*s_shift)[kPv2ShiftNodes] = sm.shift;
+  double *s_df = sm.df;
+  int *s_st = sm.st, *s_bad = sm.bad, *s_uni = sm.uni;
+  static_assert(2 * kCoopReq == 32, "two half-warps per warp share the group's requests");
+  const int i = base + lane;
   const bool act = lane < kCoopReq && i < n;
   // half-warp form: lanes j and j + kCoopReq both serve request j
   const int hl = lane & (kCoopReq - 1);
-  const bool hact = blockIdx.x * kCoopReq + hl < n;
+  const bool hact = base + hl < n;
   Request &r = s_r[lane < kCoopReq ? lane : 0];
   const GenParams &p = s_p[lane < kCoopReq ? lane : 0];
   // S0
@@ -412,7 +433,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   if (warp == 1 || warp == 2) {  // projections need only the sky position: detectors over the half-warps of warps 1, 2
     // sky_trig with the hour angle's sincos on lanes j and the declination's
     // on lanes j + kCoopReq at once
-    const int ih = blockIdx.x * kCoopReq + hl;
+    const int ih = base + hl;
     const GenParams &q = params[min(ih, n - 1)];
     double s1, c1, sps, cps;
     sincos(lane < kCoopReq ? q.gmst - q.RA : q.DEC, &s1, &c1);
@@ -439,7 +460,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
       }
     }
   }
-  __syncthreads();
+  sync();
   const bool run = act && !s_bad[lane < kCoopReq ? lane : 0];
   const bool pv2 = run && r.approximant == kPhenomPv2;
   // S1: the calibration fits in four slots, the half-warps of warps 0 and 3
@@ -453,7 +474,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     }
     if (warp == 2) model_d_pn(r.m);
   }
-  __syncthreads();
+  sync();
   // S2
   if (run && warp == 0) {
     if (pv2) post_merger(r.m.s, qnm);
@@ -461,7 +482,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   }
   if (run && warp == 1 && !pv2) finish_fref_phase(r.m, s_pc[lane]);
   if (run && warp == 2 && !pv2) finish_f3_terms(r.m, fpeak(r.m.s, r.m.l), s_pc[lane]);
-  __syncthreads();
+  sync();
   // S3
   if (run) {
     if (warp == 0) {
@@ -485,10 +506,10 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
       else phase_conn_imr2(r.m, s_pc[lane]);
     }
   }
-  __syncthreads();
+  sync();
   // S3b  Pv2: the phase connection constants (its time-shift nodes need them)
   if (run && pv2 && warp == 2) phase_conn_combine(r.m, s_pc[lane]);
-  __syncthreads();
+  sync();
   // S4
   if (run) {
     if (!pv2) {
@@ -512,7 +533,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
         s_shift[hl][j] = pv2_shift_node(rh.m, j);
     }
   }
-  __syncthreads();
+  sync();
   // S5
   if (run) {
     if (warp == 3 && pv2) r.p.t_corr = r.m.s.shift_time ? pv2_shift_solve(r.m, s_shift[lane]) : 0.0;
@@ -529,7 +550,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
       if (warp == 3 && !pv2) mixed_det_phase(r, df, x);
     }
   }
-  __syncthreads();
+  sync();
   // S6
   if (act && warp == 0) {
     int st = s_st[lane];
@@ -552,22 +573,36 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     if (st && req) req[i].m.status = st;
     status[i] = st;
   }
-  if (warp >= 1 && ord.fill && want_mixed) {
-    // this block's requests into the work order, on the warps idle in S6 (warp
-    // w takes the tiles t = w - 1 mod 3); a request is live when S6's status
-    // will be 0: valid parameters, model status 0, one uniform grid length
-    int kcut = 0, nt = 0, i0 = 0;
-    if (act) {
-      if (!s_bad[lane] && r.m.status == 0 && s_st[lane] == 0 && s_uni[lane]) {
-        const StreamDev &s0 = streams[handles[i * ndet]];
-        kcut = min(s0.N, mreq[i].n_cut - s0.n0 + 1);  // n_cut: written in S5
-      }
-      nt = ord.item_count[i];
-      i0 = ord.item_start[i];
+  if (warp >= 1 && want_mixed) {
+    // a request is live when S6's status will be 0: valid parameters, model
+    // status 0, one uniform grid length
+    int kcut = 0;
+    if (act && !s_bad[lane] && r.m.status == 0 && s_st[lane] == 0 && s_uni[lane]) {
+      const StreamDev &s0 = streams[handles[i * ndet]];
+      kcut = min(s0.N, mreq[i].n_cut - s0.n0 + 1);  // n_cut: written in S5
     }
-    order_append(ord, kcut, nt, i0, warp - 1, kCoopWarps - 1);
+    tail(warp, lane, act, i, kcut);
   }
 }
+
+__global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
+    const GenParams *__restrict__ params, const int *__restrict__ approx, int n, const int *__restrict__ handles,
+    int ndet, double T_segment, int tc_from_segment, const StreamDev *__restrict__ streams,
+    const double *__restrict__ qnm, Request *req, MixedReq *mreq, int want_mixed, int *status, const OrderArgs ord) {
+  __shared__ CoopSmem sm;
+  grid_dep_trigger();  // the bin kernel may launch and wait for this grid
+  // this block's requests into the work order, on the warps idle in S6 (warp
+  // w takes the tiles t = w - 1 mod 3)
+  auto tail = [&](int warp, int lane, bool act, int i, int kcut) {
+    if (!ord.fill) return;
+    const int nt = act ? ord.item_count[i] : 0, i0 = act ? ord.item_start[i] : 0;
+    order_append(ord, kcut, nt, i0, warp - 1, kCoopWarps - 1);
+  };
+  prologue_coop_body(sm, blockIdx.x * kCoopReq, threadIdx.x >> 5, threadIdx.x & 31, params, approx, n, handles, ndet,
+                     T_segment, tc_from_segment, streams, qnm, req, mreq, want_mixed, status,
+                     [] { __syncthreads(); }, tail);
+}
+
 
 cudaError_t launch_prologue(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
                             double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
@@ -781,28 +816,163 @@ __device__ __forceinline__ void mixed_item(const BatchArgs &a, const MixedReq &x
     for (int j = 0; j < kAccPerDet; j++) v[d * kAccPerDet + j] = j < NA ? acc[d * NA + j].s - acc[d * NA + j].c : 0.f;
 }
 
+// Shared buffers of one item of the fused bin kernel.
+template <int NDET, int MIXED>
+struct BinSmem {
+  static constexpr int NV = MIXED ? NDET * kAccPerDet : 2 * NDET;
+  // mixed form: segment node values and fitted phase / alpha polynomials
+  static constexpr int kSegBuf = MIXED ? kMaxSegs : 1;
+  // FP64 form on uniform grids: each pass's arrival-time rotations
+  static constexpr int kRotPasses = MIXED ? 1 : kMaxTile / kBatchBlock;
+  alignas(16) unsigned char req[MIXED ? sizeof(MixedReq) : sizeof(Request)];
+  StreamDev st[NDET];
+  double res[NV];
+  float red[MIXED ? NV * kBatchBlock : 1];
+  double dsm[32 * (MIXED ? 1 : NV)];
+  double node[kSegBuf * kSegEval], node_a[kSegBuf * kSegEval];
+  SegPoly poly[kSegBuf], poly_a[kSegBuf];
+  double coef[kSegBuf * 2 * kSegNodes];
+  double2 rot64[kRotPasses * NDET];
+  // detector rotations: per segment pass (first bin) and per thread offset
+  float2 rot_seg[kSegBuf * (MIXED ? NDET : 1)];
+  float2 rot_off[(MIXED ? NDET : 1) * (MIXED ? kBatchBlock : 1)];
+};
+
+// One item (iid, I) of a batch on the whole block: its partial sums into
+// a.partials[iid]; the block that finishes a request's last item sums them in
+// item order and hands log L and the status to fin(request, log L, status)
+// (called by thread 0).
+template <int NDET, int MIXED, class Fin>
+__device__ __forceinline__ void batch_item(const BatchArgs &a, const int iid, const Item I, BinSmem<NDET, MIXED> &sm,
+                                           Fin fin) {
+  using BS = BinSmem<NDET, MIXED>;
+  constexpr int NV = BS::NV;
+  constexpr int kRotPasses = BS::kRotPasses;
+  unsigned char *s_req = sm.req;
+  StreamDev *s_st = sm.st;
+  double *s_res = sm.res;
+  float *s_red = sm.red;
+  double *s_dsm = sm.dsm;
+  double *s_node = sm.node, *s_node_a = sm.node_a;
+  SegPoly *s_poly = sm.poly, *s_poly_a = sm.poly_a;
+  double *s_coef = sm.coef;
+  double2 *s_rot64 = sm.rot64;
+  float2 *s_rot_seg = sm.rot_seg, *s_rot_off = sm.rot_off;
+  const int tid = threadIdx.x;
+  // stage the request constants and its streams
+  {
+    const unsigned *src = MIXED ? (const unsigned *)(a.mreq + I.req) : (const unsigned *)(a.req + I.req);
+    unsigned *dst = (unsigned *)s_req;
+    constexpr int nw = (MIXED ? sizeof(MixedReq) : sizeof(Request)) / 4;
+    for (int w = tid; w < nw; w += blockDim.x) dst[w] = __ldcg(src + w);
+    if (tid < NDET) s_st[tid] = a.streams[__ldcg(a.handles + I.req * a.ndet + tid)];
+  }
+  __syncthreads();
+  const int N = s_st[0].N;
+  const int kend = min(I.k0 + a.tile, N);
+  if constexpr (MIXED) {
+    const MixedReq &x = *(const MixedReq *)s_req;
+    float v[NV];
+    if (x.approximant == kPhenomPv2)
+      mixed_item<NDET, true>(a, x, s_st, I, N, kend, s_node, s_node_a, s_poly, s_poly_a, s_coef, s_rot_seg,
+                             s_rot_off, v);
+    else
+      mixed_item<NDET, false>(a, x, s_st, I, N, kend, s_node, s_node_a, s_poly, s_poly_a, s_coef, s_rot_seg,
+                              s_rot_off, v);
+    block_sum_mixed<NV>(v, s_red, s_res);
+  } else {
+    const Request &r = *(const Request *)s_req;
+    double v[NV];
+#pragma unroll
+    for (int j = 0; j < NV; j++) v[j] = 0.0;
+    bool uniform = true;
+#pragma unroll
+    for (int d = 0; d < NDET; d++) uniform = uniform && s_st[d].uniform_int;
+    const int npass = (kend - I.k0 + kBatchBlock - 1) / kBatchBlock;
+    if (uniform && npass <= kRotPasses) {
+      // e^{i tau f_k} = e^{i tau f_(first bin of the pass)} e^{i tau (k - first) df}
+      for (int e = tid; e < npass * NDET; e += blockDim.x) {
+        const int pass = e / NDET, d = e - pass * NDET;
+        double sn, cs;
+        sincos(r.det[d].tau * s_st[0].freqs[I.k0 + pass * kBatchBlock], &sn, &cs);
+        s_rot64[e] = make_double2(cs, sn);
+      }
+      double oc[NDET], os[NDET];
+#pragma unroll
+      for (int d = 0; d < NDET; d++) sincos(r.det[d].tau * (tid * s_st[0].df), &os[d], &oc[d]);
+      __syncthreads();
+      if (r.m.status == 0) {
+        int pass = 0;
+        for (int k = I.k0 + tid; k < kend; k += blockDim.x, pass++) {
+          double rc[NDET], rs[NDET];
+#pragma unroll
+          for (int d = 0; d < NDET; d++) {
+            const double2 b = s_rot64[pass * NDET + d];
+            rc[d] = b.x * oc[d] - b.y * os[d];
+            rs[d] = b.y * oc[d] + b.x * os[d];
+          }
+          fp64_bin_rot<NDET>(r, s_st, k, N, rc, rs, v);
+        }
+      }
+      __syncthreads();  // s_rot64 is rewritten by the next item
+    } else if (r.m.status == 0) {
+      for (int k = I.k0 + tid; k < kend; k += blockDim.x) fp64_bin<NDET>(r, s_st, k, N, v);
+    }
+    block_sum<NV>(v, s_dsm);
+    if (tid == 0)
+#pragma unroll
+      for (int j = 0; j < NV; j++) s_res[j] = v[j];
+    __syncthreads();
+  }
+  if (tid < NV) a.partials[(size_t)iid * kAcc + tid] = s_res[tid];
+  // last item of this request: fixed-order FP64 sum and log L
+  if (arrive_last(a.req_done + I.req, (unsigned)__ldcg(a.item_count + I.req))) {
+    if constexpr (MIXED) {
+      // lane j of warp 0: sum j over the request's items, times its factor;
+      // then a fixed-order warp sum
+      if (tid < 32) {
+        const MixedReq &x = *(const MixedReq *)s_req;
+        const int i0 = __ldcg(a.item_start + I.req), ic = __ldcg(a.item_count + I.req);
+        double v = 0.0;
+        if (tid < NV) {
+          for (int q = 0; q < ic; q++) v += __ldcg(&a.partials[(size_t)(i0 + q) * kAcc + tid]);
+          v *= x.fc[tid];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (tid == 0) {
+          int st = x.status;
+          if (__ldcg(a.status + I.req) & kStatusBounds) st = 5;
+          fin(I.req, st ? __longlong_as_double(0x7ff8000000000000ll) : v, st);
+        }
+      }
+    } else if (tid == 0) {
+      double s[NV];
+#pragma unroll
+      for (int j = 0; j < NV; j++) s[j] = 0.0;
+      const int i0 = __ldcg(a.item_start + I.req), ic = __ldcg(a.item_count + I.req);
+      for (int q = 0; q < ic; q++)
+#pragma unroll
+        for (int j = 0; j < NV; j++) s[j] += __ldcg(&a.partials[(size_t)(i0 + q) * kAcc + j]);
+      double ll;
+      int st;
+      {
+        const Request &r = *(const Request *)s_req;
+        ll = fp64_finalize<NDET>(s, s_st);
+        st = r.m.status;
+      }
+      if (__ldcg(a.status + I.req) & kStatusBounds) st = 5;
+      fin(I.req, st ? __longlong_as_double(0x7ff8000000000000ll) : ll, st);
+    }
+  }
+}
+
 // OCC: the resident blocks per SM the register allocation is bounded for
 // (mixed form 3 or 4, a launch-shape choice of the autotuner; FP64 form 2).
 template <int NDET, int MIXED, int OCC>
 __global__ void __launch_bounds__(kBatchBlock, OCC) k_batch(const BatchArgs a) {
-  constexpr int NV = MIXED ? NDET * kAccPerDet : 2 * NDET;
   __shared__ int s_item;
-  __shared__ __align__(16) unsigned char s_req[MIXED ? sizeof(MixedReq) : sizeof(Request)];
-  __shared__ StreamDev s_st[NDET];
-  __shared__ double s_res[NV];
-  __shared__ float s_red[MIXED ? NV * kBatchBlock : 1];
-  __shared__ double s_dsm[32 * (MIXED ? 1 : NV)];
-  // mixed form: segment node values and fitted phase / alpha polynomials
-  constexpr int kSegBuf = MIXED ? kMaxSegs : 1;
-  __shared__ double s_node[kSegBuf * kSegEval], s_node_a[kSegBuf * kSegEval];
-  __shared__ SegPoly s_poly[kSegBuf], s_poly_a[kSegBuf];
-  __shared__ double s_coef[kSegBuf * 2 * kSegNodes];
-  // FP64 form on uniform grids: each pass's arrival-time rotations
-  constexpr int kRotPasses = MIXED ? 1 : kMaxTile / kBatchBlock;
-  __shared__ double2 s_rot64[kRotPasses * NDET];
-  // detector rotations: per segment pass (first bin) and per thread offset
-  __shared__ float2 s_rot_seg[kSegBuf * (MIXED ? NDET : 1)];
-  __shared__ float2 s_rot_off[(MIXED ? NDET : 1) * (MIXED ? kBatchBlock : 1)];
+  __shared__ BinSmem<NDET, MIXED> sm;
   __shared__ int s_iid, s_bstart[kOrderBuckets];
   const int tid = threadIdx.x;
   grid_dep_wait();  // the prologue's output
@@ -850,117 +1020,278 @@ __global__ void __launch_bounds__(kBatchBlock, OCC) k_batch(const BatchArgs a) {
     const int it = s_item;
     if (it >= a.nitems) break;
     const int iid = s_iid;  // the item's own index: its partials' slot
-    const Item I = a.items[iid];
-    // stage the request constants and its streams
-    {
-      const unsigned *src = MIXED ? (const unsigned *)(a.mreq + I.req) : (const unsigned *)(a.req + I.req);
-      unsigned *dst = (unsigned *)s_req;
-      constexpr int nw = (MIXED ? sizeof(MixedReq) : sizeof(Request)) / 4;
-      for (int w = tid; w < nw; w += blockDim.x) dst[w] = src[w];
-      if (tid < NDET) s_st[tid] = a.streams[a.handles[I.req * a.ndet + tid]];
+    batch_item<NDET, MIXED>(a, iid, a.items[iid], sm, [&](int req, double ll, int st) {
+      a.out[req] = ll;
+      a.status_out[req] = st;
+    });
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------- serving loop kernel
+__device__ __forceinline__ long long global_ns() {
+  long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned long long ld_acquire_sys(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned ld_acquire_sys(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned ld_relaxed_gpu(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_acquire_gpu(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_gpu(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_release_sys(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Copies ring entries slot0 .. slot0 + k - 1 (host memory) into the device
+// arrays the prologue reads, with their sequence numbers and claim times.
+__device__ __forceinline__ void loop_stage(const LoopArgs &L, int slot0, int k, unsigned long long seq0) {
+  static_assert(sizeof(GenParams) % 4 == 0, "parameters copied as words");
+  constexpr int kW = sizeof(GenParams) / 4;
+  const int tid = threadIdx.x, ndet = L.a.ndet;
+  for (int w = tid; w < k * kW; w += blockDim.x) {
+    const int j = w / kW, q = w - j * kW;
+    ((unsigned *)(L.dparams + slot0 + j))[q] = __ldcv((const unsigned *)&L.ring[slot0 + j].p + q);
+  }
+  const long long now = global_ns();
+  for (int j = tid; j < k; j += blockDim.x) {
+    const LoopReq *e = L.ring + slot0 + j;
+    L.dapprox[slot0 + j] = __ldcv(&e->approx);
+    for (int d = 0; d < ndet; d++) L.dhandles[(slot0 + j) * ndet + d] = __ldcv(e->handles + d);
+    L.dseq[slot0 + j] = seq0 + j;
+    L.dclaim[slot0 + j] = now;
+  }
+}
+
+// The cooperative prologue of the claimed requests on warps 0-3 (a named
+// barrier of their own), then warp 0 publishes each request's live items
+// (tiles below its cut, at least one: a request that will not be evaluated
+// finishes through its first item with its status) in its claim word.
+template <int NDET>
+__device__ __forceinline__ void loop_prologue(const LoopArgs &L, CoopSmem &cs, int slot0, int k,
+                                              unsigned long long seq0) {
+  const BatchArgs &a = L.a;
+  loop_stage(L, slot0, k, seq0);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < kCoopWarps)
+    prologue_coop_body(cs, slot0, warp, lane, L.dparams, L.dapprox, slot0 + k, L.dhandles, NDET, L.T_segment, 1,
+                       a.streams, L.qnm, nullptr, const_cast<MixedReq *>(a.mreq), 1, a.status,
+                       [] { asm volatile("bar.sync 1, 128;" ::: "memory"); }, [](int, int, bool, int, int) {});
+  __threadfence();
+  __syncthreads();
+  if (warp != 0 || lane >= k) return;
+  const int slot = slot0 + lane;
+  const StreamDev &s0 = a.streams[__ldcg(L.dhandles + slot * NDET)];
+  int nlive = 1;
+  if (__ldcg(a.status + slot) == 0) {
+    const int nt = (s0.N + a.tile - 1) / a.tile;
+    const int kcut = min(s0.N, __ldcg(&a.mreq[slot].n_cut) - s0.n0 + 1);
+    nlive = max(1, min(nt, (kcut + a.tile - 1) / a.tile));
+  }
+  L.dcount[slot] = nlive;
+  a.req_done[slot] = 0u;
+  __threadfence();
+  st_release_gpu(L.dwork + slot, loop_word(seq0 + lane, nlive, 0));
+}
+
+constexpr unsigned kLoopNapMax = 2048;  // ns between polls of an idle polling block
+template <int NDET>
+__global__ void __launch_bounds__(kBatchBlock, 3) k_serve_loop(const __grid_constant__ LoopArgs L) {
+  using BS = BinSmem<NDET, 1>;
+  constexpr size_t kRaw = sizeof(BS) > sizeof(CoopSmem) ? sizeof(BS) : sizeof(CoopSmem);
+  __shared__ __align__(16) unsigned char s_raw[kRaw];
+  __shared__ int s_kind, s_a, s_b;
+  __shared__ unsigned long long s_seq;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const unsigned full = 0xffffffffu;
+  // pollers read the host's tail and stop flag at every idle poll, the other
+  // blocks only once idle for their longest nap
+  const bool poller = blockIdx.x % kLoopPollEvery == 0;
+  const unsigned nap_max = poller ? kLoopNapMax : kLoopPollEvery * kLoopNapMax;
+  const unsigned long long R = (unsigned long long)L.R;
+  const long long t0 = global_ns();
+  long long t_work = t0;
+  unsigned nap = 0;
+  for (;;) {
+    if (tid < 32) {  // warp 0 finds the block's next work
+      int kind = 0, a0 = 0, b0 = 0;  // 0 none, 1 item, 2 prologue, 3 leave
+      unsigned long long seq = 0;
+      // an item of one of the oldest requests whose prologue is done: lane l
+      // reads the claim word of request h + 32 g + l; the block tries the
+      // candidates from the (blockIdx mod candidates)-th on, so that blocks
+      // spread over them
+      unsigned long long h = 0, pend = 0;
+      if (lane == 0) {
+        h = ld_relaxed_gpu(&L.ctl->scan_head);
+        pend = ld_relaxed_gpu(&L.ctl->pro_head);
+      }
+      h = __shfl_sync(full, h, 0);
+      pend = __shfl_sync(full, pend, 0);
+      for (int g = 0; g < kLoopWindow / 32 && !kind && h + 32ull * g < pend; g++) {
+        const unsigned long long q = h + 32ull * g + lane;
+        const int slot = (int)(q % R);
+        const unsigned long long w = q < pend ? ld_acquire_gpu(L.dwork + slot) : 0ull;
+        const bool ready = q < pend && w >> 24 == ((q + 1) & 0xffffffffffull);
+        const int cnt = (int)((w >> 12) & 0xfffu), nxt = (int)(w & 0xfffu);
+        if (g == 0) {  // requests at the head with every item claimed: move the head past them
+          const unsigned spent = __ballot_sync(full, ready && nxt >= cnt);
+          const int lead = spent == full ? 32 : __ffs(~spent) - 1;
+          if (lane == 0 && lead > 0) atomicCAS(&L.ctl->scan_head, h, h + (unsigned long long)lead);
+        }
+        unsigned mask = __ballot_sync(full, ready && nxt < cnt);
+        for (int tries = 0; mask && tries < 4; tries++) {
+          const int nc = __popc(mask);
+          const int pick = (int)__fns(mask, 0, (int)(blockIdx.x % (unsigned)nc) + 1);
+          int ok = 0;
+          if (lane == pick) ok = atomicCAS(L.dwork + slot, w, w + 1) == w;
+          if (__shfl_sync(full, ok, pick)) {
+            kind = 1;
+            a0 = __shfl_sync(full, slot, pick);
+            b0 = __shfl_sync(full, nxt, pick);
+            break;
+          }
+          mask &= ~(1u << pick);
+        }
+      }
+      if (lane == 0) {
+        const long long now = global_ns();
+        const bool old = now - t0 > L.life_ns;
+        // new requests: the prologue of up to kLoopClaim of them, in ring order
+        if (!kind && !old) {
+          const unsigned long long p = ld_relaxed_gpu(&L.ctl->pro_head);
+          unsigned long long t = ld_relaxed_gpu(&L.ctl->tail_dev);
+          if (p >= t && (poller || nap >= nap_max)) {
+            t = ld_acquire_sys(L.tail);
+            __threadfence();
+            if (t > p) atomicMax(&L.ctl->tail_dev, t);
+          }
+          if (p < t) {
+            const unsigned long long k = min(min(t - p, (unsigned long long)kLoopClaim), R - p % R);
+            if (atomicCAS(&L.ctl->pro_head, p, p + k) == p) {
+              __threadfence_system();  // the ring entries below the tail seen are read after this
+              kind = 2;
+              a0 = (int)(p % R);
+              b0 = (int)k;
+              seq = p;
+            }
+          }
+        }
+        if (kind) {
+          t_work = now;
+        } else {
+          int why = -1;
+          if (old) why = 2;
+          else if (now - t_work > L.idle_ns) why = 0;
+          else if (nap >= kLoopNapMax) {
+            if ((poller || nap >= nap_max) && ld_acquire_sys(L.stop) == L.launch_id)
+              atomicExch(&L.ctl->stop_dev, L.launch_id);
+            if (ld_relaxed_gpu(&L.ctl->stop_dev) == L.launch_id) why = 1;
+          }
+          if (why >= 0) {
+            kind = 3;
+            atomicAdd(&L.ctl->exits[why], 1u);
+          }
+        }
+        s_kind = kind;
+        s_a = a0;
+        s_b = b0;
+        s_seq = seq;
+      }
     }
     __syncthreads();
-    const int N = s_st[0].N;
-    const int kend = min(I.k0 + a.tile, N);
-    if constexpr (MIXED) {
-      const MixedReq &x = *(const MixedReq *)s_req;
-      float v[NV];
-      if (x.approximant == kPhenomPv2)
-        mixed_item<NDET, true>(a, x, s_st, I, N, kend, s_node, s_node_a, s_poly, s_poly_a, s_coef, s_rot_seg,
-                               s_rot_off, v);
-      else
-        mixed_item<NDET, false>(a, x, s_st, I, N, kend, s_node, s_node_a, s_poly, s_poly_a, s_coef, s_rot_seg,
-                                s_rot_off, v);
-      block_sum_mixed<NV>(v, s_red, s_res);
-    } else {
-      const Request &r = *(const Request *)s_req;
-      double v[NV];
-#pragma unroll
-      for (int j = 0; j < NV; j++) v[j] = 0.0;
-      bool uniform = true;
-#pragma unroll
-      for (int d = 0; d < NDET; d++) uniform = uniform && s_st[d].uniform_int;
-      const int npass = (kend - I.k0 + kBatchBlock - 1) / kBatchBlock;
-      if (uniform && npass <= kRotPasses) {
-        // e^{i tau f_k} = e^{i tau f_(first bin of the pass)} e^{i tau (k - first) df}
-        for (int e = tid; e < npass * NDET; e += blockDim.x) {
-          const int pass = e / NDET, d = e - pass * NDET;
-          double sn, cs;
-          sincos(r.det[d].tau * s_st[0].freqs[I.k0 + pass * kBatchBlock], &sn, &cs);
-          s_rot64[e] = make_double2(cs, sn);
-        }
-        double oc[NDET], os[NDET];
-#pragma unroll
-        for (int d = 0; d < NDET; d++) sincos(r.det[d].tau * (tid * s_st[0].df), &os[d], &oc[d]);
-        __syncthreads();
-        if (r.m.status == 0) {
-          int pass = 0;
-          for (int k = I.k0 + tid; k < kend; k += blockDim.x, pass++) {
-            double rc[NDET], rs[NDET];
-#pragma unroll
-            for (int d = 0; d < NDET; d++) {
-              const double2 b = s_rot64[pass * NDET + d];
-              rc[d] = b.x * oc[d] - b.y * os[d];
-              rs[d] = b.y * oc[d] + b.x * os[d];
-            }
-            fp64_bin_rot<NDET>(r, s_st, k, N, rc, rs, v);
-          }
-        }
-        __syncthreads();  // s_rot64 is rewritten by the next item
-      } else if (r.m.status == 0) {
-        for (int k = I.k0 + tid; k < kend; k += blockDim.x) fp64_bin<NDET>(r, s_st, k, N, v);
+    const int kind = s_kind, a0 = s_a, b0 = s_b;
+    const unsigned long long seq = s_seq;
+    __syncthreads();
+    if (kind == 3) break;
+    if (kind == 0) {
+      if (tid == 0) {
+        __nanosleep(nap);
+        nap = min(2 * nap + 32, nap_max);
       }
-      block_sum<NV>(v, s_dsm);
-      if (tid == 0)
-#pragma unroll
-        for (int j = 0; j < NV; j++) s_res[j] = v[j];
-      __syncthreads();
+      continue;
     }
-    if (tid < NV) a.partials[(size_t)iid * kAcc + tid] = s_res[tid];
-    // last item of this request: fixed-order FP64 sum and log L
-    if (arrive_last(a.req_done + I.req, (unsigned)a.item_count[I.req])) {
-      if constexpr (MIXED) {
-        // lane j of warp 0: sum j over the request's items, times its factor;
-        // then a fixed-order warp sum
-        if (tid < 32) {
-          const MixedReq &x = *(const MixedReq *)s_req;
-          const int i0 = a.item_start[I.req], ic = a.item_count[I.req];
-          double v = 0.0;
-          if (tid < NV) {
-            for (int q = 0; q < ic; q++) v += __ldcg(&a.partials[(size_t)(i0 + q) * kAcc + tid]);
-            v *= x.fc[tid];
-          }
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-          if (tid == 0) {
-            int st = x.status;
-            if (__ldcg(a.status + I.req) & kStatusBounds) st = 5;
-            a.out[I.req] = st ? __longlong_as_double(0x7ff8000000000000ll) : v;
-            a.status_out[I.req] = st;
-          }
-        }
-      } else if (tid == 0) {
-        double s[NV];
-#pragma unroll
-        for (int j = 0; j < NV; j++) s[j] = 0.0;
-        const int i0 = a.item_start[I.req], ic = a.item_count[I.req];
-        for (int q = 0; q < ic; q++)
-#pragma unroll
-          for (int j = 0; j < NV; j++) s[j] += __ldcg(&a.partials[(size_t)(i0 + q) * kAcc + j]);
-        double ll;
-        int st;
-        {
-          const Request &r = *(const Request *)s_req;
-          ll = fp64_finalize<NDET>(s, s_st);
-          st = r.m.status;
-        }
-        if (__ldcg(a.status + I.req) & kStatusBounds) st = 5;
-        a.out[I.req] = st ? __longlong_as_double(0x7ff8000000000000ll) : ll;
-        a.status_out[I.req] = st;
+    nap = 0;
+    const long long tw0 = tid == 0 ? global_ns() : 0;
+    if (kind == 1) {
+      batch_item<NDET, 1>(L.a, a0 * L.max_items + b0, Item{a0, b0 * L.a.tile}, *(BS *)s_raw,
+                          [&](int req, double ll, int st) {
+                            const unsigned long long c = atomicAdd(&L.ctl->comp_alloc, 1ull);
+                            LoopDone *e = L.comp + c % R;
+                            e->seq = __ldcg(L.dseq + req);
+                            e->ll = ll;
+                            e->status = st;
+                            const long long dt = global_ns() - __ldcg(L.dclaim + req);
+                            e->service_ns = (int)min(dt, 2000000000ll);
+                            st_release_sys(&e->tag, c + 1);
+                          });
+    } else {
+      loop_prologue<NDET>(L, *(CoopSmem *)s_raw, a0, b0, seq);
+    }
+    if (tid == 0) {
+      const unsigned long long dt = (unsigned long long)(global_ns() - tw0);
+      if (kind == 1) {
+        atomicAdd(&L.ctl->busy_item_ns, dt);
+        atomicAdd(&L.ctl->n_item, 1ull);
+      } else {
+        atomicAdd(&L.ctl->busy_pro_ns, dt);
+        atomicAdd(&L.ctl->n_pro, 1ull);
+        atomicAdd(&L.ctl->n_pro_req, (unsigned long long)b0);
       }
     }
     __syncthreads();
   }
+}
+
+template <int NDET>
+static const void *serve_loop_fn() {
+  return (const void *)k_serve_loop<NDET>;
+}
+static const void *serve_loop_fn(int ndet) {
+  switch (ndet) {
+    case 1: return serve_loop_fn<1>();
+    case 2: return serve_loop_fn<2>();
+    case 3: return serve_loop_fn<3>();
+    case 4: return serve_loop_fn<4>();
+    default: return nullptr;
+  }
+}
+
+int serve_loop_blocks_per_sm(int ndet) {
+  int nb = 0;
+  const void *f = serve_loop_fn(ndet);
+  if (!f || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, kBatchBlock, 0) != cudaSuccess) return 0;
+  return nb;
+}
+
+cudaError_t launch_serve_loop(const LoopArgs &L, int grid, cudaStream_t s) {
+  const void *f = serve_loop_fn(L.a.ndet);
+  if (!f || grid < 1) return cudaErrorInvalidValue;
+  void *args[] = {(void *)&L};
+  return cudaLaunchKernel(f, dim3(grid), dim3(kBatchBlock), args, 0, s);
 }
 
 int batch_block_size(int) { return kBatchBlock; }

@@ -112,6 +112,78 @@ int batch_default_occ(int mixed);
 int batch_block_size(int mixed);
 int batch_occupancy(int mixed, int ndet, int occ);  // resident blocks per SM
 
+// ---- device-resident serving loop (mixed form) ----
+// The host appends requests to a ring in mapped pinned memory and publishes
+// them by advancing `tail`; a persistent kernel claims them in order, runs
+// the cooperative prologue for up to kLoopClaim of them per block, and
+// publishes each request's live items through its claim word (sequence
+// number and next item); blocks take items by compare-and-swap on the claim
+// words of the oldest requests (warp-parallel scan, spread over the
+// candidates), and the block that finishes a request's last item appends
+// its result to a completion queue in mapped memory (tag written last,
+// release at system scope).  Every block leaves when it has found no work for
+// idle_ns, when the host sets `stop` and it finds no work, or when life_ns
+// has passed since the launch; the host relaunches while requests are
+// outstanding.  No block waits on another block.  One block in
+// kLoopPollEvery reads the host's tail and stop flag at every idle poll, the
+// others only after their longest nap.
+constexpr int kLoopClaim = 16;
+constexpr int kLoopPollEvery = 8;
+constexpr int kLoopWindow = 128;  // requests past the oldest unclaimed one scanned for items
+// A request's claim word: its sequence number + 1 (low 40 bits), its live
+// items and the next unclaimed one (12 bits each).
+constexpr int kLoopMaxItems = 4095;
+inline __host__ __device__ unsigned long long loop_word(unsigned long long seq, int count, int next) {
+  return (((seq + 1) & 0xffffffffffull) << 24) | ((unsigned long long)count << 12) | (unsigned long long)next;
+}
+struct LoopReq {  // one ring entry (host memory, written by the host)
+  GenParams p;
+  int approx;
+  int handles[gwt::kMaxDet];
+  int pad;
+};
+struct LoopDone {  // one completion (host memory, written by the device)
+  unsigned long long tag;  // completion position + 1, written last
+  unsigned long long seq;  // the request's sequence number
+  double ll;
+  int status;      // kernel status code (status_code() maps it)
+  int service_ns;  // claimed -> result written, device global timer
+};
+struct LoopCtl {  // device memory: one counter per 128-byte line
+  unsigned long long pro_head, pad0[15];    // requests claimed for the prologue
+  unsigned long long tail_dev, pad1[15];    // the largest host tail a block has seen
+  unsigned long long scan_head, pad2[15];   // every request below has all its items claimed
+  unsigned long long comp_alloc, pad3[15];  // completions written
+  unsigned exits[4], pad4[28];              // blocks that left: idle, stop, life
+  unsigned stop_dev, pad5[31];              // the launch asked to leave, as seen by a polling block
+  // where the blocks' time goes: ns in items, ns in prologues, items,
+  // prologue claims, requests claimed
+  unsigned long long busy_item_ns, busy_pro_ns, n_item, n_pro, n_pro_req, pad6[11];
+};
+struct LoopArgs {
+  BatchArgs a;  // mreq, handles, ndet, streams, tile, item_start/count, req_done, partials, status, tables
+  const LoopReq *ring;             // R entries (device view of mapped host memory)
+  LoopDone *comp;                  // R completions (device view of mapped host memory)
+  const unsigned long long *tail;  // requests published (mapped)
+  const unsigned *stop;            // equal to launch_id: leave when idle (mapped)
+  LoopCtl *ctl;
+  GenParams *dparams;              // R: claimed requests' parameters (device copy)
+  int *dapprox;                    // R
+  int *dhandles;                   // R * ndet
+  int *dcount;                     // R: live items per request (a.item_count)
+  unsigned long long *dwork;       // R: claim word (see loop_word)
+  unsigned long long *dseq;        // R: sequence number of the request in each slot
+  long long *dclaim;               // R: global timer at the claim
+  int R, max_items;
+  double T_segment;
+  const double *qnm;
+  long long idle_ns, life_ns;
+  unsigned launch_id;
+};
+// grid: blocks (at most the resident capacity, serve_loop_blocks_per_sm x SMs)
+cudaError_t launch_serve_loop(const LoopArgs &L, int grid, cudaStream_t s);
+int serve_loop_blocks_per_sm(int ndet);
+
 // Per-request kernel status -> C ABI status: 0 ok, 1 invalid request (grids of
 // different lengths, grid unusable by the mixed form), 4 outside the model
 // domain, 5 grid beyond the per-bin power tables.

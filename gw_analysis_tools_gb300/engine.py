@@ -500,17 +500,23 @@ class FisherOptions(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("max_inflight", ctypes.c_int), ("max_batch", ctypes.c_int), ("lanes", ctypes.c_int),
-                ("precision", ctypes.c_int), ("T_segment", ctypes.c_double), ("hbm_budget_bytes", ctypes.c_size_t)]
+                ("precision", ctypes.c_int), ("T_segment", ctypes.c_double), ("hbm_budget_bytes", ctypes.c_size_t),
+                ("device_loop", ctypes.c_int), ("tile", ctypes.c_int), ("idle_us", ctypes.c_int)]
 
 
 class Server:
-    """Continuous-batching log-likelihood server on a Context (serve.cu)."""
+    """Continuous-batching log-likelihood server on a Context (serve.cu).
+
+    device_loop=True: the device-resident request loop (one persistent kernel
+    consuming a mapped ring; mixed precision), with `tile` bins per item and
+    its blocks leaving after `idle_us` without work."""
 
     def __init__(self, ctx, T_segment, max_inflight=8192, max_batch=1024, lanes=4, precision=PREC_MIXED,
-                 hbm_budget=0):
+                 hbm_budget=0, device_loop=False, tile=0, idle_us=0):
         self.ctx = ctx
         self.lib = ctx.lib
-        cfg = ServerConfig(max_inflight, max_batch, lanes, precision, float(T_segment), hbm_budget)
+        cfg = ServerConfig(max_inflight, max_batch, lanes, precision, float(T_segment), hbm_budget,
+                           1 if device_loop else 0, tile, idle_us)
         h = ctypes.c_void_p()
         ctx._check(self.lib.gwgpu_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(h)), "server_create")
         self.h = h
@@ -563,6 +569,19 @@ class Server:
 
     def reset_stats(self):
         self.lib.gwgpu_server_reset_stats(self.h)
+
+    def loop_info(self):
+        """Device loop: ring slots, tile, items per request, blocks, launches, the
+        blocks of finished launches that left idle / on stop / at end of life,
+        and the device service time percentiles (claim -> result, ns)."""
+        info = (ctypes.c_longlong * 15)()
+        st = self.lib.gwgpu_server_loop_info(self.h, info)
+        if st != 0:
+            raise GwGpuError("server_loop_info: %s" % STATUS.get(st, st))
+        keys = ("ring_slots", "tile", "max_items", "blocks", "launches", "exits_idle", "exits_stop", "exits_life",
+                "service_p50_ns", "service_p99_ns", "busy_item_ns", "busy_prologue_ns", "items", "prologue_claims",
+                "requests_claimed")
+        return dict(zip(keys, list(info)))
 
     def drive(self, params, approximants, handles, arrival_s):
         """Open-loop load: request i submitted at t0 + arrival_s[i] (native thread)."""

@@ -354,7 +354,20 @@ int gwgpu_mcmc_fisher_batch(gwgpu_context *ctx, const double *theta, int dim, in
  * chains / temperatures / ensembles are submitted into request slots; a
  * scheduler keeps up to `lanes` fused batches in flight on separate streams
  * and admits queued requests into the next launch as lanes and HBM budget
- * free up.  Results are the same alone and in any mix. */
+ * free up.  Results are the same alone and in any mix.
+ *
+ * device_loop = 1 selects the device-resident request loop instead (mixed
+ * precision): requests go into a ring in mapped pinned memory, and one
+ * persistent kernel on every SM claims them as they are published, runs
+ * their prologues, queues their items and evaluates them, writing each
+ * result and a completion sequence number back into mapped memory.  The
+ * ring's size is max_inflight, reduced to what hbm_budget_bytes admits
+ * (per-slot device state allocated at creation); max_batch and lanes are
+ * not used.  A launch's blocks leave after idle_us without work (and at the
+ * latest one second after the launch); the host relaunches while requests
+ * are outstanding.  Every request of one such server has the same number
+ * of detectors, and grids no longer than the longest grid registered when
+ * the server was created. */
 typedef struct {
   int max_inflight;          /* request slots (submitted, not yet collected) */
   int max_batch;             /* requests per fused launch */
@@ -362,6 +375,9 @@ typedef struct {
   int precision;             /* GWGPU_PREC_* */
   double T_segment;          /* as for gwgpu_mcmc_likelihood_extrinsic */
   size_t hbm_budget_bytes;   /* admission budget for in-flight scratch; 0 = the context budget */
+  int device_loop;           /* 1: device-resident request loop (GWGPU_PREC_MIXED only) */
+  int tile;                  /* device loop: bins per item, a multiple of 256 (0: 4096) */
+  int idle_us;               /* device loop: idle time after which a launch's blocks leave (0: 20000) */
 } gwgpu_server_config;
 int gwgpu_server_create(gwgpu_context *ctx, const gwgpu_server_config *cfg, gwgpu_server **out);
 int gwgpu_server_destroy(gwgpu_server *srv);
@@ -376,6 +392,15 @@ int gwgpu_server_wait(gwgpu_server *srv, uint64_t ticket, int timeout_ms, double
 /* Latency percentiles (seconds, submit -> result visible on host), counts. */
 int gwgpu_server_stats(gwgpu_server *srv, double *p50, double *p99, uint64_t *completed, uint64_t *launches);
 int gwgpu_server_reset_stats(gwgpu_server *srv);
+/* Device loop state: info[0] ring slots, [1] bins per item, [2] items per
+ * request at most, [3] blocks per launch, [4] launches, [5] blocks that left
+ * idle, [6] on the host's stop, [7] at the end of a launch's life (counts
+ * of finished launches), [8] and [9] p50 and p99 of the device service time
+ * in ns (request claimed -> result written; since the last reset_stats),
+ * [10] ns the blocks spent in items, [11] in prologues, [12] items,
+ * [13] prologue claims, [14] requests claimed (since creation).
+ * GWGPU_EINVAL for a host-scheduled server. */
+int gwgpu_server_loop_info(gwgpu_server *srv, long long info[15]);
 /* Load driver: submits request i at t0 + arrival_s[i] from the calling
  * thread (open loop, arrival time counted as submit time), collects every
  * result into loglik/status (request order) and the per-request latencies

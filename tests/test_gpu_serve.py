@@ -106,3 +106,128 @@ def test_odd_batches_and_lane_errors_do_not_hang(gpu_ctx, oracle, served):
     ref = oracle.loglik_batch([oracle.params_from_dict(d) for d in draws], f, list(W.DETECTORS3), data,
                               [W.analytic_psd(f)] * 3)
     assert np.max(np.abs(got - ref)) <= 1e-3
+
+
+# ---------------------------------------------------------------- device loop
+def _mix(n, seed):
+    dd = W.prior_draws(n // 2, seed)
+    dp = W.prior_draws(n - n // 2, seed + 1, precessing=True)
+    draws = [x for pair in zip(dd, dp) for x in pair]
+    return draws, [0, 1] * (n // 2)
+
+
+def test_device_loop_matches_batch_and_oracle(gpu_ctx, oracle, served):
+    """The device-resident loop gives the batched kernel's values bit for bit
+    (same tile) and the oracle's within 1e-3, D and Pv2 mixed."""
+    s = served
+    draws, aps = _mix(120, 111)
+    srv = G.Server(gpu_ctx, s["T"], max_inflight=512, device_loop=True, tile=4096)
+    tickets = [srv.submit(G.gen_params(**d), aps[i], s["hs"]) for i, d in enumerate(draws)]
+    got = np.array([srv.wait(t) for t in tickets])
+    info = srv.loop_info()
+    srv.close()
+    assert np.all(got[:, 1] == 0)
+    assert info["tile"] == 4096 and info["launches"] >= 1 and info["ring_slots"] == 512
+    gpu_ctx.set_tile(4096)
+    try:
+        for ap in (0, 1):
+            idx = [i for i in range(len(draws)) if aps[i] == ap]
+            ref, _ = gpu_ctx.loglik_batch(G.params_array([draws[i] for i in idx]), ap, s["hs"], s["T"], G.PREC_MIXED)
+            assert np.array_equal(got[idx, 0], ref)
+    finally:
+        gpu_ctx.set_tile(0)
+    f = s["f"]
+    data = [W.noise(f, 300 + i) for i in range(3)]
+    ref = oracle.loglik_batch([oracle.params_from_dict(d) for d in draws], f, list(W.DETECTORS3), data,
+                              [W.analytic_psd(f)] * 3, approximants=aps)
+    assert np.max(np.abs(got[:, 0] - ref)) <= 1e-3
+
+
+def test_device_loop_same_alone_and_in_the_mix(gpu_ctx, served):
+    s = served
+    draws, aps = _mix(300, 121)
+    srv = G.Server(gpu_ctx, s["T"], max_inflight=1024, device_loop=True)
+    tickets = [srv.submit(G.gen_params(**d), aps[i], s["hs"]) for i, d in enumerate(draws)]
+    mixed = np.array([srv.wait(t)[0] for t in tickets])
+    for i in (0, 1, 150, 299):
+        t = srv.submit(G.gen_params(**draws[i]), aps[i], s["hs"])
+        assert srv.wait(t)[0] == mixed[i]
+    srv.close()
+
+
+def test_device_loop_leaves_when_idle_and_relaunches(gpu_ctx, served):
+    """A launch's blocks leave after idle_us without work (bounded device
+    polling); the next request relaunches the loop and gets the same value."""
+    s = served
+    d = W.prior_draws(1, 131)[0]
+    srv = G.Server(gpu_ctx, s["T"], max_inflight=16, device_loop=True, idle_us=2000)
+    a = srv.wait(srv.submit(G.gen_params(**d), 0, s["hs"]))
+    deadline = time.time() + 5.0
+    while time.time() < deadline:
+        info = srv.loop_info()
+        if info["exits_idle"] >= info["blocks"]:
+            break
+        time.sleep(0.01)
+    assert info["exits_idle"] == info["blocks"] and info["launches"] == 1
+    b = srv.wait(srv.submit(G.gen_params(**d), 0, s["hs"]))
+    assert b == a and srv.loop_info()["launches"] == 2
+    srv.close()
+
+
+def test_device_loop_relaunches_on_new_registration(gpu_ctx, served):
+    """Data registered while the loop runs: the running launch is told to leave
+    and the next one sees the new stream table; same data, same values."""
+    s = served
+    f = s["f"]
+    draws = W.prior_draws(8, 141)
+    srv = G.Server(gpu_ctx, s["T"], max_inflight=64, device_loop=True, idle_us=500000)
+    first = [srv.wait(srv.submit(G.gen_params(**d), 0, s["hs"]))[0] for d in draws]
+    h2 = [gpu_ctx.register_data(dd, f, W.noise(f, 300 + i), W.analytic_psd(f)) for i, dd in enumerate(W.DETECTORS3)]
+    try:
+        again = [srv.wait(srv.submit(G.gen_params(**d), 0, h2))[0] for d in draws]
+        info = srv.loop_info()
+        assert again == first
+        # the first launch left (told to stop, or idle if the registration waited for it)
+        assert info["launches"] == 2 and info["exits_stop"] + info["exits_idle"] == info["blocks"]
+    finally:
+        srv.close()
+        for h in h2:
+            gpu_ctx.release_data(h)
+
+
+def test_device_loop_bad_requests_and_limits(gpu_ctx, served):
+    s = served
+    good = W.prior_draws(4, 151)
+    srv = G.Server(gpu_ctx, s["T"], max_inflight=32, device_loop=True)
+    bad = dict(good[0], mass1=-1.0)
+    ts = [srv.submit(G.gen_params(**d), 0, s["hs"]) for d in (good[0], bad, good[1])]
+    out = [srv.wait(t) for t in ts]
+    assert out[0][1] == 0 and out[2][1] == 0
+    assert out[1][1] == 4 and np.isnan(out[1][0])  # outside the model domain
+    with pytest.raises(G.GwGpuError):  # one detector count per loop
+        srv.submit(G.gen_params(**good[2]), 0, s["hs"][:2])
+    srv.close()
+    with pytest.raises(G.GwGpuError):  # the loop is mixed precision only
+        G.Server(gpu_ctx, s["T"], max_inflight=32, device_loop=True, precision=G.PREC_FP64)
+    with pytest.raises(G.GwGpuError):  # tile not a multiple of 256
+        G.Server(gpu_ctx, s["T"], max_inflight=32, device_loop=True, tile=1000)
+
+
+def test_device_loop_poisson_driver(gpu_ctx, oracle, served):
+    s = served
+    n = 4000
+    draws, aps = _mix(n, 161)
+    rng = np.random.default_rng(6)
+    arrivals = np.cumsum(rng.exponential(1.0 / 1e5, n))
+    srv = G.Server(gpu_ctx, s["T"], max_inflight=4096, device_loop=True)
+    out, st, lat, wall = srv.drive(G.params_array(draws), aps, s["hs"], arrivals)
+    stats = srv.stats()
+    srv.close()
+    assert np.all(st == 0) and stats["completed"] == n
+    assert 0 < stats["p50_s"] <= stats["p99_s"] < 5.0
+    pick = list(range(0, n, 97))
+    f = s["f"]
+    data = [W.noise(f, 300 + i) for i in range(3)]
+    ref = oracle.loglik_batch([oracle.params_from_dict(draws[i]) for i in pick], f, list(W.DETECTORS3), data,
+                              [W.analytic_psd(f)] * 3, approximants=[aps[i] for i in pick])
+    assert np.max(np.abs(out[pick] - ref)) <= 1e-3
