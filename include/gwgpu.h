@@ -367,7 +367,10 @@ int gwgpu_mcmc_fisher_batch(gwgpu_context *ctx, const double *theta, int dim, in
  * latest one second after the launch); the host relaunches while requests
  * are outstanding.  Every request of one such server has the same number
  * of detectors, and grids no longer than the longest grid registered when
- * the server was created. */
+ * the server was created.  While its kernel is resident (requests flowing,
+ * and idle_us after the last) it holds every SM: other kernels on the GPU,
+ * including a second device-loop server's, start when its blocks leave, so
+ * run one device loop per GPU and lower idle_us where other calls share it. */
 typedef struct {
   int max_inflight;          /* request slots (submitted, not yet collected) */
   int max_batch;             /* requests per fused launch */
