@@ -231,3 +231,28 @@ def test_device_loop_poisson_driver(gpu_ctx, oracle, served):
     ref = oracle.loglik_batch([oracle.params_from_dict(draws[i]) for i in pick], f, list(W.DETECTORS3), data,
                               [W.analytic_psd(f)] * 3, approximants=[aps[i] for i in pick])
     assert np.max(np.abs(out[pick] - ref)) <= 1e-3
+
+
+def test_device_loop_small_ring_wraps(gpu_ctx, served):
+    """A ring of a few slots (the HBM budget admits four) reused many times:
+    every slot, claim word and completion entry goes round ~25 laps, and the
+    values stay the batched kernel's bit for bit."""
+    s = served
+    draws, aps = _mix(100, 171)
+    per_slot = 4096  # about one slot's bytes for the 32k-bin grid (model constants, partials of 8 items)
+    srv = G.Server(gpu_ctx, s["T"], max_inflight=64, device_loop=True, hbm_budget=4 * per_slot)
+    try:
+        slots = srv.loop_info()["ring_slots"]
+        assert 1 <= slots <= 8
+        out, st, lat, wall = srv.drive(G.params_array(draws), aps, s["hs"], np.zeros(len(draws)))
+    finally:
+        srv.close()
+    assert np.all(st == 0)
+    gpu_ctx.set_tile(4096)
+    try:
+        for ap in (0, 1):
+            idx = [i for i in range(len(draws)) if aps[i] == ap]
+            ref, _ = gpu_ctx.loglik_batch(G.params_array([draws[i] for i in idx]), ap, s["hs"], s["T"], G.PREC_MIXED)
+            assert np.array_equal(out[idx], ref)
+    finally:
+        gpu_ctx.set_tile(0)
