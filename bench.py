@@ -428,8 +428,7 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
             li = srv.loop_info()
         finally:
             srv.close()
-        r.update({"form": "device-resident request loop", "ensembles": ens,
-                  "loop": {k: li[k] for k in ("ring_slots", "tile", "max_items", "blocks", "launches")}})
+        r.update({"form": "device-resident request loop", "ensembles": ens, "loop": li})
         ex["served"] = r
         ex["_parity_served"] = ([sp[i] for i in pick], [sa[i] for i in pick], got)
         # the host scheduler: fused batches on 4 stream lanes

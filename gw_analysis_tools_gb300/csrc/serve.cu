@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <climits>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -251,6 +252,7 @@ int loop_create(gwgpu_server *s) {
   size_t R = (size_t)cfg.max_inflight;
   if (s->budget) R = std::min(R, s->budget / per_slot);
   if (R < 1) return GWGPU_ENOMEM;
+  R = std::min(R, (size_t)(INT_MAX / max_items));  // item indices slot * max_items + t are ints
   DeviceLoop *L = new DeviceLoop();
   L->R = (int)R;
   L->tile = tile;
