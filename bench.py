@@ -393,8 +393,9 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         sa2 = [i % 2 for i in range(nsat)]
         arr2 = np.cumsum(rng.exponential(1.0 / 5e6, nsat))
 
-        def run(srv):
-            """2e5/s, saturation (5e6/s offered) and latency against offered load."""
+        def run(srv, info=None):
+            """2e5/s, saturation (5e6/s offered) and latency against offered load;
+            info(): the device loop's counters after the first two."""
             srv.drive(G.params_array(sp[:2000]), sa[:2000], handles, arrivals[:2000] - arrivals[0])  # warm-up
             srv.reset_stats()
             out, st, lat, wall = srv.drive(G.params_array(sp), sa, handles, arrivals - arrivals[0])
@@ -402,12 +403,16 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
             r = {"evals_per_s": nserve / wall, "p50_ms": s["p50_s"] * 1e3, "p99_ms": s["p99_s"] * 1e3,
                  "offered_rate": 2e5, "requests": nserve, "launches": s["launches"], "ok": int((st == 0).sum())}
             got = out[pick].copy()
+            if info:
+                r["loop"] = info()
             srv.reset_stats()
             _, st2, _, wall2 = srv.drive(G.params_array(sp2), sa2, handles, arr2 - arr2[0])
             s2 = srv.stats()
             r["saturated"] = {"evals_per_s": nsat / wall2, "p50_ms": s2["p50_s"] * 1e3, "p99_ms": s2["p99_s"] * 1e3,
                               "offered_rate": 5e6, "requests": nsat, "launches": s2["launches"],
                               "ok": int((st2 == 0).sum())}
+            if info:
+                r["saturated"]["loop"] = info()
             curve = []
             for rate in (5e5, 1e6, 2e6, 3e6):
                 nr = int(min(100000, max(20000, rate * 0.05)))
@@ -424,11 +429,10 @@ def secondary_forms(ctx, G, W, torch, stream, flush, f, T, handles, host_params,
         # the device-resident request loop (the served form)
         srv = G.Server(ctx, T, max_inflight=65536, device_loop=True, hbm_budget=120 * 1024 ** 3)
         try:
-            r, got = run(srv)
-            li = srv.loop_info()
+            r, got = run(srv, srv.loop_info)
         finally:
             srv.close()
-        r.update({"form": "device-resident request loop", "ensembles": ens, "loop": li})
+        r.update({"form": "device-resident request loop", "ensembles": ens})
         ex["served"] = r
         ex["_parity_served"] = ([sp[i] for i in pick], [sa[i] for i in pick], got)
         # the host scheduler: fused batches on 4 stream lanes
