@@ -236,7 +236,7 @@ int loop_create(gwgpu_server *s) {
   const gwgpu_server_config &cfg = s->cfg;
   if (cfg.precision != GWGPU_PREC_MIXED) return GWGPU_EINVAL;
   const int tile = cfg.tile > 0 ? cfg.tile : 4096;
-  if (tile % 256 || tile > (1 << 20)) return GWGPU_EINVAL;
+  if (tile % 256 || tile > (1 << 20) || cfg.blocks_per_sm < 0) return GWGPU_EINVAL;
   int nmax = 0;
   {
     std::lock_guard<std::mutex> ck(c->mu);
@@ -355,7 +355,9 @@ int loop_launch(gwgpu_server *s) {
   if (!L.grid) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    L.grid = std::max(1, gwk::serve_loop_blocks_per_sm(L.ndet)) * std::max(1, sms);
+    int nb = std::max(1, gwk::serve_loop_blocks_per_sm(L.ndet));
+    if (s->cfg.blocks_per_sm > 0) nb = std::min(nb, s->cfg.blocks_per_sm);
+    L.grid = nb * std::max(1, sms);
   }
   L.args.a.ndet = L.ndet;
   L.args.a.streams = c->streams_dev;

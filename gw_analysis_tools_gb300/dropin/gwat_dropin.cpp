@@ -45,9 +45,16 @@ struct Engine {
   // registered streams, most recently used first
   std::list<std::pair<HandleKey, int>> lru;
   std::map<HandleKey, std::list<std::pair<HandleKey, int>>::iterator> handles;
-  // one continuous-batching server per segment length T: never destroyed
-  // while the process runs, so no caller can be inside a server being freed
+  // served mode: the first segment length T is served by the device-resident
+  // request loop (2 blocks per SM, leaving room for other kernels of the
+  // context); other values of T, and requests the loop does not take (another
+  // detector count, a longer grid), by one host-scheduled server per T.
+  // GWGPU_DROPIN_SERVER=host: host-scheduled servers only.  No server is
+  // destroyed while the process runs, so no caller can be inside one being freed.
   std::map<double, gwgpu_server *> servers;
+  gwgpu_server *loop = nullptr;
+  double loop_T = 0;
+  bool use_loop = true, loop_failed = false;
 };
 
 static Engine &engine() {
@@ -58,11 +65,14 @@ static Engine &engine() {
     gwgpu_context_create(dev ? std::atoi(dev) : 0, 0, &e.ctx);
     const char *mode = std::getenv("GWGPU_DROPIN_MODE");
     e.served = mode && std::strcmp(mode, "served") == 0;
+    const char *sv = std::getenv("GWGPU_DROPIN_SERVER");
+    e.use_loop = !(sv && std::strcmp(sv, "host") == 0);
   });
   return e;
 }
 
 void set_mode(const char *mode) { engine().served = mode && std::strcmp(mode, "served") == 0; }
+void set_server(const char *server) { engine().use_loop = !(server && std::strcmp(server, "host") == 0); }
 
 static uint64_t fingerprint(const double *a, int n) {
   uint64_t h = 1469598103934665603ull;
@@ -132,7 +142,7 @@ static int handle_for(Engine &e, const std::string &det, const double *f, const 
 // server may still hold requests on older streams, so nothing is released
 // there while any server exists.
 static void evict(Engine &e, const int *keep, int nkeep) {
-  if (!e.servers.empty()) return;
+  if (!e.servers.empty() || e.loop) return;
   while (e.lru.size() > kMaxHandles) {
     auto last = std::prev(e.lru.end());
     bool kept = false;
@@ -233,26 +243,51 @@ double MCMC_likelihood_extrinsic(bool save_waveform, gen_params_base<double> *pa
   int approx = generation_method.find("Pv2") != std::string::npos ? GWGPU_IMRPHENOMPV2 : GWGPU_IMRPHENOMD;
   if (e.served && !gauss) {  // the served (mixed) form wants uniform grids; Gauss-Legendre grids run plain
     gwgpu_server *srv = nullptr;
+    // the host-scheduled server of this T (e.mu held)
+    auto host_server = [&]() -> gwgpu_server * {
+      auto it = e.servers.find(T);
+      if (it != e.servers.end()) return it->second;
+      gwgpu_server_config cfg = {16384, 1024, 4, GWGPU_PREC_MIXED, T, 0, 0, 0, 0, 0};
+      gwgpu_server *h = nullptr;
+      if (gwgpu_server_create(e.ctx, &cfg, &h) != GWGPU_OK || !h) return nullptr;
+      e.servers[T] = h;
+      return h;
+    };
     {
       std::lock_guard<std::mutex> lk(e.mu);
-      auto it = e.servers.find(T);
-      if (it == e.servers.end()) {
-        gwgpu_server_config cfg = {16384, 1024, 4, GWGPU_PREC_MIXED, T, 0};
-        if (gwgpu_server_create(e.ctx, &cfg, &srv) != GWGPU_OK || !srv) return NAN;
-        e.servers[T] = srv;
-      } else {
-        srv = it->second;
+      if (e.use_loop && !e.loop && !e.loop_failed) {
+        gwgpu_server_config cfg = {16384, 1024, 4, GWGPU_PREC_MIXED, T, 0, 1, 0, 0, 2};
+        if (gwgpu_server_create(e.ctx, &cfg, &e.loop) == GWGPU_OK && e.loop) {
+          e.loop_T = T;
+        } else {
+          e.loop = nullptr;
+          e.loop_failed = true;
+        }
       }
+      srv = e.use_loop && e.loop && e.loop_T == T ? e.loop : host_server();
+      if (!srv) return NAN;
     }
     // every slot taken: back off and retry, for at most a minute
     uint64_t t;
     int st;
     const auto deadline = std::chrono::steady_clock::now() + std::chrono::seconds(60);
     auto pause = std::chrono::microseconds(20);
-    while ((st = gwgpu_server_submit(srv, &p, approx, hs, num_detectors, &t)) == GWGPU_EBUSY) {
-      if (std::chrono::steady_clock::now() > deadline) return NAN;
-      std::this_thread::sleep_for(pause);
-      pause = std::min(pause * 2, std::chrono::microseconds(2000));
+    for (;;) {
+      st = gwgpu_server_submit(srv, &p, approx, hs, num_detectors, &t);
+      if (st == GWGPU_EBUSY) {
+        if (std::chrono::steady_clock::now() > deadline) return NAN;
+        std::this_thread::sleep_for(pause);
+        pause = std::min(pause * 2, std::chrono::microseconds(2000));
+        continue;
+      }
+      if ((st == GWGPU_EINVAL || st == GWGPU_ETOOLARGE) && srv == e.loop) {
+        // another detector count or a longer grid than the loop was sized for
+        std::lock_guard<std::mutex> lk(e.mu);
+        srv = host_server();
+        if (!srv) return NAN;
+        continue;
+      }
+      break;
     }
     if (st != GWGPU_OK) return NAN;
     int rst = GWGPU_OK;
@@ -434,7 +469,8 @@ extern "C" double gwat_dropin_test_loglik(const double *f, int N, const double *
   g.DEC = pp->DEC;
   g.psi = pp->psi;
   g.gmst = pp->gmst;
-  set_mode(served ? "served" : "plain");
+  set_mode(served ? "served" : "plain");  // served: 1 the device loop, 2 the host scheduler
+  set_server(served == 2 ? "host" : "loop");
   std::vector<int> len(ndet, N);
   std::vector<double *> fs(ndet), ps(ndet), ws(ndet, nullptr);
   std::vector<std::complex<double> *> ds(ndet);

@@ -501,22 +501,24 @@ class FisherOptions(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("max_inflight", ctypes.c_int), ("max_batch", ctypes.c_int), ("lanes", ctypes.c_int),
                 ("precision", ctypes.c_int), ("T_segment", ctypes.c_double), ("hbm_budget_bytes", ctypes.c_size_t),
-                ("device_loop", ctypes.c_int), ("tile", ctypes.c_int), ("idle_us", ctypes.c_int)]
+                ("device_loop", ctypes.c_int), ("tile", ctypes.c_int), ("idle_us", ctypes.c_int),
+                ("blocks_per_sm", ctypes.c_int)]
 
 
 class Server:
     """Continuous-batching log-likelihood server on a Context (serve.cu).
 
     device_loop=True: the device-resident request loop (one persistent kernel
-    consuming a mapped ring; mixed precision), with `tile` bins per item and
-    its blocks leaving after `idle_us` without work."""
+    consuming a mapped ring; mixed precision), with `tile` bins per item, its
+    blocks leaving after `idle_us` without work, and `blocks_per_sm` of them
+    on each SM (0: as many as fit)."""
 
     def __init__(self, ctx, T_segment, max_inflight=8192, max_batch=1024, lanes=4, precision=PREC_MIXED,
-                 hbm_budget=0, device_loop=False, tile=0, idle_us=0):
+                 hbm_budget=0, device_loop=False, tile=0, idle_us=0, blocks_per_sm=0):
         self.ctx = ctx
         self.lib = ctx.lib
         cfg = ServerConfig(max_inflight, max_batch, lanes, precision, float(T_segment), hbm_budget,
-                           1 if device_loop else 0, tile, idle_us)
+                           1 if device_loop else 0, tile, idle_us, blocks_per_sm)
         h = ctypes.c_void_p()
         ctx._check(self.lib.gwgpu_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(h)), "server_create")
         self.h = h

@@ -94,10 +94,13 @@ void fisher_numerical(double *frequency, int length, std::string generation_meth
 
 // Engine behind the drop-in: GWGPU_DROPIN_DEVICE (default 0) and
 // GWGPU_DROPIN_MODE = "plain" (default: one FP64 request per launch) or
-// "served" (concurrent callers coalesced by the continuous-batching server,
-// mixed precision).
+// "served" (concurrent callers' requests served together, mixed precision);
+// GWGPU_DROPIN_SERVER = "loop" (default: the device-resident request loop for
+// the first segment length, host-scheduled batching for the rest) or "host"
+// (host-scheduled batching only).  set_mode / set_server change them later.
 namespace gwat_dropin {
 void set_mode(const char *mode);
+void set_server(const char *server);
 }
 
 #endif

@@ -370,7 +370,8 @@ int gwgpu_mcmc_fisher_batch(gwgpu_context *ctx, const double *theta, int dim, in
  * the server was created.  While its kernel is resident (requests flowing,
  * and idle_us after the last) it holds every SM: other kernels on the GPU,
  * including a second device-loop server's, start when its blocks leave, so
- * run one device loop per GPU and lower idle_us where other calls share it. */
+ * run one device loop per GPU and lower idle_us where other calls share it,
+ * or give it fewer blocks per SM (blocks_per_sm) to leave room beside it. */
 typedef struct {
   int max_inflight;          /* request slots (submitted, not yet collected) */
   int max_batch;             /* requests per fused launch */
@@ -381,6 +382,8 @@ typedef struct {
   int device_loop;           /* 1: device-resident request loop (GWGPU_PREC_MIXED only) */
   int tile;                  /* device loop: bins per item, a multiple of 256 (0: 4096) */
   int idle_us;               /* device loop: idle time after which a launch's blocks leave (0: 20000) */
+  int blocks_per_sm;         /* device loop: blocks it keeps on each SM, 1..3 (0: 3, the SM's capacity);
+                                fewer leave room for other kernels while it is resident */
 } gwgpu_server_config;
 int gwgpu_server_create(gwgpu_context *ctx, const gwgpu_server_config *cfg, gwgpu_server **out);
 int gwgpu_server_destroy(gwgpu_server *srv);

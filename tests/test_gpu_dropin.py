@@ -37,7 +37,7 @@ def _call(fn, f, data, psd, dets, p, served):
     return ll, tc
 
 
-@pytest.mark.parametrize("served", [0, 1])
+@pytest.mark.parametrize("served", [0, 1, 2])  # plain; served by the device loop; by the host scheduler
 def test_mcmc_likelihood_extrinsic_dropin(oracle, served):
     fn = _dropin()
     f = np.ascontiguousarray(workloads.uniform_grid(20.0, 512.0, 1.0 / 8.0))
