@@ -470,6 +470,12 @@ int loop_collect(gwgpu_server *s) {
     if (__atomic_load_n(&e.tag, __ATOMIC_ACQUIRE) != L.cursor + 1) break;
     if (t < 0) t = now_s();
     const int pos = (int)(e.seq % (uint64_t)L.R);
+    if (e.seq < L.retired || e.seq >= L.published || L.complete[pos] || L.slot_of[pos] < 0) {
+      // not a request outstanding in the ring: the completion is dropped
+      s->worker_error = GWGPU_ECUDA;
+      L.cursor++;
+      continue;
+    }
     Slot &sl = s->slots[L.slot_of[pos]];
     sl.ll = e.ll;
     sl.status = gwk::status_code(e.status);
