@@ -171,14 +171,20 @@ __global__ void __launch_bounds__(kBlock, 3) k_fisher_main(const FisherArgs a) {
       s_last = (prev == (unsigned)a.ntiles - 1);
     }
     __syncthreads();
-    if (s_last && tid == 0) {
+    // the source's sums over its tiles, one sum per thread in tile order
+    __shared__ double s_sum[kMaxDet * kSums];
+    if (s_last) {
       __threadfence();
-      double Ssum[kMaxDet * kSums];
-      for (int j = 0; j < NW * kSums; j++) {
-        double s = 0;
-        for (int tt = 0; tt < a.ntiles; tt++) s += __ldcg(&a.partials[((size_t)(src * a.ntiles + tt)) * kMaxDet * kSums + j]);
-        Ssum[j] = s;
+      for (int j = tid; j < NW * kSums; j += blockDim.x) {
+        double sj = 0;
+        for (int tt = 0; tt < a.ntiles; tt++)
+          sj += __ldcg(&a.partials[((size_t)(src * a.ntiles + tt)) * kMaxDet * kSums + j]);
+        s_sum[j] = sj;
       }
+    }
+    __syncthreads();
+    if (s_last && tid == 0) {
+      const double *Ssum = s_sum;
       double Gm[kDim * kDim];
       fisher_assemble(F, Ssum, a.ndet, a.wslot, a.wscale, a.fisher_df_ratio, Gm);
       double *outF = a.fisher + (size_t)src * kDim * kDim;

@@ -118,14 +118,15 @@ __global__ void k_inner(const double2 *__restrict__ data, const double *__restri
     partials[blockIdx.x * 2 + 1] = v[1];
   }
   if (arrive_last(counter, gridDim.x)) {
+    double t[2] = {0.0, 0.0};  // the blocks' partials, strided over the block, then reduced
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+      t[0] += __ldcg(&partials[b * 2 + 0]);
+      t[1] += __ldcg(&partials[b * 2 + 1]);
+    }
+    block_sum<2>(t, smem);
     if (threadIdx.x == 0) {
-      double hh = 0, dh = 0;
-      for (unsigned b = 0; b < gridDim.x; b++) {
-        hh += __ldcg(&partials[b * 2 + 0]);
-        dh += __ldcg(&partials[b * 2 + 1]);
-      }
       double c = iw ? 1.0 : 4. * simpson_df / 3.;
-      out[0] = -0.5 * (c * hh - 2 * c * dh);
+      out[0] = -0.5 * (c * t[0] - 2 * c * t[1]);
       *counter = 0;
     }
   }
@@ -199,27 +200,68 @@ __device__ __forceinline__ double fp64_finalize(const double *s, const StreamDev
 }
 
 // ------------------------------------------------------------------ plain
+// On uniform grids each block's arrival-time rotations come from a table:
+// thread t = 16 a + b of a block starting at bin k0 takes
+// e^{i tau (f_k0 + t df)} = e^{i tau f_k0} e^{i tau 16 a df} e^{i tau b df},
+// 25 sincos per detector and block (one per thread for the first 25 NDET
+// threads) instead of one per detector-bin.
+constexpr int kPlainRot = 1 + 8 + 16;
 template <int NDET>
 __global__ void __launch_bounds__(128) k_plain(const __grid_constant__ Request r, const __grid_constant__ PlainStreams ps,
                                                double *partials, unsigned *counter, double *out, int *status) {
   __shared__ double smem[32 * 2 * NDET];
+  __shared__ double2 s_rot[NDET * kPlainRot];
   const int N = ps.s[0].N;
   double v[2 * NDET];
 #pragma unroll
   for (int j = 0; j < 2 * NDET; j++) v[j] = 0.0;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) fp64_bin<NDET>(r, ps.s, k, N, v);
+  bool uniform = blockDim.x == 128 && (long long)gridDim.x * 128 >= N;  // one bin per thread
+#pragma unroll
+  for (int d = 0; d < NDET; d++) uniform = uniform && ps.s[d].uniform_int;
+  if (uniform) {
+    const int k0 = blockIdx.x * 128;
+    for (int e = threadIdx.x; e < NDET * kPlainRot; e += blockDim.x) {
+      const int d = e / kPlainRot, j = e - d * kPlainRot;
+      const double tau = r.det[d].tau, df = ps.s[0].df;
+      const double arg = j == 0 ? tau * ps.s[0].freqs[min(k0, N - 1)]
+                                : tau * ((j <= 8 ? 16.0 * (j - 1) : (double)(j - 9)) * df);
+      double sn, cs;
+      sincos(arg, &sn, &cs);
+      s_rot[e] = make_double2(cs, sn);
+    }
+    __syncthreads();
+    const int k = k0 + threadIdx.x;
+    if (k < N) {
+      const int a = threadIdx.x >> 4, b = threadIdx.x & 15;
+      double rc[NDET], rs[NDET];
+#pragma unroll
+      for (int d = 0; d < NDET; d++) {
+        const double2 B = s_rot[d * kPlainRot], A = s_rot[d * kPlainRot + 1 + a], C = s_rot[d * kPlainRot + 9 + b];
+        const double xr = B.x * A.x - B.y * A.y, xi = B.x * A.y + B.y * A.x;
+        rc[d] = xr * C.x - xi * C.y;
+        rs[d] = xr * C.y + xi * C.x;
+      }
+      fp64_bin_rot<NDET>(r, ps.s, k, N, rc, rs, v);
+    }
+  } else {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x)
+      fp64_bin<NDET>(r, ps.s, k, N, v);
+  }
   block_sum<2 * NDET>(v, smem);
   if (threadIdx.x == 0)
 #pragma unroll
     for (int j = 0; j < 2 * NDET; j++) partials[blockIdx.x * (2 * NDET) + j] = v[j];
   if (arrive_last(counter, gridDim.x)) {
+    // the blocks' partials summed by the whole block (strided, then the
+    // block reduction): a fixed order, and no serial chain of L2 loads
+    double s[2 * NDET];
+#pragma unroll
+    for (int j = 0; j < 2 * NDET; j++) s[j] = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+#pragma unroll
+      for (int j = 0; j < 2 * NDET; j++) s[j] += __ldcg(&partials[b * (2 * NDET) + j]);
+    block_sum<2 * NDET>(s, smem);
     if (threadIdx.x == 0) {
-      double s[2 * NDET];
-#pragma unroll
-      for (int j = 0; j < 2 * NDET; j++) s[j] = 0.0;
-      for (unsigned b = 0; b < gridDim.x; b++)
-#pragma unroll
-        for (int j = 0; j < 2 * NDET; j++) s[j] += __ldcg(&partials[b * (2 * NDET) + j]);
       out[0] = fp64_finalize<NDET>(s, ps.s);
       if (status) status[0] = r.m.status ? 4 : 0;
       *counter = 0;

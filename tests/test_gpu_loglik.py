@@ -71,6 +71,19 @@ def test_plain_single_detector_config1(gpu_ctx, oracle, network):
         assert abs(got - ref) <= FP64_RTOL * max(1, abs(ref))
 
 
+def test_plain_three_detectors_arrival_rotations(gpu_ctx, oracle, network):
+    """The plain form on a uniform grid with H/L/V: the arrival-time phase of
+    L and V from the per-block rotation tables, D and Pv2, within the FP64
+    tolerance of the oracle's per-bin phase."""
+    n = network
+    cases = [("IMRPhenomD", 0, d) for d in W.perturbed(n["src"], 8, seed=6) + W.prior_draws(8, 61)]
+    cases += [("IMRPhenomPv2", 1, d) for d in W.prior_draws(8, 62, precessing=True)]
+    for name, ap, d in cases:
+        ref = oracle.loglik(oracle.params_from_dict(d), n["f"], n["dets"], n["data"], n["psd"], approximant=ap)
+        got = gpu_ctx.mcmc_likelihood_extrinsic(G.gen_params(**d), name, n["handles"], n["T"])
+        assert abs(got - ref) <= FP64_RTOL * max(1, abs(ref)), (name, got, ref)
+
+
 def test_batched_forms_config2(gpu_ctx, oracle, network):
     """Config 2: 512 requests, 3 detectors, prior draws."""
     n = network
