@@ -1161,6 +1161,7 @@ __device__ __forceinline__ void loop_prologue(const LoopArgs &L, CoopSmem &cs, i
 }
 
 constexpr unsigned kLoopNapMax = 2048;  // ns between polls of an idle polling block
+constexpr int kLoopPairAt = 8;          // candidate requests from which a claim takes two items
 template <int NDET>
 __global__ void __launch_bounds__(kBatchBlock, 3) k_serve_loop(const __grid_constant__ LoopArgs L) {
   using BS = BinSmem<NDET, 1>;
@@ -1208,12 +1209,15 @@ __global__ void __launch_bounds__(kBatchBlock, 3) k_serve_loop(const __grid_cons
         for (int tries = 0; mask && tries < 4; tries++) {
           const int nc = __popc(mask);
           const int pick = (int)__fns(mask, 0, (int)(blockIdx.x % (unsigned)nc) + 1);
+          // with many requests waiting, two consecutive items per claim
+          const int take = nc >= kLoopPairAt && cnt - nxt >= 2 ? 2 : 1;
           int ok = 0;
-          if (lane == pick) ok = atomicCAS(L.dwork + slot, w, w + 1) == w;
+          if (lane == pick) ok = atomicCAS(L.dwork + slot, w, w + (unsigned long long)take) == w;
           if (__shfl_sync(full, ok, pick)) {
             kind = 1;
             a0 = __shfl_sync(full, slot, pick);
             b0 = __shfl_sync(full, nxt, pick);
+            seq = (unsigned long long)__shfl_sync(full, take, pick);  // items claimed
             break;
           }
           mask &= ~(1u << pick);
@@ -1279,17 +1283,20 @@ __global__ void __launch_bounds__(kBatchBlock, 3) k_serve_loop(const __grid_cons
     nap = 0;
     const long long tw0 = tid == 0 ? global_ns() : 0;
     if (kind == 1) {
-      batch_item<NDET, 1>(L.a, a0 * L.max_items + b0, Item{a0, b0 * L.a.tile}, *(BS *)s_raw,
-                          [&](int req, double ll, int st) {
-                            const unsigned long long c = atomicAdd(&L.ctl->comp_alloc, 1ull);
-                            LoopDone *e = L.comp + c % R;
-                            e->seq = __ldcg(L.dseq + req);
-                            e->ll = ll;
-                            e->status = st;
-                            const long long dt = global_ns() - __ldcg(L.dclaim + req);
-                            e->service_ns = (int)min(dt, 2000000000ll);
-                            st_release_sys(&e->tag, c + 1);
-                          });
+      for (int q = 0; q < (int)seq; q++) {  // seq: the number of consecutive items claimed
+        if (q) __syncthreads();
+        batch_item<NDET, 1>(L.a, a0 * L.max_items + b0 + q, Item{a0, (b0 + q) * L.a.tile}, *(BS *)s_raw,
+                            [&](int req, double ll, int st) {
+                              const unsigned long long c = atomicAdd(&L.ctl->comp_alloc, 1ull);
+                              LoopDone *e = L.comp + c % R;
+                              e->seq = __ldcg(L.dseq + req);
+                              e->ll = ll;
+                              e->status = st;
+                              const long long dt = global_ns() - __ldcg(L.dclaim + req);
+                              e->service_ns = (int)min(dt, 2000000000ll);
+                              st_release_sys(&e->tag, c + 1);
+                            });
+      }
     } else {
       loop_prologue<NDET>(L, *(CoopSmem *)s_raw, a0, b0, seq);
     }
@@ -1297,7 +1304,7 @@ __global__ void __launch_bounds__(kBatchBlock, 3) k_serve_loop(const __grid_cons
       const unsigned long long dt = (unsigned long long)(global_ns() - tw0);
       if (kind == 1) {
         atomicAdd(&L.ctl->busy_item_ns, dt);
-        atomicAdd(&L.ctl->n_item, 1ull);
+        atomicAdd(&L.ctl->n_item, seq);
       } else {
         atomicAdd(&L.ctl->busy_pro_ns, dt);
         atomicAdd(&L.ctl->n_pro, 1ull);
