@@ -256,3 +256,31 @@ def test_device_loop_small_ring_wraps(gpu_ctx, served):
             assert np.array_equal(out[idx], ref)
     finally:
         gpu_ctx.set_tile(0)
+
+
+@pytest.mark.parametrize("dets", [("Hanford",), ("Hanford", "Livingston"),
+                                  ("Hanford", "Livingston", "Virgo", "Kagra")])
+def test_device_loop_detector_counts(gpu_ctx, served, dets):
+    """The loop's kernel for 1, 2 and 4 detectors: the batched kernel's values
+    bit for bit at the same tile, D and Pv2."""
+    s = served
+    f = s["f"]
+    hs = [gpu_ctx.register_data(d, f, W.noise(f, 400 + i), W.analytic_psd(f)) for i, d in enumerate(dets)]
+    draws, aps = _mix(40, 181)
+    srv = G.Server(gpu_ctx, s["T"], max_inflight=128, device_loop=True)
+    try:
+        got = np.array([srv.wait(t)[0] for t in [srv.submit(G.gen_params(**d), aps[i], hs)
+                                                 for i, d in enumerate(draws)]])
+    finally:
+        srv.close()
+    gpu_ctx.set_tile(4096)
+    try:
+        for ap in (0, 1):
+            idx = [i for i in range(len(draws)) if aps[i] == ap]
+            ref, st = gpu_ctx.loglik_batch(G.params_array([draws[i] for i in idx]), ap, hs, s["T"], G.PREC_MIXED)
+            assert np.all(st == 0)
+            assert np.array_equal(got[idx], ref)
+    finally:
+        gpu_ctx.set_tile(0)
+        for h in hs:
+            gpu_ctx.release_data(h)
