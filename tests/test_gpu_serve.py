@@ -284,3 +284,26 @@ def test_device_loop_detector_counts(gpu_ctx, served, dets):
         gpu_ctx.set_tile(0)
         for h in hs:
             gpu_ctx.release_data(h)
+
+
+def test_device_loop_bursts_across_idle_exits(gpu_ctx, served):
+    """Bursts separated by gaps around idle_us: requests arrive while a
+    launch's blocks are leaving, and every one completes with the value it
+    has alone."""
+    s = served
+    draws, aps = _mix(40, 191)
+    srv = G.Server(gpu_ctx, s["T"], max_inflight=512, device_loop=True, idle_us=300)
+    try:
+        alone = [srv.wait(srv.submit(G.gen_params(**d), aps[i], s["hs"]))[0] for i, d in enumerate(draws)]
+        rng = np.random.default_rng(3)
+        for burst in range(30):
+            time.sleep(float(rng.choice([0.0, 0.0002, 0.0003, 0.0004, 0.001])))
+            pick = rng.choice(len(draws), size=int(rng.integers(1, 20)), replace=False)
+            ts = [(i, srv.submit(G.gen_params(**draws[i]), aps[i], s["hs"])) for i in pick]
+            for i, t in ts:
+                ll, st = srv.wait(t, timeout_ms=20000)
+                assert st == 0 and ll == alone[i]
+        info = srv.loop_info()
+        assert info["launches"] >= 2  # the loop left idle and was launched again
+    finally:
+        srv.close()
