@@ -561,7 +561,19 @@ int gwgpu_mcmc_likelihood_extrinsic(gwgpu_context *c, const gwgpu_gen_params *p,
   if (st) return st;
   cudaError_t e = cudaHostGetDevicePointer((void **)&hd, h, 0);
   if (e != cudaSuccess) return c->fail(e, "plain result mapping");
-  e = gwk::launch_plain(r, sd, ndet, part, cnt, hd, nullptr, c->stream);
+  // IMRPhenomD on uniform grids: the waveform from the request's coefficients
+  // on the grid and the power tables
+  gwk::PlainTab pt;
+  bool uni = ap == gwt::kPhenomD && !r.m.status && sd[0].n0 >= 1;
+  for (int d = 0; d < ndet; d++) uni = uni && sd[d].uniform_int;
+  if (uni && sd[0].n0 + sd[0].N - 1 <= c->tables.nmax && c->ensure_tm76d(sd[0].n0 + sd[0].N - 1) == GWGPU_OK &&
+      sd[0].n0 + sd[0].N - 1 <= c->tm76d_n) {
+    gwt::wave64_prologue(r, sd[0].df, pt.w);
+    pt.t = c->tables;
+    pt.tm76d = c->tm76d;
+    pt.use = 1;
+  }
+  e = gwk::launch_plain(r, sd, ndet, part, cnt, hd, nullptr, c->stream, &pt);
   if (e != cudaSuccess) return c->fail(e, "plain launch");
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return c->fail(e, "plain");

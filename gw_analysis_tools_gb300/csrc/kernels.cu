@@ -171,15 +171,12 @@ __device__ __forceinline__ void fp64_bin(const Request &r, const StreamDev *st, 
 // (rc, rs): the batched kernel builds it on uniform grids as the product of a
 // per-pass and a per-thread factor instead of one sincos per detector-bin.
 template <int NDET>
-__device__ __forceinline__ void fp64_bin_rot(const Request &r, const StreamDev *st, int k, int N, const double *rc,
-                                             const double *rs, double (&v)[2 * NDET]) {
-  const double f = st[0].freqs[k];
-  cd hp, hc;
-  wave_bin(r, f, hp, hc);
+__device__ __forceinline__ void fp64_acc_rot(const Request &r, const StreamDev *st, int k, int N, cd hp, cd hc,
+                                             const double *rc, const double *rs, double (&v)[2 * NDET]) {
   const double ws = simpson_weight(k, N);
 #pragma unroll
   for (int d = 0; d < NDET; d++) {
-    const cd y = response_bin(r.det[d], hp, hc, f, false);
+    const cd y = response_bin(r.det[d], hp, hc, 0.0, false);  // the frequency enters through (rc, rs)
     const cd x{y.re * rc[d] - y.im * rs[d], y.re * rs[d] + y.im * rc[d]};
     double2 dd = ((const double2 *)st[d].data)[k];
     const double iS = st[d].ipsd ? st[d].ipsd[k] : 1.0 / st[d].psd[k];
@@ -187,6 +184,33 @@ __device__ __forceinline__ void fp64_bin_rot(const Request &r, const StreamDev *
     v[2 * d] += w * ((x.re * x.re + x.im * x.im) * iS);
     v[2 * d + 1] += w * ((dd.x * x.re + dd.y * x.im) * iS);
   }
+}
+template <int NDET>
+__device__ __forceinline__ void fp64_bin_rot(const Request &r, const StreamDev *st, int k, int N, const double *rc,
+                                             const double *rs, double (&v)[2 * NDET]) {
+  cd hp, hc;
+  wave_bin(r, st[0].freqs[k], hp, hc);
+  fp64_acc_rot<NDET>(r, st, k, N, hp, hc, rc, rs, v);
+}
+// IMRPhenomD at bin n = n0 + k of a uniform grid from the coefficients and
+// tables of PlainTab (d_bin's values to ~1e-12 relative).
+__device__ __forceinline__ void d_bin_tab(const Request &r, const PlainTab &pt, int n, double f, cd &hp, cd &hc) {
+  const gwt::WaveF64 &x = pt.w;
+  if (n > x.n_cut) {
+    hp = cd{0., 0.};
+    hc = cd{0., 0.};
+    return;
+  }
+  const double t = __ldg(pt.t.t13 + n), rr = __ldg(pt.t.tm53 + n), lnn = __ldg(pt.t.tln + n),
+               t34 = __ldg(pt.t.t34 + n), m76 = __ldg(pt.tm76d + n);
+  const double amp = x.A_scale * wave64_amp(x, n, t, m76);
+  const double phase = wave64_phase(x, n, t, rr, lnn, t34) - (x.tcl * (f - x.fref) + x.phic);
+  double sn, cs;
+  sincos(phase, &sn, &cs);
+  const cd h{amp * cs, -(amp * sn)};
+  const double ci = r.m.s.cos_incl, fac = r.m.s.fac_incl;
+  hc = cd{h.im * ci, -h.re * ci};
+  hp = cd{h.re * fac, h.im * fac};
 }
 template <int NDET>
 __device__ __forceinline__ double fp64_finalize(const double *s, const StreamDev *st) {
@@ -208,7 +232,8 @@ __device__ __forceinline__ double fp64_finalize(const double *s, const StreamDev
 constexpr int kPlainRot = 1 + 8 + 16;
 template <int NDET>
 __global__ void __launch_bounds__(128) k_plain(const __grid_constant__ Request r, const __grid_constant__ PlainStreams ps,
-                                               double *partials, unsigned *counter, double *out, int *status) {
+                                               const __grid_constant__ PlainTab pt, double *partials,
+                                               unsigned *counter, double *out, int *status) {
   __shared__ double smem[32 * 2 * NDET];
   __shared__ double2 s_rot[NDET * kPlainRot];
   const int N = ps.s[0].N;
@@ -241,7 +266,10 @@ __global__ void __launch_bounds__(128) k_plain(const __grid_constant__ Request r
         rc[d] = xr * C.x - xi * C.y;
         rs[d] = xr * C.y + xi * C.x;
       }
-      fp64_bin_rot<NDET>(r, ps.s, k, N, rc, rs, v);
+      cd hp, hc;
+      if (pt.use) d_bin_tab(r, pt, ps.s[0].n0 + k, ps.s[0].freqs[k], hp, hc);
+      else wave_bin(r, ps.s[0].freqs[k], hp, hc);
+      fp64_acc_rot<NDET>(r, ps.s, k, N, hp, hc, rc, rs, v);
     }
   } else {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x)
@@ -281,15 +309,17 @@ int plain_blocks(int N) {
   return g < 1 ? 1 : g;
 }
 cudaError_t launch_plain(const Request &r, const StreamDev *streams, int ndet, double *partials, unsigned *counter,
-                         double *out, int *status, cudaStream_t s) {
+                         double *out, int *status, cudaStream_t s, const PlainTab *tab) {
   PlainStreams ps;
   for (int d = 0; d < ndet; d++) ps.s[d] = streams[d];
+  PlainTab pt;
+  if (tab) pt = *tab;
   int grid = plain_blocks(streams[0].N);
   switch (ndet) {
-    case 1: k_plain<1><<<grid, 128, 0, s>>>(r, ps, partials, counter, out, status); break;
-    case 2: k_plain<2><<<grid, 128, 0, s>>>(r, ps, partials, counter, out, status); break;
-    case 3: k_plain<3><<<grid, 128, 0, s>>>(r, ps, partials, counter, out, status); break;
-    case 4: k_plain<4><<<grid, 128, 0, s>>>(r, ps, partials, counter, out, status); break;
+    case 1: k_plain<1><<<grid, 128, 0, s>>>(r, ps, pt, partials, counter, out, status); break;
+    case 2: k_plain<2><<<grid, 128, 0, s>>>(r, ps, pt, partials, counter, out, status); break;
+    case 3: k_plain<3><<<grid, 128, 0, s>>>(r, ps, pt, partials, counter, out, status); break;
+    case 4: k_plain<4><<<grid, 128, 0, s>>>(r, ps, pt, partials, counter, out, status); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -54,9 +54,18 @@ cudaError_t launch_inner_product(const double *data, const double *psd, const do
 // The same with integration weights iw (4 w_i, times f_i ln 10 for log10F).
 cudaError_t launch_inner_product_weighted(const double *data, const double *psd, const double *resp, const double *iw,
                                           int N, double *partials, unsigned *counter, double *out, cudaStream_t s);
+// Plain form on uniform grids, IMRPhenomD: the waveform from the request's
+// FP64 coefficients on the grid (wave64_prologue) and the n-indexed power
+// tables instead of the powers, logarithm and cube root of each frequency.
+struct PlainTab {
+  gwt::WaveF64 w;
+  gwt::Tables t;
+  const double *tm76d = nullptr;  // n^(-7/6), FP64
+  int use = 0;                    // 1: the tables cover every bin of the call
+};
 // Plain form: one request, FP64, one launch.  out[0] = log L.
 cudaError_t launch_plain(const Request &r, const StreamDev *streams, int ndet, double *partials, unsigned *counter,
-                         double *out, int *status, cudaStream_t s);
+                         double *out, int *status, cudaStream_t s, const PlainTab *tab = nullptr);
 int plain_blocks(int N);
 cudaError_t plain_preload();  // loads the plain kernels' module (function-attribute query)
 
