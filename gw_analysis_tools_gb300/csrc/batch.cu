@@ -170,6 +170,12 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   if (e != cudaSuccess) return c->fail(e, "batch counters");
   // mixed form: the prologue writes the work order (most live bins first)
   const bool ordered = mixed && c->order_items && !c->prologue_serial;
+  // FP64 form: the cooperative prologue writes each IMRPhenomD request's
+  // coefficients on the grid after the Request records, for the bin
+  // kernel's table form (with the FP64 n^(-7/6) table)
+  gwt::WaveF64 *w64 = nullptr;
+  if (!mixed && !c->prologue_serial && c->tm76d && c->tm76d_n > 0)
+    w64 = (gwt::WaveF64 *)((char *)reqs + sizeof(gwt::Request) * (size_t)n);
   gwk::OrderArgs ord;
   if (ordered) {
     ord.fill = (int *)(cnt + n + 32);
@@ -186,7 +192,7 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   else
     e = gwk::launch_prologue((const gwt::GenParams *)d_params, d_approx, n, pl.handles, ndet, T_segment, 1,
                              c->streams_dev, c->qnm_dev, mixed ? nullptr : (gwt::Request *)reqs,
-                             mixed ? (gwt::MixedReq *)reqs : nullptr, mixed, d_status, L.stream, ord);
+                             mixed ? (gwt::MixedReq *)reqs : nullptr, mixed, d_status, L.stream, ord, w64);
   if (e != cudaSuccess) return c->fail(e, "prologue launch");
   if (timing) cudaEventRecord(c->t_ev[1], L.stream);
   gwk::BatchArgs a;
@@ -209,6 +215,9 @@ static int launch_sequence(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_
   a.status = d_status;
   a.status_out = status_out ? status_out : d_status;
   a.tables = c->tables;
+  a.w64 = w64;
+  a.tm76d = w64 ? c->tm76d : nullptr;
+  a.tm76d_n = w64 ? c->tm76d_n : 0;
   int grid = std::min(pl.nitems, persistent_grid(c->device, mixed, ndet, occ));
   if (grid < 1) grid = 1;
   e = gwk::launch_batch(a, mixed, grid, occ, L.stream, c->pdl);
@@ -245,6 +254,9 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
   }
   if (tile <= 0) tile = choose_tile(c, mixed, L.tk);
   const int occ = choose_occ(c, mixed, L.tk);
+  // FP64 batches: the n^(-7/6) table of the table form, built before any
+  // capture (a failure leaves the frequency form)
+  if (!mixed && c->ensure_tm76d(c->tables.nmax) != GWGPU_OK) c->last_error.clear();
   bool replanned = false;
   if (!same || !L.plan.valid || L.plan.tile != tile) {
     int st = plan_batch(c, L, n, h_handles, ndet, tile);
@@ -255,8 +267,8 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
     L.plan.valid = true;
     replanned = true;
   }
-  size_t rq = mixed ? sizeof(gwt::MixedReq) : sizeof(gwt::Request);
-  size_t bytes = rq * n + 256 + sizeof(double) * (size_t)L.plan.nitems * gwk::kAcc + 256 +
+  size_t rq = mixed ? sizeof(gwt::MixedReq) : sizeof(gwt::Request) + sizeof(gwt::WaveF64);
+  size_t bytes = rq * n + 512 + sizeof(double) * (size_t)L.plan.nitems * gwk::kAcc + 256 +
                  sizeof(unsigned) * (size_t)(n + 32 + gwk::kOrderBuckets);
   void *old = L.work;
   int st = lane_alloc(c, L, &L.work, &L.work_cap, bytes, "batch scratch");
@@ -267,7 +279,7 @@ int enqueue_batch(gwgpu_context *c, Lane &L, const gwgpu_gen_params *d_params, c
   }
   char *p = (char *)L.work;
   void *reqs = p;
-  p = align256(p + rq * n);
+  p = align256(p + rq * n);  // FP64: Request[n], then WaveF64[n] (below)
   double *partials = (double *)p;
   p = align256(p + sizeof(double) * (size_t)L.plan.nitems * gwk::kAcc);
   unsigned *cnt = (unsigned *)p;

@@ -194,15 +194,15 @@ __device__ __forceinline__ void fp64_bin_rot(const Request &r, const StreamDev *
 }
 // IMRPhenomD at bin n = n0 + k of a uniform grid from the coefficients and
 // tables of PlainTab (d_bin's values to ~1e-12 relative).
-__device__ __forceinline__ void d_bin_tab(const Request &r, const PlainTab &pt, int n, double f, cd &hp, cd &hc) {
-  const gwt::WaveF64 &x = pt.w;
+__device__ __forceinline__ void d_bin_tab(const Request &r, const gwt::WaveF64 &x, const gwt::Tables &tb,
+                                          const double *tm76d, int n, double f, cd &hp, cd &hc) {
   if (n > x.n_cut) {
     hp = cd{0., 0.};
     hc = cd{0., 0.};
     return;
   }
-  const double t = __ldg(pt.t.t13 + n), rr = __ldg(pt.t.tm53 + n), lnn = __ldg(pt.t.tln + n),
-               t34 = __ldg(pt.t.t34 + n), m76 = __ldg(pt.tm76d + n);
+  const double t = __ldg(tb.t13 + n), rr = __ldg(tb.tm53 + n), lnn = __ldg(tb.tln + n), t34 = __ldg(tb.t34 + n),
+               m76 = __ldg(tm76d + n);
   const double amp = x.A_scale * wave64_amp(x, n, t, m76);
   const double phase = wave64_phase(x, n, t, rr, lnn, t34) - (x.tcl * (f - x.fref) + x.phic);
   double sn, cs;
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(128) k_plain(const __grid_constant__ Request r
         rs[d] = xr * C.y + xi * C.x;
       }
       cd hp, hc;
-      if (pt.use) d_bin_tab(r, pt, ps.s[0].n0 + k, ps.s[0].freqs[k], hp, hc);
+      if (pt.use) d_bin_tab(r, pt.w, pt.t, pt.tm76d, ps.s[0].n0 + k, ps.s[0].freqs[k], hp, hc);
       else wave_bin(r, ps.s[0].freqs[k], hp, hc);
       fp64_acc_rot<NDET>(r, ps.s, k, N, hp, hc, rc, rs, v);
     }
@@ -462,7 +462,8 @@ __device__ __forceinline__ void prologue_coop_body(CoopSmem &sm, int base, int w
                                                    const int *__restrict__ handles, int ndet, double T_segment,
                                                    int tc_from_segment, const StreamDev *__restrict__ streams,
                                                    const double *__restrict__ qnm, Request *req, MixedReq *mreq,
-                                                   int want_mixed, int *status, Sync sync, Tail tail) {
+                                                   int want_mixed, int *status, Sync sync, Tail tail,
+                                                   gwt::WaveF64 *w64 = nullptr) {
   Request *s_r = sm.r;
   GenParams *s_p = sm.p;
   AmpConn *s_ac = sm.ac;
@@ -620,6 +621,10 @@ __device__ __forceinline__ void prologue_coop_body(CoopSmem &sm, int base, int w
         else mixed_det_factors_a(r, x, x.A_scale, s_ds[lane], s_ws[lane]);
       }
       if (warp == 3 && !pv2) mixed_det_phase(r, df, x);
+    } else if (w64 && warp == 0 && !pv2 && s_uni[lane]) {
+      // FP64 batches, IMRPhenomD on a uniform grid: the waveform's
+      // coefficients on the grid for the bin kernel's table form
+      wave64_prologue(r, s_df[lane], w64[i]);
     }
   }
   sync();
@@ -660,7 +665,8 @@ __device__ __forceinline__ void prologue_coop_body(CoopSmem &sm, int base, int w
 __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     const GenParams *__restrict__ params, const int *__restrict__ approx, int n, const int *__restrict__ handles,
     int ndet, double T_segment, int tc_from_segment, const StreamDev *__restrict__ streams,
-    const double *__restrict__ qnm, Request *req, MixedReq *mreq, int want_mixed, int *status, const OrderArgs ord) {
+    const double *__restrict__ qnm, Request *req, MixedReq *mreq, int want_mixed, int *status, const OrderArgs ord,
+    gwt::WaveF64 *w64) {
   __shared__ CoopSmem sm;
   grid_dep_trigger();  // the bin kernel may launch and wait for this grid
   // this block's requests into the work order, on the warps idle in S6 (warp
@@ -672,17 +678,17 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
   };
   prologue_coop_body(sm, blockIdx.x * kCoopReq, threadIdx.x >> 5, threadIdx.x & 31, params, approx, n, handles, ndet,
                      T_segment, tc_from_segment, streams, qnm, req, mreq, want_mixed, status,
-                     [] { __syncthreads(); }, tail);
+                     [] { __syncthreads(); }, tail, w64);
 }
 
 
 cudaError_t launch_prologue(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
                             double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
                             Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s,
-                            const OrderArgs &ord) {
+                            const OrderArgs &ord, gwt::WaveF64 *w64) {
   int grid = (n + kCoopReq - 1) / kCoopReq;
   k_prologue_coop<<<grid, kCoopWarps * 32, 0, s>>>(params, approx, n, handles, ndet, T_segment, tc_from_segment,
-                                                   streams, qnm, req, mreq, want_mixed, status, ord);
+                                                   streams, qnm, req, mreq, want_mixed, status, ord, w64);
   return cudaGetLastError();
 }
 cudaError_t launch_prologue_serial(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
@@ -908,6 +914,7 @@ struct BinSmem {
   // detector rotations: per segment pass (first bin) and per thread offset
   float2 rot_seg[kSegBuf * (MIXED ? NDET : 1)];
   float2 rot_off[(MIXED ? NDET : 1) * (MIXED ? kBatchBlock : 1)];
+  alignas(8) unsigned char w64[MIXED ? 8 : sizeof(gwt::WaveF64)];  // FP64 form: the table form's coefficients
 };
 
 // One item (iid, I) of a batch on the whole block: its partial sums into
@@ -938,6 +945,14 @@ __device__ __forceinline__ void batch_item(const BatchArgs &a, const int iid, co
     constexpr int nw = (MIXED ? sizeof(MixedReq) : sizeof(Request)) / 4;
     for (int w = tid; w < nw; w += blockDim.x) dst[w] = __ldcg(src + w);
     if (tid < NDET) s_st[tid] = a.streams[__ldcg(a.handles + I.req * a.ndet + tid)];
+    if constexpr (!MIXED) {
+      if (a.w64) {  // the request's FP64 coefficients on the grid (IMRPhenomD, uniform grids)
+        static_assert(sizeof(gwt::WaveF64) % 4 == 0, "copied as words");
+        const unsigned *ws = (const unsigned *)(a.w64 + I.req);
+        unsigned *wd = (unsigned *)sm.w64;
+        for (int w = tid; w < (int)(sizeof(gwt::WaveF64) / 4); w += blockDim.x) wd[w] = __ldcg(ws + w);
+      }
+    }
   }
   __syncthreads();
   const int N = s_st[0].N;
@@ -974,6 +989,12 @@ __device__ __forceinline__ void batch_item(const BatchArgs &a, const int iid, co
       for (int d = 0; d < NDET; d++) sincos(r.det[d].tau * (tid * s_st[0].df), &os[d], &oc[d]);
       __syncthreads();
       if (r.m.status == 0) {
+        // IMRPhenomD: the waveform from the request's coefficients and the
+        // power tables where they cover the item's bins
+        const int n0 = s_st[0].n0;
+        const bool tab = a.w64 && r.approximant == kPhenomD && n0 >= 1 && n0 + kend - 1 <= a.tables.nmax &&
+                         n0 + kend - 1 <= a.tm76d_n;
+        const gwt::WaveF64 &W = *(const gwt::WaveF64 *)sm.w64;
         int pass = 0;
         for (int k = I.k0 + tid; k < kend; k += blockDim.x, pass++) {
           double rc[NDET], rs[NDET];
@@ -983,7 +1004,10 @@ __device__ __forceinline__ void batch_item(const BatchArgs &a, const int iid, co
             rc[d] = b.x * oc[d] - b.y * os[d];
             rs[d] = b.y * oc[d] + b.x * os[d];
           }
-          fp64_bin_rot<NDET>(r, s_st, k, N, rc, rs, v);
+          cd hp, hc;
+          if (tab) d_bin_tab(r, W, a.tables, a.tm76d, n0 + k, s_st[0].freqs[k], hp, hc);
+          else wave_bin(r, s_st[0].freqs[k], hp, hc);
+          fp64_acc_rot<NDET>(r, s_st, k, N, hp, hc, rc, rs, v);
         }
       }
       __syncthreads();  // s_rot64 is rewritten by the next item

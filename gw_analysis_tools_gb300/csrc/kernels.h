@@ -83,7 +83,7 @@ struct OrderArgs {
 cudaError_t launch_prologue(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
                             double T_segment, int tc_from_segment, const StreamDev *streams, const double *qnm,
                             Request *req, MixedReq *mreq, int want_mixed, int *status, cudaStream_t s,
-                            const OrderArgs &ord = OrderArgs());
+                            const OrderArgs &ord = OrderArgs(), gwt::WaveF64 *w64 = nullptr);
 // One thread per request (the reference order of the prologue); kept to check
 // the cooperative kernel against.
 cudaError_t launch_prologue_serial(const GenParams *params, const int *approx, int n, const int *handles, int ndet,
@@ -111,6 +111,12 @@ struct BatchArgs {
   int *status;      // per-request working status (device memory: the bounds flag is set atomically)
   int *status_out;  // where the finalize writes each request's status (status itself, or mapped host memory)
   gwt::Tables tables;
+  // FP64 form: per-request coefficients on the grid written by the prologue
+  // (IMRPhenomD, uniform grids; null: every bin from the frequency) and the
+  // FP64 n^(-7/6) table for n <= tm76d_n
+  const gwt::WaveF64 *w64 = nullptr;
+  const double *tm76d = nullptr;
+  int tm76d_n = 0;
 };
 // occ: the launch shape's resident blocks per SM (mixed 3 or 4, FP64 2);
 // pdl: launched as a programmatic dependent of the kernel before it on s

@@ -229,7 +229,10 @@ def test_cooperative_prologue_matches_serial(gpu_ctx, network):
         del os.environ["GWGPU_PROLOGUE"]
     try:
         hs = [ser.register_data(d, n["f"], n["data"][i], n["psd"][i]) for i, d in enumerate(n["dets"])]
-        for prec, tol in ((G.PREC_FP64, 1e-11), (G.PREC_MIXED, 1e-6)):
+        # FP64: the cooperative prologue also writes the IMRPhenomD grid
+        # coefficients, so its batches take the table form (h within ~2e-12 of
+        # the frequency form the serial prologue's batches use)
+        for prec, tol in ((G.PREC_FP64, 1e-10), (G.PREC_MIXED, 1e-6)):
             a, sa = gpu_ctx.loglik_batch(G.params_array(draws), aps, n["handles"], n["T"], prec)
             b, sb = ser.loglik_batch(G.params_array(draws), aps, hs, n["T"], prec)
             assert np.array_equal(sa, sb)
