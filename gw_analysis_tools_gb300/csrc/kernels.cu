@@ -669,19 +669,6 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_prologue_coop(
     gwt::WaveF64 *w64) {
   __shared__ CoopSmem sm;
   grid_dep_trigger();  // the bin kernel may launch and wait for this grid
-  {
-    // tables of S1 fetched while S0 runs: the QNM spline table into L2
-    // (each block its share of the 128-byte lines) and the calibration fits'
-    // constants into this SM's constant cache
-    constexpr int kQnmLines = (kQnmArrays * kQnmLen * 8 + 127) / 128;
-    const int per = (kQnmLines + gridDim.x - 1) / gridDim.x;
-    for (int l = blockIdx.x * per + threadIdx.x; l < min(kQnmLines, (int)(blockIdx.x + 1) * per); l += blockDim.x)
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(qnm + l * 16));
-    if (threadIdx.x < 19 * 11 / 8 + 1) {
-      const double v = (&gwt_lambda_fit_d[0][0])[threadIdx.x * 8];
-      asm volatile("" ::"d"(v));
-    }
-  }
   // this block's requests into the work order, on the warps idle in S6 (warp
   // w takes the tiles t = w - 1 mod 3)
   auto tail = [&](int warp, int lane, bool act, int i, int kcut) {
